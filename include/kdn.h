@@ -1,0 +1,221 @@
+/*
+ * kdn.h -- C ABI of libkdn_gb300, the GB300 backend of the Kodanuki renderer.
+ *
+ * Plain C: every call takes plain pointers and sizes and returns a
+ * kdn_status.  No call throws, prints or exits; the host plugin maps a status
+ * to the reference's print-and-exit convention (reference rule 19,
+ * core/render.cpp:140).  Calls on one context are serialised on the
+ * context's CUDA stream; several worker threads may share a context (each
+ * call takes the context's lock).
+ *
+ * Record layouts are the reference's plain-data types byte for byte where
+ * one exists (Step, Ray, Hit) and the fields of the reference's scene types
+ * otherwise; each is cited below (paths within the reference's source/).
+ */
+#ifndef KDN_H
+#define KDN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum kdn_status {
+	KDN_OK = 0,
+	KDN_BAD_ARG = 1,    /* a null pointer, a bad block name or size, a size past a limit */
+	KDN_OOM = 2,        /* device memory or the admission budget ran out */
+	KDN_TIMEOUT = 3,    /* a device loop reached its iteration limit and stopped */
+	KDN_CUDA_ERROR = 4, /* a CUDA call failed; kdn_last_error says which */
+	KDN_NOT_READY = 5,  /* a call needs blocks or a build that are missing */
+	KDN_NO_DEVICE = 6   /* no CUDA device, or the kernels were not built for it */
+} kdn_status;
+
+typedef struct kdn_ctx kdn_ctx;
+
+/* sdf/program.h:56 Step: opcode (sdf/program.h:20 Opcode), operands, value, leaf. 32 bytes. */
+typedef struct kdn_step {
+	uint8_t opcode;
+	uint32_t a, b, c;
+	double value;
+	uint32_t leaf;
+} kdn_step;
+
+/* One object program (sdf/scene.cpp:280 objectProgram) as a run of kdn_step. */
+typedef struct kdn_program_ref {
+	uint32_t first;  /* first step in the "scene.steps" block */
+	uint32_t count;  /* number of steps */
+	uint32_t result; /* the step whose value is the program's */
+} kdn_program_ref;
+
+/* core/batch.h:125 Ray, 36 bytes. */
+typedef struct kdn_ray {
+	float origin[3];
+	float direction[3];
+	float far;
+	uint8_t inside;
+	uint8_t pad_[3];
+	uint32_t within; /* material index, 0xFFFFFFFF for none */
+} kdn_ray;
+
+/* core/batch.h:157 Hit, 56 bytes. kind: 0 missed, 1 surface, 2 solid. */
+typedef struct kdn_hit {
+	uint8_t kind;
+	uint8_t pad0_[3];
+	float distance;
+	float point[3];
+	float normal[3];
+	uint32_t leaf;
+	uint32_t other;
+	float share;
+	float loosened;
+	uint8_t leaf_kind;
+	uint8_t pad1_[3];
+	uint32_t cell;
+} kdn_hit;
+
+/* sdf/scene.h Material (its fields the backend reads), 64 bytes. */
+typedef struct kdn_material {
+	uint32_t kind;      /* sdf/scene.h MaterialKind: 0 matte, 1 plastic, 2 metal, 3 glass */
+	float albedo[3];    /* the first colour stop (a constant albedo) */
+	float roughness;
+	float refraction;
+	float dispersion;   /* Cauchy B in square micrometres */
+	float absorb[3];
+	float glow[3];
+	float strength;
+	uint32_t flags_;    /* reserved, 0 */
+	uint32_t pad_;
+} kdn_material;
+
+/* sdf/scene.h Light, 136 bytes. kind: sdf/scene.h LightKind (2 sphere, 3 quad). */
+typedef struct kdn_light {
+	uint32_t kind;
+	float radius;
+	float angle;
+	float pad_;
+	double at[3];
+	double direction[3];
+	double along[3];
+	double across[3];
+	double power[3]; /* linear RGB */
+} kdn_light;
+
+/* sdf/scene.h Sky, gradient kind: linear RGB zenith, horizon, ground. */
+typedef struct kdn_sky {
+	double zenith[3];
+	double horizon[3];
+	double ground[3];
+} kdn_sky;
+
+/* sdf/scene.h Camera and the Render fields a frame reads. */
+typedef struct kdn_camera {
+	double eye[3];
+	double target[3];
+	double up[3];
+	double fov;
+	double aperture;
+	double focus;
+} kdn_camera;
+
+/* core/geometry.h:14 Region: the box the world is built over. */
+typedef struct kdn_region {
+	double lower[3];
+	double size[3];
+} kdn_region;
+
+/* How the cut octree is grown (plugins/geometry/tree/cut.cpp:463 cutCell per
+ * cell): every surface cell is split down to min_depth, and further, down to
+ * max_depth, while its kept programs hold more than split_steps steps. */
+typedef struct kdn_build_options {
+	int32_t min_depth;
+	int32_t max_depth;
+	uint32_t split_steps;
+	uint32_t pad_;
+} kdn_build_options;
+
+/* One frame of fixed-count samples (stopping/fixed_count). */
+typedef struct kdn_frame {
+	int32_t width, height;
+	int32_t samples;  /* samples per pixel drawn by this call */
+	int32_t surfaces; /* render.surfaces: the most surfaces a path stands on */
+	int32_t seed;     /* render.seed */
+	uint32_t first;   /* sample index of this call's first sample of every pixel */
+	uint32_t accumulate; /* 1: add to the pixel sums of the previous call */
+	uint32_t pad_;
+} kdn_frame;
+
+/* Device times of the last kdn_render, from CUDA events on the context's stream. */
+typedef struct kdn_frame_stats {
+	double total_ms;
+	double trace_ms;   /* every launch of the sphere-trace kernel */
+	double shade_ms;   /* arrive + aim + scatter */
+	double other_ms;   /* camera, fold, compaction */
+	uint64_t segments; /* rays traced (camera + scatter + shadow) */
+	uint64_t march_steps;
+	uint64_t program_steps; /* program steps run by the trace kernel */
+	uint32_t launches;
+	uint32_t pad_;
+} kdn_frame_stats;
+
+const char* kdn_status_string(kdn_status status);
+/* The message of the last failed call on this context (or of kdn_open). */
+const char* kdn_last_error(const kdn_ctx* ctx);
+
+/* Open a context on one CUDA device.  Replaces the reference's per-worker
+ * Backend state (core/plugin.h:333 openWorkers).  KDN_HOST_ONLY opens a
+ * context without a device: blocks and kdn_build/kdn_world_* work, every
+ * device entry point returns KDN_NO_DEVICE. */
+#define KDN_HOST_ONLY (-1)
+kdn_status kdn_open(int device, kdn_ctx** out);
+kdn_status kdn_close(kdn_ctx* ctx);
+
+/*
+ * Copy one block into the context (core/block.h:565 Block {name, data,
+ * count, size}).  Names and element sizes:
+ *   "scene.steps"      kdn_step, 32        every object program end to end
+ *   "scene.programs"   kdn_program_ref, 12 one per object (Scene::objectPrograms)
+ *   "scene.leaves"     uint32_t, 4         the material of each leaf (Leaf::material)
+ *   "looks.materials"  kdn_material, 64
+ *   "lighting.lights"  kdn_light, 136
+ *   "lighting.sky"     kdn_sky, 72         one
+ *   "shot.camera"      kdn_camera, 96      one
+ *   "geometry.region"  kdn_region, 48      one
+ * A block replaces the one of the same name; the world must be rebuilt
+ * (kdn_build) after any scene.* or geometry.* block changes.
+ */
+kdn_status kdn_upload_block(kdn_ctx* ctx, const char* name, const void* data, size_t count, size_t size);
+
+/* Build the cut octree over the scene's programs and make the world
+ * resident on the device (plugins/geometry/tree/plugin.cpp:37 treeBuilt). */
+kdn_status kdn_build(kdn_ctx* ctx, const kdn_build_options* options);
+/* Counts of the built world: cells, leaves, kept programs, program steps. */
+kdn_status kdn_world_stats(kdn_ctx* ctx, uint64_t out[4]);
+/* Copy cell i (depth-first pre-order) of the built octree: head = level,
+ * place x/y/z, occupancy, program count; objects/results/counts get one
+ * entry per kept program, steps the programs' kdn_steps end to end.  Pass
+ * null arrays to read the head alone. */
+kdn_status kdn_world_cell(kdn_ctx* ctx, uint64_t i, uint32_t head[6], uint32_t* objects, uint32_t* results, uint32_t* counts, kdn_step* steps, size_t steps_capacity);
+
+/* ExtendRays (core/step.cpp:132): the first hit of each ray, host arrays in
+ * and out (a host-to-device and device-to-host copy each call). */
+kdn_status kdn_extend(kdn_ctx* ctx, const kdn_ray* rays, uint32_t n, kdn_hit* hits);
+/* The same over device arrays, on the given CUDA stream (0: the context's). */
+kdn_status kdn_extend_device(kdn_ctx* ctx, const kdn_ray* rays, uint32_t n, kdn_hit* hits, void* stream);
+
+/* Render samples of one frame into the context's pixel sums and write the
+ * pixel means, linear RGB float, row-major, 3 floats a pixel.  out is a host
+ * pointer (kdn_render) or a device pointer (kdn_render_device). */
+kdn_status kdn_render(kdn_ctx* ctx, const kdn_frame* frame, float* out_rgb);
+kdn_status kdn_render_device(kdn_ctx* ctx, const kdn_frame* frame, float* out_rgb, void* stream);
+kdn_status kdn_frame_stats_get(kdn_ctx* ctx, kdn_frame_stats* stats);
+
+/* Write a buffer larger than the L2 cache on the context's stream, so that
+ * the next launch starts with a cold cache. */
+kdn_status kdn_flush_l2(kdn_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

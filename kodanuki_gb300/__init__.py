@@ -1,0 +1,250 @@
+"""kodanuki_gb300 -- GB300 backend for the Kodanuki spectral SDF path tracer.
+
+The product is ``libkdn_gb300.so`` (C ABI in include/kdn.h), built in-tree
+by :mod:`kodanuki_gb300.build`.  This module is the host-side mirror of the
+reference's backend interface for Python callers and tests: it loads the
+library (and fails loudly when it is missing), uploads a compiled scene's
+blocks and runs the entry points.
+
+    from kodanuki_gb300 import Backend
+    from kodanuki_gb300.scene import Scene
+    scene = Scene.load("tests/golden/scenes/c1.npz")
+    with Backend() as b:
+        b.load(scene)
+        b.build(min_depth=6, max_depth=10, split_steps=96)
+        hits = b.extend(rays)
+        image = b.render(width=256, height=256, samples=16)
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .scene import STEP_DTYPE, Scene
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libkdn_gb300.so")
+
+KDN_OK, KDN_BAD_ARG, KDN_OOM, KDN_TIMEOUT, KDN_CUDA_ERROR, KDN_NOT_READY, KDN_NO_DEVICE = range(7)
+
+# core/batch.h:125 Ray (36 bytes) and core/batch.h:157 Hit (56 bytes).
+RAY_DTYPE = np.dtype([("origin", "<f4", 3), ("direction", "<f4", 3), ("far", "<f4"), ("inside", "u1"), ("pad", "u1", 3), ("within", "<u4")])
+HIT_DTYPE = np.dtype([("kind", "u1"), ("pad0", "u1", 3), ("distance", "<f4"), ("point", "<f4", 3), ("normal", "<f4", 3), ("leaf", "<u4"),
+                      ("other", "<u4"), ("share", "<f4"), ("loosened", "<f4"), ("leaf_kind", "u1"), ("pad1", "u1", 3), ("cell", "<u4")])
+PROGRAM_REF_DTYPE = np.dtype([("first", "<u4"), ("count", "<u4"), ("result", "<u4")])
+MATERIAL_DTYPE = np.dtype([("kind", "<u4"), ("albedo", "<f4", 3), ("roughness", "<f4"), ("refraction", "<f4"), ("dispersion", "<f4"),
+                           ("absorb", "<f4", 3), ("glow", "<f4", 3), ("strength", "<f4"), ("flags", "<u4"), ("pad", "<u4")])
+LIGHT_DTYPE = np.dtype([("kind", "<u4"), ("radius", "<f4"), ("angle", "<f4"), ("pad", "<f4"), ("at", "<f8", 3), ("direction", "<f8", 3),
+                        ("along", "<f8", 3), ("across", "<f8", 3), ("power", "<f8", 3)])
+SKY_DTYPE = np.dtype([("zenith", "<f8", 3), ("horizon", "<f8", 3), ("ground", "<f8", 3)])
+CAMERA_DTYPE = np.dtype([("eye", "<f8", 3), ("target", "<f8", 3), ("up", "<f8", 3), ("fov", "<f8"), ("aperture", "<f8"), ("focus", "<f8")])
+REGION_DTYPE = np.dtype([("lower", "<f8", 3), ("size", "<f8", 3)])
+assert RAY_DTYPE.itemsize == 36 and HIT_DTYPE.itemsize == 56 and MATERIAL_DTYPE.itemsize == 64 and LIGHT_DTYPE.itemsize == 136
+
+
+class BuildOptions(ctypes.Structure):
+    _fields_ = [("min_depth", ctypes.c_int32), ("max_depth", ctypes.c_int32), ("split_steps", ctypes.c_uint32), ("pad", ctypes.c_uint32)]
+
+
+class Frame(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("samples", ctypes.c_int32), ("surfaces", ctypes.c_int32),
+                ("seed", ctypes.c_int32), ("first", ctypes.c_uint32), ("accumulate", ctypes.c_uint32), ("pad", ctypes.c_uint32)]
+
+
+class FrameStats(ctypes.Structure):
+    _fields_ = [("total_ms", ctypes.c_double), ("trace_ms", ctypes.c_double), ("shade_ms", ctypes.c_double), ("other_ms", ctypes.c_double),
+                ("segments", ctypes.c_uint64), ("march_steps", ctypes.c_uint64), ("program_steps", ctypes.c_uint64),
+                ("launches", ctypes.c_uint32), ("pad", ctypes.c_uint32)]
+
+
+class KdnError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"kdn status {status}: {message}")
+        self.status = status
+
+
+# Every symbol include/kdn.h declares.
+EXPORTS = [
+    "kdn_status_string", "kdn_last_error", "kdn_open", "kdn_close", "kdn_upload_block", "kdn_build", "kdn_world_stats",
+    "kdn_world_cell", "kdn_extend", "kdn_extend_device", "kdn_render", "kdn_render_device", "kdn_frame_stats_get", "kdn_flush_l2",
+]
+
+_lib = None
+
+
+def library(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Load libkdn_gb300.so.  There is no fallback: a missing library is an
+    error, and :func:`kodanuki_gb300.build.build` makes it."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = ctypes.CDLL(path)
+    P = ctypes.c_void_p
+    L.kdn_status_string.restype = ctypes.c_char_p
+    L.kdn_status_string.argtypes = [ctypes.c_int]
+    L.kdn_last_error.restype = ctypes.c_char_p
+    L.kdn_last_error.argtypes = [P]
+    L.kdn_open.argtypes = [ctypes.c_int, ctypes.POINTER(P)]
+    L.kdn_close.argtypes = [P]
+    L.kdn_upload_block.argtypes = [P, ctypes.c_char_p, P, ctypes.c_size_t, ctypes.c_size_t]
+    L.kdn_build.argtypes = [P, ctypes.POINTER(BuildOptions)]
+    L.kdn_world_stats.argtypes = [P, P]
+    L.kdn_world_cell.argtypes = [P, ctypes.c_uint64, P, P, P, P, P, ctypes.c_size_t]
+    L.kdn_extend.argtypes = [P, P, ctypes.c_uint32, P]
+    L.kdn_extend_device.argtypes = [P, P, ctypes.c_uint32, P, P]
+    L.kdn_render.argtypes = [P, ctypes.POINTER(Frame), P]
+    L.kdn_render_device.argtypes = [P, ctypes.POINTER(Frame), P, P]
+    L.kdn_frame_stats_get.argtypes = [P, ctypes.POINTER(FrameStats)]
+    L.kdn_flush_l2.argtypes = [P]
+    for name in EXPORTS:
+        fn = getattr(L, name)
+        if name not in ("kdn_status_string", "kdn_last_error"):
+            fn.restype = ctypes.c_int
+    _lib = L
+    return L
+
+
+def _ptr(a: np.ndarray) -> ctypes.c_void_p:
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def scene_blocks(scene: Scene) -> dict[str, np.ndarray]:
+    """The blocks a reference host would upload for a compiled scene
+    (core/block.h Block; the names of include/kdn.h)."""
+    refs = np.zeros(scene.program_count, PROGRAM_REF_DTYPE)
+    refs["first"] = scene.program_first[:-1]
+    refs["count"] = np.diff(scene.program_first)
+    refs["result"] = scene.program_result
+    m = scene.materials
+    mats = np.zeros(len(m["kind"]), MATERIAL_DTYPE)
+    mats["kind"] = m["kind"]
+    mats["albedo"] = m["albedo"]
+    mats["roughness"] = m["roughness"]
+    mats["refraction"] = m["refraction"]
+    mats["dispersion"] = m["dispersion"]
+    mats["absorb"] = m["absorb"]
+    mats["glow"] = m["glow"]
+    mats["strength"] = m["strength"]
+    l = scene.lights
+    lights = np.zeros(len(l["kind"]), LIGHT_DTYPE)
+    for k in ("kind", "radius", "angle", "at", "direction", "along", "across", "power"):
+        lights[k] = l[k]
+    sky = np.zeros(1, SKY_DTYPE)
+    for k in ("zenith", "horizon", "ground"):
+        sky[k] = scene.sky[k]
+    cam = np.zeros(1, CAMERA_DTYPE)
+    for k in ("eye", "target", "up", "fov", "aperture", "focus"):
+        cam[k] = scene.camera[k]
+    region = np.zeros(1, REGION_DTYPE)
+    region["lower"] = scene.region_lower
+    region["size"] = scene.region_size
+    return {
+        "scene.steps": np.ascontiguousarray(scene.steps),
+        "scene.programs": refs,
+        "scene.leaves": np.ascontiguousarray(scene.leaf_material, np.uint32),
+        "looks.materials": mats,
+        "lighting.lights": lights,
+        "lighting.sky": sky,
+        "shot.camera": cam,
+        "geometry.region": region,
+    }
+
+
+class Backend:
+    """One kdn context on one CUDA device."""
+
+    def __init__(self, device: int = 0):
+        self.lib = library()
+        self.handle = ctypes.c_void_p()
+        st = self.lib.kdn_open(device, ctypes.byref(self.handle))
+        if st != KDN_OK:
+            raise KdnError(st, self.lib.kdn_last_error(None).decode())
+        self.scene: Scene | None = None
+
+    def _check(self, st: int) -> None:
+        if st != KDN_OK:
+            raise KdnError(st, self.lib.kdn_last_error(self.handle).decode())
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.kdn_close(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __enter__(self) -> "Backend":
+        return self
+
+    def __exit__(self, *exc) -> None:
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, name: str, array: np.ndarray) -> None:
+        a = np.ascontiguousarray(array)
+        self._check(self.lib.kdn_upload_block(self.handle, name.encode(), _ptr(a), a.shape[0], a.dtype.itemsize))
+
+    def load(self, scene: Scene) -> None:
+        for name, arr in scene_blocks(scene).items():
+            self.upload(name, arr)
+        self.scene = scene
+
+    def build(self, min_depth: int = 6, max_depth: int = 10, split_steps: int = 96) -> None:
+        o = BuildOptions(min_depth, max_depth, split_steps, 0)
+        self._check(self.lib.kdn_build(self.handle, ctypes.byref(o)))
+
+    def world_stats(self) -> dict:
+        out = np.zeros(4, np.uint64)
+        self._check(self.lib.kdn_world_stats(self.handle, _ptr(out)))
+        return dict(cells=int(out[0]), leaves=int(out[1]), programs=int(out[2]), steps=int(out[3]))
+
+    def world_cell(self, i: int):
+        """(level, place, occupancy, [(object, result, steps)]) of cell i in
+        depth-first pre-order, the programs in the reference's Step form."""
+        head = np.zeros(6, np.uint32)
+        self._check(self.lib.kdn_world_cell(self.handle, i, _ptr(head), None, None, None, None, 0))
+        n = int(head[5])
+        objects = np.zeros(max(n, 1), np.uint32)
+        results = np.zeros(max(n, 1), np.uint32)
+        counts = np.zeros(max(n, 1), np.uint32)
+        self._check(self.lib.kdn_world_cell(self.handle, i, _ptr(head), _ptr(objects), _ptr(results), _ptr(counts), None, 0))
+        steps = np.zeros(max(int(counts[:n].sum()), 1), STEP_DTYPE)
+        self._check(self.lib.kdn_world_cell(self.handle, i, _ptr(head), _ptr(objects), _ptr(results), _ptr(counts), _ptr(steps), steps.shape[0]))
+        progs, off = [], 0
+        for k in range(n):
+            c = int(counts[k])
+            progs.append((int(objects[k]), int(results[k]), steps[off:off + c]))
+            off += c
+        return int(head[0]), (int(head[1]), int(head[2]), int(head[3])), int(head[4]), progs
+
+    def extend(self, rays: np.ndarray) -> np.ndarray:
+        """ExtendRays over host arrays (core/step.cpp:132)."""
+        r = np.ascontiguousarray(rays, RAY_DTYPE)
+        hits = np.zeros(r.shape[0], HIT_DTYPE)
+        self._check(self.lib.kdn_extend(self.handle, _ptr(r), r.shape[0], _ptr(hits)))
+        return hits
+
+    def render(self, width: int, height: int, samples: int, surfaces: int | None = None, seed: int | None = None,
+               first: int = 0, accumulate: bool = False) -> np.ndarray:
+        """Draw `samples` samples a pixel and return the pixel means
+        (linear RGB, float32, height x width x 3)."""
+        sc = self.scene
+        f = Frame(width, height, samples, surfaces if surfaces is not None else int(sc.render["surfaces"]),
+                  seed if seed is not None else int(sc.render["seed"]), first, 1 if accumulate else 0, 0)
+        out = np.zeros((height, width, 3), np.float32)
+        self._check(self.lib.kdn_render(self.handle, ctypes.byref(f), _ptr(out)))
+        return out
+
+    def frame_stats(self) -> FrameStats:
+        s = FrameStats()
+        self._check(self.lib.kdn_frame_stats_get(self.handle, ctypes.byref(s)))
+        return s
+
+    def flush_l2(self) -> None:
+        self._check(self.lib.kdn_flush_l2(self.handle))

@@ -1,0 +1,66 @@
+// The state behind one kdn_ctx: blocks, the built world, device buffers.
+#pragma once
+
+#include "kdn.h"
+#include "kernels.h"
+#include "octree.h"
+
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace kdn {
+
+// A device allocation that grows on demand and is freed with the context.
+struct DeviceBuffer {
+	void* ptr    = nullptr;
+	size_t bytes = 0;
+};
+
+struct FrameState; // render.cpp
+
+struct Context {
+	int device          = 0;
+	int smCount         = 0;
+	cudaStream_t stream = nullptr;
+	std::mutex lock;
+	std::string error;
+	std::map<std::string, std::vector<uint8_t>> blocks;
+	bool built        = false;
+	bool sceneChanged = true;
+	Octree octree;
+	FlatWorld flat;
+	std::vector<int64_t> preorder; // cell index of each depth-first position
+	DeviceWorld world {};
+	DeviceBuffer nodes, leaves, programs, steps, ssa, leafMaterial, objectMaterial;
+	DeviceBuffer extendRays, extendHits, extendStates, counters, l2;
+	FrameState* frame = nullptr;
+
+	kdn_status open();
+	void release();
+	kdn_status fail(kdn_status status, const std::string& message);
+	bool check(cudaError_t e, const char* what);
+	kdn_status ensure(DeviceBuffer& buffer, size_t bytes);
+	kdn_status upload(DeviceBuffer& buffer, const void* data, size_t bytes);
+	template <typename T>
+	const std::vector<T> block(const char* name) const {
+		std::vector<T> out;
+		auto it = blocks.find(name);
+		if (it == blocks.end()) return out;
+		out.resize(it->second.size() / sizeof(T));
+		if (!out.empty()) std::memcpy(out.data(), it->second.data(), out.size() * sizeof(T));
+		return out;
+	}
+	bool has(const char* name) const { return blocks.count(name) != 0; }
+	kdn_status build(const BuildOptions& options);
+	int64_t preorderCell(uint64_t i) const;
+	kdn_status extend(const kdn_ray* rays, uint32_t n, kdn_hit* hits, cudaStream_t on);
+	kdn_status flushL2();
+	void releaseFrame();
+};
+
+} // namespace kdn

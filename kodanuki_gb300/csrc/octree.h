@@ -1,0 +1,57 @@
+// Host build of the cut octree and its flattening into the device layout.
+#pragma once
+
+#include "kdn.h"
+#include "world.h"
+
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace kdn {
+
+// A program as the reference keeps one (sdf/program.h:62 Program): steps in
+// SSA order and the result, plus the object it was cut from.
+struct Prog {
+	std::vector<kdn_step> steps;
+	uint32_t result = 0;
+	uint32_t object = 0;
+};
+using ProgPtr = std::shared_ptr<const Prog>;
+
+struct Cell {
+	uint8_t occupancy   = Empty;
+	uint32_t level      = 0;
+	uint32_t place[3]   = { 0, 0, 0 };
+	int64_t firstChild  = -1;
+	std::vector<ProgPtr> programs; // kept programs (cut.cpp CellPrograms)
+};
+
+struct Octree {
+	double lower[3] = { 0, 0, 0 };
+	double size[3]  = { 0, 0, 0 };
+	std::vector<Cell> cells; // children of a cell contiguous, root first
+};
+
+struct BuildOptions {
+	int min_depth        = 6;
+	int max_depth        = 10;
+	uint32_t split_steps = 96;
+	size_t max_cells     = size_t(1) << 26;
+};
+
+struct FlatWorld {
+	std::vector<int32_t> nodes;
+	std::vector<GpuLeaf> leaves;
+	std::vector<uint32_t> leafPrograms;
+	std::vector<GpuProgram> programs; // one run per leaf
+	std::vector<GpuStep> steps;
+	std::vector<SsaOps> ssa;
+};
+
+// Returns an empty string, or what went wrong.
+std::string buildOctree(const std::vector<ProgPtr>& objects, const double lower[3], const double size[3], const BuildOptions& options, Octree& tree);
+std::string flattenOctree(const Octree& tree, FlatWorld& flat);
+
+} // namespace kdn

@@ -1,0 +1,301 @@
+// The geometry kernels: sphere tracing through the cut octree.
+//
+// K-trace marches each ray (plugins/geometry/sphere_trace/sphere_trace.cpp:
+// 203 sphereFromOutside, :188 sphereFromInside) by the field read from the
+// kept programs of the octree leaf the point lies in: there the kept
+// programs are exactly the objects that can be least (cut.cpp:442 deciding),
+// so the step is the scene's field.  An empty leaf holds no surface, and
+// the ray skips to where it leaves the cell.
+// K-hit then evaluates the winning program once in duals for the normal and
+// once by step number for its source leaf (sphere_trace.cpp:115 sphereField).
+#include "kernels.h"
+#include "program.cuh"
+
+#include <cuda_runtime.h>
+
+namespace kdn {
+
+namespace {
+
+constexpr int kTraceBlock = 128;
+
+__device__ __forceinline__ float slopeOf(float part) {
+	const float tiny = 1e-12f;
+	return 1.0f / (fabsf(part) < tiny ? copysignf(tiny, part) : part);
+}
+
+__device__ __forceinline__ float tolerance(const float p[3]) {
+	const float big = fmaxf(fabsf(p[0]), fmaxf(fabsf(p[1]), fabsf(p[2])));
+	return 1e-5f * fmaxf(1.0f, big * 0.0625f);
+}
+
+__device__ __forceinline__ float nudge(float t) { return fmaxf(1e-5f, fabsf(t) * 2e-6f); }
+
+struct Located {
+	uint32_t leaf;
+	float lo[3], hi[3];
+};
+
+__device__ __forceinline__ Located locate(const DeviceWorld& w, const float p[3]) {
+	Located l;
+	for (int a = 0; a < 3; ++a) {
+		l.lo[a] = w.lower[a];
+		l.hi[a] = w.lower[a] + w.size[a];
+	}
+	int32_t node = __ldg(&w.nodes[0]);
+	uint32_t at  = 0;
+	for (int depth = 0; depth < 30 && node >= 0; ++depth) {
+		int o = 0;
+		for (int a = 0; a < 3; ++a) {
+			const float mid = 0.5f * (l.lo[a] + l.hi[a]);
+			if (p[a] >= mid) {
+				o |= 1 << a;
+				l.lo[a] = mid;
+			} else {
+				l.hi[a] = mid;
+			}
+		}
+		at   = uint32_t(node) + uint32_t(o);
+		node = __ldg(&w.nodes[at]);
+	}
+	l.leaf = uint32_t(~node);
+	return l;
+}
+
+__device__ __forceinline__ float cellExit(const float o[3], const float inv[3], const Located& l) {
+	float up = 3.0e38f;
+	for (int a = 0; a < 3; ++a) {
+		const float x = (l.lo[a] - o[a]) * inv[a];
+		const float y = (l.hi[a] - o[a]) * inv[a];
+		up            = fminf(up, fmaxf(x, y));
+	}
+	return up;
+}
+
+struct Field {
+	float least;   // least program value
+	float nearest; // least magnitude
+	uint32_t index;  // which kept program is least
+	uint32_t count;  // kept programs
+	uint32_t first;  // first GpuProgram of the leaf
+	bool empty;
+	float exit;
+};
+
+__device__ __forceinline__ Field fieldAt(const DeviceWorld& w, const float o[3], const float d[3], const float inv[3], float t, float* slots, uint32_t stride, unsigned long long& steps) {
+	Field f;
+	const float p[3] = { o[0] + d[0] * t, o[1] + d[1] * t, o[2] + d[2] * t };
+	const Located l  = locate(w, p);
+	const GpuLeaf leaf = w.leaves[l.leaf];
+	f.first  = leaf.first;
+	f.count  = leaf.count;
+	f.empty  = leaf.occupancy == Empty || leaf.count == 0;
+	f.least  = 3.0e38f;
+	f.nearest = 3.0e38f;
+	f.index  = 0;
+	f.exit   = f.empty ? cellExit(o, inv, l) : 0.0f;
+	if (f.empty) return f;
+	for (uint32_t k = 0; k < leaf.count; ++k) {
+		const GpuProgram g = w.programs[leaf.first + k];
+		const float v      = evalSlots(w.steps + g.code, g.count, g.slot, slots, stride, p);
+		steps += g.count;
+		if (v < f.least) {
+			f.least = v;
+			f.index = k;
+		}
+		f.nearest = fminf(f.nearest, fabsf(v));
+	}
+	return f;
+}
+
+// The least value at t, and the index of the kept program that is least a
+// little further along among those tied with it (sphere_trace.cpp:96).
+__device__ uint32_t winnerAt(const DeviceWorld& w, const float o[3], const float d[3], float t, const Field& f, float* slots, uint32_t stride) {
+	const float p[3] = { o[0] + d[0] * t, o[1] + d[1] * t, o[2] + d[2] * t };
+	const float big  = fmaxf(fabsf(p[0]), fmaxf(fabsf(p[1]), fabsf(p[2])));
+	const float band = 2e-6f * (1.0f + big);
+	const float q[3] = { p[0] + d[0] * 2e-5f, p[1] + d[1] * 2e-5f, p[2] + d[2] * 2e-5f };
+	uint32_t winner  = f.index;
+	float onWinner   = 3.0e38f;
+	bool tied        = false;
+	float values[kMaxLeafProgs];
+	for (uint32_t k = 0; k < f.count && k < kMaxLeafProgs; ++k) {
+		const GpuProgram g = w.programs[f.first + k];
+		values[k]          = evalSlots(w.steps + g.code, g.count, g.slot, slots, stride, p);
+		tied               = tied || (k != f.index && values[k] - f.least <= band);
+	}
+	if (!tied) return winner;
+	for (uint32_t k = 0; k < f.count && k < kMaxLeafProgs; ++k) {
+		if (!(values[k] - f.least <= band)) continue;
+		const GpuProgram g = w.programs[f.first + k];
+		const float on     = evalSlots(w.steps + g.code, g.count, g.slot, slots, stride, q);
+		if (on < onWinner) {
+			onWinner = on;
+			winner   = k;
+		}
+	}
+	return winner;
+}
+
+__global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
+	extern __shared__ float slotMemory[];
+	const DeviceWorld& w  = args.world;
+	const uint32_t stride = blockDim.x;
+	float* slots          = slotMemory + threadIdx.x;
+	unsigned long long marchSteps = 0, programSteps = 0;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < args.n; i += gridDim.x * blockDim.x) {
+		const kdn_ray ray = args.rays[i];
+		const float o[3]  = { ray.origin[0], ray.origin[1], ray.origin[2] };
+		const float d[3]  = { ray.direction[0], ray.direction[1], ray.direction[2] };
+		const float inv[3] = { slopeOf(d[0]), slopeOf(d[1]), slopeOf(d[2]) };
+		float lo = 0.0f, up = ray.far;
+		for (int a = 0; a < 3; ++a) {
+			const float x = (w.lower[a] - o[a]) * inv[a];
+			const float y = (w.lower[a] + w.size[a] - o[a]) * inv[a];
+			lo            = fmaxf(lo, fminf(x, y));
+			up            = fminf(up, fmaxf(x, y));
+		}
+		HitState h = { 0, 0.0f, kNoLeaf, 0, 0 };
+		float t    = lo;
+		uint32_t step = 0;
+		if (!(up < lo)) {
+			for (; step < args.maxSteps && t <= up; ++step) {
+				const Field f = fieldAt(w, o, d, inv, t, slots, stride, programSteps);
+				if (f.empty) {
+					t = fmaxf(f.exit, t) + nudge(t);
+					continue;
+				}
+				const float p[3] = { o[0] + d[0] * t, o[1] + d[1] * t, o[2] + d[2] * t };
+				const float tol  = tolerance(p);
+				if (!ray.inside) {
+					if (f.least < tol) {
+						h = { 1, t, f.first, winnerAt(w, o, d, t, f, slots, stride), step + 1 };
+						break;
+					}
+					t += f.least;
+					continue;
+				}
+				// sphereFromInside: stand on the nearest surface and read the field past it.
+				if (f.nearest < tol) {
+					const float inset = 2.0f * tol;
+					const Field past  = fieldAt(w, o, d, inv, t + inset, slots, stride, programSteps);
+					if (past.empty || past.least > 0.0f) {
+						h = { 1, t, f.first, winnerAt(w, o, d, t, f, slots, stride), step + 1 };
+						break;
+					}
+					const GpuProgram g   = w.programs[past.first + past.index];
+					const uint32_t there = g.object;
+					// The solid past the point is another material than the one the ray is in: stop there.
+					if (args.objectMaterial != nullptr && args.objectMaterial[there] != ray.within) {
+						h = { 2, t, past.first, past.index, step + 1 };
+						break;
+					}
+					t += inset;
+					continue;
+				}
+				t += f.nearest;
+			}
+		}
+		marchSteps += step;
+		args.states[i] = h;
+	}
+	if (args.counters) {
+		atomicAdd(&args.counters[0], marchSteps);
+		atomicAdd(&args.counters[1], programSteps);
+	}
+}
+
+__global__ void __launch_bounds__(kTraceBlock) hitKernel(HitArgs args) {
+	const DeviceWorld& w = args.world;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < args.n; i += gridDim.x * blockDim.x) {
+		const HitState h  = args.states[i];
+		const kdn_ray ray = args.rays[i];
+		kdn_hit out;
+		out.kind = 0;
+		out.pad0_[0] = out.pad0_[1] = out.pad0_[2] = 0;
+		out.distance = 0.0f;
+		for (int a = 0; a < 3; ++a) {
+			out.point[a]  = 0.0f;
+			out.normal[a] = 0.0f;
+		}
+		out.leaf      = kNoLeaf;
+		out.other     = kNoLeaf;
+		out.share     = 0.0f;
+		out.loosened  = 0.0f;
+		out.leaf_kind = 0;
+		out.pad1_[0] = out.pad1_[1] = out.pad1_[2] = 0;
+		out.cell      = kNoLeaf;
+		if (h.kind != 0) {
+			const float d[3]  = { ray.direction[0], ray.direction[1], ray.direction[2] };
+			const float t     = h.distance;
+			const float p[3]  = { ray.origin[0] + d[0] * t, ray.origin[1] + d[1] * t, ray.origin[2] + d[2] * t };
+			// For a crossing into another material the field is read past the point.
+			const float inset = h.kind == 2 ? 2.0f * tolerance(p) : 0.0f;
+			const float q[3]  = { p[0] + d[0] * inset, p[1] + d[1] * inset, p[2] + d[2] * inset };
+			const GpuProgram g = w.programs[h.first + h.index];
+			DualF dslots[kMaxSlots];
+			for (uint32_t s = 0; s < kMaxSlots; ++s) dslots[s] = dualConst(0.0f);
+			const DualF v = evalDual(w.steps + g.code, g.count, g.slot, dslots, q);
+			float values[kMaxSsa];
+			uint32_t leaf, other;
+			float share;
+			sourceOf(w.steps + g.code, w.ssa + g.code, g.count, g.result, values, q, leaf, other, share);
+			// sphereNormal (sphere_trace.cpp:140)
+			float n[3];
+			const float len = sqrtf(v.g0 * v.g0 + v.g1 * v.g1 + v.g2 * v.g2);
+			if (!(len > 0.0f)) {
+				for (int a = 0; a < 3; ++a) n[a] = -d[a];
+			} else {
+				n[0] = v.g0 / len;
+				n[1] = v.g1 / len;
+				n[2] = v.g2 / len;
+				const float along = n[0] * d[0] + n[1] * d[1] + n[2] * d[2];
+				if (ray.inside) {
+					if (along < 0.0f) {
+						for (int a = 0; a < 3; ++a) n[a] = -n[a];
+					}
+				} else if (along > 0.0f) {
+					float gz[3];
+					for (int a = 0; a < 3; ++a) gz[a] = n[a] - d[a] * (along + 0.02f);
+					const float gl = sqrtf(gz[0] * gz[0] + gz[1] * gz[1] + gz[2] * gz[2]);
+					for (int a = 0; a < 3; ++a) n[a] = gz[a] / gl;
+				}
+			}
+			out.kind     = 1;
+			out.distance = t;
+			for (int a = 0; a < 3; ++a) {
+				out.point[a]  = p[a];
+				out.normal[a] = n[a];
+			}
+			out.leaf     = leaf;
+			out.other    = other;
+			out.share    = share;
+			out.loosened = tolerance(p);
+			out.cell     = g.object;
+		}
+		args.hits[i] = out;
+	}
+}
+
+} // namespace
+
+cudaError_t launchTrace(const TraceArgs& args, cudaStream_t stream, int smCount) {
+	if (args.n == 0) return cudaSuccess;
+	const uint32_t blocks = uint32_t(std::min<uint64_t>((uint64_t(args.n) + kTraceBlock - 1) / kTraceBlock, uint64_t(smCount) * 16));
+	const size_t shared   = size_t(kMaxSlots) * kTraceBlock * sizeof(float);
+	traceKernel<<<blocks, kTraceBlock, shared, stream>>>(args);
+	return cudaGetLastError();
+}
+
+cudaError_t launchHits(const HitArgs& args, cudaStream_t stream, int smCount) {
+	if (args.n == 0) return cudaSuccess;
+	const uint32_t blocks = uint32_t(std::min<uint64_t>((uint64_t(args.n) + kTraceBlock - 1) / kTraceBlock, uint64_t(smCount) * 16));
+	hitKernel<<<blocks, kTraceBlock, 0, stream>>>(args);
+	return cudaGetLastError();
+}
+
+cudaError_t setTraceAttributes() {
+	return cudaFuncSetAttribute(traceKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kMaxSlots * kTraceBlock * sizeof(float)));
+}
+
+} // namespace kdn

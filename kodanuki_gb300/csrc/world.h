@@ -1,0 +1,82 @@
+// Device-resident world of the GB300 backend: the cut octree and the kept
+// programs of its leaves, in the layout the trace kernel reads.
+//
+// The octree is a pointer-free array of 32-bit nodes, children of a node
+// contiguous (breadth-first per parent).  A node holds the index of its first
+// child, or ~leaf for a leaf.  A leaf names a run of kept programs; a program
+// is a run of 16-byte GpuSteps whose operands are register slots (a linear
+// scan over the straight-line program reuses a slot once its value is dead),
+// so the march keeps a program's live values in a few shared-memory slots.
+// The same steps keep their SSA operand numbers in a parallel array for the
+// single evaluation at a hit that finds the source leaf (sdf/program.cpp:505).
+#pragma once
+
+#include <cstdint>
+
+namespace kdn {
+
+// sdf/program.h:20 Opcode values.
+enum Op : uint8_t {
+	OpConstant, OpArgument, OpPointX, OpPointY, OpPointZ, OpNormalX, OpNormalY, OpNormalZ,
+	OpAdd, OpSubtract, OpMultiply, OpDivide, OpNegate, OpSqrt, OpAbs, OpFloor, OpSin, OpCos,
+	OpSign, OpAtan2, OpPow, OpMin, OpMax, OpSmin, OpPosSq, OpLess, OpLessEq, OpEqual,
+	OpNotEqual, OpAnd, OpOr, OpNot, OpSelect, OpCount
+};
+
+constexpr uint32_t kNoLeaf     = 0xFFFFFFFFu;
+constexpr uint32_t kMaxSlots   = 48;   // register slots a leaf program may use
+constexpr uint32_t kMaxSsa     = 1024; // steps a leaf program may hold
+constexpr uint32_t kMaxLeafProgs = 64; // kept programs of one leaf
+
+struct GpuStep {
+	uint8_t op;
+	uint8_t dst;
+	uint8_t a, b, c;
+	uint8_t pad0;
+	uint16_t pad1;
+	float value;
+	uint32_t leaf;
+};
+static_assert(sizeof(GpuStep) == 16, "GpuStep is 16 bytes");
+
+struct SsaOps {
+	uint16_t a, b, c, pad;
+};
+static_assert(sizeof(SsaOps) == 8, "SsaOps is 8 bytes");
+
+struct GpuProgram {
+	uint32_t code;      // first GpuStep
+	uint16_t count;     // steps
+	uint16_t result;    // SSA index of the result
+	uint8_t slot;       // slot of the result
+	uint8_t slots;      // slots used
+	uint16_t pad;
+	uint32_t object;    // index into the scene's object programs
+};
+static_assert(sizeof(GpuProgram) == 16, "GpuProgram is 16 bytes");
+
+enum Occupancy : uint8_t { Empty = 0, Filled = 1, Surface = 2 };
+
+struct GpuLeaf {
+	uint32_t first;     // first GpuProgram
+	uint16_t count;     // kept programs
+	uint8_t occupancy;
+	uint8_t slots;      // most slots of its programs
+};
+static_assert(sizeof(GpuLeaf) == 8, "GpuLeaf is 8 bytes");
+
+// Everything the trace kernel reads, as device pointers.
+struct DeviceWorld {
+	const int32_t* nodes;
+	const GpuLeaf* leaves;
+	const GpuProgram* programs;
+	const GpuStep* steps;
+	const SsaOps* ssa;
+	const uint32_t* leaf_material;
+	float lower[3];
+	float size[3];
+	uint32_t leaf_count;
+	uint32_t material_count;
+};
+
+} // namespace kdn

@@ -1,0 +1,241 @@
+"""Seeded synthetic scenes in the reference renderer's `.sdf` language.
+
+The reference ships hand-written scenes only, so the workloads are written
+here from a seed: the same text is loaded by the reference renderer (which
+compiles it to object programs, target/docs/reference_language.md) and by
+the fixture exporter that turns the compiled scene into the blocks this
+backend consumes.  Every random draw comes from ``random.Random(seed)``, so
+a (config, seed) pair names one scene.
+
+Emitters that the workloads describe as blackbodies are converted to
+linear-RGB power here (the reference has RGB lights only, its
+``Light.power`` in sdf/scene.h), by integrating Planck's law against the
+CIE 1931 observer (the analytic multi-lobe fit of Wyman, Sloan and Shirley,
+JCGT 2013) and the sRGB primaries.
+"""
+from __future__ import annotations
+
+import math
+import random
+
+__all__ = ["blackbody_rgb", "scene_config1", "scene_config2", "scene_room", "scene_serving", "SCENES"]
+
+
+def _cie_xyz(nm: float) -> tuple[float, float, float]:
+    def g(x, mu, s1, s2):
+        s = s1 if x < mu else s2
+        t = (x - mu) / s
+        return math.exp(-0.5 * t * t)
+
+    x = 1.056 * g(nm, 599.8, 37.9, 31.0) + 0.362 * g(nm, 442.0, 16.0, 26.7) - 0.065 * g(nm, 501.1, 20.4, 26.2)
+    y = 0.821 * g(nm, 568.8, 46.9, 40.5) + 0.286 * g(nm, 530.9, 16.3, 31.1)
+    z = 1.217 * g(nm, 437.0, 11.8, 36.0) + 0.681 * g(nm, 459.0, 26.0, 13.8)
+    return x, y, z
+
+
+def blackbody_rgb(kelvin: float, luminance: float = 1.0) -> list[float]:
+    """Linear sRGB of a blackbody at ``kelvin``, scaled so that its CIE Y is
+    ``luminance``.  Planck's law is integrated over 380-780 nm in 1 nm steps."""
+    h, c, k = 6.62607015e-34, 2.99792458e8, 1.380649e-23
+    X = Y = Z = 0.0
+    for i in range(380, 781):
+        lam = i * 1e-9
+        b = (2 * h * c * c) / (lam ** 5) / (math.exp(h * c / (lam * k * kelvin)) - 1)
+        x, y, z = _cie_xyz(float(i))
+        X += b * x
+        Y += b * y
+        Z += b * z
+    X, Z = X / Y * luminance, Z / Y * luminance
+    Y = luminance
+    r = 3.2406 * X - 1.5372 * Y - 0.4986 * Z
+    g = -0.9689 * X + 1.8758 * Y + 0.0415 * Z
+    b = 0.0557 * X - 0.2040 * Y + 1.0570 * Z
+    return [max(r, 0.0), max(g, 0.0), max(b, 0.0)]
+
+
+def _f(x: float) -> str:
+    return repr(round(float(x), 6))
+
+
+def _v(v) -> str:
+    return "[" + ", ".join(_f(x) for x in v) + "]"
+
+
+_SHAPES = """function sphere(r) {
+	return length(p) - r;
+}
+
+function box(size, r) {
+	let q = abs(p) - size / 2 + r;
+	return length(max(q, 0)) + min(max(q.x, max(q.y, q.z)), 0) - r;
+}
+
+function plane(normal, offset) {
+	return dot(p, normal) - offset;
+}
+
+function lattice(step, r) {
+	let q = p - step * floor(p / step + 0.5);
+	return length(q) - r;
+}
+"""
+
+
+def _header(width, height, samples, surfaces, seed, eye, target, fov, far=60.0):
+    return (
+        _SHAPES
+        + "\nrender {\n"
+        + f"\twidth    = {width};\n\theight   = {height};\n\tsamples  = {samples};\n"
+        + f"\tbatch    = {samples};\n\tsplit    = 1;\n\tsurfaces = {surfaces};\n\tseed     = {seed};\n\tfar      = {_f(far)};\n}}\n\n"
+        + "camera {\n"
+        + f"\teye    = {_v(eye)};\n\ttarget = {_v(target)};\n\tfov    = {_f(fov)};\n}}\n\n"
+    )
+
+
+def _sky(rgb):
+    return (
+        "sky gradient {\n"
+        + f"\tzenith  = {_v(rgb)};\n\thorizon = {_v(rgb)};\n\tground  = {_v(rgb)};\n}}\n\n"
+    )
+
+
+def _quad(corner, along, across, power):
+    return (
+        "light quad {\n"
+        + f"\tat     = {_v(corner)};\n\talong  = {_v(along)};\n\tacross = {_v(across)};\n\tpower  = {_v(power)};\n}}\n\n"
+    )
+
+
+def scene_config1(seed: int = 1, width: int = 256, height: int = 256, samples: int = 16, surfaces: int = 8, count: int = 64) -> str:
+    """64 primitives (spheres r~U(0.1,0.5), boxes half-extents ~U(0.1,0.4)
+    rounded 0.02) uniform in [-2,2]^3 inside one merge(0.05), above a ground
+    plane; plastic(albedo~U(0.2,0.8)^3, roughness~U(0.05,0.5)); one quad
+    light emitting 5000 K; black sky."""
+    rng = random.Random(seed)
+    out = [_header(width, height, samples, surfaces, seed, [0.0, -8.5, 3.2], [0.0, 0.0, -0.6], 0.75)]
+    out.append(_sky([0.0, 0.0, 0.0]))
+    out.append(_quad([-1.25, 1.25, 4.5], [2.5, 0.0, 0.0], [0.0, -2.5, 0.0], blackbody_rgb(5000.0, 60.0)))
+    out.append("let ground = plastic([0.5, 0.5, 0.5], roughness = 0.5);\n\n")
+    out.append("paint(ground) plane([0, 0, 1], -2.2);\n\n")
+    out.append("merge(0.05) {\n")
+    for _ in range(count):
+        albedo = [rng.uniform(0.2, 0.8) for _ in range(3)]
+        rough = rng.uniform(0.05, 0.5)
+        pos = [rng.uniform(-2.0, 2.0) for _ in range(3)]
+        mat = f"plastic({_v(albedo)}, roughness = {_f(rough)})"
+        if rng.random() < 0.5:
+            shape = f"sphere({_f(rng.uniform(0.1, 0.5))})"
+        else:
+            half = [rng.uniform(0.1, 0.4) for _ in range(3)]
+            shape = f"box({_v([2 * h for h in half])}, 0.02)"
+        out.append(f"\tpaint({mat}) at({_v(pos)}) {shape};\n")
+    out.append("}\n")
+    return "".join(out)
+
+
+def scene_config2(seed: int = 1, width: int = 1920, height: int = 1080, samples: int = 64, surfaces: int = 16, groups: int = 512) -> str:
+    """4096 primitives in groups of 8 joined by union, subtraction (cut) or
+    smooth union k~U(0.01,0.1), plus floor-based 3-axis repetition inside a
+    function; materials 40% matte, 40% metal (GGX conductor), 20% glass with
+    Cauchy dispersion (A=1.76, B=0.01 um^2); two quad lights and a constant
+    6500 K environment."""
+    rng = random.Random(seed)
+    out = [_header(width, height, samples, surfaces, seed, [0.5, -15.0, 6.5], [0.0, 0.0, -0.5], 0.8)]
+    out.append(_sky(blackbody_rgb(6500.0, 0.25)))
+    out.append(_quad([-4.0, -3.0, 7.0], [3.0, 0.0, 0.0], [0.0, 2.0, 0.0], blackbody_rgb(5000.0, 120.0)))
+    out.append(_quad([2.0, 1.0, 6.0], [2.0, 0.0, 0.0], [0.0, 2.0, 0.0], blackbody_rgb(3500.0, 80.0)))
+    out.append("paint(matte([0.45, 0.45, 0.45])) plane([0, 0, 1], -3);\n\n")
+    mats = []
+    for i in range(groups):
+        r = rng.random()
+        if r < 0.4:
+            mats.append(f"matte({_v([rng.uniform(0.2, 0.8) for _ in range(3)])})")
+        elif r < 0.8:
+            mats.append(f"metal({_v([rng.uniform(0.5, 0.95) for _ in range(3)])}, roughness = {_f(rng.uniform(0.05, 0.5))})")
+        else:
+            mats.append("glass(refraction = 1.76, dispersion = 0.01)")
+    for i in range(groups):
+        center = [rng.uniform(-8.0, 8.0), rng.uniform(-6.0, 10.0), rng.uniform(-2.5, 2.5)]
+        kind = rng.random()
+        if kind < 0.35:
+            head = "merge {"
+        elif kind < 0.65:
+            head = f"merge({_f(rng.uniform(0.01, 0.1))}) {{"
+        else:
+            head = f"cut({_f(rng.uniform(0.01, 0.05))}) {{"
+        out.append(f"paint({mats[i]}) at({_v(center)}) {head}\n")
+        for j in range(8):
+            pos = [rng.uniform(-0.45, 0.45) for _ in range(3)]
+            if i % 16 == 5 and j == 0:
+                shape = f"clip {{\n\t\tlattice(0.18, 0.05);\n\t\tbox({_v([0.7, 0.7, 0.7])}, 0.02);\n\t}}"
+                out.append(f"\tat({_v(pos)}) {shape}\n")
+                continue
+            if rng.random() < 0.5:
+                shape = f"sphere({_f(rng.uniform(0.08, 0.3))})"
+            else:
+                shape = f"box({_v([rng.uniform(0.15, 0.5) for _ in range(3)])}, 0.02)"
+            out.append(f"\tat({_v(pos)}) {shape};\n")
+        out.append("}\n\n")
+    return "".join(out)
+
+
+def scene_room(seed: int = 1, width: int = 1920, height: int = 1080, samples: int = 16, surfaces: int = 8, count: int = 64) -> str:
+    """The config-1 primitives inside a closed room of five box walls and a
+    ceiling whose only opening is an aperture of about 5% of the ceiling,
+    lit from above through it: indirect-dominated transport."""
+    rng = random.Random(seed)
+    out = [_header(width, height, samples, surfaces, seed, [0.0, -4.6, 0.4], [0.0, 0.0, -0.6], 1.0)]
+    out.append(_sky([0.0, 0.0, 0.0]))
+    out.append(_quad([-0.5, 0.5, 6.0], [1.0, 0.0, 0.0], [0.0, -1.0, 0.0], blackbody_rgb(5000.0, 400.0)))
+    out.append("let wall = matte([0.7, 0.7, 0.7]);\n\n")
+    out.append("with paint(wall) {\n")
+    out.append("\tat([0, 0, -3.2]) box([10.4, 10.4, 0.4], 0);\n")
+    out.append("\tat([-5, 0, 0]) box([0.4, 10.4, 6.8], 0);\n")
+    out.append("\tat([5, 0, 0]) box([0.4, 10.4, 6.8], 0);\n")
+    out.append("\tat([0, 5, 0]) box([10.4, 0.4, 6.8], 0);\n")
+    out.append("\tat([0, -5, 0]) box([10.4, 0.4, 6.8], 0);\n")
+    out.append("\tcut {\n\t\tat([0, 0, 3.2]) box([10.4, 10.4, 0.4], 0);\n\t\tat([0, 0, 3.2]) box([2.2, 2.2, 1.0], 0);\n\t}\n")
+    out.append("}\n\n")
+    out.append("merge(0.05) {\n")
+    for _ in range(count):
+        albedo = [rng.uniform(0.2, 0.8) for _ in range(3)]
+        pos = [rng.uniform(-2.0, 2.0) for _ in range(3)]
+        mat = f"matte({_v(albedo)})"
+        if rng.random() < 0.5:
+            shape = f"sphere({_f(rng.uniform(0.1, 0.5))})"
+        else:
+            shape = f"box({_v([2 * rng.uniform(0.1, 0.4) for _ in range(3)])}, 0.02)"
+        out.append(f"\tpaint({mat}) at({_v(pos)}) {shape};\n")
+    out.append("}\n")
+    return "".join(out)
+
+
+def scene_serving(seed: int, count: int, width: int = 640, height: int = 480, samples: int = 4) -> str:
+    """A config-1-style scene of ``count`` primitives spread over a box that
+    grows with the count, split into merge(0.05) groups of 64."""
+    rng = random.Random(seed)
+    reach = 2.0 * (count / 64.0) ** (1.0 / 3.0)
+    out = [_header(width, height, samples, 8, seed, [0.0, -4.2 * reach, 1.6 * reach], [0.0, 0.0, -0.3 * reach], 0.75)]
+    out.append(_sky([0.05, 0.05, 0.06]))
+    out.append(_quad([-0.6 * reach, 0.6 * reach, 2.2 * reach], [1.2 * reach, 0.0, 0.0], [0.0, -1.2 * reach, 0.0], blackbody_rgb(5000.0, 60.0)))
+    out.append(f"paint(plastic([0.5, 0.5, 0.5], roughness = 0.5)) plane([0, 0, 1], {_f(-1.1 * reach)});\n\n")
+    for g in range(0, count, 64):
+        out.append("merge(0.05) {\n")
+        for _ in range(min(64, count - g)):
+            albedo = [rng.uniform(0.2, 0.8) for _ in range(3)]
+            pos = [rng.uniform(-reach, reach) for _ in range(3)]
+            mat = f"plastic({_v(albedo)}, roughness = {_f(rng.uniform(0.05, 0.5))})"
+            if rng.random() < 0.5:
+                shape = f"sphere({_f(rng.uniform(0.1, 0.5))})"
+            else:
+                shape = f"box({_v([2 * rng.uniform(0.1, 0.4) for _ in range(3)])}, 0.02)"
+            out.append(f"\tpaint({mat}) at({_v(pos)}) {shape};\n")
+        out.append("}\n\n")
+    return "".join(out)
+
+
+SCENES = {
+    "config1": scene_config1,
+    "config2": scene_config2,
+    "room": scene_room,
+}

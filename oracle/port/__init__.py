@@ -1,0 +1,145 @@
+"""ctypes view of the oracle's C library (kdn_port.h), built in-tree."""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(os.path.dirname(HERE), "_build")
+LIB = os.path.join(OUT, "libkdn_oracle.so")
+SOURCES = ["geometry.c", "spectral.c", "transport.c", "denoise.c"]
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with gcc (plain C, -ffp-contract=off as the
+    reference is built) into oracle/_build/libkdn_oracle.so."""
+    srcs = [os.path.join(HERE, s) for s in SOURCES if os.path.exists(os.path.join(HERE, s))]
+    newest = max(os.path.getmtime(s) for s in srcs + [os.path.join(HERE, "kdn_port.h")])
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
+        return LIB
+    os.makedirs(OUT, exist_ok=True)
+    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-std=c11", "-ffp-contract=off", "-fno-math-errno", "-D_GNU_SOURCE",
+           "-o", LIB + ".tmp"] + srcs + ["-lm", "-lpthread"]
+    subprocess.run(cmd, check=True)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+class Step(ctypes.Structure):
+    _fields_ = [("opcode", ctypes.c_uint8), ("a", ctypes.c_uint32), ("b", ctypes.c_uint32), ("c", ctypes.c_uint32),
+                ("value", ctypes.c_double), ("leaf", ctypes.c_uint32)]
+
+
+class Program(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_void_p), ("count", ctypes.c_uint32), ("result", ctypes.c_uint32)]
+
+
+RAY_DTYPE = np.dtype([("origin", "<f4", 3), ("direction", "<f4", 3), ("far", "<f4"), ("inside", "<u4"), ("within", "<u4")])
+HIT_DTYPE = np.dtype([("kind", "<u4"), ("distance", "<f4"), ("point", "<f4", 3), ("normal", "<f4", 3), ("leaf", "<u4"),
+                      ("other", "<u4"), ("share", "<f4"), ("object", "<u4"), ("steps", "<u4")])
+
+_P = ctypes.c_void_p
+_D = ctypes.POINTER(ctypes.c_double)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        L.kp_octree_build.restype = _P
+        L.kp_octree_build.argtypes = [_P, ctypes.c_uint32, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_uint32]
+        L.kp_octree_free.argtypes = [_P]
+        L.kp_octree_cells.restype = ctypes.c_uint64
+        L.kp_octree_cells.argtypes = [_P]
+        L.kp_octree_cell.restype = ctypes.c_uint32
+        L.kp_octree_cell.argtypes = [_P, ctypes.c_uint64, _P]
+        L.kp_octree_cell_program.argtypes = [_P, ctypes.c_uint64, ctypes.c_uint32, _P, ctypes.POINTER(Program)]
+        L.kp_sphere_trace.argtypes = [_P, ctypes.c_uint32, _P, _P, _P, _P, ctypes.c_uint32, _P]
+        L.kp_octree_trace.argtypes = [_P, _P, _P, ctypes.c_uint32, _P]
+        L.kp_mixed_bits.restype = ctypes.c_uint64
+        L.kp_mixed_bits.argtypes = [ctypes.c_uint64]
+        L.kp_hashed.restype = ctypes.c_double
+        L.kp_hashed.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64]
+        L.kp_sampled_wavelengths.argtypes = [ctypes.c_double, _P, _P, _P]
+        L.kp_wavelength_share.restype = ctypes.c_double
+        L.kp_wavelength_share.argtypes = [ctypes.c_double, ctypes.c_uint32]
+        L.kp_spectrum_of.argtypes = [_P, _P, _P]
+        L.kp_colour_of.argtypes = [_P, _P, _P, _P]
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Programs:
+    """The scene's object programs as a C array of kp_program, kept alive."""
+
+    def __init__(self, scene):
+        self.steps = np.ascontiguousarray(scene.steps)
+        self.array = (Program * scene.program_count)()
+        base = self.steps.ctypes.data
+        for i in range(scene.program_count):
+            self.array[i].steps = base + int(scene.program_first[i]) * 32
+            self.array[i].count = int(scene.program_first[i + 1] - scene.program_first[i])
+            self.array[i].result = int(scene.program_result[i])
+        self.count = scene.program_count
+
+
+def sphere_trace(scene, rays: np.ndarray, lower, size) -> np.ndarray:
+    progs = Programs(scene)
+    hits = np.zeros(len(rays), HIT_DTYPE)
+    lo = np.asarray(lower, np.float64)
+    sz = np.asarray(size, np.float64)
+    mat = np.ascontiguousarray(scene.leaf_material, np.uint32)
+    lib().kp_sphere_trace(ctypes.addressof(progs.array), progs.count, _ptr(mat), _ptr(lo), _ptr(sz), _ptr(rays), len(rays), _ptr(hits))
+    return hits
+
+
+class Octree:
+    """The oracle's cut octree over a scene (kp_octree_build)."""
+
+    def __init__(self, scene, min_depth: int, max_depth: int, split_steps: int):
+        self.progs = Programs(scene)
+        self.scene = scene
+        lo = np.asarray(scene.region_lower, np.float64)
+        sz = np.asarray(scene.region_size, np.float64)
+        self.handle = lib().kp_octree_build(ctypes.addressof(self.progs.array), self.progs.count, _ptr(lo), _ptr(sz),
+                                            min_depth, max_depth, split_steps)
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            lib().kp_octree_free(self.handle)
+            self.handle = None
+
+    def cells(self) -> int:
+        return int(lib().kp_octree_cells(self.handle))
+
+    def cell(self, i: int):
+        """(level, place, occupancy, [(object, result, steps array)]) of cell i
+        in depth-first pre-order."""
+        head = np.zeros(5, np.uint32)
+        n = lib().kp_octree_cell(self.handle, i, _ptr(head))
+        progs = []
+        for k in range(n):
+            obj = ctypes.c_uint32()
+            p = Program()
+            lib().kp_octree_cell_program(self.handle, i, k, ctypes.byref(obj), ctypes.byref(p))
+            from kodanuki_gb300.scene import STEP_DTYPE
+            buf = (ctypes.c_char * (p.count * 32)).from_address(p.steps)
+            steps = np.frombuffer(bytes(buf), STEP_DTYPE).copy()
+            progs.append((obj.value, p.result, steps))
+        return int(head[0]), tuple(int(x) for x in head[1:4]), int(head[4]), progs
+
+    def trace(self, rays: np.ndarray) -> np.ndarray:
+        hits = np.zeros(len(rays), HIT_DTYPE)
+        mat = np.ascontiguousarray(self.scene.leaf_material, np.uint32)
+        lib().kp_octree_trace(self.handle, _ptr(mat), _ptr(rays), len(rays), _ptr(hits))
+        return hits

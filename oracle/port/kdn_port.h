@@ -1,0 +1,122 @@
+/*
+ * kdn_port -- the CPU oracle: a plain-C restatement of the reference
+ * renderer's algorithms on the hot path, in double precision as the
+ * reference computes them.  It is test infrastructure: the parity tests, the
+ * smoke check and the CPU baseline of bench.py call it as the checker; no
+ * product code links it.
+ *
+ * Each function cites the reference file:line whose algorithm it restates
+ * (paths relative to the reference's source/ folder).
+ */
+#ifndef KDN_PORT_H
+#define KDN_PORT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* sdf/program.h:20 Opcode, in the reference's order. */
+enum kp_op {
+	KP_CONSTANT, KP_ARGUMENT, KP_POINTX, KP_POINTY, KP_POINTZ, KP_NORMALX, KP_NORMALY, KP_NORMALZ,
+	KP_ADD, KP_SUBTRACT, KP_MULTIPLY, KP_DIVIDE, KP_NEGATE, KP_SQRT, KP_ABS, KP_FLOOR, KP_SIN, KP_COS,
+	KP_SIGN, KP_ATAN2, KP_POW, KP_MIN, KP_MAX, KP_SMIN, KP_POSSQ, KP_LESS, KP_LESSEQ, KP_EQUAL,
+	KP_NOTEQUAL, KP_AND, KP_OR, KP_NOT, KP_SELECT
+};
+
+/* sdf/program.h:56 Step, field for field (the reference's is 32 bytes). */
+typedef struct kp_step {
+	uint8_t opcode;
+	uint32_t a, b, c;
+	double value;
+	uint32_t leaf;
+} kp_step;
+
+typedef struct kp_program {
+	const kp_step* steps;
+	uint32_t count;
+	uint32_t result;
+} kp_program;
+
+typedef struct kp_interval {
+	double lower, upper;
+} kp_interval;
+
+typedef struct kp_dual {
+	double v, g[3];
+} kp_dual;
+
+typedef struct kp_source {
+	uint32_t leaf, other;
+	double share;
+} kp_source;
+
+/* Program evaluation (sdf/program.cpp:57-140). regs holds count values. */
+double kp_eval(const kp_program* p, const double pt[3], double* regs);
+kp_interval kp_eval_interval(const kp_program* p, const kp_interval box[3], kp_interval* regs);
+kp_dual kp_eval_dual(const kp_program* p, const double pt[3], kp_dual* regs);
+/* sdf/program.cpp:505 keptSourceOf over a whole program, given its values. */
+kp_source kp_source_of(const kp_program* p, const double* values);
+
+/* ---- interval-cut octree (plugins/geometry/tree/cut.cpp) ---- */
+enum kp_occupancy { KP_EMPTY = 0, KP_FILLED = 1, KP_SURFACE = 2 };
+
+typedef struct kp_octree kp_octree;
+
+/*
+ * Build the cut octree: from the region's box, cutCell (cut.cpp:463) each
+ * cell with its parent's programs and split a surface cell into its eight
+ * octants (cut.cpp:519 octantBox) while it is above min_depth, or while its
+ * programs hold more than split_steps steps and it is above max_depth.
+ */
+kp_octree* kp_octree_build(const kp_program* programs, uint32_t count, const double lower[3], const double size[3], int min_depth, int max_depth, uint32_t split_steps);
+void kp_octree_free(kp_octree* tree);
+uint64_t kp_octree_cells(const kp_octree* tree);
+/*
+ * Write cell i of the build's pre-order: level, place[3], occupancy, object
+ * count; returns the number of objects.  kp_octree_cell_program gives the
+ * k-th kept program of that cell.
+ */
+uint32_t kp_octree_cell(const kp_octree* tree, uint64_t i, uint32_t head[5]);
+void kp_octree_cell_program(const kp_octree* tree, uint64_t i, uint32_t k, uint32_t* object, kp_program* program);
+
+/* ---- geometry: hits (plugins/geometry/sphere_trace/sphere_trace.cpp) ---- */
+typedef struct kp_ray {
+	float origin[3], direction[3], far;
+	uint32_t inside;
+	uint32_t within;
+} kp_ray;
+
+typedef struct kp_hit {
+	uint32_t kind; /* 0 missed, 1 surface (core/batch.h:88 HitKind) */
+	float distance;
+	float point[3];
+	float normal[3];
+	uint32_t leaf, other;
+	float share;
+	uint32_t object;
+	uint32_t steps;
+} kp_hit;
+
+/* sphereTraced (sphere_trace.cpp:216) over every object, in double. */
+void kp_sphere_trace(const kp_program* programs, uint32_t count, const uint32_t* leaf_material, const double lower[3], const double size[3], const kp_ray* rays, uint32_t n, kp_hit* hits);
+/* The same march with each step's field read from the cut programs of the
+ * octree cell the point lies in, and empty cells skipped to their exit. */
+void kp_octree_trace(const kp_octree* tree, const uint32_t* leaf_material, const kp_ray* rays, uint32_t n, kp_hit* hits);
+
+/* ---- numbers, wavelengths and colour (math/random.cpp, math/colour.cpp) ---- */
+uint64_t kp_mixed_bits(uint64_t v);
+double kp_unit_of(uint64_t bits);
+double kp_hashed(uint64_t stream, uint64_t index, uint64_t coordinate);
+/* basis: the red, green and blue upsampling curves at the four lanes */
+void kp_sampled_wavelengths(double u, double nanometres[4], double density[4], double basis[12]);
+double kp_wavelength_share(double start, uint32_t index);
+void kp_spectrum_of(const double rgb[3], const double basis[12], double out[4]);
+void kp_colour_of(const double nanometres[4], const double density[4], const double spectrum[4], double rgb[3]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

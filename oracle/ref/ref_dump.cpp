@@ -1,0 +1,219 @@
+// Fixture exporter over the reference renderer's own library (built from its
+// sources by oracle/ref/Makefile).  It is test infrastructure: it runs only in
+// the container that holds the reference checkout and writes the golden
+// inputs/outputs the parity tests read.
+//
+//   kdn_ref_dump scene  <file.sdf> <out.json>            compiled scene as JSON
+//   kdn_ref_dump trace  <file.sdf> <rays.f32> <hits.bin>  sphereTraced per ray
+//   kdn_ref_dump cut    <file.sdf> <depth> <out.bin>      cutCell down an octree
+//
+// Reference entry points used: loadScene (syntax/evaluator.cpp:2898),
+// sceneRegion (plugins/geometry/tree/build.cpp:405), sphereTraced
+// (plugins/geometry/sphere_trace/sphere_trace.cpp:216), rootPrograms/cutCell/
+// octantBox/regionBox (plugins/geometry/tree/cut.cpp:463 ff).
+#include "plugins/geometry/sphere_trace/sphere_trace.h"
+#include "plugins/geometry/tree/build.h"
+#include "plugins/geometry/tree/cut.h"
+#include "sdf/program.h"
+#include "sdf/scene.h"
+#include "syntax/evaluator.h"
+
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace kodanuki;
+
+namespace {
+
+SceneFile loaded(const char* path) {
+	LoadedScene scene = loadScene(path, 0.0);
+	if (!scene.error.empty()) {
+		std::fprintf(stderr, "%s\n", scene.error.c_str());
+		std::exit(1);
+	}
+	return scene.file;
+}
+
+void putDouble(FILE* f, double v) {
+	std::fprintf(f, "%.17g", v);
+}
+
+void putVector(FILE* f, const math::Vector& v) {
+	std::fprintf(f, "[%.17g,%.17g,%.17g]", v.x, v.y, v.z);
+}
+
+void putColour(FILE* f, const Colour& c) {
+	std::fprintf(f, "[%.17g,%.17g,%.17g]", c.red, c.green, c.blue);
+}
+
+int dumpScene(const char* sdf, const char* out) {
+	const SceneFile file = loaded(sdf);
+	const Region region  = sceneRegion(file.scene, file.shot, 8);
+	FILE* f              = std::fopen(out, "w");
+	std::fprintf(f, "{\"region\":{\"lower\":[%.17g,%.17g,%.17g],\"size\":[%.17g,%.17g,%.17g]},\n", region.lower[0], region.lower[1], region.lower[2], region.size[0], region.size[1], region.size[2]);
+	std::fprintf(f, "\"programs\":[\n");
+	for (std::size_t i = 0; i < file.scene.objectPrograms.size(); ++i) {
+		const Program& program = file.scene.objectPrograms[i];
+		std::fprintf(f, "%s{\"result\":%u,\"steps\":[", i ? ",\n" : "", program.result);
+		for (std::size_t s = 0; s < program.steps.size(); ++s) {
+			const Step& step = program.steps[s];
+			std::fprintf(f, "%s[%d,%u,%u,%u,%.17g,%u]", s ? "," : "", int(step.opcode), step.a, step.b, step.c, step.value, step.leaf);
+		}
+		std::fprintf(f, "]}");
+	}
+	std::fprintf(f, "],\n\"leaves\":[");
+	for (std::size_t i = 0; i < file.scene.leaves.size(); ++i) {
+		std::fprintf(f, "%s%u", i ? "," : "", file.scene.leaves[i].material);
+	}
+	std::fprintf(f, "],\n\"materials\":[");
+	for (std::size_t i = 0; i < file.looks.materials.size(); ++i) {
+		const Material& m = file.looks.materials[i];
+		std::fprintf(f, "%s{\"kind\":%d,\"stops\":[", i ? ",\n" : "", int(m.kind));
+		for (std::size_t s = 0; s < m.albedo.stops.size(); ++s) {
+			std::fprintf(f, "%s%.9g", s ? "," : "", double(m.albedo.stops[s]));
+		}
+		std::fprintf(f, "],\"pattern\":%d,\"roughness\":%.9g,\"refraction\":%.9g,\"dispersion\":%.9g,\"scatter\":%.9g,\"absorb\":", m.albedo.program, double(m.roughness), double(m.refraction), double(m.dispersion), double(m.scatter));
+		putColour(f, m.absorb);
+		std::fprintf(f, ",\"glow\":");
+		putColour(f, m.glow);
+		std::fprintf(f, ",\"strength\":%.9g,\"film\":[%.9g,%.9g],\"coats\":%zu}", double(m.strength), double(m.film[0]), double(m.film[1]), file.looks.coats.size());
+	}
+	std::fprintf(f, "],\n\"lights\":[");
+	for (std::size_t i = 0; i < file.lighting.lights.size(); ++i) {
+		const Light& l = file.lighting.lights[i];
+		std::fprintf(f, "%s{\"kind\":%d,\"at\":", i ? ",\n" : "", int(l.kind));
+		putVector(f, l.at);
+		std::fprintf(f, ",\"direction\":");
+		putVector(f, l.direction);
+		std::fprintf(f, ",\"along\":");
+		putVector(f, l.along);
+		std::fprintf(f, ",\"across\":");
+		putVector(f, l.across);
+		std::fprintf(f, ",\"radius\":%.9g,\"angle\":%.9g,\"power\":", double(l.radius), double(l.angle));
+		putColour(f, l.power);
+		std::fprintf(f, "}");
+	}
+	const Sky& sky = file.lighting.sky;
+	std::fprintf(f, "],\n\"sky\":{\"kind\":%d,\"zenith\":", int(sky.kind));
+	putColour(f, sky.zenith);
+	std::fprintf(f, ",\"horizon\":");
+	putColour(f, sky.horizon);
+	std::fprintf(f, ",\"ground\":");
+	putColour(f, sky.ground);
+	const Camera& c = file.shot.camera;
+	const Render& r = file.shot.render;
+	std::fprintf(f, "},\n\"camera\":{\"eye\":");
+	putVector(f, c.eye);
+	std::fprintf(f, ",\"target\":");
+	putVector(f, c.target);
+	std::fprintf(f, ",\"up\":");
+	putVector(f, c.up);
+	std::fprintf(f, ",\"fov\":%.9g,\"aperture\":%.9g,\"focus\":%.9g},\n", double(c.fov), double(c.aperture), double(c.focus));
+	std::fprintf(f, "\"render\":{\"width\":%d,\"height\":%d,\"seed\":%d,\"samples\":%d,\"surfaces\":%d,\"far\":", r.width, r.height, r.seed, r.samples, r.surfaces);
+	putDouble(f, r.far);
+	std::fprintf(f, "}}\n");
+	std::fclose(f);
+	return 0;
+}
+
+// Rays: float32 records of 8 (origin xyz, direction xyz, far, inside) plus the
+// reference region; hits: per ray {kind u32, distance f32, point f32x3,
+// normal f32x3, leaf u32, other u32, share f32} = 44 bytes.
+int dumpTrace(const char* sdf, const char* raysPath, const char* hitsPath) {
+	const SceneFile file = loaded(sdf);
+	const Region region  = reachRegion(file.shot);
+	const Geometry geo   = sphereGeometry(file.scene, region);
+	FILE* in             = std::fopen(raysPath, "rb");
+	std::vector<float> rays;
+	float record[8];
+	while (std::fread(record, sizeof(float), 8, in) == 8) {
+		rays.insert(rays.end(), record, record + 8);
+	}
+	std::fclose(in);
+	FILE* out = std::fopen(hitsPath, "wb");
+	for (std::size_t i = 0; i < rays.size(); i += 8) {
+		const Ray ray = {
+			.origin    = { rays[i], rays[i + 1], rays[i + 2] },
+			.direction = { rays[i + 3], rays[i + 4], rays[i + 5] },
+			.far       = rays[i + 6],
+			.inside    = rays[i + 7] != 0,
+			.within    = noMaterial,
+		};
+		const Hit hit           = sphereTraced(geo, ray);
+		const std::uint32_t u[] = { std::uint32_t(hit.kind) };
+		std::fwrite(u, 4, 1, out);
+		const float g[] = { hit.distance, hit.point.x, hit.point.y, hit.point.z, hit.normal.x, hit.normal.y, hit.normal.z };
+		std::fwrite(g, 4, 7, out);
+		const std::uint32_t ids[] = { hit.leaf, hit.other };
+		std::fwrite(ids, 4, 2, out);
+		std::fwrite(&hit.share, 4, 1, out);
+	}
+	std::fclose(out);
+	return 0;
+}
+
+struct CutWriter {
+	FILE* out;
+	int depth;
+	std::uint64_t leaves;
+};
+
+// Per visited cell (pre-order): level u32, place xyz u32, occupancy u32,
+// object count u32, then per object: object u32, result u32, step count u32,
+// steps (opcode u32, a, b, c u32, value f64, leaf u32).  A surface cell above
+// the depth is split into its eight octants and recursed.
+void writeCell(CutWriter& writer, const CellPrograms& programs, const Box& box, int level, const std::uint32_t place[3]) {
+	const CellCut cut       = cutCell(programs, box);
+	const std::uint32_t h[] = { std::uint32_t(level), place[0], place[1], place[2], std::uint32_t(cut.occupancy), std::uint32_t(cut.programs.objects.size()) };
+	std::fwrite(h, 4, 6, writer.out);
+	for (std::size_t i = 0; i < cut.programs.objects.size(); ++i) {
+		const Program& program  = *cut.programs.programs[i];
+		const std::uint32_t o[] = { cut.programs.objects[i], program.result, std::uint32_t(program.steps.size()) };
+		std::fwrite(o, 4, 3, writer.out);
+		for (const Step& step : program.steps) {
+			const std::uint32_t s[] = { std::uint32_t(step.opcode), step.a, step.b, step.c };
+			std::fwrite(s, 4, 4, writer.out);
+			std::fwrite(&step.value, 8, 1, writer.out);
+			std::fwrite(&step.leaf, 4, 1, writer.out);
+		}
+	}
+	++writer.leaves;
+	if (cut.occupancy != Occupancy::Surface || level >= writer.depth) {
+		return;
+	}
+	for (int octant = 0; octant < 8; ++octant) {
+		const std::uint32_t child[3] = { place[0] * 2 + (octant & 1), place[1] * 2 + ((octant >> 1) & 1), place[2] * 2 + ((octant >> 2) & 1) };
+		writeCell(writer, cut.programs, octantBox(box, octant), level + 1, child);
+	}
+}
+
+int dumpCut(const char* sdf, int depth, const char* outPath) {
+	const SceneFile file = loaded(sdf);
+	const Region region  = sceneRegion(file.scene, file.shot, 8);
+	CutWriter writer     = { std::fopen(outPath, "wb"), depth, 0 };
+	const std::uint32_t root[3] = { 0, 0, 0 };
+	writeCell(writer, rootPrograms(file.scene), regionBox(region), 0, root);
+	std::fclose(writer.out);
+	std::fprintf(stderr, "%llu cells\n", (unsigned long long) writer.leaves);
+	return 0;
+}
+
+} // namespace
+
+int main(int argc, char** argv) {
+	if (argc >= 4 && std::strcmp(argv[1], "scene") == 0) {
+		return dumpScene(argv[2], argv[3]);
+	}
+	if (argc >= 5 && std::strcmp(argv[1], "trace") == 0) {
+		return dumpTrace(argv[2], argv[3], argv[4]);
+	}
+	if (argc >= 5 && std::strcmp(argv[1], "cut") == 0) {
+		return dumpCut(argv[2], std::atoi(argv[3]), argv[4]);
+	}
+	std::fprintf(stderr, "usage: kdn_ref_dump scene|trace|cut ...\n");
+	return 2;
+}

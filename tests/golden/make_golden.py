@@ -1,0 +1,173 @@
+"""Regenerate the golden fixtures from the reference renderer itself.
+
+Run only where the reference checkout and its oracle build exist:
+
+    make -C oracle/ref REF=/root/reference -j8
+    python tests/golden/make_golden.py [--ref-bin oracle/_ref] [--only NAME]
+
+It writes, under tests/golden/:
+  scenes/<name>.npz      the compiled scene (kodanuki_gb300.scene.Scene)
+  trace_<name>.npz       seeded rays and the reference's sphereTraced hits
+  cut_<name>.npz         cutCell results down a fixed-depth octree
+  image_<name>.npz       reference frames (fixed spp, two seeds)
+Every input is seeded; rerunning gives the same files.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import struct
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from kodanuki_gb300 import scenegen  # noqa: E402
+from kodanuki_gb300.scene import STEP_DTYPE, Scene  # noqa: E402
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+# name -> (generator, kwargs, trace rays, cut depth)
+SCENES = {
+    "c1": (scenegen.scene_config1, dict(seed=1), 2000, 4),
+    "c1_small": (scenegen.scene_config1, dict(seed=2, width=48, height=48, samples=64, count=12), 0, 0),
+    "room": (scenegen.scene_room, dict(seed=1), 0, 0),
+    "room_small": (scenegen.scene_room, dict(seed=3, width=48, height=48, samples=64, count=8), 0, 0),
+    "c2": (scenegen.scene_config2, dict(seed=1), 200, 3),
+}
+
+
+def camera_rays(scene: Scene, n: int, rng: np.random.Generator) -> np.ndarray:
+    """Rays from the eye through random film points (core/camera.cpp:34)."""
+    cam = scene.camera
+    eye = np.array(cam["eye"])
+    target = np.array(cam["target"])
+    up = np.array(cam["up"])
+    fwd = (target - eye) / np.linalg.norm(target - eye)
+    right = np.cross(fwd, up)
+    right /= np.linalg.norm(right)
+    upv = np.cross(right, fwd)
+    reach = np.tan(cam["fov"] / 2)
+    w, h = scene.render["width"], scene.render["height"]
+    x = rng.uniform(0, w, n)
+    y = rng.uniform(0, h, n)
+    u = 2 * x / w - 1
+    v = 1 - 2 * y / h
+    d = fwd[None] + right[None] * (u * reach * w / h)[:, None] + upv[None] * (v * reach)[:, None]
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0:3] = eye
+    rays[:, 3:6] = d
+    rays[:, 6] = np.inf
+    return rays
+
+
+def scattered_rays(scene: Scene, n: int, rng: np.random.Generator) -> np.ndarray:
+    """Rays from random points near the objects in random directions."""
+    o = rng.uniform(-3, 3, (n, 3))
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0:3] = o
+    rays[:, 3:6] = d
+    rays[:, 6] = np.inf
+    return rays
+
+
+def step_digest(steps: np.ndarray) -> int:
+    """64-bit FNV-1a over each step's opcode, a, b, c, value bits and leaf,
+    little-endian: a golden digest of a cut program."""
+    h = 0xCBF29CE484222325
+    for s in steps:
+        rec = struct.pack("<IIIIQI", int(s["opcode"]), int(s["a"]), int(s["b"]), int(s["c"]), int(np.float64(s["value"]).view(np.uint64)), int(s["leaf"]))
+        for byte in rec:
+            h = ((h ^ byte) * 0x100000001B3) & 0xFFFFFFFFFFFFFFFF
+    return h
+
+
+def read_cut(path: str):
+    data = open(path, "rb").read()
+    off = 0
+    cells = []
+    while off < len(data):
+        level, px, py, pz, occ, n = struct.unpack_from("<6I", data, off)
+        off += 24
+        progs = []
+        for _ in range(n):
+            obj, result, count = struct.unpack_from("<3I", data, off)
+            off += 12
+            steps = np.zeros(count, STEP_DTYPE)
+            for s in range(count):
+                op, a, b, c = struct.unpack_from("<4I", data, off)
+                value, = struct.unpack_from("<d", data, off + 16)
+                leaf, = struct.unpack_from("<I", data, off + 24)
+                off += 28
+                steps[s] = (op, a, b, c, value, leaf)
+            progs.append((obj, result, steps))
+        cells.append((level, (px, py, pz), occ, progs))
+    return cells
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref-bin", default=os.path.join(ROOT, "oracle", "_ref"))
+    ap.add_argument("--only", default=None)
+    args = ap.parse_args()
+    dump = os.path.join(args.ref_bin, "kdn_ref_dump")
+    render = os.path.join(args.ref_bin, "kodanuki")
+    os.makedirs(os.path.join(HERE, "scenes"), exist_ok=True)
+    tmp = tempfile.mkdtemp()
+    for name, (gen, kw, nrays, depth) in SCENES.items():
+        if args.only and name != args.only:
+            continue
+        sdf = os.path.join(tmp, name + ".sdf")
+        open(sdf, "w").write(gen(**kw))
+        js = os.path.join(tmp, name + ".json")
+        subprocess.run([dump, "scene", sdf, js], check=True)
+        scene = Scene.from_reference_json(json.load(open(js)))
+        scene.save(os.path.join(HERE, "scenes", name + ".npz"))
+        print(name, "programs", scene.program_count, "steps", len(scene.steps))
+        if nrays:
+            rng = np.random.default_rng(1234)
+            rays = np.concatenate([camera_rays(scene, nrays // 2, rng), scattered_rays(scene, nrays - nrays // 2, rng)])
+            rp = os.path.join(tmp, name + ".rays")
+            hp = os.path.join(tmp, name + ".hits")
+            rays.tofile(rp)
+            subprocess.run([dump, "trace", sdf, rp, hp], check=True)
+            raw = np.fromfile(hp, np.uint8).reshape(-1, 44)
+            kind = raw[:, 0:4].copy().view("<u4")[:, 0]
+            geo = raw[:, 4:32].copy().view("<f4")
+            ids = raw[:, 32:40].copy().view("<u4")
+            share = raw[:, 40:44].copy().view("<f4")[:, 0]
+            far = float(scene.render["far"])
+            target = np.array(scene.camera["target"])
+            np.savez_compressed(os.path.join(HERE, f"trace_{name}.npz"), rays=rays, kind=kind, distance=geo[:, 0], point=geo[:, 1:4],
+                                normal=geo[:, 4:7], leaf=ids[:, 0], other=ids[:, 1], share=share,
+                                reach_lower=target - far, reach_size=np.full(3, 2 * far))
+            print(" trace", len(rays), "hit", int((kind == 1).sum()))
+        if depth:
+            cp = os.path.join(tmp, name + ".cut")
+            subprocess.run([dump, "cut", sdf, str(depth), cp], check=True)
+            cells = read_cut(cp)
+            head = np.array([(c[0], *c[1], c[2], len(c[3])) for c in cells], np.uint32)
+            objects, results, counts, allsteps = [], [], [], []
+            for c in cells:
+                for obj, res, steps in c[3]:
+                    objects.append(obj)
+                    results.append(res)
+                    counts.append(len(steps))
+                    allsteps.append(steps)
+            steps = np.concatenate(allsteps) if allsteps else np.zeros(0, STEP_DTYPE)
+            extra = {"steps": steps} if len(steps) < 100_000 else {"digests": np.array([step_digest(s) for s in allsteps], np.uint64)}
+            np.savez_compressed(os.path.join(HERE, f"cut_{name}.npz"), depth=depth, head=head, objects=np.array(objects, np.uint32),
+                                results=np.array(results, np.uint32), counts=np.array(counts, np.uint32), **extra)
+            print(" cut cells", len(cells), "programs", len(objects))
+
+
+if __name__ == "__main__":
+    main()

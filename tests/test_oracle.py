@@ -1,0 +1,54 @@
+"""The oracle (oracle/port) against the reference's own outputs.
+
+The fixtures under tests/golden were written by the reference renderer
+(tests/golden/make_golden.py); the oracle must reproduce them to the bit
+before the GPU path is judged against it."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle.port as op
+from helpers import GOLDEN, compare_cells, golden_rays, scene
+
+
+@pytest.mark.parametrize("name", ["c1", "c2"])
+def test_cut_lists_match_reference(name):
+    sc = scene(name)
+    cut = np.load(os.path.join(GOLDEN, f"cut_{name}.npz"))
+    d = int(cut["depth"])
+    tree = op.Octree(sc, d, d, 1 << 30)
+    assert tree.cells() == len(cut["head"])
+    assert compare_cells(tree.cell, cut) == 0
+
+
+@pytest.mark.parametrize("name", ["c1", "c2"])
+def test_sphere_trace_matches_reference(name):
+    sc = scene(name)
+    rays, tr = golden_rays(name)
+    r = np.zeros(len(rays), op.RAY_DTYPE)
+    r["origin"], r["direction"], r["far"], r["inside"], r["within"] = rays["origin"], rays["direction"], rays["far"], rays["inside"], rays["within"]
+    h = op.sphere_trace(sc, r, tr["reach_lower"], tr["reach_size"])
+    assert (h["kind"] == tr["kind"]).all()
+    hit = tr["kind"] == 1
+    assert (h["leaf"][hit] == tr["leaf"][hit]).all()
+    assert (h["other"][hit] == tr["other"][hit]).all()
+    assert (h["distance"] == tr["distance"]).all()
+    assert (h["normal"] == tr["normal"]).all()
+    assert (h["share"] == tr["share"]).all()
+
+
+def test_octree_trace_agrees_with_whole_scene_trace():
+    """Reading the field from a cell's kept programs gives the hits of the
+    march over every object (the kept programs are exact in their cell)."""
+    sc = scene("c1")
+    rays, tr = golden_rays("c1")
+    r = np.zeros(len(rays), op.RAY_DTYPE)
+    r["origin"], r["direction"], r["far"], r["inside"], r["within"] = rays["origin"], rays["direction"], rays["far"], rays["inside"], rays["within"]
+    tree = op.Octree(sc, 5, 9, 96)
+    h = tree.trace(r)
+    both = (h["kind"] == 1) & (tr["kind"] == 1)
+    assert (h["kind"] == tr["kind"]).mean() > 0.995
+    assert (h["leaf"][both] == tr["leaf"][both]).mean() > 0.995
+    rel = np.abs(h["distance"][both] - tr["distance"][both]) / np.maximum(tr["distance"][both], 1e-6)
+    assert np.quantile(rel, 0.99) < 1e-5
