@@ -1,0 +1,114 @@
+// Device-side description of one frame: lens, lamps, sky, materials and the
+// wavefront buffers of the path tracer.
+#pragma once
+
+#include "kdn.h"
+#include "kernels.h"
+#include "spectral.h"
+#include "world.h"
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace kdn {
+
+constexpr uint32_t kMaxLamps = 16;
+constexpr uint32_t kNoMaterial = 0xFFFFFFFFu;
+
+// A lamp with what aiming at it and meeting it read, worked out once
+// (plugins/transport/paths/light/light.cpp:78 lampOf).
+struct DeviceLamp {
+	uint32_t kind;   // sdf/scene.h LightKind
+	uint32_t square; // a quad whose edges are at right angles (light.cpp:145 squareQuad)
+	float at[3], along[3], across[3], facing[3], cross[3];
+	float ex[3], ey[3], raw[3];
+	float alongLength, acrossLength;
+	float radius, area;
+	float radiance[3], power[3];
+};
+
+// What the transport reads of a material (sdf/scene.h Material and the
+// finish the reference derives from it, material.cpp:204 finishWith).
+struct DeviceMaterial {
+	uint32_t kind;
+	float albedo[3];
+	float roughness;
+	float index;      // refraction (glass), 1 otherwise
+	float dispersion; // Cauchy B, square micrometres
+	float absorb[3];
+	float width;      // GGX width of the facets
+	float facetShare; // share of facet sampling for metal
+	float body;       // mean luminance of the albedo
+	float escapeAverage;
+	float coatFront, coatTwice, coatRoom;
+	uint32_t exact;   // a smooth glass answered exactly
+	uint32_t sharp;
+	uint32_t escapeFirst; // first entry of this finish's escape table
+	uint32_t pad;
+};
+
+struct FrameConstants {
+	float eye[3], forward[3], right[3], up[3];
+	float reach, aspect;
+	int32_t width, height;
+	uint64_t seedMix;
+	int32_t surfaces;
+	uint32_t spp;
+	uint32_t firstSample;
+	uint32_t lampCount;
+	uint32_t materialCount;
+	uint32_t pad;
+	float zenith[3], horizon[3], ground[3];
+	DeviceLamp lamps[kMaxLamps];
+	SpectralTables spectral;
+};
+
+// The wavefront state of one chunk of paths, structure of arrays.
+struct PathBuffers {
+	uint32_t* pixel;      // pixel index within the frame
+	uint32_t* sample;     // sample index of the pixel
+	float4* throughput;   // four lanes
+	float4* radiance;
+	float4* nanometres;
+	float4* density;
+	float* drawn;         // density of the last scattered direction, 0 when exact
+	uint32_t* state;      // depth (bits 0-7), camera leg (bit 8), dispersed (bit 9), medium + 1 (bits 16-31)
+	float4* from;         // xyz: where the leg was drawn from
+};
+
+struct QueueBuffers {
+	uint32_t* paths;      // path index of each queued ray
+	kdn_ray* rays;
+	uint32_t* count;      // device count
+};
+
+struct ShadowBuffers {
+	kdn_ray* rays;
+	uint32_t* paths;
+	float4* contribution;
+	uint32_t* count;
+	HitState* states;
+};
+
+struct ShadeArgs {
+	PathBuffers paths;
+	QueueBuffers in;
+	QueueBuffers out;
+	ShadowBuffers shadow;
+	const kdn_hit* hits;
+	const DeviceMaterial* materials;
+	const uint32_t* leafMaterial;
+	uint32_t leafCount;
+	uint32_t capacity;
+	uint32_t* error;
+};
+
+cudaError_t uploadFrameConstants(const FrameConstants& c, cudaStream_t stream);
+cudaError_t launchCamera(const PathBuffers& paths, const QueueBuffers& queue, uint32_t firstPixel, uint32_t n, cudaStream_t stream, int smCount);
+cudaError_t launchShade(const ShadeArgs& args, cudaStream_t stream, int smCount);
+cudaError_t launchLines(const PathBuffers& paths, const ShadowBuffers& shadow, uint32_t capacity, cudaStream_t stream, int smCount);
+cudaError_t launchFold(const PathBuffers& paths, uint32_t firstPixel, uint32_t pixels, uint32_t spp, double* sums, cudaStream_t stream, int smCount);
+cudaError_t launchMeans(const double* sums, uint32_t pixels, double taken, float* out, cudaStream_t stream, int smCount);
+
+} // namespace kdn

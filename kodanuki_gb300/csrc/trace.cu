@@ -26,7 +26,7 @@ __device__ __forceinline__ float slopeOf(float part) {
 
 __device__ __forceinline__ float tolerance(const float p[3]) {
 	const float big = fmaxf(fabsf(p[0]), fmaxf(fabsf(p[1]), fabsf(p[2])));
-	return 1e-5f * fmaxf(1.0f, big * 0.0625f);
+	return 2e-6f * fmaxf(1.0f, big * 0.25f);
 }
 
 __device__ __forceinline__ float nudge(float t) { return fmaxf(1e-5f, fabsf(t) * 2e-6f); }

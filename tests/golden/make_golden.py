@@ -32,6 +32,12 @@ from kodanuki_gb300.scene import STEP_DTYPE, Scene  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
+REFERENCE_FLAGS = ["--threads", "8", "--use", "stopping=fixed_count", "--use", "execution=single", "--use", "detail=none",
+                   "--use", "build=none", "--use", "strategy=none", "--use", "sampler=none", "--use", "observer=none"]
+
+# name -> (seeds, spp per seed) of the reference frames kept as image fixtures
+IMAGES = {"room_small": (12, 64), "c1_small": (12, 64)}
+
 # name -> (generator, kwargs, trace rays, cut depth)
 SCENES = {
     "c1": (scenegen.scene_config1, dict(seed=1), 2000, 4),
@@ -113,6 +119,29 @@ def read_cut(path: str):
     return cells
 
 
+def read_pfm(path: str) -> np.ndarray:
+    data = open(path, "rb").read()
+    head, dims, scale, rest = data.split(b"\n", 3)
+    w, h = map(int, dims.split())
+    a = np.frombuffer(rest[: w * h * 12], "<f4" if float(scale) < 0 else ">f4").reshape(h, w, 3)
+    return a[::-1].copy()
+
+
+def reference_images(render: str, sdf: str, name: str, tmp: str) -> None:
+    """Frames of the reference renderer at fixed spp under independent seeds:
+    their per-pixel mean and the standard error of one seed's frame."""
+    seeds, spp = IMAGES[name]
+    frames = []
+    for k in range(seeds):
+        pfm = os.path.join(tmp, f"{name}_{k}.pfm")
+        subprocess.run([render, sdf, "--out", os.path.join(tmp, f"{name}_{k}.ppm"), "--pfm", pfm, "--seed", str(1000 + k),
+                        "--samples", str(spp)] + REFERENCE_FLAGS, check=True, capture_output=True)
+        frames.append(read_pfm(pfm))
+    f = np.stack(frames)
+    np.savez_compressed(os.path.join(HERE, f"image_{name}.npz"), frames=f.astype(np.float32), spp=spp, seeds=np.arange(1000, 1000 + seeds))
+    print(" image", f.shape, "mean", f.mean(axis=(0, 1, 2)))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref-bin", default=os.path.join(ROOT, "oracle", "_ref"))
@@ -132,6 +161,8 @@ def main() -> None:
         scene = Scene.from_reference_json(json.load(open(js)))
         scene.save(os.path.join(HERE, "scenes", name + ".npz"))
         print(name, "programs", scene.program_count, "steps", len(scene.steps))
+        if name in IMAGES:
+            reference_images(render, sdf, name, tmp)
         if nrays:
             rng = np.random.default_rng(1234)
             rays = np.concatenate([camera_rays(scene, nrays // 2, rng), scattered_rays(scene, nrays - nrays // 2, rng)])
