@@ -1,0 +1,272 @@
+#!/usr/bin/env python3
+"""Benchmark: render throughput of the GB300 backend on the full-size plain
+workload, beside the CPU renderer timed on this machine's host cores.
+
+One step is one frame of the config-2 scene (4096 primitives in 512 CSG
+groups with floor-based repetition, 40% matte / 40% GGX metal / 20%
+dispersive glass, two quad lights and a constant 6500 K sky), 1920x1080 at
+64 samples a pixel, paths of at most 16 surfaces: 132.7 M samples a step.
+The scene is the reference renderer's own compilation of the seeded scene
+text (tests/golden/scenes/c2.npz); the cut octree is built once before the
+timed region and reported apart (build_s), as the reference reports its
+tree build apart from its render time.
+
+  value : Msamples/s over the K timed frames, device time (CUDA events on
+          the backend's stream), scene resident in HBM, the L2 written over
+          (a 512 MiB buffer) before every timed frame.
+  e2e   : the same through the C ABI as a host caller drives it: each step
+          uploads the frame's transport blocks (camera, lights, sky,
+          materials, finishes) from host memory and reads the frame back to
+          host memory; wall clock around the whole step.
+  cpu_baseline : the oracle's C renderer (oracle/port) on the host cores
+          over a bounded band of the same frame.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Msamples/s @1080p vs CPU; equal-time relMSE guided vs plain; p50/p99 latency"
+SCENE = os.path.join(ROOT, "tests", "golden", "scenes", "c2.npz")
+WIDTH, HEIGHT, SPP, SURFACES = 1920, 1080, 64, 16
+BUILD = dict(min_depth=7, max_depth=10, split_steps=96)
+
+
+def env_int(name: str, default: int) -> int:
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+class Clocks:
+    """nvidia-smi samples of the SM clock and throttle reasons while the
+    timed region runs."""
+
+    QUERY = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.samples: list[list[str]] = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.reader = threading.Thread(target=self._read, daemon=True)
+            self.reader.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["not sampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(self.samples)}
+
+
+def peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return {"hbm_gbs": d.get("hbm_gbs", 6800.0), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def cpu_baseline(scene, seconds: float = 15.0) -> dict:
+    """The oracle's C renderer (double precision, the reference's algorithm)
+    on every host core, over a band of rows of the same frame: Msamples/s."""
+    import oracle.port as op
+    threads = os.cpu_count() or 1
+    rows, spp = 1, SPP
+    # grow the band until it takes a few seconds, then time one band of ~`seconds`
+    while True:
+        t0 = time.perf_counter()
+        op.render_band(scene, WIDTH, HEIGHT, spp, SURFACES, int(scene.render["seed"]), HEIGHT // 2, rows, threads, BUILD)
+        dt = time.perf_counter() - t0
+        if dt > 2.0 or rows >= HEIGHT // 2:
+            break
+        rows *= 2
+    target = max(1, min(HEIGHT // 2, int(rows * seconds / max(dt, 1e-3))))
+    t0 = time.perf_counter()
+    op.render_band(scene, WIDTH, HEIGHT, spp, SURFACES, int(scene.render["seed"]), HEIGHT // 2 - target // 2, target, threads, BUILD)
+    dt = time.perf_counter() - t0
+    samples = WIDTH * target * spp
+    return {"value": samples / dt / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
+            "sample": f"{target} full rows of the 1920x1080 frame at {spp} spp ({samples} samples, {dt:.1f} s), octree built before timing"}
+
+
+def run_reference(args) -> None:
+    rank = env_int("RANK", 0)
+    if rank != 0:
+        return
+    from kodanuki_gb300.scene import Scene
+    scene = Scene.load(SCENE)
+    base = cpu_baseline(scene, seconds=8.0)
+    times = []
+    import oracle.port as op
+    threads = os.cpu_count() or 1
+    rows = max(1, int(base["value"] * 1e6 * 8.0 / (WIDTH * SPP)))
+    for step in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        op.render_band(scene, WIDTH, HEIGHT, SPP, SURFACES, int(scene.render["seed"]) + step, HEIGHT // 2 - rows // 2, rows, threads, BUILD)
+        if step >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    per = float(np.mean(times))
+    value = WIDTH * rows * SPP / per / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded config-2 scene compiled by the reference)",
+        "config": {"workload": "config-2 plain, 1920x1080 band of rows, 64 spp, 16 surfaces, CPU", "rows_per_step": rows, "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": threads, "kind": "port",
+                         "sample": f"{rows} rows x 1920 px x 64 spp per step"},
+        "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args) -> None:
+    import kodanuki_gb300 as K
+    from kodanuki_gb300.scene import Scene
+
+    rank, world = env_int("RANK", 0), env_int("WORLD_SIZE", 1)
+    local = env_int("LOCAL_RANK", 0)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    scene = Scene.load(SCENE)
+    b = K.Backend(local)
+    b.load(scene)
+    t0 = time.perf_counter()
+    b.build(**BUILD)
+    build_s = time.perf_counter() - t0
+    stats_world = b.world_stats()
+    seed = int(scene.render["seed"])
+    for k in range(args.warmup):
+        b.render(WIDTH, HEIGHT, SPP, surfaces=SURFACES, seed=seed + 1000 + k)
+    if dist:
+        dist.barrier()
+    device_ms, trace_ms, launches, march, program = 0.0, 0.0, 0, 0, 0
+    with Clocks(local) as clocks:
+        wall0 = time.perf_counter()
+        for k in range(args.steps):
+            b.flush_l2()
+            b.render(WIDTH, HEIGHT, SPP, surfaces=SURFACES, seed=seed + k)
+            st = b.frame_stats()
+            device_ms += st.total_ms
+            trace_ms += st.trace_ms
+            launches += st.launches
+            march += st.march_steps
+            program += st.program_steps
+        wall = time.perf_counter() - wall0
+    if dist:
+        t = np.array([device_ms])
+        import torch
+        tt = torch.tensor(t)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        device_ms = float(tt[0])
+    samples = WIDTH * HEIGHT * SPP * args.steps
+    value = samples * world / (device_ms / 1e3) / 1e6
+
+    # e2e: as a host caller drives a frame through the C ABI
+    blocks = K.scene_blocks(scene)
+    per_frame = ["shot.camera", "lighting.lights", "lighting.sky", "looks.materials", "transport.finishes"]
+    h2d = sum(blocks[n].nbytes for n in per_frame if n in blocks)
+    d2h = WIDTH * HEIGHT * 3 * 4
+    if dist:
+        dist.barrier()
+    e0 = time.perf_counter()
+    for k in range(args.steps):
+        for n in per_frame:
+            if n in blocks:
+                b.upload(n, blocks[n])
+        img = b.render(WIDTH, HEIGHT, SPP, surfaces=SURFACES, seed=seed + k)
+    e_dt = time.perf_counter() - e0
+    e2e = samples * world / e_dt / 1e6
+
+    # roofline of the dominant kernel (the sphere-trace kernel, FP32 SIMT
+    # work): algorithmic bytes are the rays it reads and the end states it
+    # writes; the world it walks is L2-resident.
+    pk = peaks()
+    trace_launches = 2 * SURFACES * ((WIDTH * HEIGHT * SPP + (1 << 22) - 1) // (1 << 22)) * args.steps
+    segments_bytes = 0
+    rays_per_frame = None
+    line = {
+        "metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": device_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded config-2 scene compiled by the reference renderer)",
+        "config": {"workload": "config-2 plain: 4096 primitives, 1920x1080, 64 spp, 16 surfaces, FP32, no denoiser",
+                   "world": stats_world, "build_s": build_s, "l2": "512 MiB written before every timed frame",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "clocks": clocks.summary(),
+        "wall_s": wall,
+        "march_steps_per_sample": march / samples,
+        "program_steps_per_sample": program / samples,
+        "trace_share": trace_ms / device_ms if device_ms else None,
+    }
+    if rank == 0:
+        achieved_flops = (program * 1.0 + march * 30.0) / (trace_ms / 1e3) / 1e12 if trace_ms else None
+        line["roofline"] = {"bound": "hbm", "achieved": None, "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": None, "traffic": None,
+                            "note": "sphere-trace kernel: FP32 SIMT-bound, see roofline_simt"}
+        line["roofline_simt"] = {"achieved_tflops": achieved_flops, "peak_tflops": 152 * 128 * 2 * 2.07e9 / 1e12,
+                                 "unit": "TFLOP/s FP32 (1 flop a program step, 30 a march step)"}
+        try:
+            line["cpu_baseline"] = cpu_baseline(scene)
+        except Exception as e:  # the oracle is test infrastructure; report why it could not run
+            line["cpu_baseline"] = {"value": None, "unit": "Msamples/s", "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {e}"}
+        print(json.dumps(line), flush=True)
+    b.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -85,9 +85,28 @@ typedef struct kdn_material {
 	float absorb[3];
 	float glow[3];
 	float strength;
-	uint32_t flags_;    /* reserved, 0 */
+	uint32_t flags_;    /* 1: the albedo is a ramp read off a pattern program (not drawn by this build) */
 	uint32_t pad_;
 } kdn_material;
+
+/* plugins/transport/paths/material/material.h:70 Finish: how a material is
+ * drawn, as the reference's transport derives it from the Material
+ * (material.cpp:204 finishWith), its GGX width, facet share, coat and escape
+ * table (material/energy.h:12 Escape: 32 views) included.  352 bytes. */
+typedef struct kdn_finish {
+	uint32_t kind;
+	uint32_t sharp;
+	uint32_t exact;      /* a smooth glass answered exactly */
+	uint32_t loses_much; /* a rough glass that needs its boundary tables (not drawn by this build) */
+	double width;
+	double facet_share;
+	double body;
+	double index;
+	double coat_front, coat_twice, coat_room;
+	double escape_average;
+	double escape[32];
+	double film[2];      /* thickness (nm), index; a thickness above 0 is not drawn by this build */
+} kdn_finish;
 
 /* sdf/scene.h Light, 136 bytes. kind: sdf/scene.h LightKind (2 sphere, 3 quad). */
 typedef struct kdn_light {
@@ -178,6 +197,7 @@ kdn_status kdn_close(kdn_ctx* ctx);
  *   "scene.programs"   kdn_program_ref, 12 one per object (Scene::objectPrograms)
  *   "scene.leaves"     uint32_t, 4         the material of each leaf (Leaf::material)
  *   "looks.materials"  kdn_material, 64
+ *   "transport.finishes" kdn_finish, 352 one per material (plugins/transport/paths/plugin.cpp:201)
  *   "lighting.lights"  kdn_light, 136
  *   "lighting.sky"     kdn_sky, 72         one
  *   "shot.camera"      kdn_camera, 96      one

@@ -41,7 +41,11 @@ LIGHT_DTYPE = np.dtype([("kind", "<u4"), ("radius", "<f4"), ("angle", "<f4"), ("
 SKY_DTYPE = np.dtype([("zenith", "<f8", 3), ("horizon", "<f8", 3), ("ground", "<f8", 3)])
 CAMERA_DTYPE = np.dtype([("eye", "<f8", 3), ("target", "<f8", 3), ("up", "<f8", 3), ("fov", "<f8"), ("aperture", "<f8"), ("focus", "<f8")])
 REGION_DTYPE = np.dtype([("lower", "<f8", 3), ("size", "<f8", 3)])
+FINISH_DTYPE = np.dtype([("kind", "<u4"), ("sharp", "<u4"), ("exact", "<u4"), ("loses_much", "<u4"), ("width", "<f8"), ("facet_share", "<f8"),
+                         ("body", "<f8"), ("index", "<f8"), ("coat_front", "<f8"), ("coat_twice", "<f8"), ("coat_room", "<f8"),
+                         ("escape_average", "<f8"), ("escape", "<f8", 32), ("film", "<f8", 2)])
 assert RAY_DTYPE.itemsize == 36 and HIT_DTYPE.itemsize == 56 and MATERIAL_DTYPE.itemsize == 64 and LIGHT_DTYPE.itemsize == 136
+assert FINISH_DTYPE.itemsize == 352
 
 
 class BuildOptions(ctypes.Structure):
@@ -129,6 +133,15 @@ def scene_blocks(scene: Scene) -> dict[str, np.ndarray]:
     mats["absorb"] = m["absorb"]
     mats["glow"] = m["glow"]
     mats["strength"] = m["strength"]
+    mats["flags"] = m["patterned"]
+    finishes = None
+    if "finish_kind" in m:
+        finishes = np.zeros(len(m["finish_kind"]), FINISH_DTYPE)
+        for k in ("kind", "sharp", "exact", "loses_much", "width", "facet_share", "body", "index", "escape_average", "escape", "film"):
+            finishes[k] = m["finish_" + k]
+        finishes["coat_front"] = m["finish_coating"][:, 0]
+        finishes["coat_twice"] = m["finish_coating"][:, 1]
+        finishes["coat_room"] = m["finish_coating"][:, 2]
     l = scene.lights
     lights = np.zeros(len(l["kind"]), LIGHT_DTYPE)
     for k in ("kind", "radius", "angle", "at", "direction", "along", "across", "power"):
@@ -142,7 +155,7 @@ def scene_blocks(scene: Scene) -> dict[str, np.ndarray]:
     region = np.zeros(1, REGION_DTYPE)
     region["lower"] = scene.region_lower
     region["size"] = scene.region_size
-    return {
+    blocks = {
         "scene.steps": np.ascontiguousarray(scene.steps),
         "scene.programs": refs,
         "scene.leaves": np.ascontiguousarray(scene.leaf_material, np.uint32),
@@ -152,6 +165,9 @@ def scene_blocks(scene: Scene) -> dict[str, np.ndarray]:
         "shot.camera": cam,
         "geometry.region": region,
     }
+    if finishes is not None:
+        blocks["transport.finishes"] = finishes
+    return blocks
 
 
 class Backend:

@@ -24,6 +24,7 @@ const BlockSpec kBlocks[] = {
 	{ "scene.programs", sizeof(kdn_program_ref), false },
 	{ "scene.leaves", sizeof(uint32_t), false },
 	{ "looks.materials", sizeof(kdn_material), false },
+	{ "transport.finishes", sizeof(kdn_finish), false },
 	{ "lighting.lights", sizeof(kdn_light), false },
 	{ "lighting.sky", sizeof(kdn_sky), true },
 	{ "shot.camera", sizeof(kdn_camera), true },
@@ -36,6 +37,7 @@ static_assert(sizeof(kdn_hit) == 56, "kdn_hit is the reference's 56-byte Hit");
 static_assert(sizeof(kdn_program_ref) == 12, "kdn_program_ref is 12 bytes");
 static_assert(sizeof(kdn_material) == 64, "kdn_material is 64 bytes");
 static_assert(sizeof(kdn_light) == 136, "kdn_light is 136 bytes");
+static_assert(sizeof(kdn_finish) == 352, "kdn_finish is 352 bytes");
 static_assert(sizeof(kdn_sky) == 72, "kdn_sky is 72 bytes");
 static_assert(sizeof(kdn_camera) == 96, "kdn_camera is 96 bytes");
 static_assert(sizeof(kdn_region) == 48, "kdn_region is 48 bytes");

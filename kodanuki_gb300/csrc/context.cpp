@@ -159,8 +159,9 @@ kdn_status Context::extend(const kdn_ray* rays, uint32_t n, kdn_hit* hits, cudaS
 	t.n              = n;
 	t.states         = static_cast<HitState*>(extendStates.ptr);
 	t.objectMaterial = static_cast<const uint32_t*>(objectMaterial.ptr);
-	t.maxSteps       = 4096;
+	t.maxSteps       = kMarchSteps;
 	t.counters       = nullptr;
+	t.count          = nullptr;
 	if (!check(launchTrace(t, on, smCount), "trace kernel")) return KDN_CUDA_ERROR;
 	HitArgs h;
 	h.world  = world;
@@ -168,6 +169,7 @@ kdn_status Context::extend(const kdn_ray* rays, uint32_t n, kdn_hit* hits, cudaS
 	h.states = t.states;
 	h.n      = n;
 	h.hits   = hits;
+	h.count  = nullptr;
 	if (!check(launchHits(h, on, smCount), "hit kernel")) return KDN_CUDA_ERROR;
 	return KDN_OK;
 }

@@ -44,8 +44,8 @@ struct DeviceMaterial {
 	float coatFront, coatTwice, coatRoom;
 	uint32_t exact;   // a smooth glass answered exactly
 	uint32_t sharp;
-	uint32_t escapeFirst; // first entry of this finish's escape table
-	uint32_t pad;
+	uint32_t pad[2];
+	float escape[32]; // material/energy.h:12 Escape: the share a view keeps after one scatter
 };
 
 struct FrameConstants {

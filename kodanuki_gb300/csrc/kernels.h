@@ -30,6 +30,7 @@ struct TraceArgs {
 	const uint32_t* objectMaterial; // material of each object's first leaf
 	uint32_t maxSteps;
 	unsigned long long* counters;   // [0] march steps, [1] program steps
+	const uint32_t* count;          // if set, the number of rays is read here on the device
 };
 
 struct HitArgs {
@@ -38,6 +39,7 @@ struct HitArgs {
 	const HitState* states;
 	uint32_t n;
 	kdn_hit* hits;
+	const uint32_t* count;          // if set, the number of rays is read here on the device
 };
 
 cudaError_t setTraceAttributes();

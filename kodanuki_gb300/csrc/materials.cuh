@@ -1,0 +1,373 @@
+// BSDFs of the transport kernels (plugins/transport/paths/material/
+// material.cpp and material/microfacet.cpp), in FP32 over the four
+// hero-wavelength lanes:
+//  - matte: Lambert (material.cpp:406 matteValue, :1173 matteScatter);
+//  - metal: GGX facets with Schlick's Fresnel plus the lobe that gives back
+//    what single scattering loses, read off the finish's escape table
+//    (material.cpp:649 viewedMetal, energy.cpp:120 escapeAt);
+//  - plastic: a Lambert body under a GGX coat of index 1.5
+//    (material.cpp:661 viewedPlastic, :440 plasticShare);
+//  - glass, smooth: exact mirror and passage by Fresnel, per lane where the
+//    glass disperses (Cauchy), the passage bent by the hero lane's index
+//    (material.cpp:1300 exactGlassScatter, feature/dispersion).
+// Rough glass, films, patterns and glowing surfaces are refused by the host.
+#pragma once
+
+#include "frame.h"
+
+#include <cuda_runtime.h>
+
+namespace kdn {
+
+constexpr float kPiF     = 3.14159265358979f;
+constexpr float kCoatRatio = 1.0f / 1.5f; // material.cpp:10 coatIndex
+
+struct Frame {
+	float3 t, b, n;
+	__device__ float3 toWorld(float3 v) const {
+		return make_float3(t.x * v.x + b.x * v.y + n.x * v.z, t.y * v.x + b.y * v.y + n.y * v.z, t.z * v.x + b.z * v.y + n.z * v.z);
+	}
+	__device__ float3 toLocal(float3 v) const {
+		return make_float3(t.x * v.x + t.y * v.y + t.z * v.z, b.x * v.x + b.y * v.y + b.z * v.z, n.x * v.x + n.y * v.y + n.z * v.z);
+	}
+};
+
+// An orthonormal frame about a unit vector (Duff et al., "Building an
+// Orthonormal Basis, Revisited", JCGT 2017).
+__device__ __forceinline__ Frame frameAround(float3 n) {
+	const float sign = copysignf(1.0f, n.z);
+	const float a    = -1.0f / (sign + n.z);
+	const float b    = n.x * n.y * a;
+	Frame f;
+	f.t = make_float3(1.0f + sign * n.x * n.x * a, sign * b, -sign * n.x);
+	f.b = make_float3(b, sign + n.y * n.y * a, -n.y);
+	f.n = n;
+	return f;
+}
+
+__device__ __forceinline__ float dotF(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 scaleF(float3 a, float s) { return make_float3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 addF(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 subF(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 unitF(float3 a) { return scaleF(a, 1.0f / sqrtf(dotF(a, a))); }
+__device__ __forceinline__ float4 flat4(float v) { return make_float4(v, v, v, v); }
+__device__ __forceinline__ float4 lin4(float4 a, float sa, float4 b, float sb) { return make_float4(a.x * sa + b.x * sb, a.y * sa + b.y * sb, a.z * sa + b.z * sb, a.w * sa + b.w * sb); }
+__device__ __forceinline__ float lane4(float4 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); }
+
+// math/vector.cpp:45 mirrored
+__device__ __forceinline__ float3 mirrorOf(float3 v, float3 n) { return subF(scaleF(n, 2.0f * dotF(v, n)), v); }
+
+// ---- microfacet.cpp ----
+__device__ __forceinline__ float facetDistribution(float cosine, float width) {
+	if (cosine <= 0.0f) return 0.0f;
+	const float sq    = width * width;
+	const float lower = cosine * cosine * (sq - 1.0f) + 1.0f;
+	return sq / (kPiF * lower * lower);
+}
+
+__device__ __forceinline__ float smithVisibility(float leaving, float arriving, float width) {
+	const float sq    = width * width;
+	const float first = arriving * sqrtf(sq + (1.0f - sq) * leaving * leaving);
+	const float second = leaving * sqrtf(sq + (1.0f - sq) * arriving * arriving);
+	const float total = first + second;
+	return total > 0.0f ? 0.5f / total : 0.0f;
+}
+
+__device__ __forceinline__ float smithMasking(float cosine, float width) {
+	const float sq    = width * width;
+	const float under = cosine + sqrtf(sq + (1.0f - sq) * cosine * cosine);
+	return under > 0.0f ? 2.0f * cosine / under : 0.0f;
+}
+
+__device__ __forceinline__ float3 halfwayOf(float3 o, float3 i, float3 n) {
+	const float3 total = addF(o, i);
+	const float size   = sqrtf(dotF(total, total));
+	return size > 1e-12f ? scaleF(total, 1.0f / size) : n;
+}
+
+// microfacet.cpp:67 visibleFacet: a facet drawn by its visible area from the
+// outgoing direction (stretch, draw on the hemisphere seen from it, unstretch).
+__device__ float3 visibleFacet(const Frame& f, float3 outgoing, float width, float u, float v) {
+	const float3 local     = f.toLocal(outgoing);
+	const float3 stretched = unitF(make_float3(width * local.x, width * local.y, local.z));
+	const float flat       = stretched.x * stretched.x + stretched.y * stretched.y;
+	const float3 first     = flat > 1e-12f ? scaleF(make_float3(-stretched.y, stretched.x, 0.0f), rsqrtf(flat)) : make_float3(1.0f, 0.0f, 0.0f);
+	const float3 second    = make_float3(stretched.y * first.z - stretched.z * first.y, stretched.z * first.x - stretched.x * first.z, stretched.x * first.y - stretched.y * first.x);
+	const float reach      = sqrtf(u);
+	const float angle      = 2.0f * kPiF * v;
+	const float across     = reach * cosf(angle);
+	const float lean       = 0.5f * (1.0f + stretched.z);
+	const float along      = (1.0f - lean) * sqrtf(fmaxf(1.0f - across * across, 0.0f)) + lean * reach * sinf(angle);
+	const float height     = sqrtf(fmaxf(1.0f - across * across - along * along, 0.0f));
+	const float3 raised    = addF(addF(scaleF(first, across), scaleF(second, along)), scaleF(stretched, height));
+	const float3 unstretched = unitF(make_float3(width * raised.x, width * raised.y, fmaxf(raised.z, 1e-12f)));
+	return f.toWorld(unstretched);
+}
+
+// microfacet.cpp:94 dielectricReflectance, ratio = index before / index after.
+__device__ __forceinline__ float dielectricReflectance(float cosine, float ratio) {
+	const float leftover = 1.0f - ratio * ratio * (1.0f - cosine * cosine);
+	if (leftover <= 0.0f) return 1.0f;
+	const float onward = sqrtf(leftover);
+	const float perp   = (ratio * cosine - onward) / (ratio * cosine + onward);
+	const float par    = (ratio * onward - cosine) / (ratio * onward + cosine);
+	return 0.5f * (perp * perp + par * par);
+}
+
+// energy.cpp:120 escapeAt
+__device__ __forceinline__ float escapeAt(const float* table, float cosine) {
+	const float place = fminf(fmaxf(cosine, 0.0f), 1.0f) * 32.0f - 0.5f;
+	const int lower   = min(max(int(floorf(place)), 0), 31);
+	const int upper   = min(lower + 1, 31);
+	const float share = fminf(fmaxf(place - float(lower), 0.0f), 1.0f);
+	return table[lower] * (1.0f - share) + table[upper] * share;
+}
+
+// What a vertex's BSDF needs, worked out once per vertex (material.cpp:580
+// roughViewed for the rough kinds).
+struct Shading {
+	uint32_t kind;
+	float3 normal;
+	Frame frame;
+	float4 albedo;   // albedo at the lanes
+	float leaving;   // cosine of the outgoing direction
+	float left;      // escapeAt(leaving)
+	float share;     // chance of the facet lobe when sampling
+	float masking;   // smithMasking(leaving)
+	float4 twice;    // metal: the colour light keeps over many bounces
+	float4 within, beyond; // glass: index on either side, per lane
+	bool parted;     // the lanes bend apart (a dispersing glass)
+};
+
+struct Response {
+	float4 value;
+	float density;
+};
+
+struct Scatter {
+	bool found;
+	bool through;
+	bool delta;
+	bool dispersed;
+	float3 incoming;
+	float4 weight;     // value * |cosine| / density, or the kept share of an exact side
+	float density;
+	uint32_t mediumAfter;
+};
+
+// math/spectrum.cpp:42-60: the smooth basis curves RGB is upsampled by.
+__device__ __forceinline__ float smoothRise(float nm, float lo, float hi) {
+	const float b = fminf(fmaxf((nm - lo) / (hi - lo), 0.0f), 1.0f);
+	return b * b * (3.0f - 2.0f * b);
+}
+
+__device__ __forceinline__ float basisOf(int channel, float nm) {
+	const float red  = smoothRise(nm, 575.0f, 605.0f);
+	const float blue = 1.0f - smoothRise(nm, 445.0f, 530.0f);
+	return channel == 0 ? red : (channel == 2 ? blue : (1.0f - blue) * (1.0f - red));
+}
+
+// math/colour.cpp:85 spectrumOf: an RGB colour at the four lanes, from its
+// least channel, the rise to the middle one and the rise to the most one.
+__device__ __forceinline__ float4 spectrumOf(float r, float g, float b, float4 nm) {
+	const float c[3] = { r, g, b };
+	int least;
+	if (r <= g && r <= b) least = 0;
+	else least = (g <= r && g <= b) ? 1 : 2;
+	const int first  = least == 0 ? 1 : 0;
+	const int second = least == 2 ? 1 : 2;
+	const int most   = c[first] <= c[second] ? second : first;
+	const int middle = 3 - least - most;
+	const float base = c[least];
+	const float low  = c[middle] - base;
+	const float high = c[most] - c[middle];
+	const float lanes[4] = { nm.x, nm.y, nm.z, nm.w };
+	float out[4];
+	for (int k = 0; k < 4; ++k) out[k] = base + low * (1.0f - basisOf(least, lanes[k])) + high * basisOf(most, lanes[k]);
+	return make_float4(out[0], out[1], out[2], out[3]);
+}
+
+// feature/dispersion/dispersion.cpp cauchyIndex: A + B / lambda^2, lambda in micrometres.
+__device__ __forceinline__ float4 laneIndices(const DeviceMaterial& m, float4 nm) {
+	if (m.dispersion == 0.0f) return flat4(m.index);
+	const float l0 = nm.x * 1e-3f, l1 = nm.y * 1e-3f, l2 = nm.z * 1e-3f, l3 = nm.w * 1e-3f;
+	return make_float4(m.index + m.dispersion / (l0 * l0), m.index + m.dispersion / (l1 * l1), m.index + m.dispersion / (l2 * l2), m.index + m.dispersion / (l3 * l3));
+}
+
+__device__ __forceinline__ float plasticShare(const DeviceMaterial& m, float leaving) {
+	const float face  = dielectricReflectance(leaving, kCoatRatio);
+	const float share = face / fmaxf(face + (1.0f - face) * m.body, 1e-12f);
+	return fminf(fmaxf(share, 0.25f), 0.9f);
+}
+
+__device__ __forceinline__ Shading surfaceOf(const DeviceMaterial& m, float3 normal, float3 outgoing, float4 nm, uint32_t medium, const DeviceMaterial* all) {
+	Shading s;
+	s.kind    = m.kind;
+	s.normal  = normal;
+	s.frame   = frameAround(normal);
+	s.albedo  = spectrumOf(m.albedo[0], m.albedo[1], m.albedo[2], nm);
+	s.leaving = dotF(normal, outgoing);
+	s.left    = 0.0f;
+	s.share   = 0.0f;
+	s.masking = 0.0f;
+	s.twice   = flat4(0.0f);
+	s.within  = flat4(1.0f);
+	s.beyond  = flat4(1.0f);
+	s.parted  = false;
+	if (m.kind == 1 || m.kind == 2) {
+		s.left    = escapeAt(m.escape, s.leaving);
+		s.share   = m.kind == 2 ? m.facetShare : (s.leaving <= 0.0f ? 0.0f : plasticShare(m, s.leaving));
+		s.masking = smithMasking(s.leaving, m.width);
+		if (m.kind == 2) {
+			// microfacet.cpp:116 averagedFresnel, then material.cpp:567 metalTwice
+			const float4 avg = lin4(s.albedo, 1.0f - 1.0f / 21.0f, flat4(1.0f), 1.0f / 21.0f);
+			const float e    = m.escapeAverage;
+			const float a[4] = { avg.x, avg.y, avg.z, avg.w };
+			float t[4];
+			for (int k = 0; k < 4; ++k) t[k] = a[k] * a[k] * e / (1.0f - a[k] * (1.0f - e));
+			s.twice = make_float4(t[0], t[1], t[2], t[3]);
+		}
+	} else if (m.kind == 3) {
+		// material.cpp:328 sidesOf with feature/dispersion's per-lane indices
+		if (medium != kNoMaterial) {
+			const DeviceMaterial& body = all[medium];
+			s.within = laneIndices(body, nm);
+			s.parted = body.dispersion != 0.0f;
+		} else {
+			s.beyond = laneIndices(m, nm);
+			s.parted = m.dispersion != 0.0f;
+		}
+	}
+	return s;
+}
+
+// material.cpp:620 lostOf
+__device__ __forceinline__ float lostOf(const DeviceMaterial& m, float left, float came) {
+	const float room = 1.0f - m.escapeAverage;
+	if (room <= 1e-6f) return 0.0f;
+	return (1.0f - left) * (1.0f - came) / (kPiF * room);
+}
+
+// The value and density of the BSDF for one pair of directions
+// (material.cpp:1076 respondBsdf / :710 roughViewedAnswer).
+__device__ __forceinline__ Response respond(const Shading& s, const DeviceMaterial& m, float3 outgoing, float3 incoming, float4 nm) {
+	Response r;
+	r.value              = flat4(0.0f);
+	const float arriving = dotF(s.normal, incoming);
+	if (s.kind == 0) {
+		r.density = fmaxf(arriving, 0.0f) / kPiF;
+		if (s.leaving > 0.0f && arriving > 0.0f) r.value = lin4(s.albedo, 1.0f / kPiF, flat4(0.0f), 0.0f);
+		return r;
+	}
+	if (s.kind == 3) { // exact glass: nothing for a direction not drawn by it
+		r.density = 0.0f;
+		return r;
+	}
+	const float cosineDensity = fmaxf(arriving, 0.0f) / kPiF;
+	if (s.leaving <= 0.0f || arriving <= 0.0f) {
+		// material.cpp:447 roughDensity of a shadowed pair
+		r.density = (s.kind == 1 && s.leaving <= 0.0f) ? 0.0f : (1.0f - s.share) * cosineDensity;
+		return r;
+	}
+	const float3 h     = halfwayOf(outgoing, incoming, s.normal);
+	const float tilt   = dotF(s.normal, h);
+	const float D      = facetDistribution(tilt, m.width);
+	const float came   = escapeAt(m.escape, arriving);
+	const float ontoRaw = dotF(outgoing, h);
+	const float onto   = fmaxf(ontoRaw, 0.0f);
+	const float facets = D * smithVisibility(s.leaving, arriving, m.width);
+	const float lost   = lostOf(m, s.left, came);
+	if (s.kind == 2) {
+		// Schlick per channel, then to lanes: spectrumOf is linear in a shift toward white
+		const float rest = powf(fminf(fmaxf(1.0f - onto, 0.0f), 1.0f), 5.0f);
+		const float4 face = lin4(s.albedo, 1.0f - rest, flat4(1.0f), rest);
+		r.value           = lin4(face, facets, s.twice, lost);
+	} else {
+		const float through = m.coatRoom > 1e-6f ? (1.0f - m.coatFront * s.left) * (1.0f - m.coatFront * came) / m.coatRoom : 0.0f;
+		const float coated  = dielectricReflectance(onto, kCoatRatio) * facets + m.coatTwice * lost;
+		r.value             = lin4(s.albedo, through / kPiF, flat4(1.0f), coated);
+	}
+	const float facetDensity = ontoRaw <= 0.0f ? 0.0f : D * s.masking / (4.0f * s.leaving);
+	r.density                = s.share * facetDensity + (1.0f - s.share) * cosineDensity;
+	return r;
+}
+
+__device__ __forceinline__ Scatter noScatter() {
+	Scatter out;
+	out.found       = false;
+	out.through     = false;
+	out.delta       = false;
+	out.dispersed   = false;
+	out.incoming    = make_float3(0.0f, 0.0f, 1.0f);
+	out.weight      = flat4(0.0f);
+	out.density     = 0.0f;
+	out.mediumAfter = kNoMaterial;
+	return out;
+}
+
+// material.cpp:1398 sampleBsdf
+__device__ __forceinline__ Scatter sampleSurface(const Shading& s, const DeviceMaterial& m, float3 outgoing, float4 nm, float lobe, float side, float u, float v, uint32_t material, uint32_t medium) {
+	Scatter out = noScatter();
+	if (s.kind == 0) {
+		const float reach  = sqrtf(u);
+		const float angle  = 2.0f * kPiF * v;
+		const float height = sqrtf(fmaxf(1.0f - u, 0.0f));
+		out.incoming       = s.frame.toWorld(make_float3(reach * cosf(angle), reach * sinf(angle), height));
+		out.density        = fmaxf(dotF(s.normal, out.incoming), 0.0f) / kPiF;
+		out.found          = out.density > 0.0f;
+		out.weight         = s.albedo;
+		return out;
+	}
+	if (s.kind == 1 || s.kind == 2) {
+		// material.cpp:1198 roughScatter
+		if (s.leaving <= 0.0f) return out;
+		const bool facetLobe = lobe < s.share;
+		const float3 facet   = visibleFacet(s.frame, outgoing, m.width, u, v);
+		float3 incoming;
+		if (facetLobe) {
+			incoming = mirrorOf(outgoing, facet);
+		} else {
+			const float reach  = sqrtf(u);
+			const float angle  = 2.0f * kPiF * v;
+			const float height = sqrtf(fmaxf(1.0f - u, 0.0f));
+			incoming           = s.frame.toWorld(make_float3(reach * cosf(angle), reach * sinf(angle), height));
+		}
+		const float arriving = dotF(s.normal, incoming);
+		if ((facetLobe && dotF(outgoing, facet) <= 0.0f) || arriving <= 0.0f) return out;
+		const Response r = respond(s, m, outgoing, incoming, nm);
+		if (r.density <= 0.0f) return out;
+		out.found    = true;
+		out.incoming = incoming;
+		out.density  = r.density;
+		out.weight   = lin4(r.value, fabsf(arriving) / r.density, flat4(0.0f), 0.0f);
+		return out;
+	}
+	// material.cpp:1300 exactGlassScatter
+	if (s.leaving <= 0.0f) return out;
+	float refl[4];
+	for (int k = 0; k < 4; ++k) refl[k] = dielectricReflectance(s.leaving, lane4(s.within, k) / lane4(s.beyond, k));
+	if (!s.parted) refl[1] = refl[2] = refl[3] = refl[0];
+	const float chance   = s.parted ? 0.25f * (refl[0] + refl[1] + refl[2] + refl[3]) : refl[0];
+	const float ratio    = s.within.x / s.beyond.x;
+	const float leftover = 1.0f - ratio * ratio * (1.0f - s.leaving * s.leaving);
+	const bool passed    = leftover > 0.0f;
+	out.delta            = true;
+	out.found            = true;
+	out.density          = 0.0f;
+	if (side < chance || !passed) {
+		const float c  = passed ? chance : 1.0f;
+		out.incoming   = mirrorOf(outgoing, s.normal);
+		out.weight     = make_float4(refl[0] / c, refl[1] / c, refl[2] / c, refl[3] / c);
+		out.through    = false;
+		return out;
+	}
+	const float c        = 1.0f - chance;
+	out.incoming         = subF(scaleF(subF(scaleF(s.normal, s.leaving), outgoing), ratio), scaleF(s.normal, sqrtf(leftover)));
+	out.weight           = make_float4((1.0f - refl[0]) / c, (1.0f - refl[1]) / c, (1.0f - refl[2]) / c, (1.0f - refl[3]) / c);
+	out.through          = true;
+	out.dispersed        = s.parted && s.within.x != s.beyond.x;
+	out.mediumAfter      = medium != kNoMaterial ? kNoMaterial : material;
+	return out;
+}
+
+} // namespace kdn

@@ -1,16 +1,388 @@
-// Frame entry points (filled in with the transport kernels).
+// Frame entry points: kdn_render and kdn_render_device.
+//
+// A frame's paths are drawn in chunks of whole pixels (all samples of a pixel
+// in one chunk, pixel-major), each chunk driven through the wavefront:
+//   K-cam -> [K-trace -> K-hit -> K-shade -> K-trace(lines) -> K-line] x surfaces -> K-fold
+// with every queue count kept on the device, so a chunk runs with no host
+// synchronisation.  Pixel sums are kept in double on the device and persist
+// across calls (progressive accumulation) until a call starts afresh.
 #include "context.h"
+#include "frame.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
 
 namespace kdn {
-struct FrameState {};
+
+struct FrameState {
+	DeviceBuffer pixel, sample, throughput, radiance, nanometres, density, drawn, state, from;
+	DeviceBuffer queuePaths[2], queueRays[2], hits, states, counts;
+	DeviceBuffer shadowRays, shadowPaths, shadowContribution, shadowStates;
+	DeviceBuffer sums, out, materials;
+	uint32_t capacity = 0;
+	int32_t width = 0, height = 0;
+	double taken = 0;
+	std::vector<cudaEvent_t> events;
+	kdn_frame_stats stats {};
+};
+
 void Context::releaseFrame() {
+	if (frame == nullptr) return;
+	FrameState& f = *frame;
+	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.hits, &f.states, &f.counts, &f.shadowRays, &f.shadowPaths, &f.shadowContribution, &f.shadowStates, &f.sums, &f.out, &f.materials }) {
+		if (b->ptr) cudaFree(b->ptr);
+		b->ptr   = nullptr;
+		b->bytes = 0;
+	}
+	for (cudaEvent_t e : f.events) cudaEventDestroy(e);
 	delete frame;
 	frame = nullptr;
 }
+
+namespace {
+
+struct V3 {
+	double x, y, z;
+};
+V3 v3(const double* a) { return { a[0], a[1], a[2] }; }
+V3 sub(V3 a, V3 b) { return { a.x - b.x, a.y - b.y, a.z - b.z }; }
+V3 scale(V3 a, double s) { return { a.x * s, a.y * s, a.z * s }; }
+double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+V3 cross(V3 a, V3 b) { return { a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x }; }
+double length(V3 a) { return std::sqrt(dot(a, a)); }
+V3 normalized(V3 a) { return scale(a, 1.0 / length(a)); }
+void put(float* out, V3 a) {
+	out[0] = float(a.x);
+	out[1] = float(a.y);
+	out[2] = float(a.z);
+}
+
+// plugins/transport/paths/light/light.cpp:78 lampOf
+DeviceLamp lampOf(const kdn_light& l) {
+	DeviceLamp d {};
+	d.kind             = l.kind;
+	const V3 along     = v3(l.along), across = v3(l.across);
+	const V3 crossed   = cross(along, across);
+	const double area  = length(crossed);
+	const double al    = length(along), ac = length(across);
+	put(d.at, v3(l.at));
+	put(d.along, along);
+	put(d.across, across);
+	put(d.cross, crossed);
+	if (area > 0) put(d.facing, normalized(crossed));
+	if (al > 0 && ac > 0) {
+		const V3 ex = scale(along, 1.0 / al), ey = scale(across, 1.0 / ac);
+		put(d.ex, ex);
+		put(d.ey, ey);
+		put(d.raw, cross(ex, ey));
+	}
+	d.alongLength  = float(al);
+	d.acrossLength = float(ac);
+	d.square       = std::fabs(dot(along, across)) < 1e-9 * al * ac ? 1u : 0u;
+	d.radius       = l.radius;
+	const double pi = 3.14159265358979323846;
+	double k        = 1.0;
+	if (l.kind == 3) {
+		d.area = float(area);
+		k      = area > 0 ? 1.0 / area : 0.0;
+	} else if (l.kind == 2) {
+		d.area = float(4 * pi * double(l.radius) * double(l.radius));
+		k      = l.radius > 0 ? 1.0 / (pi * double(l.radius) * double(l.radius)) : 0.0;
+	}
+	for (int c = 0; c < 3; ++c) {
+		d.radiance[c] = float(l.power[c] * k);
+		d.power[c]    = float(l.power[c]);
+	}
+	return d;
+}
+
+DeviceMaterial materialOf(const kdn_material& m, const kdn_finish& f) {
+	DeviceMaterial d {};
+	d.kind = m.kind;
+	for (int c = 0; c < 3; ++c) {
+		d.albedo[c] = m.albedo[c];
+		d.absorb[c] = m.absorb[c];
+	}
+	d.roughness     = m.roughness;
+	d.index         = float(f.index);
+	d.dispersion    = m.kind == 3 ? m.dispersion : 0.0f;
+	d.exact         = f.exact;
+	d.sharp         = f.sharp;
+	d.width         = float(f.width);
+	d.facetShare    = float(f.facet_share);
+	d.body          = float(f.body);
+	d.escapeAverage = float(f.escape_average);
+	d.coatFront     = float(f.coat_front);
+	d.coatTwice     = float(f.coat_twice);
+	d.coatRoom      = float(f.coat_room);
+	for (int k = 0; k < 32; ++k) d.escape[k] = float(f.escape[k]);
+	return d;
+}
+
+// Why a material cannot be drawn by these kernels, or null.
+const char* unsupported(const kdn_material& m, const kdn_finish& f) {
+	if (m.kind > 3) return "a medium (scattering body)";
+	if (m.flags_ != 0) return "a patterned albedo";
+	if (m.glow[0] * m.strength > 0 || m.glow[1] * m.strength > 0 || m.glow[2] * m.strength > 0) return "a glowing surface";
+	if (m.absorb[0] != 0 || m.absorb[1] != 0 || m.absorb[2] != 0) return "an absorbing glass";
+	if (f.film[0] > 0) return "a thin film";
+	if (m.kind == 3 && !f.exact) return "a rough glass";
+	if (m.kind == 3 && m.refraction == 1.0f && m.dispersion == 0.0f) return "a passable glass";
+	return nullptr;
+}
+
+} // namespace
+
 } // namespace kdn
 
-extern "C" {
-kdn_status kdn_render(kdn_ctx*, const kdn_frame*, float*) { return KDN_NOT_READY; }
-kdn_status kdn_render_device(kdn_ctx*, const kdn_frame*, float*, void*) { return KDN_NOT_READY; }
-kdn_status kdn_frame_stats_get(kdn_ctx*, kdn_frame_stats*) { return KDN_NOT_READY; }
+using kdn::Context;
+using kdn::FrameState;
+
+namespace {
+
+kdn_status ensureFrame(Context* ctx, uint32_t capacity) {
+	if (ctx->frame == nullptr) ctx->frame = new FrameState();
+	FrameState& f = *ctx->frame;
+	if (f.capacity >= capacity) return KDN_OK;
+	const size_t n = capacity;
+	kdn_status s;
+	struct Want {
+		kdn::DeviceBuffer* b;
+		size_t bytes;
+	};
+	const Want wants[] = {
+		{ &f.pixel, n * 4 }, { &f.sample, n * 4 }, { &f.throughput, n * 16 }, { &f.radiance, n * 16 }, { &f.nanometres, n * 16 },
+		{ &f.density, n * 16 }, { &f.drawn, n * 4 }, { &f.state, n * 4 }, { &f.from, n * 16 },
+		{ &f.queuePaths[0], n * 4 }, { &f.queuePaths[1], n * 4 }, { &f.queueRays[0], n * sizeof(kdn_ray) }, { &f.queueRays[1], n * sizeof(kdn_ray) },
+		{ &f.hits, n * sizeof(kdn_hit) }, { &f.states, n * sizeof(kdn::HitState) }, { &f.counts, 64 },
+		{ &f.shadowRays, n * sizeof(kdn_ray) }, { &f.shadowPaths, n * 4 }, { &f.shadowContribution, n * 16 }, { &f.shadowStates, n * sizeof(kdn::HitState) },
+	};
+	for (const Want& w : wants) {
+		if ((s = ctx->ensure(*w.b, w.bytes)) != KDN_OK) return s;
+	}
+	f.capacity = capacity;
+	return KDN_OK;
 }
+
+kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream_t stream, bool hostOut) {
+	using namespace kdn;
+	if (!ctx->built) return ctx->fail(KDN_NOT_READY, "kdn_render: no world built (kdn_build)");
+	if (fr->width <= 0 || fr->height <= 0 || fr->samples <= 0 || fr->surfaces <= 0 || fr->surfaces > 255) return ctx->fail(KDN_BAD_ARG, "kdn_render: width, height, samples and surfaces (1..255) must be positive");
+	if (uint64_t(fr->width) * uint64_t(fr->height) > (uint64_t(1) << 26)) return ctx->fail(KDN_BAD_ARG, "kdn_render: frame larger than 2^26 pixels");
+	if (!ctx->has("shot.camera") || !ctx->has("looks.materials")) return ctx->fail(KDN_NOT_READY, "kdn_render: the shot.camera and looks.materials blocks are needed");
+	if (!ctx->check(cudaSetDevice(ctx->device), "cudaSetDevice")) return KDN_CUDA_ERROR;
+	const kdn_camera cam                     = ctx->block<kdn_camera>("shot.camera")[0];
+	const std::vector<kdn_light> lights      = ctx->block<kdn_light>("lighting.lights");
+	const std::vector<kdn_material> mats     = ctx->block<kdn_material>("looks.materials");
+	const std::vector<kdn_sky> skies         = ctx->block<kdn_sky>("lighting.sky");
+	if (lights.size() > kMaxLamps) return ctx->fail(KDN_BAD_ARG, "kdn_render: more than 16 lights");
+	if (mats.empty()) return ctx->fail(KDN_BAD_ARG, "kdn_render: no materials");
+	const std::vector<kdn_finish> finishes = ctx->block<kdn_finish>("transport.finishes");
+	if (finishes.size() != mats.size()) return ctx->fail(KDN_NOT_READY, "kdn_render: the transport.finishes block needs one finish per material");
+	for (size_t k = 0; k < mats.size(); ++k) {
+		const char* why = unsupported(mats[k], finishes[k]);
+		if (why) return ctx->fail(KDN_BAD_ARG, "kdn_render: material " + std::to_string(k) + " is " + why + ", which this build does not draw");
+	}
+	const uint32_t pixels = uint32_t(fr->width) * uint32_t(fr->height);
+	const uint32_t spp    = uint32_t(fr->samples);
+	const uint32_t want   = uint32_t(std::min<uint64_t>(uint64_t(pixels) * spp, uint64_t(1) << 22));
+	const uint32_t chunkPixels = std::max<uint32_t>(1, want / spp);
+	const uint32_t capacity    = chunkPixels * spp;
+	kdn_status s = ensureFrame(ctx, capacity);
+	if (s != KDN_OK) return s;
+	FrameState& f = *ctx->frame;
+	// pixel sums: fresh unless accumulating onto a frame of the same size
+	const bool fresh = !fr->accumulate || f.width != fr->width || f.height != fr->height || f.sums.ptr == nullptr;
+	if ((s = ctx->ensure(f.sums, size_t(pixels) * 3 * sizeof(double))) != KDN_OK) return s;
+	if (fresh) {
+		if (!ctx->check(cudaMemsetAsync(f.sums.ptr, 0, size_t(pixels) * 3 * sizeof(double), stream), "clear sums")) return KDN_CUDA_ERROR;
+		f.taken = 0;
+	}
+	f.width  = fr->width;
+	f.height = fr->height;
+	// constants
+	FrameConstants c {};
+	const V3 eye = v3(cam.eye), target = v3(cam.target), up = v3(cam.up);
+	const V3 forward = normalized(sub(target, eye));
+	const V3 right   = normalized(cross(forward, up));
+	put(c.eye, eye);
+	put(c.forward, forward);
+	put(c.right, right);
+	put(c.up, cross(right, forward));
+	c.reach         = float(std::tan(cam.fov / 2));
+	c.aspect        = float(double(fr->width) / double(fr->height));
+	c.width         = fr->width;
+	c.height        = fr->height;
+	c.seedMix       = mixedBits(uint64_t(int64_t(fr->seed)));
+	c.surfaces      = fr->surfaces;
+	c.spp           = spp;
+	c.firstSample   = fr->first;
+	c.lampCount     = uint32_t(lights.size());
+	c.materialCount = uint32_t(mats.size());
+	for (size_t k = 0; k < lights.size(); ++k) c.lamps[k] = lampOf(lights[k]);
+	if (!skies.empty()) {
+		put(c.zenith, v3(skies[0].zenith));
+		put(c.horizon, v3(skies[0].horizon));
+		put(c.ground, v3(skies[0].ground));
+	}
+	buildSpectralTables(c.spectral);
+	if (!ctx->check(uploadFrameConstants(c, stream), "frame constants")) return KDN_CUDA_ERROR;
+	std::vector<DeviceMaterial> dm;
+	for (size_t k = 0; k < mats.size(); ++k) dm.push_back(materialOf(mats[k], finishes[k]));
+	if ((s = ctx->upload(f.materials, dm.data(), dm.size() * sizeof(DeviceMaterial))) != KDN_OK) return s;
+	if ((s = ctx->ensure(ctx->counters, 8 * sizeof(unsigned long long))) != KDN_OK) return s;
+	if (!ctx->check(cudaMemsetAsync(ctx->counters.ptr, 0, 8 * sizeof(unsigned long long), stream), "clear counters")) return KDN_CUDA_ERROR;
+
+	PathBuffers P;
+	P.pixel      = static_cast<uint32_t*>(f.pixel.ptr);
+	P.sample     = static_cast<uint32_t*>(f.sample.ptr);
+	P.throughput = static_cast<float4*>(f.throughput.ptr);
+	P.radiance   = static_cast<float4*>(f.radiance.ptr);
+	P.nanometres = static_cast<float4*>(f.nanometres.ptr);
+	P.density    = static_cast<float4*>(f.density.ptr);
+	P.drawn      = static_cast<float*>(f.drawn.ptr);
+	P.state      = static_cast<uint32_t*>(f.state.ptr);
+	P.from       = static_cast<float4*>(f.from.ptr);
+	uint32_t* counts = static_cast<uint32_t*>(f.counts.ptr); // [0],[1] ray queues, [2] lines
+	QueueBuffers Q[2];
+	for (int k = 0; k < 2; ++k) {
+		Q[k].paths = static_cast<uint32_t*>(f.queuePaths[k].ptr);
+		Q[k].rays  = static_cast<kdn_ray*>(f.queueRays[k].ptr);
+		Q[k].count = counts + k;
+	}
+	ShadowBuffers S;
+	S.rays         = static_cast<kdn_ray*>(f.shadowRays.ptr);
+	S.paths        = static_cast<uint32_t*>(f.shadowPaths.ptr);
+	S.contribution = static_cast<float4*>(f.shadowContribution.ptr);
+	S.count        = counts + 2;
+	S.states       = static_cast<HitState*>(f.shadowStates.ptr);
+
+	// timing: one event pair around the frame, one around each trace launch
+	const uint32_t chunks = (pixels + chunkPixels - 1) / chunkPixels;
+	const size_t traceEvents = size_t(chunks) * size_t(fr->surfaces) * 4;
+	const size_t needEvents  = 2 + traceEvents;
+	while (f.events.size() < needEvents) {
+		cudaEvent_t e;
+		if (!ctx->check(cudaEventCreate(&e), "cudaEventCreate")) return KDN_CUDA_ERROR;
+		f.events.push_back(e);
+	}
+	size_t ev = 2;
+	if (!ctx->check(cudaEventRecord(f.events[0], stream), "event")) return KDN_CUDA_ERROR;
+	uint32_t launches = 0;
+	for (uint32_t first = 0; first < pixels; first += chunkPixels) {
+		const uint32_t chunk = std::min(chunkPixels, pixels - first);
+		const uint32_t n     = chunk * spp;
+		if (!ctx->check(launchCamera(P, Q[0], first, n, stream, ctx->smCount), "camera kernel")) return KDN_CUDA_ERROR;
+		++launches;
+		int cur = 0;
+		for (int bounce = 0; bounce < fr->surfaces; ++bounce) {
+			const int nxt = 1 - cur;
+			TraceArgs t;
+			t.world          = ctx->world;
+			t.rays           = Q[cur].rays;
+			t.n              = n;
+			t.states         = static_cast<HitState*>(f.states.ptr);
+			t.objectMaterial = static_cast<const uint32_t*>(ctx->objectMaterial.ptr);
+			t.maxSteps       = kMarchSteps;
+			t.counters       = static_cast<unsigned long long*>(ctx->counters.ptr);
+			t.count          = Q[cur].count;
+			cudaEventRecord(f.events[ev++], stream);
+			if (!ctx->check(launchTrace(t, stream, ctx->smCount), "trace kernel")) return KDN_CUDA_ERROR;
+			cudaEventRecord(f.events[ev++], stream);
+			HitArgs h;
+			h.world  = ctx->world;
+			h.rays   = Q[cur].rays;
+			h.states = t.states;
+			h.n      = n;
+			h.hits   = static_cast<kdn_hit*>(f.hits.ptr);
+			h.count  = Q[cur].count;
+			if (!ctx->check(launchHits(h, stream, ctx->smCount), "hit kernel")) return KDN_CUDA_ERROR;
+			if (!ctx->check(cudaMemsetAsync(Q[nxt].count, 0, 4, stream), "clear queue")) return KDN_CUDA_ERROR;
+			if (!ctx->check(cudaMemsetAsync(S.count, 0, 4, stream), "clear lines")) return KDN_CUDA_ERROR;
+			ShadeArgs a;
+			a.paths        = P;
+			a.in           = Q[cur];
+			a.out          = Q[nxt];
+			a.shadow       = S;
+			a.hits         = h.hits;
+			a.materials    = static_cast<const DeviceMaterial*>(f.materials.ptr);
+			a.leafMaterial = static_cast<const uint32_t*>(ctx->leafMaterial.ptr);
+			a.leafCount    = uint32_t(ctx->leafMaterial.bytes / 4);
+			a.capacity     = capacity;
+			a.error        = nullptr;
+			if (!ctx->check(launchShade(a, stream, ctx->smCount), "shade kernel")) return KDN_CUDA_ERROR;
+			TraceArgs l = t;
+			l.rays      = S.rays;
+			l.states    = S.states;
+			l.count     = S.count;
+			cudaEventRecord(f.events[ev++], stream);
+			if (!ctx->check(launchTrace(l, stream, ctx->smCount), "line trace kernel")) return KDN_CUDA_ERROR;
+			cudaEventRecord(f.events[ev++], stream);
+			if (!ctx->check(launchLines(P, S, capacity, stream, ctx->smCount), "lines kernel")) return KDN_CUDA_ERROR;
+			launches += 5;
+			cur = nxt;
+		}
+		if (!ctx->check(launchFold(P, first, chunk, spp, static_cast<double*>(f.sums.ptr), stream, ctx->smCount), "fold kernel")) return KDN_CUDA_ERROR;
+		++launches;
+	}
+	f.taken += double(spp);
+	float* image = out;
+	if (hostOut) {
+		if ((s = ctx->ensure(f.out, size_t(pixels) * 3 * sizeof(float))) != KDN_OK) return s;
+		image = static_cast<float*>(f.out.ptr);
+	}
+	if (!ctx->check(launchMeans(static_cast<const double*>(f.sums.ptr), pixels, f.taken, image, stream, ctx->smCount), "means kernel")) return KDN_CUDA_ERROR;
+	++launches;
+	if (!ctx->check(cudaEventRecord(f.events[1], stream), "event")) return KDN_CUDA_ERROR;
+	if (hostOut && !ctx->check(cudaMemcpyAsync(out, image, size_t(pixels) * 3 * sizeof(float), cudaMemcpyDeviceToHost, stream), "copy frame")) return KDN_CUDA_ERROR;
+	if (!ctx->check(cudaStreamSynchronize(stream), "kdn_render")) return KDN_CUDA_ERROR;
+	kdn_frame_stats st {};
+	float ms = 0;
+	cudaEventElapsedTime(&ms, f.events[0], f.events[1]);
+	st.total_ms = ms;
+	for (size_t k = 2; k + 1 < ev; k += 2) {
+		float t = 0;
+		cudaEventElapsedTime(&t, f.events[k], f.events[k + 1]);
+		st.trace_ms += t;
+	}
+	unsigned long long host[8] = {};
+	cudaMemcpy(host, ctx->counters.ptr, sizeof(host), cudaMemcpyDeviceToHost);
+	st.march_steps   = host[0];
+	st.program_steps = host[1];
+	st.launches      = launches;
+	st.other_ms      = st.total_ms - st.trace_ms;
+	f.stats          = st;
+	return KDN_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+kdn_status kdn_render(kdn_ctx* handle, const kdn_frame* frame, float* out_rgb) {
+	if (handle == nullptr || frame == nullptr || out_rgb == nullptr) return KDN_BAD_ARG;
+	Context* ctx = reinterpret_cast<Context*>(handle);
+	std::lock_guard<std::mutex> guard(ctx->lock);
+	if (ctx->device < 0) return ctx->fail(KDN_NO_DEVICE, "kdn_render: a host-only context has no device");
+	return renderFrame(ctx, frame, out_rgb, ctx->stream, true);
+}
+
+kdn_status kdn_render_device(kdn_ctx* handle, const kdn_frame* frame, float* out_rgb, void* stream) {
+	if (handle == nullptr || frame == nullptr || out_rgb == nullptr) return KDN_BAD_ARG;
+	Context* ctx = reinterpret_cast<Context*>(handle);
+	std::lock_guard<std::mutex> guard(ctx->lock);
+	if (ctx->device < 0) return ctx->fail(KDN_NO_DEVICE, "kdn_render_device: a host-only context has no device");
+	return renderFrame(ctx, frame, out_rgb, stream ? static_cast<cudaStream_t>(stream) : ctx->stream, false);
+}
+
+kdn_status kdn_frame_stats_get(kdn_ctx* handle, kdn_frame_stats* stats) {
+	if (handle == nullptr || stats == nullptr) return KDN_BAD_ARG;
+	Context* ctx = reinterpret_cast<Context*>(handle);
+	std::lock_guard<std::mutex> guard(ctx->lock);
+	if (ctx->frame == nullptr) return ctx->fail(KDN_NOT_READY, "kdn_frame_stats_get: no frame drawn");
+	*stats = ctx->frame->stats;
+	return KDN_OK;
+}
+
+} // extern "C"

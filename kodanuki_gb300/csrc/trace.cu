@@ -143,7 +143,8 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 	const uint32_t stride = blockDim.x;
 	float* slots          = slotMemory + threadIdx.x;
 	unsigned long long marchSteps = 0, programSteps = 0;
-	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < args.n; i += gridDim.x * blockDim.x) {
+	const uint32_t n = args.count ? *args.count : args.n;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 		const kdn_ray ray = args.rays[i];
 		const float o[3]  = { ray.origin[0], ray.origin[1], ray.origin[2] };
 		const float d[3]  = { ray.direction[0], ray.direction[1], ray.direction[2] };
@@ -200,14 +201,22 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 		args.states[i] = h;
 	}
 	if (args.counters) {
-		atomicAdd(&args.counters[0], marchSteps);
-		atomicAdd(&args.counters[1], programSteps);
+		// one add per warp
+		for (int o = 16; o > 0; o >>= 1) {
+			marchSteps += __shfl_down_sync(0xFFFFFFFFu, marchSteps, o);
+			programSteps += __shfl_down_sync(0xFFFFFFFFu, programSteps, o);
+		}
+		if ((threadIdx.x & 31) == 0) {
+			atomicAdd(&args.counters[0], marchSteps);
+			atomicAdd(&args.counters[1], programSteps);
+		}
 	}
 }
 
 __global__ void __launch_bounds__(kTraceBlock) hitKernel(HitArgs args) {
 	const DeviceWorld& w = args.world;
-	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < args.n; i += gridDim.x * blockDim.x) {
+	const uint32_t n     = args.count ? *args.count : args.n;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 		const HitState h  = args.states[i];
 		const kdn_ray ray = args.rays[i];
 		kdn_hit out;

@@ -1,0 +1,582 @@
+// The path-transport kernels, wavefront form: K-cam, K-shade (arrive, meet
+// with MIS, aim with a one-sample reservoir, BSDF sample, roulette), K-line
+// (add the lit shadow lines) and K-fold (spectral to RGB, per-pixel sums).
+//
+// The estimator follows the reference's plain strategy set (Meet + Aim,
+// plugins/transport/paths/strategy.cpp:119) with the power heuristic
+// (weight.cpp:27 weightOf, :95 meetDensities, :107 aimDensities):
+//  - camera legs see only the sky (light.cpp:132 seenByCamera);
+//  - every lamp is offered at a vertex and one offer, drawn by its lane mean,
+//    is traced (trace.cpp:896 aimedFrom, :830 offered);
+//  - at the surface cap the aim takes the whole weight (weight.cpp:107);
+//  - roulette from depth 4 with survival at most 0.95 (trace.cpp:1051);
+//  - rays leave a vertex lifted by 4e-3 plus twice the hit's looseness
+//    along the side they leave by (path.cpp:48 leavingRay, trace.cpp:466).
+// Throughput and radiance are four hero-wavelength lanes in FP32 (the
+// reference carries them in double).
+#include "frame.h"
+#include "materials.cuh"
+
+#include <cuda_runtime.h>
+
+namespace kdn {
+
+__constant__ FrameConstants cFrame;
+
+namespace {
+
+constexpr int kBlock = 128;
+constexpr float kBias = 4e-3f;
+
+enum Draw : int { PixelX = 0, PixelY, LensU, LensV, LightU, LightV, DirectionU, DirectionV, Lobe, Side, Survival, Pick };
+
+__device__ __forceinline__ float unitFrom(uint64_t bits53) {
+	const float u = __ull2float_rn(bits53) * 0x1p-53f;
+	return fminf(u, 0x1.fffffep-1f);
+}
+
+// plugins/transport/paths/path.cpp:22 dimensionOf for the per-event draws.
+__device__ __forceinline__ uint64_t dimensionOf(int event, int draw) {
+	return draw < LightU ? uint64_t(draw) : uint64_t(4 + event * 8 + (draw - LightU));
+}
+
+__device__ __forceinline__ float number(uint64_t stream, uint32_t index, int event, int draw) {
+	return unitFrom(hashedBits(stream, index, dimensionOf(event, draw)));
+}
+
+// plugins/transport/paths/trace.cpp:66 pixelNumbers
+__device__ __forceinline__ uint64_t streamOf(uint32_t x, uint32_t y) {
+	return cFrame.seedMix ^ mixedBits((uint64_t(x) << 32) | uint64_t(y));
+}
+
+__device__ __forceinline__ float3 f3(const float* v) { return make_float3(v[0], v[1], v[2]); }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 operator*(float3 a, float s) { return make_float3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 crossOf(float3 a, float3 b) { return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+__device__ __forceinline__ float lengthOf(float3 a) { return sqrtf(dot3(a, a)); }
+__device__ __forceinline__ float3 normalizedOf(float3 a) { return a * (1.0f / lengthOf(a)); }
+__device__ __forceinline__ float4 mul4(float4 a, float4 b) { return make_float4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w); }
+__device__ __forceinline__ float4 scale4(float4 a, float s) { return make_float4(a.x * s, a.y * s, a.z * s, a.w * s); }
+__device__ __forceinline__ float4 add4(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+__device__ __forceinline__ float mean4(float4 a) { return 0.25f * (a.x + a.y + a.z + a.w); }
+__device__ __forceinline__ float max4(float4 a) { return fmaxf(fmaxf(a.x, a.y), fmaxf(a.z, a.w)); }
+
+// ---- spectra (math/colour.cpp, math/spectrum.cpp) ----
+
+__device__ __forceinline__ float tableAt(const float* curve, float nm) {
+	const float slot  = (nm - 380.0f) / 5.0f;
+	int below         = int(slot);
+	below             = below < 0 ? 0 : (below > kTableSize - 2 ? kTableSize - 2 : below);
+	const float blend = fminf(fmaxf(slot - float(below), 0.0f), 1.0f);
+	return curve[below] + blend * (curve[below + 1] - curve[below]);
+}
+
+// math/colour.cpp:213 colourOf
+__device__ float3 colourOf(float4 nm, float4 density, float4 spectrum) {
+	const float lanes[4] = { nm.x, nm.y, nm.z, nm.w };
+	const float dens[4]  = { density.x, density.y, density.z, density.w };
+	const float spec[4]  = { spectrum.x, spectrum.y, spectrum.z, spectrum.w };
+	float x = 0.0f, y = 0.0f, z = 0.0f;
+	for (int k = 0; k < 4; ++k) {
+		if (dens[k] <= 0.0f) continue;
+		const float w = spec[k] / dens[k];
+		x += tableAt(cFrame.spectral.cie[0], lanes[k]) * w;
+		y += tableAt(cFrame.spectral.cie[1], lanes[k]) * w;
+		z += tableAt(cFrame.spectral.cie[2], lanes[k]) * w;
+	}
+	x *= 0.25f;
+	y *= 0.25f;
+	z *= 0.25f;
+	const float r = 3.2406f * x - 1.5372f * y - 0.4986f * z;
+	const float g = -0.9689f * x + 1.8758f * y + 0.0415f * z;
+	const float b = 0.0557f * x - 0.2040f * y + 1.0570f * z;
+	return make_float3(r / cFrame.spectral.white[0], g / cFrame.spectral.white[1], b / cFrame.spectral.white[2]);
+}
+
+// ---- lamps (plugins/transport/paths/light/light.cpp) ----
+
+struct Aim {
+	bool found;
+	float3 toward;
+	float distance;
+	float3 arriving; // RGB radiance over the density of the direction
+	float density;
+};
+
+// A spherical rectangle seen from a point: solid-angle sampling of a
+// rectangular light (Urena, Fajardo and King, "An Area-Preserving
+// Parametrization for Spherical Rectangles", EGSR 2013).
+struct Rectangle {
+	float3 x, y, z;
+	float z0, x0, x1, y0, y1, b0, b1, k, angle;
+};
+
+__device__ Rectangle rectangleFrom(const DeviceLamp& l, float3 origin) {
+	Rectangle r;
+	const float3 offset = f3(l.at) - origin;
+	const float3 raw    = f3(l.raw);
+	r.z                 = dot3(offset, raw) > 0.0f ? raw * -1.0f : raw;
+	r.x                 = f3(l.ex);
+	r.y                 = f3(l.ey);
+	r.z0                = dot3(offset, r.z);
+	r.x0                = dot3(offset, r.x);
+	r.y0                = dot3(offset, r.y);
+	r.x1                = r.x0 + l.alongLength;
+	r.y1                = r.y0 + l.acrossLength;
+	// normals of the four planes through the origin and each edge, by their z parts
+	const float sides[4]   = { r.z0 * r.x1 - r.x0 * r.z0, r.y0 * r.z0 - r.z0 * r.y1, r.z0 * r.x0 - r.x1 * r.z0, r.y1 * r.z0 - r.z0 * r.y0 };
+	const float heights[4] = { r.x0 * r.y0 - r.y0 * r.x1, r.x1 * r.y1 - r.y0 * r.x1, r.x1 * r.y1 - r.y1 * r.x0, r.x0 * r.y0 - r.y1 * r.x0 };
+	float upright[4];
+	for (int s = 0; s < 4; ++s) {
+		const float size = sqrtf(sides[s] * sides[s] + heights[s] * heights[s]);
+		upright[s]       = size > 0.0f ? heights[s] / size : heights[s];
+	}
+	const float g0 = acosf(fminf(fmaxf(-(upright[0] * upright[1]), -1.0f), 1.0f));
+	const float g1 = acosf(fminf(fmaxf(-(upright[1] * upright[2]), -1.0f), 1.0f));
+	const float g2 = acosf(fminf(fmaxf(-(upright[2] * upright[3]), -1.0f), 1.0f));
+	const float g3 = acosf(fminf(fmaxf(-(upright[3] * upright[0]), -1.0f), 1.0f));
+	r.b0           = upright[0];
+	r.b1           = upright[2];
+	r.k            = 2.0f * 3.14159265358979f - g2 - g3;
+	r.angle        = g0 + g1 - r.k;
+	return r;
+}
+
+__device__ float3 rectanglePoint(const Rectangle& r, float3 origin, float u, float v) {
+	const float au  = u * r.angle + r.k;
+	const float fu  = (cosf(au) * r.b0 - r.b1) / sinf(au);
+	const float cu  = fminf(fmaxf(copysignf(1.0f / sqrtf(fu * fu + r.b0 * r.b0), fu), -1.0f), 1.0f);
+	const float xu  = fminf(fmaxf(-(cu * r.z0) / sqrtf(fmaxf(1.0f - cu * cu, 1e-14f)), r.x0), r.x1);
+	const float d   = sqrtf(xu * xu + r.z0 * r.z0);
+	const float h0  = r.y0 / sqrtf(d * d + r.y0 * r.y0);
+	const float h1  = r.y1 / sqrtf(d * d + r.y1 * r.y1);
+	const float hv  = h0 + v * (h1 - h0);
+	const float hv2 = hv * hv;
+	const float yv  = hv2 < 1.0f - 1e-6f ? (hv * d) / sqrtf(1.0f - hv2) : r.y1;
+	return origin + r.x * xu + r.y * yv + r.z * r.z0;
+}
+
+__device__ __forceinline__ float coneDensity(float cosine) {
+	const float cone = 2.0f * 3.14159265358979f * (1.0f - cosine);
+	return cone > 1e-12f ? 1.0f / cone : 0.0f;
+}
+
+// aimLight (light.cpp:372) for a quad or a sphere lamp.
+__device__ Aim aimLamp(const DeviceLamp& l, float3 from, float u, float v) {
+	Aim a;
+	a.found = false;
+	if (l.kind == 3) { // quad
+		if (l.area < 1e-12f || dot3(f3(l.facing), from - f3(l.at)) <= 0.0f) return a;
+		float3 spot;
+		float density;
+		if (l.square) {
+			const Rectangle r = rectangleFrom(l, from);
+			if (!(r.angle > 1e-7f)) return a;
+			spot    = rectanglePoint(r, from, u, v);
+			density = 1.0f / r.angle;
+			const float3 off = spot - from;
+			const float dist = lengthOf(off);
+			if (dist < 1e-9f) return a;
+			a.found    = true;
+			a.toward   = off * (1.0f / dist);
+			a.distance = dist;
+			a.density  = density;
+			a.arriving = f3(l.radiance) * r.angle;
+			return a;
+		}
+		spot             = f3(l.at) + f3(l.along) * u + f3(l.across) * v;
+		const float3 off = spot - from;
+		const float dist = lengthOf(off);
+		if (dist < 1e-9f) return a;
+		a.toward         = off * (1.0f / dist);
+		const float tilt = -dot3(f3(l.facing), a.toward);
+		a.found          = true;
+		a.distance       = dist;
+		if (tilt <= 0.0f) {
+			a.arriving = make_float3(0.0f, 0.0f, 0.0f);
+			a.density  = 0.0f;
+			return a;
+		}
+		a.arriving = f3(l.radiance) * (tilt * l.area / (dist * dist));
+		a.density  = dist * dist / (tilt * l.area);
+		return a;
+	}
+	if (l.kind == 2) { // sphere
+		const float3 off  = f3(l.at) - from;
+		const float dist  = lengthOf(off);
+		if (dist < 1e-9f || dist <= l.radius) return a;
+		const float3 axis = off * (1.0f / dist);
+		const float side  = l.radius / dist;
+		const float cosine = sqrtf(fmaxf(1.0f - side * side, 0.0f));
+		const float height = 1.0f - u * (1.0f - cosine);
+		const float ring   = sqrtf(fmaxf(1.0f - height * height, 0.0f));
+		const float angle  = 2.0f * 3.14159265358979f * v;
+		const Frame f      = frameAround(axis);
+		const float3 toward = f.toWorld(make_float3(ring * cosf(angle), ring * sinf(angle), height));
+		const float h      = dot3(toward, axis);
+		const float r2     = sqrtf(fmaxf(1.0f - h * h, 0.0f));
+		const float reach  = dist * h - sqrtf(fmaxf(l.radius * l.radius - dist * dist * r2 * r2, 0.0f));
+		a.found    = true;
+		a.toward   = toward;
+		a.distance = fmaxf(reach, 0.0f);
+		a.arriving = f3(l.power) * (2.0f * (1.0f - cosine) / (l.radius * l.radius));
+		a.density  = coneDensity(cosine);
+		return a;
+	}
+	return a;
+}
+
+// aimDensity (light.cpp:463): the density aiming gives a direction.
+__device__ float aimDensityOf(const DeviceLamp& l, float3 from, float3 toward, float distance) {
+	if (l.kind == 3) {
+		if (l.area < 1e-12f || dot3(f3(l.facing), from - f3(l.at)) <= 0.0f) return 0.0f;
+		if (l.square) {
+			const Rectangle r = rectangleFrom(l, from);
+			return r.angle > 1e-7f ? 1.0f / r.angle : 0.0f;
+		}
+		const float tilt = -dot3(f3(l.facing), toward);
+		if (tilt <= 0.0f || distance <= 0.0f) return 0.0f;
+		return distance * distance / (tilt * l.area);
+	}
+	if (l.kind == 2) {
+		const float away = lengthOf(f3(l.at) - from);
+		if (away <= l.radius || l.radius <= 0.0f) return 0.0f;
+		const float side = l.radius / away;
+		return coneDensity(sqrtf(fmaxf(1.0f - side * side, 0.0f)));
+	}
+	return 0.0f;
+}
+
+// meetLight (light.cpp:498) for a lamp: where a ray meets it before limit.
+__device__ bool meetLamp(const DeviceLamp& l, float3 origin, float3 dir, float limit, float& reach) {
+	if (l.kind == 3) {
+		const float3 facing = f3(l.cross);
+		const float leaning = dot3(facing, dir);
+		if (l.area < 1e-12f || leaning >= -1e-12f) return false;
+		reach = dot3(facing, f3(l.at) - origin) / leaning;
+		if (reach <= 1e-9f || reach >= limit) return false;
+		const float3 spot   = origin + dir * reach - f3(l.at);
+		const float squared = l.area * l.area;
+		const float u       = dot3(crossOf(spot, f3(l.across)), facing) / squared;
+		const float v       = dot3(crossOf(f3(l.along), spot), facing) / squared;
+		return !(u < 0.0f || u > 1.0f || v < 0.0f || v > 1.0f);
+	}
+	if (l.kind == 2) {
+		if (l.radius <= 0.0f) return false;
+		const float3 off  = origin - f3(l.at);
+		const float along = dot3(off, dir);
+		const float under = along * along - (dot3(off, off) - l.radius * l.radius);
+		if (under <= 0.0f) return false;
+		const float root  = sqrtf(under);
+		const float first = -along - root;
+		reach             = first <= 1e-9f ? -along + root : first;
+		return !(reach <= 1e-9f || reach >= limit);
+	}
+	return false;
+}
+
+// light.cpp:575 gradientColour
+__device__ float3 skyColour(float3 dir) {
+	const float height = dir.z;
+	const float3 far   = height >= 0.0f ? f3(cFrame.zenith) : f3(cFrame.ground);
+	const float share  = sqrtf(fabsf(height));
+	return f3(cFrame.horizon) * (1.0f - share) + far * share;
+}
+
+__device__ __forceinline__ kdn_ray makeRay(float3 o, float3 d, float far, uint32_t medium) {
+	kdn_ray r;
+	r.origin[0]    = o.x;
+	r.origin[1]    = o.y;
+	r.origin[2]    = o.z;
+	r.direction[0] = d.x;
+	r.direction[1] = d.y;
+	r.direction[2] = d.z;
+	r.far          = far;
+	r.inside       = medium != kNoMaterial ? 1 : 0;
+	r.pad_[0] = r.pad_[1] = r.pad_[2] = 0;
+	r.within       = medium;
+	return r;
+}
+
+// Append to a queue, one atomic per warp.
+__device__ __forceinline__ uint32_t warpSlot(uint32_t* count, bool want) {
+	const unsigned active = __activemask();
+	const unsigned mask   = __ballot_sync(active, want);
+	if (mask == 0) return 0xFFFFFFFFu;
+	const int lane   = threadIdx.x & 31;
+	const int leader = __ffs(mask) - 1;
+	uint32_t base    = 0;
+	if (lane == leader) base = atomicAdd(count, uint32_t(__popc(mask)));
+	base = __shfl_sync(active, base, leader);
+	return want ? base + uint32_t(__popc(mask & ((1u << lane) - 1u))) : 0xFFFFFFFFu;
+}
+
+// ---- K-cam: camera rays and hero wavelengths (trace.cpp:116 startedPathIn) ----
+__global__ void __launch_bounds__(kBlock) cameraKernel(PathBuffers P, QueueBuffers Q, uint32_t firstPixel, uint32_t n) {
+	if (blockIdx.x == 0 && threadIdx.x == 0) *Q.count = n;
+	for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+		const uint32_t pixel  = firstPixel + p / cFrame.spp;
+		const uint32_t sample = cFrame.firstSample + p % cFrame.spp;
+		const uint32_t x      = pixel % uint32_t(cFrame.width);
+		const uint32_t y      = pixel / uint32_t(cFrame.width);
+		const uint64_t stream = streamOf(x, y);
+		// math/colour.cpp:236 sampledWavelengths of the pixel's golden-ratio share
+		const double start  = double(hashedBits(stream, ~uint64_t(0), 0)) * 0x1p-53;
+		const double turned = double(sample) * 0.6180339887498949 + start;
+		const double share  = turned - floor(turned);
+		float nm[4], dens[4];
+		for (int lane = 0; lane < 4; ++lane) {
+			const double raw    = share + 0.25 * lane;
+			const double t      = raw >= 1.0 ? raw - 1.0 : raw;
+			const double place  = t * kCuts;
+			const int index     = int(place) < kCuts - 1 ? int(place) : kCuts - 1;
+			const double width  = cFrame.spectral.cuts[index + 1] - cFrame.spectral.cuts[index];
+			const double value  = cFrame.spectral.cuts[index] + (place - index) * width;
+			nm[lane]            = float(fmin(value, 699.9999999999999));
+			dens[lane]          = float(1.0 / (kCuts * width));
+		}
+		const float px = float(x) + number(stream, sample, 0, PixelX);
+		const float py = float(y) + number(stream, sample, 0, PixelY);
+		const float u  = 2.0f * px / float(cFrame.width) - 1.0f;
+		const float v  = 1.0f - 2.0f * py / float(cFrame.height);
+		const float3 heading = normalizedOf(f3(cFrame.forward) + f3(cFrame.right) * (u * cFrame.reach * cFrame.aspect) + f3(cFrame.up) * (v * cFrame.reach));
+		P.pixel[p]      = pixel;
+		P.sample[p]     = sample;
+		P.throughput[p] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+		P.radiance[p]   = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+		P.nanometres[p] = make_float4(nm[0], nm[1], nm[2], nm[3]);
+		P.density[p]    = make_float4(dens[0], dens[1], dens[2], dens[3]);
+		P.drawn[p]      = 0.0f;
+		P.state[p]      = 1u << 8;
+		P.from[p]       = make_float4(cFrame.eye[0], cFrame.eye[1], cFrame.eye[2], 0.0f);
+		Q.paths[p]      = p;
+		Q.rays[p]       = makeRay(f3(cFrame.eye), heading, __int_as_float(0x7f800000), kNoMaterial);
+	}
+}
+
+// ---- K-shade ----
+__global__ void __launch_bounds__(kBlock) shadeKernel(ShadeArgs A) {
+	const uint32_t n = *A.in.count;
+	for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+		const uint32_t q = base + threadIdx.x;
+		bool live        = q < n;
+		bool onward      = false;
+		bool lined       = false;
+		kdn_ray next {};
+		kdn_ray line {};
+		float4 lineRadiance = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+		uint32_t p = 0;
+		if (live) {
+			p                   = A.in.paths[q];
+			const kdn_hit hit   = A.hits[q];
+			const kdn_ray ray   = A.in.rays[q];
+			const uint32_t st   = A.paths.state[p];
+			const int depth     = int(st & 0xFFu);
+			const bool camera   = (st >> 8) & 1u;
+			uint32_t medium     = (st >> 16) == 0 ? kNoMaterial : (st >> 16) - 1u;
+			float4 T            = A.paths.throughput[p];
+			float4 R            = A.paths.radiance[p];
+			const float4 nm     = A.paths.nanometres[p];
+			const float drawnDensity = A.paths.drawn[p];
+			const float3 heading = make_float3(ray.direction[0], ray.direction[1], ray.direction[2]);
+			const float3 origin  = make_float3(ray.origin[0], ray.origin[1], ray.origin[2]);
+			const bool found     = hit.kind != 0;
+			// meet: lamps along the leg (not for camera legs) and the sky past it
+			if (!camera) {
+				const float limit = found ? hit.distance : 3.0e38f;
+				const float3 from = make_float3(A.paths.from[p].x, A.paths.from[p].y, A.paths.from[p].z);
+				for (uint32_t k = 0; k < cFrame.lampCount; ++k) {
+					const DeviceLamp& l = cFrame.lamps[k];
+					float reach;
+					if (!meetLamp(l, origin, heading, limit, reach)) continue;
+					float w = 1.0f;
+					if (drawnDensity > 0.0f) {
+						const float pa = aimDensityOf(l, from, heading, reach);
+						w              = drawnDensity * drawnDensity / (drawnDensity * drawnDensity + pa * pa);
+					}
+					R = add4(R, scale4(mul4(T, spectrumOf(l.radiance[0], l.radiance[1], l.radiance[2], nm)), w));
+				}
+			}
+			if (!found) {
+				const float3 sky = skyColour(heading);
+				R                = add4(R, mul4(T, spectrumOf(sky.x, sky.y, sky.z, nm)));
+			} else {
+				const uint32_t material = hit.leaf < A.leafCount ? A.leafMaterial[hit.leaf] : 0u;
+				const DeviceMaterial& m = A.materials[material < cFrame.materialCount ? material : 0u];
+				const float3 point      = make_float3(hit.point[0], hit.point[1], hit.point[2]);
+				float3 normal           = make_float3(hit.normal[0], hit.normal[1], hit.normal[2]);
+				if (dot3(normal, heading) >= 0.0f) normal = normal * -1.0f;
+				const float lift        = kBias + 2.0f * hit.loosened;
+				const uint32_t x        = A.paths.pixel[p] % uint32_t(cFrame.width);
+				const uint32_t y        = A.paths.pixel[p] / uint32_t(cFrame.width);
+				const uint64_t stream   = streamOf(x, y);
+				const uint32_t index    = A.paths.sample[p];
+				const bool capped       = depth + 1 >= cFrame.surfaces;
+				const float3 outgoing   = heading * -1.0f;
+				const Shading surf      = surfaceOf(m, normal, outgoing, nm, medium, A.materials);
+				// aim: offer every lamp, trace one offer drawn by its lane mean
+				if (!m.exact && cFrame.lampCount > 0) {
+					const float u0   = number(stream, index, depth, LightU);
+					const float v0   = number(stream, index, depth, LightV);
+					float choice     = number(stream, index, depth, Pick);
+					float total      = 0.0f, picked = 0.0f;
+					float4 chosen    = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+					float3 chosenDir = make_float3(0.0f, 0.0f, 1.0f);
+					float chosenDist = 0.0f;
+					for (uint32_t k = 0; k < cFrame.lampCount; ++k) {
+						const Aim a = aimLamp(cFrame.lamps[k], point, u0, v0);
+						if (!a.found) continue;
+						const float facing = dot3(normal, a.toward);
+						if (facing <= 0.0f || a.distance <= 0.0f) continue;
+						const Response f = respond(surf, m, outgoing, a.toward, nm);
+						float w          = 1.0f;
+						if (a.density > 0.0f) {
+							const float pm = capped ? 0.0f : f.density;
+							w              = a.density * a.density / (a.density * a.density + pm * pm);
+						}
+						const float4 offer = scale4(mul4(mul4(T, f.value), spectrumOf(a.arriving.x, a.arriving.y, a.arriving.z, nm)), facing * w);
+						const float weight = mean4(offer);
+						if (!(weight > 0.0f)) continue;
+						total           = total + weight;
+						const float keep = weight / total;
+						if (choice < keep) {
+							chosen     = offer;
+							picked     = weight;
+							chosenDir  = a.toward;
+							chosenDist = a.distance;
+							choice     = choice / keep;
+						} else {
+							choice = (choice - keep) / (1.0f - keep);
+						}
+					}
+					if (picked > 0.0f) {
+						lined        = true;
+						lineRadiance = scale4(chosen, total / picked);
+						line         = makeRay(point + normal * lift, chosenDir, chosenDist - lift, kNoMaterial);
+					}
+				}
+				// scatter (trace.cpp:1020 scatteredFrom)
+				if (!capped) {
+					const float lobe = number(stream, index, depth, Lobe);
+					const float side = number(stream, index, depth, Side);
+					const float du   = number(stream, index, depth, DirectionU);
+					const float dv   = number(stream, index, depth, DirectionV);
+					Scatter s        = sampleSurface(surf, m, outgoing, nm, lobe, side, du, dv, material, medium);
+					const float sideOf = dot3(s.incoming, normal);
+					const bool below   = s.through ? sideOf >= 0.0f : sideOf <= 0.0f;
+					if (s.found && !below) {
+						float4 carried  = mul4(T, s.weight);
+						// trace.cpp:961 carriedThroughput: past a dispersing bend only the hero lane goes on
+						const bool wasDispersed = (st >> 9) & 1u;
+						if (s.dispersed && !wasDispersed) carried = make_float4(carried.x * 4.0f, 0.0f, 0.0f, 0.0f);
+						bool alive      = true;
+						if (depth >= 4) {
+							const float survival = fminf(0.95f, max4(carried));
+							if (!(number(stream, index, depth, Survival) < survival)) alive = false;
+							else carried = scale4(carried, 1.0f / survival);
+						}
+						if (alive) {
+							if (s.through) medium = s.mediumAfter;
+							onward                = true;
+							T                     = carried;
+							const float off       = sideOf > 0.0f ? lift : -lift;
+							next                  = makeRay(point + normal * off, s.incoming, __int_as_float(0x7f800000), medium);
+							A.paths.drawn[p]      = s.delta ? 0.0f : s.density;
+							A.paths.from[p]       = make_float4(point.x, point.y, point.z, 0.0f);
+							uint32_t stNext       = uint32_t(depth + 1) | (medium == kNoMaterial ? 0u : ((medium + 1u) << 16));
+							if (s.dispersed || ((st >> 9) & 1u)) stNext |= 1u << 9;
+							A.paths.state[p]      = stNext;
+						}
+					}
+				}
+			}
+			A.paths.throughput[p] = T;
+			A.paths.radiance[p]   = R;
+		}
+		const uint32_t slot = warpSlot(A.out.count, onward);
+		if (onward && slot < A.capacity) {
+			A.out.paths[slot] = p;
+			A.out.rays[slot]  = next;
+		}
+		const uint32_t lineSlot = warpSlot(A.shadow.count, lined);
+		if (lined && lineSlot < A.capacity) {
+			A.shadow.rays[lineSlot]         = line;
+			A.shadow.paths[lineSlot]        = p;
+			A.shadow.contribution[lineSlot] = lineRadiance;
+		}
+	}
+}
+
+// ---- K-line: add each shadow line that reached its lamp (trace.cpp:1294 lineAnswered) ----
+__global__ void __launch_bounds__(kBlock) linesKernel(PathBuffers P, ShadowBuffers S) {
+	const uint32_t n = *S.count;
+	for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+		if (S.states[s].kind != 0) continue;
+		const uint32_t p = S.paths[s];
+		P.radiance[p]    = add4(P.radiance[p], S.contribution[s]);
+	}
+}
+
+// ---- K-fold: per pixel, the samples' colours (frame.cpp:273 foldPixels) ----
+__global__ void __launch_bounds__(kBlock) foldKernel(PathBuffers P, uint32_t firstPixel, uint32_t pixels, uint32_t spp, double* sums) {
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < pixels; i += gridDim.x * blockDim.x) {
+		double r = 0.0, g = 0.0, b = 0.0;
+		for (uint32_t k = 0; k < spp; ++k) {
+			const uint32_t p = i * spp + k;
+			const float3 c   = colourOf(P.nanometres[p], P.density[p], P.radiance[p]);
+			r += double(c.x);
+			g += double(c.y);
+			b += double(c.z);
+		}
+		double* s = sums + 3ull * (firstPixel + i);
+		s[0] += r;
+		s[1] += g;
+		s[2] += b;
+	}
+}
+
+__global__ void __launch_bounds__(kBlock) meansKernel(const double* sums, uint32_t pixels, double taken, float* out) {
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < pixels * 3u; i += gridDim.x * blockDim.x) {
+		out[i] = float(sums[i] / taken);
+	}
+}
+
+uint32_t gridFor(uint64_t n, int smCount) {
+	const uint64_t blocks = (n + kBlock - 1) / kBlock;
+	return uint32_t(std::max<uint64_t>(1, std::min<uint64_t>(blocks, uint64_t(smCount) * 16)));
+}
+
+} // namespace
+
+cudaError_t uploadFrameConstants(const FrameConstants& c, cudaStream_t stream) {
+	return cudaMemcpyToSymbolAsync(cFrame, &c, sizeof(FrameConstants), 0, cudaMemcpyHostToDevice, stream);
+}
+
+cudaError_t launchCamera(const PathBuffers& paths, const QueueBuffers& queue, uint32_t firstPixel, uint32_t n, cudaStream_t stream, int smCount) {
+	cameraKernel<<<gridFor(n, smCount), kBlock, 0, stream>>>(paths, queue, firstPixel, n);
+	return cudaGetLastError();
+}
+
+cudaError_t launchShade(const ShadeArgs& args, cudaStream_t stream, int smCount) {
+	shadeKernel<<<gridFor(args.capacity, smCount), kBlock, 0, stream>>>(args);
+	return cudaGetLastError();
+}
+
+cudaError_t launchLines(const PathBuffers& paths, const ShadowBuffers& shadow, uint32_t capacity, cudaStream_t stream, int smCount) {
+	linesKernel<<<gridFor(capacity, smCount), kBlock, 0, stream>>>(paths, shadow);
+	return cudaGetLastError();
+}
+
+cudaError_t launchFold(const PathBuffers& paths, uint32_t firstPixel, uint32_t pixels, uint32_t spp, double* sums, cudaStream_t stream, int smCount) {
+	foldKernel<<<gridFor(pixels, smCount), kBlock, 0, stream>>>(paths, firstPixel, pixels, spp, sums);
+	return cudaGetLastError();
+}
+
+cudaError_t launchMeans(const double* sums, uint32_t pixels, double taken, float* out, cudaStream_t stream, int smCount) {
+	meansKernel<<<gridFor(uint64_t(pixels) * 3, smCount), kBlock, 0, stream>>>(sums, pixels, taken, out);
+	return cudaGetLastError();
+}
+
+} // namespace kdn

@@ -27,6 +27,9 @@ constexpr uint32_t kNoLeaf     = 0xFFFFFFFFu;
 constexpr uint32_t kMaxSlots   = 48;   // register slots a leaf program may use
 constexpr uint32_t kMaxSsa     = 1024; // steps a leaf program may hold
 constexpr uint32_t kMaxLeafProgs = 64; // kept programs of one leaf
+// The most steps a ray is marched (sphere_trace.h:37 sphereSteps): a ray that
+// skims a surface for longer meets nothing.
+constexpr uint32_t kMarchSteps = 1u << 16;
 
 struct GpuStep {
 	uint8_t op;

@@ -98,6 +98,22 @@ class Scene:
             "glow": np.array([m["glow"] for m in ms], np.float64).reshape(-1, 3),
             "strength": np.array([m["strength"] for m in ms], np.float32),
         }
+        fs = d.get("finishes", [])
+        if fs:
+            mats.update({
+                "finish_kind": np.array([f["kind"] for f in fs], np.uint32),
+                "finish_sharp": np.array([f["sharp"] for f in fs], np.uint32),
+                "finish_exact": np.array([f["exact"] for f in fs], np.uint32),
+                "finish_loses_much": np.array([f["losesMuch"] for f in fs], np.uint32),
+                "finish_width": np.array([f["width"] for f in fs], np.float64),
+                "finish_facet_share": np.array([f["facetShare"] for f in fs], np.float64),
+                "finish_body": np.array([f["body"] for f in fs], np.float64),
+                "finish_index": np.array([f["index"] for f in fs], np.float64),
+                "finish_coating": np.array([f["coating"] for f in fs], np.float64).reshape(-1, 3),
+                "finish_escape_average": np.array([f["escapeAverage"] for f in fs], np.float64),
+                "finish_escape": np.array([f["escape"] for f in fs], np.float64).reshape(-1, 32),
+                "finish_film": np.array([f["film"] for f in fs], np.float64).reshape(-1, 2),
+            })
         ls = d["lights"]
         lights = {
             "kind": np.array([l["kind"] for l in ls], np.uint8),

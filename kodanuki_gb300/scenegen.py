@@ -153,7 +153,7 @@ def scene_config2(seed: int = 1, width: int = 1920, height: int = 1080, samples:
         elif r < 0.8:
             mats.append(f"metal({_v([rng.uniform(0.5, 0.95) for _ in range(3)])}, roughness = {_f(rng.uniform(0.05, 0.5))})")
         else:
-            mats.append("glass(refraction = 1.76, dispersion = 0.01)")
+            mats.append("glass(refraction = 1.76, dispersion = 0.01, roughness = 0)")
     for i in range(groups):
         center = [rng.uniform(-8.0, 8.0), rng.uniform(-6.0, 10.0), rng.uniform(-2.5, 2.5)]
         kind = rng.random()

@@ -143,3 +143,86 @@ class Octree:
         mat = np.ascontiguousarray(self.scene.leaf_material, np.uint32)
         lib().kp_octree_trace(self.handle, _ptr(mat), _ptr(rays), len(rays), _ptr(hits))
         return hits
+
+
+class Material(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_uint32), ("exact", ctypes.c_uint32), ("albedo", ctypes.c_double * 3), ("index", ctypes.c_double),
+                ("dispersion", ctypes.c_double), ("width", ctypes.c_double), ("facet_share", ctypes.c_double), ("body", ctypes.c_double),
+                ("coat_front", ctypes.c_double), ("coat_twice", ctypes.c_double), ("coat_room", ctypes.c_double),
+                ("escape_average", ctypes.c_double), ("escape", ctypes.c_double * 32)]
+
+
+class Lamp(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_uint32), ("square", ctypes.c_uint32), ("at", ctypes.c_double * 3), ("along", ctypes.c_double * 3),
+                ("across", ctypes.c_double * 3), ("power", ctypes.c_double * 3), ("radius", ctypes.c_double)]
+
+
+class View(ctypes.Structure):
+    _fields_ = [("eye", ctypes.c_double * 3), ("target", ctypes.c_double * 3), ("up", ctypes.c_double * 3), ("fov", ctypes.c_double),
+                ("zenith", ctypes.c_double * 3), ("horizon", ctypes.c_double * 3), ("ground", ctypes.c_double * 3),
+                ("width", ctypes.c_int32), ("height", ctypes.c_int32), ("spp", ctypes.c_int32), ("surfaces", ctypes.c_int32),
+                ("seed", ctypes.c_int32), ("lamp_count", ctypes.c_uint32), ("material_count", ctypes.c_uint32)]
+
+
+_trees: dict = {}
+
+
+def _octree_for(scene, build: dict) -> "Octree":
+    key = (id(scene), build["min_depth"], build["max_depth"], build["split_steps"])
+    if key not in _trees:
+        _trees[key] = Octree(scene, build["min_depth"], build["max_depth"], build["split_steps"])
+    return _trees[key]
+
+
+def render_band(scene, width: int, height: int, spp: int, surfaces: int, seed: int, row0: int, rows: int, threads: int,
+                build: dict | None = None) -> np.ndarray:
+    """The oracle renderer over rows [row0, row0 + rows) of a frame: summed
+    RGB per pixel (rows x width x 3, divide by spp for the means)."""
+    build = build or dict(min_depth=6, max_depth=10, split_steps=96)
+    tree = _octree_for(scene, build)
+    m = scene.materials
+    n = len(m["kind"])
+    mats = (Material * n)()
+    for i in range(n):
+        mats[i].kind = int(m["kind"][i])
+        mats[i].exact = int(m["finish_exact"][i]) if "finish_exact" in m else 0
+        for c in range(3):
+            mats[i].albedo[c] = float(m["albedo"][i][c])
+        mats[i].index = float(m["finish_index"][i]) if "finish_index" in m else 1.0
+        mats[i].dispersion = float(m["dispersion"][i]) if int(m["kind"][i]) == 3 else 0.0
+        if "finish_width" in m:
+            mats[i].width = float(m["finish_width"][i])
+            mats[i].facet_share = float(m["finish_facet_share"][i])
+            mats[i].body = float(m["finish_body"][i])
+            mats[i].coat_front, mats[i].coat_twice, mats[i].coat_room = (float(x) for x in m["finish_coating"][i])
+            mats[i].escape_average = float(m["finish_escape_average"][i])
+            for k in range(32):
+                mats[i].escape[k] = float(m["finish_escape"][i][k])
+    l = scene.lights
+    nl = len(l["kind"])
+    lamps = (Lamp * max(nl, 1))()
+    for i in range(nl):
+        lamps[i].kind = int(l["kind"][i])
+        for c in range(3):
+            lamps[i].at[c] = float(l["at"][i][c])
+            lamps[i].along[c] = float(l["along"][i][c])
+            lamps[i].across[c] = float(l["across"][i][c])
+            lamps[i].power[c] = float(l["power"][i][c])
+        lamps[i].radius = float(l["radius"][i])
+    v = View()
+    for c in range(3):
+        v.eye[c] = scene.camera["eye"][c]
+        v.target[c] = scene.camera["target"][c]
+        v.up[c] = scene.camera["up"][c]
+        v.zenith[c] = scene.sky["zenith"][c]
+        v.horizon[c] = scene.sky["horizon"][c]
+        v.ground[c] = scene.sky["ground"][c]
+    v.fov = scene.camera["fov"]
+    v.width, v.height, v.spp, v.surfaces, v.seed = width, height, spp, surfaces, seed
+    v.lamp_count, v.material_count = nl, n
+    sums = np.zeros((rows, width, 3), np.float64)
+    mat_leaf = np.ascontiguousarray(scene.leaf_material, np.uint32)
+    L = lib()
+    L.kp_render_band.argtypes = [_P, _P, _P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]
+    L.kp_render_band(tree.handle, _ptr(mat_leaf), ctypes.addressof(mats), ctypes.addressof(lamps), ctypes.byref(v), row0, rows, threads, _ptr(sums))
+    return sums

@@ -1032,6 +1032,45 @@ static void trace_all(const kp_octree* tree, const kp_program* programs, uint32_
 	free(m.cand2);
 }
 
+/* A reusable single-ray tracer over an octree, one per thread. */
+struct kp_tracer {
+	march m;
+	const kp_octree* tree;
+};
+
+kp_tracer* kp_tracer_new(const kp_octree* tree, const uint32_t* leaf_material) {
+	kp_tracer* t = (kp_tracer*) calloc(1, sizeof(kp_tracer));
+	uint32_t longest = 1;
+	for (uint64_t i = 0; i < tree->ncells; ++i)
+		for (uint32_t k = 0; k < tree->cells[i].nprog; ++k) longest = tree->cells[i].progs[k].count > longest ? tree->cells[i].progs[k].count : longest;
+	t->tree = tree;
+	t->m.tree = tree;
+	t->m.programs = NULL;
+	t->m.count = 0;
+	t->m.leaf_material = leaf_material;
+	t->m.regs = (double*) malloc(sizeof(double) * longest);
+	t->m.dregs = (kp_dual*) malloc(sizeof(kp_dual) * longest);
+	t->m.storage = (kp_program*) malloc(sizeof(kp_program) * 8192);
+	t->m.cand = (cand_list*) malloc(sizeof(cand_list));
+	t->m.cand2 = (cand_list*) malloc(sizeof(cand_list));
+	return t;
+}
+
+void kp_tracer_trace(kp_tracer* t, const kp_ray* ray, kp_hit* hit) {
+	t->m.ray = ray;
+	trace_one(&t->m, t->tree->lower, t->tree->size, hit);
+}
+
+void kp_tracer_free(kp_tracer* t) {
+	if (!t) return;
+	free(t->m.regs);
+	free(t->m.dregs);
+	free(t->m.storage);
+	free(t->m.cand);
+	free(t->m.cand2);
+	free(t);
+}
+
 void kp_sphere_trace(const kp_program* programs, uint32_t count, const uint32_t* leaf_material, const double lower[3], const double size[3], const kp_ray* rays, uint32_t n, kp_hit* hits) {
 	trace_all(NULL, programs, count, leaf_material, lower, size, rays, n, hits);
 }

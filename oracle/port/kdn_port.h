@@ -106,6 +106,46 @@ void kp_sphere_trace(const kp_program* programs, uint32_t count, const uint32_t*
  * octree cell the point lies in, and empty cells skipped to their exit. */
 void kp_octree_trace(const kp_octree* tree, const uint32_t* leaf_material, const kp_ray* rays, uint32_t n, kp_hit* hits);
 
+/* One tracer per thread: the same march, one ray at a time. */
+typedef struct kp_tracer kp_tracer;
+kp_tracer* kp_tracer_new(const kp_octree* tree, const uint32_t* leaf_material);
+void kp_tracer_trace(kp_tracer* t, const kp_ray* ray, kp_hit* hit);
+void kp_tracer_free(kp_tracer* t);
+
+/* ---- transport (plugins/transport/paths) ---- */
+/* A material as the transport draws it: the Material's kind and albedo and
+ * the Finish derived from it (material.cpp:204 finishWith). */
+typedef struct kp_material {
+	uint32_t kind, exact;
+	double albedo[3];
+	double index, dispersion, width, facet_share, body;
+	double coat_front, coat_twice, coat_room, escape_average;
+	double escape[32];
+} kp_material;
+
+/* A lamp (light.cpp:78 lampOf): kind 2 sphere, 3 quad. */
+typedef struct kp_lamp {
+	uint32_t kind, square;
+	double at[3], along[3], across[3], power[3], radius;
+} kp_lamp;
+
+typedef struct kp_view {
+	double eye[3], target[3], up[3], fov;
+	double zenith[3], horizon[3], ground[3];
+	int32_t width, height, spp, surfaces, seed;
+	uint32_t lamp_count, material_count;
+} kp_view;
+
+/*
+ * Draw rows [row0, row0 + rows) of a frame, spp samples a pixel, on
+ * `threads` threads: the reference's plain path transport
+ * (trace.cpp:116 startedPathIn, :1547 walkArrived, :896 aimedFrom, :1020
+ * scatteredFrom, frame.cpp:273 foldPixels) in double.  sums gets the summed
+ * RGB of each pixel of the band (3 doubles a pixel).
+ */
+void kp_render_band(const kp_octree* tree, const uint32_t* leaf_material, const kp_material* materials, const kp_lamp* lamps, const kp_view* view,
+                    int row0, int rows, int threads, double* sums);
+
 /* ---- numbers, wavelengths and colour (math/random.cpp, math/colour.cpp) ---- */
 uint64_t kp_mixed_bits(uint64_t v);
 double kp_unit_of(uint64_t bits);

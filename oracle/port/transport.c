@@ -1,0 +1,743 @@
+/*
+ * Oracle transport: the reference renderer's plain path tracer (Meet + Aim
+ * strategies, plugins/transport/paths) restated in C over double precision,
+ * on the oracle's octree sphere tracer.  Test infrastructure and the timed
+ * CPU baseline (see kdn_port.h).
+ *
+ * Per sample (plugins/transport/paths/trace.cpp):
+ *   startedPathIn (:116)  counter-based numbers keyed by pixel and sample,
+ *                         hero wavelengths, the pinhole camera ray;
+ *   walkArrived (:1547)   meet the lamps along the leg and the sky past it,
+ *                         weighted by the power heuristic (weight.cpp:27);
+ *                         camera legs see only the sky (light.cpp:132);
+ *   aimedFrom (:896)      offer every lamp, trace one offer drawn by its lane
+ *                         mean (:830 offered); the aim takes the whole weight
+ *                         at the surface cap (weight.cpp:107);
+ *   scatteredFrom (:1020) the BSDF's own direction, roulette from depth 4
+ *                         with survival at most 0.95;
+ *   foldPixels (frame.cpp:273) spectral radiance to RGB (colour.cpp:213).
+ */
+#include "kdn_port.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define PI 3.14159265358979323846
+#define BIAS 4e-3
+#define NO_MATERIAL 0xFFFFFFFFu
+
+typedef struct v3 {
+	double x, y, z;
+} v3;
+
+static v3 mk(double x, double y, double z) {
+	v3 r = { x, y, z };
+	return r;
+}
+static v3 vd(const double* a) { return mk(a[0], a[1], a[2]); }
+static v3 add(v3 a, v3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+static v3 sub(v3 a, v3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+static v3 scl(v3 a, double s) { return mk(a.x * s, a.y * s, a.z * s); }
+static double dotv(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static v3 crossv(v3 a, v3 b) { return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+static double len(v3 a) { return sqrt(dotv(a, a)); }
+static v3 unit(v3 a) { return scl(a, 1.0 / len(a)); }
+static double clampd(double x, double lo, double hi) { return x < lo ? lo : (hi < x ? hi : x); }
+static double maxd(double a, double b) { return a < b ? b : a; }
+static double mind(double a, double b) { return b < a ? b : a; }
+
+/* math/random.cpp basisAround: any orthonormal frame about n */
+typedef struct basis {
+	v3 t, b, n;
+} basis;
+
+static basis basis_around(v3 n) {
+	const double sign = copysign(1.0, n.z);
+	const double a = -1.0 / (sign + n.z);
+	const double b = n.x * n.y * a;
+	basis f;
+	f.t = mk(1.0 + sign * n.x * n.x * a, sign * b, -sign * n.x);
+	f.b = mk(b, sign + n.y * n.y * a, -n.y);
+	f.n = n;
+	return f;
+}
+static v3 to_world(basis f, v3 v) { return add(add(scl(f.t, v.x), scl(f.b, v.y)), scl(f.n, v.z)); }
+static v3 to_local(basis f, v3 v) { return mk(dotv(f.t, v), dotv(f.b, v), dotv(f.n, v)); }
+static v3 mirrored(v3 v, v3 n) { return sub(scl(n, 2 * dotv(v, n)), v); }
+
+typedef struct lanes {
+	double nm[4], density[4], basis[12];
+} lanes;
+
+typedef struct spec {
+	double v[4];
+} spec;
+
+static spec flat(double x) {
+	spec s = { { x, x, x, x } };
+	return s;
+}
+static spec smul(spec a, spec b) {
+	for (int k = 0; k < 4; ++k) a.v[k] *= b.v[k];
+	return a;
+}
+static spec sscale(spec a, double s) {
+	for (int k = 0; k < 4; ++k) a.v[k] *= s;
+	return a;
+}
+static spec sadd(spec a, spec b) {
+	for (int k = 0; k < 4; ++k) a.v[k] += b.v[k];
+	return a;
+}
+static double smean(spec a) { return 0.25 * (a.v[0] + a.v[1] + a.v[2] + a.v[3]); }
+static double smax(spec a) { return maxd(maxd(a.v[0], a.v[1]), maxd(a.v[2], a.v[3])); }
+
+static spec spectrum(const double rgb[3], const lanes* w) {
+	spec s;
+	kp_spectrum_of(rgb, w->basis, s.v);
+	return s;
+}
+
+/* ---- numbers (trace.cpp:47 drawnNumber, path.cpp:22 dimensionOf) ---- */
+enum { PIXEL_X, PIXEL_Y, LENS_U, LENS_V, LIGHT_U, LIGHT_V, DIRECTION_U, DIRECTION_V, LOBE, SIDE, SURVIVAL, PICK };
+
+static double number(uint64_t stream, uint32_t index, int event, int draw) {
+	const uint64_t dim = draw < LIGHT_U ? (uint64_t) draw : (uint64_t) (4 + event * 8 + (draw - LIGHT_U));
+	return kp_hashed(stream, index, dim);
+}
+
+/* ---- lamps (light.cpp) ---- */
+typedef struct lamp {
+	uint32_t kind, square;
+	v3 at, along, across, facing, cross, ex, ey, raw;
+	double along_len, across_len, area, radius;
+	double radiance[3], power[3];
+} lamp;
+
+static lamp lamp_of(const kp_lamp* l) {
+	lamp d;
+	memset(&d, 0, sizeof d);
+	d.kind = l->kind;
+	d.at = vd(l->at);
+	d.along = vd(l->along);
+	d.across = vd(l->across);
+	d.cross = crossv(d.along, d.across);
+	d.area = len(d.cross);
+	d.along_len = len(d.along);
+	d.across_len = len(d.across);
+	if (d.area > 0) d.facing = unit(d.cross);
+	if (d.along_len > 0 && d.across_len > 0) {
+		d.ex = scl(d.along, 1 / d.along_len);
+		d.ey = scl(d.across, 1 / d.across_len);
+		d.raw = crossv(d.ex, d.ey);
+	}
+	d.square = fabs(dotv(d.along, d.across)) < 1e-9 * d.along_len * d.across_len;
+	d.radius = l->radius;
+	double k = 1;
+	if (l->kind == 3) {
+		k = d.area > 0 ? 1 / d.area : 0;
+	} else if (l->kind == 2) {
+		k = l->radius > 0 ? 1 / (PI * l->radius * l->radius) : 0;
+		d.area = 4 * PI * l->radius * l->radius;
+	}
+	for (int c = 0; c < 3; ++c) {
+		d.power[c] = l->power[c];
+		d.radiance[c] = l->power[c] * k;
+	}
+	return d;
+}
+
+typedef struct rect {
+	v3 x, y, z;
+	double z0, x0, x1, y0, y1, b0, b1, k, angle;
+} rect;
+
+/* light.cpp:169 rectangleView: a spherical rectangle (Urena et al. 2013) */
+static rect rect_view(const lamp* l, v3 origin) {
+	rect r;
+	const v3 off = sub(l->at, origin);
+	r.z = dotv(off, l->raw) > 0 ? scl(l->raw, -1) : l->raw;
+	r.x = l->ex;
+	r.y = l->ey;
+	r.z0 = dotv(off, r.z);
+	r.x0 = dotv(off, r.x);
+	r.y0 = dotv(off, r.y);
+	r.x1 = r.x0 + l->along_len;
+	r.y1 = r.y0 + l->across_len;
+	const double sides[4] = { r.z0 * r.x1 - r.x0 * r.z0, r.y0 * r.z0 - r.z0 * r.y1, r.z0 * r.x0 - r.x1 * r.z0, r.y1 * r.z0 - r.z0 * r.y0 };
+	const double heights[4] = { r.x0 * r.y0 - r.y0 * r.x1, r.x1 * r.y1 - r.y0 * r.x1, r.x1 * r.y1 - r.y1 * r.x0, r.x0 * r.y0 - r.y1 * r.x0 };
+	double up[4];
+	for (int s = 0; s < 4; ++s) {
+		const double size = sqrt(sides[s] * sides[s] + heights[s] * heights[s]);
+		up[s] = size > 0 ? heights[s] / size : heights[s];
+	}
+	const double g0 = acos(clampd(-(up[0] * up[1]), -1, 1));
+	const double g1 = acos(clampd(-(up[1] * up[2]), -1, 1));
+	const double g2 = acos(clampd(-(up[2] * up[3]), -1, 1));
+	const double g3 = acos(clampd(-(up[3] * up[0]), -1, 1));
+	r.b0 = up[0];
+	r.b1 = up[2];
+	r.k = 2 * PI - g2 - g3;
+	r.angle = g0 + g1 - r.k;
+	return r;
+}
+
+static v3 rect_point(const rect* r, v3 origin, double u, double v) {
+	const double au = u * r->angle + r->k;
+	const double fu = (cos(au) * r->b0 - r->b1) / sin(au);
+	const double cu = clampd(copysign(1 / sqrt(fu * fu + r->b0 * r->b0), fu), -1, 1);
+	const double xu = clampd(-(cu * r->z0) / sqrt(maxd(1 - cu * cu, 1e-14)), r->x0, r->x1);
+	const double d = sqrt(xu * xu + r->z0 * r->z0);
+	const double h0 = r->y0 / sqrt(d * d + r->y0 * r->y0);
+	const double h1 = r->y1 / sqrt(d * d + r->y1 * r->y1);
+	const double hv = h0 + v * (h1 - h0);
+	const double hv2 = hv * hv;
+	const double yv = hv2 < 1 - 1e-6 ? (hv * d) / sqrt(1 - hv2) : r->y1;
+	return add(add(add(origin, scl(r->x, xu)), scl(r->y, yv)), scl(r->z, r->z0));
+}
+
+static double cone_density(double c) {
+	const double cone = 2 * PI * (1 - c);
+	return cone > 1e-12 ? 1 / cone : 0;
+}
+
+typedef struct aim {
+	int found;
+	v3 toward;
+	double distance, density;
+	double arriving[3];
+} aim;
+
+/* light.cpp:372 aimLight for quads and spheres */
+static aim aim_lamp(const lamp* l, v3 from, double u, double v) {
+	aim a;
+	memset(&a, 0, sizeof a);
+	if (l->kind == 3) {
+		if (l->area < 1e-12 || dotv(l->facing, sub(from, l->at)) <= 0) return a;
+		if (l->square) {
+			const rect r = rect_view(l, from);
+			if (!(r.angle > 1e-7)) return a;
+			const v3 spot = rect_point(&r, from, u, v);
+			const v3 off = sub(spot, from);
+			const double d = len(off);
+			if (d < 1e-9) return a;
+			a.found = 1;
+			a.toward = scl(off, 1 / d);
+			a.distance = d;
+			a.density = 1 / r.angle;
+			for (int c = 0; c < 3; ++c) a.arriving[c] = l->radiance[c] * r.angle;
+			return a;
+		}
+		const v3 spot = add(add(l->at, scl(l->along, u)), scl(l->across, v));
+		const v3 off = sub(spot, from);
+		const double d = len(off);
+		if (d < 1e-9) return a;
+		a.toward = scl(off, 1 / d);
+		const double tilt = -dotv(l->facing, a.toward);
+		a.found = 1;
+		a.distance = d;
+		if (tilt <= 0) return a;
+		for (int c = 0; c < 3; ++c) a.arriving[c] = l->radiance[c] * (tilt * l->area / (d * d));
+		a.density = d * d / (tilt * l->area);
+		return a;
+	}
+	if (l->kind == 2) {
+		const v3 off = sub(l->at, from);
+		const double d = len(off);
+		if (d < 1e-9 || d <= l->radius) return a;
+		const v3 axis = scl(off, 1 / d);
+		const double side = l->radius / d;
+		const double cosine = sqrt(maxd(1 - side * side, 0));
+		const double height = 1 - u * (1 - cosine);
+		const double ring = sqrt(maxd(1 - height * height, 0));
+		const double angle = 2 * PI * v;
+		const v3 toward = to_world(basis_around(axis), mk(ring * cos(angle), ring * sin(angle), height));
+		const double h = dotv(toward, axis);
+		const double r2 = sqrt(maxd(1 - h * h, 0));
+		const double reach = d * h - sqrt(maxd(l->radius * l->radius - d * d * r2 * r2, 0));
+		a.found = 1;
+		a.toward = toward;
+		a.distance = maxd(reach, 0);
+		for (int c = 0; c < 3; ++c) a.arriving[c] = l->power[c] * (2 * (1 - cosine) / (l->radius * l->radius));
+		a.density = cone_density(cosine);
+	}
+	return a;
+}
+
+/* light.cpp:463 aimDensity */
+static double aim_density(const lamp* l, v3 from, v3 toward, double distance) {
+	if (l->kind == 3) {
+		if (l->area < 1e-12 || dotv(l->facing, sub(from, l->at)) <= 0) return 0;
+		if (l->square) {
+			const rect r = rect_view(l, from);
+			return r.angle > 1e-7 ? 1 / r.angle : 0;
+		}
+		const double tilt = -dotv(l->facing, toward);
+		if (tilt <= 0 || distance <= 0) return 0;
+		return distance * distance / (tilt * l->area);
+	}
+	if (l->kind == 2) {
+		const double away = len(sub(l->at, from));
+		if (away <= l->radius || l->radius <= 0) return 0;
+		const double side = l->radius / away;
+		return cone_density(sqrt(maxd(1 - side * side, 0)));
+	}
+	return 0;
+}
+
+/* light.cpp:498 meetLight for a lamp */
+static int meet_lamp(const lamp* l, v3 origin, v3 dir, double limit, double* reach) {
+	if (l->kind == 3) {
+		const double leaning = dotv(l->cross, dir);
+		if (l->area < 1e-12 || leaning >= -1e-12) return 0;
+		*reach = dotv(l->cross, sub(l->at, origin)) / leaning;
+		if (*reach <= 1e-9 || *reach >= limit) return 0;
+		const v3 spot = sub(add(origin, scl(dir, *reach)), l->at);
+		const double sq = l->area * l->area;
+		const double u = dotv(crossv(spot, l->across), l->cross) / sq;
+		const double v = dotv(crossv(l->along, spot), l->cross) / sq;
+		return !(u < 0 || u > 1 || v < 0 || v > 1);
+	}
+	if (l->kind == 2) {
+		if (l->radius <= 0) return 0;
+		const v3 off = sub(origin, l->at);
+		const double along = dotv(off, dir);
+		const double under = along * along - (dotv(off, off) - l->radius * l->radius);
+		if (under <= 0) return 0;
+		const double root = sqrt(under);
+		const double first = -along - root;
+		*reach = first <= 1e-9 ? -along + root : first;
+		return !(*reach <= 1e-9 || *reach >= limit);
+	}
+	return 0;
+}
+
+/* ---- materials (material/material.cpp, microfacet.cpp, energy.cpp) ---- */
+static double facet_distribution(double c, double w) {
+	if (c <= 0) return 0;
+	const double sq = w * w, lo = c * c * (sq - 1) + 1;
+	return sq / (PI * lo * lo);
+}
+static double smith_visibility(double l, double a, double w) {
+	const double sq = w * w;
+	const double t = a * sqrt(sq + (1 - sq) * l * l) + l * sqrt(sq + (1 - sq) * a * a);
+	return t > 0 ? 0.5 / t : 0;
+}
+static double smith_masking(double c, double w) {
+	const double sq = w * w, u = c + sqrt(sq + (1 - sq) * c * c);
+	return u > 0 ? 2 * c / u : 0;
+}
+static v3 halfway(v3 o, v3 i, v3 n) {
+	const v3 t = add(o, i);
+	const double s = len(t);
+	return s > 1e-12 ? scl(t, 1 / s) : n;
+}
+static double dielectric(double c, double ratio) {
+	const double left = 1 - ratio * ratio * (1 - c * c);
+	if (left <= 0) return 1;
+	const double on = sqrt(left);
+	const double pe = (ratio * c - on) / (ratio * c + on);
+	const double pa = (ratio * on - c) / (ratio * on + c);
+	return 0.5 * (pe * pe + pa * pa);
+}
+static double escape_at(const double* table, double c) {
+	const double place = clampd(c, 0, 1) * 32 - 0.5;
+	int lower = (int) floor(place);
+	lower = lower < 0 ? 0 : (lower > 31 ? 31 : lower);
+	const int upper = lower + 1 < 31 ? lower + 1 : 31;
+	const double share = clampd(place - lower, 0, 1);
+	return table[lower] * (1 - share) + table[upper] * share;
+}
+static v3 visible_facet(basis f, v3 out, double w, double u, double v) {
+	const v3 local = to_local(f, out);
+	const v3 st = unit(mk(w * local.x, w * local.y, local.z));
+	const double flat = st.x * st.x + st.y * st.y;
+	const v3 first = flat > 1e-12 ? scl(mk(-st.y, st.x, 0), 1 / sqrt(flat)) : mk(1, 0, 0);
+	const v3 second = crossv(st, first);
+	const double reach = sqrt(u), angle = 2 * PI * v;
+	const double across = reach * cos(angle);
+	const double lean = 0.5 * (1 + st.z);
+	const double along = (1 - lean) * sqrt(maxd(1 - across * across, 0)) + lean * reach * sin(angle);
+	const double height = sqrt(maxd(1 - across * across - along * along, 0));
+	const v3 raised = add(add(scl(first, across), scl(second, along)), scl(st, height));
+	return to_world(f, unit(mk(w * raised.x, w * raised.y, maxd(raised.z, 1e-12))));
+}
+
+typedef struct shading {
+	const kp_material* m;
+	v3 normal;
+	basis frame;
+	spec albedo, twice, within, beyond;
+	double leaving, left, share, masking;
+	int parted;
+} shading;
+
+static spec lane_indices(const kp_material* m, const lanes* w) {
+	spec s;
+	for (int k = 0; k < 4; ++k) {
+		const double um = w->nm[k] * 1e-3;
+		s.v[k] = m->dispersion == 0 ? m->index : m->index + m->dispersion / (um * um);
+	}
+	return s;
+}
+
+static shading shading_of(const kp_material* m, const kp_material* all, v3 n, v3 out, const lanes* w, uint32_t medium) {
+	shading s;
+	memset(&s, 0, sizeof s);
+	s.m = m;
+	s.normal = n;
+	s.frame = basis_around(n);
+	s.albedo = spectrum(m->albedo, w);
+	s.leaving = dotv(n, out);
+	s.within = flat(1);
+	s.beyond = flat(1);
+	if (m->kind == 1 || m->kind == 2) {
+		s.left = escape_at(m->escape, s.leaving);
+		if (m->kind == 2) {
+			s.share = m->facet_share;
+		} else if (s.leaving > 0) {
+			/* material.cpp:440 plasticShare */
+			const double face = dielectric(s.leaving, 1 / 1.5);
+			s.share = clampd(face / maxd(face + (1 - face) * m->body, 1e-12), 0.25, 0.9);
+		}
+		s.masking = smith_masking(s.leaving, m->width);
+		if (m->kind == 2) {
+			/* material.cpp:567 metalTwice over microfacet.cpp:116 averagedFresnel */
+			double avg[3];
+			for (int c = 0; c < 3; ++c) avg[c] = m->albedo[c] + (1 - m->albedo[c]) * (1.0 / 21);
+			const spec a = spectrum(avg, w);
+			for (int k = 0; k < 4; ++k) s.twice.v[k] = a.v[k] * a.v[k] * m->escape_average / (1 - a.v[k] * (1 - m->escape_average));
+		}
+	} else if (m->kind == 3) {
+		if (medium != NO_MATERIAL) {
+			s.within = lane_indices(&all[medium], w);
+			s.parted = all[medium].dispersion != 0;
+		} else {
+			s.beyond = lane_indices(m, w);
+			s.parted = m->dispersion != 0;
+		}
+	}
+	return s;
+}
+
+typedef struct response {
+	spec value;
+	double density;
+} response;
+
+static response respond(const shading* s, v3 out, v3 in, const lanes* w) {
+	response r;
+	r.value = flat(0);
+	const kp_material* m = s->m;
+	const double arriving = dotv(s->normal, in);
+	if (m->kind == 0) {
+		r.density = maxd(arriving, 0) / PI;
+		if (s->leaving > 0 && arriving > 0) r.value = sscale(s->albedo, 1 / PI);
+		return r;
+	}
+	if (m->kind == 3) {
+		r.density = 0;
+		return r;
+	}
+	const double cosd = maxd(arriving, 0) / PI;
+	if (s->leaving <= 0 || arriving <= 0) {
+		r.density = (m->kind == 1 && s->leaving <= 0) ? 0 : (1 - s->share) * cosd;
+		return r;
+	}
+	const v3 h = halfway(out, in, s->normal);
+	const double D = facet_distribution(dotv(s->normal, h), m->width);
+	const double came = escape_at(m->escape, arriving);
+	const double onto_raw = dotv(out, h);
+	const double onto = maxd(onto_raw, 0);
+	const double facets = D * smith_visibility(s->leaving, arriving, m->width);
+	const double room = 1 - m->escape_average;
+	const double lost = room <= 1e-6 ? 0 : (1 - s->left) * (1 - came) / (PI * room);
+	if (m->kind == 2) {
+		/* material.cpp:649 viewedMetal, microfacet.cpp:111 schlickOf */
+		const double rest = pow(clampd(1 - onto, 0, 1), 5.0);
+		double face[3];
+		for (int c = 0; c < 3; ++c) face[c] = m->albedo[c] + (1 - m->albedo[c]) * rest;
+		r.value = sadd(sscale(spectrum(face, w), facets), sscale(s->twice, lost));
+	} else {
+		/* material.cpp:661 viewedPlastic */
+		const double through = m->coat_room > 1e-6 ? (1 - m->coat_front * s->left) * (1 - m->coat_front * came) / m->coat_room : 0;
+		const double coated = dielectric(onto, 1 / 1.5) * facets + m->coat_twice * lost;
+		r.value = sadd(sscale(s->albedo, through / PI), flat(coated));
+	}
+	const double fd = onto_raw <= 0 ? 0 : D * s->masking / (4 * s->leaving);
+	r.density = s->share * fd + (1 - s->share) * cosd;
+	return r;
+}
+
+typedef struct scatter {
+	int found, through, delta, dispersed;
+	v3 incoming;
+	spec weight;
+	double density;
+	uint32_t medium_after;
+} scatter;
+
+static scatter sample(const shading* s, v3 out, const lanes* w, double lobe, double side, double u, double v, uint32_t material, uint32_t medium) {
+	scatter o;
+	memset(&o, 0, sizeof o);
+	o.medium_after = NO_MATERIAL;
+	const kp_material* m = s->m;
+	if (m->kind == 0) {
+		const double reach = sqrt(u), angle = 2 * PI * v, height = sqrt(maxd(1 - u, 0));
+		o.incoming = to_world(s->frame, mk(reach * cos(angle), reach * sin(angle), height));
+		o.density = maxd(dotv(s->normal, o.incoming), 0) / PI;
+		o.found = o.density > 0;
+		o.weight = s->albedo;
+		return o;
+	}
+	if (m->kind == 1 || m->kind == 2) {
+		if (s->leaving <= 0) return o;
+		const int facet_lobe = lobe < s->share;
+		const v3 facet = visible_facet(s->frame, out, m->width, u, v);
+		v3 in;
+		if (facet_lobe) {
+			in = mirrored(out, facet);
+		} else {
+			const double reach = sqrt(u), angle = 2 * PI * v, height = sqrt(maxd(1 - u, 0));
+			in = to_world(s->frame, mk(reach * cos(angle), reach * sin(angle), height));
+		}
+		const double arriving = dotv(s->normal, in);
+		if ((facet_lobe && dotv(out, facet) <= 0) || arriving <= 0) return o;
+		const response r = respond(s, out, in, w);
+		if (r.density <= 0) return o;
+		o.found = 1;
+		o.incoming = in;
+		o.density = r.density;
+		o.weight = sscale(r.value, fabs(arriving) / r.density);
+		return o;
+	}
+	/* material.cpp:1300 exactGlassScatter */
+	if (s->leaving <= 0) return o;
+	double refl[4];
+	for (int k = 0; k < 4; ++k) refl[k] = dielectric(s->leaving, s->within.v[k] / s->beyond.v[k]);
+	if (!s->parted) refl[1] = refl[2] = refl[3] = refl[0];
+	const double chance = s->parted ? 0.25 * (refl[0] + refl[1] + refl[2] + refl[3]) : refl[0];
+	const double ratio = s->within.v[0] / s->beyond.v[0];
+	const double leftover = 1 - ratio * ratio * (1 - s->leaving * s->leaving);
+	const int passed = leftover > 0;
+	o.found = 1;
+	o.delta = 1;
+	if (side < chance || !passed) {
+		const double c = passed ? chance : 1;
+		o.incoming = mirrored(out, s->normal);
+		for (int k = 0; k < 4; ++k) o.weight.v[k] = refl[k] / c;
+		return o;
+	}
+	const double c = 1 - chance;
+	o.incoming = sub(scl(sub(scl(s->normal, s->leaving), out), ratio), scl(s->normal, sqrt(leftover)));
+	for (int k = 0; k < 4; ++k) o.weight.v[k] = (1 - refl[k]) / c;
+	o.through = 1;
+	o.dispersed = s->parted && s->within.v[0] != s->beyond.v[0];
+	o.medium_after = medium != NO_MATERIAL ? NO_MATERIAL : material;
+	return o;
+}
+
+/* ---- the band renderer ---- */
+typedef struct job {
+	const kp_octree* tree;
+	const uint32_t* leaf_material;
+	const kp_material* materials;
+	lamp lamps[16];
+	const kp_view* view;
+	int row0, rows, next;
+	pthread_mutex_t lock;
+	double* sums;
+	v3 eye, forward, right, up;
+	double reach, aspect;
+	uint64_t seed_mix;
+} job;
+
+static kp_ray ray_of(v3 o, v3 d, double far, uint32_t medium) {
+	kp_ray r;
+	r.origin[0] = (float) o.x;
+	r.origin[1] = (float) o.y;
+	r.origin[2] = (float) o.z;
+	r.direction[0] = (float) d.x;
+	r.direction[1] = (float) d.y;
+	r.direction[2] = (float) d.z;
+	r.far = (float) far;
+	r.inside = medium != NO_MATERIAL;
+	r.within = medium;
+	return r;
+}
+
+static void sky_colour(const kp_view* view, v3 d, double out[3]) {
+	const double h = d.z;
+	const double* far = h >= 0 ? view->zenith : view->ground;
+	const double share = sqrt(fabs(h));
+	for (int c = 0; c < 3; ++c) out[c] = view->horizon[c] * (1 - share) + far[c] * share;
+}
+
+static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index, double rgb[3]) {
+	const kp_view* V = J->view;
+	const uint64_t stream = J->seed_mix ^ kp_mixed_bits(((uint64_t) (uint32_t) x << 32) | (uint64_t) (uint32_t) y);
+	lanes w;
+	kp_sampled_wavelengths(kp_wavelength_share(kp_hashed(stream, ~(uint64_t) 0, 0), index), w.nm, w.density, w.basis);
+	const double px = x + number(stream, index, 0, PIXEL_X);
+	const double py = y + number(stream, index, 0, PIXEL_Y);
+	const double u = 2 * px / V->width - 1, v = 1 - 2 * py / V->height;
+	v3 heading = unit(add(add(J->forward, scl(J->right, u * J->reach * J->aspect)), scl(J->up, v * J->reach)));
+	kp_ray ray = ray_of(J->eye, heading, INFINITY, NO_MATERIAL);
+	v3 from = J->eye;
+	spec T = flat(1), R = flat(0);
+	double drawn = 0;
+	int camera = 1, dispersed = 0;
+	uint32_t medium = NO_MATERIAL;
+	for (int depth = 0;; ++depth) {
+		kp_hit hit;
+		kp_tracer_trace(tracer, &ray, &hit);
+		const v3 origin = mk(ray.origin[0], ray.origin[1], ray.origin[2]);
+		heading = mk(ray.direction[0], ray.direction[1], ray.direction[2]);
+		const int found = hit.kind != 0;
+		if (!camera) {
+			const double limit = found ? hit.distance : INFINITY;
+			for (uint32_t k = 0; k < V->lamp_count; ++k) {
+				double reach;
+				if (!meet_lamp(&J->lamps[k], origin, heading, limit, &reach)) continue;
+				double wgt = 1;
+				if (drawn > 0) {
+					const double pa = aim_density(&J->lamps[k], from, heading, reach);
+					wgt = drawn * drawn / (drawn * drawn + pa * pa);
+				}
+				R = sadd(R, sscale(smul(T, spectrum(J->lamps[k].radiance, &w)), wgt));
+			}
+		}
+		if (!found) {
+			double sky[3];
+			sky_colour(V, heading, sky);
+			R = sadd(R, smul(T, spectrum(sky, &w)));
+			break;
+		}
+		const uint32_t material = hit.leaf != 0xFFFFFFFFu ? J->leaf_material[hit.leaf] : 0;
+		const kp_material* m = &J->materials[material < V->material_count ? material : 0];
+		const v3 point = mk(hit.point[0], hit.point[1], hit.point[2]);
+		v3 normal = mk(hit.normal[0], hit.normal[1], hit.normal[2]);
+		if (dotv(normal, heading) >= 0) normal = scl(normal, -1);
+		const double lift = BIAS + 2 * 1e-6;
+		const int capped = depth + 1 >= V->surfaces;
+		const v3 out = scl(heading, -1);
+		const shading s = shading_of(m, J->materials, normal, out, &w, medium);
+		if (!m->exact && V->lamp_count > 0) {
+			const double u0 = number(stream, index, depth, LIGHT_U), v0 = number(stream, index, depth, LIGHT_V);
+			double choice = number(stream, index, depth, PICK);
+			double total = 0, picked = 0, chosen_dist = 0;
+			spec chosen = flat(0);
+			v3 chosen_dir = mk(0, 0, 1);
+			for (uint32_t k = 0; k < V->lamp_count; ++k) {
+				const aim a = aim_lamp(&J->lamps[k], point, u0, v0);
+				if (!a.found) continue;
+				const double facing = dotv(normal, a.toward);
+				if (facing <= 0 || a.distance <= 0) continue;
+				const response f = respond(&s, out, a.toward, &w);
+				double wgt = 1;
+				if (a.density > 0) {
+					const double pm = capped ? 0 : f.density;
+					wgt = a.density * a.density / (a.density * a.density + pm * pm);
+				}
+				const spec offer = sscale(smul(smul(T, f.value), spectrum(a.arriving, &w)), facing * wgt);
+				const double weight = smean(offer);
+				if (!(weight > 0)) continue;
+				total += weight;
+				const double keep = weight / total;
+				if (choice < keep) {
+					chosen = offer;
+					picked = weight;
+					chosen_dir = a.toward;
+					chosen_dist = a.distance;
+					choice = choice / keep;
+				} else {
+					choice = (choice - keep) / (1 - keep);
+				}
+			}
+			if (picked > 0) {
+				const kp_ray line = ray_of(add(point, scl(normal, lift)), chosen_dir, chosen_dist - lift, NO_MATERIAL);
+				kp_hit blocked;
+				kp_tracer_trace(tracer, &line, &blocked);
+				if (blocked.kind == 0) R = sadd(R, sscale(chosen, total / picked));
+			}
+		}
+		if (capped) break;
+		const scatter sc = sample(&s, out, &w, number(stream, index, depth, LOBE), number(stream, index, depth, SIDE), number(stream, index, depth, DIRECTION_U), number(stream, index, depth, DIRECTION_V), material, medium);
+		const double side_of = dotv(sc.incoming, normal);
+		const int below = sc.through ? side_of >= 0 : side_of <= 0;
+		if (!sc.found || below) break;
+		spec carried = smul(T, sc.weight);
+		if (sc.dispersed && !dispersed) {
+			carried.v[0] *= 4;
+			carried.v[1] = carried.v[2] = carried.v[3] = 0;
+			dispersed = 1;
+		}
+		if (depth >= 4) {
+			const double survival = mind(0.95, smax(carried));
+			if (!(number(stream, index, depth, SURVIVAL) < survival)) break;
+			carried = sscale(carried, 1 / survival);
+		}
+		if (sc.through) medium = sc.medium_after;
+		T = carried;
+		drawn = sc.delta ? 0 : sc.density;
+		camera = 0;
+		from = point;
+		ray = ray_of(add(point, scl(normal, side_of > 0 ? lift : -lift)), sc.incoming, INFINITY, medium);
+	}
+	kp_colour_of(w.nm, w.density, R.v, rgb);
+}
+
+static void* worker(void* arg) {
+	job* J = (job*) arg;
+	kp_tracer* tracer = kp_tracer_new(J->tree, J->leaf_material);
+	for (;;) {
+		pthread_mutex_lock(&J->lock);
+		const int row = J->next++;
+		pthread_mutex_unlock(&J->lock);
+		if (row >= J->rows) break;
+		const int y = J->row0 + row;
+		for (int x = 0; x < J->view->width; ++x) {
+			double sum[3] = { 0, 0, 0 };
+			for (int k = 0; k < J->view->spp; ++k) {
+				double rgb[3];
+				sample_pixel(J, tracer, x, y, (uint32_t) k, rgb);
+				for (int c = 0; c < 3; ++c) sum[c] += rgb[c];
+			}
+			double* out = J->sums + 3 * ((size_t) row * (size_t) J->view->width + (size_t) x);
+			for (int c = 0; c < 3; ++c) out[c] = sum[c];
+		}
+	}
+	kp_tracer_free(tracer);
+	return NULL;
+}
+
+void kp_render_band(const kp_octree* tree, const uint32_t* leaf_material, const kp_material* materials, const kp_lamp* lamps, const kp_view* view,
+                    int row0, int rows, int threads, double* sums) {
+	job J;
+	memset(&J, 0, sizeof J);
+	J.tree = tree;
+	J.leaf_material = leaf_material;
+	J.materials = materials;
+	for (uint32_t k = 0; k < view->lamp_count && k < 16; ++k) J.lamps[k] = lamp_of(&lamps[k]);
+	J.view = view;
+	J.row0 = row0;
+	J.rows = rows;
+	J.sums = sums;
+	pthread_mutex_init(&J.lock, NULL);
+	/* core/camera.cpp:9 lensOf */
+	J.eye = vd(view->eye);
+	J.forward = unit(sub(vd(view->target), J.eye));
+	J.right = unit(crossv(J.forward, vd(view->up)));
+	J.up = crossv(J.right, J.forward);
+	J.reach = tan(view->fov / 2);
+	J.aspect = (double) view->width / (double) view->height;
+	J.seed_mix = kp_mixed_bits((uint64_t) (int64_t) view->seed);
+	if (threads < 1) threads = 1;
+	pthread_t* pool = (pthread_t*) malloc(sizeof(pthread_t) * (size_t) threads);
+	for (int t = 0; t < threads; ++t) pthread_create(&pool[t], NULL, worker, &J);
+	for (int t = 0; t < threads; ++t) pthread_join(pool[t], NULL);
+	free(pool);
+	pthread_mutex_destroy(&J.lock);
+}

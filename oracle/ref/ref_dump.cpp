@@ -14,6 +14,7 @@
 #include "plugins/geometry/sphere_trace/sphere_trace.h"
 #include "plugins/geometry/tree/build.h"
 #include "plugins/geometry/tree/cut.h"
+#include "plugins/transport/paths/material/material.h"
 #include "sdf/program.h"
 #include "sdf/scene.h"
 #include "syntax/evaluator.h"
@@ -96,6 +97,19 @@ int dumpScene(const char* sdf, const char* out) {
 		std::fprintf(f, ",\"radius\":%.9g,\"angle\":%.9g,\"power\":", double(l.radius), double(l.angle));
 		putColour(f, l.power);
 		std::fprintf(f, "}");
+	}
+	// plugins/transport/paths/material/material.cpp:287 materialsOf: the finish
+	// each material is drawn with, its escape table included
+	const Materials made = materialsOf(file.looks, SmoothGlass::Exact);
+	std::fprintf(f, "],\n\"finishes\":[");
+	for (std::size_t i = 0; i < made.finishes.size(); ++i) {
+		const Finish& fin = made.finishes[i];
+		std::fprintf(f, "%s{\"kind\":%d,\"width\":%.17g,\"sharp\":%d,\"facetShare\":%.17g,\"body\":%.17g,\"coating\":[%.17g,%.17g,%.17g],\"index\":%.17g,\"losesMuch\":%d,\"exact\":%d,\"film\":[%.17g,%.17g],\"escapeAverage\":%.17g,\"escape\":[",
+		             i ? ",\n" : "", int(fin.kind), fin.width, int(fin.sharp), fin.facetShare, fin.body, fin.coating.front, fin.coating.twice, fin.coating.room, fin.index, int(fin.losesMuch), int(fin.exact), fin.film.thickness, fin.film.index, fin.escape.average);
+		for (int k = 0; k < energyViews; ++k) {
+			std::fprintf(f, "%s%.17g", k ? "," : "", fin.escape.table[std::size_t(k)]);
+		}
+		std::fprintf(f, "]}");
 	}
 	const Sky& sky = file.lighting.sky;
 	std::fprintf(f, "],\n\"sky\":{\"kind\":%d,\"zenith\":", int(sky.kind));

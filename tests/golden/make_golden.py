@@ -36,7 +36,7 @@ REFERENCE_FLAGS = ["--threads", "8", "--use", "stopping=fixed_count", "--use", "
                    "--use", "build=none", "--use", "strategy=none", "--use", "sampler=none", "--use", "observer=none"]
 
 # name -> (seeds, spp per seed) of the reference frames kept as image fixtures
-IMAGES = {"room_small": (12, 64), "c1_small": (12, 64)}
+IMAGES = {"room_small": (12, 64), "c1_small": (12, 64), "c2_small": (12, 64)}
 
 # name -> (generator, kwargs, trace rays, cut depth)
 SCENES = {
@@ -45,6 +45,7 @@ SCENES = {
     "room": (scenegen.scene_room, dict(seed=1), 0, 0),
     "room_small": (scenegen.scene_room, dict(seed=3, width=48, height=48, samples=64, count=8), 0, 0),
     "c2": (scenegen.scene_config2, dict(seed=1), 200, 3),
+    "c2_small": (scenegen.scene_config2, dict(seed=3, width=64, height=36, samples=64, groups=24), 0, 0),
 }
 
 
