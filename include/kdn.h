@@ -231,6 +231,38 @@ kdn_status kdn_render(kdn_ctx* ctx, const kdn_frame* frame, float* out_rgb);
 kdn_status kdn_render_device(kdn_ctx* ctx, const kdn_frame* frame, float* out_rgb, void* stream);
 kdn_status kdn_frame_stats_get(kdn_ctx* ctx, kdn_frame_stats* stats);
 
+/* One frame of the denoiser's feature buffers: the frame size, whether the
+ * light is already divided by the albedo (TemporalState::demodulated), and
+ * the camera the frame was drawn with (core/camera.h Lens: eye, forward,
+ * right, up, reach = tan(fov / 2), aspect = width / height). */
+typedef struct kdn_denoise_frame {
+	int32_t width, height;
+	uint32_t demodulated;
+	uint32_t pad_;
+	double eye[3], forward[3], right[3], up[3];
+	double reach, aspect;
+} kdn_denoise_frame;
+
+/*
+ * The SVGF-like a-trous denoiser (plugins/reconstruction/atrous/atrous.cpp:513
+ * denoisedFrame) over one frame's feature buffers, a pixel each, row-major:
+ *   colour   float x3   the temporal light (TemporalPixel::colour)
+ *   moment   float      its second moment of luminance
+ *   length   float      the history length in samples
+ *   distance FP16       camera distance of the first surface (inf or 0: sky)
+ *   normal   FP16 x3    its normal
+ *   albedo   FP16 x3    its albedo
+ *   leaf     uint32     its leaf, 0xFFFFFFFF for the sky
+ * out gets RGB float x3.  kdn_denoise takes host arrays (copied in and out
+ * on the context's stream); kdn_denoise_device takes device arrays.  The
+ * context keeps 68 bytes a pixel of scratch between calls.
+ */
+kdn_status kdn_denoise(kdn_ctx* ctx, const kdn_denoise_frame* frame, const float* colour, const float* moment, const float* length,
+                       const uint16_t* distance, const uint16_t* normal, const uint16_t* albedo, const uint32_t* leaf, float* out_rgb);
+kdn_status kdn_denoise_device(kdn_ctx* ctx, const kdn_denoise_frame* frame, const float* colour, const float* moment, const float* length,
+                              const uint16_t* distance, const uint16_t* normal, const uint16_t* albedo, const uint32_t* leaf, float* out_rgb,
+                              void* stream);
+
 /* Write a buffer larger than the L2 cache on the context's stream, so that
  * the next launch starts with a cold cache. */
 kdn_status kdn_flush_l2(kdn_ctx* ctx);

@@ -73,7 +73,14 @@ class KdnError(RuntimeError):
 EXPORTS = [
     "kdn_status_string", "kdn_last_error", "kdn_open", "kdn_close", "kdn_upload_block", "kdn_build", "kdn_world_stats",
     "kdn_world_cell", "kdn_extend", "kdn_extend_device", "kdn_render", "kdn_render_device", "kdn_frame_stats_get", "kdn_flush_l2",
+    "kdn_denoise", "kdn_denoise_device",
 ]
+
+
+class DenoiseFrame(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("demodulated", ctypes.c_uint32), ("pad", ctypes.c_uint32),
+                ("eye", ctypes.c_double * 3), ("forward", ctypes.c_double * 3), ("right", ctypes.c_double * 3), ("up", ctypes.c_double * 3),
+                ("reach", ctypes.c_double), ("aspect", ctypes.c_double)]
 
 _lib = None
 
@@ -104,6 +111,8 @@ def library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.kdn_render_device.argtypes = [P, ctypes.POINTER(Frame), P, P]
     L.kdn_frame_stats_get.argtypes = [P, ctypes.POINTER(FrameStats)]
     L.kdn_flush_l2.argtypes = [P]
+    L.kdn_denoise.argtypes = [P, ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P]
+    L.kdn_denoise_device.argtypes = [P, ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P, P]
     for name in EXPORTS:
         fn = getattr(L, name)
         if name not in ("kdn_status_string", "kdn_last_error"):
@@ -264,3 +273,19 @@ class Backend:
 
     def flush_l2(self) -> None:
         self._check(self.lib.kdn_flush_l2(self.handle))
+
+    def denoise(self, width: int, height: int, demodulated: bool, lens, colour, moment, length, distance, normal, albedo, leaf) -> np.ndarray:
+        """The a-trous denoiser over host feature buffers (include/kdn.h
+        kdn_denoise).  lens: eye, forward, right, up (3 each), reach,
+        aspect.  distance, normal and albedo are stored as FP16."""
+        f = DenoiseFrame(width, height, 1 if demodulated else 0, 0)
+        lens = np.asarray(lens, np.float64)
+        for k in range(3):
+            f.eye[k], f.forward[k], f.right[k], f.up[k] = lens[k], lens[3 + k], lens[6 + k], lens[9 + k]
+        f.reach, f.aspect = float(lens[12]), float(lens[13])
+        arrs = [np.ascontiguousarray(colour, np.float32), np.ascontiguousarray(moment, np.float32), np.ascontiguousarray(length, np.float32),
+                np.ascontiguousarray(distance, np.float16), np.ascontiguousarray(normal, np.float16), np.ascontiguousarray(albedo, np.float16),
+                np.ascontiguousarray(leaf, np.uint32)]
+        out = np.zeros((width * height, 3), np.float32)
+        self._check(self.lib.kdn_denoise(self.handle, ctypes.byref(f), *[_ptr(a) for a in arrs], _ptr(out)))
+        return out

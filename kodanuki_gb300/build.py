@@ -17,6 +17,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libkdn_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+EXACT_FLOAT = {"denoise.cu"}
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc")
 
 
@@ -28,7 +29,9 @@ def _compile(src: str, verbose: bool) -> str:
     obj = os.path.join(OUT, os.path.basename(src) + ".o")
     common = ["-O3", "-std=c++17", "-I", INCLUDE, "-I", CSRC, "-Xcompiler", "-fPIC,-ffp-contract=off", "--expt-relaxed-constexpr"]
     if src.endswith(".cu"):
-        cmd = [NVCC] + ARCH + ["-lineinfo"] + common + (["-Xptxas", "-v"] if verbose else []) + ["-c", src, "-o", obj]
+        # the denoiser keeps the reference's float order: no FMA contraction there
+        exact = ["-fmad=false"] if os.path.basename(src) in EXACT_FLOAT else []
+        cmd = [NVCC] + ARCH + ["-lineinfo"] + common + exact + (["-Xptxas", "-v"] if verbose else []) + ["-c", src, "-o", obj]
     else:
         cmd = [NVCC] + common + ["-x", "c++", "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -27,7 +27,7 @@ void Context::release() {
 	cudaSetDevice(device);
 	if (stream) cudaStreamSynchronize(stream);
 	releaseFrame();
-	for (DeviceBuffer* b : { &nodes, &leaves, &programs, &steps, &ssa, &leafMaterial, &objectMaterial, &extendRays, &extendHits, &extendStates, &counters, &l2 }) freeBuffer(*b);
+	for (DeviceBuffer* b : { &nodes, &leaves, &programs, &steps, &ssa, &leafMaterial, &objectMaterial, &extendRays, &extendHits, &extendStates, &counters, &l2, &denoiseScratch, &denoiseIo }) freeBuffer(*b);
 	if (stream) cudaStreamDestroy(stream);
 	stream = nullptr;
 }

@@ -38,6 +38,7 @@ struct Context {
 	DeviceWorld world {};
 	DeviceBuffer nodes, leaves, programs, steps, ssa, leafMaterial, objectMaterial;
 	DeviceBuffer extendRays, extendHits, extendStates, counters, l2;
+	DeviceBuffer denoiseScratch, denoiseIo;
 	FrameState* frame = nullptr;
 
 	kdn_status open();

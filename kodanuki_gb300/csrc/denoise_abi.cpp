@@ -1,0 +1,123 @@
+// kdn_denoise / kdn_denoise_device: the denoiser's entry points.
+#include "context.h"
+#include "denoise.h"
+
+#include <cstring>
+
+using kdn::Context;
+
+namespace {
+
+constexpr int64_t kMostPixels = int64_t(1) << 26;
+
+kdn_status checkFrame(Context* ctx, const kdn_denoise_frame* f) {
+	if (f->width <= 0 || f->height <= 0 || int64_t(f->width) * int64_t(f->height) > kMostPixels) return ctx->fail(KDN_BAD_ARG, "kdn_denoise: frame size out of range");
+	if (!(f->reach > 0) || !(f->aspect > 0)) return ctx->fail(KDN_BAD_ARG, "kdn_denoise: the lens needs a positive reach and aspect");
+	return KDN_OK;
+}
+
+void lensOf(const kdn_denoise_frame* f, double lens[14]) {
+	for (int k = 0; k < 3; ++k) {
+		lens[k]     = f->eye[k];
+		lens[3 + k] = f->forward[k];
+		lens[6 + k] = f->right[k];
+		lens[9 + k] = f->up[k];
+	}
+	lens[12] = f->reach;
+	lens[13] = f->aspect;
+}
+
+// The context's scratch for n pixels, carved from one allocation.
+kdn_status scratch(Context* ctx, size_t n, kdn::DenoiseArgs& a) {
+	const kdn_status s = ctx->ensure(ctx->denoiseScratch, n * kdn::kDenoiseScratchPerPixel + 16 * sizeof(double));
+	if (s != KDN_OK) return s;
+	char* base = static_cast<char*>(ctx->denoiseScratch.ptr);
+	a.lens     = reinterpret_cast<const double*>(base);
+	base += 16 * sizeof(double);
+	a.guideA = reinterpret_cast<float4*>(base);
+	a.guideB = a.guideA + n;
+	a.lightA = a.guideB + n;
+	a.lightB = a.lightA + n;
+	a.sky    = reinterpret_cast<float*>(a.lightB + n);
+	return KDN_OK;
+}
+
+kdn_status run(Context* ctx, const kdn_denoise_frame* f, kdn::DenoiseArgs& a, cudaStream_t stream) {
+	double lens[14];
+	lensOf(f, lens);
+	if (!ctx->check(cudaMemcpyAsync(const_cast<double*>(a.lens), lens, sizeof(lens), cudaMemcpyHostToDevice, stream), "kdn_denoise lens")) return KDN_CUDA_ERROR;
+	a.width       = f->width;
+	a.height      = f->height;
+	a.demodulated = f->demodulated ? 1 : 0;
+	if (!ctx->check(kdn::launchDenoise(a, stream), "denoise kernels")) return KDN_CUDA_ERROR;
+	return KDN_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+kdn_status kdn_denoise_device(kdn_ctx* handle, const kdn_denoise_frame* frame, const float* colour, const float* moment, const float* length,
+                              const uint16_t* distance, const uint16_t* normal, const uint16_t* albedo, const uint32_t* leaf, float* out, void* stream) {
+	if (handle == nullptr || frame == nullptr || !colour || !moment || !length || !distance || !normal || !albedo || !leaf || !out) return KDN_BAD_ARG;
+	Context* ctx = reinterpret_cast<Context*>(handle);
+	std::lock_guard<std::mutex> guard(ctx->lock);
+	if (ctx->device < 0) return ctx->fail(KDN_NO_DEVICE, "kdn_denoise_device: a host-only context has no device");
+	kdn_status s = checkFrame(ctx, frame);
+	if (s != KDN_OK) return s;
+	if (!ctx->check(cudaSetDevice(ctx->device), "cudaSetDevice")) return KDN_CUDA_ERROR;
+	const size_t n = size_t(frame->width) * size_t(frame->height);
+	kdn::DenoiseArgs a {};
+	if ((s = scratch(ctx, n, a)) != KDN_OK) return s;
+	a.colour   = colour;
+	a.moment   = moment;
+	a.length   = length;
+	a.distance = distance;
+	a.normal   = normal;
+	a.albedo   = albedo;
+	a.leaf     = leaf;
+	a.out      = out;
+	return run(ctx, frame, a, stream ? static_cast<cudaStream_t>(stream) : ctx->stream);
+}
+
+kdn_status kdn_denoise(kdn_ctx* handle, const kdn_denoise_frame* frame, const float* colour, const float* moment, const float* length,
+                       const uint16_t* distance, const uint16_t* normal, const uint16_t* albedo, const uint32_t* leaf, float* out) {
+	if (handle == nullptr || frame == nullptr || !colour || !moment || !length || !distance || !normal || !albedo || !leaf || !out) return KDN_BAD_ARG;
+	Context* ctx = reinterpret_cast<Context*>(handle);
+	std::lock_guard<std::mutex> guard(ctx->lock);
+	if (ctx->device < 0) return ctx->fail(KDN_NO_DEVICE, "kdn_denoise: a host-only context has no device");
+	kdn_status s = checkFrame(ctx, frame);
+	if (s != KDN_OK) return s;
+	if (!ctx->check(cudaSetDevice(ctx->device), "cudaSetDevice")) return KDN_CUDA_ERROR;
+	const size_t n = size_t(frame->width) * size_t(frame->height);
+	// inputs and output, one device allocation reused between calls
+	const size_t bytes[] = { n * 12, n * 4, n * 4, n * 2, n * 6, n * 6, n * 4, n * 12 };
+	size_t total         = 0;
+	size_t offsets[8];
+	for (int k = 0; k < 8; ++k) {
+		offsets[k] = total;
+		total += (bytes[k] + 255) & ~size_t(255);
+	}
+	if ((s = ctx->ensure(ctx->denoiseIo, total)) != KDN_OK) return s;
+	char* base          = static_cast<char*>(ctx->denoiseIo.ptr);
+	const void* hosts[] = { colour, moment, length, distance, normal, albedo, leaf };
+	for (int k = 0; k < 7; ++k) {
+		if (!ctx->check(cudaMemcpyAsync(base + offsets[k], hosts[k], bytes[k], cudaMemcpyHostToDevice, ctx->stream), "kdn_denoise copy in")) return KDN_CUDA_ERROR;
+	}
+	kdn::DenoiseArgs a {};
+	if ((s = scratch(ctx, n, a)) != KDN_OK) return s;
+	a.colour   = reinterpret_cast<const float*>(base + offsets[0]);
+	a.moment   = reinterpret_cast<const float*>(base + offsets[1]);
+	a.length   = reinterpret_cast<const float*>(base + offsets[2]);
+	a.distance = reinterpret_cast<const uint16_t*>(base + offsets[3]);
+	a.normal   = reinterpret_cast<const uint16_t*>(base + offsets[4]);
+	a.albedo   = reinterpret_cast<const uint16_t*>(base + offsets[5]);
+	a.leaf     = reinterpret_cast<const uint32_t*>(base + offsets[6]);
+	a.out      = reinterpret_cast<float*>(base + offsets[7]);
+	if ((s = run(ctx, frame, a, ctx->stream)) != KDN_OK) return s;
+	if (!ctx->check(cudaMemcpyAsync(out, a.out, bytes[7], cudaMemcpyDeviceToHost, ctx->stream), "kdn_denoise copy out")) return KDN_CUDA_ERROR;
+	if (!ctx->check(cudaStreamSynchronize(ctx->stream), "kdn_denoise")) return KDN_CUDA_ERROR;
+	return KDN_OK;
+}
+
+} // extern "C"

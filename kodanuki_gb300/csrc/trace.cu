@@ -93,7 +93,10 @@ __device__ __forceinline__ Field fieldAt(const DeviceWorld& w, const float o[3],
 	f.least  = 3.0e38f;
 	f.nearest = 3.0e38f;
 	f.index  = 0;
-	f.exit   = f.empty ? cellExit(o, inv, l) : 0.0f;
+	// A cell keeps only the objects whose surface may pass through it
+	// (cut.cpp:442 deciding), so past its walls its field is no distance
+	// bound: a step stops where the ray leaves the cell.
+	f.exit   = cellExit(o, inv, l);
 	if (f.empty) return f;
 	for (uint32_t k = 0; k < leaf.count; ++k) {
 		const GpuProgram g = w.programs[leaf.first + k];
@@ -173,7 +176,7 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 						h = { 1, t, f.first, winnerAt(w, o, d, t, f, slots, stride), step + 1 };
 						break;
 					}
-					t += f.least;
+					t = fminf(t + f.least, fmaxf(f.exit, t) + nudge(t));
 					continue;
 				}
 				// sphereFromInside: stand on the nearest surface and read the field past it.
@@ -194,7 +197,7 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 					t += inset;
 					continue;
 				}
-				t += f.nearest;
+				t = fminf(t + f.nearest, fmaxf(f.exit, t) + nudge(t));
 			}
 		}
 		marchSteps += step;

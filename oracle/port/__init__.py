@@ -226,3 +226,14 @@ def render_band(scene, width: int, height: int, spp: int, surfaces: int, seed: i
     L.kp_render_band.argtypes = [_P, _P, _P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]
     L.kp_render_band(tree.handle, _ptr(mat_leaf), ctypes.addressof(mats), ctypes.addressof(lamps), ctypes.byref(v), row0, rows, threads, _ptr(sums))
     return sums
+
+
+def denoise(width: int, height: int, demodulated: int, lens, colour, moment, length, distance, normal, leaf, albedo) -> np.ndarray:
+    """The oracle's a-trous denoiser over one frame's feature buffers."""
+    L = lib()
+    L.kp_denoise.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P, _P, _P, _P, _P, _P, _P, _P]
+    arrs = [np.ascontiguousarray(a, t) for a, t in ((lens, np.float64), (colour, np.float64), (moment, np.float64), (length, np.float32),
+                                                     (distance, np.float32), (normal, np.float64), (leaf, np.uint32), (albedo, np.float64))]
+    out = np.zeros((width * height, 3), np.float32)
+    L.kp_denoise(width, height, demodulated, *[_ptr(a) for a in arrs], _ptr(out))
+    return out

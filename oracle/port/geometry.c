@@ -804,6 +804,7 @@ static double box_exit(const kp_ray* ray, const double lo[3], const double hi[3]
 static void candidates(const kp_octree* tree, const kp_program* programs, uint32_t count, const kp_ray* ray, const double p[3], cand_list* out, kp_program* storage) {
 	out->n = 0;
 	out->empty = 0;
+	out->exit_t = INFINITY;
 	if (!tree) {
 		for (uint32_t i = 0; i < count && i < 4096; ++i) {
 			out->progs[out->n] = &programs[i];
@@ -831,9 +832,12 @@ static void candidates(const kp_octree* tree, const kp_program* programs, uint32
 		node = (uint64_t) tree->first_child[node] + (uint64_t) o;
 	}
 	const cell_rec* c = &tree->cells[node];
+	/* A cell keeps only the objects whose surface may pass through it
+	 * (cut.cpp:442 deciding), so past its walls its field is no distance
+	 * bound: a step stops where the ray leaves the cell. */
+	out->exit_t = box_exit(ray, lo, hi);
 	if (c->occupancy == KP_EMPTY) {
 		out->empty = 1;
-		out->exit_t = box_exit(ray, lo, hi);
 		return;
 	}
 	for (uint32_t i = 0; i < c->nprog && i < 4096; ++i) {
@@ -970,7 +974,7 @@ static void trace_one(march* m, const double lower[3], const double size[3], kp_
 				landed(m, values, m->cand->n, t, hit);
 				return;
 			}
-			t += least;
+			t = dmin(t + least, dmax(m->cand->exit_t, t) + SPHERE_TOL);
 			continue;
 		}
 		/* sphereFromInside (sphere_trace.cpp:188) */
@@ -998,7 +1002,7 @@ static void trace_one(march* m, const double lower[3], const double size[3], kp_
 				return;
 			}
 		}
-		t += nearest < SPHERE_TOL ? SPHERE_INSET : nearest;
+		t = nearest < SPHERE_TOL ? t + SPHERE_INSET : dmin(t + nearest, dmax(m->cand->exit_t, t) + SPHERE_TOL);
 	}
 	missed(hit);
 }

@@ -146,6 +146,13 @@ typedef struct kp_view {
 void kp_render_band(const kp_octree* tree, const uint32_t* leaf_material, const kp_material* materials, const kp_lamp* lamps, const kp_view* view,
                     int row0, int rows, int threads, double* sums);
 
+/* ---- denoiser (plugins/reconstruction/atrous/atrous.cpp:513 denoisedFrame) ----
+ * lens: eye[3], forward[3], right[3], up[3], reach, aspect.  Per pixel:
+ * colour[3], moment, length, distance, normal[3], leaf, albedo[3] (the
+ * reference's TemporalPixel); out: RGB. */
+void kp_denoise(int width, int height, int demodulated, const double lens[14], const double* colour, const double* moment, const float* length,
+                const float* distance, const double* normal, const uint32_t* leaf, const double* albedo, float* out);
+
 /* ---- numbers, wavelengths and colour (math/random.cpp, math/colour.cpp) ---- */
 uint64_t kp_mixed_bits(uint64_t v);
 double kp_unit_of(uint64_t bits);

@@ -14,6 +14,7 @@
 #include "plugins/geometry/sphere_trace/sphere_trace.h"
 #include "plugins/geometry/tree/build.h"
 #include "plugins/geometry/tree/cut.h"
+#include "plugins/reconstruction/atrous/atrous.h"
 #include "plugins/transport/paths/material/material.h"
 #include "sdf/program.h"
 #include "sdf/scene.h"
@@ -216,9 +217,81 @@ int dumpCut(const char* sdf, int depth, const char* outPath) {
 	return 0;
 }
 
+// Feature buffers in, the reference's denoised frame out
+// (plugins/reconstruction/atrous/atrous.cpp:513 denoisedFrame).  Input: int32
+// width, height, demodulated; doubles eye[3], forward[3], right[3], up[3],
+// reach, aspect; then per pixel colour[3] f64, moment f64, length f32,
+// distance f32, normal[3] f64, leaf u32, albedo[3] f64.  Output: RGB f32.
+int dumpDenoise(const char* inPath, const char* outPath) {
+	FILE* in = std::fopen(inPath, "rb");
+	std::int32_t head[3];
+	double lensValues[14];
+	if (std::fread(head, 4, 3, in) != 3 || std::fread(lensValues, 8, 14, in) != 14) return 1;
+	TemporalState temporal = emptyTemporal();
+	temporal.width         = head[0];
+	temporal.height        = head[1];
+	temporal.demodulated   = head[2] != 0;
+	for (int k = 0; k < head[0] * head[1]; ++k) {
+		double colour[3], moment, normal[3], albedo[3];
+		float length, distance;
+		std::uint32_t leaf;
+		if (std::fread(colour, 8, 3, in) != 3 || std::fread(&moment, 8, 1, in) != 1 || std::fread(&length, 4, 1, in) != 1 || std::fread(&distance, 4, 1, in) != 1 ||
+		    std::fread(normal, 8, 3, in) != 3 || std::fread(&leaf, 4, 1, in) != 1 || std::fread(albedo, 8, 3, in) != 3) {
+			return 1;
+		}
+		temporal.pixels.push_back(TemporalPixel {
+			.colour   = { colour[0], colour[1], colour[2] },
+			.moment   = moment,
+			.length   = length,
+			.distance = distance,
+			.normal   = { normal[0], normal[1], normal[2] },
+			.leaf     = leaf,
+			.albedo   = { albedo[0], albedo[1], albedo[2] },
+		});
+	}
+	std::fclose(in);
+	const Lens lens = {
+		.eye      = { lensValues[0], lensValues[1], lensValues[2] },
+		.forward  = { lensValues[3], lensValues[4], lensValues[5] },
+		.right    = { lensValues[6], lensValues[7], lensValues[8] },
+		.up       = { lensValues[9], lensValues[10], lensValues[11] },
+		.reach    = lensValues[12],
+		.aspect   = lensValues[13],
+		.aperture = 0,
+		.focus    = 10,
+		.width    = head[0],
+		.height   = head[1],
+	};
+	static const FrameRecord record = emptyFrameRecord();
+	static const std::vector<PixelSum> estimates;
+	const ShownFrame frame = {
+		.width     = head[0],
+		.height    = head[1],
+		.lens      = lens,
+		.before    = lens,
+		.film      = { .factor = 1, .phase = 0 },
+		.moved     = false,
+		.restarted = false,
+		.recounted = false,
+		.still     = 1,
+		.record    = record,
+		.estimates = estimates,
+		.surfaces  = noSurfaces(),
+		.threads   = 4,
+	};
+	const Denoised denoised = denoisedFrame(emptyDenoise(), temporal, frame);
+	FILE* out               = std::fopen(outPath, "wb");
+	std::fwrite(denoised.image.rgb.data(), 4, denoised.image.rgb.size(), out);
+	std::fclose(out);
+	return 0;
+}
+
 } // namespace
 
 int main(int argc, char** argv) {
+	if (argc >= 4 && std::strcmp(argv[1], "denoise") == 0) {
+		return dumpDenoise(argv[2], argv[3]);
+	}
 	if (argc >= 4 && std::strcmp(argv[1], "scene") == 0) {
 		return dumpScene(argv[2], argv[3]);
 	}

@@ -143,6 +143,86 @@ def reference_images(render: str, sdf: str, name: str, tmp: str) -> None:
     print(" image", f.shape, "mean", f.mean(axis=(0, 1, 2)))
 
 
+def denoise_fields(width: int = 64, height: int = 48):
+    """Seeded feature buffers in the manner of the reference's own denoiser
+    checks (target/tests/denoise.cpp: a noisy plane, depth and tilt edges, a
+    checker albedo, young history) plus a random mix with sky pixels.  The
+    distance, normal and albedo are rounded to FP16, the storage the GPU
+    keeps them in, so both denoisers read identical features."""
+    rng = np.random.default_rng(99)
+    aspect = width / height
+    reach = 0.5
+    lens = np.array([0, 0, 0, 0, 0, -1, 1, 0, 0, 0, 1, 0, reach, aspect], np.float64)
+    xs, ys = np.meshgrid(np.arange(width), np.arange(height))
+    across = (2 * (xs + 0.5) / width - 1) * reach * aspect
+    down = (1 - 2 * (ys + 0.5) / height) * reach
+    ray = np.sqrt(1 + across ** 2 + down ** 2)
+    fields = {}
+
+    def field(value, length=8.0, depth=10.0, normal=(0, 0, 1), albedo=(0, 0, 0), leaf=1, demodulated=0, extra=0.0):
+        n = width * height
+        colour = np.broadcast_to(np.asarray(value, np.float64).reshape(height, width, -1), (height, width, 3)).reshape(n, 3).copy()
+        lum = 0.2126 * colour[:, 0] + 0.7152 * colour[:, 1] + 0.0722 * colour[:, 2]
+        moment = lum * lum + np.broadcast_to(np.asarray(extra, np.float64), (height, width)).reshape(n)
+        dist = (np.broadcast_to(np.asarray(depth, np.float64), (height, width)) * ray).reshape(n).astype(np.float16).astype(np.float32)
+        nrm = np.broadcast_to(np.asarray(normal, np.float64).reshape(-1, 3) if np.ndim(normal) == 1 else np.asarray(normal), (n, 3)).astype(np.float16).astype(np.float64)
+        alb = np.broadcast_to(np.asarray(albedo, np.float64).reshape(-1, 3) if np.ndim(albedo) == 1 else np.asarray(albedo), (n, 3)).astype(np.float16).astype(np.float64)
+        return dict(colour=colour, moment=moment, length=np.broadcast_to(np.asarray(length, np.float32), (height, width)).reshape(n).copy(),
+                    distance=dist, normal=nrm.copy(), leaf=np.broadcast_to(np.asarray(leaf, np.uint32), (height, width)).reshape(n).copy(),
+                    albedo=alb.copy(), demodulated=demodulated)
+
+    noise = rng.uniform(-1, 1, (height, width))
+    v = 0.5 + 0.3 * noise
+    fields["plane"] = field(np.stack([v, v, v], -1), extra=0.01)
+    right = xs >= width // 2
+    v = np.where(right, 0.6, 0.4) + 0.3 * rng.uniform(-1, 1, (height, width))
+    fields["depth_edge"] = field(np.stack([v, v, v], -1), depth=np.where(right, 12.0, 10.0), extra=0.02)
+    tilt = np.where(right[..., None], np.array([0.8, 0, 0.6]), np.array([0, 0, 1.0])).reshape(-1, 3)
+    fields["tilt_edge"] = field(np.stack([v, v, v], -1), normal=tilt, extra=0.02)
+    checker = np.where(((xs // 4 + ys // 4) % 2) == 0, 0.2, 0.8)
+    lit = 0.7 + 0.2 * rng.uniform(-1, 1, (height, width))
+    alb = np.stack([checker, checker, checker], -1).reshape(-1, 3)
+    fields["checker"] = field(np.stack([lit * checker] * 3, -1), albedo=alb, demodulated=1, extra=0.005)
+    young = rng.integers(1, 6, (height, width)).astype(np.float32)
+    v = 0.5 + 0.3 * rng.uniform(-1, 1, (height, width))
+    fields["young"] = field(np.stack([v, v * 0.9, v * 0.8], -1), length=young, extra=0.01)
+    n = width * height
+    col = rng.gamma(1.5, 0.3, (n, 3))
+    nrm = rng.normal(size=(n, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    nrm[:, 2] = np.abs(nrm[:, 2])
+    leaf = np.where(rng.random((height, width)) < 0.08, 0xFFFFFFFF, 3).astype(np.uint32)
+    f = field(col.reshape(height, width, 3), length=rng.integers(1, 40, (height, width)).astype(np.float32), depth=rng.uniform(2, 30, (height, width)),
+              normal=nrm, albedo=rng.uniform(0, 1, (n, 3)), leaf=leaf, demodulated=1, extra=rng.uniform(0, 0.05, (height, width)))
+    fields["mixed"] = f
+    return lens, fields
+
+
+def denoise_fixture(dump: str, tmp: str) -> None:
+    lens, fields = denoise_fields()
+    out = {"lens": lens, "width": 64, "height": 48}
+    for name, f in fields.items():
+        path = os.path.join(tmp, f"denoise_{name}.bin")
+        with open(path, "wb") as fh:
+            fh.write(struct.pack("<3i", 64, 48, int(f["demodulated"])))
+            fh.write(lens.astype("<f8").tobytes())
+            for k in range(64 * 48):
+                fh.write(f["colour"][k].astype("<f8").tobytes())
+                fh.write(struct.pack("<d", float(f["moment"][k])))
+                fh.write(struct.pack("<ff", float(f["length"][k]), float(f["distance"][k])))
+                fh.write(f["normal"][k].astype("<f8").tobytes())
+                fh.write(struct.pack("<I", int(f["leaf"][k])))
+                fh.write(f["albedo"][k].astype("<f8").tobytes())
+        res = os.path.join(tmp, f"denoise_{name}.out")
+        subprocess.run([dump, "denoise", path, res], check=True)
+        rgb = np.fromfile(res, "<f4").reshape(-1, 3)
+        for k, v in f.items():
+            out[f"{name}.{k}"] = v
+        out[f"{name}.out"] = rgb
+        print(" denoise", name, "mean in", f["colour"].mean(0), "out", rgb.mean(0))
+    np.savez_compressed(os.path.join(HERE, "denoise.npz"), **out)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref-bin", default=os.path.join(ROOT, "oracle", "_ref"))
@@ -152,6 +232,8 @@ def main() -> None:
     render = os.path.join(args.ref_bin, "kodanuki")
     os.makedirs(os.path.join(HERE, "scenes"), exist_ok=True)
     tmp = tempfile.mkdtemp()
+    if args.only in (None, "denoise"):
+        denoise_fixture(dump, tmp)
     for name, (gen, kw, nrays, depth) in SCENES.items():
         if args.only and name != args.only:
             continue

@@ -52,3 +52,22 @@ def test_octree_trace_agrees_with_whole_scene_trace():
     assert (h["leaf"][both] == tr["leaf"][both]).mean() > 0.995
     rel = np.abs(h["distance"][both] - tr["distance"][both]) / np.maximum(tr["distance"][both], 1e-6)
     assert np.quantile(rel, 0.99) < 1e-5
+
+
+def denoise_cases():
+    z = np.load(os.path.join(GOLDEN, "denoise.npz"))
+    d = {k: z[k] for k in z.files}
+    names = sorted({k.split(".", 1)[0] for k in d if "." in k})
+    return d, names
+
+
+def test_denoiser_matches_reference():
+    """The oracle's a-trous denoiser reproduces the reference's
+    denoisedFrame float for float on every fixture field."""
+    d, names = denoise_cases()
+    assert len(names) >= 6
+    for name in names:
+        f = {k.split(".", 1)[1]: v for k, v in d.items() if k.startswith(name + ".")}
+        out = op.denoise(int(d["width"]), int(d["height"]), int(f["demodulated"]), d["lens"], f["colour"], f["moment"], f["length"],
+                         f["distance"], f["normal"], f["leaf"], f["albedo"])
+        assert np.array_equal(out, f["out"]), name
