@@ -245,10 +245,13 @@ def run_gpu(args) -> None:
                             "note": "sphere-trace kernel: FP32 SIMT-bound, see roofline_simt"}
         line["roofline_simt"] = {"achieved_tflops": achieved_flops, "peak_tflops": 152 * 128 * 2 * 2.07e9 / 1e12,
                                  "unit": "TFLOP/s FP32 (1 flop a program step, 30 a march step)"}
-        try:
-            line["cpu_baseline"] = cpu_baseline(scene)
-        except Exception as e:  # the oracle is test infrastructure; report why it could not run
-            line["cpu_baseline"] = {"value": None, "unit": "Msamples/s", "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {e}"}
+        if args.no_cpu:
+            line["cpu_baseline"] = None
+        else:
+            try:
+                line["cpu_baseline"] = cpu_baseline(scene)
+            except Exception as e:  # the oracle is test infrastructure; report why it could not run
+                line["cpu_baseline"] = {"value": None, "unit": "Msamples/s", "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {e}"}
         print(json.dumps(line), flush=True)
     b.close()
     if dist:
@@ -256,12 +259,18 @@ def run_gpu(args) -> None:
 
 
 def main() -> None:
+    global WIDTH, HEIGHT, SPP
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--width", type=int, default=WIDTH, help="a smaller frame for profiling captures only")
+    ap.add_argument("--height", type=int, default=HEIGHT)
+    ap.add_argument("--spp", type=int, default=SPP)
+    ap.add_argument("--no-cpu", action="store_true", help="leave out the CPU baseline (profiling captures)")
     args = ap.parse_args()
+    WIDTH, HEIGHT, SPP = args.width, args.height, args.spp
     if args.impl == "reference":
         run_reference(args)
     else:
