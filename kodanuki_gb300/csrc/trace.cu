@@ -82,10 +82,21 @@ struct Field {
 	float exit;
 };
 
-__device__ __forceinline__ Field fieldAt(const DeviceWorld& w, const float o[3], const float d[3], const float inv[3], float t, float* slots, uint32_t stride, unsigned long long& steps) {
+// Whether a point is in a located cell: the half-open box the descent gives
+// it (a coordinate equal to a midpoint goes to the upper half), so a point
+// found here is the point the descent would find there.
+__device__ __forceinline__ bool within(const Located& l, const float p[3]) {
+	return l.leaf != kNoLeaf && p[0] >= l.lo[0] && p[0] < l.hi[0] && p[1] >= l.lo[1] && p[1] < l.hi[1] && p[2] >= l.lo[2] && p[2] < l.hi[2];
+}
+
+// The field at t from the kept programs of the cell the point lies in.  The
+// cell of the previous step is kept in `cell`: a ray takes several steps in
+// one cell, and only a point that has left it descends the octree again.
+__device__ __forceinline__ Field fieldAt(const DeviceWorld& w, const float o[3], const float d[3], const float inv[3], float t, float* slots, uint32_t stride, unsigned long long& steps, Located& cell) {
 	Field f;
 	const float p[3] = { o[0] + d[0] * t, o[1] + d[1] * t, o[2] + d[2] * t };
-	const Located l  = locate(w, p);
+	if (!within(cell, p)) cell = locate(w, p);
+	const Located& l   = cell;
 	const GpuLeaf leaf = w.leaves[l.leaf];
 	f.first  = leaf.first;
 	f.count  = leaf.count;
@@ -162,9 +173,11 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 		HitState h = { 0, 0.0f, kNoLeaf, 0, 0 };
 		float t    = lo;
 		uint32_t step = 0;
+		Located cell;
+		cell.leaf = kNoLeaf;
 		if (!(up < lo)) {
 			for (; step < args.maxSteps && t <= up; ++step) {
-				const Field f = fieldAt(w, o, d, inv, t, slots, stride, programSteps);
+				const Field f = fieldAt(w, o, d, inv, t, slots, stride, programSteps, cell);
 				if (f.empty) {
 					t = fmaxf(f.exit, t) + nudge(t);
 					continue;
@@ -182,7 +195,8 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 				// sphereFromInside: stand on the nearest surface and read the field past it.
 				if (f.nearest < tol) {
 					const float inset = 2.0f * tol;
-					const Field past  = fieldAt(w, o, d, inv, t + inset, slots, stride, programSteps);
+					Located beyond   = cell;
+					const Field past  = fieldAt(w, o, d, inv, t + inset, slots, stride, programSteps, beyond);
 					if (past.empty || past.least > 0.0f) {
 						h = { 1, t, f.first, winnerAt(w, o, d, t, f, slots, stride), step + 1 };
 						break;
