@@ -263,6 +263,25 @@ kdn_status kdn_denoise_device(kdn_ctx* ctx, const kdn_denoise_frame* frame, cons
                               const uint16_t* distance, const uint16_t* normal, const uint16_t* albedo, const uint32_t* leaf, float* out_rgb,
                               void* stream);
 
+/*
+ * kdn_denoise_device without a context and without allocating: for callers
+ * that may not allocate device memory once running (a frame loop that
+ * reserved its device-memory budget at start-up, or one that must not stall
+ * its other streams on the synchronisation cudaMalloc/cudaFree can cause).
+ * No counterpart in the reference: its denoiser runs on the host.
+ *
+ * Its scratch is a static device array of 17 MiB that every GPU loading
+ * the library holds until exit; frames of more than 262144 pixels (512x512)
+ * are refused with KDN_BAD_ARG.  It runs on the current device, on the given
+ * stream; the arrays are device pointers as for kdn_denoise_device.  The
+ * first call on a device looks the array's device address up; make that
+ * first call before any stream capture.  All calls share the array: calls
+ * whose work overlaps on the GPU race.  Nothing in it has to start at zero.
+ * The message of a failed call is kdn_last_error(NULL) on the calling thread.
+ */
+kdn_status kdn_denoise_static(const kdn_denoise_frame* frame, const float* colour, const float* moment, const float* length, const uint16_t* distance,
+                              const uint16_t* normal, const uint16_t* albedo, const uint32_t* leaf, float* out_rgb, void* stream);
+
 /* Write a buffer larger than the L2 cache on the context's stream, so that
  * the next launch starts with a cold cache. */
 kdn_status kdn_flush_l2(kdn_ctx* ctx);

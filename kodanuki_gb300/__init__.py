@@ -73,7 +73,7 @@ class KdnError(RuntimeError):
 EXPORTS = [
     "kdn_status_string", "kdn_last_error", "kdn_open", "kdn_close", "kdn_upload_block", "kdn_build", "kdn_world_stats",
     "kdn_world_cell", "kdn_extend", "kdn_extend_device", "kdn_render", "kdn_render_device", "kdn_frame_stats_get", "kdn_flush_l2",
-    "kdn_denoise", "kdn_denoise_device",
+    "kdn_denoise", "kdn_denoise_device", "kdn_denoise_static",
 ]
 
 
@@ -113,6 +113,7 @@ def library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.kdn_flush_l2.argtypes = [P]
     L.kdn_denoise.argtypes = [P, ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P]
     L.kdn_denoise_device.argtypes = [P, ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P, P]
+    L.kdn_denoise_static.argtypes = [ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P, P]
     for name in EXPORTS:
         fn = getattr(L, name)
         if name not in ("kdn_status_string", "kdn_last_error"):

@@ -46,6 +46,12 @@ thread_local std::string openError;
 
 } // namespace
 
+namespace kdn {
+
+void setThreadError(const std::string& message) { openError = message; }
+
+} // namespace kdn
+
 extern "C" {
 
 const char* kdn_status_string(kdn_status status) {
