@@ -13,7 +13,8 @@ kdn_status Context::open() {
 	if (!check(setTraceAttributes(), "the trace kernel is not built for this device")) return KDN_NO_DEVICE;
 	if (!check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate")) return KDN_CUDA_ERROR;
 	kdn_status s = ensure(counters, 8 * sizeof(unsigned long long));
-	return s;
+	if (s != KDN_OK) return s;
+	return ensure(fetch, 256);
 }
 
 static void freeBuffer(DeviceBuffer& b) {
@@ -27,7 +28,7 @@ void Context::release() {
 	cudaSetDevice(device);
 	if (stream) cudaStreamSynchronize(stream);
 	releaseFrame();
-	for (DeviceBuffer* b : { &nodes, &leaves, &programs, &steps, &ssa, &leafMaterial, &objectMaterial, &extendRays, &extendHits, &extendStates, &counters, &l2, &denoiseScratch, &denoiseIo }) freeBuffer(*b);
+	for (DeviceBuffer* b : { &nodes, &leaves, &programs, &steps, &march, &ssa, &leafMaterial, &objectMaterial, &extendRays, &extendHits, &extendStates, &counters, &l2, &denoiseScratch, &denoiseIo, &fetch }) freeBuffer(*b);
 	if (stream) cudaStreamDestroy(stream);
 	stream = nullptr;
 }
@@ -124,6 +125,7 @@ kdn_status Context::build(const BuildOptions& options) {
 	if ((s = upload(programs, flat.programs.data(), flat.programs.size() * sizeof(GpuProgram))) != KDN_OK) return s;
 	if ((s = upload(steps, flat.steps.data(), flat.steps.size() * sizeof(GpuStep))) != KDN_OK) return s;
 	if ((s = upload(ssa, flat.ssa.data(), flat.ssa.size() * sizeof(SsaOps))) != KDN_OK) return s;
+	if ((s = upload(march, flat.march.data(), flat.march.size() * sizeof(GpuStep))) != KDN_OK) return s;
 	if ((s = upload(leafMaterial, leafMaterials.data(), leafMaterials.size() * sizeof(uint32_t))) != KDN_OK) return s;
 	if ((s = upload(objectMaterial, firstLeafMaterial.data(), firstLeafMaterial.size() * sizeof(uint32_t))) != KDN_OK) return s;
 	if (!check(cudaStreamSynchronize(stream), "kdn_build upload")) return KDN_CUDA_ERROR;
@@ -132,6 +134,7 @@ kdn_status Context::build(const BuildOptions& options) {
 	world.programs      = static_cast<const GpuProgram*>(programs.ptr);
 	world.steps         = static_cast<const GpuStep*>(steps.ptr);
 	world.ssa           = static_cast<const SsaOps*>(ssa.ptr);
+	world.march         = static_cast<const GpuStep*>(march.ptr);
 	world.leaf_material = static_cast<const uint32_t*>(leafMaterial.ptr);
 	for (int a = 0; a < 3; ++a) {
 		world.lower[a] = float(regions[0].lower[a]);
@@ -162,6 +165,7 @@ kdn_status Context::extend(const kdn_ray* rays, uint32_t n, kdn_hit* hits, cudaS
 	t.maxSteps       = kMarchSteps;
 	t.counters       = nullptr;
 	t.count          = nullptr;
+	t.fetch          = static_cast<uint32_t*>(fetch.ptr);
 	if (!check(launchTrace(t, on, smCount), "trace kernel")) return KDN_CUDA_ERROR;
 	HitArgs h;
 	h.world  = world;

@@ -36,9 +36,9 @@ struct Context {
 	FlatWorld flat;
 	std::vector<int64_t> preorder; // cell index of each depth-first position
 	DeviceWorld world {};
-	DeviceBuffer nodes, leaves, programs, steps, ssa, leafMaterial, objectMaterial;
+	DeviceBuffer nodes, leaves, programs, steps, march, ssa, leafMaterial, objectMaterial;
 	DeviceBuffer extendRays, extendHits, extendStates, counters, l2;
-	DeviceBuffer denoiseScratch, denoiseIo;
+	DeviceBuffer denoiseScratch, denoiseIo, fetch;
 	FrameState* frame = nullptr;
 
 	kdn_status open();

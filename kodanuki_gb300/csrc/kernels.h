@@ -31,6 +31,7 @@ struct TraceArgs {
 	uint32_t maxSteps;
 	unsigned long long* counters;   // [0] march steps, [1] program steps
 	const uint32_t* count;          // if set, the number of rays is read here on the device
+	uint32_t* fetch;                // the next ray to take; launchTrace zeroes it
 };
 
 struct HitArgs {

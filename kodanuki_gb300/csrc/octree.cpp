@@ -517,6 +517,83 @@ std::string slotted(const Prog& p, std::vector<GpuStep>& steps, std::vector<SsaO
 	return "";
 }
 
+// The march form of a program: every constant a step reads becomes that
+// step's immediate (one a step, the last constant operand), constants no
+// step reads from a slot any more are left out, and the slots are allocated
+// again over what remains.
+std::string marchCode(const Prog& p, std::vector<GpuStep>& steps, GpuProgram& out) {
+	const uint32_t n = uint32_t(p.steps.size());
+	std::vector<uint8_t> imm(n, 0), needed(n, 0);
+	needed[p.result] = 1;
+	for (uint32_t i = 0; i < n; ++i) {
+		const kdn_step& s    = p.steps[i];
+		const int k          = operandCount(s.opcode);
+		const uint32_t op[3] = { s.a, s.b, s.c };
+		if (s.opcode != OpConstant && s.opcode != OpArgument) {
+			for (int j = k - 1; j >= 0; --j) {
+				if (p.steps[op[j]].opcode == OpConstant) {
+					imm[i] = uint8_t(j + 1);
+					break;
+				}
+			}
+		}
+		for (int j = 0; j < k; ++j) {
+			if (imm[i] != j + 1) needed[op[j]] = 1;
+		}
+	}
+	std::vector<uint32_t> lastUse(n);
+	for (uint32_t i = 0; i < n; ++i) lastUse[i] = i;
+	for (uint32_t i = 0; i < n; ++i) {
+		const kdn_step& s    = p.steps[i];
+		const int k          = operandCount(s.opcode);
+		const uint32_t op[3] = { s.a, s.b, s.c };
+		for (int j = 0; j < k; ++j) {
+			if (imm[i] != j + 1) lastUse[op[j]] = std::max(lastUse[op[j]], i);
+		}
+	}
+	lastUse[p.result] = n;
+	std::vector<uint8_t> slot(n, 0);
+	std::vector<uint8_t> freeSlots;
+	uint32_t used  = 0;
+	uint32_t kept  = 0;
+	out.march      = uint32_t(steps.size());
+	for (uint32_t i = 0; i < n; ++i) {
+		const kdn_step& s = p.steps[i];
+		if (s.opcode == OpConstant && !needed[i]) continue;
+		const int k          = operandCount(s.opcode);
+		const uint32_t op[3] = { s.a, s.b, s.c };
+		GpuStep g            = {};
+		g.op                 = s.opcode;
+		g.imm                = imm[i];
+		g.a                  = k > 0 && imm[i] != 1 ? slot[op[0]] : 0;
+		g.b                  = k > 1 && imm[i] != 2 ? slot[op[1]] : 0;
+		g.c                  = k > 2 && imm[i] != 3 ? slot[op[2]] : 0;
+		g.value              = imm[i] ? float(p.steps[op[imm[i] - 1]].value) : (s.opcode == OpArgument ? 0.0f : float(s.value));
+		g.leaf               = s.leaf;
+		for (int j = 0; j < k; ++j) {
+			if (imm[i] == j + 1) continue;
+			bool first = true;
+			for (int m = 0; m < j; ++m) first = first && (imm[i] == m + 1 || op[m] != op[j]);
+			if (first && lastUse[op[j]] == i) freeSlots.push_back(slot[op[j]]);
+		}
+		if (!freeSlots.empty()) {
+			slot[i] = freeSlots.back();
+			freeSlots.pop_back();
+		} else {
+			if (used >= kMaxSlots) return "a leaf program needs more than " + std::to_string(kMaxSlots) + " register slots";
+			slot[i] = uint8_t(used++);
+		}
+		if (lastUse[i] == i) freeSlots.push_back(slot[i]);
+		g.dst = slot[i];
+		steps.push_back(g);
+		++kept;
+	}
+	out.marchCount = uint16_t(kept);
+	out.marchSlot  = slot[p.result];
+	out.marchSlots = uint8_t(std::max(used, 1u));
+	return "";
+}
+
 } // namespace
 
 std::string flattenOctree(const Octree& tree, FlatWorld& flat) {
@@ -540,7 +617,9 @@ std::string flattenOctree(const Octree& tree, FlatWorld& flat) {
 			uint32_t index;
 			if (found == made.end()) {
 				GpuProgram g     = {};
-				const std::string error = slotted(*p, flat.steps, flat.ssa, g);
+				std::string error = slotted(*p, flat.steps, flat.ssa, g);
+				if (!error.empty()) return error;
+				error = marchCode(*p, flat.march, g);
 				if (!error.empty()) return error;
 				index = uint32_t(flat.programs.size());
 				flat.programs.push_back(g);

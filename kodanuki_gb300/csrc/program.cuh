@@ -64,16 +64,19 @@ __device__ __forceinline__ float stepValue(uint8_t op, float a, float b, float c
 	}
 }
 
+// One step of the march form: its operands from the slots or, for the one
+// its `imm` names, from its value.
+__device__ __forceinline__ void runSlotStep(const GpuStep& s, float* slots, uint32_t stride, const float p[3]) {
+	const float a = s.imm == 1 ? s.value : slots[s.a * stride];
+	const float b = s.imm == 2 ? s.value : slots[s.b * stride];
+	const float c = s.imm == 3 ? s.value : slots[s.c * stride];
+	slots[s.dst * stride] = stepValue(s.op, a, b, c, s.value, p);
+}
+
 // One program at one point; slots is this thread's column base (stride
 // blockDim.x).  Returns the program's value.
 __device__ __forceinline__ float evalSlots(const GpuStep* __restrict__ code, uint32_t count, uint32_t resultSlot, float* slots, uint32_t stride, const float p[3]) {
-	for (uint32_t i = 0; i < count; ++i) {
-		const GpuStep s = code[i];
-		const float a   = slots[s.a * stride];
-		const float b   = slots[s.b * stride];
-		const float c   = slots[s.c * stride];
-		slots[s.dst * stride] = stepValue(s.op, a, b, c, s.value, p);
-	}
+	for (uint32_t i = 0; i < count; ++i) runSlotStep(code[i], slots, stride, p);
 	return slots[resultSlot * stride];
 }
 

@@ -287,6 +287,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 			t.maxSteps       = kMarchSteps;
 			t.counters       = static_cast<unsigned long long*>(ctx->counters.ptr);
 			t.count          = Q[cur].count;
+			t.fetch          = static_cast<uint32_t*>(ctx->fetch.ptr);
 			cudaEventRecord(f.events[ev++], stream);
 			if (!ctx->check(launchTrace(t, stream, ctx->smCount), "trace kernel")) return KDN_CUDA_ERROR;
 			cudaEventRecord(f.events[ev++], stream);

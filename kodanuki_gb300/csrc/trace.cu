@@ -111,8 +111,8 @@ __device__ __forceinline__ Field fieldAt(const DeviceWorld& w, const float o[3],
 	if (f.empty) return f;
 	for (uint32_t k = 0; k < leaf.count; ++k) {
 		const GpuProgram g = w.programs[leaf.first + k];
-		const float v      = evalSlots(w.steps + g.code, g.count, g.slot, slots, stride, p);
-		steps += g.count;
+		const float v      = evalSlots(w.march + g.march, g.marchCount, g.marchSlot, slots, stride, p);
+		steps += g.marchCount;
 		if (v < f.least) {
 			f.least = v;
 			f.index = k;
@@ -135,14 +135,14 @@ __device__ uint32_t winnerAt(const DeviceWorld& w, const float o[3], const float
 	float values[kMaxLeafProgs];
 	for (uint32_t k = 0; k < f.count && k < kMaxLeafProgs; ++k) {
 		const GpuProgram g = w.programs[f.first + k];
-		values[k]          = evalSlots(w.steps + g.code, g.count, g.slot, slots, stride, p);
+		values[k]          = evalSlots(w.march + g.march, g.marchCount, g.marchSlot, slots, stride, p);
 		tied               = tied || (k != f.index && values[k] - f.least <= band);
 	}
 	if (!tied) return winner;
 	for (uint32_t k = 0; k < f.count && k < kMaxLeafProgs; ++k) {
 		if (!(values[k] - f.least <= band)) continue;
 		const GpuProgram g = w.programs[f.first + k];
-		const float on     = evalSlots(w.steps + g.code, g.count, g.slot, slots, stride, q);
+		const float on     = evalSlots(w.march + g.march, g.marchCount, g.marchSlot, slots, stride, q);
 		if (on < onWinner) {
 			onWinner = on;
 			winner   = k;
@@ -151,6 +151,15 @@ __device__ uint32_t winnerAt(const DeviceWorld& w, const float o[3], const float
 	return winner;
 }
 
+// The march as a step machine.  Each thread holds one ray at a time and
+// every turn of the loop runs one program step for every thread that is
+// evaluating, so threads whose cells hold programs of different lengths, or
+// whose rays take different numbers of march steps, stay busy: a thread that
+// finishes a program moves on to the next program of its cell, a thread that
+// finishes a march step locates its next cell, and a thread whose ray ends
+// takes the next ray of the launch (one atomic a warp).
+enum LaneMode : uint32_t { Fetch = 0, Locating = 1, Evaluating = 2, Finished = 3 };
+
 __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 	extern __shared__ float slotMemory[];
 	const DeviceWorld& w  = args.world;
@@ -158,64 +167,177 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 	float* slots          = slotMemory + threadIdx.x;
 	unsigned long long marchSteps = 0, programSteps = 0;
 	const uint32_t n = args.count ? *args.count : args.n;
-	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-		const kdn_ray ray = args.rays[i];
-		const float o[3]  = { ray.origin[0], ray.origin[1], ray.origin[2] };
-		const float d[3]  = { ray.direction[0], ray.direction[1], ray.direction[2] };
-		const float inv[3] = { slopeOf(d[0]), slopeOf(d[1]), slopeOf(d[2]) };
-		float lo = 0.0f, up = ray.far;
-		for (int a = 0; a < 3; ++a) {
-			const float x = (w.lower[a] - o[a]) * inv[a];
-			const float y = (w.lower[a] + w.size[a] - o[a]) * inv[a];
-			lo            = fmaxf(lo, fminf(x, y));
-			up            = fminf(up, fmaxf(x, y));
-		}
-		HitState h = { 0, 0.0f, kNoLeaf, 0, 0 };
-		float t    = lo;
-		uint32_t step = 0;
-		Located cell;
-		cell.leaf = kNoLeaf;
-		if (!(up < lo)) {
-			for (; step < args.maxSteps && t <= up; ++step) {
-				const Field f = fieldAt(w, o, d, inv, t, slots, stride, programSteps, cell);
-				if (f.empty) {
-					t = fmaxf(f.exit, t) + nudge(t);
-					continue;
-				}
-				const float p[3] = { o[0] + d[0] * t, o[1] + d[1] * t, o[2] + d[2] * t };
-				const float tol  = tolerance(p);
-				if (!ray.inside) {
-					if (f.least < tol) {
-						h = { 1, t, f.first, winnerAt(w, o, d, t, f, slots, stride), step + 1 };
-						break;
+	const unsigned lane = threadIdx.x & 31u;
+
+	uint32_t mode = Fetch;
+	uint32_t ray  = 0;
+	float o[3], d[3], inv[3];
+	float t = 0.0f, up = 0.0f;
+	bool inside      = false;
+	uint32_t medium  = kNoLeaf;
+	uint32_t step    = 0;
+	Located cell;
+	cell.leaf = kNoLeaf;
+	float exitT = 0.0f;
+	// the cell being evaluated: its run of kept programs and the one in hand
+	uint32_t first = 0, count = 0, k = 0;
+	const GpuStep* code = nullptr;
+	uint32_t pc = 0, length = 0, resultSlot = 0;
+	float p[3]  = { 0.0f, 0.0f, 0.0f };
+	float least = 0.0f, second = 0.0f, nearest = 0.0f;
+	uint32_t index = 0;
+
+	for (;;) {
+		// take new rays, one atomic a warp
+		const bool want     = mode == Fetch;
+		const unsigned mask = __ballot_sync(0xFFFFFFFFu, want);
+		if (mask) {
+			uint32_t base = 0;
+			const int leader = __ffs(mask) - 1;
+			if (int(lane) == leader) base = atomicAdd(args.fetch, uint32_t(__popc(mask)));
+			base = __shfl_sync(0xFFFFFFFFu, base, leader);
+			if (want) {
+				ray = base + uint32_t(__popc(mask & ((1u << lane) - 1u)));
+				if (ray >= n) {
+					mode = Finished;
+				} else {
+					const kdn_ray r = args.rays[ray];
+					for (int a = 0; a < 3; ++a) {
+						o[a]   = r.origin[a];
+						d[a]   = r.direction[a];
+						inv[a] = slopeOf(d[a]);
 					}
-					t = fminf(t + f.least, fmaxf(f.exit, t) + nudge(t));
-					continue;
-				}
-				// sphereFromInside: stand on the nearest surface and read the field past it.
-				if (f.nearest < tol) {
-					const float inset = 2.0f * tol;
-					Located beyond   = cell;
-					const Field past  = fieldAt(w, o, d, inv, t + inset, slots, stride, programSteps, beyond);
-					if (past.empty || past.least > 0.0f) {
-						h = { 1, t, f.first, winnerAt(w, o, d, t, f, slots, stride), step + 1 };
-						break;
+					float lo = 0.0f;
+					up       = r.far;
+					for (int a = 0; a < 3; ++a) {
+						const float x = (w.lower[a] - o[a]) * inv[a];
+						const float y = (w.lower[a] + w.size[a] - o[a]) * inv[a];
+						lo            = fmaxf(lo, fminf(x, y));
+						up            = fminf(up, fmaxf(x, y));
 					}
-					const GpuProgram g   = w.programs[past.first + past.index];
-					const uint32_t there = g.object;
-					// The solid past the point is another material than the one the ray is in: stop there.
-					if (args.objectMaterial != nullptr && args.objectMaterial[there] != ray.within) {
-						h = { 2, t, past.first, past.index, step + 1 };
-						break;
+					t         = lo;
+					inside    = r.inside != 0;
+					medium    = r.within;
+					step      = 0;
+					cell.leaf = kNoLeaf;
+					if (up < lo) {
+						args.states[ray] = HitState { 0, 0.0f, kNoLeaf, 0, 0 };
+						mode             = Fetch;
+					} else {
+						mode = Locating;
 					}
-					t += inset;
-					continue;
 				}
-				t = fminf(t + f.nearest, fmaxf(f.exit, t) + nudge(t));
 			}
 		}
-		marchSteps += step;
-		args.states[i] = h;
+		if (__all_sync(0xFFFFFFFFu, mode == Finished)) break;
+
+		// find the cell of the point, skipping empty cells, and start its first program
+		if (mode == Locating) {
+			for (;;) {
+				if (!(step < args.maxSteps && t <= up)) {
+					marchSteps += step;
+					args.states[ray] = HitState { 0, 0.0f, kNoLeaf, 0, step };
+					mode             = Fetch;
+					break;
+				}
+				for (int a = 0; a < 3; ++a) p[a] = o[a] + d[a] * t;
+				if (!within(cell, p)) cell = locate(w, p);
+				const GpuLeaf leaf = w.leaves[cell.leaf];
+				exitT              = cellExit(o, inv, cell);
+				if (leaf.occupancy == Empty || leaf.count == 0) {
+					t = fmaxf(exitT, t) + nudge(t);
+					++step;
+					continue;
+				}
+				first   = leaf.first;
+				count   = leaf.count;
+				k       = 0;
+				least   = 3.0e38f;
+				second  = 3.0e38f;
+				nearest = 3.0e38f;
+				index   = 0;
+				const GpuProgram g = w.programs[first];
+				code       = w.march + g.march;
+				length     = g.marchCount;
+				resultSlot = g.marchSlot;
+				pc         = 0;
+				mode       = Evaluating;
+				break;
+			}
+		}
+
+		// one program step
+		if (mode == Evaluating) {
+			runSlotStep(code[pc], slots, stride, p);
+			if (++pc == length) {
+				const float v = slots[resultSlot * stride];
+				programSteps += length;
+				if (v < least) {
+					second = least;
+					least  = v;
+					index  = k;
+				} else if (v < second) {
+					second = v;
+				}
+				nearest = fminf(nearest, fabsf(v));
+				if (++k < count) {
+					const GpuProgram g = w.programs[first + k];
+					code       = w.march + g.march;
+					length     = g.marchCount;
+					resultSlot = g.marchSlot;
+					pc         = 0;
+				} else {
+					// the march step: stop on the surface or go on by the field
+					const float tol = tolerance(p);
+					++step;
+					mode = Locating;
+					if (!inside) {
+						if (least < tol) {
+							Field f;
+							f.least = least;
+							f.index = index;
+							f.count = count;
+							f.first = first;
+							const float big  = fmaxf(fabsf(p[0]), fmaxf(fabsf(p[1]), fabsf(p[2])));
+							const bool tied  = second - least <= 2e-6f * (1.0f + big);
+							const uint32_t winner = tied ? winnerAt(w, o, d, t, f, slots, stride) : index;
+							args.states[ray] = HitState { 1, t, first, winner, step };
+							marchSteps += step;
+							mode = Fetch;
+						} else {
+							t = fminf(t + least, fmaxf(exitT, t) + nudge(t));
+						}
+					} else if (nearest < tol) {
+						// sphereFromInside: stand on the nearest surface and read the field past it
+						Field f;
+						f.least = least;
+						f.index = index;
+						f.count = count;
+						f.first = first;
+						const float inset = 2.0f * tol;
+						Located beyond    = cell;
+						const Field past  = fieldAt(w, o, d, inv, t + inset, slots, stride, programSteps, beyond);
+						if (past.empty || past.least > 0.0f) {
+							args.states[ray] = HitState { 1, t, first, winnerAt(w, o, d, t, f, slots, stride), step };
+							marchSteps += step;
+							mode = Fetch;
+						} else {
+							const GpuProgram g = w.programs[past.first + past.index];
+							// a solid of another material than the one the ray is in: stop there
+							if (args.objectMaterial != nullptr && args.objectMaterial[g.object] != medium) {
+								args.states[ray] = HitState { 2, t, past.first, past.index, step };
+								marchSteps += step;
+								mode = Fetch;
+							} else {
+								t += inset;
+							}
+						}
+					} else {
+						t = fminf(t + nearest, fmaxf(exitT, t) + nudge(t));
+					}
+				}
+			}
+		}
 	}
 	if (args.counters) {
 		// one add per warp
@@ -307,8 +429,18 @@ __global__ void __launch_bounds__(kTraceBlock) hitKernel(HitArgs args) {
 
 cudaError_t launchTrace(const TraceArgs& args, cudaStream_t stream, int smCount) {
 	if (args.n == 0) return cudaSuccess;
-	const uint32_t blocks = uint32_t(std::min<uint64_t>((uint64_t(args.n) + kTraceBlock - 1) / kTraceBlock, uint64_t(smCount) * 16));
-	const size_t shared   = size_t(kMaxSlots) * kTraceBlock * sizeof(float);
+	const size_t shared = size_t(kMaxSlots) * kTraceBlock * sizeof(float);
+	// persistent blocks: as many as fit on the SMs at once, fewer for a small launch
+	static int resident = 0;
+	if (resident == 0) {
+		int perSm = 0;
+		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, traceKernel, kTraceBlock, shared) != cudaSuccess || perSm < 1) perSm = 1;
+		resident = perSm;
+	}
+	const uint64_t wanted = (uint64_t(args.n) + kTraceBlock - 1) / kTraceBlock;
+	const uint32_t blocks = uint32_t(std::max<uint64_t>(1, std::min<uint64_t>(wanted, uint64_t(smCount) * uint64_t(resident))));
+	cudaError_t e = cudaMemsetAsync(args.fetch, 0, sizeof(uint32_t), stream);
+	if (e != cudaSuccess) return e;
 	traceKernel<<<blocks, kTraceBlock, shared, stream>>>(args);
 	return cudaGetLastError();
 }

@@ -31,11 +31,14 @@ constexpr uint32_t kMaxLeafProgs = 64; // kept programs of one leaf
 // skims a surface for longer meets nothing.
 constexpr uint32_t kMarchSteps = 1u << 16;
 
+// In the march form a step may read one operand as an immediate: `imm` says
+// which (1 a, 2 b, 3 c; 0 none) and `value` holds it, so the constants a
+// program's steps read take no step and no slot of their own.
 struct GpuStep {
 	uint8_t op;
 	uint8_t dst;
 	uint8_t a, b, c;
-	uint8_t pad0;
+	uint8_t imm;
 	uint16_t pad1;
 	float value;
 	uint32_t leaf;
@@ -48,15 +51,20 @@ struct SsaOps {
 static_assert(sizeof(SsaOps) == 8, "SsaOps is 8 bytes");
 
 struct GpuProgram {
-	uint32_t code;      // first GpuStep
-	uint16_t count;     // steps
-	uint16_t result;    // SSA index of the result
-	uint8_t slot;       // slot of the result
-	uint8_t slots;      // slots used
-	uint16_t pad;
-	uint32_t object;    // index into the scene's object programs
+	uint32_t code;       // first GpuStep of the whole program (read at a hit)
+	uint16_t count;      // its steps
+	uint16_t result;     // SSA index of the result
+	uint8_t slot;        // slot of the result
+	uint8_t slots;       // slots used
+	uint16_t marchCount; // steps of the march form
+	uint32_t object;     // index into the scene's object programs
+	uint32_t march;      // first GpuStep of the march form (constants as immediates)
+	uint8_t marchSlot;   // slot of the result in the march form
+	uint8_t marchSlots;
+	uint16_t pad0;
+	uint32_t pad1[2];
 };
-static_assert(sizeof(GpuProgram) == 16, "GpuProgram is 16 bytes");
+static_assert(sizeof(GpuProgram) == 32, "GpuProgram is 32 bytes");
 
 enum Occupancy : uint8_t { Empty = 0, Filled = 1, Surface = 2 };
 
@@ -74,6 +82,7 @@ struct DeviceWorld {
 	const GpuLeaf* leaves;
 	const GpuProgram* programs;
 	const GpuStep* steps;
+	const GpuStep* march;
 	const SsaOps* ssa;
 	const uint32_t* leaf_material;
 	float lower[3];
