@@ -162,13 +162,26 @@ typedef struct kdn_frame {
 	int32_t seed;     /* render.seed */
 	uint32_t first;   /* sample index of this call's first sample of every pixel */
 	uint32_t accumulate; /* 1: add to the pixel sums of the previous call */
-	uint32_t pad_;
+	uint32_t flags;      /* KDN_FRAME_DENOISE: return the denoised frame */
 } kdn_frame;
+
+/* With KDN_FRAME_DENOISE a frame also traces its first surfaces, one ray
+ * through each pixel's centre (core/surfaces.cpp:133 tracedSurfaces: distance
+ * from the eye, the normal facing the ray and the albedo as FP16, and the
+ * leaf), keeps the luminance moment of a still camera's temporal state
+ * (plugins/reconstruction/temporal/temporal.cpp:797 freshBlend, :835
+ * heldBlend: each frame's pixel luminance squared, blended in by
+ * max(1 / (length + 1), 1 / 256) over the frames accumulated), and returns
+ * the pixel means put through the a-trous denoiser (kdn_denoise) with those
+ * features, the history length being the frames accumulated (at most 256).
+ * The colour is the exact mean of every sample so far, which is the
+ * temporal blend of equal frames until the cap of 256 frames. */
+#define KDN_FRAME_DENOISE 1u
 
 /* Device times of the last kdn_render, from CUDA events on the context's stream. */
 typedef struct kdn_frame_stats {
 	double total_ms;
-	double trace_ms;   /* every launch of the sphere-trace kernel */
+	double trace_ms;   /* every launch of the sphere-trace kernel (paths and lines) */
 	double shade_ms;   /* arrive + aim + scatter */
 	double other_ms;   /* camera, fold, compaction */
 	uint64_t segments; /* rays traced (camera + scatter + shadow) */
@@ -230,6 +243,13 @@ kdn_status kdn_extend_device(kdn_ctx* ctx, const kdn_ray* rays, uint32_t n, kdn_
 kdn_status kdn_render(kdn_ctx* ctx, const kdn_frame* frame, float* out_rgb);
 kdn_status kdn_render_device(kdn_ctx* ctx, const kdn_frame* frame, float* out_rgb, void* stream);
 kdn_status kdn_frame_stats_get(kdn_ctx* ctx, kdn_frame_stats* stats);
+
+/* The first surfaces of the last frame drawn with KDN_FRAME_DENOISE, a pixel
+ * each, row-major, into host arrays: distance (FP16, infinite where the ray
+ * missed), normal and albedo (FP16 x3), leaf (0xFFFFFFFF where missed).
+ * Replaces core/frame.cpp:508 shownSurfaces.  KDN_NOT_READY when the last
+ * frame kept none. */
+kdn_status kdn_frame_surfaces(kdn_ctx* ctx, uint16_t* distance, uint16_t* normal, uint16_t* albedo, uint32_t* leaf);
 
 /* One frame of the denoiser's feature buffers: the frame size, whether the
  * light is already divided by the albedo (TemporalState::demodulated), and

@@ -54,7 +54,10 @@ class BuildOptions(ctypes.Structure):
 
 class Frame(ctypes.Structure):
     _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("samples", ctypes.c_int32), ("surfaces", ctypes.c_int32),
-                ("seed", ctypes.c_int32), ("first", ctypes.c_uint32), ("accumulate", ctypes.c_uint32), ("pad", ctypes.c_uint32)]
+                ("seed", ctypes.c_int32), ("first", ctypes.c_uint32), ("accumulate", ctypes.c_uint32), ("flags", ctypes.c_uint32)]
+
+
+FRAME_DENOISE = 1  # include/kdn.h KDN_FRAME_DENOISE
 
 
 class FrameStats(ctypes.Structure):
@@ -73,7 +76,7 @@ class KdnError(RuntimeError):
 EXPORTS = [
     "kdn_status_string", "kdn_last_error", "kdn_open", "kdn_close", "kdn_upload_block", "kdn_build", "kdn_world_stats",
     "kdn_world_cell", "kdn_extend", "kdn_extend_device", "kdn_render", "kdn_render_device", "kdn_frame_stats_get", "kdn_flush_l2",
-    "kdn_denoise", "kdn_denoise_device", "kdn_denoise_static",
+    "kdn_frame_surfaces", "kdn_denoise", "kdn_denoise_device", "kdn_denoise_static",
 ]
 
 
@@ -111,6 +114,7 @@ def library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.kdn_render_device.argtypes = [P, ctypes.POINTER(Frame), P, P]
     L.kdn_frame_stats_get.argtypes = [P, ctypes.POINTER(FrameStats)]
     L.kdn_flush_l2.argtypes = [P]
+    L.kdn_frame_surfaces.argtypes = [P, P, P, P, P]
     L.kdn_denoise.argtypes = [P, ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P]
     L.kdn_denoise_device.argtypes = [P, ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P, P]
     L.kdn_denoise_static.argtypes = [ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P, P]
@@ -257,12 +261,14 @@ class Backend:
         return hits
 
     def render(self, width: int, height: int, samples: int, surfaces: int | None = None, seed: int | None = None,
-               first: int = 0, accumulate: bool = False) -> np.ndarray:
+               first: int = 0, accumulate: bool = False, denoise: bool = False) -> np.ndarray:
         """Draw `samples` samples a pixel and return the pixel means
-        (linear RGB, float32, height x width x 3)."""
+        (linear RGB, float32, height x width x 3), or with `denoise` the
+        means filtered by the a-trous denoiser over the first surfaces."""
         sc = self.scene
         f = Frame(width, height, samples, surfaces if surfaces is not None else int(sc.render["surfaces"]),
-                  seed if seed is not None else int(sc.render["seed"]), first, 1 if accumulate else 0, 0)
+                  seed if seed is not None else int(sc.render["seed"]), first, 1 if accumulate else 0,
+                  FRAME_DENOISE if denoise else 0)
         out = np.zeros((height, width, 3), np.float32)
         self._check(self.lib.kdn_render(self.handle, ctypes.byref(f), _ptr(out)))
         return out
@@ -271,6 +277,16 @@ class Backend:
         s = FrameStats()
         self._check(self.lib.kdn_frame_stats_get(self.handle, ctypes.byref(s)))
         return s
+
+    def frame_surfaces(self, width: int, height: int) -> dict:
+        """The first surfaces of the last frame drawn with denoise=True
+        (include/kdn.h kdn_frame_surfaces); FP16 fields as float16 arrays."""
+        distance = np.zeros((height, width), np.float16)
+        normal = np.zeros((height, width, 3), np.float16)
+        albedo = np.zeros((height, width, 3), np.float16)
+        leaf = np.zeros((height, width), np.uint32)
+        self._check(self.lib.kdn_frame_surfaces(self.handle, _ptr(distance), _ptr(normal), _ptr(albedo), _ptr(leaf)))
+        return {"distance": distance, "normal": normal, "albedo": albedo, "leaf": leaf}
 
     def flush_l2(self) -> None:
         self._check(self.lib.kdn_flush_l2(self.handle))

@@ -64,4 +64,8 @@ struct Context {
 	void releaseFrame();
 };
 
+// denoise_abi.cpp: the denoiser over device buffers with the context's scratch.
+kdn_status denoiseOnDevice(Context* ctx, const kdn_denoise_frame* frame, const float* colour, const float* moment, const float* length, const uint16_t* distance,
+                           const uint16_t* normal, const uint16_t* albedo, const uint32_t* leaf, float* out, cudaStream_t stream);
+
 } // namespace kdn

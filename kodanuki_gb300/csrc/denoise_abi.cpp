@@ -55,19 +55,16 @@ kdn_status run(Context* ctx, const kdn_denoise_frame* f, kdn::DenoiseArgs& a, cu
 
 } // namespace
 
-extern "C" {
+namespace kdn {
 
-kdn_status kdn_denoise_device(kdn_ctx* handle, const kdn_denoise_frame* frame, const float* colour, const float* moment, const float* length,
-                              const uint16_t* distance, const uint16_t* normal, const uint16_t* albedo, const uint32_t* leaf, float* out, void* stream) {
-	if (handle == nullptr || frame == nullptr || !colour || !moment || !length || !distance || !normal || !albedo || !leaf || !out) return KDN_BAD_ARG;
-	Context* ctx = reinterpret_cast<Context*>(handle);
-	std::lock_guard<std::mutex> guard(ctx->lock);
-	if (ctx->device < 0) return ctx->fail(KDN_NO_DEVICE, "kdn_denoise_device: a host-only context has no device");
+// The denoiser over device feature buffers with the context's scratch; the
+// caller holds the context's lock and has made its device current.
+kdn_status denoiseOnDevice(Context* ctx, const kdn_denoise_frame* frame, const float* colour, const float* moment, const float* length, const uint16_t* distance,
+                           const uint16_t* normal, const uint16_t* albedo, const uint32_t* leaf, float* out, cudaStream_t stream) {
 	kdn_status s = checkFrame(ctx, frame);
 	if (s != KDN_OK) return s;
-	if (!ctx->check(cudaSetDevice(ctx->device), "cudaSetDevice")) return KDN_CUDA_ERROR;
 	const size_t n = size_t(frame->width) * size_t(frame->height);
-	kdn::DenoiseArgs a {};
+	DenoiseArgs a {};
 	if ((s = scratch(ctx, n, a)) != KDN_OK) return s;
 	a.colour   = colour;
 	a.moment   = moment;
@@ -77,7 +74,21 @@ kdn_status kdn_denoise_device(kdn_ctx* handle, const kdn_denoise_frame* frame, c
 	a.albedo   = albedo;
 	a.leaf     = leaf;
 	a.out      = out;
-	return run(ctx, frame, a, stream ? static_cast<cudaStream_t>(stream) : ctx->stream);
+	return run(ctx, frame, a, stream);
+}
+
+} // namespace kdn
+
+extern "C" {
+
+kdn_status kdn_denoise_device(kdn_ctx* handle, const kdn_denoise_frame* frame, const float* colour, const float* moment, const float* length,
+                              const uint16_t* distance, const uint16_t* normal, const uint16_t* albedo, const uint32_t* leaf, float* out, void* stream) {
+	if (handle == nullptr || frame == nullptr || !colour || !moment || !length || !distance || !normal || !albedo || !leaf || !out) return KDN_BAD_ARG;
+	Context* ctx = reinterpret_cast<Context*>(handle);
+	std::lock_guard<std::mutex> guard(ctx->lock);
+	if (ctx->device < 0) return ctx->fail(KDN_NO_DEVICE, "kdn_denoise_device: a host-only context has no device");
+	if (!ctx->check(cudaSetDevice(ctx->device), "cudaSetDevice")) return KDN_CUDA_ERROR;
+	return kdn::denoiseOnDevice(ctx, frame, colour, moment, length, distance, normal, albedo, leaf, out, stream ? static_cast<cudaStream_t>(stream) : ctx->stream);
 }
 
 kdn_status kdn_denoise(kdn_ctx* handle, const kdn_denoise_frame* frame, const float* colour, const float* moment, const float* length,

@@ -104,11 +104,31 @@ struct ShadeArgs {
 	uint32_t* error;
 };
 
+// The surfaces pass: the first surface through each pixel's centre, as the
+// denoiser's features (FP16 bits; leaf 0xFFFFFFFF where the ray missed).
+struct SurfaceArgs {
+	QueueBuffers rays;    // paths[i] is the pixel of ray i
+	const kdn_hit* hits;
+	const DeviceMaterial* materials;
+	const uint32_t* leafMaterial;
+	uint32_t leafCount;
+	uint16_t* distance;
+	uint16_t* normal;
+	uint16_t* albedo;
+	uint32_t* leaf;
+};
+
 cudaError_t uploadFrameConstants(const FrameConstants& c, cudaStream_t stream);
 cudaError_t launchCamera(const PathBuffers& paths, const QueueBuffers& queue, uint32_t firstPixel, uint32_t n, cudaStream_t stream, int smCount);
 cudaError_t launchShade(const ShadeArgs& args, cudaStream_t stream, int smCount);
 cudaError_t launchLines(const PathBuffers& paths, const ShadowBuffers& shadow, uint32_t capacity, cudaStream_t stream, int smCount);
-cudaError_t launchFold(const PathBuffers& paths, uint32_t firstPixel, uint32_t pixels, uint32_t spp, double* sums, cudaStream_t stream, int smCount);
+// moments (may be null): the denoiser's luminance moment, blended with share alpha
+cudaError_t launchFold(const PathBuffers& paths, uint32_t firstPixel, uint32_t pixels, uint32_t spp, double* sums, double* moments, double alpha, cudaStream_t stream, int smCount);
 cudaError_t launchMeans(const double* sums, uint32_t pixels, double taken, float* out, cudaStream_t stream, int smCount);
+// The denoiser's per-pixel inputs: the luminance moment and the history
+// length (frames blended, at most the still cap).
+cudaError_t launchDenoiseInputs(const double* moments, uint32_t pixels, float history, float* moment, float* length, cudaStream_t stream, int smCount);
+cudaError_t launchSurfaceRays(const QueueBuffers& queue, uint32_t firstPixel, uint32_t n, cudaStream_t stream, int smCount);
+cudaError_t launchSurfaces(const SurfaceArgs& args, uint32_t n, cudaStream_t stream, int smCount);
 
 } // namespace kdn

@@ -200,12 +200,13 @@ __device__ __forceinline__ float plasticShare(const DeviceMaterial& m, float lea
 	return fminf(fmaxf(share, 0.25f), 0.9f);
 }
 
-__device__ __forceinline__ Shading surfaceOf(const DeviceMaterial& m, float3 normal, float3 outgoing, float4 nm, uint32_t medium, const DeviceMaterial* all) {
+// rgb: the albedo at the hit (the material's, or mixed across a blend seam)
+__device__ __forceinline__ Shading surfaceOf(const DeviceMaterial& m, float3 rgb, float3 normal, float3 outgoing, float4 nm, uint32_t medium, const DeviceMaterial* all) {
 	Shading s;
 	s.kind    = m.kind;
 	s.normal  = normal;
 	s.frame   = frameAround(normal);
-	s.albedo  = spectrumOf(m.albedo[0], m.albedo[1], m.albedo[2], nm);
+	s.albedo  = spectrumOf(rgb.x, rgb.y, rgb.z, nm);
 	s.leaving = dotF(normal, outgoing);
 	s.left    = 0.0f;
 	s.share   = 0.0f;

@@ -20,9 +20,15 @@ struct FrameState {
 	DeviceBuffer queuePaths[2], queueRays[2], hits, states, counts;
 	DeviceBuffer shadowRays, shadowPaths, shadowContribution, shadowStates;
 	DeviceBuffer sums, out, materials;
+	// the denoised form: luminance moments, first surfaces, denoiser inputs
+	DeviceBuffer moments, surfDistance, surfNormal, surfAlbedo, surfLeaf, denoiseMoment, denoiseLength, means;
 	uint32_t capacity = 0;
 	int32_t width = 0, height = 0;
 	double taken = 0;
+	// frames in the denoiser's moment history (temporal.cpp:838 heldBlend),
+	// 0 when the last frame kept none
+	float history = 0;
+	bool surfaced = false; // the last frame traced its first surfaces
 	std::vector<cudaEvent_t> events;
 	kdn_frame_stats stats {};
 };
@@ -30,7 +36,7 @@ struct FrameState {
 void Context::releaseFrame() {
 	if (frame == nullptr) return;
 	FrameState& f = *frame;
-	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.hits, &f.states, &f.counts, &f.shadowRays, &f.shadowPaths, &f.shadowContribution, &f.shadowStates, &f.sums, &f.out, &f.materials }) {
+	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.hits, &f.states, &f.counts, &f.shadowRays, &f.shadowPaths, &f.shadowContribution, &f.shadowStates, &f.sums, &f.out, &f.materials, &f.moments, &f.surfDistance, &f.surfNormal, &f.surfAlbedo, &f.surfLeaf, &f.denoiseMoment, &f.denoiseLength, &f.means }) {
 		if (b->ptr) cudaFree(b->ptr);
 		b->ptr   = nullptr;
 		b->bytes = 0;
@@ -195,9 +201,30 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	// pixel sums: fresh unless accumulating onto a frame of the same size
 	const bool fresh = !fr->accumulate || f.width != fr->width || f.height != fr->height || f.sums.ptr == nullptr;
 	if ((s = ctx->ensure(f.sums, size_t(pixels) * 3 * sizeof(double))) != KDN_OK) return s;
+	const bool denoised = (fr->flags & KDN_FRAME_DENOISE) != 0;
+	if (denoised) {
+		const size_t px = pixels;
+		const struct {
+			DeviceBuffer* b;
+			size_t bytes;
+		} wants[] = { { &f.moments, px * 8 }, { &f.surfDistance, px * 2 }, { &f.surfNormal, px * 6 }, { &f.surfAlbedo, px * 6 }, { &f.surfLeaf, px * 4 },
+			          { &f.denoiseMoment, px * 4 }, { &f.denoiseLength, px * 4 }, { &f.means, px * 12 } };
+		for (const auto& w : wants) {
+			if ((s = ctx->ensure(*w.b, w.bytes)) != KDN_OK) return s;
+		}
+	}
 	if (fresh) {
 		if (!ctx->check(cudaMemsetAsync(f.sums.ptr, 0, size_t(pixels) * 3 * sizeof(double), stream), "clear sums")) return KDN_CUDA_ERROR;
-		f.taken = 0;
+		f.taken   = 0;
+		f.history = 0;
+	}
+	// temporal.cpp:831 historyShare: a fresh pixel takes the frame whole, a
+	// held one blends it in by 1 / (length + 1), at least 1 / the still cap
+	constexpr float kStillCap = 256;
+	double alpha              = 1.0;
+	if (denoised) {
+		if (f.history > 0) alpha = std::max(1.0 / (double(std::min(f.history, kStillCap)) + 1.0), 1.0 / double(kStillCap));
+		else if (!ctx->check(cudaMemsetAsync(f.moments.ptr, 0, size_t(pixels) * sizeof(double), stream), "clear moments")) return KDN_CUDA_ERROR;
 	}
 	f.width  = fr->width;
 	f.height = fr->height;
@@ -270,6 +297,44 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	size_t ev = 2;
 	if (!ctx->check(cudaEventRecord(f.events[0], stream), "event")) return KDN_CUDA_ERROR;
 	uint32_t launches = 0;
+	if (denoised) {
+		// core/surfaces.cpp:133 tracedSurfaces: the denoiser's features
+		for (uint32_t first = 0; first < pixels; first += capacity) {
+			const uint32_t n = std::min(capacity, pixels - first);
+			if (!ctx->check(launchSurfaceRays(Q[0], first, n, stream, ctx->smCount), "surface rays kernel")) return KDN_CUDA_ERROR;
+			TraceArgs t;
+			t.world          = ctx->world;
+			t.rays           = Q[0].rays;
+			t.n              = n;
+			t.states         = static_cast<HitState*>(f.states.ptr);
+			t.objectMaterial = static_cast<const uint32_t*>(ctx->objectMaterial.ptr);
+			t.maxSteps       = kMarchSteps;
+			t.counters       = nullptr;
+			t.count          = Q[0].count;
+			t.fetch          = static_cast<uint32_t*>(ctx->fetch.ptr);
+			if (!ctx->check(launchTrace(t, stream, ctx->smCount), "surface trace kernel")) return KDN_CUDA_ERROR;
+			HitArgs h;
+			h.world  = ctx->world;
+			h.rays   = Q[0].rays;
+			h.states = t.states;
+			h.n      = n;
+			h.hits   = static_cast<kdn_hit*>(f.hits.ptr);
+			h.count  = Q[0].count;
+			if (!ctx->check(launchHits(h, stream, ctx->smCount), "surface hit kernel")) return KDN_CUDA_ERROR;
+			SurfaceArgs g;
+			g.rays         = Q[0];
+			g.hits         = h.hits;
+			g.materials    = static_cast<const DeviceMaterial*>(f.materials.ptr);
+			g.leafMaterial = static_cast<const uint32_t*>(ctx->leafMaterial.ptr);
+			g.leafCount    = uint32_t(ctx->leafMaterial.bytes / 4);
+			g.distance     = static_cast<uint16_t*>(f.surfDistance.ptr);
+			g.normal       = static_cast<uint16_t*>(f.surfNormal.ptr);
+			g.albedo       = static_cast<uint16_t*>(f.surfAlbedo.ptr);
+			g.leaf         = static_cast<uint32_t*>(f.surfLeaf.ptr);
+			if (!ctx->check(launchSurfaces(g, n, stream, ctx->smCount), "surfaces kernel")) return KDN_CUDA_ERROR;
+			launches += 4;
+		}
+	}
 	for (uint32_t first = 0; first < pixels; first += chunkPixels) {
 		const uint32_t chunk = std::min(chunkPixels, pixels - first);
 		const uint32_t n     = chunk * spp;
@@ -324,17 +389,49 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 			launches += 5;
 			cur = nxt;
 		}
-		if (!ctx->check(launchFold(P, first, chunk, spp, static_cast<double*>(f.sums.ptr), stream, ctx->smCount), "fold kernel")) return KDN_CUDA_ERROR;
+		if (!ctx->check(launchFold(P, first, chunk, spp, static_cast<double*>(f.sums.ptr), denoised ? static_cast<double*>(f.moments.ptr) : nullptr, alpha, stream, ctx->smCount), "fold kernel")) return KDN_CUDA_ERROR;
 		++launches;
 	}
 	f.taken += double(spp);
+	f.history  = denoised ? std::min(f.history + 1.0f, kStillCap) : 0.0f;
+	f.surfaced = denoised;
 	float* image = out;
 	if (hostOut) {
 		if ((s = ctx->ensure(f.out, size_t(pixels) * 3 * sizeof(float))) != KDN_OK) return s;
 		image = static_cast<float*>(f.out.ptr);
 	}
-	if (!ctx->check(launchMeans(static_cast<const double*>(f.sums.ptr), pixels, f.taken, image, stream, ctx->smCount), "means kernel")) return KDN_CUDA_ERROR;
+	float* means = denoised ? static_cast<float*>(f.means.ptr) : image;
+	if (!ctx->check(launchMeans(static_cast<const double*>(f.sums.ptr), pixels, f.taken, means, stream, ctx->smCount), "means kernel")) return KDN_CUDA_ERROR;
 	++launches;
+	if (denoised) {
+		// the shown frame: a still camera's temporal state (temporal.cpp:797
+		// freshBlend, :835 heldBlend; the colour is the exact running mean)
+		// through the a-trous filter (plugins/reconstruction/atrous/atrous.cpp:513
+		// denoisedFrame)
+		if (!ctx->check(launchDenoiseInputs(static_cast<const double*>(f.moments.ptr), pixels, f.history, static_cast<float*>(f.denoiseMoment.ptr),
+		                                    static_cast<float*>(f.denoiseLength.ptr), stream, ctx->smCount),
+		                "denoise inputs kernel"))
+			return KDN_CUDA_ERROR;
+		kdn_denoise_frame df {};
+		df.width  = fr->width;
+		df.height = fr->height;
+		const V3 lensUp = cross(right, forward);
+		const V3* lens[4] = { &eye, &forward, &right, &lensUp };
+		double* into[4]   = { df.eye, df.forward, df.right, df.up };
+		for (int k = 0; k < 4; ++k) {
+			into[k][0] = lens[k]->x;
+			into[k][1] = lens[k]->y;
+			into[k][2] = lens[k]->z;
+		}
+		df.reach       = std::tan(cam.fov / 2);
+		df.aspect      = double(fr->width) / double(fr->height);
+		df.demodulated = 0;
+		if ((s = denoiseOnDevice(ctx, &df, means, static_cast<const float*>(f.denoiseMoment.ptr), static_cast<const float*>(f.denoiseLength.ptr),
+		                         static_cast<const uint16_t*>(f.surfDistance.ptr), static_cast<const uint16_t*>(f.surfNormal.ptr),
+		                         static_cast<const uint16_t*>(f.surfAlbedo.ptr), static_cast<const uint32_t*>(f.surfLeaf.ptr), image, stream)) != KDN_OK)
+			return s;
+		launches += 8;
+	}
 	if (!ctx->check(cudaEventRecord(f.events[1], stream), "event")) return KDN_CUDA_ERROR;
 	if (hostOut && !ctx->check(cudaMemcpyAsync(out, image, size_t(pixels) * 3 * sizeof(float), cudaMemcpyDeviceToHost, stream), "copy frame")) return KDN_CUDA_ERROR;
 	if (!ctx->check(cudaStreamSynchronize(stream), "kdn_render")) return KDN_CUDA_ERROR;
@@ -383,6 +480,26 @@ kdn_status kdn_frame_stats_get(kdn_ctx* handle, kdn_frame_stats* stats) {
 	std::lock_guard<std::mutex> guard(ctx->lock);
 	if (ctx->frame == nullptr) return ctx->fail(KDN_NOT_READY, "kdn_frame_stats_get: no frame drawn");
 	*stats = ctx->frame->stats;
+	return KDN_OK;
+}
+
+kdn_status kdn_frame_surfaces(kdn_ctx* handle, uint16_t* distance, uint16_t* normal, uint16_t* albedo, uint32_t* leaf) {
+	if (handle == nullptr || !distance || !normal || !albedo || !leaf) return KDN_BAD_ARG;
+	Context* ctx = reinterpret_cast<Context*>(handle);
+	std::lock_guard<std::mutex> guard(ctx->lock);
+	if (ctx->frame == nullptr || !ctx->frame->surfaced) return ctx->fail(KDN_NOT_READY, "kdn_frame_surfaces: the last frame was not drawn with KDN_FRAME_DENOISE");
+	const kdn::FrameState& f = *ctx->frame;
+	const size_t n           = size_t(f.width) * size_t(f.height);
+	if (!ctx->check(cudaSetDevice(ctx->device), "cudaSetDevice")) return KDN_CUDA_ERROR;
+	const struct {
+		void* to;
+		const void* from;
+		size_t bytes;
+	} copies[] = { { distance, f.surfDistance.ptr, n * 2 }, { normal, f.surfNormal.ptr, n * 6 }, { albedo, f.surfAlbedo.ptr, n * 6 }, { leaf, f.surfLeaf.ptr, n * 4 } };
+	for (const auto& c : copies) {
+		if (!ctx->check(cudaMemcpyAsync(c.to, c.from, c.bytes, cudaMemcpyDeviceToHost, ctx->stream), "kdn_frame_surfaces copy")) return KDN_CUDA_ERROR;
+	}
+	if (!ctx->check(cudaStreamSynchronize(ctx->stream), "kdn_frame_surfaces")) return KDN_CUDA_ERROR;
 	return KDN_OK;
 }
 

@@ -17,6 +17,7 @@
 #include "frame.h"
 #include "materials.cuh"
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 namespace kdn {
@@ -356,6 +357,72 @@ __global__ void __launch_bounds__(kBlock) cameraKernel(PathBuffers P, QueueBuffe
 	}
 }
 
+// material.cpp:345 bsdfAt: the leaf's albedo, mixed with the other leaf's by
+// the hit's share where a blend joins two leaves.
+__device__ __forceinline__ const DeviceMaterial& materialOfLeaf(uint32_t leaf, const DeviceMaterial* materials, const uint32_t* leafMaterial, uint32_t leafCount) {
+	const uint32_t m = leaf < leafCount ? leafMaterial[leaf] : 0u;
+	return materials[m < cFrame.materialCount ? m : 0u];
+}
+
+__device__ __forceinline__ float3 albedoAt(const kdn_hit& hit, const DeviceMaterial* materials, const uint32_t* leafMaterial, uint32_t leafCount) {
+	const DeviceMaterial& m = materialOfLeaf(hit.leaf, materials, leafMaterial, leafCount);
+	float3 a                = make_float3(m.albedo[0], m.albedo[1], m.albedo[2]);
+	if (hit.other != kNoLeaf && hit.share > 0.0f) {
+		const DeviceMaterial& o = materialOfLeaf(hit.other, materials, leafMaterial, leafCount);
+		const float s           = hit.share;
+		a = make_float3(a.x * (1.0f - s) + o.albedo[0] * s, a.y * (1.0f - s) + o.albedo[1] * s, a.z * (1.0f - s) + o.albedo[2] * s);
+	}
+	return a;
+}
+
+// ---- the surfaces pass: one ray through each pixel's centre (core/surfaces.cpp:39 surfaceRay) ----
+__global__ void __launch_bounds__(kBlock) surfaceRaysKernel(QueueBuffers Q, uint32_t firstPixel, uint32_t n) {
+	if (blockIdx.x == 0 && threadIdx.x == 0) *Q.count = n;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		const uint32_t pixel = firstPixel + i;
+		const uint32_t x     = pixel % uint32_t(cFrame.width);
+		const uint32_t y     = pixel / uint32_t(cFrame.width);
+		const float u        = 2.0f * (float(x) + 0.5f) / float(cFrame.width) - 1.0f;
+		const float v        = 1.0f - 2.0f * (float(y) + 0.5f) / float(cFrame.height);
+		const float3 heading = normalizedOf(f3(cFrame.forward) + f3(cFrame.right) * (u * cFrame.reach * cFrame.aspect) + f3(cFrame.up) * (v * cFrame.reach));
+		Q.paths[i]           = pixel;
+		Q.rays[i]            = makeRay(f3(cFrame.eye), heading, __int_as_float(0x7f800000), kNoMaterial);
+	}
+}
+
+// trace.cpp:1640 cameraSurface over trace.cpp:1445 vertexSurface: distance
+// from the eye, the normal facing the ray, the albedo and the leaf; a missed
+// ray keeps batch.cpp:46 missedSurface (infinite distance, no leaf).  Stored
+// as the denoiser's FP16 features.
+__global__ void __launch_bounds__(kBlock) surfacesKernel(SurfaceArgs A) {
+	const uint32_t n = *A.rays.count;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		const kdn_hit hit    = A.hits[i];
+		const kdn_ray ray    = A.rays.rays[i];
+		const uint32_t px    = A.rays.paths[i];
+		const bool found     = hit.kind != 0;
+		float3 normal        = make_float3(0.0f, 0.0f, 0.0f);
+		float3 albedo        = make_float3(0.0f, 0.0f, 0.0f);
+		float distance       = __int_as_float(0x7f800000);
+		if (found) {
+			const float3 heading = make_float3(ray.direction[0], ray.direction[1], ray.direction[2]);
+			normal               = make_float3(hit.normal[0], hit.normal[1], hit.normal[2]);
+			if (dot3(normal, heading) >= 0.0f) normal = normal * -1.0f;
+			albedo = albedoAt(hit, A.materials, A.leafMaterial, A.leafCount);
+			const float dx = hit.point[0] - ray.origin[0], dy = hit.point[1] - ray.origin[1], dz = hit.point[2] - ray.origin[2];
+			distance       = sqrtf(dx * dx + dy * dy + dz * dz);
+		}
+		A.distance[px]       = __half_as_ushort(__float2half_rn(distance));
+		A.leaf[px]           = found ? hit.leaf : kNoLeaf;
+		A.normal[3 * px]     = __half_as_ushort(__float2half_rn(normal.x));
+		A.normal[3 * px + 1] = __half_as_ushort(__float2half_rn(normal.y));
+		A.normal[3 * px + 2] = __half_as_ushort(__float2half_rn(normal.z));
+		A.albedo[3 * px]     = __half_as_ushort(__float2half_rn(albedo.x));
+		A.albedo[3 * px + 1] = __half_as_ushort(__float2half_rn(albedo.y));
+		A.albedo[3 * px + 2] = __half_as_ushort(__float2half_rn(albedo.z));
+	}
+}
+
 // ---- K-shade ----
 __global__ void __launch_bounds__(kBlock) shadeKernel(ShadeArgs A) {
 	const uint32_t n = *A.in.count;
@@ -415,7 +482,8 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(ShadeArgs A) {
 				const uint32_t index    = A.paths.sample[p];
 				const bool capped       = depth + 1 >= cFrame.surfaces;
 				const float3 outgoing   = heading * -1.0f;
-				const Shading surf      = surfaceOf(m, normal, outgoing, nm, medium, A.materials);
+				const float3 rgb        = albedoAt(hit, A.materials, A.leafMaterial, A.leafCount);
+				const Shading surf      = surfaceOf(m, rgb, normal, outgoing, nm, medium, A.materials);
 				// aim: offer every lamp, trace one offer drawn by its lane mean
 				if (!m.exact && cFrame.lampCount > 0) {
 					const float u0   = number(stream, index, depth, LightU);
@@ -520,7 +588,10 @@ __global__ void __launch_bounds__(kBlock) linesKernel(PathBuffers P, ShadowBuffe
 }
 
 // ---- K-fold: per pixel, the samples' colours (frame.cpp:273 foldPixels) ----
-__global__ void __launch_bounds__(kBlock) foldKernel(PathBuffers P, uint32_t firstPixel, uint32_t pixels, uint32_t spp, double* sums) {
+// With moments, also the denoiser's history of the luminance moment: this
+// frame's pixel colour (its spp samples) blended in with share alpha
+// (temporal.cpp:848 heldBlend, moment = history * (1 - alpha) + L^2 * alpha).
+__global__ void __launch_bounds__(kBlock) foldKernel(PathBuffers P, uint32_t firstPixel, uint32_t pixels, uint32_t spp, double* sums, double* moments, double alpha) {
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < pixels; i += gridDim.x * blockDim.x) {
 		double r = 0.0, g = 0.0, b = 0.0;
 		for (uint32_t k = 0; k < spp; ++k) {
@@ -534,12 +605,25 @@ __global__ void __launch_bounds__(kBlock) foldKernel(PathBuffers P, uint32_t fir
 		s[0] += r;
 		s[1] += g;
 		s[2] += b;
+		if (moments) {
+			// math/colour.cpp:49 luminanceOf
+			const double l = (0.2126 * r + 0.7152 * g + 0.0722 * b) / double(spp);
+			double& m      = moments[firstPixel + i];
+			m              = m * (1.0 - alpha) + l * l * alpha;
+		}
 	}
 }
 
 __global__ void __launch_bounds__(kBlock) meansKernel(const double* sums, uint32_t pixels, double taken, float* out) {
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < pixels * 3u; i += gridDim.x * blockDim.x) {
 		out[i] = float(sums[i] / taken);
+	}
+}
+
+__global__ void __launch_bounds__(kBlock) denoiseInputsKernel(const double* moments, uint32_t pixels, float history, float* moment, float* length) {
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < pixels; i += gridDim.x * blockDim.x) {
+		moment[i] = float(moments[i]);
+		length[i] = history;
 	}
 }
 
@@ -569,8 +653,23 @@ cudaError_t launchLines(const PathBuffers& paths, const ShadowBuffers& shadow, u
 	return cudaGetLastError();
 }
 
-cudaError_t launchFold(const PathBuffers& paths, uint32_t firstPixel, uint32_t pixels, uint32_t spp, double* sums, cudaStream_t stream, int smCount) {
-	foldKernel<<<gridFor(pixels, smCount), kBlock, 0, stream>>>(paths, firstPixel, pixels, spp, sums);
+cudaError_t launchFold(const PathBuffers& paths, uint32_t firstPixel, uint32_t pixels, uint32_t spp, double* sums, double* moments, double alpha, cudaStream_t stream, int smCount) {
+	foldKernel<<<gridFor(pixels, smCount), kBlock, 0, stream>>>(paths, firstPixel, pixels, spp, sums, moments, alpha);
+	return cudaGetLastError();
+}
+
+cudaError_t launchDenoiseInputs(const double* moments, uint32_t pixels, float history, float* moment, float* length, cudaStream_t stream, int smCount) {
+	denoiseInputsKernel<<<gridFor(pixels, smCount), kBlock, 0, stream>>>(moments, pixels, history, moment, length);
+	return cudaGetLastError();
+}
+
+cudaError_t launchSurfaceRays(const QueueBuffers& queue, uint32_t firstPixel, uint32_t n, cudaStream_t stream, int smCount) {
+	surfaceRaysKernel<<<gridFor(n, smCount), kBlock, 0, stream>>>(queue, firstPixel, n);
+	return cudaGetLastError();
+}
+
+cudaError_t launchSurfaces(const SurfaceArgs& args, uint32_t n, cudaStream_t stream, int smCount) {
+	surfacesKernel<<<gridFor(n, smCount), kBlock, 0, stream>>>(args);
 	return cudaGetLastError();
 }
 

@@ -228,6 +228,67 @@ def render_band(scene, width: int, height: int, spp: int, surfaces: int, seed: i
     return sums
 
 
+def lens_of(scene, width: int, height: int) -> np.ndarray:
+    """core/camera.cpp:9 lensOf: eye, forward, right, up (3 each), reach,
+    aspect, in double."""
+    cam = scene.camera
+    eye = np.asarray(cam["eye"], np.float64)
+    forward = np.asarray(cam["target"], np.float64) - eye
+    forward /= np.sqrt(forward @ forward)
+    right = np.cross(forward, np.asarray(cam["up"], np.float64))
+    right /= np.sqrt(right @ right)
+    up = np.cross(right, forward)
+    return np.concatenate([eye, forward, right, up, [np.tan(float(cam["fov"]) / 2), width / height]])
+
+
+def traced_surfaces(scene, width: int, height: int, build: dict | None = None) -> dict:
+    """core/surfaces.cpp:133 tracedSurfaces: one ray through each pixel's
+    centre (core/camera.cpp:34 filmDirection), the first surface's distance
+    from the eye, normal facing the ray, albedo (mixed across a blend seam,
+    material.cpp:345 bsdfAt) and leaf; a missed ray keeps batch.cpp:46
+    missedSurface.  Pixel-major arrays of width * height."""
+    build = build or dict(min_depth=6, max_depth=10, split_steps=96)
+    tree = _octree_for(scene, build)
+    lens = lens_of(scene, width, height)
+    eye, forward, right, up, reach, aspect = lens[0:3], lens[3:6], lens[6:9], lens[9:12], lens[12], lens[13]
+    y, x = np.mgrid[0:height, 0:width]
+    u = 2 * (x.ravel() + 0.5) / width - 1
+    v = 1 - 2 * (y.ravel() + 0.5) / height
+    heading = forward[None, :] + right[None, :] * (u * reach * aspect)[:, None] + up[None, :] * (v * reach)[:, None]
+    heading /= np.sqrt((heading * heading).sum(1))[:, None]
+    rays = np.zeros(width * height, RAY_DTYPE)
+    rays["origin"] = eye.astype(np.float32)
+    rays["direction"] = heading.astype(np.float32)
+    rays["far"] = np.inf
+    rays["inside"] = 0
+    rays["within"] = 0xFFFFFFFF
+    hits = tree.trace(rays)
+    found = hits["kind"] != 0
+    normal = hits["normal"].astype(np.float64)
+    facing = (normal * rays["direction"].astype(np.float64)).sum(1) >= 0
+    normal[facing] *= -1
+    normal[~found] = 0
+    albedo_of = np.asarray(scene.materials["albedo"], np.float64)
+    leaf_material = np.asarray(scene.leaf_material, np.int64)
+    material_count = len(albedo_of)
+
+    def material(leaf):
+        m = np.where(leaf != 0xFFFFFFFF, leaf_material[np.where(leaf != 0xFFFFFFFF, leaf, 0)], 0)
+        return np.where(m < material_count, m, 0)
+
+    albedo = albedo_of[material(hits["leaf"].astype(np.int64))]
+    share = hits["share"].astype(np.float64)
+    mixed = (hits["other"] != 0xFFFFFFFF) & (share > 0)
+    other = albedo_of[material(hits["other"].astype(np.int64))]
+    albedo = np.where(mixed[:, None], albedo * (1 - share[:, None]) + other * share[:, None], albedo)
+    albedo[~found] = 0
+    delta = hits["point"].astype(np.float32) - rays["origin"]
+    distance = np.sqrt((delta * delta).sum(1, dtype=np.float32)).astype(np.float32)
+    distance[~found] = np.inf
+    leaf = np.where(found, hits["leaf"], 0xFFFFFFFF).astype(np.uint32)
+    return {"distance": distance, "normal": normal, "albedo": albedo, "leaf": leaf}
+
+
 def denoise(width: int, height: int, demodulated: int, lens, colour, moment, length, distance, normal, leaf, albedo) -> np.ndarray:
     """The oracle's a-trous denoiser over one frame's feature buffers."""
     L = lib()

@@ -370,6 +370,7 @@ typedef struct shading {
 	v3 normal;
 	basis frame;
 	spec albedo, twice, within, beyond;
+	double rgb[3]; /* the albedo at the hit, blended across a shared seam */
 	double leaving, left, share, masking;
 	int parted;
 } shading;
@@ -383,13 +384,14 @@ static spec lane_indices(const kp_material* m, const lanes* w) {
 	return s;
 }
 
-static shading shading_of(const kp_material* m, const kp_material* all, v3 n, v3 out, const lanes* w, uint32_t medium) {
+static shading shading_of(const kp_material* m, const double* rgb, const kp_material* all, v3 n, v3 out, const lanes* w, uint32_t medium) {
 	shading s;
 	memset(&s, 0, sizeof s);
 	s.m = m;
 	s.normal = n;
 	s.frame = basis_around(n);
-	s.albedo = spectrum(m->albedo, w);
+	for (int c = 0; c < 3; ++c) s.rgb[c] = rgb[c];
+	s.albedo = spectrum(s.rgb, w);
 	s.leaving = dotv(n, out);
 	s.within = flat(1);
 	s.beyond = flat(1);
@@ -406,7 +408,7 @@ static shading shading_of(const kp_material* m, const kp_material* all, v3 n, v3
 		if (m->kind == 2) {
 			/* material.cpp:567 metalTwice over microfacet.cpp:116 averagedFresnel */
 			double avg[3];
-			for (int c = 0; c < 3; ++c) avg[c] = m->albedo[c] + (1 - m->albedo[c]) * (1.0 / 21);
+			for (int c = 0; c < 3; ++c) avg[c] = s.rgb[c] + (1 - s.rgb[c]) * (1.0 / 21);
 			const spec a = spectrum(avg, w);
 			for (int k = 0; k < 4; ++k) s.twice.v[k] = a.v[k] * a.v[k] * m->escape_average / (1 - a.v[k] * (1 - m->escape_average));
 		}
@@ -458,7 +460,7 @@ static response respond(const shading* s, v3 out, v3 in, const lanes* w) {
 		/* material.cpp:649 viewedMetal, microfacet.cpp:111 schlickOf */
 		const double rest = pow(clampd(1 - onto, 0, 1), 5.0);
 		double face[3];
-		for (int c = 0; c < 3; ++c) face[c] = m->albedo[c] + (1 - m->albedo[c]) * rest;
+		for (int c = 0; c < 3; ++c) face[c] = s->rgb[c] + (1 - s->rgb[c]) * rest;
 		r.value = sadd(sscale(spectrum(face, w), facets), sscale(s->twice, lost));
 	} else {
 		/* material.cpp:661 viewedPlastic */
@@ -575,6 +577,22 @@ static void sky_colour(const kp_view* view, v3 d, double out[3]) {
 	for (int c = 0; c < 3; ++c) out[c] = view->horizon[c] * (1 - share) + far[c] * share;
 }
 
+/* material.cpp:345 bsdfAt: the leaf's albedo, mixed with the other leaf's by
+ * the hit's share where a blend joins two leaves */
+static const kp_material* material_of_leaf(const job* J, uint32_t leaf) {
+	const uint32_t material = leaf != 0xFFFFFFFFu ? J->leaf_material[leaf] : 0;
+	return &J->materials[material < J->view->material_count ? material : 0];
+}
+
+static void albedo_at(const job* J, const kp_hit* hit, double rgb[3]) {
+	const kp_material* m = material_of_leaf(J, hit->leaf);
+	for (int c = 0; c < 3; ++c) rgb[c] = m->albedo[c];
+	if (hit->other != 0xFFFFFFFFu && hit->share > 0) {
+		const kp_material* o = material_of_leaf(J, hit->other);
+		for (int c = 0; c < 3; ++c) rgb[c] = rgb[c] * (1 - (double) hit->share) + o->albedo[c] * (double) hit->share;
+	}
+}
+
 static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index, double rgb[3]) {
 	const kp_view* V = J->view;
 	const uint64_t stream = J->seed_mix ^ kp_mixed_bits(((uint64_t) (uint32_t) x << 32) | (uint64_t) (uint32_t) y);
@@ -623,7 +641,9 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 		const double lift = BIAS + 2 * 1e-6;
 		const int capped = depth + 1 >= V->surfaces;
 		const v3 out = scl(heading, -1);
-		const shading s = shading_of(m, J->materials, normal, out, &w, medium);
+		double rgb[3];
+		albedo_at(J, &hit, rgb);
+		const shading s = shading_of(m, rgb, J->materials, normal, out, &w, medium);
 		if (!m->exact && V->lamp_count > 0) {
 			const double u0 = number(stream, index, depth, LIGHT_U), v0 = number(stream, index, depth, LIGHT_V);
 			double choice = number(stream, index, depth, PICK);
