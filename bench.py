@@ -5,7 +5,9 @@ workload, beside the CPU renderer timed on this machine's host cores.
 One step is one frame of the config-2 scene (4096 primitives in 512 CSG
 groups with floor-based repetition, 40% matte / 40% GGX metal / 20%
 dispersive glass, two quad lights and a constant 6500 K sky), 1920x1080 at
-64 samples a pixel, paths of at most 16 surfaces: 132.7 M samples a step.
+64 samples a pixel, paths of at most 16 surfaces: 132.7 M samples a step,
+shown through the a-trous denoiser (pixel-centre surfaces as FP16
+features, a still camera's first frame of temporal history).
 The scene is the reference renderer's own compilation of the seeded scene
 text (tests/golden/scenes/c2.npz); the cut octree is built once before the
 timed region and reported apart (build_s), as the reference reports its
@@ -41,6 +43,7 @@ sys.path.insert(0, ROOT)
 METRIC = "Msamples/s @1080p vs CPU; equal-time relMSE guided vs plain; p50/p99 latency"
 SCENE = os.path.join(ROOT, "tests", "golden", "scenes", "c2.npz")
 WIDTH, HEIGHT, SPP, SURFACES = 1920, 1080, 64, 16
+DENOISE = True  # the a-trous denoiser on the frame's FP16 features
 BUILD = dict(min_depth=7, max_depth=10, split_steps=96)
 
 
@@ -176,21 +179,24 @@ def run_gpu(args) -> None:
     stats_world = b.world_stats()
     seed = int(scene.render["seed"])
     for k in range(args.warmup):
-        b.render(WIDTH, HEIGHT, SPP, surfaces=SURFACES, seed=seed + 1000 + k)
+        b.render(WIDTH, HEIGHT, SPP, surfaces=SURFACES, seed=seed + 1000 + k, denoise=DENOISE)
     if dist:
         dist.barrier()
-    device_ms, trace_ms, launches, march, program = 0.0, 0.0, 0, 0, 0
+    device_ms, trace_ms, launches, march, program, segments, longest, capped = 0.0, 0.0, 0, 0, 0, 0, 0, 0
     with Clocks(local) as clocks:
         wall0 = time.perf_counter()
         for k in range(args.steps):
             b.flush_l2()
-            b.render(WIDTH, HEIGHT, SPP, surfaces=SURFACES, seed=seed + k)
+            b.render(WIDTH, HEIGHT, SPP, surfaces=SURFACES, seed=seed + k, denoise=DENOISE)
             st = b.frame_stats()
             device_ms += st.total_ms
             trace_ms += st.trace_ms
             launches += st.launches
             march += st.march_steps
             program += st.program_steps
+            segments += st.segments
+            longest = max(longest, st.longest_march)
+            capped += st.capped_rays
         wall = time.perf_counter() - wall0
     if dist:
         t = np.array([device_ms])
@@ -213,7 +219,7 @@ def run_gpu(args) -> None:
         for n in per_frame:
             if n in blocks:
                 b.upload(n, blocks[n])
-        img = b.render(WIDTH, HEIGHT, SPP, surfaces=SURFACES, seed=seed + k)
+        img = b.render(WIDTH, HEIGHT, SPP, surfaces=SURFACES, seed=seed + k, denoise=DENOISE)
     e_dt = time.perf_counter() - e0
     e2e = samples * world / e_dt / 1e6
 
@@ -228,7 +234,8 @@ def run_gpu(args) -> None:
         "metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": device_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded config-2 scene compiled by the reference renderer)",
-        "config": {"workload": "config-2 plain: 4096 primitives, 1920x1080, 64 spp, 16 surfaces, FP32, no denoiser",
+        "config": {"workload": "config-2: 4096 primitives, 1920x1080, 64 spp, 16 surfaces, FP32, a-trous denoiser on FP16 features"
+                                + ("" if DENOISE else " (off)"),
                    "world": stats_world, "build_s": build_s, "l2": "512 MiB written before every timed frame",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
@@ -236,6 +243,9 @@ def run_gpu(args) -> None:
         "clocks": clocks.summary(),
         "wall_s": wall,
         "march_steps_per_sample": march / samples,
+        "segments_per_sample": segments / samples,
+        "longest_march": int(longest),
+        "capped_rays": int(capped),
         "program_steps_per_sample": program / samples,
         "trace_share": trace_ms / device_ms if device_ms else None,
     }

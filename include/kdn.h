@@ -188,7 +188,8 @@ typedef struct kdn_frame_stats {
 	uint64_t march_steps;
 	uint64_t program_steps; /* program steps run by the trace kernel */
 	uint32_t launches;
-	uint32_t pad_;
+	uint32_t longest_march; /* the most march steps one ray took */
+	uint64_t capped_rays;   /* rays that ran out of march steps (65536) */
 } kdn_frame_stats;
 
 const char* kdn_status_string(kdn_status status);

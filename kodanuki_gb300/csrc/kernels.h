@@ -29,7 +29,7 @@ struct TraceArgs {
 	HitState* states;
 	const uint32_t* objectMaterial; // material of each object's first leaf
 	uint32_t maxSteps;
-	unsigned long long* counters;   // [0] march steps, [1] program steps
+	unsigned long long* counters;   // [0] march steps, [1] program steps, [2] longest march, [3] capped rays, [4] rays
 	const uint32_t* count;          // if set, the number of rays is read here on the device
 	uint32_t* fetch;                // the next ray to take; launchTrace zeroes it
 };

@@ -448,6 +448,9 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	cudaMemcpy(host, ctx->counters.ptr, sizeof(host), cudaMemcpyDeviceToHost);
 	st.march_steps   = host[0];
 	st.program_steps = host[1];
+	st.longest_march = uint32_t(host[2]);
+	st.capped_rays   = host[3];
+	st.segments      = host[4];
 	st.launches      = launches;
 	st.other_ms      = st.total_ms - st.trace_ms;
 	f.stats          = st;

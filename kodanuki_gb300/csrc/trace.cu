@@ -165,7 +165,8 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 	const DeviceWorld& w  = args.world;
 	const uint32_t stride = blockDim.x;
 	float* slots          = slotMemory + threadIdx.x;
-	unsigned long long marchSteps = 0, programSteps = 0;
+	unsigned long long marchSteps = 0, programSteps = 0, traced = 0, capped = 0;
+	uint32_t longest = 0;
 	const uint32_t n = args.count ? *args.count : args.n;
 	const unsigned lane = threadIdx.x & 31u;
 
@@ -186,6 +187,14 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 	float p[3]  = { 0.0f, 0.0f, 0.0f };
 	float least = 0.0f, second = 0.0f, nearest = 0.0f;
 	uint32_t index = 0;
+	// a ray ends: its state, the step counts, and the next ray
+	auto done = [&](HitState h) {
+		args.states[ray] = h;
+		marchSteps += h.steps;
+		longest = max(longest, h.steps);
+		capped += h.steps >= args.maxSteps ? 1u : 0u;
+		mode = Fetch;
+	};
 
 	for (;;) {
 		// take new rays, one atomic a warp
@@ -221,8 +230,7 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 					step      = 0;
 					cell.leaf = kNoLeaf;
 					if (up < lo) {
-						args.states[ray] = HitState { 0, 0.0f, kNoLeaf, 0, 0 };
-						mode             = Fetch;
+						done(HitState { 0, 0.0f, kNoLeaf, 0, 0 });
 					} else {
 						mode = Locating;
 					}
@@ -235,9 +243,7 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 		if (mode == Locating) {
 			for (;;) {
 				if (!(step < args.maxSteps && t <= up)) {
-					marchSteps += step;
-					args.states[ray] = HitState { 0, 0.0f, kNoLeaf, 0, step };
-					mode             = Fetch;
+					done(HitState { 0, 0.0f, kNoLeaf, 0, step });
 					break;
 				}
 				for (int a = 0; a < 3; ++a) p[a] = o[a] + d[a] * t;
@@ -301,9 +307,7 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 							const float big  = fmaxf(fabsf(p[0]), fmaxf(fabsf(p[1]), fabsf(p[2])));
 							const bool tied  = second - least <= 2e-6f * (1.0f + big);
 							const uint32_t winner = tied ? winnerAt(w, o, d, t, f, slots, stride) : index;
-							args.states[ray] = HitState { 1, t, first, winner, step };
-							marchSteps += step;
-							mode = Fetch;
+							done(HitState { 1, t, first, winner, step });
 						} else {
 							t = fminf(t + least, fmaxf(exitT, t) + nudge(t));
 						}
@@ -318,16 +322,12 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 						Located beyond    = cell;
 						const Field past  = fieldAt(w, o, d, inv, t + inset, slots, stride, programSteps, beyond);
 						if (past.empty || past.least > 0.0f) {
-							args.states[ray] = HitState { 1, t, first, winnerAt(w, o, d, t, f, slots, stride), step };
-							marchSteps += step;
-							mode = Fetch;
+							done(HitState { 1, t, first, winnerAt(w, o, d, t, f, slots, stride), step });
 						} else {
 							const GpuProgram g = w.programs[past.first + past.index];
 							// a solid of another material than the one the ray is in: stop there
 							if (args.objectMaterial != nullptr && args.objectMaterial[g.object] != medium) {
-								args.states[ray] = HitState { 2, t, past.first, past.index, step };
-								marchSteps += step;
-								mode = Fetch;
+								done(HitState { 2, t, past.first, past.index, step });
 							} else {
 								t += inset;
 							}
@@ -344,10 +344,16 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 		for (int o = 16; o > 0; o >>= 1) {
 			marchSteps += __shfl_down_sync(0xFFFFFFFFu, marchSteps, o);
 			programSteps += __shfl_down_sync(0xFFFFFFFFu, programSteps, o);
+			traced += __shfl_down_sync(0xFFFFFFFFu, traced, o);
+			capped += __shfl_down_sync(0xFFFFFFFFu, capped, o);
+			longest = max(longest, __shfl_down_sync(0xFFFFFFFFu, longest, o));
 		}
 		if ((threadIdx.x & 31) == 0) {
 			atomicAdd(&args.counters[0], marchSteps);
 			atomicAdd(&args.counters[1], programSteps);
+			atomicMax(&args.counters[2], (unsigned long long) longest);
+			atomicAdd(&args.counters[3], capped);
+			atomicAdd(&args.counters[4], traced);
 		}
 	}
 }

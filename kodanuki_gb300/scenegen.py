@@ -142,8 +142,8 @@ def scene_config2(seed: int = 1, width: int = 1920, height: int = 1080, samples:
     rng = random.Random(seed)
     out = [_header(width, height, samples, surfaces, seed, [0.5, -15.0, 6.5], [0.0, 0.0, -0.5], 0.8)]
     out.append(_sky(blackbody_rgb(6500.0, 0.25)))
-    out.append(_quad([-4.0, -3.0, 7.0], [3.0, 0.0, 0.0], [0.0, 2.0, 0.0], blackbody_rgb(5000.0, 120.0)))
-    out.append(_quad([2.0, 1.0, 6.0], [2.0, 0.0, 0.0], [0.0, 2.0, 0.0], blackbody_rgb(3500.0, 80.0)))
+    out.append(_quad([-4.0, -1.0, 7.0], [3.0, 0.0, 0.0], [0.0, -2.0, 0.0], blackbody_rgb(5000.0, 120.0)))
+    out.append(_quad([2.0, 3.0, 6.0], [2.0, 0.0, 0.0], [0.0, -2.0, 0.0], blackbody_rgb(3500.0, 80.0)))
     out.append("paint(matte([0.45, 0.45, 0.45])) plane([0, 0, 1], -3);\n\n")
     mats = []
     for i in range(groups):
