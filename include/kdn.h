@@ -157,7 +157,7 @@ typedef struct kdn_build_options {
 /* One frame of fixed-count samples (stopping/fixed_count). */
 typedef struct kdn_frame {
 	int32_t width, height;
-	int32_t samples;  /* samples per pixel drawn by this call */
+	int32_t samples;  /* samples per pixel drawn by this call, 1 .. 2^20 */
 	int32_t surfaces; /* render.surfaces: the most surfaces a path stands on */
 	int32_t seed;     /* render.seed */
 	uint32_t first;   /* sample index of this call's first sample of every pixel */

@@ -142,6 +142,8 @@ kdn_status Context::build(const BuildOptions& options) {
 	}
 	world.leaf_count     = uint32_t(flat.leaves.size());
 	world.material_count = uint32_t(block<kdn_material>("looks.materials").size());
+	world.marchSlots     = 1;
+	for (const GpuProgram& g : flat.programs) world.marchSlots = std::max<uint32_t>(world.marchSlots, g.marchSlots);
 	built                = true;
 	return KDN_OK;
 }

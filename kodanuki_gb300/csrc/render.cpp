@@ -147,6 +147,25 @@ using kdn::FrameState;
 
 namespace {
 
+// Device bytes one path of a chunk holds (the buffers ensureFrame sizes).
+// pixel, sample, drawn, state; throughput, radiance, nanometres, density,
+// from; the two queues' path indices and rays; hits and hit states; the
+// shadow lines' rays, path indices, contributions and hit states.
+constexpr size_t kPathBytes = 4 * 4 + 5 * 16 + 2 * 4 + 2 * sizeof(kdn_ray) + sizeof(kdn_hit) + sizeof(kdn::HitState) + sizeof(kdn_ray) + 4 + 16 + sizeof(kdn::HitState);
+static_assert(kPathBytes == 328, "path bytes");
+
+// The paths one chunk of a frame holds.  The whole frame where the device
+// has room for it (at most 2^28 paths, half the free memory): every launch
+// then has the frame's rays to spread over the GPU, and the slow rays of a
+// launch hold back one lane each rather than a small chunk's whole tail.
+uint64_t chunkPaths(Context* ctx, uint64_t framePaths) {
+	size_t freeBytes = 0, totalBytes = 0;
+	if (cudaMemGetInfo(&freeBytes, &totalBytes) != cudaSuccess) freeBytes = 0;
+	const uint64_t held = ctx->frame ? uint64_t(ctx->frame->capacity) * kPathBytes : 0;
+	const uint64_t room = (uint64_t(freeBytes) + held) / 2 / kPathBytes;
+	return std::min<uint64_t>(framePaths, std::min<uint64_t>(uint64_t(1) << 28, std::max<uint64_t>(room, uint64_t(1) << 20)));
+}
+
 kdn_status ensureFrame(Context* ctx, uint32_t capacity) {
 	if (ctx->frame == nullptr) ctx->frame = new FrameState();
 	FrameState& f = *ctx->frame;
@@ -176,6 +195,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	if (!ctx->built) return ctx->fail(KDN_NOT_READY, "kdn_render: no world built (kdn_build)");
 	if (fr->width <= 0 || fr->height <= 0 || fr->samples <= 0 || fr->surfaces <= 0 || fr->surfaces > 255) return ctx->fail(KDN_BAD_ARG, "kdn_render: width, height, samples and surfaces (1..255) must be positive");
 	if (uint64_t(fr->width) * uint64_t(fr->height) > (uint64_t(1) << 26)) return ctx->fail(KDN_BAD_ARG, "kdn_render: frame larger than 2^26 pixels");
+	if (fr->samples > (1 << 20)) return ctx->fail(KDN_BAD_ARG, "kdn_render: more than 2^20 samples a pixel in one call (accumulate over calls)");
 	if (!ctx->has("shot.camera") || !ctx->has("looks.materials")) return ctx->fail(KDN_NOT_READY, "kdn_render: the shot.camera and looks.materials blocks are needed");
 	if (!ctx->check(cudaSetDevice(ctx->device), "cudaSetDevice")) return KDN_CUDA_ERROR;
 	const kdn_camera cam                     = ctx->block<kdn_camera>("shot.camera")[0];
@@ -192,8 +212,8 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	}
 	const uint32_t pixels = uint32_t(fr->width) * uint32_t(fr->height);
 	const uint32_t spp    = uint32_t(fr->samples);
-	const uint32_t want   = uint32_t(std::min<uint64_t>(uint64_t(pixels) * spp, uint64_t(1) << 22));
-	const uint32_t chunkPixels = std::max<uint32_t>(1, want / spp);
+	const uint64_t want        = chunkPaths(ctx, uint64_t(pixels) * spp);
+	const uint32_t chunkPixels = uint32_t(std::max<uint64_t>(1, want / spp));
 	const uint32_t capacity    = chunkPixels * spp;
 	kdn_status s = ensureFrame(ctx, capacity);
 	if (s != KDN_OK) return s;

@@ -18,6 +18,9 @@ namespace kdn {
 namespace {
 
 constexpr int kTraceBlock = 128;
+// program steps a thread runs a turn of the step machine before the warp
+// looks again for threads that need a new ray or a new cell
+constexpr uint32_t kStepsPerTurn = 4;
 
 __device__ __forceinline__ float slopeOf(float part) {
 	const float tiny = 1e-12f;
@@ -183,6 +186,7 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 	// the cell being evaluated: its run of kept programs and the one in hand
 	uint32_t first = 0, count = 0, k = 0;
 	const GpuStep* code = nullptr;
+	GpuStep next {};
 	uint32_t pc = 0, length = 0, resultSlot = 0;
 	float p[3]  = { 0.0f, 0.0f, 0.0f };
 	float least = 0.0f, second = 0.0f, nearest = 0.0f;
@@ -210,6 +214,7 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 				if (ray >= n) {
 					mode = Finished;
 				} else {
+					++traced;
 					const kdn_ray r = args.rays[ray];
 					for (int a = 0; a < 3; ++a) {
 						o[a]   = r.origin[a];
@@ -267,15 +272,21 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 				length     = g.marchCount;
 				resultSlot = g.marchSlot;
 				pc         = 0;
+				next       = code[0];
 				mode       = Evaluating;
 				break;
 			}
 		}
 
-		// one program step
+		// a few program steps; each step's code is loaded a step ahead
 		if (mode == Evaluating) {
-			runSlotStep(code[pc], slots, stride, p);
-			if (++pc == length) {
+			for (uint32_t u = 0; u < kStepsPerTurn; ++u) {
+				const GpuStep s = next;
+				if (pc + 1 < length) next = code[pc + 1];
+				runSlotStep(s, slots, stride, p);
+				if (++pc == length) break;
+			}
+			if (pc == length) {
 				const float v = slots[resultSlot * stride];
 				programSteps += length;
 				if (v < least) {
@@ -292,6 +303,7 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 					length     = g.marchCount;
 					resultSlot = g.marchSlot;
 					pc         = 0;
+					next       = code[0];
 				} else {
 					// the march step: stop on the surface or go on by the field
 					const float tol = tolerance(p);
@@ -435,13 +447,18 @@ __global__ void __launch_bounds__(kTraceBlock) hitKernel(HitArgs args) {
 
 cudaError_t launchTrace(const TraceArgs& args, cudaStream_t stream, int smCount) {
 	if (args.n == 0) return cudaSuccess;
-	const size_t shared = size_t(kMaxSlots) * kTraceBlock * sizeof(float);
+	// a thread's register slots in shared memory, as many as the world's
+	// largest march program uses: the rest of the SM's shared memory stays
+	// L1 for the programs' code
+	const size_t shared = size_t(std::max<uint32_t>(1, std::min(args.world.marchSlots, kMaxSlots))) * kTraceBlock * sizeof(float);
 	// persistent blocks: as many as fit on the SMs at once, fewer for a small launch
-	static int resident = 0;
-	if (resident == 0) {
+	static thread_local size_t sizedFor = 0;
+	static thread_local int resident    = 0;
+	if (sizedFor != shared) {
 		int perSm = 0;
 		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, traceKernel, kTraceBlock, shared) != cudaSuccess || perSm < 1) perSm = 1;
 		resident = perSm;
+		sizedFor = shared;
 	}
 	const uint64_t wanted = (uint64_t(args.n) + kTraceBlock - 1) / kTraceBlock;
 	const uint32_t blocks = uint32_t(std::max<uint64_t>(1, std::min<uint64_t>(wanted, uint64_t(smCount) * uint64_t(resident))));

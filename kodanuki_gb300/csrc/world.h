@@ -89,6 +89,7 @@ struct DeviceWorld {
 	float size[3];
 	uint32_t leaf_count;
 	uint32_t material_count;
+	uint32_t marchSlots; // the most slots a march-form program uses: the trace kernel's shared memory a thread
 };
 
 } // namespace kdn
