@@ -44,6 +44,9 @@ METRIC = "Msamples/s @1080p vs CPU; equal-time relMSE guided vs plain; p50/p99 l
 SCENE = os.path.join(ROOT, "tests", "golden", "scenes", "c2.npz")
 WIDTH, HEIGHT, SPP, SURFACES = 1920, 1080, 64, 16
 DENOISE = True  # the a-trous denoiser on the frame's FP16 features
+# DRAM bytes the trace kernel moves a ray (read + write), from the ncu
+# capture of one launch of known rays (profiles/trace_kernel_ncu.md)
+TRACE_DRAM_BYTES_PER_RAY = None
 BUILD = dict(min_depth=7, max_depth=10, split_steps=96)
 
 
@@ -182,7 +185,7 @@ def run_gpu(args) -> None:
         b.render(WIDTH, HEIGHT, SPP, surfaces=SURFACES, seed=seed + 1000 + k, denoise=DENOISE)
     if dist:
         dist.barrier()
-    device_ms, trace_ms, launches, march, program, segments, longest, capped = 0.0, 0.0, 0, 0, 0, 0, 0, 0
+    device_ms, trace_ms, launches, march, program, segments, longest, capped, trace_launches = 0.0, 0.0, 0, 0, 0, 0, 0, 0, 0
     with Clocks(local) as clocks:
         wall0 = time.perf_counter()
         for k in range(args.steps):
@@ -197,6 +200,7 @@ def run_gpu(args) -> None:
             segments += st.segments
             longest = max(longest, st.longest_march)
             capped += st.capped_rays
+            trace_launches += st.trace_launches
         wall = time.perf_counter() - wall0
     if dist:
         t = np.array([device_ms])
@@ -223,13 +227,13 @@ def run_gpu(args) -> None:
     e_dt = time.perf_counter() - e0
     e2e = samples * world / e_dt / 1e6
 
-    # roofline of the dominant kernel (the sphere-trace kernel, FP32 SIMT
-    # work): algorithmic bytes are the rays it reads and the end states it
-    # writes; the world it walks is L2-resident.
+    # roofline of the dominant kernel, the sphere-trace kernel: its
+    # algorithmic bytes are the rays it reads (36 B) and the end states it
+    # writes (20 B); the world it walks (programs, octree) stays in L2.
     pk = peaks()
-    trace_launches = 2 * SURFACES * ((WIDTH * HEIGHT * SPP + (1 << 22) - 1) // (1 << 22)) * args.steps
-    segments_bytes = 0
-    rays_per_frame = None
+    ray_bytes = 36 + 20
+    achieved_gbs = segments * ray_bytes / (trace_ms / 1e3) / 1e9 if trace_ms else None
+    rays_per_launch = segments / trace_launches if trace_launches else None
     line = {
         "metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": device_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -250,11 +254,19 @@ def run_gpu(args) -> None:
         "trace_share": trace_ms / device_ms if device_ms else None,
     }
     if rank == 0:
-        achieved_flops = (program * 1.0 + march * 30.0) / (trace_ms / 1e3) / 1e12 if trace_ms else None
-        line["roofline"] = {"bound": "hbm", "achieved": None, "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": None, "traffic": None,
-                            "note": "sphere-trace kernel: FP32 SIMT-bound, see roofline_simt"}
-        line["roofline_simt"] = {"achieved_tflops": achieved_flops, "peak_tflops": 152 * 128 * 2 * 2.07e9 / 1e12,
-                                 "unit": "TFLOP/s FP32 (1 flop a program step, 30 a march step)"}
+        line["roofline"] = {
+            "bound": "hbm", "achieved": achieved_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved_gbs / pk["hbm_gbs"] if achieved_gbs else None,
+            "traffic": TRACE_DRAM_BYTES_PER_RAY * rays_per_launch if (rays_per_launch and TRACE_DRAM_BYTES_PER_RAY) else None,
+            "kernel": "traceKernel", "peak_source": pk["source"],
+            "algorithmic": f"{ray_bytes} B a ray (ray in, end state out) x {rays_per_launch:.0f} rays a launch" if rays_per_launch else None,
+            "note": "the trace kernel is bound by FP32 issue and latency, not HBM; traffic scaled by rays from the ncu capture in profiles/",
+        }
+        line["trace_rates"] = {
+            "rays_per_s": segments / (trace_ms / 1e3) if trace_ms else None,
+            "program_steps_per_s": program / (trace_ms / 1e3) if trace_ms else None,
+            "march_steps_per_s": march / (trace_ms / 1e3) if trace_ms else None,
+        }
         if args.no_cpu:
             line["cpu_baseline"] = None
         else:

@@ -190,6 +190,8 @@ typedef struct kdn_frame_stats {
 	uint32_t launches;
 	uint32_t longest_march; /* the most march steps one ray took */
 	uint64_t capped_rays;   /* rays that ran out of march steps (65536) */
+	uint32_t trace_launches; /* launches of the sphere-trace kernel in trace_ms */
+	uint32_t pad_;
 } kdn_frame_stats;
 
 const char* kdn_status_string(kdn_status status);

@@ -63,7 +63,8 @@ FRAME_DENOISE = 1  # include/kdn.h KDN_FRAME_DENOISE
 class FrameStats(ctypes.Structure):
     _fields_ = [("total_ms", ctypes.c_double), ("trace_ms", ctypes.c_double), ("shade_ms", ctypes.c_double), ("other_ms", ctypes.c_double),
                 ("segments", ctypes.c_uint64), ("march_steps", ctypes.c_uint64), ("program_steps", ctypes.c_uint64),
-                ("launches", ctypes.c_uint32), ("longest_march", ctypes.c_uint32), ("capped_rays", ctypes.c_uint64)]
+                ("launches", ctypes.c_uint32), ("longest_march", ctypes.c_uint32), ("capped_rays", ctypes.c_uint64),
+                ("trace_launches", ctypes.c_uint32), ("pad", ctypes.c_uint32)]
 
 
 class KdnError(RuntimeError):

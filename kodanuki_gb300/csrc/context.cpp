@@ -28,7 +28,7 @@ void Context::release() {
 	cudaSetDevice(device);
 	if (stream) cudaStreamSynchronize(stream);
 	releaseFrame();
-	for (DeviceBuffer* b : { &nodes, &leaves, &programs, &steps, &march, &ssa, &leafMaterial, &objectMaterial, &extendRays, &extendHits, &extendStates, &counters, &l2, &denoiseScratch, &denoiseIo, &fetch }) freeBuffer(*b);
+	for (DeviceBuffer* b : { &nodes, &leaves, &programs, &steps, &march, &ssa, &leafMaterial, &objectMaterial, &grid, &extendRays, &extendHits, &extendStates, &counters, &l2, &denoiseScratch, &denoiseIo, &fetch }) freeBuffer(*b);
 	if (stream) cudaStreamDestroy(stream);
 	stream = nullptr;
 }
@@ -128,6 +128,8 @@ kdn_status Context::build(const BuildOptions& options) {
 	if ((s = upload(march, flat.march.data(), flat.march.size() * sizeof(GpuStep))) != KDN_OK) return s;
 	if ((s = upload(leafMaterial, leafMaterials.data(), leafMaterials.size() * sizeof(uint32_t))) != KDN_OK) return s;
 	if ((s = upload(objectMaterial, firstLeafMaterial.data(), firstLeafMaterial.size() * sizeof(uint32_t))) != KDN_OK) return s;
+	const std::vector<GridCell> cut = gridOf(flat, kGridLevel);
+	if ((s = upload(grid, cut.data(), cut.size() * sizeof(GridCell))) != KDN_OK) return s;
 	if (!check(cudaStreamSynchronize(stream), "kdn_build upload")) return KDN_CUDA_ERROR;
 	world.nodes         = static_cast<const int32_t*>(nodes.ptr);
 	world.leaves        = static_cast<const GpuLeaf*>(leaves.ptr);
@@ -136,6 +138,8 @@ kdn_status Context::build(const BuildOptions& options) {
 	world.ssa           = static_cast<const SsaOps*>(ssa.ptr);
 	world.march         = static_cast<const GpuStep*>(march.ptr);
 	world.leaf_material = static_cast<const uint32_t*>(leafMaterial.ptr);
+	world.grid          = static_cast<const GridCell*>(grid.ptr);
+	world.gridLevel     = kGridLevel;
 	for (int a = 0; a < 3; ++a) {
 		world.lower[a] = float(regions[0].lower[a]);
 		world.size[a]  = float(regions[0].size[a]);

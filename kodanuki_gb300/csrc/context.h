@@ -36,7 +36,7 @@ struct Context {
 	FlatWorld flat;
 	std::vector<int64_t> preorder; // cell index of each depth-first position
 	DeviceWorld world {};
-	DeviceBuffer nodes, leaves, programs, steps, march, ssa, leafMaterial, objectMaterial;
+	DeviceBuffer nodes, leaves, programs, steps, march, ssa, leafMaterial, objectMaterial, grid;
 	DeviceBuffer extendRays, extendHits, extendStates, counters, l2;
 	DeviceBuffer denoiseScratch, denoiseIo, fetch;
 	FrameState* frame = nullptr;

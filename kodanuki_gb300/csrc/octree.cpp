@@ -517,6 +517,25 @@ std::string slotted(const Prog& p, std::vector<GpuStep>& steps, std::vector<SsaO
 	return "";
 }
 
+// world.h MarchOp of a reference opcode.
+uint8_t marchOpOf(uint8_t op) {
+	switch (op) {
+		case OpConstant: return MarchConstant;
+		case OpPointX: return MarchPointX;
+		case OpPointY: return MarchPointY;
+		case OpPointZ: return MarchPointZ;
+		case OpAdd: return MarchAdd;
+		case OpSubtract: return MarchSubtract;
+		case OpMultiply: return MarchMultiply;
+		case OpSqrt: return MarchSqrt;
+		case OpAbs: return MarchAbs;
+		case OpMin: return MarchMin;
+		case OpMax: return MarchMax;
+		case OpPosSq: return MarchPosSq;
+		default: return uint8_t(kMarchRare + op);
+	}
+}
+
 // The march form of a program: every constant a step reads becomes that
 // step's immediate (one a step, the last constant operand), constants no
 // step reads from a slot any more are left out, and the slots are allocated
@@ -563,13 +582,34 @@ std::string marchCode(const Prog& p, std::vector<GpuStep>& steps, GpuProgram& ou
 		const int k          = operandCount(s.opcode);
 		const uint32_t op[3] = { s.a, s.b, s.c };
 		GpuStep g            = {};
-		g.op                 = s.opcode;
+		g.op                 = marchOpOf(s.opcode);
 		g.imm                = imm[i];
 		g.a                  = k > 0 && imm[i] != 1 ? slot[op[0]] : 0;
 		g.b                  = k > 1 && imm[i] != 2 ? slot[op[1]] : 0;
 		g.c                  = k > 2 && imm[i] != 3 ? slot[op[2]] : 0;
 		g.value              = imm[i] ? float(p.steps[op[imm[i] - 1]].value) : (s.opcode == OpArgument ? 0.0f : float(s.value));
 		g.leaf               = s.leaf;
+		if (s.opcode == OpNegate) {
+			// -x as 0 - x; a negated constant is a constant
+			if (imm[i] == 1) {
+				g.op    = MarchConstant;
+				g.imm   = 0;
+				g.value = -g.value;
+			} else {
+				g.op    = MarchSubtract;
+				g.b     = g.a;
+				g.a     = 0;
+				g.imm   = 1;
+				g.value = 0.0f;
+			}
+		} else if (s.opcode == OpSmin && imm[i] == 3 && g.value != 0.0f) {
+			// a constant radius r: the march form carries 0.25 / r beside it
+			const float quarter = 0.25f / g.value;
+			g.op                = MarchSminK;
+			std::memcpy(&g.leaf, &quarter, sizeof quarter);
+		} else if (s.opcode == OpSmin) {
+			g.op = uint8_t(kMarchRare + OpSmin);
+		}
 		for (int j = 0; j < k; ++j) {
 			if (imm[i] == j + 1) continue;
 			bool first = true;
@@ -641,6 +681,27 @@ std::string flattenOctree(const Octree& tree, FlatWorld& flat) {
 	for (uint32_t k : flat.leafPrograms) runs.push_back(flat.programs[k]);
 	flat.programs.swap(runs);
 	return "";
+}
+
+std::vector<GridCell> gridOf(const FlatWorld& flat, uint32_t level) {
+	const uint32_t side = 1u << level;
+	std::vector<GridCell> grid(size_t(side) * side * side);
+	for (uint32_t z = 0; z < side; ++z) {
+		for (uint32_t y = 0; y < side; ++y) {
+			for (uint32_t x = 0; x < side; ++x) {
+				int32_t node = flat.nodes[0];
+				uint32_t at  = 0;
+				for (; at < level && node >= 0; ++at) {
+					// the child of the cell holding (x, y, z): its bit at this level per axis
+					const uint32_t shift = level - 1 - at;
+					const uint32_t o     = ((x >> shift) & 1u) | (((y >> shift) & 1u) << 1) | (((z >> shift) & 1u) << 2);
+					node                 = flat.nodes[size_t(node) + o];
+				}
+				grid[(size_t(z) * side + y) * side + x] = GridCell { node, at };
+			}
+		}
+	}
+	return grid;
 }
 
 } // namespace kdn

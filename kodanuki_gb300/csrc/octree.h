@@ -54,5 +54,7 @@ struct FlatWorld {
 // Returns an empty string, or what went wrong.
 std::string buildOctree(const std::vector<ProgPtr>& objects, const double lower[3], const double size[3], const BuildOptions& options, Octree& tree);
 std::string flattenOctree(const Octree& tree, FlatWorld& flat);
+// The grid of `level` over a flattened octree (world.h GridCell).
+std::vector<GridCell> gridOf(const FlatWorld& flat, uint32_t level);
 
 } // namespace kdn

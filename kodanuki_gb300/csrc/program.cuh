@@ -64,13 +64,43 @@ __device__ __forceinline__ float stepValue(uint8_t op, float a, float b, float c
 	}
 }
 
+// A rare step of the march form (marchOp >= kMarchRare): the reference
+// opcode it carries.
+__device__ __forceinline__ float rareMarchValue(uint8_t op, float a, float b, float c, float value, float x, float y, float z) {
+	const float p[3] = { x, y, z };
+	return stepValue(uint8_t(op - kMarchRare), a, b, c, value, p);
+}
+
 // One step of the march form: its operands from the slots or, for the one
-// its `imm` names, from its value.
+// its `imm` names, from its value.  The common operations are worked out
+// together and the step's picked, so the lanes of a warp running different
+// operations do not split.
+__device__ __forceinline__ float marchValue(uint8_t op, float a, float b, float c, float value, float quarter, const float p[3]) {
+	if (op >= kMarchRare) return rareMarchValue(op, a, b, c, value, p[0], p[1], p[2]);
+	// the smooth minimum of constant radius c: min - max(c - |a - b|, 0)^2 * 0.25 / c
+	const float m = fmaxf(c - fabsf(a - b), 0.0f);
+	const float q = fmaxf(a, 0.0f);
+	float r       = value;
+	r             = op == MarchPointX ? p[0] : r;
+	r             = op == MarchPointY ? p[1] : r;
+	r             = op == MarchPointZ ? p[2] : r;
+	r             = op == MarchAdd ? a + b : r;
+	r             = op == MarchSubtract ? a - b : r;
+	r             = op == MarchMultiply ? a * b : r;
+	r             = op == MarchSqrt ? sqrtf(a) : r;
+	r             = op == MarchAbs ? fabsf(a) : r;
+	r             = op == MarchMin ? (b < a ? b : a) : r;
+	r             = op == MarchMax ? (a < b ? b : a) : r;
+	r             = op == MarchSminK ? fminf(a, b) - m * m * quarter : r;
+	r             = op == MarchPosSq ? q * q : r;
+	return r;
+}
+
 __device__ __forceinline__ void runSlotStep(const GpuStep& s, float* slots, uint32_t stride, const float p[3]) {
 	const float a = s.imm == 1 ? s.value : slots[s.a * stride];
 	const float b = s.imm == 2 ? s.value : slots[s.b * stride];
 	const float c = s.imm == 3 ? s.value : slots[s.c * stride];
-	slots[s.dst * stride] = stepValue(s.op, a, b, c, s.value, p);
+	slots[s.dst * stride] = marchValue(s.op, a, b, c, s.value, __uint_as_float(s.leaf), p);
 }
 
 // One program at one point; slots is this thread's column base (stride

@@ -471,6 +471,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	st.longest_march = uint32_t(host[2]);
 	st.capped_rays   = host[3];
 	st.segments      = host[4];
+	st.trace_launches = uint32_t((ev - 2) / 2);
 	st.launches      = launches;
 	st.other_ms      = st.total_ms - st.trace_ms;
 	f.stats          = st;

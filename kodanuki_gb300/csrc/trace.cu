@@ -39,14 +39,46 @@ struct Located {
 	float lo[3], hi[3];
 };
 
-__device__ __forceinline__ Located locate(const DeviceWorld& w, const float p[3]) {
-	Located l;
+// The midpoint tests of `levels` levels of descent, in registers: the box
+// they leave and the grid coordinates of the cell.
+__device__ __forceinline__ uint32_t descendBox(const DeviceWorld& w, const float p[3], uint32_t levels, Located& l) {
 	for (int a = 0; a < 3; ++a) {
 		l.lo[a] = w.lower[a];
 		l.hi[a] = w.lower[a] + w.size[a];
 	}
-	int32_t node = __ldg(&w.nodes[0]);
-	uint32_t at  = 0;
+	uint32_t cx = 0, cy = 0, cz = 0;
+	for (uint32_t level = 0; level < levels; ++level) {
+		uint32_t bit[3];
+		for (int a = 0; a < 3; ++a) {
+			const float mid = 0.5f * (l.lo[a] + l.hi[a]);
+			bit[a]          = p[a] >= mid ? 1u : 0u;
+			if (bit[a]) l.lo[a] = mid;
+			else l.hi[a] = mid;
+		}
+		cx = (cx << 1) | bit[0];
+		cy = (cy << 1) | bit[1];
+		cz = (cz << 1) | bit[2];
+	}
+	return (cz << (2 * levels)) | (cy << levels) | cx;
+}
+
+__device__ __forceinline__ Located locate(const DeviceWorld& w, const float p[3]) {
+	Located l;
+	int32_t node;
+	if (w.grid != nullptr) {
+		// the grid's level of the descent without loads, then the node there
+		const GridCell g = w.grid[descendBox(w, p, w.gridLevel, l)];
+		node             = g.node;
+		// a leaf above the grid's level: the box of that level
+		if (g.level < w.gridLevel) descendBox(w, p, g.level, l);
+	} else {
+		for (int a = 0; a < 3; ++a) {
+			l.lo[a] = w.lower[a];
+			l.hi[a] = w.lower[a] + w.size[a];
+		}
+		node = __ldg(&w.nodes[0]);
+	}
+	uint32_t at = 0;
 	for (int depth = 0; depth < 30 && node >= 0; ++depth) {
 		int o = 0;
 		for (int a = 0; a < 3; ++a) {
@@ -65,12 +97,13 @@ __device__ __forceinline__ Located locate(const DeviceWorld& w, const float p[3]
 	return l;
 }
 
-__device__ __forceinline__ float cellExit(const float o[3], const float inv[3], const Located& l) {
+__device__ __forceinline__ float cellExit(const float o[3], const float d[3], const Located& l) {
 	float up = 3.0e38f;
 	for (int a = 0; a < 3; ++a) {
-		const float x = (l.lo[a] - o[a]) * inv[a];
-		const float y = (l.hi[a] - o[a]) * inv[a];
-		up            = fminf(up, fmaxf(x, y));
+		const float inv = slopeOf(d[a]);
+		const float x   = (l.lo[a] - o[a]) * inv;
+		const float y   = (l.hi[a] - o[a]) * inv;
+		up              = fminf(up, fmaxf(x, y));
 	}
 	return up;
 }
@@ -95,7 +128,7 @@ __device__ __forceinline__ bool within(const Located& l, const float p[3]) {
 // The field at t from the kept programs of the cell the point lies in.  The
 // cell of the previous step is kept in `cell`: a ray takes several steps in
 // one cell, and only a point that has left it descends the octree again.
-__device__ __forceinline__ Field fieldAt(const DeviceWorld& w, const float o[3], const float d[3], const float inv[3], float t, float* slots, uint32_t stride, unsigned long long& steps, Located& cell) {
+__device__ __forceinline__ Field fieldAt(const DeviceWorld& w, const float o[3], const float d[3], float t, float* slots, uint32_t stride, uint32_t& steps, Located& cell) {
 	Field f;
 	const float p[3] = { o[0] + d[0] * t, o[1] + d[1] * t, o[2] + d[2] * t };
 	if (!within(cell, p)) cell = locate(w, p);
@@ -110,7 +143,7 @@ __device__ __forceinline__ Field fieldAt(const DeviceWorld& w, const float o[3],
 	// A cell keeps only the objects whose surface may pass through it
 	// (cut.cpp:442 deciding), so past its walls its field is no distance
 	// bound: a step stops where the ray leaves the cell.
-	f.exit   = cellExit(o, inv, l);
+	f.exit   = cellExit(o, d, l);
 	if (f.empty) return f;
 	for (uint32_t k = 0; k < leaf.count; ++k) {
 		const GpuProgram g = w.programs[leaf.first + k];
@@ -127,7 +160,7 @@ __device__ __forceinline__ Field fieldAt(const DeviceWorld& w, const float o[3],
 
 // The least value at t, and the index of the kept program that is least a
 // little further along among those tied with it (sphere_trace.cpp:96).
-__device__ uint32_t winnerAt(const DeviceWorld& w, const float o[3], const float d[3], float t, const Field& f, float* slots, uint32_t stride) {
+__device__ __forceinline__ uint32_t winnerAt(const DeviceWorld& w, const float o[3], const float d[3], float t, const Field& f, float* slots, uint32_t stride) {
 	const float p[3] = { o[0] + d[0] * t, o[1] + d[1] * t, o[2] + d[2] * t };
 	const float big  = fmaxf(fabsf(p[0]), fmaxf(fabsf(p[1]), fabsf(p[2])));
 	const float band = 2e-6f * (1.0f + big);
@@ -154,6 +187,25 @@ __device__ uint32_t winnerAt(const DeviceWorld& w, const float o[3], const float
 	return winner;
 }
 
+// sphereFromInside at a point within the tolerance of the nearest surface:
+// read the field a little past it.  kind 0: go on past (t += inset); 1: the
+// ray leaves its solid here (winner among the cell's programs); 2: it meets
+// a solid of another material (the program past the point).
+struct InsideStop {
+	uint32_t kind, first, index;
+};
+
+__device__ __forceinline__ InsideStop insideStop(const DeviceWorld& w, const uint32_t* objectMaterial, uint32_t medium, const float o[3], const float d[3], float t,
+                                             float inset, const Field& f, const Located& cell, float* slots, uint32_t stride, uint32_t& steps) {
+	Located beyond   = cell;
+	const Field past = fieldAt(w, o, d, t + inset, slots, stride, steps, beyond);
+	if (past.empty || past.least > 0.0f) return InsideStop { 1, f.first, winnerAt(w, o, d, t, f, slots, stride) };
+	const GpuProgram g = w.programs[past.first + past.index];
+	// a solid of another material than the one the ray is in: stop there
+	if (objectMaterial != nullptr && objectMaterial[g.object] != medium) return InsideStop { 2, past.first, past.index };
+	return InsideStop { 0, 0, 0 };
+}
+
 // The march as a step machine.  Each thread holds one ray at a time and
 // every turn of the loop runs one program step for every thread that is
 // evaluating, so threads whose cells hold programs of different lengths, or
@@ -168,14 +220,13 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 	const DeviceWorld& w  = args.world;
 	const uint32_t stride = blockDim.x;
 	float* slots          = slotMemory + threadIdx.x;
-	unsigned long long marchSteps = 0, programSteps = 0, traced = 0, capped = 0;
-	uint32_t longest = 0;
+	uint32_t marchSteps = 0, programSteps = 0, traced = 0, capped = 0, longest = 0;
 	const uint32_t n = args.count ? *args.count : args.n;
 	const unsigned lane = threadIdx.x & 31u;
 
 	uint32_t mode = Fetch;
 	uint32_t ray  = 0;
-	float o[3], d[3], inv[3];
+	float o[3], d[3];
 	float t = 0.0f, up = 0.0f;
 	bool inside      = false;
 	uint32_t medium  = kNoLeaf;
@@ -217,15 +268,15 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 					++traced;
 					const kdn_ray r = args.rays[ray];
 					for (int a = 0; a < 3; ++a) {
-						o[a]   = r.origin[a];
-						d[a]   = r.direction[a];
-						inv[a] = slopeOf(d[a]);
+						o[a] = r.origin[a];
+						d[a] = r.direction[a];
 					}
 					float lo = 0.0f;
 					up       = r.far;
 					for (int a = 0; a < 3; ++a) {
-						const float x = (w.lower[a] - o[a]) * inv[a];
-						const float y = (w.lower[a] + w.size[a] - o[a]) * inv[a];
+						const float inv = slopeOf(d[a]);
+						const float x   = (w.lower[a] - o[a]) * inv;
+						const float y   = (w.lower[a] + w.size[a] - o[a]) * inv;
 						lo            = fmaxf(lo, fminf(x, y));
 						up            = fminf(up, fmaxf(x, y));
 					}
@@ -254,7 +305,7 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 				for (int a = 0; a < 3; ++a) p[a] = o[a] + d[a] * t;
 				if (!within(cell, p)) cell = locate(w, p);
 				const GpuLeaf leaf = w.leaves[cell.leaf];
-				exitT              = cellExit(o, inv, cell);
+				exitT              = cellExit(o, d, cell);
 				if (leaf.occupancy == Empty || leaf.count == 0) {
 					t = fmaxf(exitT, t) + nudge(t);
 					++step;
@@ -330,20 +381,10 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 						f.index = index;
 						f.count = count;
 						f.first = first;
-						const float inset = 2.0f * tol;
-						Located beyond    = cell;
-						const Field past  = fieldAt(w, o, d, inv, t + inset, slots, stride, programSteps, beyond);
-						if (past.empty || past.least > 0.0f) {
-							done(HitState { 1, t, first, winnerAt(w, o, d, t, f, slots, stride), step });
-						} else {
-							const GpuProgram g = w.programs[past.first + past.index];
-							// a solid of another material than the one the ray is in: stop there
-							if (args.objectMaterial != nullptr && args.objectMaterial[g.object] != medium) {
-								done(HitState { 2, t, past.first, past.index, step });
-							} else {
-								t += inset;
-							}
-						}
+						const float inset   = 2.0f * tol;
+						const InsideStop at = insideStop(w, args.objectMaterial, medium, o, d, t, inset, f, cell, slots, stride, programSteps);
+						if (at.kind == 0) t += inset;
+						else done(HitState { at.kind, t, at.first, at.index, step });
 					} else {
 						t = fminf(t + nearest, fmaxf(exitT, t) + nudge(t));
 					}
@@ -361,11 +402,11 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 			longest = max(longest, __shfl_down_sync(0xFFFFFFFFu, longest, o));
 		}
 		if ((threadIdx.x & 31) == 0) {
-			atomicAdd(&args.counters[0], marchSteps);
-			atomicAdd(&args.counters[1], programSteps);
+			atomicAdd(&args.counters[0], (unsigned long long) marchSteps);
+			atomicAdd(&args.counters[1], (unsigned long long) programSteps);
 			atomicMax(&args.counters[2], (unsigned long long) longest);
-			atomicAdd(&args.counters[3], capped);
-			atomicAdd(&args.counters[4], traced);
+			atomicAdd(&args.counters[3], (unsigned long long) capped);
+			atomicAdd(&args.counters[4], (unsigned long long) traced);
 		}
 	}
 }

@@ -23,6 +23,17 @@ enum Op : uint8_t {
 	OpNotEqual, OpAnd, OpOr, OpNot, OpSelect, OpCount
 };
 
+// The march form's own operation codes: the common operations dense from 0,
+// every other one as kMarchRare + its reference opcode.
+// A negation is 0 - x, and a smooth minimum of constant radius r carries
+// 0.25 / r in the step's `leaf` field (MarchSminK); other smooth minima are
+// rare steps.
+enum MarchOp : uint8_t {
+	MarchConstant, MarchPointX, MarchPointY, MarchPointZ, MarchAdd, MarchSubtract, MarchMultiply,
+	MarchSqrt, MarchAbs, MarchMin, MarchMax, MarchSminK, MarchPosSq
+};
+constexpr uint8_t kMarchRare = 64;
+
 constexpr uint32_t kNoLeaf     = 0xFFFFFFFFu;
 constexpr uint32_t kMaxSlots   = 48;   // register slots a leaf program may use
 constexpr uint32_t kMaxSsa     = 1024; // steps a leaf program may hold
@@ -76,6 +87,17 @@ struct GpuLeaf {
 };
 static_assert(sizeof(GpuLeaf) == 8, "GpuLeaf is 8 bytes");
 
+// The octree cut across at one level: for each cell of the uniform grid of
+// that level, the node value there (first child, or ~leaf) and its level,
+// less than the grid's where a leaf above it covers the cell.  A point is
+// located by the grid's level of midpoint tests in registers, one load, and
+// the descent below it.
+struct GridCell {
+	int32_t node;
+	uint32_t level;
+};
+constexpr uint32_t kGridLevel = 6;
+
 // Everything the trace kernel reads, as device pointers.
 struct DeviceWorld {
 	const int32_t* nodes;
@@ -85,6 +107,8 @@ struct DeviceWorld {
 	const GpuStep* march;
 	const SsaOps* ssa;
 	const uint32_t* leaf_material;
+	const GridCell* grid; // (2^gridLevel)^3 cells, x fastest; null: descend from the root
+	uint32_t gridLevel;
 	float lower[3];
 	float size[3];
 	uint32_t leaf_count;
