@@ -47,7 +47,7 @@ DENOISE = True  # the a-trous denoiser on the frame's FP16 features
 # DRAM bytes the trace kernel moves a ray (read + write), from the ncu
 # capture of one launch of known rays (profiles/trace_kernel_ncu.md)
 TRACE_DRAM_BYTES_PER_RAY = None
-BUILD = dict(min_depth=7, max_depth=10, split_steps=96)
+BUILD = dict(min_depth=7, max_depth=11, split_steps=32)
 
 
 def env_int(name: str, default: int) -> int:

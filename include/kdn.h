@@ -233,6 +233,13 @@ kdn_status kdn_world_stats(kdn_ctx* ctx, uint64_t out[4]);
  * entry per kept program, steps the programs' kdn_steps end to end.  Pass
  * null arrays to read the head alone. */
 kdn_status kdn_world_cell(kdn_ctx* ctx, uint64_t i, uint32_t head[6], uint32_t* objects, uint32_t* results, uint32_t* counts, kdn_step* steps, size_t steps_capacity);
+/* The march form the trace kernel runs for cell i (depth-first pre-order),
+ * run on the host: every kept program of the cell at n points (x, y, z
+ * floats), values[k * n + j] for program k at point j, up to capacity
+ * values; *programs gets the count.  A check of the march form against the
+ * cell's programs (the same interpreter as the device's, FP32).
+ * KDN_NOT_READY where the device layout could not be made. */
+kdn_status kdn_world_march(kdn_ctx* ctx, uint64_t i, const float* points, uint32_t n, float* values, size_t capacity, uint32_t* programs);
 
 /* ExtendRays (core/step.cpp:132): the first hit of each ray, host arrays in
  * and out (a host-to-device and device-to-host copy each call). */

@@ -77,7 +77,7 @@ class KdnError(RuntimeError):
 EXPORTS = [
     "kdn_status_string", "kdn_last_error", "kdn_open", "kdn_close", "kdn_upload_block", "kdn_build", "kdn_world_stats",
     "kdn_world_cell", "kdn_extend", "kdn_extend_device", "kdn_render", "kdn_render_device", "kdn_frame_stats_get", "kdn_flush_l2",
-    "kdn_frame_surfaces", "kdn_denoise", "kdn_denoise_device", "kdn_denoise_static",
+    "kdn_frame_surfaces", "kdn_world_march", "kdn_denoise", "kdn_denoise_device", "kdn_denoise_static",
 ]
 
 
@@ -116,6 +116,7 @@ def library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.kdn_frame_stats_get.argtypes = [P, ctypes.POINTER(FrameStats)]
     L.kdn_flush_l2.argtypes = [P]
     L.kdn_frame_surfaces.argtypes = [P, P, P, P, P]
+    L.kdn_world_march.argtypes = [P, ctypes.c_uint64, P, ctypes.c_uint32, P, ctypes.c_size_t, P]
     L.kdn_denoise.argtypes = [P, ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P]
     L.kdn_denoise_device.argtypes = [P, ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P, P]
     L.kdn_denoise_static.argtypes = [ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P, P]
@@ -278,6 +279,16 @@ class Backend:
         s = FrameStats()
         self._check(self.lib.kdn_frame_stats_get(self.handle, ctypes.byref(s)))
         return s
+
+    def world_march(self, i: int, points: np.ndarray) -> np.ndarray:
+        """The march form of cell i's kept programs run on the host at the
+        points (n x 3): programs x n float32 (include/kdn.h kdn_world_march)."""
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+        count = ctypes.c_uint32()
+        cap = 64 * max(pts.shape[0], 1)  # a leaf keeps at most 64 programs
+        values = np.zeros(cap, np.float32)
+        self._check(self.lib.kdn_world_march(self.handle, i, _ptr(pts), pts.shape[0], _ptr(values), cap, ctypes.byref(count)))
+        return values[: count.value * pts.shape[0]].reshape(count.value, pts.shape[0])
 
     def frame_surfaces(self, width: int, height: int) -> dict:
         """The first surfaces of the last frame drawn with denoise=True

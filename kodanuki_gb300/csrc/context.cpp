@@ -94,12 +94,15 @@ kdn_status Context::build(const BuildOptions& options) {
 	}
 	std::string message = buildOctree(objects, regions[0].lower, regions[0].size, options, octree);
 	if (!message.empty()) return fail(KDN_BAD_ARG, "kdn_build: " + message);
-	// a host-only context keeps the octree alone; the device layout and its
-	// limits (kMaxSsa, kMaxSlots) apply where there is a device
+	// the device layout and its limits (kMaxSsa, kMaxSlots): a device needs
+	// it; a host-only context keeps it where the limits allow, for checks
 	flat = FlatWorld();
-	if (device >= 0) {
-		message = flattenOctree(octree, flat);
-		if (!message.empty()) return fail(KDN_BAD_ARG, "kdn_build: " + message);
+	flatError.clear();
+	message = flattenOctree(octree, flat);
+	if (!message.empty()) {
+		if (device >= 0) return fail(KDN_BAD_ARG, "kdn_build: " + message);
+		flat      = FlatWorld();
+		flatError = message;
 	}
 	// depth-first order of the cells, for kdn_world_cell
 	preorder.clear();

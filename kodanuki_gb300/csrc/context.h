@@ -34,6 +34,7 @@ struct Context {
 	bool sceneChanged = true;
 	Octree octree;
 	FlatWorld flat;
+	std::string flatError; // why a host-only context has no device layout
 	std::vector<int64_t> preorder; // cell index of each depth-first position
 	DeviceWorld world {};
 	DeviceBuffer nodes, leaves, programs, steps, march, ssa, leafMaterial, objectMaterial, grid;

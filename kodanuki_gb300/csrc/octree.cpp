@@ -536,12 +536,20 @@ uint8_t marchOpOf(uint8_t op) {
 	}
 }
 
-// The march form of a program: every constant a step reads becomes that
-// step's immediate (one a step, the last constant operand), constants no
-// step reads from a slot any more are left out, and the slots are allocated
-// again over what remains.
+// The march form of a program (world.h MarchOp):
+//  - every constant a step reads becomes that step's immediate (one a step,
+//    the last constant operand); constants no step reads from a slot any
+//    more are left out;
+//  - a common operation takes its immediate as b (the operands of +, *, min
+//    and max are swapped, const - x is x subtracted from b), a smooth minimum
+//    of constant radius carries the radius and 0.25 / radius;
+//  - an operand that is the result of the step just before is read from a
+//    register (kFromPrevious*), and a result read only that way is not
+//    stored (kNoStore) and takes no slot;
+//  - the slots are allocated again over what remains.
 std::string marchCode(const Prog& p, std::vector<GpuStep>& steps, GpuProgram& out) {
 	const uint32_t n = uint32_t(p.steps.size());
+	constexpr uint32_t kNone = 0xFFFFFFFFu;
 	std::vector<uint8_t> imm(n, 0), needed(n, 0);
 	needed[p.result] = 1;
 	for (uint32_t i = 0; i < n; ++i) {
@@ -560,75 +568,128 @@ std::string marchCode(const Prog& p, std::vector<GpuStep>& steps, GpuProgram& ou
 			if (imm[i] != j + 1) needed[op[j]] = 1;
 		}
 	}
-	std::vector<uint32_t> lastUse(n);
-	for (uint32_t i = 0; i < n; ++i) lastUse[i] = i;
-	for (uint32_t i = 0; i < n; ++i) {
-		const kdn_step& s    = p.steps[i];
-		const int k          = operandCount(s.opcode);
-		const uint32_t op[3] = { s.a, s.b, s.c };
-		for (int j = 0; j < k; ++j) {
-			if (imm[i] != j + 1) lastUse[op[j]] = std::max(lastUse[op[j]], i);
-		}
-	}
-	lastUse[p.result] = n;
-	std::vector<uint8_t> slot(n, 0);
-	std::vector<uint8_t> freeSlots;
-	uint32_t used  = 0;
-	uint32_t kept  = 0;
-	out.march      = uint32_t(steps.size());
+	// the kept steps, and each one's form: op, operand sources (SSA index or kNone), immediate
+	struct Form {
+		uint8_t op;
+		uint8_t imm;
+		uint32_t src[3];
+		float value;
+		uint32_t leaf;
+		bool rare;
+	};
+	std::vector<Form> form(n);
+	std::vector<uint32_t> order;
 	for (uint32_t i = 0; i < n; ++i) {
 		const kdn_step& s = p.steps[i];
 		if (s.opcode == OpConstant && !needed[i]) continue;
+		order.push_back(i);
 		const int k          = operandCount(s.opcode);
 		const uint32_t op[3] = { s.a, s.b, s.c };
-		GpuStep g            = {};
-		g.op                 = marchOpOf(s.opcode);
-		g.imm                = imm[i];
-		g.a                  = k > 0 && imm[i] != 1 ? slot[op[0]] : 0;
-		g.b                  = k > 1 && imm[i] != 2 ? slot[op[1]] : 0;
-		g.c                  = k > 2 && imm[i] != 3 ? slot[op[2]] : 0;
-		g.value              = imm[i] ? float(p.steps[op[imm[i] - 1]].value) : (s.opcode == OpArgument ? 0.0f : float(s.value));
-		g.leaf               = s.leaf;
+		Form f;
+		f.op    = marchOpOf(s.opcode);
+		f.imm   = imm[i];
+		f.value = imm[i] ? float(p.steps[op[imm[i] - 1]].value) : (s.opcode == OpArgument ? 0.0f : float(s.value));
+		f.leaf  = s.leaf;
+		f.rare  = f.op >= kMarchRare;
+		for (int j = 0; j < 3; ++j) f.src[j] = j < k && imm[i] != j + 1 ? op[j] : kNone;
+		const bool commutes = s.opcode == OpAdd || s.opcode == OpMultiply || s.opcode == OpMin || s.opcode == OpMax;
 		if (s.opcode == OpNegate) {
-			// -x as 0 - x; a negated constant is a constant
-			if (imm[i] == 1) {
-				g.op    = MarchConstant;
-				g.imm   = 0;
-				g.value = -g.value;
-			} else {
-				g.op    = MarchSubtract;
-				g.b     = g.a;
-				g.a     = 0;
-				g.imm   = 1;
-				g.value = 0.0f;
+			if (imm[i] == 1) { // a negated constant is a constant
+				f.op    = MarchConstant;
+				f.imm   = 0;
+				f.value = -f.value;
+				f.src[0] = kNone;
+			} else { // -x as 0 - x
+				f.op  = MarchSubtractFrom;
+				f.imm = 2;
+				f.value = 0.0f;
 			}
-		} else if (s.opcode == OpSmin && imm[i] == 3 && g.value != 0.0f) {
-			// a constant radius r: the march form carries 0.25 / r beside it
-			const float quarter = 0.25f / g.value;
-			g.op                = MarchSminK;
-			std::memcpy(&g.leaf, &quarter, sizeof quarter);
-		} else if (s.opcode == OpSmin) {
-			g.op = uint8_t(kMarchRare + OpSmin);
+			f.rare = false;
+		} else if (s.opcode == OpSubtract && imm[i] == 1) {
+			f.op     = MarchSubtractFrom;
+			f.imm    = 2;
+			f.src[0] = op[1];
+			f.src[1] = kNone;
+		} else if (commutes && imm[i] == 1) {
+			f.imm    = 2;
+			f.src[0] = op[1];
+			f.src[1] = kNone;
+		} else if (s.opcode == OpSmin && imm[i] == 3 && f.value != 0.0f) {
+			const float quarter = 0.25f / f.value;
+			f.op                = MarchSminK;
+			std::memcpy(&f.leaf, &quarter, sizeof quarter);
+		} else if (!f.rare && imm[i] == 1) {
+			// a common unary operation of a constant: the general form
+			f.op   = uint8_t(kMarchRare + s.opcode);
+			f.rare = true;
 		}
-		for (int j = 0; j < k; ++j) {
-			if (imm[i] == j + 1) continue;
-			bool first = true;
-			for (int m = 0; m < j; ++m) first = first && (imm[i] == m + 1 || op[m] != op[j]);
-			if (first && lastUse[op[j]] == i) freeSlots.push_back(slot[op[j]]);
+		if (s.opcode == OpSmin && f.op != MarchSminK) {
+			f.op   = uint8_t(kMarchRare + OpSmin);
+			f.rare = true;
 		}
-		if (!freeSlots.empty()) {
-			slot[i] = freeSlots.back();
-			freeSlots.pop_back();
-		} else {
-			if (used >= kMaxSlots) return "a leaf program needs more than " + std::to_string(kMaxSlots) + " register slots";
-			slot[i] = uint8_t(used++);
-		}
-		if (lastUse[i] == i) freeSlots.push_back(slot[i]);
-		g.dst = slot[i];
-		steps.push_back(g);
-		++kept;
+		form[i] = f;
 	}
-	out.marchCount = uint16_t(kept);
+	// forwarding: an a or b operand that is the step just before
+	std::vector<uint16_t> flags(n, 0);
+	std::vector<uint8_t> stored(n, 0);
+	std::vector<uint32_t> lastRead(n, 0);
+	for (size_t e = 0; e < order.size(); ++e) {
+		const uint32_t i    = order[e];
+		const uint32_t prev = e > 0 ? order[e - 1] : kNone;
+		for (int j = 0; j < 3; ++j) {
+			const uint32_t src = form[i].src[j];
+			if (src == kNone) continue;
+			if (j < 2 && src == prev) {
+				flags[i] |= uint16_t(j == 0 ? kFromPreviousA : kFromPreviousB);
+			} else {
+				stored[src]   = 1;
+				lastRead[src] = std::max(lastRead[src], i);
+			}
+		}
+	}
+	stored[p.result]   = 1;
+	lastRead[p.result] = n;
+	std::vector<uint8_t> slot(n, 0);
+	std::vector<uint8_t> freeSlots;
+	uint32_t used = 0;
+	out.march     = uint32_t(steps.size());
+	for (const uint32_t i : order) {
+		const Form& f = form[i];
+		GpuStep g     = {};
+		g.op          = f.op;
+		g.imm         = f.imm;
+		g.value       = f.value;
+		g.leaf        = f.leaf;
+		g.flags       = flags[i];
+		g.a           = f.src[0] != kNone && !(flags[i] & kFromPreviousA) ? slot[f.src[0]] : 0;
+		g.b           = f.src[1] != kNone && !(flags[i] & kFromPreviousB) ? slot[f.src[1]] : 0;
+		g.c           = f.src[2] != kNone ? slot[f.src[2]] : 0;
+		// free the slots whose last read is this step (each value once)
+		for (int j = 0; j < 3; ++j) {
+			const uint32_t src = f.src[j];
+			if (src == kNone || (j == 0 && (flags[i] & kFromPreviousA)) || (j == 1 && (flags[i] & kFromPreviousB))) continue;
+			bool first = true;
+			for (int m = 0; m < j; ++m) {
+				const bool viaSlot = !((m == 0 && (flags[i] & kFromPreviousA)) || (m == 1 && (flags[i] & kFromPreviousB)));
+				first              = first && !(viaSlot && f.src[m] == src);
+			}
+			if (first && stored[src] && lastRead[src] == i) freeSlots.push_back(slot[src]);
+		}
+		if (stored[i]) {
+			if (!freeSlots.empty()) {
+				slot[i] = freeSlots.back();
+				freeSlots.pop_back();
+			} else {
+				if (used >= kMaxSlots) return "a leaf program needs more than " + std::to_string(kMaxSlots) + " register slots";
+				slot[i] = uint8_t(used++);
+			}
+			g.dst = slot[i];
+		} else {
+			g.flags |= kNoStore;
+		}
+		steps.push_back(g);
+	}
+	out.marchCount = uint16_t(order.size());
 	out.marchSlot  = slot[p.result];
 	out.marchSlots = uint8_t(std::max(used, 1u));
 	return "";

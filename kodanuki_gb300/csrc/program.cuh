@@ -13,18 +13,36 @@
 
 #include "world.h"
 
+#include <cuda_runtime.h>
+
+#include <cmath>
 #include <cstdint>
+#include <cstring>
+
+// The march form's interpreter compiles for the host too, where
+// kdn_world_march runs it to check the march form against the programs.
+#define KDN_HD __host__ __device__ __forceinline__
 
 namespace kdn {
 
-__device__ __forceinline__ float smoothMinF(float a, float b, float r) {
+KDN_HD float floatOfBits(uint32_t bits) {
+#ifdef __CUDA_ARCH__
+	return __uint_as_float(bits);
+#else
+	float f;
+	std::memcpy(&f, &bits, sizeof f);
+	return f;
+#endif
+}
+
+KDN_HD float smoothMinF(float a, float b, float r) {
 	const float blend = fmaxf(r - fabsf(a - b), 0.0f) / r;
 	return fminf(a, b) - blend * blend * r * 0.25f;
 }
 
-__device__ __forceinline__ float truthF(bool b) { return b ? 1.0f : 0.0f; }
+KDN_HD float truthF(bool b) { return b ? 1.0f : 0.0f; }
 
-__device__ __forceinline__ float stepValue(uint8_t op, float a, float b, float c, float value, const float p[3]) {
+KDN_HD float stepValue(uint8_t op, float a, float b, float c, float value, const float p[3]) {
 	switch (op) {
 		case OpConstant: return value;
 		case OpArgument: return 0.0f;
@@ -66,19 +84,18 @@ __device__ __forceinline__ float stepValue(uint8_t op, float a, float b, float c
 
 // A rare step of the march form (marchOp >= kMarchRare): the reference
 // opcode it carries.
-__device__ __forceinline__ float rareMarchValue(uint8_t op, float a, float b, float c, float value, float x, float y, float z) {
+KDN_HD float rareMarchValue(uint8_t op, float a, float b, float c, float value, float x, float y, float z) {
 	const float p[3] = { x, y, z };
 	return stepValue(uint8_t(op - kMarchRare), a, b, c, value, p);
 }
 
-// One step of the march form: its operands from the slots or, for the one
-// its `imm` names, from its value.  The common operations are worked out
-// together and the step's picked, so the lanes of a warp running different
-// operations do not split.
-__device__ __forceinline__ float marchValue(uint8_t op, float a, float b, float c, float value, float quarter, const float p[3]) {
-	if (op >= kMarchRare) return rareMarchValue(op, a, b, c, value, p[0], p[1], p[2]);
-	// the smooth minimum of constant radius c: min - max(c - |a - b|, 0)^2 * 0.25 / c
-	const float m = fmaxf(c - fabsf(a - b), 0.0f);
+// A common step of the march form (world.h MarchOp): the operations are
+// worked out together and the step's picked, so the lanes of a warp running
+// different operations do not split.  b may be the immediate; `value` is
+// the constant, or the radius of a smooth minimum with `quarter` = 0.25 / r.
+KDN_HD float marchValue(uint8_t op, float a, float b, float value, float quarter, const float p[3]) {
+	// the smooth minimum of constant radius r: min - max(r - |a - b|, 0)^2 * 0.25 / r
+	const float m = fmaxf(value - fabsf(a - b), 0.0f);
 	const float q = fmaxf(a, 0.0f);
 	float r       = value;
 	r             = op == MarchPointX ? p[0] : r;
@@ -86,6 +103,7 @@ __device__ __forceinline__ float marchValue(uint8_t op, float a, float b, float 
 	r             = op == MarchPointZ ? p[2] : r;
 	r             = op == MarchAdd ? a + b : r;
 	r             = op == MarchSubtract ? a - b : r;
+	r             = op == MarchSubtractFrom ? b - a : r;
 	r             = op == MarchMultiply ? a * b : r;
 	r             = op == MarchSqrt ? sqrtf(a) : r;
 	r             = op == MarchAbs ? fabsf(a) : r;
@@ -96,17 +114,31 @@ __device__ __forceinline__ float marchValue(uint8_t op, float a, float b, float 
 	return r;
 }
 
-__device__ __forceinline__ void runSlotStep(const GpuStep& s, float* slots, uint32_t stride, const float p[3]) {
-	const float a = s.imm == 1 ? s.value : slots[s.a * stride];
-	const float b = s.imm == 2 ? s.value : slots[s.b * stride];
-	const float c = s.imm == 3 ? s.value : slots[s.c * stride];
-	slots[s.dst * stride] = marchValue(s.op, a, b, c, s.value, __uint_as_float(s.leaf), p);
+// One step of the march form.  Operands come from the thread's slots, from
+// the immediate, or (kFromPrevious*) from `prev`, the result of the step
+// before, which stays in a register; a kNoStore result is not written.
+// Returns the step's result, the next step's `prev`.
+KDN_HD float marchStep(const GpuStep& s, float* slots, uint32_t stride, const float p[3], float prev) {
+	float r;
+	if (s.op >= kMarchRare) {
+		const float a = s.imm == 1 ? s.value : ((s.flags & kFromPreviousA) ? prev : slots[s.a * stride]);
+		const float b = s.imm == 2 ? s.value : ((s.flags & kFromPreviousB) ? prev : slots[s.b * stride]);
+		const float c = s.imm == 3 ? s.value : slots[s.c * stride];
+		r             = rareMarchValue(s.op, a, b, c, s.value, p[0], p[1], p[2]);
+	} else {
+		const float a = (s.flags & kFromPreviousA) ? prev : slots[s.a * stride];
+		const float b = s.imm == 2 ? s.value : ((s.flags & kFromPreviousB) ? prev : slots[s.b * stride]);
+		r             = marchValue(s.op, a, b, s.value, floatOfBits(s.leaf), p);
+	}
+	if (!(s.flags & kNoStore)) slots[s.dst * stride] = r;
+	return r;
 }
 
 // One program at one point; slots is this thread's column base (stride
 // blockDim.x).  Returns the program's value.
-__device__ __forceinline__ float evalSlots(const GpuStep* __restrict__ code, uint32_t count, uint32_t resultSlot, float* slots, uint32_t stride, const float p[3]) {
-	for (uint32_t i = 0; i < count; ++i) runSlotStep(code[i], slots, stride, p);
+KDN_HD float evalSlots(const GpuStep* __restrict__ code, uint32_t count, uint32_t resultSlot, float* slots, uint32_t stride, const float p[3]) {
+	float prev = 0.0f;
+	for (uint32_t i = 0; i < count; ++i) prev = marchStep(code[i], slots, stride, p, prev);
 	return slots[resultSlot * stride];
 }
 

@@ -238,6 +238,7 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 	uint32_t first = 0, count = 0, k = 0;
 	const GpuStep* code = nullptr;
 	GpuStep next {};
+	float prev = 0.0f; // the result of the program's last step
 	uint32_t pc = 0, length = 0, resultSlot = 0;
 	float p[3]  = { 0.0f, 0.0f, 0.0f };
 	float least = 0.0f, second = 0.0f, nearest = 0.0f;
@@ -334,7 +335,7 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 			for (uint32_t u = 0; u < kStepsPerTurn; ++u) {
 				const GpuStep s = next;
 				if (pc + 1 < length) next = code[pc + 1];
-				runSlotStep(s, slots, stride, p);
+				prev            = marchStep(s, slots, stride, p, prev);
 				if (++pc == length) break;
 			}
 			if (pc == length) {

@@ -25,13 +25,17 @@ enum Op : uint8_t {
 
 // The march form's own operation codes: the common operations dense from 0,
 // every other one as kMarchRare + its reference opcode.
-// A negation is 0 - x, and a smooth minimum of constant radius r carries
-// 0.25 / r in the step's `leaf` field (MarchSminK); other smooth minima are
-// rare steps.
+// A negation is 0 - x (MarchSubtractFrom: b - a), and a smooth minimum of
+// constant radius r carries 0.25 / r in the step's `leaf` field
+// (MarchSminK); other smooth minima are rare steps.
 enum MarchOp : uint8_t {
-	MarchConstant, MarchPointX, MarchPointY, MarchPointZ, MarchAdd, MarchSubtract, MarchMultiply,
+	MarchConstant, MarchPointX, MarchPointY, MarchPointZ, MarchAdd, MarchSubtract, MarchSubtractFrom, MarchMultiply,
 	MarchSqrt, MarchAbs, MarchMin, MarchMax, MarchSminK, MarchPosSq
 };
+// GpuStep.flags of the march form
+constexpr uint16_t kFromPreviousA = 1; // operand a is the previous step's result, in a register
+constexpr uint16_t kFromPreviousB = 2; // operand b likewise
+constexpr uint16_t kNoStore       = 4; // the result is read only that way: no slot
 constexpr uint8_t kMarchRare = 64;
 
 constexpr uint32_t kNoLeaf     = 0xFFFFFFFFu;
@@ -50,7 +54,7 @@ struct GpuStep {
 	uint8_t dst;
 	uint8_t a, b, c;
 	uint8_t imm;
-	uint16_t pad1;
+	uint16_t flags; // the march form's kFromPrevious* / kNoStore
 	float value;
 	uint32_t leaf;
 };
