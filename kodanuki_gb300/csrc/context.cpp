@@ -128,7 +128,7 @@ kdn_status Context::build(const BuildOptions& options) {
 	if ((s = upload(programs, flat.programs.data(), flat.programs.size() * sizeof(GpuProgram))) != KDN_OK) return s;
 	if ((s = upload(steps, flat.steps.data(), flat.steps.size() * sizeof(GpuStep))) != KDN_OK) return s;
 	if ((s = upload(ssa, flat.ssa.data(), flat.ssa.size() * sizeof(SsaOps))) != KDN_OK) return s;
-	if ((s = upload(march, flat.march.data(), flat.march.size() * sizeof(GpuStep))) != KDN_OK) return s;
+	if ((s = upload(march, flat.march.data(), flat.march.size() * sizeof(MarchStep))) != KDN_OK) return s;
 	if ((s = upload(leafMaterial, leafMaterials.data(), leafMaterials.size() * sizeof(uint32_t))) != KDN_OK) return s;
 	if ((s = upload(objectMaterial, firstLeafMaterial.data(), firstLeafMaterial.size() * sizeof(uint32_t))) != KDN_OK) return s;
 	const std::vector<GridCell> cut = gridOf(flat, kGridLevel);
@@ -139,7 +139,7 @@ kdn_status Context::build(const BuildOptions& options) {
 	world.programs      = static_cast<const GpuProgram*>(programs.ptr);
 	world.steps         = static_cast<const GpuStep*>(steps.ptr);
 	world.ssa           = static_cast<const SsaOps*>(ssa.ptr);
-	world.march         = static_cast<const GpuStep*>(march.ptr);
+	world.march         = static_cast<const MarchStep*>(march.ptr);
 	world.leaf_material = static_cast<const uint32_t*>(leafMaterial.ptr);
 	world.grid          = static_cast<const GridCell*>(grid.ptr);
 	world.gridLevel     = kGridLevel;

@@ -517,181 +517,370 @@ std::string slotted(const Prog& p, std::vector<GpuStep>& steps, std::vector<SsaO
 	return "";
 }
 
-// world.h MarchOp of a reference opcode.
-uint8_t marchOpOf(uint8_t op) {
+// The march form of a program (world.h MarchStep).
+namespace march {
+
+// Where a lowered value lives: the result of lowered step `node`, an
+// immediate (kept in double until it is written), or a reserved slot (0, 1,
+// -1, the point's coordinates).  `from` is the reference step whose value
+// it is; `shared` marks a value read around a negation, which another step
+// may still read.
+struct Operand {
+	enum Kind : uint8_t { Node, Immediate, Reserved } kind = Reserved;
+	uint32_t node = 0;
+	double value  = 0.0;
+	uint8_t slot  = SlotZero;
+	uint32_t from = 0xFFFFFFFFu;
+	bool shared   = false;
+};
+
+Operand immediate(double v) {
+	Operand o;
+	o.kind  = Operand::Immediate;
+	o.value = v;
+	return o;
+}
+Operand reserved(uint8_t slot) {
+	Operand o;
+	o.kind = Operand::Reserved;
+	o.slot = slot;
+	return o;
+}
+
+// r = post(fma(a, b, c), w), or a rare reference operation over a, b, c.
+struct Node {
+	bool rare     = false;
+	uint8_t refOp = 0;
+	Operand a, b, c, w;
+	uint8_t post  = PostNone;
+	double radius = 0.0;
+	bool negation = false; // fma(x, -1, 0): -x
+	bool product  = false; // fma(x, y, 0) from a multiplication
+};
+
+// sdf/program.cpp:57 runStep in double, for steps of constants alone.
+double folded(uint8_t op, double a, double b, double c) {
 	switch (op) {
-		case OpConstant: return MarchConstant;
-		case OpPointX: return MarchPointX;
-		case OpPointY: return MarchPointY;
-		case OpPointZ: return MarchPointZ;
-		case OpAdd: return MarchAdd;
-		case OpSubtract: return MarchSubtract;
-		case OpMultiply: return MarchMultiply;
-		case OpSqrt: return MarchSqrt;
-		case OpAbs: return MarchAbs;
-		case OpMin: return MarchMin;
-		case OpMax: return MarchMax;
-		case OpPosSq: return MarchPosSq;
-		default: return uint8_t(kMarchRare + op);
+		case OpAdd: return a + b;
+		case OpSubtract: return a - b;
+		case OpMultiply: return a * b;
+		case OpDivide: return a / b;
+		case OpNegate: return -a;
+		case OpSqrt: return std::sqrt(a);
+		case OpAbs: return std::fabs(a);
+		case OpFloor: return std::floor(a);
+		case OpSin: return std::sin(a);
+		case OpCos: return std::cos(a);
+		case OpSign: return signOf(a);
+		case OpAtan2: return std::atan2(a, b);
+		case OpPow: return std::pow(a, b);
+		case OpMin: return lesser(a, b);
+		case OpMax: return greater(a, b);
+		case OpSmin: return smoothMin(a, b, c);
+		case OpPosSq: return positiveSquare(a);
+		case OpLess: return a < b ? 1.0 : 0.0;
+		case OpLessEq: return a <= b ? 1.0 : 0.0;
+		case OpEqual: return a == b ? 1.0 : 0.0;
+		case OpNotEqual: return a != b ? 1.0 : 0.0;
+		case OpAnd: return a != 0.0 && b != 0.0 ? 1.0 : 0.0;
+		case OpOr: return a != 0.0 || b != 0.0 ? 1.0 : 0.0;
+		case OpNot: return a == 0.0 ? 1.0 : 0.0;
+		case OpSelect: return a != 0.0 ? b : c;
+		default: return 0.0;
 	}
 }
 
-// The march form of a program (world.h MarchOp):
-//  - every constant a step reads becomes that step's immediate (one a step,
-//    the last constant operand); constants no step reads from a slot any
-//    more are left out;
-//  - a common operation takes its immediate as b (the operands of +, *, min
-//    and max are swapped, const - x is x subtracted from b), a smooth minimum
-//    of constant radius carries the radius and 0.25 / radius;
-//  - an operand that is the result of the step just before is read from a
-//    register (kFromPrevious*), and a result read only that way is not
-//    stored (kNoStore) and takes no slot;
-//  - the slots are allocated again over what remains.
-std::string marchCode(const Prog& p, std::vector<GpuStep>& steps, GpuProgram& out) {
+struct Lowering {
+	std::vector<Node> nodes;
+	std::vector<uint32_t> refUses; // consumers of each reference step (the result counts one)
+
+	Operand make(const Node& n, uint32_t from) {
+		nodes.push_back(n);
+		Operand o;
+		o.kind = Operand::Node;
+		o.node = uint32_t(nodes.size() - 1);
+		o.from = from;
+		return o;
+	}
+	static int immediates(const Node& n) {
+		return (n.a.kind == Operand::Immediate) + (n.b.kind == Operand::Immediate) + (n.c.kind == Operand::Immediate) +
+		       (n.w.kind == Operand::Immediate) + (n.post == PostSminK ? 1 : 0);
+	}
+	// a step that may take on more: its value has one reader, this one
+	bool open(const Operand& o) const {
+		return o.kind == Operand::Node && !o.shared && o.from != 0xFFFFFFFFu && refUses[o.from] == 1 && !nodes[o.node].rare &&
+		       nodes[o.node].post == PostNone;
+	}
+	// an immediate as a step of its own, where a step has room for one
+	Operand alone(const Operand& o, uint32_t from) {
+		if (o.kind != Operand::Immediate) return o;
+		Node n;
+		n.a = o;
+		n.b = reserved(SlotOne);
+		n.c = reserved(SlotZero);
+		Operand r = make(n, from);
+		r.shared  = true;
+		return r;
+	}
+};
+
+} // namespace march
+
+// Lower a program to the march form (world.h MarchStep): constants become
+// immediates (a step of constants alone is folded in double), the point is
+// read from reserved slots, +, -, * and negation become fused multiply-adds,
+// a product read only by a sum folds into it, double negations cancel, and
+// sqrt, |x|, max(x, 0)^2, min, max and a smooth minimum of constant radius
+// ride on the step that makes their operand where nothing else reads it.
+// Slots are then allocated over the steps the result needs.
+std::string marchCode(const Prog& p, std::vector<MarchStep>& steps, GpuProgram& out) {
+	using namespace march;
 	const uint32_t n = uint32_t(p.steps.size());
-	constexpr uint32_t kNone = 0xFFFFFFFFu;
-	std::vector<uint8_t> imm(n, 0), needed(n, 0);
-	needed[p.result] = 1;
+	Lowering L;
+	L.refUses.assign(n, 0);
 	for (uint32_t i = 0; i < n; ++i) {
 		const kdn_step& s    = p.steps[i];
-		const int k          = operandCount(s.opcode);
 		const uint32_t op[3] = { s.a, s.b, s.c };
-		if (s.opcode != OpConstant && s.opcode != OpArgument) {
-			for (int j = k - 1; j >= 0; --j) {
-				if (p.steps[op[j]].opcode == OpConstant) {
-					imm[i] = uint8_t(j + 1);
-					break;
-				}
-			}
-		}
-		for (int j = 0; j < k; ++j) {
-			if (imm[i] != j + 1) needed[op[j]] = 1;
-		}
+		for (int j = 0; j < operandCount(s.opcode); ++j) L.refUses[op[j]] += 1;
 	}
-	// the kept steps, and each one's form: op, operand sources (SSA index or kNone), immediate
-	struct Form {
-		uint8_t op;
-		uint8_t imm;
-		uint32_t src[3];
-		float value;
-		uint32_t leaf;
-		bool rare;
+	L.refUses[p.result] += 1;
+	const Operand zero = reserved(SlotZero), one = reserved(SlotOne), minusOne = reserved(SlotMinusOne);
+	const auto fma3 = [](const Operand& a, const Operand& b, const Operand& c) {
+		Node f;
+		f.a = a;
+		f.b = b;
+		f.c = c;
+		return f;
 	};
-	std::vector<Form> form(n);
-	std::vector<uint32_t> order;
+	std::vector<Operand> val(n);
 	for (uint32_t i = 0; i < n; ++i) {
 		const kdn_step& s = p.steps[i];
-		if (s.opcode == OpConstant && !needed[i]) continue;
-		order.push_back(i);
-		const int k          = operandCount(s.opcode);
-		const uint32_t op[3] = { s.a, s.b, s.c };
-		Form f;
-		f.op    = marchOpOf(s.opcode);
-		f.imm   = imm[i];
-		f.value = imm[i] ? float(p.steps[op[imm[i] - 1]].value) : (s.opcode == OpArgument ? 0.0f : float(s.value));
-		f.leaf  = s.leaf;
-		f.rare  = f.op >= kMarchRare;
-		for (int j = 0; j < 3; ++j) f.src[j] = j < k && imm[i] != j + 1 ? op[j] : kNone;
-		const bool commutes = s.opcode == OpAdd || s.opcode == OpMultiply || s.opcode == OpMin || s.opcode == OpMax;
-		if (s.opcode == OpNegate) {
-			if (imm[i] == 1) { // a negated constant is a constant
-				f.op    = MarchConstant;
-				f.imm   = 0;
-				f.value = -f.value;
-				f.src[0] = kNone;
-			} else { // -x as 0 - x
-				f.op  = MarchSubtractFrom;
-				f.imm = 2;
-				f.value = 0.0f;
+		const int k       = operandCount(s.opcode);
+		const Operand A = k > 0 ? val[s.a] : zero, B = k > 1 ? val[s.b] : zero, C = k > 2 ? val[s.c] : zero;
+		switch (s.opcode) {
+			case OpConstant: val[i] = immediate(s.value); continue;
+			case OpArgument: case OpNormalX: case OpNormalY: case OpNormalZ: val[i] = immediate(0.0); continue;
+			case OpPointX: val[i] = reserved(SlotX); continue;
+			case OpPointY: val[i] = reserved(SlotY); continue;
+			case OpPointZ: val[i] = reserved(SlotZ); continue;
+			default: break;
+		}
+		if (k > 0 && A.kind == Operand::Immediate && (k < 2 || B.kind == Operand::Immediate) && (k < 3 || C.kind == Operand::Immediate)) {
+			val[i] = immediate(folded(s.opcode, A.value, B.value, C.value));
+			continue;
+		}
+		const auto isNeg = [&](const Operand& o) { return o.kind == Operand::Node && L.nodes[o.node].negation; };
+		const auto inner = [&](const Operand& o) {
+			Operand x = L.nodes[o.node].a;
+			x.shared  = true;
+			return x;
+		};
+		switch (s.opcode) {
+			case OpNegate: {
+				if (isNeg(A)) {
+					val[i] = inner(A); // -(-x) = x
+				} else {
+					Node f     = fma3(A, minusOne, zero);
+					f.negation = true;
+					val[i]     = L.make(f, i);
+				}
+				continue;
 			}
-			f.rare = false;
-		} else if (s.opcode == OpSubtract && imm[i] == 1) {
-			f.op     = MarchSubtractFrom;
-			f.imm    = 2;
-			f.src[0] = op[1];
-			f.src[1] = kNone;
-		} else if (commutes && imm[i] == 1) {
-			f.imm    = 2;
-			f.src[0] = op[1];
-			f.src[1] = kNone;
-		} else if (s.opcode == OpSmin && imm[i] == 3 && f.value != 0.0f) {
-			const float quarter = 0.25f / f.value;
-			f.op                = MarchSminK;
-			std::memcpy(&f.leaf, &quarter, sizeof quarter);
-		} else if (!f.rare && imm[i] == 1) {
-			// a common unary operation of a constant: the general form
-			f.op   = uint8_t(kMarchRare + s.opcode);
-			f.rare = true;
-		}
-		if (s.opcode == OpSmin && f.op != MarchSminK) {
-			f.op   = uint8_t(kMarchRare + OpSmin);
-			f.rare = true;
-		}
-		form[i] = f;
-	}
-	// forwarding: an a or b operand that is the step just before
-	std::vector<uint16_t> flags(n, 0);
-	std::vector<uint8_t> stored(n, 0);
-	std::vector<uint32_t> lastRead(n, 0);
-	for (size_t e = 0; e < order.size(); ++e) {
-		const uint32_t i    = order[e];
-		const uint32_t prev = e > 0 ? order[e - 1] : kNone;
-		for (int j = 0; j < 3; ++j) {
-			const uint32_t src = form[i].src[j];
-			if (src == kNone) continue;
-			if (j < 2 && src == prev) {
-				flags[i] |= uint16_t(j == 0 ? kFromPreviousA : kFromPreviousB);
-			} else {
-				stored[src]   = 1;
-				lastRead[src] = std::max(lastRead[src], i);
+			case OpAdd: case OpSubtract: {
+				// x + y or x - y; x + (-y) = x - y, x - (-y) = x + y, (-x) + y = y - x
+				Operand x = A, y = B;
+				bool minus = s.opcode == OpSubtract;
+				if (isNeg(y)) {
+					y     = inner(y);
+					minus = !minus;
+				} else if (!minus && isNeg(x)) {
+					const Operand t = inner(x);
+					x               = y;
+					y               = t;
+					minus           = true;
+				}
+				if (!minus) {
+					// a product read only here: fma(p, q, other)
+					const Operand* pr[2] = { &x, &y };
+					bool done            = false;
+					for (int j = 0; j < 2 && !done; ++j) {
+						const Operand& m = *pr[j];
+						if (!L.open(m) || !L.nodes[m.node].product) continue;
+						const Node f = fma3(L.nodes[m.node].a, L.nodes[m.node].b, *pr[1 - j]);
+						if (Lowering::immediates(f) > 1) continue;
+						val[i] = L.make(f, i);
+						done   = true;
+					}
+					if (done) continue;
+					val[i] = L.make(fma3(x, one, y), i);
+				} else {
+					val[i] = L.make(fma3(y, minusOne, x), i);
+				}
+				continue;
 			}
+			case OpMultiply: {
+				Operand x = A, y = B;
+				if (isNeg(x) && isNeg(y)) {
+					x = inner(x);
+					y = inner(y);
+				}
+				Node f    = fma3(x, y, zero);
+				f.product = true;
+				if (Lowering::immediates(f) > 1) f.a = L.alone(f.a, i);
+				val[i] = L.make(f, i);
+				continue;
+			}
+			case OpSqrt: case OpAbs: case OpPosSq: {
+				const uint8_t post = s.opcode == OpSqrt ? PostSqrt : (s.opcode == OpAbs ? PostAbs : PostPosSq);
+				if (L.open(A)) {
+					Node& f    = L.nodes[A.node];
+					f.post     = post;
+					f.product  = false;
+					f.negation = false;
+					val[i]     = A;
+					val[i].from = i;
+				} else {
+					Node f = fma3(A, one, zero);
+					f.post = post;
+					val[i] = L.make(f, i);
+				}
+				continue;
+			}
+			case OpMin: case OpMax: case OpSmin: {
+				const bool smooth = s.opcode == OpSmin;
+				if (smooth && !(C.kind == Operand::Immediate && C.value != 0.0)) break; // a rare step
+				const uint8_t post = smooth ? PostSminK : (s.opcode == OpMin ? PostMin : PostMax);
+				Operand x = A, y = B;
+				if (smooth) { // the radius takes the step's immediate
+					x = L.alone(x, i);
+					y = L.alone(y, i);
+				}
+				// ride on the step making one operand (the operations are symmetric); the other is w
+				Operand host = x, other = y;
+				bool ride    = L.open(x);
+				if (!ride && L.open(y)) {
+					host  = y;
+					other = x;
+					ride  = true;
+				}
+				Operand wOp = other;
+				Node f      = ride ? L.nodes[host.node] : fma3(host, one, zero);
+				f.post      = post;
+				f.w         = wOp;
+				f.radius    = smooth ? C.value : 0.0;
+				f.product   = false;
+				f.negation  = false;
+				if (Lowering::immediates(f) > 1 && wOp.kind == Operand::Immediate) {
+					// w an immediate beside the step's own: w as a step of its own
+					wOp = L.alone(other, i);
+					f.w = wOp;
+				}
+				if (Lowering::immediates(f) > 1) {
+					// the riding step's immediate beside the radius: a step of its own
+					ride     = false;
+					f        = fma3(host, one, zero);
+					f.post   = post;
+					f.w      = wOp;
+					f.radius = smooth ? C.value : 0.0;
+				}
+				// the riding step is made again after its new operand w (the old one
+				// has no reader left), so every step still follows what it reads
+				val[i] = L.make(f, i);
+				continue;
+			}
+			default: break;
+		}
+		// a rare step: the reference operation over slots, one immediate at most
+		Node r;
+		r.rare  = true;
+		r.refOp = s.opcode;
+		r.a     = A;
+		r.b     = k > 1 ? B : zero;
+		r.c     = k > 2 ? C : zero;
+		bool seen = false;
+		for (Operand* o : { &r.a, &r.b, &r.c }) {
+			if (o->kind != Operand::Immediate) continue;
+			if (seen) *o = L.alone(*o, i);
+			seen = true;
+		}
+		val[i] = L.make(r, i);
+	}
+	// the result as a step
+	Operand result = val[p.result];
+	if (result.kind != Operand::Node) result = L.make(fma3(result, one, zero), p.result);
+	// the steps the result needs, and each one's last reader
+	const uint32_t m = uint32_t(L.nodes.size());
+	std::vector<uint8_t> live(m, 0);
+	live[result.node] = 1;
+	for (uint32_t j = m; j-- > 0;) {
+		if (!live[j]) continue;
+		const Node& x = L.nodes[j];
+		for (const Operand* o : { &x.a, &x.b, &x.c, &x.w }) {
+			if (o->kind == Operand::Node) live[o->node] = 1;
 		}
 	}
-	stored[p.result]   = 1;
-	lastRead[p.result] = n;
-	std::vector<uint8_t> slot(n, 0);
+	std::vector<uint32_t> lastRead(m, 0);
+	for (uint32_t j = 0; j < m; ++j) {
+		if (!live[j]) continue;
+		const Node& x   = L.nodes[j];
+		const bool usesW = x.post == PostMin || x.post == PostMax || x.post == PostSminK;
+		for (const Operand* o : { &x.a, &x.b, &x.c, &x.w }) {
+			if (o == &x.w && !usesW) continue;
+			if (o->kind == Operand::Node) lastRead[o->node] = std::max(lastRead[o->node], j);
+		}
+	}
+	lastRead[result.node] = m;
+	std::vector<uint8_t> slot(m, 0);
 	std::vector<uint8_t> freeSlots;
-	uint32_t used = 0;
+	uint32_t used = kMarchFirstSlot;
+	uint32_t kept = 0;
 	out.march     = uint32_t(steps.size());
-	for (const uint32_t i : order) {
-		const Form& f = form[i];
-		GpuStep g     = {};
-		g.op          = f.op;
-		g.imm         = f.imm;
-		g.value       = f.value;
-		g.leaf        = f.leaf;
-		g.flags       = flags[i];
-		g.a           = f.src[0] != kNone && !(flags[i] & kFromPreviousA) ? slot[f.src[0]] : 0;
-		g.b           = f.src[1] != kNone && !(flags[i] & kFromPreviousB) ? slot[f.src[1]] : 0;
-		g.c           = f.src[2] != kNone ? slot[f.src[2]] : 0;
-		// free the slots whose last read is this step (each value once)
-		for (int j = 0; j < 3; ++j) {
-			const uint32_t src = f.src[j];
-			if (src == kNone || (j == 0 && (flags[i] & kFromPreviousA)) || (j == 1 && (flags[i] & kFromPreviousB))) continue;
+	for (uint32_t j = 0; j < m; ++j) {
+		if (!live[j]) continue;
+		const Node& x    = L.nodes[j];
+		const bool usesW = x.post == PostMin || x.post == PostMax || x.post == PostSminK;
+		MarchStep g      = {};
+		g.op             = x.rare ? uint8_t(kMarchRare + x.refOp) : x.post;
+		double immValue  = 0.0;
+		const auto slotOf = [&](const Operand& o) -> uint8_t {
+			if (o.kind == Operand::Node) return slot[o.node];
+			if (o.kind == Operand::Immediate) {
+				immValue = o.value;
+				return SlotImm;
+			}
+			return o.slot;
+		};
+		g.a       = slotOf(x.a);
+		g.b       = slotOf(x.b);
+		g.c       = slotOf(x.c);
+		g.w       = usesW ? slotOf(x.w) : uint8_t(SlotZero);
+		g.value   = float(x.post == PostSminK ? x.radius : immValue);
+		g.quarter = x.post == PostSminK ? float(0.25 / x.radius) : 0.0f;
+		// free the slots read here for the last time (each value once)
+		const Operand* reads[4] = { &x.a, &x.b, &x.c, &x.w };
+		for (int r = 0; r < 4; ++r) {
+			const Operand* o = reads[r];
+			if (r == 3 && !usesW) continue;
+			if (o->kind != Operand::Node || lastRead[o->node] != j) continue;
 			bool first = true;
-			for (int m = 0; m < j; ++m) {
-				const bool viaSlot = !((m == 0 && (flags[i] & kFromPreviousA)) || (m == 1 && (flags[i] & kFromPreviousB)));
-				first              = first && !(viaSlot && f.src[m] == src);
-			}
-			if (first && stored[src] && lastRead[src] == i) freeSlots.push_back(slot[src]);
+			for (int q = 0; q < r; ++q) first = first && !(reads[q]->kind == Operand::Node && reads[q]->node == o->node);
+			if (first) freeSlots.push_back(slot[o->node]);
 		}
-		if (stored[i]) {
-			if (!freeSlots.empty()) {
-				slot[i] = freeSlots.back();
-				freeSlots.pop_back();
-			} else {
-				if (used >= kMaxSlots) return "a leaf program needs more than " + std::to_string(kMaxSlots) + " register slots";
-				slot[i] = uint8_t(used++);
-			}
-			g.dst = slot[i];
+		if (!freeSlots.empty()) {
+			slot[j] = freeSlots.back();
+			freeSlots.pop_back();
 		} else {
-			g.flags |= kNoStore;
+			if (used >= kMaxSlots) return "a leaf program needs more than " + std::to_string(kMaxSlots) + " register slots";
+			slot[j] = uint8_t(used++);
 		}
+		if (lastRead[j] == j) freeSlots.push_back(slot[j]);
+		g.dst = slot[j];
 		steps.push_back(g);
+		++kept;
 	}
-	out.marchCount = uint16_t(order.size());
-	out.marchSlot  = slot[p.result];
-	out.marchSlots = uint8_t(std::max(used, 1u));
+	out.marchCount = uint16_t(kept);
+	out.marchSlot  = slot[result.node];
+	out.marchSlots = uint8_t(used);
 	return "";
 }
 

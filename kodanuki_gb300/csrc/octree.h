@@ -48,7 +48,7 @@ struct FlatWorld {
 	std::vector<GpuProgram> programs; // one run per leaf
 	std::vector<GpuStep> steps;
 	std::vector<SsaOps> ssa;
-	std::vector<GpuStep> march; // the march form, constants as immediates
+	std::vector<MarchStep> march; // the march form (world.h MarchStep)
 };
 
 // Returns an empty string, or what went wrong.

@@ -82,63 +82,54 @@ KDN_HD float stepValue(uint8_t op, float a, float b, float c, float value, const
 	}
 }
 
-// A rare step of the march form (marchOp >= kMarchRare): the reference
-// opcode it carries.
-KDN_HD float rareMarchValue(uint8_t op, float a, float b, float c, float value, float x, float y, float z) {
-	const float p[3] = { x, y, z };
-	return stepValue(uint8_t(op - kMarchRare), a, b, c, value, p);
+// The reserved slots of a thread's column: 0, 1 and -1 once, the point at
+// each new point.
+KDN_HD void setConstants(float* slots, uint32_t stride) {
+	slots[SlotZero * stride]     = 0.0f;
+	slots[SlotOne * stride]      = 1.0f;
+	slots[SlotMinusOne * stride] = -1.0f;
 }
 
-// A common step of the march form (world.h MarchOp): the operations are
-// worked out together and the step's picked, so the lanes of a warp running
-// different operations do not split.  b may be the immediate; `value` is
-// the constant, or the radius of a smooth minimum with `quarter` = 0.25 / r.
-KDN_HD float marchValue(uint8_t op, float a, float b, float value, float quarter, const float p[3]) {
-	// the smooth minimum of constant radius r: min - max(r - |a - b|, 0)^2 * 0.25 / r
-	const float m = fmaxf(value - fabsf(a - b), 0.0f);
-	const float q = fmaxf(a, 0.0f);
-	float r       = value;
-	r             = op == MarchPointX ? p[0] : r;
-	r             = op == MarchPointY ? p[1] : r;
-	r             = op == MarchPointZ ? p[2] : r;
-	r             = op == MarchAdd ? a + b : r;
-	r             = op == MarchSubtract ? a - b : r;
-	r             = op == MarchSubtractFrom ? b - a : r;
-	r             = op == MarchMultiply ? a * b : r;
-	r             = op == MarchSqrt ? sqrtf(a) : r;
-	r             = op == MarchAbs ? fabsf(a) : r;
-	r             = op == MarchMin ? (b < a ? b : a) : r;
-	r             = op == MarchMax ? (a < b ? b : a) : r;
-	r             = op == MarchSminK ? fminf(a, b) - m * m * quarter : r;
-	r             = op == MarchPosSq ? q * q : r;
-	return r;
+KDN_HD void setPoint(float* slots, uint32_t stride, const float p[3]) {
+	slots[SlotX * stride] = p[0];
+	slots[SlotY * stride] = p[1];
+	slots[SlotZ * stride] = p[2];
 }
 
-// One step of the march form.  Operands come from the thread's slots, from
-// the immediate, or (kFromPrevious*) from `prev`, the result of the step
-// before, which stays in a register; a kNoStore result is not written.
-// Returns the step's result, the next step's `prev`.
-KDN_HD float marchStep(const GpuStep& s, float* slots, uint32_t stride, const float p[3], float prev) {
+// One step of the march form (world.h MarchStep): r = post(fma(a, b, c), w)
+// with the post operations worked out together and the step's picked, so
+// the lanes of a warp on different steps do not split; a rare step runs the
+// reference operation.  Writes the result to its slot and returns it.
+KDN_HD float marchStep(const MarchStep& s, float* slots, uint32_t stride) {
+	slots[SlotImm * stride] = s.value;
+	const float a = slots[s.a * stride], b = slots[s.b * stride], c = slots[s.c * stride];
 	float r;
 	if (s.op >= kMarchRare) {
-		const float a = s.imm == 1 ? s.value : ((s.flags & kFromPreviousA) ? prev : slots[s.a * stride]);
-		const float b = s.imm == 2 ? s.value : ((s.flags & kFromPreviousB) ? prev : slots[s.b * stride]);
-		const float c = s.imm == 3 ? s.value : slots[s.c * stride];
-		r             = rareMarchValue(s.op, a, b, c, s.value, p[0], p[1], p[2]);
+		const float p[3] = { slots[SlotX * stride], slots[SlotY * stride], slots[SlotZ * stride] };
+		r                = stepValue(uint8_t(s.op - kMarchRare), a, b, c, s.value, p);
 	} else {
-		const float a = (s.flags & kFromPreviousA) ? prev : slots[s.a * stride];
-		const float b = s.imm == 2 ? s.value : ((s.flags & kFromPreviousB) ? prev : slots[s.b * stride]);
-		r             = marchValue(s.op, a, b, s.value, floatOfBits(s.leaf), p);
+		const float w = slots[s.w * stride];
+		const float f = fmaf(a, b, c);
+		const float q = fmaxf(f, 0.0f);
+		// the smooth minimum of radius r = value: min - max(r - |f - w|, 0)^2 * 0.25 / r
+		const float m = fmaxf(s.value - fabsf(f - w), 0.0f);
+		r             = f;
+		r             = s.op == PostSqrt ? sqrtf(f) : r;
+		r             = s.op == PostAbs ? fabsf(f) : r;
+		r             = s.op == PostPosSq ? q * q : r;
+		r             = s.op == PostMin ? (w < f ? w : f) : r;
+		r             = s.op == PostMax ? (f < w ? w : f) : r;
+		r             = s.op == PostSminK ? fminf(f, w) - m * m * s.quarter : r;
 	}
-	if (!(s.flags & kNoStore)) slots[s.dst * stride] = r;
+	slots[s.dst * stride] = r;
 	return r;
 }
 
 // One program at one point; slots is this thread's column base (stride
-// blockDim.x).  Returns the program's value.
-KDN_HD float evalSlots(const GpuStep* __restrict__ code, uint32_t count, uint32_t resultSlot, float* slots, uint32_t stride, const float p[3]) {
-	float prev = 0.0f;
-	for (uint32_t i = 0; i < count; ++i) prev = marchStep(code[i], slots, stride, p, prev);
+// blockDim.x), with the constants set.  Returns the program's value.
+KDN_HD float evalSlots(const MarchStep* __restrict__ code, uint32_t count, uint32_t resultSlot, float* slots, uint32_t stride, const float p[3]) {
+	setPoint(slots, stride, p);
+	for (uint32_t i = 0; i < count; ++i) marchStep(code[i], slots, stride);
 	return slots[resultSlot * stride];
 }
 

@@ -220,6 +220,7 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 	const DeviceWorld& w  = args.world;
 	const uint32_t stride = blockDim.x;
 	float* slots          = slotMemory + threadIdx.x;
+	setConstants(slots, stride);
 	uint32_t marchSteps = 0, programSteps = 0, traced = 0, capped = 0, longest = 0;
 	const uint32_t n = args.count ? *args.count : args.n;
 	const unsigned lane = threadIdx.x & 31u;
@@ -236,9 +237,8 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 	float exitT = 0.0f;
 	// the cell being evaluated: its run of kept programs and the one in hand
 	uint32_t first = 0, count = 0, k = 0;
-	const GpuStep* code = nullptr;
-	GpuStep next {};
-	float prev = 0.0f; // the result of the program's last step
+	const MarchStep* code = nullptr;
+	MarchStep next {};
 	uint32_t pc = 0, length = 0, resultSlot = 0;
 	float p[3]  = { 0.0f, 0.0f, 0.0f };
 	float least = 0.0f, second = 0.0f, nearest = 0.0f;
@@ -326,6 +326,7 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 				pc         = 0;
 				next       = code[0];
 				mode       = Evaluating;
+				setPoint(slots, stride, p);
 				break;
 			}
 		}
@@ -333,9 +334,9 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 		// a few program steps; each step's code is loaded a step ahead
 		if (mode == Evaluating) {
 			for (uint32_t u = 0; u < kStepsPerTurn; ++u) {
-				const GpuStep s = next;
+				const MarchStep s = next;
 				if (pc + 1 < length) next = code[pc + 1];
-				prev            = marchStep(s, slots, stride, p, prev);
+				marchStep(s, slots, stride);
 				if (++pc == length) break;
 			}
 			if (pc == length) {

@@ -23,20 +23,29 @@ enum Op : uint8_t {
 	OpNotEqual, OpAnd, OpOr, OpNot, OpSelect, OpCount
 };
 
-// The march form's own operation codes: the common operations dense from 0,
-// every other one as kMarchRare + its reference opcode.
-// A negation is 0 - x (MarchSubtractFrom: b - a), and a smooth minimum of
-// constant radius r carries 0.25 / r in the step's `leaf` field
-// (MarchSminK); other smooth minima are rare steps.
-enum MarchOp : uint8_t {
-	MarchConstant, MarchPointX, MarchPointY, MarchPointZ, MarchAdd, MarchSubtract, MarchSubtractFrom, MarchMultiply,
-	MarchSqrt, MarchAbs, MarchMin, MarchMax, MarchSminK, MarchPosSq
-};
-// GpuStep.flags of the march form
-constexpr uint16_t kFromPreviousA = 1; // operand a is the previous step's result, in a register
-constexpr uint16_t kFromPreviousB = 2; // operand b likewise
-constexpr uint16_t kNoStore       = 4; // the result is read only that way: no slot
+// The march form: a program lowered to steps r = post(fma(a, b, c), w).
+// +, -, * and negation are one fused multiply-add each (x + y = fma(x, 1,
+// y), x - y = fma(y, -1, x), x * y = fma(x, y, 0)); a product that feeds only
+// a sum folds into it; sqrt, |x|, max(x, 0)^2, min, max and a smooth minimum
+// of constant radius ride on the step that makes their operand where that
+// step's result has no other use; double negations cancel.  Operands are
+// slots of the thread's column: the first kMarchFirstSlot hold 0, 1, -1, the
+// point and the step's immediate.  Every other reference operation is a
+// rare step (kMarchRare + opcode) over slots a, b, c.
+enum MarchPost : uint8_t { PostNone, PostSqrt, PostAbs, PostPosSq, PostMin, PostMax, PostSminK };
 constexpr uint8_t kMarchRare = 64;
+enum MarchSlot : uint8_t { SlotZero, SlotOne, SlotMinusOne, SlotX, SlotY, SlotZ, SlotImm, kMarchFirstSlot };
+
+struct MarchStep {
+	uint8_t op;  // MarchPost, or kMarchRare + reference opcode
+	uint8_t dst; // slot of the result
+	uint8_t a, b, c;
+	uint8_t w;   // the post operation's second operand (min, max, smooth minimum)
+	uint16_t pad;
+	float value;   // the immediate (SlotImm); a smooth minimum's radius
+	float quarter; // 0.25 / radius of a smooth minimum
+};
+static_assert(sizeof(MarchStep) == 16, "MarchStep is 16 bytes");
 
 constexpr uint32_t kNoLeaf     = 0xFFFFFFFFu;
 constexpr uint32_t kMaxSlots   = 48;   // register slots a leaf program may use
@@ -46,15 +55,14 @@ constexpr uint32_t kMaxLeafProgs = 64; // kept programs of one leaf
 // skims a surface for longer meets nothing.
 constexpr uint32_t kMarchSteps = 1u << 16;
 
-// In the march form a step may read one operand as an immediate: `imm` says
-// which (1 a, 2 b, 3 c; 0 none) and `value` holds it, so the constants a
-// program's steps read take no step and no slot of their own.
+// A step of a program's full form, read once a hit: register slots a, b,
+// c, the reference opcode and constant, and the leaf a step names.
 struct GpuStep {
 	uint8_t op;
 	uint8_t dst;
 	uint8_t a, b, c;
 	uint8_t imm;
-	uint16_t flags; // the march form's kFromPrevious* / kNoStore
+	uint16_t pad1;
 	float value;
 	uint32_t leaf;
 };
@@ -73,7 +81,7 @@ struct GpuProgram {
 	uint8_t slots;       // slots used
 	uint16_t marchCount; // steps of the march form
 	uint32_t object;     // index into the scene's object programs
-	uint32_t march;      // first GpuStep of the march form (constants as immediates)
+	uint32_t march;      // first MarchStep of the march form
 	uint8_t marchSlot;   // slot of the result in the march form
 	uint8_t marchSlots;
 	uint16_t pad0;
@@ -108,7 +116,7 @@ struct DeviceWorld {
 	const GpuLeaf* leaves;
 	const GpuProgram* programs;
 	const GpuStep* steps;
-	const GpuStep* march;
+	const MarchStep* march;
 	const SsaOps* ssa;
 	const uint32_t* leaf_material;
 	const GridCell* grid; // (2^gridLevel)^3 cells, x fastest; null: descend from the root

@@ -24,9 +24,10 @@ extern "C" kdn_status kdn_world_march(kdn_ctx* handle, uint64_t i, const float* 
 	*programs                = leaf.count;
 	if (size_t(leaf.count) * n > capacity) return ctx->fail(KDN_BAD_ARG, "kdn_world_march: values too small");
 	std::vector<float> slots(kdn::kMaxSlots);
+	kdn::setConstants(slots.data(), 1);
 	for (uint32_t k = 0; k < leaf.count; ++k) {
 		const kdn::GpuProgram& g = ctx->flat.programs[leaf.first + k];
-		const kdn::GpuStep* code = ctx->flat.march.data() + g.march;
+		const kdn::MarchStep* code = ctx->flat.march.data() + g.march;
 		for (uint32_t j = 0; j < n; ++j) values[size_t(k) * n + j] = kdn::evalSlots(code, g.marchCount, g.marchSlot, slots.data(), 1, points + 3 * size_t(j));
 	}
 	return KDN_OK;

@@ -712,13 +712,19 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 static void* worker(void* arg) {
 	job* J = (job*) arg;
 	kp_tracer* tracer = kp_tracer_new(J->tree, J->leaf_material);
+	/* work in runs of 16 pixels of a row, so a band of few rows still
+	 * spreads over every thread */
+	const int runs = (J->view->width + 15) / 16;
 	for (;;) {
 		pthread_mutex_lock(&J->lock);
-		const int row = J->next++;
+		const int item = J->next++;
 		pthread_mutex_unlock(&J->lock);
-		if (row >= J->rows) break;
+		if (item >= J->rows * runs) break;
+		const int row = item / runs;
 		const int y = J->row0 + row;
-		for (int x = 0; x < J->view->width; ++x) {
+		const int x0 = (item % runs) * 16;
+		const int x1 = x0 + 16 < J->view->width ? x0 + 16 : J->view->width;
+		for (int x = x0; x < x1; ++x) {
 			double sum[3] = { 0, 0, 0 };
 			for (int k = 0; k < J->view->spp; ++k) {
 				double rgb[3];
