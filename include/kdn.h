@@ -240,6 +240,10 @@ kdn_status kdn_world_cell(kdn_ctx* ctx, uint64_t i, uint32_t head[6], uint32_t* 
  * cell's programs (the same interpreter as the device's, FP32).
  * KDN_NOT_READY where the device layout could not be made. */
 kdn_status kdn_world_march(kdn_ctx* ctx, uint64_t i, const float* points, uint32_t n, float* values, size_t capacity, uint32_t* programs);
+/* The leaf of each of n points (x, y, z floats) as the trace kernel locates
+ * it (the level-6 grid, then the descent) and by the descent from the root,
+ * both run on the host: the two must name the same leaf for every point. */
+kdn_status kdn_world_locate(kdn_ctx* ctx, const float* points, uint32_t n, uint32_t* by_grid, uint32_t* by_descent);
 
 /* ExtendRays (core/step.cpp:132): the first hit of each ray, host arrays in
  * and out (a host-to-device and device-to-host copy each call). */

@@ -77,7 +77,7 @@ class KdnError(RuntimeError):
 EXPORTS = [
     "kdn_status_string", "kdn_last_error", "kdn_open", "kdn_close", "kdn_upload_block", "kdn_build", "kdn_world_stats",
     "kdn_world_cell", "kdn_extend", "kdn_extend_device", "kdn_render", "kdn_render_device", "kdn_frame_stats_get", "kdn_flush_l2",
-    "kdn_frame_surfaces", "kdn_world_march", "kdn_denoise", "kdn_denoise_device", "kdn_denoise_static",
+    "kdn_frame_surfaces", "kdn_world_march", "kdn_world_locate", "kdn_denoise", "kdn_denoise_device", "kdn_denoise_static",
 ]
 
 
@@ -117,6 +117,7 @@ def library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.kdn_flush_l2.argtypes = [P]
     L.kdn_frame_surfaces.argtypes = [P, P, P, P, P]
     L.kdn_world_march.argtypes = [P, ctypes.c_uint64, P, ctypes.c_uint32, P, ctypes.c_size_t, P]
+    L.kdn_world_locate.argtypes = [P, P, ctypes.c_uint32, P, P]
     L.kdn_denoise.argtypes = [P, ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P]
     L.kdn_denoise_device.argtypes = [P, ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P, P]
     L.kdn_denoise_static.argtypes = [ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P, P]
@@ -289,6 +290,15 @@ class Backend:
         values = np.zeros(cap, np.float32)
         self._check(self.lib.kdn_world_march(self.handle, i, _ptr(pts), pts.shape[0], _ptr(values), cap, ctypes.byref(count)))
         return values[: count.value * pts.shape[0]].reshape(count.value, pts.shape[0])
+
+    def world_locate(self, points: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        """The leaf of each point by the trace kernel's grid locate and by the
+        descent from the root, on the host (include/kdn.h kdn_world_locate)."""
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+        a = np.zeros(len(pts), np.uint32)
+        b = np.zeros(len(pts), np.uint32)
+        self._check(self.lib.kdn_world_locate(self.handle, _ptr(pts), len(pts), _ptr(a), _ptr(b)))
+        return a, b
 
     def frame_surfaces(self, width: int, height: int) -> dict:
         """The first surfaces of the last frame drawn with denoise=True

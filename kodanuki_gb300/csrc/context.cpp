@@ -28,7 +28,7 @@ void Context::release() {
 	cudaSetDevice(device);
 	if (stream) cudaStreamSynchronize(stream);
 	releaseFrame();
-	for (DeviceBuffer* b : { &nodes, &leaves, &programs, &steps, &march, &ssa, &leafMaterial, &objectMaterial, &grid, &extendRays, &extendHits, &extendStates, &counters, &l2, &denoiseScratch, &denoiseIo, &fetch }) freeBuffer(*b);
+	for (DeviceBuffer* b : { &nodes, &leaves, &programs, &steps, &march, &ssa, &leafMaterial, &objectMaterial, &grid, &gridWalls, &extendRays, &extendHits, &extendStates, &counters, &l2, &denoiseScratch, &denoiseIo, &fetch }) freeBuffer(*b);
 	if (stream) cudaStreamDestroy(stream);
 	stream = nullptr;
 }
@@ -104,6 +104,17 @@ kdn_status Context::build(const BuildOptions& options) {
 		flat      = FlatWorld();
 		flatError = message;
 	}
+	// the grid over the flat octree, for locating points
+	gridCells.clear();
+	walls.clear();
+	for (int a = 0; a < 3; ++a) {
+		lowerF[a] = float(regions[0].lower[a]);
+		sizeF[a]  = float(regions[0].size[a]);
+	}
+	if (!flat.nodes.empty()) {
+		gridCells = gridOf(flat, kGridLevel);
+		walls     = gridWallsOf(lowerF, sizeF, kGridLevel);
+	}
 	// depth-first order of the cells, for kdn_world_cell
 	preorder.clear();
 	preorder.reserve(octree.cells.size());
@@ -131,8 +142,8 @@ kdn_status Context::build(const BuildOptions& options) {
 	if ((s = upload(march, flat.march.data(), flat.march.size() * sizeof(MarchStep))) != KDN_OK) return s;
 	if ((s = upload(leafMaterial, leafMaterials.data(), leafMaterials.size() * sizeof(uint32_t))) != KDN_OK) return s;
 	if ((s = upload(objectMaterial, firstLeafMaterial.data(), firstLeafMaterial.size() * sizeof(uint32_t))) != KDN_OK) return s;
-	const std::vector<GridCell> cut = gridOf(flat, kGridLevel);
-	if ((s = upload(grid, cut.data(), cut.size() * sizeof(GridCell))) != KDN_OK) return s;
+	if ((s = upload(grid, gridCells.data(), gridCells.size() * sizeof(GridCell))) != KDN_OK) return s;
+	if ((s = upload(gridWalls, walls.data(), walls.size() * sizeof(float))) != KDN_OK) return s;
 	if (!check(cudaStreamSynchronize(stream), "kdn_build upload")) return KDN_CUDA_ERROR;
 	world.nodes         = static_cast<const int32_t*>(nodes.ptr);
 	world.leaves        = static_cast<const GpuLeaf*>(leaves.ptr);
@@ -142,10 +153,12 @@ kdn_status Context::build(const BuildOptions& options) {
 	world.march         = static_cast<const MarchStep*>(march.ptr);
 	world.leaf_material = static_cast<const uint32_t*>(leafMaterial.ptr);
 	world.grid          = static_cast<const GridCell*>(grid.ptr);
+	world.gridWalls     = static_cast<const float*>(gridWalls.ptr);
 	world.gridLevel     = kGridLevel;
 	for (int a = 0; a < 3; ++a) {
 		world.lower[a] = float(regions[0].lower[a]);
 		world.size[a]  = float(regions[0].size[a]);
+		world.gridScale[a] = float(double(1u << kGridLevel) / double(world.size[a]));
 	}
 	world.leaf_count     = uint32_t(flat.leaves.size());
 	world.material_count = uint32_t(block<kdn_material>("looks.materials").size());

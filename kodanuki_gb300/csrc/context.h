@@ -35,9 +35,12 @@ struct Context {
 	Octree octree;
 	FlatWorld flat;
 	std::string flatError; // why a host-only context has no device layout
+	std::vector<GridCell> gridCells; // the grid over the flat octree (world.h GridCell)
+	std::vector<float> walls;        // its walls per axis
+	float lowerF[3] = {}, sizeF[3] = {};
 	std::vector<int64_t> preorder; // cell index of each depth-first position
 	DeviceWorld world {};
-	DeviceBuffer nodes, leaves, programs, steps, march, ssa, leafMaterial, objectMaterial, grid;
+	DeviceBuffer nodes, leaves, programs, steps, march, ssa, leafMaterial, objectMaterial, grid, gridWalls;
 	DeviceBuffer extendRays, extendHits, extendStates, counters, l2;
 	DeviceBuffer denoiseScratch, denoiseIo, fetch;
 	FrameState* frame = nullptr;

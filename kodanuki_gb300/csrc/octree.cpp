@@ -930,7 +930,31 @@ std::string flattenOctree(const Octree& tree, FlatWorld& flat) {
 	runs.reserve(flat.leafPrograms.size());
 	for (uint32_t k : flat.leafPrograms) runs.push_back(flat.programs[k]);
 	flat.programs.swap(runs);
+	for (GpuLeaf& leaf : flat.leaves) {
+		if (leaf.count == 0) continue;
+		const GpuProgram& g = flat.programs[leaf.first];
+		leaf.march          = g.march;
+		leaf.marchCount     = g.marchCount;
+		leaf.marchSlot      = g.marchSlot;
+	}
 	return "";
+}
+
+std::vector<float> gridWallsOf(const float lower[3], const float size[3], uint32_t level) {
+	const uint32_t n = 1u << level;
+	std::vector<float> walls(3 * size_t(n + 1));
+	for (int a = 0; a < 3; ++a) {
+		float* w = walls.data() + size_t(a) * (n + 1);
+		w[0]     = lower[a];
+		w[n]     = lower[a] + size[a];
+		for (uint32_t stride = n; stride > 1; stride /= 2) {
+			for (uint32_t i = 0; i < n; i += stride) {
+				const volatile float sum = w[i] + w[i + stride]; // as the descent: the sum, then the half
+				w[i + stride / 2]        = 0.5f * sum;
+			}
+		}
+	}
+	return walls;
 }
 
 std::vector<GridCell> gridOf(const FlatWorld& flat, uint32_t level) {

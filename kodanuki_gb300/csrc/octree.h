@@ -56,5 +56,8 @@ std::string buildOctree(const std::vector<ProgPtr>& objects, const double lower[
 std::string flattenOctree(const Octree& tree, FlatWorld& flat);
 // The grid of `level` over a flattened octree (world.h GridCell).
 std::vector<GridCell> gridOf(const FlatWorld& flat, uint32_t level);
+// The walls of that grid per axis (3 x (2^level + 1)): the descent's
+// midpoints in FP32 over [lower, lower + size].
+std::vector<float> gridWallsOf(const float lower[3], const float size[3], uint32_t level);
 
 } // namespace kdn

@@ -9,6 +9,7 @@
 // K-hit then evaluates the winning program once in duals for the normal and
 // once by step number for its source leaf (sphere_trace.cpp:115 sphereField).
 #include "kernels.h"
+#include "locate.cuh"
 #include "program.cuh"
 
 #include <cuda_runtime.h>
@@ -34,67 +35,14 @@ __device__ __forceinline__ float tolerance(const float p[3]) {
 
 __device__ __forceinline__ float nudge(float t) { return fmaxf(1e-5f, fabsf(t) * 2e-6f); }
 
-struct Located {
-	uint32_t leaf;
-	float lo[3], hi[3];
-};
-
-// The midpoint tests of `levels` levels of descent, in registers: the box
-// they leave and the grid coordinates of the cell.
-__device__ __forceinline__ uint32_t descendBox(const DeviceWorld& w, const float p[3], uint32_t levels, Located& l) {
+__device__ __forceinline__ float cellExitBy(const float o[3], const float inv[3], const Located& l) {
+	float up = 3.0e38f;
 	for (int a = 0; a < 3; ++a) {
-		l.lo[a] = w.lower[a];
-		l.hi[a] = w.lower[a] + w.size[a];
+		const float x = (l.lo[a] - o[a]) * inv[a];
+		const float y = (l.hi[a] - o[a]) * inv[a];
+		up            = fminf(up, fmaxf(x, y));
 	}
-	uint32_t cx = 0, cy = 0, cz = 0;
-	for (uint32_t level = 0; level < levels; ++level) {
-		uint32_t bit[3];
-		for (int a = 0; a < 3; ++a) {
-			const float mid = 0.5f * (l.lo[a] + l.hi[a]);
-			bit[a]          = p[a] >= mid ? 1u : 0u;
-			if (bit[a]) l.lo[a] = mid;
-			else l.hi[a] = mid;
-		}
-		cx = (cx << 1) | bit[0];
-		cy = (cy << 1) | bit[1];
-		cz = (cz << 1) | bit[2];
-	}
-	return (cz << (2 * levels)) | (cy << levels) | cx;
-}
-
-__device__ __forceinline__ Located locate(const DeviceWorld& w, const float p[3]) {
-	Located l;
-	int32_t node;
-	if (w.grid != nullptr) {
-		// the grid's level of the descent without loads, then the node there
-		const GridCell g = w.grid[descendBox(w, p, w.gridLevel, l)];
-		node             = g.node;
-		// a leaf above the grid's level: the box of that level
-		if (g.level < w.gridLevel) descendBox(w, p, g.level, l);
-	} else {
-		for (int a = 0; a < 3; ++a) {
-			l.lo[a] = w.lower[a];
-			l.hi[a] = w.lower[a] + w.size[a];
-		}
-		node = __ldg(&w.nodes[0]);
-	}
-	uint32_t at = 0;
-	for (int depth = 0; depth < 30 && node >= 0; ++depth) {
-		int o = 0;
-		for (int a = 0; a < 3; ++a) {
-			const float mid = 0.5f * (l.lo[a] + l.hi[a]);
-			if (p[a] >= mid) {
-				o |= 1 << a;
-				l.lo[a] = mid;
-			} else {
-				l.hi[a] = mid;
-			}
-		}
-		at   = uint32_t(node) + uint32_t(o);
-		node = __ldg(&w.nodes[at]);
-	}
-	l.leaf = uint32_t(~node);
-	return l;
+	return up;
 }
 
 __device__ __forceinline__ float cellExit(const float o[3], const float d[3], const Located& l) {
@@ -227,7 +175,7 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 
 	uint32_t mode = Fetch;
 	uint32_t ray  = 0;
-	float o[3], d[3];
+	float o[3], d[3], inv[3];
 	float t = 0.0f, up = 0.0f;
 	bool inside      = false;
 	uint32_t medium  = kNoLeaf;
@@ -269,15 +217,15 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 					++traced;
 					const kdn_ray r = args.rays[ray];
 					for (int a = 0; a < 3; ++a) {
-						o[a] = r.origin[a];
-						d[a] = r.direction[a];
+						o[a]   = r.origin[a];
+						d[a]   = r.direction[a];
+						inv[a] = slopeOf(d[a]);
 					}
 					float lo = 0.0f;
 					up       = r.far;
 					for (int a = 0; a < 3; ++a) {
-						const float inv = slopeOf(d[a]);
-						const float x   = (w.lower[a] - o[a]) * inv;
-						const float y   = (w.lower[a] + w.size[a] - o[a]) * inv;
+						const float x = (w.lower[a] - o[a]) * inv[a];
+						const float y = (w.lower[a] + w.size[a] - o[a]) * inv[a];
 						lo            = fmaxf(lo, fminf(x, y));
 						up            = fminf(up, fmaxf(x, y));
 					}
@@ -306,7 +254,7 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 				for (int a = 0; a < 3; ++a) p[a] = o[a] + d[a] * t;
 				if (!within(cell, p)) cell = locate(w, p);
 				const GpuLeaf leaf = w.leaves[cell.leaf];
-				exitT              = cellExit(o, d, cell);
+				exitT              = cellExitBy(o, inv, cell);
 				if (leaf.occupancy == Empty || leaf.count == 0) {
 					t = fmaxf(exitT, t) + nudge(t);
 					++step;
@@ -319,10 +267,9 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 				second  = 3.0e38f;
 				nearest = 3.0e38f;
 				index   = 0;
-				const GpuProgram g = w.programs[first];
-				code       = w.march + g.march;
-				length     = g.marchCount;
-				resultSlot = g.marchSlot;
+				code       = w.march + leaf.march;
+				length     = leaf.marchCount;
+				resultSlot = leaf.marchSlot;
 				pc         = 0;
 				next       = code[0];
 				mode       = Evaluating;

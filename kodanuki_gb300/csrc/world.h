@@ -96,14 +96,21 @@ struct GpuLeaf {
 	uint16_t count;     // kept programs
 	uint8_t occupancy;
 	uint8_t slots;      // most slots of its programs
+	// the first program's march form, read with the leaf
+	uint32_t march;
+	uint16_t marchCount;
+	uint8_t marchSlot;
+	uint8_t pad;
 };
-static_assert(sizeof(GpuLeaf) == 8, "GpuLeaf is 8 bytes");
+static_assert(sizeof(GpuLeaf) == 16, "GpuLeaf is 16 bytes");
 
 // The octree cut across at one level: for each cell of the uniform grid of
 // that level, the node value there (first child, or ~leaf) and its level,
 // less than the grid's where a leaf above it covers the cell.  A point is
-// located by the grid's level of midpoint tests in registers, one load, and
-// the descent below it.
+// located by its grid cell (an estimate from its coordinates, set right
+// against the grid's walls), one load, and the descent below it.  The walls
+// are the descent's own midpoints, 0.5 * (lo + hi) level by level in FP32,
+// so a point lands in the cell the descent from the root would give it.
 struct GridCell {
 	int32_t node;
 	uint32_t level;
@@ -120,7 +127,9 @@ struct DeviceWorld {
 	const SsaOps* ssa;
 	const uint32_t* leaf_material;
 	const GridCell* grid; // (2^gridLevel)^3 cells, x fastest; null: descend from the root
+	const float* gridWalls; // per axis 2^gridLevel + 1 walls
 	uint32_t gridLevel;
+	float gridScale[3];   // 2^gridLevel / size
 	float lower[3];
 	float size[3];
 	uint32_t leaf_count;

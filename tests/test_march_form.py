@@ -127,3 +127,31 @@ def test_march_form_matches_programs(name, build):
         assert worst <= 2e-5
     finally:
         b.close()
+
+
+@pytest.mark.parametrize("name,build", [("c2", (7, 11, 32)), ("room", (5, 8, 64))])
+def test_grid_locate_matches_descent(name, build):
+    """The trace kernel's locate (a grid of the octree's level 6 set right
+    against its walls, then the descent) names the leaf the descent from the
+    root names, for points anywhere, on cell walls and outside the region."""
+    sc = scene(name)
+    b = host_backend()
+    try:
+        b.load(sc)
+        b.build(*build)
+        rng = np.random.default_rng(11)
+        lower = np.asarray(sc.region_lower, np.float32)
+        size = np.asarray(sc.region_size, np.float32)
+        inside = lower + size * rng.random((20000, 3)).astype(np.float32)
+        # points on the walls of every level: the descent's own midpoints
+        walls = []
+        for level in range(1, 12):
+            k = rng.integers(0, 1 << level, (2000, 3))
+            w = lower.astype(np.float64) + size.astype(np.float64) * k / (1 << level)
+            walls.append(w.astype(np.float32))
+        outside = lower + size * (rng.random((2000, 3)).astype(np.float32) * 1.4 - 0.2)
+        pts = np.concatenate([inside] + walls + [outside])
+        by_grid, by_descent = b.world_locate(pts)
+        assert np.array_equal(by_grid, by_descent)
+    finally:
+        b.close()
