@@ -44,9 +44,10 @@ METRIC = "Msamples/s @1080p vs CPU; equal-time relMSE guided vs plain; p50/p99 l
 SCENE = os.path.join(ROOT, "tests", "golden", "scenes", "c2.npz")
 WIDTH, HEIGHT, SPP, SURFACES = 1920, 1080, 64, 16
 DENOISE = True  # the a-trous denoiser on the frame's FP16 features
-# DRAM bytes the trace kernel moves a ray (read + write), from the ncu
-# capture of one launch of known rays (profiles/trace_kernel_ncu.md)
-TRACE_DRAM_BYTES_PER_RAY = None
+# DRAM bytes the trace kernel moves a ray (read + write): every trace
+# launch of a 960x540x8 config-2 frame captured by ncu (cold L2 a launch),
+# over the rays the kernel counted (profiles/trace_kernel_config2_960x540.md)
+TRACE_DRAM_BYTES_PER_RAY = 245.0
 BUILD = dict(min_depth=7, max_depth=11, split_steps=32)
 
 
@@ -273,7 +274,7 @@ def run_gpu(args) -> None:
             "traffic": TRACE_DRAM_BYTES_PER_RAY * rays_per_launch if (rays_per_launch and TRACE_DRAM_BYTES_PER_RAY) else None,
             "kernel": "traceKernel", "peak_source": pk["source"],
             "algorithmic": f"{ray_bytes} B a ray (ray in, end state out) x {rays_per_launch:.0f} rays a launch" if rays_per_launch else None,
-            "note": "the trace kernel is bound by FP32 issue and latency, not HBM; traffic scaled by rays from the ncu capture in profiles/",
+            "note": "the trace kernel is bound by FP32 issue and latency, not HBM; traffic = DRAM bytes a ray from the ncu capture in profiles/ (cold L2) x rays a launch",
         }
         line["trace_rates"] = {
             "rays_per_s": segments / (trace_ms / 1e3) if trace_ms else None,
