@@ -32,6 +32,10 @@ struct TraceArgs {
 	unsigned long long* counters;   // [0] march steps, [1] program steps, [2] longest march, [3] capped rays, [4] rays
 	const uint32_t* count;          // if set, the number of rays is read here on the device
 	uint32_t* fetch;                // the next ray to take; launchTrace zeroes it
+	// a second run of rays in the same arrays, from index `second` on, its
+	// count read on the device (null: none); traced in the same launch
+	const uint32_t* secondCount = nullptr;
+	uint32_t second             = 0;
 };
 
 struct HitArgs {

@@ -18,7 +18,7 @@ namespace kdn {
 struct FrameState {
 	DeviceBuffer pixel, sample, throughput, radiance, nanometres, density, drawn, state, from;
 	DeviceBuffer queuePaths[2], queueRays[2], hits, states, counts;
-	DeviceBuffer shadowRays, shadowPaths, shadowContribution, shadowStates;
+	DeviceBuffer shadowPaths, shadowContribution;
 	DeviceBuffer sums, out, materials;
 	// the denoised form: luminance moments, first surfaces, denoiser inputs
 	DeviceBuffer moments, surfDistance, surfNormal, surfAlbedo, surfLeaf, denoiseMoment, denoiseLength, means;
@@ -36,7 +36,7 @@ struct FrameState {
 void Context::releaseFrame() {
 	if (frame == nullptr) return;
 	FrameState& f = *frame;
-	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.hits, &f.states, &f.counts, &f.shadowRays, &f.shadowPaths, &f.shadowContribution, &f.shadowStates, &f.sums, &f.out, &f.materials, &f.moments, &f.surfDistance, &f.surfNormal, &f.surfAlbedo, &f.surfLeaf, &f.denoiseMoment, &f.denoiseLength, &f.means }) {
+	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.hits, &f.states, &f.counts, &f.shadowPaths, &f.shadowContribution, &f.sums, &f.out, &f.materials, &f.moments, &f.surfDistance, &f.surfNormal, &f.surfAlbedo, &f.surfLeaf, &f.denoiseMoment, &f.denoiseLength, &f.means }) {
 		if (b->ptr) cudaFree(b->ptr);
 		b->ptr   = nullptr;
 		b->bytes = 0;
@@ -149,10 +149,11 @@ namespace {
 
 // Device bytes one path of a chunk holds (the buffers ensureFrame sizes).
 // pixel, sample, drawn, state; throughput, radiance, nanometres, density,
-// from; the two queues' path indices and rays; hits and hit states; the
-// shadow lines' rays, path indices, contributions and hit states.
-constexpr size_t kPathBytes = 4 * 4 + 5 * 16 + 2 * 4 + 2 * sizeof(kdn_ray) + sizeof(kdn_hit) + sizeof(kdn::HitState) + sizeof(kdn_ray) + 4 + 16 + sizeof(kdn::HitState);
-static_assert(kPathBytes == 328, "path bytes");
+// from; the two queues' path indices and rays (a path ray and a shadow line
+// each); hits; hit states of a path ray and a line; the lines' path indices
+// and contributions.
+constexpr size_t kPathBytes = 4 * 4 + 5 * 16 + 2 * 4 + 2 * 2 * sizeof(kdn_ray) + sizeof(kdn_hit) + 2 * sizeof(kdn::HitState) + 4 + 16;
+static_assert(kPathBytes == 364, "path bytes");
 
 // The paths one chunk of a frame holds.  The whole frame where the device
 // has room for it (at most 2^28 paths, half the free memory): every launch
@@ -179,9 +180,11 @@ kdn_status ensureFrame(Context* ctx, uint32_t capacity) {
 	const Want wants[] = {
 		{ &f.pixel, n * 4 }, { &f.sample, n * 4 }, { &f.throughput, n * 16 }, { &f.radiance, n * 16 }, { &f.nanometres, n * 16 },
 		{ &f.density, n * 16 }, { &f.drawn, n * 4 }, { &f.state, n * 4 }, { &f.from, n * 16 },
-		{ &f.queuePaths[0], n * 4 }, { &f.queuePaths[1], n * 4 }, { &f.queueRays[0], n * sizeof(kdn_ray) }, { &f.queueRays[1], n * sizeof(kdn_ray) },
-		{ &f.hits, n * sizeof(kdn_hit) }, { &f.states, n * sizeof(kdn::HitState) }, { &f.counts, 64 },
-		{ &f.shadowRays, n * sizeof(kdn_ray) }, { &f.shadowPaths, n * 4 }, { &f.shadowContribution, n * 16 }, { &f.shadowStates, n * sizeof(kdn::HitState) },
+		// a queue holds a bounce's path rays in [0, n) and the shadow lines of
+		// the bounce before in [n, 2n): one trace launch takes both
+		{ &f.queuePaths[0], n * 4 }, { &f.queuePaths[1], n * 4 }, { &f.queueRays[0], 2 * n * sizeof(kdn_ray) }, { &f.queueRays[1], 2 * n * sizeof(kdn_ray) },
+		{ &f.hits, n * sizeof(kdn_hit) }, { &f.states, 2 * n * sizeof(kdn::HitState) }, { &f.counts, 64 },
+		{ &f.shadowPaths, n * 4 }, { &f.shadowContribution, n * 16 },
 	};
 	for (const Want& w : wants) {
 		if ((s = ctx->ensure(*w.b, w.bytes)) != KDN_OK) return s;
@@ -298,16 +301,22 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		Q[k].rays  = static_cast<kdn_ray*>(f.queueRays[k].ptr);
 		Q[k].count = counts + k;
 	}
+	// the shadow lines a shade writes go to the second half of the next
+	// queue's rays (and of the hit states), so the next bounce's trace launch
+	// takes them with its path rays
+	HitState* states = static_cast<HitState*>(f.states.ptr);
 	ShadowBuffers S;
-	S.rays         = static_cast<kdn_ray*>(f.shadowRays.ptr);
+	S.rays         = nullptr; // set a bounce: the second half of the next queue
 	S.paths        = static_cast<uint32_t*>(f.shadowPaths.ptr);
 	S.contribution = static_cast<float4*>(f.shadowContribution.ptr);
 	S.count        = counts + 2;
-	S.states       = static_cast<HitState*>(f.shadowStates.ptr);
+	S.states       = states + capacity;
+	uint32_t* none = counts + 3; // a count of zero
+	if (!ctx->check(cudaMemsetAsync(counts, 0, 64, stream), "clear counts")) return KDN_CUDA_ERROR;
 
 	// timing: one event pair around the frame, one around each trace launch
 	const uint32_t chunks = (pixels + chunkPixels - 1) / chunkPixels;
-	const size_t traceEvents = size_t(chunks) * size_t(fr->surfaces) * 4;
+	const size_t traceEvents = size_t(chunks) * size_t(fr->surfaces + 1) * 2;
 	const size_t needEvents  = 2 + traceEvents;
 	while (f.events.size() < needEvents) {
 		cudaEvent_t e;
@@ -360,30 +369,48 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		const uint32_t n     = chunk * spp;
 		if (!ctx->check(launchCamera(P, Q[0], first, n, stream, ctx->smCount), "camera kernel")) return KDN_CUDA_ERROR;
 		++launches;
+		if (!ctx->check(cudaMemsetAsync(S.count, 0, 4, stream), "clear lines")) return KDN_CUDA_ERROR;
 		int cur = 0;
-		for (int bounce = 0; bounce < fr->surfaces; ++bounce) {
-			const int nxt = 1 - cur;
+		// each round traces the bounce's path rays and the bounce before's
+		// shadow lines in one launch; a last round traces the last lines alone
+		for (int bounce = 0; bounce <= fr->surfaces; ++bounce) {
+			const bool last = bounce == fr->surfaces;
+			const int nxt   = 1 - cur;
 			TraceArgs t;
 			t.world          = ctx->world;
 			t.rays           = Q[cur].rays;
 			t.n              = n;
-			t.states         = static_cast<HitState*>(f.states.ptr);
+			t.states         = states;
 			t.objectMaterial = static_cast<const uint32_t*>(ctx->objectMaterial.ptr);
 			t.maxSteps       = kMarchSteps;
 			t.counters       = static_cast<unsigned long long*>(ctx->counters.ptr);
-			t.count          = Q[cur].count;
+			t.count          = last ? none : Q[cur].count;
 			t.fetch          = static_cast<uint32_t*>(ctx->fetch.ptr);
+			t.secondCount    = S.count;
+			t.second         = capacity;
 			cudaEventRecord(f.events[ev++], stream);
 			if (!ctx->check(launchTrace(t, stream, ctx->smCount), "trace kernel")) return KDN_CUDA_ERROR;
 			cudaEventRecord(f.events[ev++], stream);
-			HitArgs h;
-			h.world  = ctx->world;
-			h.rays   = Q[cur].rays;
-			h.states = t.states;
-			h.n      = n;
-			h.hits   = static_cast<kdn_hit*>(f.hits.ptr);
-			h.count  = Q[cur].count;
-			if (!ctx->check(launchHits(h, stream, ctx->smCount), "hit kernel")) return KDN_CUDA_ERROR;
+			++launches;
+			if (!last) {
+				HitArgs h;
+				h.world  = ctx->world;
+				h.rays   = Q[cur].rays;
+				h.states = states;
+				h.n      = n;
+				h.hits   = static_cast<kdn_hit*>(f.hits.ptr);
+				h.count  = Q[cur].count;
+				if (!ctx->check(launchHits(h, stream, ctx->smCount), "hit kernel")) return KDN_CUDA_ERROR;
+				++launches;
+			}
+			if (bounce > 0) {
+				// the bounce before's lines that reached their lamps
+				ShadowBuffers lines = S;
+				lines.rays          = Q[cur].rays + capacity;
+				if (!ctx->check(launchLines(P, lines, capacity, stream, ctx->smCount), "lines kernel")) return KDN_CUDA_ERROR;
+				++launches;
+			}
+			if (last) break;
 			if (!ctx->check(cudaMemsetAsync(Q[nxt].count, 0, 4, stream), "clear queue")) return KDN_CUDA_ERROR;
 			if (!ctx->check(cudaMemsetAsync(S.count, 0, 4, stream), "clear lines")) return KDN_CUDA_ERROR;
 			ShadeArgs a;
@@ -391,22 +418,15 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 			a.in           = Q[cur];
 			a.out          = Q[nxt];
 			a.shadow       = S;
-			a.hits         = h.hits;
+			a.shadow.rays  = Q[nxt].rays + capacity;
+			a.hits         = static_cast<const kdn_hit*>(f.hits.ptr);
 			a.materials    = static_cast<const DeviceMaterial*>(f.materials.ptr);
 			a.leafMaterial = static_cast<const uint32_t*>(ctx->leafMaterial.ptr);
 			a.leafCount    = uint32_t(ctx->leafMaterial.bytes / 4);
 			a.capacity     = capacity;
 			a.error        = nullptr;
 			if (!ctx->check(launchShade(a, stream, ctx->smCount), "shade kernel")) return KDN_CUDA_ERROR;
-			TraceArgs l = t;
-			l.rays      = S.rays;
-			l.states    = S.states;
-			l.count     = S.count;
-			cudaEventRecord(f.events[ev++], stream);
-			if (!ctx->check(launchTrace(l, stream, ctx->smCount), "line trace kernel")) return KDN_CUDA_ERROR;
-			cudaEventRecord(f.events[ev++], stream);
-			if (!ctx->check(launchLines(P, S, capacity, stream, ctx->smCount), "lines kernel")) return KDN_CUDA_ERROR;
-			launches += 5;
+			++launches;
 			cur = nxt;
 		}
 		if (!ctx->check(launchFold(P, first, chunk, spp, static_cast<double*>(f.sums.ptr), denoised ? static_cast<double*>(f.moments.ptr) : nullptr, alpha, stream, ctx->smCount), "fold kernel")) return KDN_CUDA_ERROR;

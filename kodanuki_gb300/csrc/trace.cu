@@ -22,6 +22,8 @@ constexpr int kTraceBlock = 128;
 // program steps a thread runs a turn of the step machine before the warp
 // looks again for threads that need a new ray or a new cell
 constexpr uint32_t kStepsPerTurn = 4;
+// empty cells a thread passes a turn before the warp moves on
+constexpr uint32_t kCellsPerTurn = 1u << 30;
 
 __device__ __forceinline__ float slopeOf(float part) {
 	const float tiny = 1e-12f;
@@ -170,7 +172,9 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 	float* slots          = slotMemory + threadIdx.x;
 	setConstants(slots, stride);
 	uint32_t marchSteps = 0, programSteps = 0, traced = 0, capped = 0, longest = 0;
-	const uint32_t n = args.count ? *args.count : args.n;
+	// the rays: [0, n1) and, after them in the fetch order, [second, second + n2)
+	const uint32_t n1 = args.count ? *args.count : args.n;
+	const uint32_t n  = n1 + (args.secondCount ? *args.secondCount : 0u);
 	const unsigned lane = threadIdx.x & 31u;
 
 	uint32_t mode = Fetch;
@@ -214,6 +218,7 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 				if (ray >= n) {
 					mode = Finished;
 				} else {
+					if (ray >= n1) ray = args.second + (ray - n1);
 					++traced;
 					const kdn_ray r = args.rays[ray];
 					for (int a = 0; a < 3; ++a) {
@@ -246,7 +251,7 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 
 		// find the cell of the point, skipping empty cells, and start its first program
 		if (mode == Locating) {
-			for (;;) {
+			for (uint32_t skipped = 0;;) {
 				if (!(step < args.maxSteps && t <= up)) {
 					done(HitState { 0, 0.0f, kNoLeaf, 0, step });
 					break;
@@ -258,7 +263,8 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 				if (leaf.occupancy == Empty || leaf.count == 0) {
 					t = fmaxf(exitT, t) + nudge(t);
 					++step;
-					continue;
+					if (++skipped < kCellsPerTurn) continue;
+					break; // the next turn goes on locating
 				}
 				first   = leaf.first;
 				count   = leaf.count;
