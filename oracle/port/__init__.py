@@ -10,7 +10,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(os.path.dirname(HERE), "_build")
 LIB = os.path.join(OUT, "libkdn_oracle.so")
-SOURCES = ["geometry.c", "spectral.c", "transport.c", "denoise.c"]
+SOURCES = ["geometry.c", "spectral.c", "transport.c", "denoise.c", "temporal.c"]
 
 _lib = None
 
@@ -241,19 +241,22 @@ def lens_of(scene, width: int, height: int) -> np.ndarray:
     return np.concatenate([eye, forward, right, up, [np.tan(float(cam["fov"]) / 2), width / height]])
 
 
-def traced_surfaces(scene, width: int, height: int, build: dict | None = None) -> dict:
+def traced_surfaces(scene, width: int, height: int, build: dict | None = None, lens=None, offsets=None) -> dict:
     """core/surfaces.cpp:133 tracedSurfaces: one ray through each pixel's
     centre (core/camera.cpp:34 filmDirection), the first surface's distance
     from the eye, normal facing the ray, albedo (mixed across a blend seam,
     material.cpp:345 bsdfAt) and leaf; a missed ray keeps batch.cpp:46
-    missedSurface.  Pixel-major arrays of width * height."""
+    missedSurface.  Pixel-major arrays of width * height.  `lens` (14
+    doubles) replaces the scene's camera, `offsets` (n x 2, in [0, 1)) the
+    pixel centres."""
     build = build or dict(min_depth=6, max_depth=10, split_steps=96)
     tree = _octree_for(scene, build)
-    lens = lens_of(scene, width, height)
+    lens = lens_of(scene, width, height) if lens is None else np.asarray(lens, np.float64)
     eye, forward, right, up, reach, aspect = lens[0:3], lens[3:6], lens[6:9], lens[9:12], lens[12], lens[13]
     y, x = np.mgrid[0:height, 0:width]
-    u = 2 * (x.ravel() + 0.5) / width - 1
-    v = 1 - 2 * (y.ravel() + 0.5) / height
+    off = np.full((width * height, 2), 0.5) if offsets is None else np.asarray(offsets, np.float64)
+    u = 2 * (x.ravel() + off[:, 0]) / width - 1
+    v = 1 - 2 * (y.ravel() + off[:, 1]) / height
     heading = forward[None, :] + right[None, :] * (u * reach * aspect)[:, None] + up[None, :] * (v * reach)[:, None]
     heading /= np.sqrt((heading * heading).sum(1))[:, None]
     rays = np.zeros(width * height, RAY_DTYPE)
@@ -298,3 +301,35 @@ def denoise(width: int, height: int, demodulated: int, lens, colour, moment, len
     out = np.zeros((width * height, 3), np.float32)
     L.kp_denoise(width, height, demodulated, *[_ptr(a) for a in arrs], _ptr(out))
     return out
+
+
+SURFACE_DTYPE = np.dtype([("distance", "<f4"), ("normal", "<f4", 3), ("leaf", "<u4"), ("albedo", "<f4", 3)])
+TPIXEL_DTYPE = np.dtype([("colour", "<f8", 3), ("moment", "<f8"), ("length", "<f4"), ("distance", "<f4"), ("normal", "<f8", 3), ("leaf", "<u4"),
+                         ("albedo", "<f8", 3)], align=True)
+
+
+def surfaces_array(surf: dict) -> np.ndarray:
+    out = np.zeros(len(surf["leaf"]), SURFACE_DTYPE)
+    for key in ("distance", "normal", "leaf", "albedo"):
+        out[key] = surf[key]
+    return out
+
+
+def temporal(width: int, height: int, moved: bool, recounted: bool, kept: bool, lens_now, lens_before, light, first: dict, centre: dict,
+             before: np.ndarray | None):
+    """The oracle's temporal member over one frame (kp_temporal): the state
+    after (TPIXEL_DTYPE) and the image."""
+    L = lib()
+    L.kp_temporal.argtypes = [ctypes.c_int] * 5 + [_P] * 8
+    n = width * height
+    prev = np.zeros(n, TPIXEL_DTYPE) if before is None else np.ascontiguousarray(before, TPIXEL_DTYPE)
+    after = np.zeros(n, TPIXEL_DTYPE)
+    image = np.zeros((n, 3), np.float32)
+    ln = np.ascontiguousarray(lens_now, np.float64)
+    lb = np.ascontiguousarray(lens_before, np.float64)
+    li = np.ascontiguousarray(light, np.float64)
+    fs = surfaces_array(first)
+    cs = surfaces_array(centre)
+    L.kp_temporal(width, height, int(moved), int(recounted), int(kept), _ptr(ln), _ptr(lb), _ptr(li), _ptr(fs), _ptr(cs), _ptr(prev), _ptr(after),
+                  _ptr(image))
+    return after, image

@@ -153,6 +153,34 @@ void kp_render_band(const kp_octree* tree, const uint32_t* leaf_material, const 
 void kp_denoise(int width, int height, int demodulated, const double lens[14], const double* colour, const double* moment, const float* length,
                 const float* distance, const double* normal, const uint32_t* leaf, const double* albedo, float* out);
 
+/* ---- the temporal member (plugins/reconstruction/temporal/temporal.cpp) ---- */
+/* One frame of temporalFrame (:1001) at a film factor of 1 with a G-buffer
+ * (the demodulated grid: what the reference runs before the a-trous
+ * denoiser).  lens now / before: eye[3], forward[3], right[3], up[3], reach,
+ * aspect.  Per pixel: light[3] (the record's), first (the record's first
+ * surface of the pixel's last sample) and centre (the G-buffer's) as
+ * kp_surface, before (the state before, ignored when kept is 0); out: the
+ * state after and the image, RGB. */
+typedef struct kp_surface {
+	float distance;
+	float normal[3];
+	uint32_t leaf;
+	float albedo[3];
+} kp_surface;
+
+typedef struct kp_tpixel {
+	double colour[3];
+	double moment;
+	float length;
+	float distance;
+	double normal[3];
+	uint32_t leaf;
+	double albedo[3];
+} kp_tpixel;
+
+void kp_temporal(int width, int height, int moved, int recounted, int kept, const double lens_now[14], const double lens_before[14], const double* light,
+                 const kp_surface* first, const kp_surface* centre, const kp_tpixel* before, kp_tpixel* after, float* image);
+
 /* ---- numbers, wavelengths and colour (math/random.cpp, math/colour.cpp) ---- */
 uint64_t kp_mixed_bits(uint64_t v);
 double kp_unit_of(uint64_t bits);

@@ -6,6 +6,8 @@
 //   kdn_ref_dump scene  <file.sdf> <out.json>            compiled scene as JSON
 //   kdn_ref_dump trace  <file.sdf> <rays.f32> <hits.bin>  sphereTraced per ray
 //   kdn_ref_dump cut    <file.sdf> <depth> <out.bin>      cutCell down an octree
+//   kdn_ref_dump denoise  <in.bin> <out.f32>              denoisedFrame
+//   kdn_ref_dump temporal <in.bin> <out.bin>              temporalFrame
 //
 // Reference entry points used: loadScene (syntax/evaluator.cpp:2898),
 // sceneRegion (plugins/geometry/tree/build.cpp:405), sphereTraced
@@ -15,6 +17,7 @@
 #include "plugins/geometry/tree/build.h"
 #include "plugins/geometry/tree/cut.h"
 #include "plugins/reconstruction/atrous/atrous.h"
+#include "plugins/reconstruction/temporal/temporal.h"
 #include "plugins/transport/paths/material/material.h"
 #include "sdf/program.h"
 #include "sdf/scene.h"
@@ -286,9 +289,135 @@ int dumpDenoise(const char* inPath, const char* outPath) {
 	return 0;
 }
 
+Lens lensOf14(const double* v, int width, int height) {
+	return Lens {
+		.eye      = { v[0], v[1], v[2] },
+		.forward  = { v[3], v[4], v[5] },
+		.right    = { v[6], v[7], v[8] },
+		.up       = { v[9], v[10], v[11] },
+		.reach    = v[12],
+		.aspect   = v[13],
+		.aperture = 0,
+		.focus    = 10,
+		.width    = width,
+		.height   = height,
+	};
+}
+
+bool readSurface(FILE* in, Surface& s) {
+	float distance, normal[3], albedo[3];
+	std::uint32_t leaf;
+	if (std::fread(&distance, 4, 1, in) != 1 || std::fread(normal, 4, 3, in) != 3 || std::fread(&leaf, 4, 1, in) != 1 || std::fread(albedo, 4, 3, in) != 3) return false;
+	s          = missedSurface();
+	s.distance = distance;
+	s.normal   = { normal[0], normal[1], normal[2] };
+	s.leaf     = leaf;
+	s.albedo   = { albedo[0], albedo[1], albedo[2] };
+	return true;
+}
+
+bool readPixel(FILE* in, TemporalPixel& p) {
+	double colour[3], moment, normal[3], albedo[3];
+	float length, distance;
+	std::uint32_t leaf;
+	if (std::fread(colour, 8, 3, in) != 3 || std::fread(&moment, 8, 1, in) != 1 || std::fread(&length, 4, 1, in) != 1 || std::fread(&distance, 4, 1, in) != 1 ||
+	    std::fread(normal, 8, 3, in) != 3 || std::fread(&leaf, 4, 1, in) != 1 || std::fread(albedo, 8, 3, in) != 3) {
+		return false;
+	}
+	p = TemporalPixel {
+		.colour   = { colour[0], colour[1], colour[2] },
+		.moment   = moment,
+		.length   = length,
+		.distance = distance,
+		.normal   = { normal[0], normal[1], normal[2] },
+		.leaf     = leaf,
+		.albedo   = { albedo[0], albedo[1], albedo[2] },
+	};
+	return true;
+}
+
+void writePixel(FILE* out, const TemporalPixel& p) {
+	const double colour[3] = { p.colour.red, p.colour.green, p.colour.blue };
+	const double normal[3] = { p.normal.x, p.normal.y, p.normal.z };
+	const double albedo[3] = { p.albedo.red, p.albedo.green, p.albedo.blue };
+	std::fwrite(colour, 8, 3, out);
+	std::fwrite(&p.moment, 8, 1, out);
+	std::fwrite(&p.length, 4, 1, out);
+	std::fwrite(&p.distance, 4, 1, out);
+	std::fwrite(normal, 8, 3, out);
+	std::fwrite(&p.leaf, 4, 1, out);
+	std::fwrite(albedo, 8, 3, out);
+}
+
+// One frame of the temporal member (plugins/reconstruction/temporal/
+// temporal.cpp:1001 temporalFrame) at a film factor of 1.  Input: int32
+// width, height, moved, recounted, kept (the state before holds a frame),
+// demodulated (the state before's flag); doubles lens now[14], lens
+// before[14] (eye, forward, right, up, reach, aspect); then per pixel the
+// record's light (3 f64), the record's surface and the G-buffer's surface
+// (each distance f32, normal 3 f32, leaf u32, albedo 3 f32), and the state
+// before's pixel (colour 3 f64, moment f64, length f32, distance f32,
+// normal 3 f64, leaf u32, albedo 3 f64).  Output: the new state's pixels
+// (the same layout), then the image, RGB f32.
+int dumpTemporal(const char* inPath, const char* outPath) {
+	FILE* in = std::fopen(inPath, "rb");
+	std::int32_t head[6];
+	double now[14], before[14];
+	if (std::fread(head, 4, 6, in) != 6 || std::fread(now, 8, 14, in) != 14 || std::fread(before, 8, 14, in) != 14) return 1;
+	const int width = head[0], height = head[1];
+	const std::size_t n = std::size_t(width) * std::size_t(height);
+	FrameRecord record  = emptyFrameRecord();
+	record.width        = width;
+	record.height       = height;
+	std::vector<Surface> gbuffer(n);
+	TemporalState state = emptyTemporal();
+	state.width         = head[4] ? width : 0;
+	state.height        = head[4] ? height : 0;
+	state.demodulated   = head[5] != 0;
+	state.film          = { .factor = 1, .phase = 0 };
+	for (std::size_t k = 0; k < n; ++k) {
+		double light[3];
+		Surface first, centre;
+		TemporalPixel last;
+		if (std::fread(light, 8, 3, in) != 3 || !readSurface(in, first) || !readSurface(in, centre) || !readPixel(in, last)) return 1;
+		record.parts.push_back(Parts { .total = { light[0], light[1], light[2] } });
+		record.surfaces.push_back(first);
+		gbuffer[k] = centre;
+		if (head[4]) state.pixels.push_back(last);
+	}
+	std::fclose(in);
+	const Lens lensNow    = lensOf14(now, width, height);
+	const Lens lensBefore = lensOf14(before, width, height);
+	static const std::vector<PixelSum> estimates;
+	const ShownFrame frame = {
+		.width     = width,
+		.height    = height,
+		.lens      = lensNow,
+		.before    = lensBefore,
+		.film      = { .factor = 1, .phase = 0 },
+		.moved     = head[2] != 0,
+		.restarted = false,
+		.recounted = head[3] != 0,
+		.still     = head[2] ? 1u : 2u,
+		.record    = record,
+		.estimates = estimates,
+		.surfaces  = gbuffer,
+		.threads   = 4,
+	};
+	const Temporal next = temporalFrame(state, frame);
+	FILE* out           = std::fopen(outPath, "wb");
+	for (const TemporalPixel& p : next.state.pixels) writePixel(out, p);
+	std::fwrite(next.image.rgb.data(), 4, next.image.rgb.size(), out);
+	std::fclose(out);
+	return 0;
+}
+
 } // namespace
 
 int main(int argc, char** argv) {
+	if (argc >= 4 && std::strcmp(argv[1], "temporal") == 0) {
+		return dumpTemporal(argv[2], argv[3]);
+	}
 	if (argc >= 4 && std::strcmp(argv[1], "denoise") == 0) {
 		return dumpDenoise(argv[2], argv[3]);
 	}

@@ -223,6 +223,98 @@ def denoise_fixture(dump: str, tmp: str) -> None:
     np.savez_compressed(os.path.join(HERE, "denoise.npz"), **out)
 
 
+TEMPORAL_SIZE = (48, 32)
+
+
+def _surface_record(surf: dict, k: int) -> bytes:
+    return struct.pack("<f", float(surf["distance"][k])) + surf["normal"][k].astype("<f4").tobytes() + struct.pack("<I", int(surf["leaf"][k])) + \
+        surf["albedo"][k].astype("<f4").tobytes()
+
+
+def _fp16_surfaces(surf: dict) -> dict:
+    """The first surfaces as the GPU stores them: FP16 distance, normal, albedo."""
+    return {"distance": surf["distance"].astype(np.float16).astype(np.float32), "normal": surf["normal"].astype(np.float16).astype(np.float32),
+            "albedo": surf["albedo"].astype(np.float16).astype(np.float32), "leaf": surf["leaf"].astype(np.uint32)}
+
+
+def temporal_frames(scene: Scene, rng: np.random.Generator):
+    """A seeded sequence of frames over config 2's small scene, the camera
+    still, then moving, then still again: per frame the lens now and before,
+    the record's light and first surfaces (each pixel's last sample, jittered)
+    and the G-buffer (pixel centres)."""
+    import oracle.port as op
+    w, h = TEMPORAL_SIZE
+    build = dict(min_depth=5, max_depth=9, split_steps=64)
+    base = op.lens_of(scene, w, h)
+
+    def moved(lens, shift, turn):
+        eye = lens[0:3] + np.asarray(shift)
+        fw = lens[3:6] + turn * lens[6:9]
+        fw = fw / np.linalg.norm(fw)
+        rt = np.cross(fw, np.array([0.0, 0.0, 1.0]))
+        rt = rt / np.linalg.norm(rt)
+        up = np.cross(rt, fw)
+        return np.concatenate([eye, fw, rt, up, lens[12:14]])
+
+    lenses = [base, base, moved(base, [0.15, 0.05, 0.0], 0.01), moved(base, [0.3, 0.1, 0.02], 0.02), moved(base, [0.3, 0.1, 0.02], 0.02)]
+    plan = [(0, 0), (1, 0), (1, 1), (1, 1), (1, 0)]  # (kept, moved)
+    sun = np.array([0.3, -0.4, 0.87])
+    sun = sun / np.linalg.norm(sun)
+    frames = []
+    for f, (kept, move) in enumerate(plan):
+        lens = lenses[f]
+        gbuffer = _fp16_surfaces(op.traced_surfaces(scene, w, h, build, lens=lens))
+        first = _fp16_surfaces(op.traced_surfaces(scene, w, h, build, lens=lens, offsets=rng.random((w * h, 2))))
+        hit = first["leaf"] != 0xFFFFFFFF
+        shade = 0.3 + 0.7 * np.clip(first["normal"].astype(np.float64) @ sun, 0, None)
+        light = np.where(hit[:, None], first["albedo"].astype(np.float64) * shade[:, None], np.array([0.4, 0.5, 0.7]))
+        light = light * (1 + 0.3 * rng.normal(size=light.shape))
+        light = np.clip(light, 0, None)
+        frames.append(dict(lens=lens, before=lenses[max(f - 1, 0)], kept=kept, moved=move, light=light, first=first, gbuffer=gbuffer))
+    return frames
+
+
+def temporal_fixture(dump: str, tmp: str) -> None:
+    """tests/golden/temporal.npz: the reference's temporalFrame over a
+    sequence of frames, each fed the state the one before left."""
+    scene = Scene.load(os.path.join(HERE, "scenes", "c2_small.npz"))
+    w, h = TEMPORAL_SIZE
+    n = w * h
+    frames = temporal_frames(scene, np.random.default_rng(2024))
+    state = None
+    out = {"width": w, "height": h, "frames": len(frames)}
+    pixel = np.dtype([("colour", "<f8", 3), ("moment", "<f8"), ("length", "<f4"), ("distance", "<f4"), ("normal", "<f8", 3), ("leaf", "<u4"),
+                      ("albedo", "<f8", 3)])
+    for f, fr in enumerate(frames):
+        path = os.path.join(tmp, f"temporal_{f}.bin")
+        with open(path, "wb") as fh:
+            fh.write(struct.pack("<6i", w, h, fr["moved"], 0, fr["kept"], 1))
+            fh.write(fr["lens"].astype("<f8").tobytes())
+            fh.write(fr["before"].astype("<f8").tobytes())
+            before = state if state is not None else np.zeros(n, pixel)
+            for k in range(n):
+                fh.write(fr["light"][k].astype("<f8").tobytes())
+                fh.write(_surface_record(fr["first"], k))
+                fh.write(_surface_record(fr["gbuffer"], k))
+                fh.write(before[k].tobytes())
+        res = os.path.join(tmp, f"temporal_{f}.out")
+        subprocess.run([dump, "temporal", path, res], check=True)
+        raw = open(res, "rb").read()
+        after = np.frombuffer(raw[: n * pixel.itemsize], pixel).copy()
+        image = np.frombuffer(raw[n * pixel.itemsize:], "<f4").reshape(n, 3).copy()
+        for key in ("lens", "before", "kept", "moved", "light"):
+            out[f"{f}.{key}"] = fr[key]
+        for part in ("first", "gbuffer"):
+            for key, v in fr[part].items():
+                out[f"{f}.{part}.{key}"] = v
+        for key in pixel.names:
+            out[f"{f}.state.{key}"] = after[key]
+        out[f"{f}.image"] = image
+        state = after
+        print(" temporal frame", f, "kept", fr["kept"], "moved", fr["moved"], "held", float((after["length"] > 1).mean()), "image", image.mean(0))
+    np.savez_compressed(os.path.join(HERE, "temporal.npz"), **out)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref-bin", default=os.path.join(ROOT, "oracle", "_ref"))
@@ -234,6 +326,8 @@ def main() -> None:
     tmp = tempfile.mkdtemp()
     if args.only in (None, "denoise"):
         denoise_fixture(dump, tmp)
+    if args.only in (None, "temporal"):
+        temporal_fixture(dump, tmp)
     for name, (gen, kw, nrays, depth) in SCENES.items():
         if args.only and name != args.only:
             continue
