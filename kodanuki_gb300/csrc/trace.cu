@@ -23,7 +23,7 @@ constexpr int kTraceBlock = 128;
 // looks again for threads that need a new ray or a new cell
 constexpr uint32_t kStepsPerTurn = 4;
 // empty cells a thread passes a turn before the warp moves on
-constexpr uint32_t kCellsPerTurn = 1u << 30;
+constexpr uint32_t kCellsPerTurn = 1;
 
 __device__ __forceinline__ float slopeOf(float part) {
 	const float tiny = 1e-12f;
