@@ -316,6 +316,53 @@ kdn_status kdn_denoise_device(kdn_ctx* ctx, const kdn_denoise_frame* frame, cons
 kdn_status kdn_denoise_static(const kdn_denoise_frame* frame, const float* colour, const float* moment, const float* length, const uint16_t* distance,
                               const uint16_t* normal, const uint16_t* albedo, const uint32_t* leaf, float* out_rgb, void* stream);
 
+/*
+ * The temporal member (plugins/reconstruction/temporal/temporal.cpp:1001
+ * temporalFrame) for one frame at a film factor of 1 with a G-buffer: the
+ * grid the reference runs before the a-trous denoiser, each pixel's light
+ * divided by the albedo of its sample's first surface.  Each pixel blends
+ * this frame's light into its history: its own on a still camera, else the
+ * frame before's pixels around where its G-buffer point was seen whose
+ * surface lies on its plane (bilinear), clamped to this frame's 3x3
+ * neighbourhood while the history is young or the camera moves; the state
+ * after is its colour, moment and length, and what it shows is its
+ * G-buffer surface.  kdn_render with KDN_FRAME_DENOISE runs it between the
+ * frame and the a-trous denoiser; kdn_temporal_device runs it alone.
+ */
+typedef struct kdn_temporal_frame {
+	int32_t width, height;
+	uint32_t moved;     /* the camera moved since the frame before */
+	uint32_t recounted; /* the scene's shapes changed: leaves compare as hit or sky alone */
+	uint32_t kept;      /* the state before holds a frame of this size */
+	uint32_t pad_;
+	double now[14], before[14]; /* lenses: eye, forward, right, up, reach, aspect */
+} kdn_temporal_frame;
+
+/* Device arrays, a pixel each, row-major.  FP16 fields are bit patterns. */
+typedef struct kdn_temporal_buffers {
+	const float* light;              /* x3: the frame's pixel means */
+	const uint16_t* first_distance;  /* the first surface of each pixel's last sample */
+	const uint16_t* first_normal;    /* x3 */
+	const uint16_t* first_albedo;    /* x3 */
+	const uint32_t* first_leaf;
+	const uint16_t* centre_distance; /* the G-buffer: the surface through the pixel's centre */
+	const uint16_t* centre_normal;
+	const uint16_t* centre_albedo;
+	const uint32_t* centre_leaf;
+	const float* before_colour;      /* x3: the state before (read when kept) */
+	const float* before_moment;
+	const float* before_length;
+	const uint16_t* before_distance; /* the frame before's G-buffer */
+	const uint16_t* before_normal;
+	const uint32_t* before_leaf;
+	float* colour;                   /* x3: the state after (demodulated light) */
+	float* moment;
+	float* length;
+	float* image;                    /* x3: the shown light, or null */
+} kdn_temporal_buffers;
+
+kdn_status kdn_temporal_device(kdn_ctx* ctx, const kdn_temporal_frame* frame, const kdn_temporal_buffers* buffers, void* stream);
+
 /* Write a buffer larger than the L2 cache on the context's stream, so that
  * the next launch starts with a cold cache. */
 kdn_status kdn_flush_l2(kdn_ctx* ctx);

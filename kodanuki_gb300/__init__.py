@@ -77,7 +77,7 @@ class KdnError(RuntimeError):
 EXPORTS = [
     "kdn_status_string", "kdn_last_error", "kdn_open", "kdn_close", "kdn_upload_block", "kdn_build", "kdn_world_stats",
     "kdn_world_cell", "kdn_extend", "kdn_extend_device", "kdn_render", "kdn_render_device", "kdn_frame_stats_get", "kdn_flush_l2",
-    "kdn_frame_surfaces", "kdn_world_march", "kdn_world_locate", "kdn_denoise", "kdn_denoise_device", "kdn_denoise_static",
+    "kdn_frame_surfaces", "kdn_world_march", "kdn_world_locate", "kdn_temporal_device", "kdn_denoise", "kdn_denoise_device", "kdn_denoise_static",
 ]
 
 
@@ -85,6 +85,21 @@ class DenoiseFrame(ctypes.Structure):
     _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("demodulated", ctypes.c_uint32), ("pad", ctypes.c_uint32),
                 ("eye", ctypes.c_double * 3), ("forward", ctypes.c_double * 3), ("right", ctypes.c_double * 3), ("up", ctypes.c_double * 3),
                 ("reach", ctypes.c_double), ("aspect", ctypes.c_double)]
+
+
+
+class TemporalFrame(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("moved", ctypes.c_uint32), ("recounted", ctypes.c_uint32),
+                ("kept", ctypes.c_uint32), ("pad", ctypes.c_uint32), ("now", ctypes.c_double * 14), ("before", ctypes.c_double * 14)]
+
+
+class TemporalBuffers(ctypes.Structure):
+    """include/kdn.h kdn_temporal_buffers: device pointers."""
+    _fields_ = [(name, ctypes.c_void_p) for name in (
+        "light", "first_distance", "first_normal", "first_albedo", "first_leaf", "centre_distance", "centre_normal", "centre_albedo",
+        "centre_leaf", "before_colour", "before_moment", "before_length", "before_distance", "before_normal", "before_leaf", "colour",
+        "moment", "length", "image")]
+
 
 _lib = None
 
@@ -118,6 +133,7 @@ def library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.kdn_frame_surfaces.argtypes = [P, P, P, P, P]
     L.kdn_world_march.argtypes = [P, ctypes.c_uint64, P, ctypes.c_uint32, P, ctypes.c_size_t, P]
     L.kdn_world_locate.argtypes = [P, P, ctypes.c_uint32, P, P]
+    L.kdn_temporal_device.argtypes = [P, ctypes.POINTER(TemporalFrame), ctypes.POINTER(TemporalBuffers), P]
     L.kdn_denoise.argtypes = [P, ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P]
     L.kdn_denoise_device.argtypes = [P, ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P, P]
     L.kdn_denoise_static.argtypes = [ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P, P]

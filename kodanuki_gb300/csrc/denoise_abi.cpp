@@ -132,3 +132,31 @@ kdn_status kdn_denoise(kdn_ctx* handle, const kdn_denoise_frame* frame, const fl
 }
 
 } // extern "C"
+
+#include "temporal.h"
+
+extern "C" kdn_status kdn_temporal_device(kdn_ctx* handle, const kdn_temporal_frame* frame, const kdn_temporal_buffers* io, void* stream) {
+	if (handle == nullptr || frame == nullptr || io == nullptr) return KDN_BAD_ARG;
+	Context* ctx = reinterpret_cast<Context*>(handle);
+	std::lock_guard<std::mutex> guard(ctx->lock);
+	if (ctx->device < 0) return ctx->fail(KDN_NO_DEVICE, "kdn_temporal_device: a host-only context has no device");
+	if (frame->width <= 0 || frame->height <= 0 || int64_t(frame->width) * int64_t(frame->height) > (int64_t(1) << 26))
+		return ctx->fail(KDN_BAD_ARG, "kdn_temporal_device: frame size out of range");
+	const bool reads = frame->kept != 0;
+	if (!io->light || !io->first_distance || !io->first_normal || !io->first_albedo || !io->first_leaf || !io->centre_distance || !io->centre_normal ||
+	    !io->centre_albedo || !io->centre_leaf || !io->colour || !io->moment || !io->length ||
+	    (reads && (!io->before_colour || !io->before_moment || !io->before_length || !io->before_distance || !io->before_normal || !io->before_leaf)))
+		return ctx->fail(KDN_BAD_ARG, "kdn_temporal_device: a buffer is missing");
+	if (!ctx->check(cudaSetDevice(ctx->device), "cudaSetDevice")) return KDN_CUDA_ERROR;
+	kdn::TemporalArgs a {};
+	a.width     = frame->width;
+	a.height    = frame->height;
+	a.moved     = frame->moved;
+	a.recounted = frame->recounted;
+	a.kept      = frame->kept;
+	a.now       = kdn::temporalCameraOf(frame->now, frame->width, frame->height);
+	a.before    = kdn::temporalCameraOf(frame->before, frame->width, frame->height);
+	a.io        = *io;
+	if (!ctx->check(kdn::launchTemporal(a, stream ? static_cast<cudaStream_t>(stream) : ctx->stream), "temporal kernel")) return KDN_CUDA_ERROR;
+	return KDN_OK;
+}
