@@ -165,18 +165,21 @@ typedef struct kdn_frame {
 	uint32_t flags;      /* KDN_FRAME_DENOISE: return the denoised frame */
 } kdn_frame;
 
-/* With KDN_FRAME_DENOISE a frame also traces its first surfaces, one ray
- * through each pixel's centre (core/surfaces.cpp:133 tracedSurfaces: distance
- * from the eye, the normal facing the ray and the albedo as FP16, and the
- * leaf), keeps the luminance moment of a still camera's temporal state
- * (plugins/reconstruction/temporal/temporal.cpp:797 freshBlend, :835
- * heldBlend: each frame's pixel luminance squared, blended in by
- * max(1 / (length + 1), 1 / 256) over the frames accumulated), and returns
- * the pixel means put through the a-trous denoiser (kdn_denoise) with those
- * features, the history length being the frames accumulated (at most 256).
- * The colour is the exact mean of every sample so far, which is the
- * temporal blend of equal frames until the cap of 256 frames. */
+/* With KDN_FRAME_DENOISE a frame returns what the reference shows through
+ * its reconstruction chain temporal + a-trous: it also records each pixel's
+ * light of this call and the first surface of its last sample, traces the
+ * G-buffer (one ray through each pixel's centre, core/surfaces.cpp:133
+ * tracedSurfaces: distance, normal facing the ray and albedo as FP16, and
+ * the leaf), runs the temporal member (kdn_temporal_device: its history is
+ * the last denoised frame's where that was of this size, reprojected when
+ * the camera moved) and puts the temporal state through the a-trous
+ * denoiser (kdn_denoise, demodulated).  A frame without the flag drops the
+ * history.  `accumulate` still adds this call's samples to the pixel sums,
+ * which a frame without the flag shows. */
 #define KDN_FRAME_DENOISE 1u
+/* With KDN_FRAME_DENOISE: start the temporal history over (the sequence's
+ * cut: every member drops its history). */
+#define KDN_FRAME_RESTART 2u
 
 /* Device times of the last kdn_render, from CUDA events on the context's stream. */
 typedef struct kdn_frame_stats {
@@ -264,6 +267,11 @@ kdn_status kdn_frame_stats_get(kdn_ctx* ctx, kdn_frame_stats* stats);
  * Replaces core/frame.cpp:508 shownSurfaces.  KDN_NOT_READY when the last
  * frame kept none. */
 kdn_status kdn_frame_surfaces(kdn_ctx* ctx, uint16_t* distance, uint16_t* normal, uint16_t* albedo, uint32_t* leaf);
+/* The record of the last frame drawn with KDN_FRAME_DENOISE (core/shown.h
+ * FrameRecord): each pixel's light of that call (RGB float), and the first
+ * surface of its last sample (FP16 distance, normal, albedo; leaf), into
+ * host arrays.  KDN_NOT_READY when the last frame kept none. */
+kdn_status kdn_frame_record(kdn_ctx* ctx, float* light, uint16_t* distance, uint16_t* normal, uint16_t* albedo, uint32_t* leaf);
 
 /* One frame of the denoiser's feature buffers: the frame size, whether the
  * light is already divided by the albedo (TemporalState::demodulated), and

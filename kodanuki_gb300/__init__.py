@@ -58,6 +58,7 @@ class Frame(ctypes.Structure):
 
 
 FRAME_DENOISE = 1  # include/kdn.h KDN_FRAME_DENOISE
+FRAME_RESTART = 2  # include/kdn.h KDN_FRAME_RESTART
 
 
 class FrameStats(ctypes.Structure):
@@ -77,7 +78,7 @@ class KdnError(RuntimeError):
 EXPORTS = [
     "kdn_status_string", "kdn_last_error", "kdn_open", "kdn_close", "kdn_upload_block", "kdn_build", "kdn_world_stats",
     "kdn_world_cell", "kdn_extend", "kdn_extend_device", "kdn_render", "kdn_render_device", "kdn_frame_stats_get", "kdn_flush_l2",
-    "kdn_frame_surfaces", "kdn_world_march", "kdn_world_locate", "kdn_temporal_device", "kdn_denoise", "kdn_denoise_device", "kdn_denoise_static",
+    "kdn_frame_surfaces", "kdn_frame_record", "kdn_world_march", "kdn_world_locate", "kdn_temporal_device", "kdn_denoise", "kdn_denoise_device", "kdn_denoise_static",
 ]
 
 
@@ -131,6 +132,7 @@ def library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.kdn_frame_stats_get.argtypes = [P, ctypes.POINTER(FrameStats)]
     L.kdn_flush_l2.argtypes = [P]
     L.kdn_frame_surfaces.argtypes = [P, P, P, P, P]
+    L.kdn_frame_record.argtypes = [P, P, P, P, P, P]
     L.kdn_world_march.argtypes = [P, ctypes.c_uint64, P, ctypes.c_uint32, P, ctypes.c_size_t, P]
     L.kdn_world_locate.argtypes = [P, P, ctypes.c_uint32, P, P]
     L.kdn_temporal_device.argtypes = [P, ctypes.POINTER(TemporalFrame), ctypes.POINTER(TemporalBuffers), P]
@@ -280,14 +282,14 @@ class Backend:
         return hits
 
     def render(self, width: int, height: int, samples: int, surfaces: int | None = None, seed: int | None = None,
-               first: int = 0, accumulate: bool = False, denoise: bool = False) -> np.ndarray:
+               first: int = 0, accumulate: bool = False, denoise: bool = False, restart: bool = False) -> np.ndarray:
         """Draw `samples` samples a pixel and return the pixel means
         (linear RGB, float32, height x width x 3), or with `denoise` the
         means filtered by the a-trous denoiser over the first surfaces."""
         sc = self.scene
         f = Frame(width, height, samples, surfaces if surfaces is not None else int(sc.render["surfaces"]),
                   seed if seed is not None else int(sc.render["seed"]), first, 1 if accumulate else 0,
-                  FRAME_DENOISE if denoise else 0)
+                  (FRAME_DENOISE if denoise else 0) | (FRAME_RESTART if restart else 0))
         out = np.zeros((height, width, 3), np.float32)
         self._check(self.lib.kdn_render(self.handle, ctypes.byref(f), _ptr(out)))
         return out
@@ -315,6 +317,18 @@ class Backend:
         b = np.zeros(len(pts), np.uint32)
         self._check(self.lib.kdn_world_locate(self.handle, _ptr(pts), len(pts), _ptr(a), _ptr(b)))
         return a, b
+
+    def frame_record(self, width: int, height: int) -> dict:
+        """The record of the last frame drawn with denoise=True: each pixel's
+        light of that call and the first surface of its last sample
+        (include/kdn.h kdn_frame_record); FP16 fields as float16 arrays."""
+        light = np.zeros((height, width, 3), np.float32)
+        distance = np.zeros((height, width), np.float16)
+        normal = np.zeros((height, width, 3), np.float16)
+        albedo = np.zeros((height, width, 3), np.float16)
+        leaf = np.zeros((height, width), np.uint32)
+        self._check(self.lib.kdn_frame_record(self.handle, _ptr(light), _ptr(distance), _ptr(normal), _ptr(albedo), _ptr(leaf)))
+        return {"light": light, "distance": distance, "normal": normal, "albedo": albedo, "leaf": leaf}
 
     def frame_surfaces(self, width: int, height: int) -> dict:
         """The first surfaces of the last frame drawn with denoise=True

@@ -102,6 +102,12 @@ struct ShadeArgs {
 	uint32_t leafCount;
 	uint32_t capacity;
 	uint32_t* error;
+	// where set (a denoised frame), the first surface of each pixel's last
+	// sample (core/frame.cpp record surfaces): FP16 bits, the leaf
+	uint16_t* firstDistance;
+	uint16_t* firstNormal;
+	uint16_t* firstAlbedo;
+	uint32_t* firstLeaf;
 };
 
 // The surfaces pass: the first surface through each pixel's centre, as the
@@ -122,12 +128,9 @@ cudaError_t uploadFrameConstants(const FrameConstants& c, cudaStream_t stream);
 cudaError_t launchCamera(const PathBuffers& paths, const QueueBuffers& queue, uint32_t firstPixel, uint32_t n, cudaStream_t stream, int smCount);
 cudaError_t launchShade(const ShadeArgs& args, cudaStream_t stream, int smCount);
 cudaError_t launchLines(const PathBuffers& paths, const ShadowBuffers& shadow, uint32_t capacity, cudaStream_t stream, int smCount);
-// moments (may be null): the denoiser's luminance moment, blended with share alpha
-cudaError_t launchFold(const PathBuffers& paths, uint32_t firstPixel, uint32_t pixels, uint32_t spp, double* sums, double* moments, double alpha, cudaStream_t stream, int smCount);
+// light (may be null): each pixel's mean of this call's samples, RGB float
+cudaError_t launchFold(const PathBuffers& paths, uint32_t firstPixel, uint32_t pixels, uint32_t spp, double* sums, float* light, cudaStream_t stream, int smCount);
 cudaError_t launchMeans(const double* sums, uint32_t pixels, double taken, float* out, cudaStream_t stream, int smCount);
-// The denoiser's per-pixel inputs: the luminance moment and the history
-// length (frames blended, at most the still cap).
-cudaError_t launchDenoiseInputs(const double* moments, uint32_t pixels, float history, float* moment, float* length, cudaStream_t stream, int smCount);
 cudaError_t launchSurfaceRays(const QueueBuffers& queue, uint32_t firstPixel, uint32_t n, cudaStream_t stream, int smCount);
 cudaError_t launchSurfaces(const SurfaceArgs& args, uint32_t n, cudaStream_t stream, int smCount);
 

@@ -7,6 +7,7 @@
 // synchronisation.  Pixel sums are kept in double on the device and persist
 // across calls (progressive accumulation) until a call starts afresh.
 #include "context.h"
+#include "temporal.h"
 #include "frame.h"
 
 #include <algorithm>
@@ -20,15 +21,21 @@ struct FrameState {
 	DeviceBuffer queuePaths[2], queueRays[2], hits, states, counts;
 	DeviceBuffer shadowPaths, shadowContribution;
 	DeviceBuffer sums, out, materials;
-	// the denoised form: luminance moments, first surfaces, denoiser inputs
-	DeviceBuffer moments, surfDistance, surfNormal, surfAlbedo, surfLeaf, denoiseMoment, denoiseLength, means;
+	// the shown frame (KDN_FRAME_DENOISE): the record of this frame (each
+	// pixel's light and the first surface of its last sample), and the
+	// G-buffer and the temporal state twice, this frame's and the one before
+	DeviceBuffer frameLight, firstDistance, firstNormal, firstAlbedo, firstLeaf;
+	DeviceBuffer gDistance[2], gNormal[2], gAlbedo[2], gLeaf[2];
+	DeviceBuffer tColour[2], tMoment[2], tLength[2];
 	uint32_t capacity = 0;
 	int32_t width = 0, height = 0;
 	double taken = 0;
-	// frames in the denoiser's moment history (temporal.cpp:838 heldBlend),
-	// 0 when the last frame kept none
-	float history = 0;
-	bool surfaced = false; // the last frame traced its first surfaces
+	int current    = 0;     // which of the pairs the next denoised frame writes
+	int shown      = -1;    // which of them the last denoised frame wrote; -1: none
+	double lens[14] = {};   // the last denoised frame's lens
+	int32_t stateWidth = 0, stateHeight = 0;
+	bool last_denoised = false; // the last frame drawn was a denoised one
+	bool surfaced() const { return last_denoised && shown >= 0; }
 	std::vector<cudaEvent_t> events;
 	kdn_frame_stats stats {};
 };
@@ -36,7 +43,7 @@ struct FrameState {
 void Context::releaseFrame() {
 	if (frame == nullptr) return;
 	FrameState& f = *frame;
-	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.hits, &f.states, &f.counts, &f.shadowPaths, &f.shadowContribution, &f.sums, &f.out, &f.materials, &f.moments, &f.surfDistance, &f.surfNormal, &f.surfAlbedo, &f.surfLeaf, &f.denoiseMoment, &f.denoiseLength, &f.means }) {
+	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.hits, &f.states, &f.counts, &f.shadowPaths, &f.shadowContribution, &f.sums, &f.out, &f.materials, &f.frameLight, &f.firstDistance, &f.firstNormal, &f.firstAlbedo, &f.firstLeaf, &f.gDistance[0], &f.gDistance[1], &f.gNormal[0], &f.gNormal[1], &f.gAlbedo[0], &f.gAlbedo[1], &f.gLeaf[0], &f.gLeaf[1], &f.tColour[0], &f.tColour[1], &f.tMoment[0], &f.tMoment[1], &f.tLength[0], &f.tLength[1] }) {
 		if (b->ptr) cudaFree(b->ptr);
 		b->ptr   = nullptr;
 		b->bytes = 0;
@@ -230,25 +237,20 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		const struct {
 			DeviceBuffer* b;
 			size_t bytes;
-		} wants[] = { { &f.moments, px * 8 }, { &f.surfDistance, px * 2 }, { &f.surfNormal, px * 6 }, { &f.surfAlbedo, px * 6 }, { &f.surfLeaf, px * 4 },
-			          { &f.denoiseMoment, px * 4 }, { &f.denoiseLength, px * 4 }, { &f.means, px * 12 } };
+		} wants[] = { { &f.frameLight, px * 12 }, { &f.firstDistance, px * 2 }, { &f.firstNormal, px * 6 }, { &f.firstAlbedo, px * 6 }, { &f.firstLeaf, px * 4 },
+			          { &f.gDistance[0], px * 2 }, { &f.gDistance[1], px * 2 }, { &f.gNormal[0], px * 6 }, { &f.gNormal[1], px * 6 },
+			          { &f.gAlbedo[0], px * 6 }, { &f.gAlbedo[1], px * 6 }, { &f.gLeaf[0], px * 4 }, { &f.gLeaf[1], px * 4 },
+			          { &f.tColour[0], px * 12 }, { &f.tColour[1], px * 12 }, { &f.tMoment[0], px * 4 }, { &f.tMoment[1], px * 4 },
+			          { &f.tLength[0], px * 4 }, { &f.tLength[1], px * 4 } };
 		for (const auto& w : wants) {
 			if ((s = ctx->ensure(*w.b, w.bytes)) != KDN_OK) return s;
 		}
 	}
 	if (fresh) {
 		if (!ctx->check(cudaMemsetAsync(f.sums.ptr, 0, size_t(pixels) * 3 * sizeof(double), stream), "clear sums")) return KDN_CUDA_ERROR;
-		f.taken   = 0;
-		f.history = 0;
+		f.taken = 0;
 	}
-	// temporal.cpp:831 historyShare: a fresh pixel takes the frame whole, a
-	// held one blends it in by 1 / (length + 1), at least 1 / the still cap
-	constexpr float kStillCap = 256;
-	double alpha              = 1.0;
-	if (denoised) {
-		if (f.history > 0) alpha = std::max(1.0 / (double(std::min(f.history, kStillCap)) + 1.0), 1.0 / double(kStillCap));
-		else if (!ctx->check(cudaMemsetAsync(f.moments.ptr, 0, size_t(pixels) * sizeof(double), stream), "clear moments")) return KDN_CUDA_ERROR;
-	}
+	const int cur = f.current; // the G-buffer and state pair this frame writes
 	f.width  = fr->width;
 	f.height = fr->height;
 	// constants
@@ -356,10 +358,10 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 			g.materials    = static_cast<const DeviceMaterial*>(f.materials.ptr);
 			g.leafMaterial = static_cast<const uint32_t*>(ctx->leafMaterial.ptr);
 			g.leafCount    = uint32_t(ctx->leafMaterial.bytes / 4);
-			g.distance     = static_cast<uint16_t*>(f.surfDistance.ptr);
-			g.normal       = static_cast<uint16_t*>(f.surfNormal.ptr);
-			g.albedo       = static_cast<uint16_t*>(f.surfAlbedo.ptr);
-			g.leaf         = static_cast<uint32_t*>(f.surfLeaf.ptr);
+			g.distance     = static_cast<uint16_t*>(f.gDistance[cur].ptr);
+			g.normal       = static_cast<uint16_t*>(f.gNormal[cur].ptr);
+			g.albedo       = static_cast<uint16_t*>(f.gAlbedo[cur].ptr);
+			g.leaf         = static_cast<uint32_t*>(f.gLeaf[cur].ptr);
 			if (!ctx->check(launchSurfaces(g, n, stream, ctx->smCount), "surfaces kernel")) return KDN_CUDA_ERROR;
 			launches += 4;
 		}
@@ -425,52 +427,98 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 			a.leafCount    = uint32_t(ctx->leafMaterial.bytes / 4);
 			a.capacity     = capacity;
 			a.error        = nullptr;
+			a.firstDistance = denoised ? static_cast<uint16_t*>(f.firstDistance.ptr) : nullptr;
+			a.firstNormal   = denoised ? static_cast<uint16_t*>(f.firstNormal.ptr) : nullptr;
+			a.firstAlbedo   = denoised ? static_cast<uint16_t*>(f.firstAlbedo.ptr) : nullptr;
+			a.firstLeaf     = denoised ? static_cast<uint32_t*>(f.firstLeaf.ptr) : nullptr;
 			if (!ctx->check(launchShade(a, stream, ctx->smCount), "shade kernel")) return KDN_CUDA_ERROR;
 			++launches;
 			cur = nxt;
 		}
-		if (!ctx->check(launchFold(P, first, chunk, spp, static_cast<double*>(f.sums.ptr), denoised ? static_cast<double*>(f.moments.ptr) : nullptr, alpha, stream, ctx->smCount), "fold kernel")) return KDN_CUDA_ERROR;
+		if (!ctx->check(launchFold(P, first, chunk, spp, static_cast<double*>(f.sums.ptr), denoised ? static_cast<float*>(f.frameLight.ptr) : nullptr, stream, ctx->smCount), "fold kernel")) return KDN_CUDA_ERROR;
 		++launches;
 	}
 	f.taken += double(spp);
-	f.history  = denoised ? std::min(f.history + 1.0f, kStillCap) : 0.0f;
-	f.surfaced = denoised;
+	f.last_denoised = denoised;
+	if (!denoised) f.shown = -1; // a frame without the shown chain drops the temporal history
+
 	float* image = out;
 	if (hostOut) {
 		if ((s = ctx->ensure(f.out, size_t(pixels) * 3 * sizeof(float))) != KDN_OK) return s;
 		image = static_cast<float*>(f.out.ptr);
 	}
-	float* means = denoised ? static_cast<float*>(f.means.ptr) : image;
-	if (!ctx->check(launchMeans(static_cast<const double*>(f.sums.ptr), pixels, f.taken, means, stream, ctx->smCount), "means kernel")) return KDN_CUDA_ERROR;
-	++launches;
-	if (denoised) {
-		// the shown frame: a still camera's temporal state (temporal.cpp:797
-		// freshBlend, :835 heldBlend; the colour is the exact running mean)
-		// through the a-trous filter (plugins/reconstruction/atrous/atrous.cpp:513
-		// denoisedFrame)
-		if (!ctx->check(launchDenoiseInputs(static_cast<const double*>(f.moments.ptr), pixels, f.history, static_cast<float*>(f.denoiseMoment.ptr),
-		                                    static_cast<float*>(f.denoiseLength.ptr), stream, ctx->smCount),
-		                "denoise inputs kernel"))
-			return KDN_CUDA_ERROR;
+	if (!denoised) {
+		if (!ctx->check(launchMeans(static_cast<const double*>(f.sums.ptr), pixels, f.taken, image, stream, ctx->smCount), "means kernel")) return KDN_CUDA_ERROR;
+		++launches;
+	} else {
+		// the shown frame (core/frame.cpp shownSurfaces, then the reconstruction
+		// chain temporal + a-trous): this frame's record and G-buffer through
+		// the temporal member (its history kept where the frame before was of
+		// this size and not restarted; moved where the lens changed), then its
+		// state through the a-trous filter, demodulated
+		// (plugins/reconstruction/atrous/atrous.cpp:513 denoisedFrame)
+		const V3 lensUp = cross(right, forward);
+		double lens[14];
+		const V3* parts[4] = { &eye, &forward, &right, &lensUp };
+		for (int k = 0; k < 4; ++k) {
+			lens[3 * k]     = parts[k]->x;
+			lens[3 * k + 1] = parts[k]->y;
+			lens[3 * k + 2] = parts[k]->z;
+		}
+		lens[12]        = std::tan(cam.fov / 2);
+		lens[13]        = double(fr->width) / double(fr->height);
+		const int prev  = 1 - cur;
+		const bool kept = f.shown == prev && f.stateWidth == fr->width && f.stateHeight == fr->height && !(fr->flags & KDN_FRAME_RESTART);
+		const bool moved = kept && std::memcmp(lens, f.lens, sizeof lens) != 0;
+		TemporalArgs ta {};
+		ta.width                  = fr->width;
+		ta.height                 = fr->height;
+		ta.moved                  = moved ? 1u : 0u;
+		ta.recounted              = 0;
+		ta.kept                   = kept ? 1u : 0u;
+		ta.now                    = temporalCameraOf(lens, fr->width, fr->height);
+		ta.before                 = temporalCameraOf(kept ? f.lens : lens, fr->width, fr->height);
+		ta.io.light               = static_cast<const float*>(f.frameLight.ptr);
+		ta.io.first_distance      = static_cast<const uint16_t*>(f.firstDistance.ptr);
+		ta.io.first_normal        = static_cast<const uint16_t*>(f.firstNormal.ptr);
+		ta.io.first_albedo        = static_cast<const uint16_t*>(f.firstAlbedo.ptr);
+		ta.io.first_leaf          = static_cast<const uint32_t*>(f.firstLeaf.ptr);
+		ta.io.centre_distance     = static_cast<const uint16_t*>(f.gDistance[cur].ptr);
+		ta.io.centre_normal       = static_cast<const uint16_t*>(f.gNormal[cur].ptr);
+		ta.io.centre_albedo       = static_cast<const uint16_t*>(f.gAlbedo[cur].ptr);
+		ta.io.centre_leaf         = static_cast<const uint32_t*>(f.gLeaf[cur].ptr);
+		ta.io.before_colour       = static_cast<const float*>(f.tColour[prev].ptr);
+		ta.io.before_moment       = static_cast<const float*>(f.tMoment[prev].ptr);
+		ta.io.before_length       = static_cast<const float*>(f.tLength[prev].ptr);
+		ta.io.before_distance     = static_cast<const uint16_t*>(f.gDistance[prev].ptr);
+		ta.io.before_normal       = static_cast<const uint16_t*>(f.gNormal[prev].ptr);
+		ta.io.before_leaf         = static_cast<const uint32_t*>(f.gLeaf[prev].ptr);
+		ta.io.colour              = static_cast<float*>(f.tColour[cur].ptr);
+		ta.io.moment              = static_cast<float*>(f.tMoment[cur].ptr);
+		ta.io.length              = static_cast<float*>(f.tLength[cur].ptr);
+		ta.io.image               = nullptr;
+		if (!ctx->check(launchTemporal(ta, stream), "temporal kernel")) return KDN_CUDA_ERROR;
 		kdn_denoise_frame df {};
 		df.width  = fr->width;
 		df.height = fr->height;
-		const V3 lensUp = cross(right, forward);
-		const V3* lens[4] = { &eye, &forward, &right, &lensUp };
-		double* into[4]   = { df.eye, df.forward, df.right, df.up };
-		for (int k = 0; k < 4; ++k) {
-			into[k][0] = lens[k]->x;
-			into[k][1] = lens[k]->y;
-			into[k][2] = lens[k]->z;
+		for (int k = 0; k < 3; ++k) {
+			df.eye[k]     = lens[k];
+			df.forward[k] = lens[3 + k];
+			df.right[k]   = lens[6 + k];
+			df.up[k]      = lens[9 + k];
 		}
-		df.reach       = std::tan(cam.fov / 2);
-		df.aspect      = double(fr->width) / double(fr->height);
-		df.demodulated = 0;
-		if ((s = denoiseOnDevice(ctx, &df, means, static_cast<const float*>(f.denoiseMoment.ptr), static_cast<const float*>(f.denoiseLength.ptr),
-		                         static_cast<const uint16_t*>(f.surfDistance.ptr), static_cast<const uint16_t*>(f.surfNormal.ptr),
-		                         static_cast<const uint16_t*>(f.surfAlbedo.ptr), static_cast<const uint32_t*>(f.surfLeaf.ptr), image, stream)) != KDN_OK)
+		df.reach       = lens[12];
+		df.aspect      = lens[13];
+		df.demodulated = 1;
+		if ((s = denoiseOnDevice(ctx, &df, ta.io.colour, ta.io.moment, ta.io.length, ta.io.centre_distance, ta.io.centre_normal, ta.io.centre_albedo,
+		                         ta.io.centre_leaf, image, stream)) != KDN_OK)
 			return s;
 		launches += 8;
+		std::memcpy(f.lens, lens, sizeof lens);
+		f.stateWidth  = fr->width;
+		f.stateHeight = fr->height;
+		f.shown       = cur;
+		f.current     = prev;
 	}
 	if (!ctx->check(cudaEventRecord(f.events[1], stream), "event")) return KDN_CUDA_ERROR;
 	if (hostOut && !ctx->check(cudaMemcpyAsync(out, image, size_t(pixels) * 3 * sizeof(float), cudaMemcpyDeviceToHost, stream), "copy frame")) return KDN_CUDA_ERROR;
@@ -527,11 +575,11 @@ kdn_status kdn_frame_stats_get(kdn_ctx* handle, kdn_frame_stats* stats) {
 	return KDN_OK;
 }
 
-kdn_status kdn_frame_surfaces(kdn_ctx* handle, uint16_t* distance, uint16_t* normal, uint16_t* albedo, uint32_t* leaf) {
-	if (handle == nullptr || !distance || !normal || !albedo || !leaf) return KDN_BAD_ARG;
+kdn_status kdn_frame_record(kdn_ctx* handle, float* light, uint16_t* distance, uint16_t* normal, uint16_t* albedo, uint32_t* leaf) {
+	if (handle == nullptr || !light || !distance || !normal || !albedo || !leaf) return KDN_BAD_ARG;
 	Context* ctx = reinterpret_cast<Context*>(handle);
 	std::lock_guard<std::mutex> guard(ctx->lock);
-	if (ctx->frame == nullptr || !ctx->frame->surfaced) return ctx->fail(KDN_NOT_READY, "kdn_frame_surfaces: the last frame was not drawn with KDN_FRAME_DENOISE");
+	if (ctx->frame == nullptr || !ctx->frame->surfaced()) return ctx->fail(KDN_NOT_READY, "kdn_frame_record: the last frame was not drawn with KDN_FRAME_DENOISE");
 	const kdn::FrameState& f = *ctx->frame;
 	const size_t n           = size_t(f.width) * size_t(f.height);
 	if (!ctx->check(cudaSetDevice(ctx->device), "cudaSetDevice")) return KDN_CUDA_ERROR;
@@ -539,7 +587,29 @@ kdn_status kdn_frame_surfaces(kdn_ctx* handle, uint16_t* distance, uint16_t* nor
 		void* to;
 		const void* from;
 		size_t bytes;
-	} copies[] = { { distance, f.surfDistance.ptr, n * 2 }, { normal, f.surfNormal.ptr, n * 6 }, { albedo, f.surfAlbedo.ptr, n * 6 }, { leaf, f.surfLeaf.ptr, n * 4 } };
+	} copies[] = { { light, f.frameLight.ptr, n * 12 }, { distance, f.firstDistance.ptr, n * 2 }, { normal, f.firstNormal.ptr, n * 6 },
+		           { albedo, f.firstAlbedo.ptr, n * 6 }, { leaf, f.firstLeaf.ptr, n * 4 } };
+	for (const auto& c : copies) {
+		if (!ctx->check(cudaMemcpyAsync(c.to, c.from, c.bytes, cudaMemcpyDeviceToHost, ctx->stream), "kdn_frame_record copy")) return KDN_CUDA_ERROR;
+	}
+	if (!ctx->check(cudaStreamSynchronize(ctx->stream), "kdn_frame_record")) return KDN_CUDA_ERROR;
+	return KDN_OK;
+}
+
+kdn_status kdn_frame_surfaces(kdn_ctx* handle, uint16_t* distance, uint16_t* normal, uint16_t* albedo, uint32_t* leaf) {
+	if (handle == nullptr || !distance || !normal || !albedo || !leaf) return KDN_BAD_ARG;
+	Context* ctx = reinterpret_cast<Context*>(handle);
+	std::lock_guard<std::mutex> guard(ctx->lock);
+	if (ctx->frame == nullptr || !ctx->frame->surfaced()) return ctx->fail(KDN_NOT_READY, "kdn_frame_surfaces: the last frame was not drawn with KDN_FRAME_DENOISE");
+	const kdn::FrameState& f = *ctx->frame;
+	const size_t n           = size_t(f.width) * size_t(f.height);
+	if (!ctx->check(cudaSetDevice(ctx->device), "cudaSetDevice")) return KDN_CUDA_ERROR;
+	const struct {
+		void* to;
+		const void* from;
+		size_t bytes;
+	} copies[] = { { distance, f.gDistance[f.shown].ptr, n * 2 }, { normal, f.gNormal[f.shown].ptr, n * 6 }, { albedo, f.gAlbedo[f.shown].ptr, n * 6 },
+		           { leaf, f.gLeaf[f.shown].ptr, n * 4 } };
 	for (const auto& c : copies) {
 		if (!ctx->check(cudaMemcpyAsync(c.to, c.from, c.bytes, cudaMemcpyDeviceToHost, ctx->stream), "kdn_frame_surfaces copy")) return KDN_CUDA_ERROR;
 	}

@@ -466,6 +466,29 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(ShadeArgs A) {
 					R = add4(R, scale4(mul4(T, spectrumOf(l.radiance[0], l.radiance[1], l.radiance[2], nm)), w));
 				}
 			}
+			// the record's first surface of the pixel's last sample
+			// (trace.cpp:1469 recordedStand, :1445 vertexSurface; missed: batch.cpp:46)
+			if (camera && A.firstLeaf != nullptr && A.paths.sample[p] + 1u == cFrame.firstSample + cFrame.spp) {
+				const uint32_t px = A.paths.pixel[p];
+				float3 n          = make_float3(0.0f, 0.0f, 0.0f);
+				float3 albedo     = make_float3(0.0f, 0.0f, 0.0f);
+				float distance    = __int_as_float(0x7f800000);
+				if (found) {
+					n = make_float3(hit.normal[0], hit.normal[1], hit.normal[2]);
+					if (dot3(n, heading) >= 0.0f) n = n * -1.0f;
+					albedo         = albedoAt(hit, A.materials, A.leafMaterial, A.leafCount);
+					const float3 d = make_float3(hit.point[0], hit.point[1], hit.point[2]) - origin;
+					distance       = sqrtf(dot3(d, d));
+				}
+				A.firstDistance[px]       = __half_as_ushort(__float2half_rn(distance));
+				A.firstLeaf[px]           = found ? hit.leaf : kNoLeaf;
+				A.firstNormal[3 * px]     = __half_as_ushort(__float2half_rn(n.x));
+				A.firstNormal[3 * px + 1] = __half_as_ushort(__float2half_rn(n.y));
+				A.firstNormal[3 * px + 2] = __half_as_ushort(__float2half_rn(n.z));
+				A.firstAlbedo[3 * px]     = __half_as_ushort(__float2half_rn(albedo.x));
+				A.firstAlbedo[3 * px + 1] = __half_as_ushort(__float2half_rn(albedo.y));
+				A.firstAlbedo[3 * px + 2] = __half_as_ushort(__float2half_rn(albedo.z));
+			}
 			if (!found) {
 				const float3 sky = skyColour(heading);
 				R                = add4(R, mul4(T, spectrumOf(sky.x, sky.y, sky.z, nm)));
@@ -588,10 +611,8 @@ __global__ void __launch_bounds__(kBlock) linesKernel(PathBuffers P, ShadowBuffe
 }
 
 // ---- K-fold: per pixel, the samples' colours (frame.cpp:273 foldPixels) ----
-// With moments, also the denoiser's history of the luminance moment: this
-// frame's pixel colour (its spp samples) blended in with share alpha
-// (temporal.cpp:848 heldBlend, moment = history * (1 - alpha) + L^2 * alpha).
-__global__ void __launch_bounds__(kBlock) foldKernel(PathBuffers P, uint32_t firstPixel, uint32_t pixels, uint32_t spp, double* sums, double* moments, double alpha) {
+// With light, also this call's mean a pixel (the frame record's light).
+__global__ void __launch_bounds__(kBlock) foldKernel(PathBuffers P, uint32_t firstPixel, uint32_t pixels, uint32_t spp, double* sums, float* light) {
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < pixels; i += gridDim.x * blockDim.x) {
 		double r = 0.0, g = 0.0, b = 0.0;
 		for (uint32_t k = 0; k < spp; ++k) {
@@ -605,11 +626,11 @@ __global__ void __launch_bounds__(kBlock) foldKernel(PathBuffers P, uint32_t fir
 		s[0] += r;
 		s[1] += g;
 		s[2] += b;
-		if (moments) {
-			// math/colour.cpp:49 luminanceOf
-			const double l = (0.2126 * r + 0.7152 * g + 0.0722 * b) / double(spp);
-			double& m      = moments[firstPixel + i];
-			m              = m * (1.0 - alpha) + l * l * alpha;
+		if (light) {
+			float* l = light + 3ull * (firstPixel + i);
+			l[0]     = float(r / double(spp));
+			l[1]     = float(g / double(spp));
+			l[2]     = float(b / double(spp));
 		}
 	}
 }
@@ -617,13 +638,6 @@ __global__ void __launch_bounds__(kBlock) foldKernel(PathBuffers P, uint32_t fir
 __global__ void __launch_bounds__(kBlock) meansKernel(const double* sums, uint32_t pixels, double taken, float* out) {
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < pixels * 3u; i += gridDim.x * blockDim.x) {
 		out[i] = float(sums[i] / taken);
-	}
-}
-
-__global__ void __launch_bounds__(kBlock) denoiseInputsKernel(const double* moments, uint32_t pixels, float history, float* moment, float* length) {
-	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < pixels; i += gridDim.x * blockDim.x) {
-		moment[i] = float(moments[i]);
-		length[i] = history;
 	}
 }
 
@@ -653,13 +667,8 @@ cudaError_t launchLines(const PathBuffers& paths, const ShadowBuffers& shadow, u
 	return cudaGetLastError();
 }
 
-cudaError_t launchFold(const PathBuffers& paths, uint32_t firstPixel, uint32_t pixels, uint32_t spp, double* sums, double* moments, double alpha, cudaStream_t stream, int smCount) {
-	foldKernel<<<gridFor(pixels, smCount), kBlock, 0, stream>>>(paths, firstPixel, pixels, spp, sums, moments, alpha);
-	return cudaGetLastError();
-}
-
-cudaError_t launchDenoiseInputs(const double* moments, uint32_t pixels, float history, float* moment, float* length, cudaStream_t stream, int smCount) {
-	denoiseInputsKernel<<<gridFor(pixels, smCount), kBlock, 0, stream>>>(moments, pixels, history, moment, length);
+cudaError_t launchFold(const PathBuffers& paths, uint32_t firstPixel, uint32_t pixels, uint32_t spp, double* sums, float* light, cudaStream_t stream, int smCount) {
+	foldKernel<<<gridFor(pixels, smCount), kBlock, 0, stream>>>(paths, firstPixel, pixels, spp, sums, light);
 	return cudaGetLastError();
 }
 

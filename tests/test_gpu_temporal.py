@@ -6,7 +6,8 @@ reference left after the frame before.
 The device works in FP32 and the reference in double; the bar: the state's
 length equal and its colour, moment and the shown light within 1e-3
 relative for at least 99.5% of pixels (a surface test on a plane's edge may
-fall the other way in FP32), and within 1e-4 relative at the median.
+fall the other way in FP32), and within 1e-4 relative at the median; the
+length within 1e-5 (a reprojected history's length is a bilinear blend).
 """
 import ctypes
 import os
@@ -85,7 +86,9 @@ def test_temporal_matches_reference(backend, frame):
         got = got.cpu().numpy().astype(np.float64).reshape(want.shape)
         return np.abs(got - want) / (np.abs(want) + 1e-3)
 
-    length_same = (length.cpu().numpy() == g[f"{frame}.state.length"].astype(np.float32)).mean()
+    # a reprojected history's length is a bilinear blend: FP32 against double
+    want_length = g[f"{frame}.state.length"].astype(np.float64)
+    length_same = (np.abs(length.cpu().numpy().astype(np.float64) - want_length) <= 1e-5 * np.maximum(want_length, 1.0)).mean()
     errs = {"colour": rel(colour, g[f"{frame}.state.colour"]).max(axis=1), "moment": rel(moment, g[f"{frame}.state.moment"]),
             "image": rel(image, g[f"{frame}.image"].astype(np.float64)).max(axis=1)}
     print(f"frame {frame}: length equal {length_same:.4f}; " + "; ".join(f"{k} p50 {np.median(e):.1e} within 1e-3 {np.mean(e <= 1e-3):.4f}"
