@@ -6,8 +6,9 @@ One step is one frame of the config-2 scene (4096 primitives in 512 CSG
 groups with floor-based repetition, 40% matte / 40% GGX metal / 20%
 dispersive glass, two quad lights and a constant 6500 K sky), 1920x1080 at
 64 samples a pixel, paths of at most 16 surfaces: 132.7 M samples a step,
-shown through the a-trous denoiser (pixel-centre surfaces as FP16
-features, a still camera's first frame of temporal history).
+shown through the reference's reconstruction chain temporal + a-trous
+(the record and the pixel-centre G-buffer as FP16 features; a still
+camera, so each frame's history is the frame before's).
 The scene is the reference renderer's own compilation of the seeded scene
 text (tests/golden/scenes/c2.npz); the cut octree is built once before the
 timed region and reported apart (build_s), as the reference reports its
@@ -43,7 +44,7 @@ sys.path.insert(0, ROOT)
 METRIC = "Msamples/s @1080p vs CPU; equal-time relMSE guided vs plain; p50/p99 latency"
 SCENE = os.path.join(ROOT, "tests", "golden", "scenes", "c2.npz")
 WIDTH, HEIGHT, SPP, SURFACES = 1920, 1080, 64, 16
-DENOISE = True  # the a-trous denoiser on the frame's FP16 features
+DENOISE = True  # the temporal member and the a-trous denoiser on the frame's FP16 features
 # DRAM bytes the trace kernel moves a ray (read + write): every trace
 # launch of a 960x540x8 config-2 frame captured by ncu (cold L2 a launch),
 # over the rays the kernel counted (profiles/trace_kernel_config2_960x540.md)
@@ -111,7 +112,7 @@ def peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-WORKLOAD = "config-2: 4096 primitives, 1920x1080, 64 spp, 16 surfaces, FP32, a-trous denoiser on FP16 features"
+WORKLOAD = "config-2: 4096 primitives, 1920x1080, 64 spp, 16 surfaces, FP32, temporal + a-trous denoiser on FP16 features"
 
 
 def spread_rows(count: int) -> list[int]:

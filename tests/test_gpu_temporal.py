@@ -4,7 +4,7 @@ still sequence (tests/golden/temporal.npz), each frame fed the state the
 reference left after the frame before.
 
 The device works in FP32 and the reference in double; the bar: the state's
-length equal and its colour, moment and the shown light within 1e-3
+colour, moment and the shown light within 1e-3
 relative for at least 99.5% of pixels (a surface test on a plane's edge may
 fall the other way in FP32), and within 1e-4 relative at the median; the
 length within 1e-5 (a reprojected history's length is a bilinear blend).
