@@ -395,8 +395,8 @@ __global__ void __launch_bounds__(kTraceBlock) hitKernel(HitArgs args) {
 			const float inset = h.kind == 2 ? 2.0f * tolerance(p) : 0.0f;
 			const float q[3]  = { p[0] + d[0] * inset, p[1] + d[1] * inset, p[2] + d[2] * inset };
 			const GpuProgram g = w.programs[h.first + h.index];
+			// every slot is written before a step reads it (the slots follow the SSA order)
 			DualF dslots[kMaxSlots];
-			for (uint32_t s = 0; s < kMaxSlots; ++s) dslots[s] = dualConst(0.0f);
 			const DualF v = evalDual(w.steps + g.code, g.count, g.slot, dslots, q);
 			float values[kMaxSsa];
 			uint32_t leaf, other;
