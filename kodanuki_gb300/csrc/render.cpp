@@ -37,6 +37,8 @@ struct FrameState {
 	bool last_denoised = false; // the last frame drawn was a denoised one
 	bool surfaced() const { return last_denoised && shown >= 0; }
 	std::vector<cudaEvent_t> events;
+	cudaStream_t side     = nullptr;              // the second lane's stream
+	cudaEvent_t joined[2] = { nullptr, nullptr }; // the lanes' start and end
 	kdn_frame_stats stats {};
 };
 
@@ -49,6 +51,13 @@ void Context::releaseFrame() {
 		b->bytes = 0;
 	}
 	for (cudaEvent_t e : f.events) cudaEventDestroy(e);
+	for (cudaEvent_t e : f.joined) {
+		if (e) cudaEventDestroy(e);
+	}
+	if (f.side) {
+		cudaStreamSynchronize(f.side);
+		cudaStreamDestroy(f.side);
+	}
 	delete frame;
 	frame = nullptr;
 }
@@ -162,23 +171,28 @@ namespace {
 constexpr size_t kPathBytes = 4 * 4 + 5 * 16 + 2 * 4 + 2 * 2 * sizeof(kdn_ray) + sizeof(kdn_hit) + 2 * sizeof(kdn::HitState) + 4 + 16;
 static_assert(kPathBytes == 364, "path bytes");
 
-// The paths one chunk of a frame holds.  The whole frame where the device
-// has room for it (at most 2^28 paths, half the free memory): every launch
-// then has the frame's rays to spread over the GPU, and the slow rays of a
-// launch hold back one lane each rather than a small chunk's whole tail.
+// Streams a frame's chunks go round (render lanes).
+constexpr int kLanes = 2;
+
+// The paths the lanes' chunks hold together: the whole frame where the
+// device has room for it (at most 2^28 paths, half the free memory), so
+// every launch has a large share of the frame's rays to spread over the GPU
+// and the slow rays of a launch hold back one thread each, not a small
+// chunk's whole tail.
 uint64_t chunkPaths(Context* ctx, uint64_t framePaths) {
 	size_t freeBytes = 0, totalBytes = 0;
 	if (cudaMemGetInfo(&freeBytes, &totalBytes) != cudaSuccess) freeBytes = 0;
-	const uint64_t held = ctx->frame ? uint64_t(ctx->frame->capacity) * kPathBytes : 0;
+	const uint64_t held = ctx->frame ? uint64_t(ctx->frame->capacity) * kLanes * kPathBytes : 0;
 	const uint64_t room = (uint64_t(freeBytes) + held) / 2 / kPathBytes;
 	return std::min<uint64_t>(framePaths, std::min<uint64_t>(uint64_t(1) << 28, std::max<uint64_t>(room, uint64_t(1) << 20)));
 }
 
+// The path buffers for a chunk of `capacity` paths on each lane.
 kdn_status ensureFrame(Context* ctx, uint32_t capacity) {
 	if (ctx->frame == nullptr) ctx->frame = new FrameState();
 	FrameState& f = *ctx->frame;
 	if (f.capacity >= capacity) return KDN_OK;
-	const size_t n = capacity;
+	const size_t n = size_t(capacity) * kLanes;
 	kdn_status s;
 	struct Want {
 		kdn::DeviceBuffer* b;
@@ -222,8 +236,10 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	}
 	const uint32_t pixels = uint32_t(fr->width) * uint32_t(fr->height);
 	const uint32_t spp    = uint32_t(fr->samples);
-	const uint64_t want        = chunkPaths(ctx, uint64_t(pixels) * spp);
-	const uint32_t chunkPixels = uint32_t(std::max<uint64_t>(1, want / spp));
+	// a chunk a lane: the frame's paths halved where they fit, else as many as
+	// the lanes' share of the room holds
+	const uint64_t want        = chunkPaths(ctx, uint64_t(pixels) * spp) / kLanes;
+	const uint32_t chunkPixels = uint32_t(std::max<uint64_t>(1, (want + spp - 1) / spp));
 	const uint32_t capacity    = chunkPixels * spp;
 	kdn_status s = ensureFrame(ctx, capacity);
 	if (s != KDN_OK) return s;
@@ -296,25 +312,60 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	P.drawn      = static_cast<float*>(f.drawn.ptr);
 	P.state      = static_cast<uint32_t*>(f.state.ptr);
 	P.from       = static_cast<float4*>(f.from.ptr);
-	uint32_t* counts = static_cast<uint32_t*>(f.counts.ptr); // [0],[1] ray queues, [2] lines
-	QueueBuffers Q[2];
-	for (int k = 0; k < 2; ++k) {
-		Q[k].paths = static_cast<uint32_t*>(f.queuePaths[k].ptr);
-		Q[k].rays  = static_cast<kdn_ray*>(f.queueRays[k].ptr);
-		Q[k].count = counts + k;
-	}
-	// the shadow lines a shade writes go to the second half of the next
-	// queue's rays (and of the hit states), so the next bounce's trace launch
-	// takes them with its path rays
-	HitState* states = static_cast<HitState*>(f.states.ptr);
-	ShadowBuffers S;
-	S.rays         = nullptr; // set a bounce: the second half of the next queue
-	S.paths        = static_cast<uint32_t*>(f.shadowPaths.ptr);
-	S.contribution = static_cast<float4*>(f.shadowContribution.ptr);
-	S.count        = counts + 2;
-	S.states       = states + capacity;
-	uint32_t* none = counts + 3; // a count of zero
+	// Lanes: the frame's chunks go round two streams, each lane with its own
+	// share of the path buffers, queues and counters, so one chunk's work
+	// fills the SMs another chunk's launch leaves idle in its tail (the
+	// slowest rays of a trace launch).
+	uint32_t* counts = static_cast<uint32_t*>(f.counts.ptr); // a lane: [0],[1] ray queues, [2] lines, [3] zero
 	if (!ctx->check(cudaMemsetAsync(counts, 0, 64, stream), "clear counts")) return KDN_CUDA_ERROR;
+	if (f.side == nullptr && !ctx->check(cudaStreamCreateWithFlags(&f.side, cudaStreamNonBlocking), "cudaStreamCreate")) return KDN_CUDA_ERROR;
+	if (f.joined[0] == nullptr) {
+		for (cudaEvent_t& e : f.joined) {
+			if (!ctx->check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate")) return KDN_CUDA_ERROR;
+		}
+	}
+	const cudaStream_t lanes[kLanes] = { stream, f.side };
+	struct Lane {
+		PathBuffers P;
+		QueueBuffers Q[2];
+		ShadowBuffers S;
+		HitState* states;
+		kdn_hit* hits;
+		uint32_t* none;
+		uint32_t* fetch;
+	};
+	Lane lane[kLanes];
+	for (int l = 0; l < kLanes; ++l) {
+		const size_t base = size_t(l) * capacity;
+		Lane& L           = lane[l];
+		L.P               = P;
+		L.P.pixel         = P.pixel + base;
+		L.P.sample        = P.sample + base;
+		L.P.throughput    = P.throughput + base;
+		L.P.radiance      = P.radiance + base;
+		L.P.nanometres    = P.nanometres + base;
+		L.P.density       = P.density + base;
+		L.P.drawn         = P.drawn + base;
+		L.P.state         = P.state + base;
+		L.P.from          = P.from + base;
+		for (int k = 0; k < 2; ++k) {
+			L.Q[k].paths = static_cast<uint32_t*>(f.queuePaths[k].ptr) + base;
+			L.Q[k].rays  = static_cast<kdn_ray*>(f.queueRays[k].ptr) + 2 * base;
+			L.Q[k].count = counts + 4 * l + k;
+		}
+		// the shadow lines a shade writes go to the second half of the next
+		// queue's rays (and of the hit states), so the next bounce's trace
+		// launch takes them with its path rays
+		L.states         = static_cast<HitState*>(f.states.ptr) + 2 * base;
+		L.hits           = static_cast<kdn_hit*>(f.hits.ptr) + base;
+		L.S.rays         = nullptr; // set a bounce: the second half of the next queue
+		L.S.paths        = static_cast<uint32_t*>(f.shadowPaths.ptr) + base;
+		L.S.contribution = static_cast<float4*>(f.shadowContribution.ptr) + base;
+		L.S.count        = counts + 4 * l + 2;
+		L.S.states       = L.states + capacity;
+		L.none           = counts + 4 * l + 3;
+		L.fetch          = static_cast<uint32_t*>(ctx->fetch.ptr) + l;
+	}
 
 	// timing: one event pair around the frame, one around each trace launch
 	const uint32_t chunks = (pixels + chunkPixels - 1) / chunkPixels;
@@ -329,31 +380,33 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	if (!ctx->check(cudaEventRecord(f.events[0], stream), "event")) return KDN_CUDA_ERROR;
 	uint32_t launches = 0;
 	if (denoised) {
-		// core/surfaces.cpp:133 tracedSurfaces: the denoiser's features
+		// core/surfaces.cpp:133 tracedSurfaces: the denoiser's features, on the
+		// first lane before its chunks
+		const Lane& L = lane[0];
 		for (uint32_t first = 0; first < pixels; first += capacity) {
 			const uint32_t n = std::min(capacity, pixels - first);
-			if (!ctx->check(launchSurfaceRays(Q[0], first, n, stream, ctx->smCount), "surface rays kernel")) return KDN_CUDA_ERROR;
+			if (!ctx->check(launchSurfaceRays(L.Q[0], first, n, stream, ctx->smCount), "surface rays kernel")) return KDN_CUDA_ERROR;
 			TraceArgs t;
 			t.world          = ctx->world;
-			t.rays           = Q[0].rays;
+			t.rays           = L.Q[0].rays;
 			t.n              = n;
-			t.states         = static_cast<HitState*>(f.states.ptr);
+			t.states         = L.states;
 			t.objectMaterial = static_cast<const uint32_t*>(ctx->objectMaterial.ptr);
 			t.maxSteps       = kMarchSteps;
 			t.counters       = nullptr;
-			t.count          = Q[0].count;
-			t.fetch          = static_cast<uint32_t*>(ctx->fetch.ptr);
+			t.count          = L.Q[0].count;
+			t.fetch          = L.fetch;
 			if (!ctx->check(launchTrace(t, stream, ctx->smCount), "surface trace kernel")) return KDN_CUDA_ERROR;
 			HitArgs h;
 			h.world  = ctx->world;
-			h.rays   = Q[0].rays;
+			h.rays   = L.Q[0].rays;
 			h.states = t.states;
 			h.n      = n;
-			h.hits   = static_cast<kdn_hit*>(f.hits.ptr);
-			h.count  = Q[0].count;
+			h.hits   = L.hits;
+			h.count  = L.Q[0].count;
 			if (!ctx->check(launchHits(h, stream, ctx->smCount), "surface hit kernel")) return KDN_CUDA_ERROR;
 			SurfaceArgs g;
-			g.rays         = Q[0];
+			g.rays         = L.Q[0];
 			g.hits         = h.hits;
 			g.materials    = static_cast<const DeviceMaterial*>(f.materials.ptr);
 			g.leafMaterial = static_cast<const uint32_t*>(ctx->leafMaterial.ptr);
@@ -366,78 +419,87 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 			launches += 4;
 		}
 	}
-	for (uint32_t first = 0; first < pixels; first += chunkPixels) {
-		const uint32_t chunk = std::min(chunkPixels, pixels - first);
-		const uint32_t n     = chunk * spp;
-		if (!ctx->check(launchCamera(P, Q[0], first, n, stream, ctx->smCount), "camera kernel")) return KDN_CUDA_ERROR;
+	// the second lane starts after what the first holds so far
+	if (!ctx->check(cudaEventRecord(f.joined[0], stream), "event") || !ctx->check(cudaStreamWaitEvent(f.side, f.joined[0], 0), "stream wait")) return KDN_CUDA_ERROR;
+	uint32_t chunkIndex = 0;
+	for (uint32_t first = 0; first < pixels; first += chunkPixels, ++chunkIndex) {
+		const int l              = int(chunkIndex % kLanes);
+		const Lane& L            = lane[l];
+		const cudaStream_t on    = lanes[l];
+		const uint32_t chunk     = std::min(chunkPixels, pixels - first);
+		const uint32_t n         = chunk * spp;
+		const PathBuffers& LP    = L.P;
+		if (!ctx->check(launchCamera(LP, L.Q[0], first, n, on, ctx->smCount), "camera kernel")) return KDN_CUDA_ERROR;
 		++launches;
-		if (!ctx->check(cudaMemsetAsync(S.count, 0, 4, stream), "clear lines")) return KDN_CUDA_ERROR;
-		int cur = 0;
+		if (!ctx->check(cudaMemsetAsync(L.S.count, 0, 4, on), "clear lines")) return KDN_CUDA_ERROR;
+		int q = 0;
 		// each round traces the bounce's path rays and the bounce before's
 		// shadow lines in one launch; a last round traces the last lines alone
 		for (int bounce = 0; bounce <= fr->surfaces; ++bounce) {
 			const bool last = bounce == fr->surfaces;
-			const int nxt   = 1 - cur;
+			const int nxt   = 1 - q;
 			TraceArgs t;
 			t.world          = ctx->world;
-			t.rays           = Q[cur].rays;
+			t.rays           = L.Q[q].rays;
 			t.n              = n;
-			t.states         = states;
+			t.states         = L.states;
 			t.objectMaterial = static_cast<const uint32_t*>(ctx->objectMaterial.ptr);
 			t.maxSteps       = kMarchSteps;
 			t.counters       = static_cast<unsigned long long*>(ctx->counters.ptr);
-			t.count          = last ? none : Q[cur].count;
-			t.fetch          = static_cast<uint32_t*>(ctx->fetch.ptr);
-			t.secondCount    = S.count;
+			t.count          = last ? L.none : L.Q[q].count;
+			t.fetch          = L.fetch;
+			t.secondCount    = L.S.count;
 			t.second         = capacity;
-			cudaEventRecord(f.events[ev++], stream);
-			if (!ctx->check(launchTrace(t, stream, ctx->smCount), "trace kernel")) return KDN_CUDA_ERROR;
-			cudaEventRecord(f.events[ev++], stream);
+			cudaEventRecord(f.events[ev++], on);
+			if (!ctx->check(launchTrace(t, on, ctx->smCount), "trace kernel")) return KDN_CUDA_ERROR;
+			cudaEventRecord(f.events[ev++], on);
 			++launches;
 			if (!last) {
 				HitArgs h;
 				h.world  = ctx->world;
-				h.rays   = Q[cur].rays;
-				h.states = states;
+				h.rays   = L.Q[q].rays;
+				h.states = L.states;
 				h.n      = n;
-				h.hits   = static_cast<kdn_hit*>(f.hits.ptr);
-				h.count  = Q[cur].count;
-				if (!ctx->check(launchHits(h, stream, ctx->smCount), "hit kernel")) return KDN_CUDA_ERROR;
+				h.hits   = L.hits;
+				h.count  = L.Q[q].count;
+				if (!ctx->check(launchHits(h, on, ctx->smCount), "hit kernel")) return KDN_CUDA_ERROR;
 				++launches;
 			}
 			if (bounce > 0) {
 				// the bounce before's lines that reached their lamps
-				ShadowBuffers lines = S;
-				lines.rays          = Q[cur].rays + capacity;
-				if (!ctx->check(launchLines(P, lines, capacity, stream, ctx->smCount), "lines kernel")) return KDN_CUDA_ERROR;
+				ShadowBuffers lines = L.S;
+				lines.rays          = L.Q[q].rays + capacity;
+				if (!ctx->check(launchLines(LP, lines, capacity, on, ctx->smCount), "lines kernel")) return KDN_CUDA_ERROR;
 				++launches;
 			}
 			if (last) break;
-			if (!ctx->check(cudaMemsetAsync(Q[nxt].count, 0, 4, stream), "clear queue")) return KDN_CUDA_ERROR;
-			if (!ctx->check(cudaMemsetAsync(S.count, 0, 4, stream), "clear lines")) return KDN_CUDA_ERROR;
+			if (!ctx->check(cudaMemsetAsync(L.Q[nxt].count, 0, 4, on), "clear queue")) return KDN_CUDA_ERROR;
+			if (!ctx->check(cudaMemsetAsync(L.S.count, 0, 4, on), "clear lines")) return KDN_CUDA_ERROR;
 			ShadeArgs a;
-			a.paths        = P;
-			a.in           = Q[cur];
-			a.out          = Q[nxt];
-			a.shadow       = S;
-			a.shadow.rays  = Q[nxt].rays + capacity;
-			a.hits         = static_cast<const kdn_hit*>(f.hits.ptr);
-			a.materials    = static_cast<const DeviceMaterial*>(f.materials.ptr);
-			a.leafMaterial = static_cast<const uint32_t*>(ctx->leafMaterial.ptr);
-			a.leafCount    = uint32_t(ctx->leafMaterial.bytes / 4);
-			a.capacity     = capacity;
-			a.error        = nullptr;
+			a.paths         = LP;
+			a.in            = L.Q[q];
+			a.out           = L.Q[nxt];
+			a.shadow        = L.S;
+			a.shadow.rays   = L.Q[nxt].rays + capacity;
+			a.hits          = L.hits;
+			a.materials     = static_cast<const DeviceMaterial*>(f.materials.ptr);
+			a.leafMaterial  = static_cast<const uint32_t*>(ctx->leafMaterial.ptr);
+			a.leafCount     = uint32_t(ctx->leafMaterial.bytes / 4);
+			a.capacity      = capacity;
+			a.error         = nullptr;
 			a.firstDistance = denoised ? static_cast<uint16_t*>(f.firstDistance.ptr) : nullptr;
 			a.firstNormal   = denoised ? static_cast<uint16_t*>(f.firstNormal.ptr) : nullptr;
 			a.firstAlbedo   = denoised ? static_cast<uint16_t*>(f.firstAlbedo.ptr) : nullptr;
 			a.firstLeaf     = denoised ? static_cast<uint32_t*>(f.firstLeaf.ptr) : nullptr;
-			if (!ctx->check(launchShade(a, stream, ctx->smCount), "shade kernel")) return KDN_CUDA_ERROR;
+			if (!ctx->check(launchShade(a, on, ctx->smCount), "shade kernel")) return KDN_CUDA_ERROR;
 			++launches;
-			cur = nxt;
+			q = nxt;
 		}
-		if (!ctx->check(launchFold(P, first, chunk, spp, static_cast<double*>(f.sums.ptr), denoised ? static_cast<float*>(f.frameLight.ptr) : nullptr, stream, ctx->smCount), "fold kernel")) return KDN_CUDA_ERROR;
+		if (!ctx->check(launchFold(LP, first, chunk, spp, static_cast<double*>(f.sums.ptr), denoised ? static_cast<float*>(f.frameLight.ptr) : nullptr, on, ctx->smCount), "fold kernel")) return KDN_CUDA_ERROR;
 		++launches;
 	}
+	// the first lane goes on once the second is done
+	if (!ctx->check(cudaEventRecord(f.joined[1], f.side), "event") || !ctx->check(cudaStreamWaitEvent(stream, f.joined[1], 0), "stream wait")) return KDN_CUDA_ERROR;
 	f.taken += double(spp);
 	f.last_denoised = denoised;
 	if (!denoised) f.shown = -1; // a frame without the shown chain drops the temporal history
