@@ -44,7 +44,8 @@ struct DeviceMaterial {
 	float coatFront, coatTwice, coatRoom;
 	uint32_t exact;   // a smooth glass answered exactly
 	uint32_t sharp;
-	uint32_t pad[2];
+	float glow[3];    // material.cpp:325 glowOf: the glow colour times its strength
+	uint32_t pad;
 	float escape[32]; // material/energy.h:12 Escape: the share a view keeps after one scatter
 };
 
@@ -58,7 +59,7 @@ struct FrameConstants {
 	uint32_t firstSample;
 	uint32_t lampCount;
 	uint32_t materialCount;
-	uint32_t pad;
+	uint32_t absorbs; // absorption.cpp:18 sceneAbsorbs: some glass absorbs
 	float zenith[3], horizon[3], ground[3];
 	DeviceLamp lamps[kMaxLamps];
 	SpectralTables spectral;

@@ -16,6 +16,10 @@
 
 namespace kdn {
 
+// Streams a frame's chunks go round (render lanes).
+constexpr int kLanes = 4;
+static_assert(kLanes >= 1 && kLanes <= 64, "a lane takes one of the context's 64 fetch counters");
+
 struct FrameState {
 	DeviceBuffer pixel, sample, throughput, radiance, nanometres, density, drawn, state, from;
 	DeviceBuffer queuePaths[2], queueRays[2], hits, states, counts;
@@ -37,8 +41,9 @@ struct FrameState {
 	bool last_denoised = false; // the last frame drawn was a denoised one
 	bool surfaced() const { return last_denoised && shown >= 0; }
 	std::vector<cudaEvent_t> events;
-	cudaStream_t side     = nullptr;              // the second lane's stream
-	cudaEvent_t joined[2] = { nullptr, nullptr }; // the lanes' start and end
+	cudaStream_t side[kLanes - 1] = {};   // the streams of the lanes after the first
+	cudaEvent_t started           = nullptr; // the first lane's work before the chunks
+	cudaEvent_t ended[kLanes - 1] = {};   // each other lane's end of the chunks
 	kdn_frame_stats stats {};
 };
 
@@ -51,12 +56,14 @@ void Context::releaseFrame() {
 		b->bytes = 0;
 	}
 	for (cudaEvent_t e : f.events) cudaEventDestroy(e);
-	for (cudaEvent_t e : f.joined) {
+	if (f.started) cudaEventDestroy(f.started);
+	for (cudaEvent_t e : f.ended) {
 		if (e) cudaEventDestroy(e);
 	}
-	if (f.side) {
-		cudaStreamSynchronize(f.side);
-		cudaStreamDestroy(f.side);
+	for (cudaStream_t side : f.side) {
+		if (side == nullptr) continue;
+		cudaStreamSynchronize(side);
+		cudaStreamDestroy(side);
 	}
 	delete frame;
 	frame = nullptr;
@@ -125,6 +132,7 @@ DeviceMaterial materialOf(const kdn_material& m, const kdn_finish& f) {
 	for (int c = 0; c < 3; ++c) {
 		d.albedo[c] = m.albedo[c];
 		d.absorb[c] = m.absorb[c];
+		d.glow[c]   = float(double(m.glow[c]) * double(m.strength));
 	}
 	d.roughness     = m.roughness;
 	d.index         = float(f.index);
@@ -146,8 +154,6 @@ DeviceMaterial materialOf(const kdn_material& m, const kdn_finish& f) {
 const char* unsupported(const kdn_material& m, const kdn_finish& f) {
 	if (m.kind > 3) return "a medium (scattering body)";
 	if (m.flags_ != 0) return "a patterned albedo";
-	if (m.glow[0] * m.strength > 0 || m.glow[1] * m.strength > 0 || m.glow[2] * m.strength > 0) return "a glowing surface";
-	if (m.absorb[0] != 0 || m.absorb[1] != 0 || m.absorb[2] != 0) return "an absorbing glass";
 	if (f.film[0] > 0) return "a thin film";
 	if (m.kind == 3 && !f.exact) return "a rough glass";
 	if (m.kind == 3 && m.refraction == 1.0f && m.dispersion == 0.0f) return "a passable glass";
@@ -160,6 +166,7 @@ const char* unsupported(const kdn_material& m, const kdn_finish& f) {
 
 using kdn::Context;
 using kdn::FrameState;
+using kdn::kLanes;
 
 namespace {
 
@@ -170,9 +177,6 @@ namespace {
 // and contributions.
 constexpr size_t kPathBytes = 4 * 4 + 5 * 16 + 2 * 4 + 2 * 2 * sizeof(kdn_ray) + sizeof(kdn_hit) + 2 * sizeof(kdn::HitState) + 4 + 16;
 static_assert(kPathBytes == 364, "path bytes");
-
-// Streams a frame's chunks go round (render lanes).
-constexpr int kLanes = 2;
 
 // The paths the lanes' chunks hold together: the whole frame where the
 // device has room for it (at most 2^28 paths, half the free memory), so
@@ -204,7 +208,7 @@ kdn_status ensureFrame(Context* ctx, uint32_t capacity) {
 		// a queue holds a bounce's path rays in [0, n) and the shadow lines of
 		// the bounce before in [n, 2n): one trace launch takes both
 		{ &f.queuePaths[0], n * 4 }, { &f.queuePaths[1], n * 4 }, { &f.queueRays[0], 2 * n * sizeof(kdn_ray) }, { &f.queueRays[1], 2 * n * sizeof(kdn_ray) },
-		{ &f.hits, n * sizeof(kdn_hit) }, { &f.states, 2 * n * sizeof(kdn::HitState) }, { &f.counts, 64 },
+		{ &f.hits, n * sizeof(kdn_hit) }, { &f.states, 2 * n * sizeof(kdn::HitState) }, { &f.counts, kLanes * 4 * sizeof(uint32_t) },
 		{ &f.shadowPaths, n * 4 }, { &f.shadowContribution, n * 16 },
 	};
 	for (const Want& w : wants) {
@@ -288,6 +292,9 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	c.firstSample   = fr->first;
 	c.lampCount     = uint32_t(lights.size());
 	c.materialCount = uint32_t(mats.size());
+	for (const kdn_material& m : mats) {
+		if (m.kind == 3 && (m.absorb[0] > 0 || m.absorb[1] > 0 || m.absorb[2] > 0)) c.absorbs = 1;
+	}
 	for (size_t k = 0; k < lights.size(); ++k) c.lamps[k] = lampOf(lights[k]);
 	if (!skies.empty()) {
 		put(c.zenith, v3(skies[0].zenith));
@@ -312,19 +319,19 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	P.drawn      = static_cast<float*>(f.drawn.ptr);
 	P.state      = static_cast<uint32_t*>(f.state.ptr);
 	P.from       = static_cast<float4*>(f.from.ptr);
-	// Lanes: the frame's chunks go round two streams, each lane with its own
+	// Lanes: the frame's chunks go round kLanes streams, each lane with its own
 	// share of the path buffers, queues and counters, so one chunk's work
 	// fills the SMs another chunk's launch leaves idle in its tail (the
 	// slowest rays of a trace launch).
 	uint32_t* counts = static_cast<uint32_t*>(f.counts.ptr); // a lane: [0],[1] ray queues, [2] lines, [3] zero
-	if (!ctx->check(cudaMemsetAsync(counts, 0, 64, stream), "clear counts")) return KDN_CUDA_ERROR;
-	if (f.side == nullptr && !ctx->check(cudaStreamCreateWithFlags(&f.side, cudaStreamNonBlocking), "cudaStreamCreate")) return KDN_CUDA_ERROR;
-	if (f.joined[0] == nullptr) {
-		for (cudaEvent_t& e : f.joined) {
-			if (!ctx->check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate")) return KDN_CUDA_ERROR;
-		}
+	if (!ctx->check(cudaMemsetAsync(counts, 0, kLanes * 4 * sizeof(uint32_t), stream), "clear counts")) return KDN_CUDA_ERROR;
+	cudaStream_t lanes[kLanes] = { stream };
+	for (int l = 1; l < kLanes; ++l) {
+		if (f.side[l - 1] == nullptr && !ctx->check(cudaStreamCreateWithFlags(&f.side[l - 1], cudaStreamNonBlocking), "cudaStreamCreate")) return KDN_CUDA_ERROR;
+		if (f.ended[l - 1] == nullptr && !ctx->check(cudaEventCreateWithFlags(&f.ended[l - 1], cudaEventDisableTiming), "cudaEventCreate")) return KDN_CUDA_ERROR;
+		lanes[l] = f.side[l - 1];
 	}
-	const cudaStream_t lanes[kLanes] = { stream, f.side };
+	if (f.started == nullptr && !ctx->check(cudaEventCreateWithFlags(&f.started, cudaEventDisableTiming), "cudaEventCreate")) return KDN_CUDA_ERROR;
 	struct Lane {
 		PathBuffers P;
 		QueueBuffers Q[2];
@@ -419,8 +426,11 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 			launches += 4;
 		}
 	}
-	// the second lane starts after what the first holds so far
-	if (!ctx->check(cudaEventRecord(f.joined[0], stream), "event") || !ctx->check(cudaStreamWaitEvent(f.side, f.joined[0], 0), "stream wait")) return KDN_CUDA_ERROR;
+	// the other lanes start after what the first holds so far
+	if (!ctx->check(cudaEventRecord(f.started, stream), "event")) return KDN_CUDA_ERROR;
+	for (int l = 1; l < kLanes; ++l) {
+		if (!ctx->check(cudaStreamWaitEvent(lanes[l], f.started, 0), "stream wait")) return KDN_CUDA_ERROR;
+	}
 	uint32_t chunkIndex = 0;
 	for (uint32_t first = 0; first < pixels; first += chunkPixels, ++chunkIndex) {
 		const int l              = int(chunkIndex % kLanes);
@@ -498,8 +508,10 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		if (!ctx->check(launchFold(LP, first, chunk, spp, static_cast<double*>(f.sums.ptr), denoised ? static_cast<float*>(f.frameLight.ptr) : nullptr, on, ctx->smCount), "fold kernel")) return KDN_CUDA_ERROR;
 		++launches;
 	}
-	// the first lane goes on once the second is done
-	if (!ctx->check(cudaEventRecord(f.joined[1], f.side), "event") || !ctx->check(cudaStreamWaitEvent(stream, f.joined[1], 0), "stream wait")) return KDN_CUDA_ERROR;
+	// the first lane goes on once the others are done
+	for (int l = 1; l < kLanes; ++l) {
+		if (!ctx->check(cudaEventRecord(f.ended[l - 1], lanes[l]), "event") || !ctx->check(cudaStreamWaitEvent(stream, f.ended[l - 1], 0), "stream wait")) return KDN_CUDA_ERROR;
+	}
 	f.taken += double(spp);
 	f.last_denoised = denoised;
 	if (!denoised) f.shown = -1; // a frame without the shown chain drops the temporal history

@@ -450,6 +450,19 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(ShadeArgs A) {
 			const float3 heading = make_float3(ray.direction[0], ray.direction[1], ray.direction[2]);
 			const float3 origin  = make_float3(ray.origin[0], ray.origin[1], ray.origin[2]);
 			const bool found     = hit.kind != 0;
+			// trace.cpp:179 keptOnLeg, absorption.cpp:28 keptThrough: what
+			// the leg's body keeps over a distance, exp(-absorption x
+			// distance) a lane; whole outside any body or where no glass absorbs
+			const bool absorbing = medium != kNoMaterial && cFrame.absorbs != 0;
+			float4 thickness     = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+			if (absorbing) {
+				const DeviceMaterial& body = A.materials[medium < cFrame.materialCount ? medium : 0u];
+				thickness                  = spectrumOf(body.absorb[0], body.absorb[1], body.absorb[2], nm);
+			}
+			const auto keptOver = [&](float distance) {
+				return absorbing ? make_float4(expf(-thickness.x * distance), expf(-thickness.y * distance), expf(-thickness.z * distance), expf(-thickness.w * distance))
+				                 : make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+			};
 			// meet: lamps along the leg (not for camera legs) and the sky past it
 			if (!camera) {
 				const float limit = found ? hit.distance : 3.0e38f;
@@ -463,7 +476,7 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(ShadeArgs A) {
 						const float pa = aimDensityOf(l, from, heading, reach);
 						w              = drawnDensity * drawnDensity / (drawnDensity * drawnDensity + pa * pa);
 					}
-					R = add4(R, scale4(mul4(T, spectrumOf(l.radiance[0], l.radiance[1], l.radiance[2], nm)), w));
+					R = add4(R, scale4(mul4(mul4(T, keptOver(reach)), spectrumOf(l.radiance[0], l.radiance[1], l.radiance[2], nm)), w));
 				}
 			}
 			// the record's first surface of the pixel's last sample
@@ -491,12 +504,29 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(ShadeArgs A) {
 			}
 			if (!found) {
 				const float3 sky = skyColour(heading);
-				R                = add4(R, mul4(T, spectrumOf(sky.x, sky.y, sky.z, nm)));
+				R                = add4(R, mul4(mul4(T, keptOver(__int_as_float(0x7f800000))), spectrumOf(sky.x, sky.y, sky.z, nm)));
 			} else {
 				const uint32_t material = hit.leaf < A.leafCount ? A.leafMaterial[hit.leaf] : 0u;
 				const DeviceMaterial& m = A.materials[material < cFrame.materialCount ? material : 0u];
 				const float3 point      = make_float3(hit.point[0], hit.point[1], hit.point[2]);
 				float3 normal           = make_float3(hit.normal[0], hit.normal[1], hit.normal[2]);
+				// trace.cpp:529 stoodOn: the leg's body keeps its share
+				if (absorbing) {
+					const float3 leg = point - origin;
+					T                = mul4(T, keptOver(sqrtf(dot3(leg, leg))));
+				}
+				// meet a glow (trace.cpp:415 metGlow): the glow bsdfAt gives
+				// where the ray arrives from outside, mixed across a blend
+				// seam; no sampler aims at it, so the meet takes it whole
+				if (dot3(normal, heading) < 0.0f) {
+					float3 glow = make_float3(m.glow[0], m.glow[1], m.glow[2]);
+					if (hit.other != kNoLeaf && hit.share > 0.0f) {
+						const DeviceMaterial& o = materialOfLeaf(hit.other, A.materials, A.leafMaterial, A.leafCount);
+						const float s           = hit.share;
+						glow = make_float3(glow.x * (1.0f - s) + o.glow[0] * s, glow.y * (1.0f - s) + o.glow[1] * s, glow.z * (1.0f - s) + o.glow[2] * s);
+					}
+					if (glow.x > 0.0f || glow.y > 0.0f || glow.z > 0.0f) R = add4(R, mul4(T, spectrumOf(glow.x, glow.y, glow.z, nm)));
+				}
 				if (dot3(normal, heading) >= 0.0f) normal = normal * -1.0f;
 				const float lift        = kBias + 2.0f * hit.loosened;
 				const uint32_t x        = A.paths.pixel[p] % uint32_t(cFrame.width);

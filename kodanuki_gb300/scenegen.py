@@ -210,6 +210,74 @@ def scene_room(seed: int = 1, width: int = 1920, height: int = 1080, samples: in
     return "".join(out)
 
 
+def scene_glow(seed: int = 1, width: int = 256, height: int = 256, samples: int = 16, surfaces: int = 8, count: int = 12) -> str:
+    """Glowing surfaces (a material's glow times its strength, seen where a
+    ray arrives from outside): config-1 primitives in one merge(0.05), a
+    third glowing dark mattes, a third glowing plastics, the rest plain
+    plastics, so blend seams mix glowing and plain leaves; one glowing
+    smooth glass sphere, whose inside hits see no glow; a dim quad light
+    and a dim grey sky."""
+    rng = random.Random(seed)
+    out = [_header(width, height, samples, surfaces, seed, [0.0, -8.5, 3.2], [0.0, 0.0, -0.6], 0.75)]
+    out.append(_sky([0.02, 0.02, 0.03]))
+    out.append(_quad([-1.25, 1.25, 4.5], [2.5, 0.0, 0.0], [0.0, -2.5, 0.0], blackbody_rgb(5000.0, 20.0)))
+    out.append("paint(plastic([0.5, 0.5, 0.5], roughness = 0.5)) plane([0, 0, 1], -2.2);\n\n")
+    out.append(f"paint(glass(refraction = 1.5, roughness = 0, glow = {_v([0.9, 0.4, 0.1])}, strength = 2)) at([0.4, -2.6, -1.4]) sphere(0.6);\n\n")
+    out.append("merge(0.05) {\n")
+    for k in range(count):
+        albedo = [rng.uniform(0.2, 0.8) for _ in range(3)]
+        glow = [rng.uniform(0.1, 1.0) for _ in range(3)]
+        strength = rng.uniform(1.0, 8.0)
+        pos = [rng.uniform(-2.0, 2.0) for _ in range(3)]
+        if k % 3 == 0:
+            mat = f"matte([0.05, 0.05, 0.05], glow = {_v(glow)}, strength = {_f(strength)})"
+        elif k % 3 == 1:
+            mat = f"plastic({_v(albedo)}, roughness = {_f(rng.uniform(0.05, 0.5))}, glow = {_v(glow)}, strength = {_f(strength)})"
+        else:
+            mat = f"plastic({_v(albedo)}, roughness = {_f(rng.uniform(0.05, 0.5))})"
+        if rng.random() < 0.5:
+            shape = f"sphere({_f(rng.uniform(0.2, 0.6))})"
+        else:
+            shape = f"box({_v([2 * rng.uniform(0.15, 0.45) for _ in range(3)])}, 0.02)"
+        out.append(f"\tpaint({mat}) at({_v(pos)}) {shape};\n")
+    out.append("}\n")
+    return "".join(out)
+
+
+def scene_glass(seed: int = 1, width: int = 256, height: int = 256, samples: int = 16, surfaces: int = 12, count: int = 8) -> str:
+    """Absorbing glass bodies (each leg inside keeps exp(-absorb x length)
+    a wavelength): ``count`` smooth glass spheres and rounded boxes,
+    absorb~U(0.1,2.5)^3, every other one dispersive, over a merge(0.05) of
+    plastic primitives on a ground plane; one quad light, a dim sky."""
+    rng = random.Random(seed)
+    out = [_header(width, height, samples, surfaces, seed, [0.0, -8.5, 3.2], [0.0, 0.0, -0.6], 0.75)]
+    out.append(_sky([0.08, 0.08, 0.1]))
+    out.append(_quad([-1.25, 1.25, 4.5], [2.5, 0.0, 0.0], [0.0, -2.5, 0.0], blackbody_rgb(5000.0, 60.0)))
+    out.append("paint(plastic([0.5, 0.5, 0.5], roughness = 0.5)) plane([0, 0, 1], -2.2);\n\n")
+    for k in range(count):
+        absorb = [rng.uniform(0.1, 2.5) for _ in range(3)]
+        pos = [rng.uniform(-2.0, 2.0), rng.uniform(-2.5, 0.5), rng.uniform(-1.8, 1.0)]
+        dispersion = ", dispersion = 0.01" if k % 2 else ""
+        mat = f"glass(refraction = 1.5{dispersion}, roughness = 0, absorb = {_v(absorb)})"
+        if rng.random() < 0.5:
+            shape = f"sphere({_f(rng.uniform(0.3, 0.7))})"
+        else:
+            shape = f"box({_v([2 * rng.uniform(0.2, 0.5) for _ in range(3)])}, 0.05)"
+        out.append(f"paint({mat}) at({_v(pos)}) {shape};\n")
+    out.append("\nmerge(0.05) {\n")
+    for _ in range(count):
+        albedo = [rng.uniform(0.2, 0.8) for _ in range(3)]
+        pos = [rng.uniform(-2.0, 2.0), rng.uniform(0.5, 2.5), rng.uniform(-1.8, 1.0)]
+        mat = f"plastic({_v(albedo)}, roughness = {_f(rng.uniform(0.05, 0.5))})"
+        if rng.random() < 0.5:
+            shape = f"sphere({_f(rng.uniform(0.2, 0.6))})"
+        else:
+            shape = f"box({_v([2 * rng.uniform(0.15, 0.45) for _ in range(3)])}, 0.02)"
+        out.append(f"\tpaint({mat}) at({_v(pos)}) {shape};\n")
+    out.append("}\n")
+    return "".join(out)
+
+
 def scene_serving(seed: int, count: int, width: int = 640, height: int = 480, samples: int = 4) -> str:
     """A config-1-style scene of ``count`` primitives spread over a box that
     grows with the count, split into merge(0.05) groups of 64."""

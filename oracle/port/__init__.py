@@ -149,7 +149,8 @@ class Material(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_uint32), ("exact", ctypes.c_uint32), ("albedo", ctypes.c_double * 3), ("index", ctypes.c_double),
                 ("dispersion", ctypes.c_double), ("width", ctypes.c_double), ("facet_share", ctypes.c_double), ("body", ctypes.c_double),
                 ("coat_front", ctypes.c_double), ("coat_twice", ctypes.c_double), ("coat_room", ctypes.c_double),
-                ("escape_average", ctypes.c_double), ("escape", ctypes.c_double * 32)]
+                ("escape_average", ctypes.c_double), ("escape", ctypes.c_double * 32), ("glow", ctypes.c_double * 3),
+                ("absorb", ctypes.c_double * 3)]
 
 
 class Lamp(ctypes.Structure):
@@ -188,6 +189,9 @@ def render_band(scene, width: int, height: int, spp: int, surfaces: int, seed: i
         mats[i].exact = int(m["finish_exact"][i]) if "finish_exact" in m else 0
         for c in range(3):
             mats[i].albedo[c] = float(m["albedo"][i][c])
+            # material.cpp:325 glowOf: glow x double(strength)
+            mats[i].glow[c] = float(m["glow"][i][c]) * float(np.float32(m["strength"][i])) if "glow" in m else 0.0
+            mats[i].absorb[c] = float(m["absorb"][i][c]) if "absorb" in m else 0.0
         mats[i].index = float(m["finish_index"][i]) if "finish_index" in m else 1.0
         mats[i].dispersion = float(m["dispersion"][i]) if int(m["kind"][i]) == 3 else 0.0
         if "finish_width" in m:

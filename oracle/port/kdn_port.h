@@ -121,6 +121,8 @@ typedef struct kp_material {
 	double index, dispersion, width, facet_share, body;
 	double coat_front, coat_twice, coat_room, escape_average;
 	double escape[32];
+	double glow[3];   /* material.cpp:325 glowOf: the glow colour times its strength */
+	double absorb[3]; /* absorption.cpp:28 keptThrough: the body's absorption a unit length */
 } kp_material;
 
 /* A lamp (light.cpp:78 lampOf): kind 2 sphere, 3 quad. */

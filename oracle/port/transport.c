@@ -10,6 +10,9 @@
  *   walkArrived (:1547)   meet the lamps along the leg and the sky past it,
  *                         weighted by the power heuristic (weight.cpp:27);
  *                         camera legs see only the sky (light.cpp:132);
+ *   stoodOn (:529)        the leg's absorbing body (absorption.cpp:28);
+ *   metGlow (:415)        a surface's glow where the ray arrives from
+ *                         outside, whole (the plain sampler aims at no glow);
  *   aimedFrom (:896)      offer every lamp, trace one offer drawn by its lane
  *                         mean (:830 offered); the aim takes the whole weight
  *                         at the surface cap (weight.cpp:107);
@@ -554,7 +557,20 @@ typedef struct job {
 	v3 eye, forward, right, up;
 	double reach, aspect;
 	uint64_t seed_mix;
+	int absorbs; /* absorption.cpp:18 sceneAbsorbs: some glass absorbs */
 } job;
+
+/* trace.cpp:179 keptOnLeg with absorption.cpp:28 keptThrough: what a leg of
+ * `distance` inside `medium` keeps, exp(-absorption x distance) a lane;
+ * whole outside any body or where no glass absorbs */
+static spec kept_along(const job* J, uint32_t medium, double distance, const lanes* w) {
+	if (medium == NO_MATERIAL || !J->absorbs) return flat(1);
+	const kp_material* m = &J->materials[medium < J->view->material_count ? medium : 0];
+	const spec depth = spectrum(m->absorb, w);
+	spec kept;
+	for (int k = 0; k < 4; ++k) kept.v[k] = exp(-depth.v[k] * distance);
+	return kept;
+}
 
 static kp_ray ray_of(v3 o, v3 d, double far, uint32_t medium) {
 	kp_ray r;
@@ -624,19 +640,34 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 					const double pa = aim_density(&J->lamps[k], from, heading, reach);
 					wgt = drawn * drawn / (drawn * drawn + pa * pa);
 				}
-				R = sadd(R, sscale(smul(T, spectrum(J->lamps[k].radiance, &w)), wgt));
+				R = sadd(R, sscale(smul(smul(T, kept_along(J, medium, reach, &w)), spectrum(J->lamps[k].radiance, &w)), wgt));
 			}
 		}
 		if (!found) {
 			double sky[3];
 			sky_colour(V, heading, sky);
-			R = sadd(R, smul(T, spectrum(sky, &w)));
+			R = sadd(R, smul(smul(T, kept_along(J, medium, INFINITY, &w)), spectrum(sky, &w)));
 			break;
 		}
 		const uint32_t material = hit.leaf != 0xFFFFFFFFu ? J->leaf_material[hit.leaf] : 0;
 		const kp_material* m = &J->materials[material < V->material_count ? material : 0];
 		const v3 point = mk(hit.point[0], hit.point[1], hit.point[2]);
 		v3 normal = mk(hit.normal[0], hit.normal[1], hit.normal[2]);
+		/* trace.cpp:529 stoodOn: the leg's body keeps its share */
+		T = smul(T, kept_along(J, medium, sqrt(dotv(sub(point, origin), sub(point, origin))), &w));
+		/* trace.cpp:415 metGlow at the vertex: the glow bsdfAt
+		 * (material.cpp:345) gives where the ray arrives from outside,
+		 * mixed across a blend seam; not aimed at by the plain sampler, so
+		 * the meet takes it whole (weight 1) */
+		if (dotv(normal, heading) < 0) {
+			double glow[3];
+			for (int c = 0; c < 3; ++c) glow[c] = m->glow[c];
+			if (hit.other != 0xFFFFFFFFu && hit.share > 0) {
+				const kp_material* o = material_of_leaf(J, hit.other);
+				for (int c = 0; c < 3; ++c) glow[c] = glow[c] * (1 - (double) hit.share) + o->glow[c] * (double) hit.share;
+			}
+			if (glow[0] > 0 || glow[1] > 0 || glow[2] > 0) R = sadd(R, smul(T, spectrum(glow, &w)));
+		}
 		if (dotv(normal, heading) >= 0) normal = scl(normal, -1);
 		const double lift = BIAS + 2 * 1e-6;
 		const int capped = depth + 1 >= V->surfaces;
@@ -760,6 +791,10 @@ void kp_render_band(const kp_octree* tree, const uint32_t* leaf_material, const 
 	J.reach = tan(view->fov / 2);
 	J.aspect = (double) view->width / (double) view->height;
 	J.seed_mix = kp_mixed_bits((uint64_t) (int64_t) view->seed);
+	for (uint32_t k = 0; k < view->material_count; ++k) {
+		const kp_material* m = &materials[k];
+		if (m->kind == 3 && (m->absorb[0] > 0 || m->absorb[1] > 0 || m->absorb[2] > 0)) J.absorbs = 1;
+	}
 	if (threads < 1) threads = 1;
 	pthread_t* pool = (pthread_t*) malloc(sizeof(pthread_t) * (size_t) threads);
 	for (int t = 0; t < threads; ++t) pthread_create(&pool[t], NULL, worker, &J);

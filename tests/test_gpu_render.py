@@ -48,7 +48,7 @@ def compare(a, b):
     return (np.abs(z) > 3).mean(), cz, ca.mean(0), cb.mean(0)
 
 
-@pytest.mark.parametrize("name", ["room_small", "c1_small", "c2_small"])
+@pytest.mark.parametrize("name", ["room_small", "c1_small", "c2_small", "glow_small", "glass_small"])
 def test_frame_matches_oracle_and_reference(backend, name):
     import oracle.port as op
     sc = scene(name)

@@ -71,3 +71,25 @@ def test_denoiser_matches_reference():
         out = op.denoise(int(d["width"]), int(d["height"]), int(f["demodulated"]), d["lens"], f["colour"], f["moment"], f["length"],
                          f["distance"], f["normal"], f["leaf"], f["albedo"])
         assert np.array_equal(out, f["out"]), name
+
+
+@pytest.mark.parametrize("name", ["room_small", "c1_small", "c2_small", "glow_small", "glass_small"])
+def test_renderer_matches_reference_frames(name):
+    """The oracle's frames against the reference renderer's own
+    (tests/golden/image_*.npz, 12 seeds at the scene's spp): both are
+    unbiased estimates of the same image, so each channel's image mean
+    agrees within 4 standard errors of the two seed sets, and at most 1.5%
+    of pixel channels are more than 3 standard errors apart."""
+    sc = scene(name)
+    ref = np.load(os.path.join(GOLDEN, f"image_{name}.npz"))
+    frames = ref["frames"].astype(np.float64)
+    spp = int(ref["spp"])
+    h, w = sc.render["height"], sc.render["width"]
+    build = dict(min_depth=5, max_depth=10, split_steps=64)
+    got = np.stack([op.render_band(sc, w, h, spp, int(sc.render["surfaces"]), s, 0, h, os.cpu_count() or 4, build) / spp for s in range(1, 9)])
+    z = (got.mean(0) - frames.mean(0)) / np.sqrt(got.var(0, ddof=1) / len(got) + frames.var(0, ddof=1) / len(frames) + 1e-12)
+    ca, cb = got.mean(axis=(1, 2)), frames.mean(axis=(1, 2))
+    cz = (ca.mean(0) - cb.mean(0)) / np.sqrt(ca.var(0, ddof=1) / len(ca) + cb.var(0, ddof=1) / len(cb))
+    print(f"{name}: oracle {ca.mean(0)} reference {cb.mean(0)} z {cz} far px {(np.abs(z) > 3).mean():.4f}")
+    assert np.all(np.abs(cz) < 4)
+    assert (np.abs(z) > 3).mean() <= 0.015
