@@ -85,9 +85,47 @@ typedef struct kdn_material {
 	float absorb[3];
 	float glow[3];
 	float strength;
-	uint32_t flags_;    /* 1: the albedo is a ramp read off a pattern program (not drawn by this build) */
+	uint32_t flags_;    /* 1: the albedo is a ramp read off a pattern program ("looks.patterns") */
 	uint32_t pad_;
 } kdn_material;
+
+/* plugins/transport/paths/material/energy.h Boundary of a glass, 9112
+ * bytes: what one bounce off a rough dielectric boundary returns, seen from
+ * the rarer and the denser side (17 index ratios from 1 to 3 by 32 views),
+ * their cosine-weighted averages and the share of the rarer side's loss
+ * that comes back on the far side.  Part of the reference's Finish
+ * (material.cpp:187 finishWith, boundaryOf); one per material in
+ * "transport.boundaries" (zeros for a material that is no glass). */
+typedef struct kdn_boundary {
+	double rarer[17][32];
+	double denser[17][32];
+	double rarer_average[17];
+	double denser_average[17];
+	double rarer_through[17];
+} kdn_boundary;
+
+/* sdf/scene.h Albedo of one material, 32 bytes: a ramp over a pattern
+ * program.  The program's steps are [first, first + count) of the
+ * "looks.pattern_steps" block (at most 64 steps; operands index steps of
+ * the same program, as sdf/program.h Step), its value is step `result`; an
+ * Argument step reads "looks.pattern_arguments"[argument_first + a] (the
+ * Scene::arguments the Albedo names); the ramp's stops are
+ * [stop_first, stop_first + stop_count) of "looks.stops" (3 floats a stop,
+ * spread evenly over 0..1); world: read in world space rather than the
+ * painted leaf's (its "looks.placements" entry).  count 0 for a flat colour. */
+typedef struct kdn_pattern {
+	uint32_t first, count, result;
+	uint32_t argument_first, argument_count;
+	uint32_t stop_first, stop_count;
+	uint32_t world;
+} kdn_pattern;
+
+/* sdf/scene.h Placement of one leaf, 96 bytes: the painted shape's space is
+ * linear x (p - origin) (material.cpp:292 placedVector). */
+typedef struct kdn_placement {
+	double linear[3][3];
+	double origin[3];
+} kdn_placement;
 
 /* plugins/transport/paths/material/material.h:70 Finish: how a material is
  * drawn, as the reference's transport derives it from the Material
@@ -221,6 +259,12 @@ kdn_status kdn_close(kdn_ctx* ctx);
  *   "lighting.sky"     kdn_sky, 72         one
  *   "shot.camera"      kdn_camera, 96      one
  *   "geometry.region"  kdn_region, 48      one
+ *   "looks.patterns"   kdn_pattern, 32     one per material, where any albedo is patterned
+ *   "looks.pattern_steps" kdn_step, 32     the pattern programs end to end (Scene::programs)
+ *   "looks.pattern_arguments" double, 8    the arguments they read (Scene::arguments)
+ *   "looks.stops"      float, 4            the ramps' stops, 3 floats a stop
+ *   "looks.placements" kdn_placement, 96   one per leaf (Leaf::placement)
+ *   "transport.boundaries" kdn_boundary, 9112 one per material, where a rough glass loses much
  * A block replaces the one of the same name; the world must be rebuilt
  * (kdn_build) after any scene.* or geometry.* block changes.
  */

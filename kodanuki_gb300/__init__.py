@@ -41,6 +41,11 @@ LIGHT_DTYPE = np.dtype([("kind", "<u4"), ("radius", "<f4"), ("angle", "<f4"), ("
 SKY_DTYPE = np.dtype([("zenith", "<f8", 3), ("horizon", "<f8", 3), ("ground", "<f8", 3)])
 CAMERA_DTYPE = np.dtype([("eye", "<f8", 3), ("target", "<f8", 3), ("up", "<f8", 3), ("fov", "<f8"), ("aperture", "<f8"), ("focus", "<f8")])
 REGION_DTYPE = np.dtype([("lower", "<f8", 3), ("size", "<f8", 3)])
+PATTERN_DTYPE = np.dtype([("first", "<u4"), ("count", "<u4"), ("result", "<u4"), ("argument_first", "<u4"), ("argument_count", "<u4"),
+                          ("stop_first", "<u4"), ("stop_count", "<u4"), ("world", "<u4")])
+PLACEMENT_DTYPE = np.dtype([("linear", "<f8", (3, 3)), ("origin", "<f8", 3)])
+BOUNDARY_DTYPE = np.dtype([("rarer", "<f8", (17, 32)), ("denser", "<f8", (17, 32)), ("rarer_average", "<f8", 17), ("denser_average", "<f8", 17),
+                           ("rarer_through", "<f8", 17)])
 FINISH_DTYPE = np.dtype([("kind", "<u4"), ("sharp", "<u4"), ("exact", "<u4"), ("loses_much", "<u4"), ("width", "<f8"), ("facet_share", "<f8"),
                          ("body", "<f8"), ("index", "<f8"), ("coat_front", "<f8"), ("coat_twice", "<f8"), ("coat_room", "<f8"),
                          ("escape_average", "<f8"), ("escape", "<f8", 32), ("film", "<f8", 2)])
@@ -202,6 +207,36 @@ def scene_blocks(scene: Scene) -> dict[str, np.ndarray]:
     }
     if finishes is not None:
         blocks["transport.finishes"] = finishes
+    if "finish_boundary" in m and np.any((np.asarray(m["kind"]) == 3) & (np.asarray(m["finish_exact"]) == 0)):
+        flat = np.ascontiguousarray(m["finish_boundary"], np.float64)
+        boundaries = np.zeros(len(flat), BOUNDARY_DTYPE)
+        boundaries["rarer"] = flat[:, :544].reshape(-1, 17, 32)
+        boundaries["denser"] = flat[:, 544:1088].reshape(-1, 17, 32)
+        boundaries["rarer_average"] = flat[:, 1088:1105]
+        boundaries["denser_average"] = flat[:, 1105:1122]
+        boundaries["rarer_through"] = flat[:, 1122:1139]
+        blocks["transport.boundaries"] = boundaries
+    pat = scene.patterns
+    if pat and np.any(np.asarray(m["patterned"]) != 0):
+        count = np.diff(pat["first"])
+        patterns = np.zeros(len(count), PATTERN_DTYPE)
+        patterns["first"] = pat["first"][:-1]
+        patterns["count"] = count
+        patterns["result"] = pat["result"]
+        patterns["argument_first"] = pat["argument_first"][:-1]
+        patterns["argument_count"] = np.diff(pat["argument_first"])
+        patterns["stop_first"] = pat["stop_first"][:-1]
+        patterns["stop_count"] = np.diff(pat["stop_first"])
+        patterns["world"] = pat["world"]
+        blocks["looks.patterns"] = patterns
+        blocks["looks.pattern_steps"] = np.ascontiguousarray(pat["steps"])
+        blocks["looks.pattern_arguments"] = np.ascontiguousarray(pat["arguments"], np.float64)
+        blocks["looks.stops"] = np.ascontiguousarray(pat["stops"], np.float32).reshape(-1)
+        if scene.leaf_placement is not None:
+            placements = np.zeros(len(scene.leaf_placement), PLACEMENT_DTYPE)
+            placements["linear"] = scene.leaf_placement[:, :9].reshape(-1, 3, 3)
+            placements["origin"] = scene.leaf_placement[:, 9:]
+            blocks["looks.placements"] = placements
     return blocks
 
 

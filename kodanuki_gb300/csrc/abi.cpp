@@ -29,7 +29,16 @@ const BlockSpec kBlocks[] = {
 	{ "lighting.sky", sizeof(kdn_sky), true },
 	{ "shot.camera", sizeof(kdn_camera), true },
 	{ "geometry.region", sizeof(kdn_region), true },
+	{ "looks.patterns", sizeof(kdn_pattern), false },
+	{ "looks.pattern_steps", sizeof(kdn_step), false },
+	{ "looks.pattern_arguments", sizeof(double), false },
+	{ "looks.stops", sizeof(float), false },
+	{ "looks.placements", sizeof(kdn_placement), false },
+	{ "transport.boundaries", sizeof(kdn_boundary), false },
 };
+static_assert(sizeof(kdn_boundary) == 9112, "kdn_boundary is 9112 bytes");
+static_assert(sizeof(kdn_pattern) == 32, "kdn_pattern is 32 bytes");
+static_assert(sizeof(kdn_placement) == 96, "kdn_placement is 96 bytes");
 
 static_assert(sizeof(kdn_step) == 32, "kdn_step is the reference's 32-byte Step");
 static_assert(sizeof(kdn_ray) == 36, "kdn_ray is the reference's 36-byte Ray");

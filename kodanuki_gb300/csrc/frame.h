@@ -45,8 +45,47 @@ struct DeviceMaterial {
 	uint32_t exact;   // a smooth glass answered exactly
 	uint32_t sharp;
 	float glow[3];    // material.cpp:325 glowOf: the glow colour times its strength
-	uint32_t pad;
+	uint32_t world;   // the pattern is read in world space (sdf/scene.h Albedo::world)
 	float escape[32]; // material/energy.h:12 Escape: the share a view keeps after one scatter
+	// sdf/scene.h Albedo as a ramp over a pattern program: its steps in the
+	// frame's pattern steps (count 0: the flat albedo) and its stops (3
+	// floats each) in the frame's stops
+	uint32_t patternFirst, patternCount, patternResult;
+	uint32_t stopFirst, stopCount;
+	// a rough glass: gives back what single scattering loses, read off its
+	// boundary tables (kBoundaryFloats floats at boundaryFirst of Looks::boundaries)
+	uint32_t losesMuch, boundaryFirst;
+	uint32_t pad;
+};
+
+// material/energy.h Boundary as floats: rarer and denser (17 ratios x 32
+// views each), then 17 rarer averages, 17 denser averages, 17 rarer-through
+// shares.
+constexpr int kBoundaryRatios = 17, kBoundaryViews = 32;
+constexpr int kBoundaryFloats = 2 * kBoundaryRatios * kBoundaryViews + 3 * kBoundaryRatios;
+
+// A step of a pattern program (sdf/program.h Step) on the device: operands
+// are steps of the same program (a pattern has at most kPatternSteps), an
+// argument is folded to the constant it reads.
+constexpr uint32_t kPatternSteps = 64;
+struct PatternStep {
+	uint8_t op;
+	uint8_t a, b, c;
+	float value;
+};
+
+// What the albedo at a hit reads (material.cpp:345 bsdfAt): the materials,
+// each leaf's material and placement (12 floats: linear row by row, then
+// origin), the pattern steps and the ramps' stops.
+struct Looks {
+	const DeviceMaterial* materials;
+	const uint32_t* leafMaterial;
+	uint32_t leafCount;
+	uint32_t placementCount;
+	const float* placements;
+	const PatternStep* patternSteps;
+	const float* stops;
+	const float* boundaries;
 };
 
 struct FrameConstants {
@@ -98,9 +137,7 @@ struct ShadeArgs {
 	QueueBuffers out;
 	ShadowBuffers shadow;
 	const kdn_hit* hits;
-	const DeviceMaterial* materials;
-	const uint32_t* leafMaterial;
-	uint32_t leafCount;
+	Looks looks;
 	uint32_t capacity;
 	uint32_t* error;
 	// where set (a denoised frame), the first surface of each pixel's last
@@ -116,9 +153,7 @@ struct ShadeArgs {
 struct SurfaceArgs {
 	QueueBuffers rays;    // paths[i] is the pixel of ray i
 	const kdn_hit* hits;
-	const DeviceMaterial* materials;
-	const uint32_t* leafMaterial;
-	uint32_t leafCount;
+	Looks looks;
 	uint16_t* distance;
 	uint16_t* normal;
 	uint16_t* albedo;

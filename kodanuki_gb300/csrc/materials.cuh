@@ -9,8 +9,13 @@
 //    (material.cpp:661 viewedPlastic, :440 plasticShare);
 //  - glass, smooth: exact mirror and passage by Fresnel, per lane where the
 //    glass disperses (Cauchy), the passage bent by the hero lane's index
-//    (material.cpp:1300 exactGlassScatter, feature/dispersion).
-// Rough glass, films, patterns and glowing surfaces are refused by the host.
+//    (material.cpp:1300 exactGlassScatter, feature/dispersion);
+//  - glass, rough: GGX facets mirrored or bent (Walter et al. 2007), per
+//    lane, plus the broad lobe that gives back what single scattering
+//    loses, read off the finish's boundary tables (material.cpp:884
+//    glassReflection, :986 glassPassage, :1328 glassScatter, energy.cpp:284
+//    lossAt, :317 boundaryAt).
+// Films are refused by the host.
 #pragma once
 
 #include "frame.h"
@@ -137,6 +142,9 @@ struct Shading {
 	float4 twice;    // metal: the colour light keeps over many bounces
 	float4 within, beyond; // glass: index on either side, per lane
 	bool parted;     // the lanes bend apart (a dispersing glass)
+	bool inside;     // glass: the vertex is seen from inside the body
+	float width;     // glass: GGX width of the facets
+	const float* boundary; // rough glass that loses much: its boundary tables
 };
 
 struct Response {
@@ -201,7 +209,8 @@ __device__ __forceinline__ float plasticShare(const DeviceMaterial& m, float lea
 }
 
 // rgb: the albedo at the hit (the material's, or mixed across a blend seam)
-__device__ __forceinline__ Shading surfaceOf(const DeviceMaterial& m, float3 rgb, float3 normal, float3 outgoing, float4 nm, uint32_t medium, const DeviceMaterial* all) {
+__device__ __forceinline__ Shading surfaceOf(const DeviceMaterial& m, float3 rgb, float3 normal, float3 outgoing, float4 nm, uint32_t medium, const DeviceMaterial* all,
+                                             const float* boundaries) {
 	Shading s;
 	s.kind    = m.kind;
 	s.normal  = normal;
@@ -215,6 +224,9 @@ __device__ __forceinline__ Shading surfaceOf(const DeviceMaterial& m, float3 rgb
 	s.within  = flat4(1.0f);
 	s.beyond  = flat4(1.0f);
 	s.parted  = false;
+	s.inside  = medium != kNoMaterial;
+	s.width   = m.width;
+	s.boundary = (m.kind == 3 && m.losesMuch && boundaries != nullptr) ? boundaries + size_t(m.boundaryFirst) * kBoundaryFloats : nullptr;
 	if (m.kind == 1 || m.kind == 2) {
 		s.left    = escapeAt(m.escape, s.leaving);
 		s.share   = m.kind == 2 ? m.facetShare : (s.leaving <= 0.0f ? 0.0f : plasticShare(m, s.leaving));
@@ -249,6 +261,169 @@ __device__ __forceinline__ float lostOf(const DeviceMaterial& m, float left, flo
 	return (1.0f - left) * (1.0f - came) / (kPiF * room);
 }
 
+// ---- rough glass ----
+struct TableRow {
+	int lower, upper;
+	float share;
+};
+
+// energy.cpp:255 rowOf: the place of the indices' ratio among the rows (1 to 3)
+__device__ __forceinline__ TableRow rowOf(float near, float far) {
+	const float ratio = fmaxf(near, far) / fminf(near, far);
+	const float place = (fminf(ratio, 3.0f) - 1.0f) / 2.0f * float(kBoundaryRatios - 1);
+	TableRow r;
+	r.lower = min(max(int(floorf(place)), 0), kBoundaryRatios - 1);
+	r.upper = min(r.lower + 1, kBoundaryRatios - 1);
+	r.share = fminf(fmaxf(place - float(r.lower), 0.0f), 1.0f);
+	return r;
+}
+
+__device__ __forceinline__ float blendedRow(const float* v, TableRow r) { return v[r.lower] * (1.0f - r.share) + v[r.upper] * r.share; }
+
+struct Loss {
+	float back, through, share;
+};
+
+// energy.cpp:284 lossAt (its back, through and share)
+__device__ Loss lossAt(const float* b, float near, float far) {
+	const TableRow row   = rowOf(near, far);
+	const float* tail    = b + 2 * kBoundaryRatios * kBoundaryViews;
+	const float rarer    = blendedRow(tail, row);
+	const float denser   = blendedRow(tail + kBoundaryRatios, row);
+	const float share    = blendedRow(tail + 2 * kBoundaryRatios, row);
+	const bool fromRarer = near <= far;
+	const float nearAvg  = fromRarer ? rarer : denser;
+	const float farAvg   = fromRarer ? denser : rarer;
+	Loss l { 0.0f, 0.0f, 0.0f };
+	const float nearLost = 1.0f - nearAvg, denserLost = 1.0f - denser;
+	if (!(nearLost > 1e-9f) || !(denserLost > 1e-9f)) return l;
+	const float turned = (far / near) * (far / near);
+	l.through          = fromRarer ? share / denserLost : share / denserLost * turned;
+	const float given  = fminf(l.through * (1.0f - farAvg), 1.0f);
+	l.back             = (1.0f - given) / nearLost;
+	l.share            = given;
+	return l;
+}
+
+// energy.cpp:309 rowAt, :317 boundaryAt, material.cpp:780 lossLeft
+__device__ __forceinline__ float rowAt(const float* table, int row, float cosine) {
+	const float place = fminf(fmaxf(cosine, 0.0f), 1.0f) * float(kBoundaryViews) - 0.5f;
+	const int lower   = min(max(int(floorf(place)), 0), kBoundaryViews - 1);
+	const int upper   = min(lower + 1, kBoundaryViews - 1);
+	const float share = fminf(fmaxf(place - float(lower), 0.0f), 1.0f);
+	return table[row * kBoundaryViews + lower] * (1.0f - share) + table[row * kBoundaryViews + upper] * share;
+}
+
+__device__ float lossLeft(const float* b, float near, float far, float cosine) {
+	const TableRow row  = rowOf(near, far);
+	const float* table  = near <= far ? b : b + kBoundaryRatios * kBoundaryViews;
+	const float reached = rowAt(table, row.lower, cosine) * (1.0f - row.share) + rowAt(table, row.upper, cosine) * row.share;
+	return fmaxf(1.0f - reached, 0.0f);
+}
+
+struct Broad {
+	float share, through;
+};
+
+// material.cpp:789 broadOf over the hero lane's indices
+__device__ __forceinline__ Broad broadOf(const Shading& s, float leaving) {
+	Broad w { 0.0f, 0.0f };
+	if (s.boundary != nullptr) {
+		w.share   = fminf(fmaxf(lossLeft(s.boundary, s.within.x, s.beyond.x, leaving), 0.0f), 1.0f);
+		w.through = lossAt(s.boundary, s.within.x, s.beyond.x).share;
+	}
+	return w;
+}
+
+// material.cpp:797 laneReflectance (no film), :814 laneReflectances, :821 reflectChance
+__device__ __forceinline__ float laneReflectance(const Shading& s, float cosine, int k) { return dielectricReflectance(cosine, lane4(s.within, k) / lane4(s.beyond, k)); }
+
+__device__ __forceinline__ float4 laneReflectances(const Shading& s, float cosine) {
+	if (!s.parted) return flat4(laneReflectance(s, cosine, 0));
+	return make_float4(laneReflectance(s, cosine, 0), laneReflectance(s, cosine, 1), laneReflectance(s, cosine, 2), laneReflectance(s, cosine, 3));
+}
+
+__device__ __forceinline__ float reflectChance(const Shading& s, float cosine) {
+	if (!s.parted) return laneReflectance(s, cosine, 0);
+	const float4 r = laneReflectances(s, cosine);
+	return 0.25f * (r.x + r.y + r.z + r.w);
+}
+
+// material.cpp:836 reflectanceAcross: from the denser side, Fresnel of the arriving cosine
+__device__ __forceinline__ float reflectanceAcross(const Shading& s, float leaving, float arriving, int k) {
+	const float within = lane4(s.within, k), beyond = lane4(s.beyond, k);
+	if (within <= beyond) return laneReflectance(s, leaving, k);
+	return dielectricReflectance(arriving, beyond / within);
+}
+
+// material.cpp:846 backLoss, :850 throughLoss, :859 givenBack
+__device__ float4 givenBack(const Shading& s, float leaving, float arriving, bool through) {
+	if (s.boundary == nullptr) return flat4(0.0f);
+	const int lanes = s.parted ? 4 : 1;
+	float g[4]      = { 0.0f, 0.0f, 0.0f, 0.0f };
+	for (int k = 0; k < lanes; ++k) {
+		const float near = lane4(s.within, k), far = lane4(s.beyond, k);
+		const Loss l     = lossAt(s.boundary, near, far);
+		g[k] = through ? l.through * lossLeft(s.boundary, near, far, leaving) * lossLeft(s.boundary, far, near, -arriving) / kPiF
+		               : l.back * lossLeft(s.boundary, near, far, leaving) * lossLeft(s.boundary, near, far, arriving) / kPiF;
+	}
+	return s.parted ? make_float4(g[0], g[1], g[2], g[3]) : flat4(g[0]);
+}
+
+// material.cpp:884 glassReflection
+__device__ Response glassReflection(const Shading& s, float3 outgoing, float3 incoming, float leaving, float arriving) {
+	const float3 facet  = halfwayOf(outgoing, incoming, s.normal);
+	const float onto    = dotF(outgoing, facet);
+	const float4 each   = laneReflectances(s, fmaxf(onto, 0.0f));
+	const float lobe    = onto > 0.0f ? facetDistribution(dotF(s.normal, facet), s.width) : 0.0f;
+	const float back    = s.parted ? 0.25f * (each.x + each.y + each.z + each.w) : each.x;
+	const float facets  = lobe * smithMasking(leaving, s.width) / (4.0f * leaving);
+	const Broad wide    = broadOf(s, leaving);
+	Response r;
+	r.value   = lin4(each, lobe * smithVisibility(leaving, arriving, s.width), givenBack(s, leaving, arriving, false), 1.0f);
+	r.density = (1.0f - wide.share) * back * facets + wide.share * (1.0f - wide.through) * arriving / kPiF;
+	return r;
+}
+
+// material.cpp:947 lanePassage over :925 bentFacet: what lane k sends
+// through the facet that bends the outgoing into the incoming direction,
+// and (lane 0) the density of drawing it
+__device__ void lanePassage(const Shading& s, float3 outgoing, float3 incoming, float leaving, float arriving, int k, float& sent, float& facets) {
+	sent = facets     = 0.0f;
+	const float near  = lane4(s.within, k), far = lane4(s.beyond, k);
+	const float3 sum  = addF(scaleF(outgoing, near), scaleF(incoming, far));
+	const float size  = sqrtf(dotF(sum, sum));
+	if (!(size > 1e-12f)) return;
+	const float3 facet = scaleF(sum, (dotF(sum, s.normal) < 0.0f ? -1.0f : 1.0f) / size);
+	const float into   = dotF(incoming, facet);
+	if (dotF(outgoing, facet) <= 0.0f || into >= 0.0f) return;
+	const float stretch = far * far * -into / (size * size);
+	if (stretch <= 0.0f) return;
+	const float onto = dotF(outgoing, facet);
+	const float lobe = facetDistribution(dotF(s.normal, facet), s.width) * onto * stretch;
+	const float kept = 1.0f - reflectanceAcross(s, onto, -into, k);
+	sent             = kept * lobe * 4.0f * smithVisibility(leaving, -arriving, s.width);
+	facets           = (1.0f - reflectChance(s, onto)) * lobe * smithMasking(leaving, s.width) / leaving;
+}
+
+// material.cpp:986 glassPassage
+__device__ Response glassPassage(const Shading& s, float3 outgoing, float3 incoming, float leaving, float arriving) {
+	const int lanes = s.parted ? 4 : 1;
+	float sent[4]   = { 0.0f, 0.0f, 0.0f, 0.0f };
+	float facets    = 0.0f;
+	for (int k = 0; k < lanes; ++k) {
+		float f;
+		lanePassage(s, outgoing, incoming, leaving, arriving, k, sent[k], f);
+		if (k == 0) facets = f;
+	}
+	const Broad wide = broadOf(s, leaving);
+	const float4 bent = s.parted ? make_float4(sent[0], sent[1], sent[2], sent[3]) : flat4(sent[0]);
+	Response r;
+	r.value   = lin4(bent, 1.0f, givenBack(s, leaving, arriving, true), 1.0f);
+	r.density = (1.0f - wide.share) * facets + wide.share * wide.through * -arriving / kPiF;
+	return r;
+}
+
 // The value and density of the BSDF for one pair of directions
 // (material.cpp:1076 respondBsdf / :710 roughViewedAnswer).
 __device__ __forceinline__ Response respond(const Shading& s, const DeviceMaterial& m, float3 outgoing, float3 incoming, float4 nm) {
@@ -260,9 +435,12 @@ __device__ __forceinline__ Response respond(const Shading& s, const DeviceMateri
 		if (s.leaving > 0.0f && arriving > 0.0f) r.value = lin4(s.albedo, 1.0f / kPiF, flat4(0.0f), 0.0f);
 		return r;
 	}
-	if (s.kind == 3) { // exact glass: nothing for a direction not drawn by it
+	if (s.kind == 3) {
+		// material.cpp:1002 glassResponse: exact glass answers no direction
+		// not drawn by it
 		r.density = 0.0f;
-		return r;
+		if (s.leaving <= 0.0f || m.exact) return r;
+		return arriving < 0.0f ? glassPassage(s, outgoing, incoming, s.leaving, arriving) : glassReflection(s, outgoing, incoming, s.leaving, arriving);
 	}
 	const float cosineDensity = fmaxf(arriving, 0.0f) / kPiF;
 	if (s.leaving <= 0.0f || arriving <= 0.0f) {
@@ -341,6 +519,49 @@ __device__ __forceinline__ Scatter sampleSurface(const Shading& s, const DeviceM
 		out.incoming = incoming;
 		out.density  = r.density;
 		out.weight   = lin4(r.value, fabsf(arriving) / r.density, flat4(0.0f), 0.0f);
+		return out;
+	}
+	if (!m.exact) {
+		// material.cpp:1328 glassScatter: the broad lobe (cosine about either
+		// side, :1236 broadChoice) or a visible facet, mirrored or bent by the
+		// hero lane (:1246 facetChoice)
+		const float leaving = s.leaving;
+		if (leaving <= 0.0f) return out;
+		const Broad wide = broadOf(s, leaving);
+		bool found = true, reflected;
+		float3 incoming;
+		if (lobe < wide.share) {
+			reflected          = side >= wide.through;
+			const Frame around = frameAround(reflected ? s.normal : scaleF(s.normal, -1.0f));
+			const float reach  = sqrtf(u);
+			const float angle  = 2.0f * kPiF * v;
+			const float height = sqrtf(fmaxf(1.0f - u, 0.0f));
+			incoming           = around.toWorld(make_float3(reach * cosf(angle), reach * sinf(angle), height));
+		} else {
+			const float3 facet = visibleFacet(s.frame, outgoing, s.width, u, v);
+			const float onto   = dotF(outgoing, facet);
+			if (onto <= 0.0f) return out;
+			reflected = side < reflectChance(s, onto);
+			if (reflected) {
+				incoming = mirrorOf(outgoing, facet);
+			} else {
+				const float ratio    = s.within.x / s.beyond.x;
+				const float leftover = 1.0f - ratio * ratio * (1.0f - onto * onto);
+				found                = leftover > 0.0f;
+				incoming             = found ? subF(scaleF(subF(scaleF(facet, onto), outgoing), ratio), scaleF(facet, sqrtf(leftover))) : make_float3(0.0f, 0.0f, 0.0f);
+			}
+		}
+		const float arriving = dotF(s.normal, incoming);
+		if (!found || (reflected ? arriving <= 0.0f : arriving >= 0.0f)) return out;
+		const Response r = reflected ? glassReflection(s, outgoing, incoming, leaving, arriving) : glassPassage(s, outgoing, incoming, leaving, arriving);
+		if (r.density <= 0.0f) return out;
+		out.found       = true;
+		out.incoming    = incoming;
+		out.density     = r.density;
+		out.weight      = lin4(r.value, fabsf(arriving) / r.density, flat4(0.0f), 0.0f);
+		out.through     = !reflected;
+		out.dispersed   = out.through && s.parted && s.within.x != s.beyond.x;
+		out.mediumAfter = out.through ? (medium != kNoMaterial ? kNoMaterial : material) : kNoMaterial;
 		return out;
 	}
 	// material.cpp:1300 exactGlassScatter

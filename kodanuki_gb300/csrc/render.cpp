@@ -25,6 +25,8 @@ struct FrameState {
 	DeviceBuffer queuePaths[2], queueRays[2], hits, states, counts;
 	DeviceBuffer shadowPaths, shadowContribution;
 	DeviceBuffer sums, out, materials;
+	DeviceBuffer patternSteps, stops, placements; // what patterned albedos read (Looks)
+	DeviceBuffer boundaries;                      // rough glasses' boundary tables (Looks)
 	// the shown frame (KDN_FRAME_DENOISE): the record of this frame (each
 	// pixel's light and the first surface of its last sample), and the
 	// G-buffer and the temporal state twice, this frame's and the one before
@@ -50,7 +52,7 @@ struct FrameState {
 void Context::releaseFrame() {
 	if (frame == nullptr) return;
 	FrameState& f = *frame;
-	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.hits, &f.states, &f.counts, &f.shadowPaths, &f.shadowContribution, &f.sums, &f.out, &f.materials, &f.frameLight, &f.firstDistance, &f.firstNormal, &f.firstAlbedo, &f.firstLeaf, &f.gDistance[0], &f.gDistance[1], &f.gNormal[0], &f.gNormal[1], &f.gAlbedo[0], &f.gAlbedo[1], &f.gLeaf[0], &f.gLeaf[1], &f.tColour[0], &f.tColour[1], &f.tMoment[0], &f.tMoment[1], &f.tLength[0], &f.tLength[1] }) {
+	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.hits, &f.states, &f.counts, &f.shadowPaths, &f.shadowContribution, &f.sums, &f.out, &f.materials, &f.patternSteps, &f.stops, &f.placements, &f.boundaries, &f.frameLight, &f.firstDistance, &f.firstNormal, &f.firstAlbedo, &f.firstLeaf, &f.gDistance[0], &f.gDistance[1], &f.gNormal[0], &f.gNormal[1], &f.gAlbedo[0], &f.gAlbedo[1], &f.gLeaf[0], &f.gLeaf[1], &f.tColour[0], &f.tColour[1], &f.tMoment[0], &f.tMoment[1], &f.tLength[0], &f.tLength[1] }) {
 		if (b->ptr) cudaFree(b->ptr);
 		b->ptr   = nullptr;
 		b->bytes = 0;
@@ -146,16 +148,85 @@ DeviceMaterial materialOf(const kdn_material& m, const kdn_finish& f) {
 	d.coatFront     = float(f.coat_front);
 	d.coatTwice     = float(f.coat_twice);
 	d.coatRoom      = float(f.coat_room);
+	d.losesMuch     = m.kind == 3 && !f.exact && f.loses_much ? 1u : 0u;
 	for (int k = 0; k < 32; ++k) d.escape[k] = float(f.escape[k]);
 	return d;
+}
+
+// sdf/scene.h Albedo as the device reads it: each patterned material's
+// program with its arguments folded in, its stops, and the leaves'
+// placements where a pattern is read in a painted leaf's space.
+struct PatternTables {
+	std::vector<PatternStep> steps;
+	std::vector<float> stops;
+	std::vector<float> placements;
+};
+
+kdn_status patternTables(Context* ctx, const std::vector<kdn_material>& mats, std::vector<DeviceMaterial>& dm, PatternTables& t) {
+	bool any = false;
+	for (const kdn_material& m : mats) any = any || (m.flags_ & 1u) != 0;
+	if (!any) return KDN_OK;
+	const std::vector<kdn_pattern> patterns = ctx->block<kdn_pattern>("looks.patterns");
+	if (patterns.size() != mats.size()) return ctx->fail(KDN_NOT_READY, "kdn_render: a patterned albedo needs the looks.patterns block, one pattern per material");
+	const std::vector<kdn_step> steps     = ctx->block<kdn_step>("looks.pattern_steps");
+	const std::vector<double> arguments   = ctx->block<double>("looks.pattern_arguments");
+	const std::vector<float> stops        = ctx->block<float>("looks.stops");
+	const std::vector<kdn_placement> placements = ctx->block<kdn_placement>("looks.placements");
+	bool local = false;
+	for (size_t k = 0; k < mats.size(); ++k) {
+		if ((mats[k].flags_ & 1u) == 0) continue;
+		const kdn_pattern& p   = patterns[k];
+		const std::string what = "kdn_render: the pattern of material " + std::to_string(k);
+		if (p.count == 0 || p.count > kPatternSteps) return ctx->fail(KDN_BAD_ARG, what + " has " + std::to_string(p.count) + " steps (1 to 64 are drawn)");
+		if (uint64_t(p.first) + p.count > steps.size() || p.result >= p.count) return ctx->fail(KDN_BAD_ARG, what + " lies outside looks.pattern_steps");
+		if (p.stop_count == 0 || (uint64_t(p.stop_first) + p.stop_count) * 3 > stops.size()) return ctx->fail(KDN_BAD_ARG, what + ": its stops lie outside looks.stops");
+		if (uint64_t(p.argument_first) + p.argument_count > arguments.size()) return ctx->fail(KDN_BAD_ARG, what + ": its arguments lie outside looks.pattern_arguments");
+		DeviceMaterial& d = dm[k];
+		d.patternFirst    = uint32_t(t.steps.size());
+		d.patternCount    = p.count;
+		d.patternResult   = p.result;
+		d.stopFirst       = uint32_t(t.stops.size() / 3);
+		d.stopCount       = p.stop_count;
+		d.world           = p.world ? 1u : 0u;
+		local             = local || !p.world;
+		for (uint32_t i = 0; i < p.count; ++i) {
+			const kdn_step& s = steps[size_t(p.first) + i];
+			if (s.opcode >= OpCount) return ctx->fail(KDN_BAD_ARG, what + ": step " + std::to_string(i) + " has an unknown opcode");
+			if (s.a >= p.count || s.b >= p.count || s.c >= p.count) return ctx->fail(KDN_BAD_ARG, what + ": step " + std::to_string(i) + " reads past the program");
+			PatternStep q {};
+			q.op    = s.opcode;
+			q.a     = uint8_t(s.a);
+			q.b     = uint8_t(s.b);
+			q.c     = uint8_t(s.c);
+			q.value = float(s.value);
+			if (s.opcode == OpArgument) {
+				// sdf/program.cpp runStep: Argument reads arguments[a]
+				if (s.a >= p.argument_count) return ctx->fail(KDN_BAD_ARG, what + ": step " + std::to_string(i) + " reads an argument past its own");
+				q.op    = OpConstant;
+				q.value = float(arguments[size_t(p.argument_first) + s.a]);
+			}
+			t.steps.push_back(q);
+		}
+		for (uint32_t i = 0; i < 3 * p.stop_count; ++i) t.stops.push_back(stops[3 * size_t(p.stop_first) + i]);
+	}
+	if (local) {
+		const size_t leaves = ctx->block<uint32_t>("scene.leaves").size();
+		if (placements.size() != leaves) return ctx->fail(KDN_NOT_READY, "kdn_render: a pattern read in a painted leaf's space needs the looks.placements block, one placement per leaf");
+		t.placements.reserve(placements.size() * 12);
+		for (const kdn_placement& pl : placements) {
+			for (int r = 0; r < 3; ++r) {
+				for (int c = 0; c < 3; ++c) t.placements.push_back(float(pl.linear[r][c]));
+			}
+			for (int c = 0; c < 3; ++c) t.placements.push_back(float(pl.origin[c]));
+		}
+	}
+	return KDN_OK;
 }
 
 // Why a material cannot be drawn by these kernels, or null.
 const char* unsupported(const kdn_material& m, const kdn_finish& f) {
 	if (m.kind > 3) return "a medium (scattering body)";
-	if (m.flags_ != 0) return "a patterned albedo";
 	if (f.film[0] > 0) return "a thin film";
-	if (m.kind == 3 && !f.exact) return "a rough glass";
 	if (m.kind == 3 && m.refraction == 1.0f && m.dispersion == 0.0f) return "a passable glass";
 	return nullptr;
 }
@@ -305,7 +376,42 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	if (!ctx->check(uploadFrameConstants(c, stream), "frame constants")) return KDN_CUDA_ERROR;
 	std::vector<DeviceMaterial> dm;
 	for (size_t k = 0; k < mats.size(); ++k) dm.push_back(materialOf(mats[k], finishes[k]));
+	// material/energy.h Boundary of each rough glass that loses much
+	std::vector<float> boundaryTables;
+	{
+		const std::vector<kdn_boundary> boundaries = ctx->block<kdn_boundary>("transport.boundaries");
+		for (size_t k = 0; k < dm.size(); ++k) {
+			if (!dm[k].losesMuch) continue;
+			if (boundaries.size() != mats.size()) return ctx->fail(KDN_NOT_READY, "kdn_render: a rough glass that loses much needs the transport.boundaries block, one boundary per material");
+			const kdn_boundary& b = boundaries[k];
+			dm[k].boundaryFirst   = uint32_t(boundaryTables.size() / kBoundaryFloats);
+			for (int r = 0; r < kBoundaryRatios; ++r) {
+				for (int v = 0; v < kBoundaryViews; ++v) boundaryTables.push_back(float(b.rarer[r][v]));
+			}
+			for (int r = 0; r < kBoundaryRatios; ++r) {
+				for (int v = 0; v < kBoundaryViews; ++v) boundaryTables.push_back(float(b.denser[r][v]));
+			}
+			for (int r = 0; r < kBoundaryRatios; ++r) boundaryTables.push_back(float(b.rarer_average[r]));
+			for (int r = 0; r < kBoundaryRatios; ++r) boundaryTables.push_back(float(b.denser_average[r]));
+			for (int r = 0; r < kBoundaryRatios; ++r) boundaryTables.push_back(float(b.rarer_through[r]));
+		}
+	}
+	if ((s = ctx->upload(f.boundaries, boundaryTables.data(), boundaryTables.size() * sizeof(float))) != KDN_OK) return s;
+	PatternTables tables;
+	if ((s = patternTables(ctx, mats, dm, tables)) != KDN_OK) return s;
 	if ((s = ctx->upload(f.materials, dm.data(), dm.size() * sizeof(DeviceMaterial))) != KDN_OK) return s;
+	if ((s = ctx->upload(f.patternSteps, tables.steps.data(), tables.steps.size() * sizeof(PatternStep))) != KDN_OK) return s;
+	if ((s = ctx->upload(f.stops, tables.stops.data(), tables.stops.size() * sizeof(float))) != KDN_OK) return s;
+	if ((s = ctx->upload(f.placements, tables.placements.data(), tables.placements.size() * sizeof(float))) != KDN_OK) return s;
+	Looks looks {};
+	looks.materials      = static_cast<const DeviceMaterial*>(f.materials.ptr);
+	looks.leafMaterial   = static_cast<const uint32_t*>(ctx->leafMaterial.ptr);
+	looks.leafCount      = uint32_t(ctx->leafMaterial.bytes / 4);
+	looks.placementCount = uint32_t(tables.placements.size() / 12);
+	looks.placements     = static_cast<const float*>(f.placements.ptr);
+	looks.patternSteps   = static_cast<const PatternStep*>(f.patternSteps.ptr);
+	looks.stops          = static_cast<const float*>(f.stops.ptr);
+	looks.boundaries     = static_cast<const float*>(f.boundaries.ptr);
 	if ((s = ctx->ensure(ctx->counters, 8 * sizeof(unsigned long long))) != KDN_OK) return s;
 	if (!ctx->check(cudaMemsetAsync(ctx->counters.ptr, 0, 8 * sizeof(unsigned long long), stream), "clear counters")) return KDN_CUDA_ERROR;
 
@@ -415,9 +521,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 			SurfaceArgs g;
 			g.rays         = L.Q[0];
 			g.hits         = h.hits;
-			g.materials    = static_cast<const DeviceMaterial*>(f.materials.ptr);
-			g.leafMaterial = static_cast<const uint32_t*>(ctx->leafMaterial.ptr);
-			g.leafCount    = uint32_t(ctx->leafMaterial.bytes / 4);
+			g.looks        = looks;
 			g.distance     = static_cast<uint16_t*>(f.gDistance[cur].ptr);
 			g.normal       = static_cast<uint16_t*>(f.gNormal[cur].ptr);
 			g.albedo       = static_cast<uint16_t*>(f.gAlbedo[cur].ptr);
@@ -492,9 +596,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 			a.shadow        = L.S;
 			a.shadow.rays   = L.Q[nxt].rays + capacity;
 			a.hits          = L.hits;
-			a.materials     = static_cast<const DeviceMaterial*>(f.materials.ptr);
-			a.leafMaterial  = static_cast<const uint32_t*>(ctx->leafMaterial.ptr);
-			a.leafCount     = uint32_t(ctx->leafMaterial.bytes / 4);
+			a.looks         = looks;
 			a.capacity      = capacity;
 			a.error         = nullptr;
 			a.firstDistance = denoised ? static_cast<uint16_t*>(f.firstDistance.ptr) : nullptr;

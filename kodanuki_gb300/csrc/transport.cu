@@ -16,6 +16,7 @@
 // reference carries them in double).
 #include "frame.h"
 #include "materials.cuh"
+#include "program.cuh"
 
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -357,20 +358,64 @@ __global__ void __launch_bounds__(kBlock) cameraKernel(PathBuffers P, QueueBuffe
 	}
 }
 
-// material.cpp:345 bsdfAt: the leaf's albedo, mixed with the other leaf's by
-// the hit's share where a blend joins two leaves.
-__device__ __forceinline__ const DeviceMaterial& materialOfLeaf(uint32_t leaf, const DeviceMaterial* materials, const uint32_t* leafMaterial, uint32_t leafCount) {
-	const uint32_t m = leaf < leafCount ? leafMaterial[leaf] : 0u;
-	return materials[m < cFrame.materialCount ? m : 0u];
+__device__ __forceinline__ const DeviceMaterial& materialOfLeaf(uint32_t leaf, const Looks& L) {
+	const uint32_t m = leaf < L.leafCount ? L.leafMaterial[leaf] : 0u;
+	return L.materials[m < cFrame.materialCount ? m : 0u];
 }
 
-__device__ __forceinline__ float3 albedoAt(const kdn_hit& hit, const DeviceMaterial* materials, const uint32_t* leafMaterial, uint32_t leafCount) {
-	const DeviceMaterial& m = materialOfLeaf(hit.leaf, materials, leafMaterial, leafCount);
-	float3 a                = make_float3(m.albedo[0], m.albedo[1], m.albedo[2]);
+// sdf/program.cpp evaluate over a pattern program's steps, with the point
+// and the normal as inputs (its arguments are folded to constants).
+__device__ float patternValue(const PatternStep* steps, uint32_t count, uint32_t result, const float p[3], const float n[3]) {
+	float r[kPatternSteps];
+	r[0] = 0.0f;
+	for (uint32_t i = 0; i < count && i < kPatternSteps; ++i) {
+		const PatternStep s = steps[i];
+		float v;
+		if (s.op == OpNormalX) v = n[0];
+		else if (s.op == OpNormalY) v = n[1];
+		else if (s.op == OpNormalZ) v = n[2];
+		else v = stepValue(s.op, r[s.a], r[s.b], r[s.c], s.value, p);
+		r[i] = v;
+	}
+	return r[result < kPatternSteps ? result : 0u];
+}
+
+// material.cpp:314 albedoAt over :299 patternAt and :281 rampAt: a flat
+// colour, or the ramp (its stops spread evenly over 0..1) at the pattern's
+// value at the point and the normal facing the ray, in the painted leaf's
+// space (material.cpp:292 placedVector) unless read in world space.
+__device__ float3 colourAt(const DeviceMaterial& m, uint32_t leaf, float3 point, float3 normal, const Looks& L) {
+	if (m.patternCount == 0) return make_float3(m.albedo[0], m.albedo[1], m.albedo[2]);
+	float3 p = point, n = normal;
+	if (!m.world && leaf < L.placementCount) {
+		const float* pl = L.placements + 12 * size_t(leaf);
+		const float3 d  = point - make_float3(pl[9], pl[10], pl[11]);
+		p               = make_float3(pl[0] * d.x + pl[1] * d.y + pl[2] * d.z, pl[3] * d.x + pl[4] * d.y + pl[5] * d.z, pl[6] * d.x + pl[7] * d.y + pl[8] * d.z);
+		const float3 t  = make_float3(pl[0] * normal.x + pl[1] * normal.y + pl[2] * normal.z, pl[3] * normal.x + pl[4] * normal.y + pl[5] * normal.z,
+		                              pl[6] * normal.x + pl[7] * normal.y + pl[8] * normal.z);
+		const float size = sqrtf(dot3(t, t));
+		n                = size > 0.0f ? t * (1.0f / size) : t;
+	}
+	const float pp[3] = { p.x, p.y, p.z }, nn[3] = { n.x, n.y, n.z };
+	const float value = patternValue(L.patternSteps + m.patternFirst, m.patternCount, m.patternResult, pp, nn);
+	const float* stops = L.stops + 3 * size_t(m.stopFirst);
+	if (m.stopCount <= 1) return make_float3(stops[0], stops[1], stops[2]);
+	const float place    = fminf(fmaxf(value, 0.0f), 1.0f) * float(m.stopCount - 1);
+	const uint32_t lower = min(uint32_t(place), m.stopCount - 2);
+	const float share    = place - float(lower);
+	const float* a       = stops + 3 * lower;
+	return make_float3(a[0] * (1.0f - share) + a[3] * share, a[1] * (1.0f - share) + a[4] * share, a[2] * (1.0f - share) + a[5] * share);
+}
+
+// material.cpp:345 bsdfAt: the leaf's albedo, mixed with the other leaf's by
+// the hit's share where a blend joins two leaves.
+__device__ __forceinline__ float3 albedoAt(const kdn_hit& hit, float3 normal, const Looks& L) {
+	const float3 point = make_float3(hit.point[0], hit.point[1], hit.point[2]);
+	float3 a           = colourAt(materialOfLeaf(hit.leaf, L), hit.leaf, point, normal, L);
 	if (hit.other != kNoLeaf && hit.share > 0.0f) {
-		const DeviceMaterial& o = materialOfLeaf(hit.other, materials, leafMaterial, leafCount);
-		const float s           = hit.share;
-		a = make_float3(a.x * (1.0f - s) + o.albedo[0] * s, a.y * (1.0f - s) + o.albedo[1] * s, a.z * (1.0f - s) + o.albedo[2] * s);
+		const float3 o = colourAt(materialOfLeaf(hit.other, L), hit.other, point, normal, L);
+		const float s  = hit.share;
+		a = make_float3(a.x * (1.0f - s) + o.x * s, a.y * (1.0f - s) + o.y * s, a.z * (1.0f - s) + o.z * s);
 	}
 	return a;
 }
@@ -408,7 +453,7 @@ __global__ void __launch_bounds__(kBlock) surfacesKernel(SurfaceArgs A) {
 			const float3 heading = make_float3(ray.direction[0], ray.direction[1], ray.direction[2]);
 			normal               = make_float3(hit.normal[0], hit.normal[1], hit.normal[2]);
 			if (dot3(normal, heading) >= 0.0f) normal = normal * -1.0f;
-			albedo = albedoAt(hit, A.materials, A.leafMaterial, A.leafCount);
+			albedo = albedoAt(hit, normal, A.looks);
 			const float dx = hit.point[0] - ray.origin[0], dy = hit.point[1] - ray.origin[1], dz = hit.point[2] - ray.origin[2];
 			distance       = sqrtf(dx * dx + dy * dy + dz * dz);
 		}
@@ -456,7 +501,7 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(ShadeArgs A) {
 			const bool absorbing = medium != kNoMaterial && cFrame.absorbs != 0;
 			float4 thickness     = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 			if (absorbing) {
-				const DeviceMaterial& body = A.materials[medium < cFrame.materialCount ? medium : 0u];
+				const DeviceMaterial& body = A.looks.materials[medium < cFrame.materialCount ? medium : 0u];
 				thickness                  = spectrumOf(body.absorb[0], body.absorb[1], body.absorb[2], nm);
 			}
 			const auto keptOver = [&](float distance) {
@@ -489,7 +534,7 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(ShadeArgs A) {
 				if (found) {
 					n = make_float3(hit.normal[0], hit.normal[1], hit.normal[2]);
 					if (dot3(n, heading) >= 0.0f) n = n * -1.0f;
-					albedo         = albedoAt(hit, A.materials, A.leafMaterial, A.leafCount);
+					albedo         = albedoAt(hit, n, A.looks);
 					const float3 d = make_float3(hit.point[0], hit.point[1], hit.point[2]) - origin;
 					distance       = sqrtf(dot3(d, d));
 				}
@@ -506,8 +551,8 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(ShadeArgs A) {
 				const float3 sky = skyColour(heading);
 				R                = add4(R, mul4(mul4(T, keptOver(__int_as_float(0x7f800000))), spectrumOf(sky.x, sky.y, sky.z, nm)));
 			} else {
-				const uint32_t material = hit.leaf < A.leafCount ? A.leafMaterial[hit.leaf] : 0u;
-				const DeviceMaterial& m = A.materials[material < cFrame.materialCount ? material : 0u];
+				const uint32_t material = hit.leaf < A.looks.leafCount ? A.looks.leafMaterial[hit.leaf] : 0u;
+				const DeviceMaterial& m = A.looks.materials[material < cFrame.materialCount ? material : 0u];
 				const float3 point      = make_float3(hit.point[0], hit.point[1], hit.point[2]);
 				float3 normal           = make_float3(hit.normal[0], hit.normal[1], hit.normal[2]);
 				// trace.cpp:529 stoodOn: the leg's body keeps its share
@@ -521,7 +566,7 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(ShadeArgs A) {
 				if (dot3(normal, heading) < 0.0f) {
 					float3 glow = make_float3(m.glow[0], m.glow[1], m.glow[2]);
 					if (hit.other != kNoLeaf && hit.share > 0.0f) {
-						const DeviceMaterial& o = materialOfLeaf(hit.other, A.materials, A.leafMaterial, A.leafCount);
+						const DeviceMaterial& o = materialOfLeaf(hit.other, A.looks);
 						const float s           = hit.share;
 						glow = make_float3(glow.x * (1.0f - s) + o.glow[0] * s, glow.y * (1.0f - s) + o.glow[1] * s, glow.z * (1.0f - s) + o.glow[2] * s);
 					}
@@ -535,10 +580,15 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(ShadeArgs A) {
 				const uint32_t index    = A.paths.sample[p];
 				const bool capped       = depth + 1 >= cFrame.surfaces;
 				const float3 outgoing   = heading * -1.0f;
-				const float3 rgb        = albedoAt(hit, A.materials, A.leafMaterial, A.leafCount);
-				const Shading surf      = surfaceOf(m, rgb, normal, outgoing, nm, medium, A.materials);
+				const float3 rgb        = albedoAt(hit, normal, A.looks);
+				const Shading surf      = surfaceOf(m, rgb, normal, outgoing, nm, medium, A.looks.materials, A.looks.boundaries);
+				// trace.cpp:583 aimable: from outside every body, or from inside
+				// the glass being crossed where it bends; trace.cpp:590
+				// openSide: the side a line leaves by
+				const bool aimable = medium == kNoMaterial || (medium == material && m.kind == 3 && surf.within.x != surf.beyond.x);
+				const float3 open  = surf.inside ? normal * -1.0f : normal;
 				// aim: offer every lamp, trace one offer drawn by its lane mean
-				if (!m.exact && cFrame.lampCount > 0) {
+				if (!m.exact && aimable && cFrame.lampCount > 0) {
 					const float u0   = number(stream, index, depth, LightU);
 					const float v0   = number(stream, index, depth, LightV);
 					float choice     = number(stream, index, depth, Pick);
@@ -549,7 +599,7 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(ShadeArgs A) {
 					for (uint32_t k = 0; k < cFrame.lampCount; ++k) {
 						const Aim a = aimLamp(cFrame.lamps[k], point, u0, v0);
 						if (!a.found) continue;
-						const float facing = dot3(normal, a.toward);
+						const float facing = dot3(open, a.toward);
 						if (facing <= 0.0f || a.distance <= 0.0f) continue;
 						const Response f = respond(surf, m, outgoing, a.toward, nm);
 						float w          = 1.0f;
@@ -575,7 +625,7 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(ShadeArgs A) {
 					if (picked > 0.0f) {
 						lined        = true;
 						lineRadiance = scale4(chosen, total / picked);
-						line         = makeRay(point + normal * lift, chosenDir, chosenDist - lift, kNoMaterial);
+						line         = makeRay(point + open * lift, chosenDir, chosenDist - lift, kNoMaterial);
 					}
 				}
 				// scatter (trace.cpp:1020 scatteredFrom)
@@ -599,12 +649,16 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(ShadeArgs A) {
 							else carried = scale4(carried, 1.0f / survival);
 						}
 						if (alive) {
+							// trace.cpp:956 aimedAlong: the next leg's meets are weighed
+							// against aiming where the scatter left by the open side of
+							// an aimable vertex
+							const bool aimed = !s.delta && s.density > 0.0f && s.through == (medium != kNoMaterial) && aimable;
 							if (s.through) medium = s.mediumAfter;
 							onward                = true;
 							T                     = carried;
 							const float off       = sideOf > 0.0f ? lift : -lift;
 							next                  = makeRay(point + normal * off, s.incoming, __int_as_float(0x7f800000), medium);
-							A.paths.drawn[p]      = s.delta ? 0.0f : s.density;
+							A.paths.drawn[p]      = aimed ? s.density : 0.0f;
 							A.paths.from[p]       = make_float4(point.x, point.y, point.z, 0.0f);
 							uint32_t stNext       = uint32_t(depth + 1) | (medium == kNoMaterial ? 0u : ((medium + 1u) << 16));
 							if (s.dispersed || ((st >> 9) & 1u)) stNext |= 1u << 9;

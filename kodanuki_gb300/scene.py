@@ -18,6 +18,11 @@ import numpy as np
 
 STEP_DTYPE = np.dtype([("opcode", "u1"), ("a", "<u4"), ("b", "<u4"), ("c", "<u4"), ("value", "<f8"), ("leaf", "<u4")], align=True)
 
+# material/energy.h Boundary: 17 index ratios x 32 views, twice, then three
+# rows of 17.
+BOUNDARY_RATIOS, ENERGY_VIEWS = 17, 32
+BOUNDARY_DOUBLES = 2 * BOUNDARY_RATIOS * ENERGY_VIEWS + 3 * BOUNDARY_RATIOS
+
 # sdf/scene.h MaterialKind and LightKind, in the reference's order.
 MATTE, PLASTIC, METAL, GLASS, MEDIUM = range(5)
 POINT, DIRECTIONAL, SPHERE, QUAD, SUN, MOON = range(6)
@@ -36,6 +41,14 @@ class Scene:
     render: dict
     region_lower: np.ndarray     # f64 [3]
     region_size: np.ndarray      # f64 [3]
+    # sdf/scene.h Placement of each leaf, f64 [L, 12]: linear row by row,
+    # then origin (what a pattern read in the painted shape's space uses)
+    leaf_placement: np.ndarray | None = None
+    # sdf/scene.h Albedo over the materials, end to end: the pattern
+    # programs' steps (first/result per material, count 0 for a flat
+    # colour), the arguments they read, the ramps' stops (3 floats a stop)
+    # and whether each is read in world space
+    patterns: dict = dataclasses.field(default_factory=dict)
 
     @property
     def program_count(self) -> int:
@@ -57,6 +70,10 @@ class Scene:
             arrays["material_" + k] = v
         for k, v in self.lights.items():
             arrays["light_" + k] = v
+        if self.leaf_placement is not None:
+            arrays["leaf_placement"] = self.leaf_placement
+        for k, v in self.patterns.items():
+            arrays["pattern_" + k] = v
         arrays["meta"] = np.frombuffer(json.dumps({"sky": self.sky, "camera": self.camera, "render": self.render}).encode(), np.uint8)
         np.savez_compressed(path, **arrays)
 
@@ -66,8 +83,10 @@ class Scene:
         meta = json.loads(bytes(z["meta"]).decode())
         mats = {k[len("material_"):]: z[k] for k in z.files if k.startswith("material_")}
         lights = {k[len("light_"):]: z[k] for k in z.files if k.startswith("light_")}
+        patterns = {k[len("pattern_"):]: z[k] for k in z.files if k.startswith("pattern_")}
+        placement = z["leaf_placement"] if "leaf_placement" in z.files else None
         return Scene(z["steps"], z["program_first"], z["program_result"], z["leaf_material"], mats, lights,
-                     meta["sky"], meta["camera"], meta["render"], z["region_lower"], z["region_size"])
+                     meta["sky"], meta["camera"], meta["render"], z["region_lower"], z["region_size"], placement, patterns)
 
     @staticmethod
     def from_reference_json(d: dict) -> "Scene":
@@ -113,7 +132,34 @@ class Scene:
                 "finish_escape_average": np.array([f["escapeAverage"] for f in fs], np.float64),
                 "finish_escape": np.array([f["escape"] for f in fs], np.float64).reshape(-1, 32),
                 "finish_film": np.array([f["film"] for f in fs], np.float64).reshape(-1, 2),
+                # material/energy.h Boundary of each glass (zeros elsewhere):
+                # rarer and denser (17 ratios x 32 views each), then the
+                # rarer and denser averages and the rarer-through shares
+                "finish_boundary": np.array([f.get("boundary", [0.0] * BOUNDARY_DOUBLES) for f in fs], np.float64).reshape(-1, BOUNDARY_DOUBLES),
             })
+        # the patterns (ref_dump.cpp writes them with each material)
+        pat_rows, pat_first, pat_result, args, arg_first, stops, stop_first = [], [0], [], [], [0], [], [0]
+        for m in ms:
+            for srow in m.get("patternSteps", []):
+                pat_rows.append(tuple(srow))
+            pat_first.append(len(pat_rows))
+            pat_result.append(m.get("patternResult", 0))
+            args.extend(m.get("patternArguments", []))
+            arg_first.append(len(args))
+            stops.extend(m["stops"])
+            stop_first.append(len(stops) // 3)
+        pat_steps = np.zeros(len(pat_rows), STEP_DTYPE)
+        if pat_rows:
+            arr = np.array(pat_rows, dtype=object)
+            for i, k in enumerate(("opcode", "a", "b", "c", "value", "leaf")):
+                pat_steps[k] = arr[:, i].astype(pat_steps.dtype[k])
+        patterns = {
+            "steps": pat_steps, "first": np.array(pat_first, np.uint32), "result": np.array(pat_result, np.uint32),
+            "arguments": np.array(args, np.float64), "argument_first": np.array(arg_first, np.uint32),
+            "stops": np.array(stops, np.float32).reshape(-1, 3), "stop_first": np.array(stop_first, np.uint32),
+            "world": np.array([m.get("world", 0) for m in ms], np.uint8),
+        }
+        placement = np.array(d["placements"], np.float64).reshape(-1, 12) if "placements" in d else None
         ls = d["lights"]
         lights = {
             "kind": np.array([l["kind"] for l in ls], np.uint8),
@@ -127,4 +173,4 @@ class Scene:
         }
         return Scene(steps, np.array(first, np.uint32), np.array(result, np.uint32), np.array(d["leaves"], np.uint32),
                      mats, lights, d["sky"], d["camera"], d["render"],
-                     np.array(d["region"]["lower"], np.float64), np.array(d["region"]["size"], np.float64))
+                     np.array(d["region"]["lower"], np.float64), np.array(d["region"]["size"], np.float64), placement, patterns)

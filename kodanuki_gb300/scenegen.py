@@ -244,11 +244,13 @@ def scene_glow(seed: int = 1, width: int = 256, height: int = 256, samples: int 
     return "".join(out)
 
 
-def scene_glass(seed: int = 1, width: int = 256, height: int = 256, samples: int = 16, surfaces: int = 12, count: int = 8) -> str:
+def scene_glass(seed: int = 1, width: int = 256, height: int = 256, samples: int = 16, surfaces: int = 12, count: int = 8, rough: bool = False) -> str:
     """Absorbing glass bodies (each leg inside keeps exp(-absorb x length)
-    a wavelength): ``count`` smooth glass spheres and rounded boxes,
+    a wavelength): ``count`` glass spheres and rounded boxes,
     absorb~U(0.1,2.5)^3, every other one dispersive, over a merge(0.05) of
-    plastic primitives on a ground plane; one quad light, a dim sky."""
+    plastic primitives on a ground plane; one quad light, a dim sky.  The
+    glass is smooth, or with ``rough`` of roughness U(0.05, 0.5) for all
+    but every fourth body."""
     rng = random.Random(seed)
     out = [_header(width, height, samples, surfaces, seed, [0.0, -8.5, 3.2], [0.0, 0.0, -0.6], 0.75)]
     out.append(_sky([0.08, 0.08, 0.1]))
@@ -258,7 +260,8 @@ def scene_glass(seed: int = 1, width: int = 256, height: int = 256, samples: int
         absorb = [rng.uniform(0.1, 2.5) for _ in range(3)]
         pos = [rng.uniform(-2.0, 2.0), rng.uniform(-2.5, 0.5), rng.uniform(-1.8, 1.0)]
         dispersion = ", dispersion = 0.01" if k % 2 else ""
-        mat = f"glass(refraction = 1.5{dispersion}, roughness = 0, absorb = {_v(absorb)})"
+        roughness = _f(rng.uniform(0.05, 0.5)) if rough and k % 4 else "0"
+        mat = f"glass(refraction = 1.5{dispersion}, roughness = {roughness}, absorb = {_v(absorb)})"
         if rng.random() < 0.5:
             shape = f"sphere({_f(rng.uniform(0.3, 0.7))})"
         else:
@@ -274,6 +277,51 @@ def scene_glass(seed: int = 1, width: int = 256, height: int = 256, samples: int
         else:
             shape = f"box({_v([2 * rng.uniform(0.15, 0.45) for _ in range(3)])}, 0.02)"
         out.append(f"\tpaint({mat}) at({_v(pos)}) {shape};\n")
+    out.append("}\n")
+    return "".join(out)
+
+
+_PATTERNS = """function bands(count) {
+	return 0.5 + 0.5 * sin(p.z * count);
+}
+
+function cells(size) {
+	let c = floor(p.x * size) + floor(p.y * size) + floor(p.z * size);
+	return c - 2 * floor(c / 2);
+}
+
+function facing(axis) {
+	return clamp(dot(n, axis) * 0.5 + 0.5, 0, 1);
+}
+"""
+
+
+def scene_patterns(seed: int = 1, width: int = 256, height: int = 256, samples: int = 16, surfaces: int = 8, count: int = 12) -> str:
+    """Patterned albedos (a ramp of 2-4 colour stops read off a pattern
+    program of the point and the normal): a world-space cell pattern on the
+    ground, and config-1 primitives in one merge(0.05), some turned, painted
+    with bands (sine of height), cells (a 3-D checker) or facing (the
+    normal against an axis) in the painted shape's space, or plain, so
+    blend seams mix patterned and plain leaves; one quad light."""
+    rng = random.Random(seed)
+    out = [_header(width, height, samples, surfaces, seed, [0.0, -8.5, 3.2], [0.0, 0.0, -0.6], 0.75).replace(_SHAPES, _SHAPES + "\n" + _PATTERNS)]
+    out.append(_sky([0.05, 0.05, 0.06]))
+    out.append(_quad([-1.25, 1.25, 4.5], [2.5, 0.0, 0.0], [0.0, -2.5, 0.0], blackbody_rgb(5000.0, 60.0)))
+    out.append("paint(matte(world(ramp(cells(1), [0.25, 0.25, 0.25], [0.7, 0.7, 0.7])))) plane([0, 0, 1], -2.2);\n\n")
+    out.append("merge(0.05) {\n")
+    for k in range(count):
+        stops = ", ".join(_v([rng.uniform(0.1, 0.9) for _ in range(3)]) for _ in range(2 + k % 3))
+        pos = [rng.uniform(-2.0, 2.0) for _ in range(3)]
+        pattern = [f"bands({_f(rng.uniform(4.0, 12.0))})", f"cells({_f(rng.uniform(2.0, 6.0))})",
+                   f"facing({_v([rng.uniform(-1.0, 1.0) for _ in range(3)])})", None][k % 4]
+        albedo = f"ramp({pattern}, {stops})" if pattern else _v([rng.uniform(0.2, 0.8) for _ in range(3)])
+        mat = f"matte({albedo})" if k % 2 == 0 else f"plastic({albedo}, roughness = {_f(rng.uniform(0.1, 0.5))})"
+        turn = f" turn(z, {_f(rng.uniform(0.0, 3.0))})" if k % 3 == 0 else ""
+        if rng.random() < 0.5:
+            shape = f"sphere({_f(rng.uniform(0.25, 0.6))})"
+        else:
+            shape = f"box({_v([2 * rng.uniform(0.15, 0.45) for _ in range(3)])}, 0.02)"
+        out.append(f"\tpaint({mat}) at({_v(pos)}){turn} {shape};\n")
     out.append("}\n")
     return "".join(out)
 

@@ -150,7 +150,61 @@ class Material(ctypes.Structure):
                 ("dispersion", ctypes.c_double), ("width", ctypes.c_double), ("facet_share", ctypes.c_double), ("body", ctypes.c_double),
                 ("coat_front", ctypes.c_double), ("coat_twice", ctypes.c_double), ("coat_room", ctypes.c_double),
                 ("escape_average", ctypes.c_double), ("escape", ctypes.c_double * 32), ("glow", ctypes.c_double * 3),
-                ("absorb", ctypes.c_double * 3)]
+                ("absorb", ctypes.c_double * 3), ("pattern", Program), ("pattern_arguments", ctypes.c_void_p),
+                ("stops", ctypes.c_void_p), ("stop_count", ctypes.c_uint32), ("world", ctypes.c_uint32),
+                ("loses_much", ctypes.c_uint32), ("boundary", ctypes.c_void_p)]
+
+
+def _materials(scene):
+    """The scene's materials as a C array of kp_material, with the arrays
+    their patterns point into (kept alive by the caller)."""
+    m = scene.materials
+    n = len(m["kind"])
+    mats = (Material * n)()
+    keep = []
+    pat = scene.patterns
+    for i in range(n):
+        mats[i].kind = int(m["kind"][i])
+        mats[i].exact = int(m["finish_exact"][i]) if "finish_exact" in m else 0
+        for c in range(3):
+            mats[i].albedo[c] = float(m["albedo"][i][c])
+            # material.cpp:325 glowOf: glow x double(strength)
+            mats[i].glow[c] = float(m["glow"][i][c]) * float(np.float32(m["strength"][i])) if "glow" in m else 0.0
+            mats[i].absorb[c] = float(m["absorb"][i][c]) if "absorb" in m else 0.0
+        mats[i].index = float(m["finish_index"][i]) if "finish_index" in m else 1.0
+        mats[i].dispersion = float(m["dispersion"][i]) if int(m["kind"][i]) == 3 else 0.0
+        if "finish_width" in m:
+            mats[i].width = float(m["finish_width"][i])
+            mats[i].facet_share = float(m["finish_facet_share"][i])
+            mats[i].body = float(m["finish_body"][i])
+            mats[i].coat_front, mats[i].coat_twice, mats[i].coat_room = (float(x) for x in m["finish_coating"][i])
+            mats[i].escape_average = float(m["finish_escape_average"][i])
+            for k in range(32):
+                mats[i].escape[k] = float(m["finish_escape"][i][k])
+        if "finish_boundary" in m and int(m["kind"][i]) == 3:
+            boundary = np.ascontiguousarray(m["finish_boundary"][i], np.float64)
+            keep.append(boundary)
+            mats[i].boundary = boundary.ctypes.data
+            mats[i].loses_much = int(m["finish_loses_much"][i])
+        if pat and int(pat["first"][i + 1]) > int(pat["first"][i]):
+            steps = np.ascontiguousarray(pat["steps"][pat["first"][i]:pat["first"][i + 1]])
+            args = np.ascontiguousarray(pat["arguments"][pat["argument_first"][i]:pat["argument_first"][i + 1]], np.float64)
+            stops = np.ascontiguousarray(pat["stops"][pat["stop_first"][i]:pat["stop_first"][i + 1]], np.float64)
+            keep += [steps, args, stops]
+            mats[i].pattern.steps = steps.ctypes.data
+            mats[i].pattern.count = len(steps)
+            mats[i].pattern.result = int(pat["result"][i])
+            mats[i].pattern_arguments = args.ctypes.data if len(args) else None
+            mats[i].stops = stops.ctypes.data
+            mats[i].stop_count = len(stops)
+            mats[i].world = int(pat["world"][i])
+    return mats, keep
+
+
+def _placements(scene):
+    if scene.leaf_placement is None:
+        return None
+    return np.ascontiguousarray(scene.leaf_placement, np.float64)
 
 
 class Lamp(ctypes.Structure):
@@ -181,27 +235,8 @@ def render_band(scene, width: int, height: int, spp: int, surfaces: int, seed: i
     RGB per pixel (rows x width x 3, divide by spp for the means)."""
     build = build or dict(min_depth=6, max_depth=10, split_steps=96)
     tree = _octree_for(scene, build)
-    m = scene.materials
-    n = len(m["kind"])
-    mats = (Material * n)()
-    for i in range(n):
-        mats[i].kind = int(m["kind"][i])
-        mats[i].exact = int(m["finish_exact"][i]) if "finish_exact" in m else 0
-        for c in range(3):
-            mats[i].albedo[c] = float(m["albedo"][i][c])
-            # material.cpp:325 glowOf: glow x double(strength)
-            mats[i].glow[c] = float(m["glow"][i][c]) * float(np.float32(m["strength"][i])) if "glow" in m else 0.0
-            mats[i].absorb[c] = float(m["absorb"][i][c]) if "absorb" in m else 0.0
-        mats[i].index = float(m["finish_index"][i]) if "finish_index" in m else 1.0
-        mats[i].dispersion = float(m["dispersion"][i]) if int(m["kind"][i]) == 3 else 0.0
-        if "finish_width" in m:
-            mats[i].width = float(m["finish_width"][i])
-            mats[i].facet_share = float(m["finish_facet_share"][i])
-            mats[i].body = float(m["finish_body"][i])
-            mats[i].coat_front, mats[i].coat_twice, mats[i].coat_room = (float(x) for x in m["finish_coating"][i])
-            mats[i].escape_average = float(m["finish_escape_average"][i])
-            for k in range(32):
-                mats[i].escape[k] = float(m["finish_escape"][i][k])
+    mats, keep = _materials(scene)
+    n = len(mats)
     l = scene.lights
     nl = len(l["kind"])
     lamps = (Lamp * max(nl, 1))()
@@ -227,8 +262,11 @@ def render_band(scene, width: int, height: int, spp: int, surfaces: int, seed: i
     sums = np.zeros((rows, width, 3), np.float64)
     mat_leaf = np.ascontiguousarray(scene.leaf_material, np.uint32)
     L = lib()
-    L.kp_render_band.argtypes = [_P, _P, _P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]
-    L.kp_render_band(tree.handle, _ptr(mat_leaf), ctypes.addressof(mats), ctypes.addressof(lamps), ctypes.byref(v), row0, rows, threads, _ptr(sums))
+    placements = _placements(scene)
+    L.kp_render_band.argtypes = [_P, _P, _P, _P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]
+    L.kp_render_band(tree.handle, _ptr(mat_leaf), ctypes.addressof(mats), ctypes.addressof(lamps), ctypes.byref(v),
+                     _ptr(placements) if placements is not None else None, row0, rows, threads, _ptr(sums))
+    del keep
     return sums
 
 
@@ -275,25 +313,34 @@ def traced_surfaces(scene, width: int, height: int, build: dict | None = None, l
     facing = (normal * rays["direction"].astype(np.float64)).sum(1) >= 0
     normal[facing] *= -1
     normal[~found] = 0
-    albedo_of = np.asarray(scene.materials["albedo"], np.float64)
-    leaf_material = np.asarray(scene.leaf_material, np.int64)
-    material_count = len(albedo_of)
-
-    def material(leaf):
-        m = np.where(leaf != 0xFFFFFFFF, leaf_material[np.where(leaf != 0xFFFFFFFF, leaf, 0)], 0)
-        return np.where(m < material_count, m, 0)
-
-    albedo = albedo_of[material(hits["leaf"].astype(np.int64))]
-    share = hits["share"].astype(np.float64)
-    mixed = (hits["other"] != 0xFFFFFFFF) & (share > 0)
-    other = albedo_of[material(hits["other"].astype(np.int64))]
-    albedo = np.where(mixed[:, None], albedo * (1 - share[:, None]) + other * share[:, None], albedo)
+    albedo = albedos(scene, hits["leaf"], hits["other"], hits["share"], hits["point"], normal)
     albedo[~found] = 0
     delta = hits["point"].astype(np.float32) - rays["origin"]
     distance = np.sqrt((delta * delta).sum(1, dtype=np.float32)).astype(np.float32)
     distance[~found] = np.inf
     leaf = np.where(found, hits["leaf"], 0xFFFFFFFF).astype(np.uint32)
     return {"distance": distance, "normal": normal, "albedo": albedo, "leaf": leaf}
+
+
+def albedos(scene, leaf, other, share, point, normal) -> np.ndarray:
+    """material.cpp:345 bsdfAt's albedo at n hits (the normal facing the
+    ray): the material's colour or its ramp over its pattern program, mixed
+    across a blend seam (n x 3, double)."""
+    mats, keep = _materials(scene)
+    placements = _placements(scene)
+    leaf_material = np.ascontiguousarray(scene.leaf_material, np.uint32)
+    leaf = np.ascontiguousarray(leaf, np.uint32)
+    other = np.ascontiguousarray(other, np.uint32)
+    share = np.ascontiguousarray(share, np.float32)
+    point = np.ascontiguousarray(point, np.float64)
+    normal = np.ascontiguousarray(normal, np.float64)
+    out = np.zeros((len(leaf), 3), np.float64)
+    L = lib()
+    L.kp_albedos.argtypes = [_P, ctypes.c_uint32, _P, ctypes.c_uint32, _P, ctypes.c_uint32, _P, _P, _P, _P, _P, _P]
+    L.kp_albedos(ctypes.addressof(mats), len(mats), _ptr(leaf_material), len(leaf_material), _ptr(placements) if placements is not None else None,
+                 len(leaf), _ptr(leaf), _ptr(other), _ptr(share), _ptr(point), _ptr(normal), _ptr(out))
+    del keep
+    return out
 
 
 def denoise(width: int, height: int, demodulated: int, lens, colour, moment, length, distance, normal, leaf, albedo) -> np.ndarray:

@@ -51,15 +51,17 @@ static double compare_d(int op, double a, double b) {
 	}
 }
 
-static double step_d(const kp_step* s, const double* r, const double pt[3]) {
+static double step_d(const kp_step* s, const double* r, const double pt[3], const double* n, const double* arguments) {
 	const double a = r[s->a], b = r[s->b];
 	switch (s->opcode) {
 		case KP_CONSTANT: return s->value;
-		case KP_ARGUMENT: return 0.0;
+		case KP_ARGUMENT: return arguments ? arguments[s->a] : 0.0;
 		case KP_POINTX: return pt[0];
 		case KP_POINTY: return pt[1];
 		case KP_POINTZ: return pt[2];
-		case KP_NORMALX: case KP_NORMALY: case KP_NORMALZ: return 0.0;
+		case KP_NORMALX: return n ? n[0] : 0.0;
+		case KP_NORMALY: return n ? n[1] : 0.0;
+		case KP_NORMALZ: return n ? n[2] : 0.0;
 		case KP_ADD: return a + b;
 		case KP_SUBTRACT: return a - b;
 		case KP_MULTIPLY: return a * b;
@@ -84,7 +86,14 @@ static double step_d(const kp_step* s, const double* r, const double pt[3]) {
 
 double kp_eval(const kp_program* p, const double pt[3], double* regs) {
 	for (uint32_t i = 0; i < p->count; ++i) {
-		regs[i] = step_d(&p->steps[i], regs, pt);
+		regs[i] = step_d(&p->steps[i], regs, pt, NULL, NULL);
+	}
+	return regs[p->result];
+}
+
+double kp_eval_inputs(const kp_program* p, const double pt[3], const double n[3], const double* arguments, double* regs) {
+	for (uint32_t i = 0; i < p->count; ++i) {
+		regs[i] = step_d(&p->steps[i], regs, pt, n, arguments);
 	}
 	return regs[p->result];
 }

@@ -55,6 +55,9 @@ typedef struct kp_source {
 
 /* Program evaluation (sdf/program.cpp:57-140). regs holds count values. */
 double kp_eval(const kp_program* p, const double pt[3], double* regs);
+/* sdf/program.cpp evaluate<double> with every input: the point, the normal
+ * and the arguments the program reads (a pattern's) */
+double kp_eval_inputs(const kp_program* p, const double pt[3], const double n[3], const double* arguments, double* regs);
 kp_interval kp_eval_interval(const kp_program* p, const kp_interval box[3], kp_interval* regs);
 kp_dual kp_eval_dual(const kp_program* p, const double pt[3], kp_dual* regs);
 /* sdf/program.cpp:505 keptSourceOf over a whole program, given its values. */
@@ -123,6 +126,19 @@ typedef struct kp_material {
 	double escape[32];
 	double glow[3];   /* material.cpp:325 glowOf: the glow colour times its strength */
 	double absorb[3]; /* absorption.cpp:28 keptThrough: the body's absorption a unit length */
+	/* sdf/scene.h Albedo: a ramp over a pattern program (pattern.count 0:
+	 * the flat albedo above), its arguments, stops (3 a stop) and space */
+	kp_program pattern;
+	const double* pattern_arguments;
+	const double* stops;
+	uint32_t stop_count;
+	uint32_t world;
+	/* a rough glass (material.cpp:1002 glassResponse): whether it gives back
+	 * what single scattering loses, and its material/energy.h Boundary (17 x
+	 * 32 rarer, 17 x 32 denser, 17 rarer averages, 17 denser averages, 17
+	 * rarer-through shares) */
+	uint32_t loses_much;
+	const double* boundary;
 } kp_material;
 
 /* A lamp (light.cpp:78 lampOf): kind 2 sphere, 3 quad. */
@@ -146,7 +162,14 @@ typedef struct kp_view {
  * RGB of each pixel of the band (3 doubles a pixel).
  */
 void kp_render_band(const kp_octree* tree, const uint32_t* leaf_material, const kp_material* materials, const kp_lamp* lamps, const kp_view* view,
-                    int row0, int rows, int threads, double* sums);
+                    const double* placements, int row0, int rows, int threads, double* sums);
+
+/* material.cpp:345 bsdfAt's albedo for n hits (leaf, other, share, point,
+ * the normal facing the ray): the leaf's material's colour or ramp over its
+ * pattern, mixed with the other leaf's across a blend seam.  placements: 12
+ * doubles a leaf (sdf/scene.h Placement: linear row by row, origin). */
+void kp_albedos(const kp_material* materials, uint32_t material_count, const uint32_t* leaf_material, uint32_t leaf_count, const double* placements,
+                uint32_t n, const uint32_t* leaf, const uint32_t* other, const float* share, const double* point, const double* normal, double* rgb);
 
 /* ---- denoiser (plugins/reconstruction/atrous/atrous.cpp:513 denoisedFrame) ----
  * lens: eye[3], forward[3], right[3], up[3], reach, aspect.  Per pixel:

@@ -375,7 +375,7 @@ typedef struct shading {
 	spec albedo, twice, within, beyond;
 	double rgb[3]; /* the albedo at the hit, blended across a shared seam */
 	double leaving, left, share, masking;
-	int parted;
+	int parted, inside;
 } shading;
 
 static spec lane_indices(const kp_material* m, const lanes* w) {
@@ -416,6 +416,7 @@ static shading shading_of(const kp_material* m, const double* rgb, const kp_mate
 			for (int k = 0; k < 4; ++k) s.twice.v[k] = a.v[k] * a.v[k] * m->escape_average / (1 - a.v[k] * (1 - m->escape_average));
 		}
 	} else if (m->kind == 3) {
+		s.inside = medium != NO_MATERIAL;
 		if (medium != NO_MATERIAL) {
 			s.within = lane_indices(&all[medium], w);
 			s.parted = all[medium].dispersion != 0;
@@ -432,6 +433,179 @@ typedef struct response {
 	double density;
 } response;
 
+/* ---- rough glass (material.cpp:766-1032, energy.cpp:255-320) ---- */
+#define RATIOS 17
+#define VIEWS 32
+#define DENSEST_RATIO 3.0
+
+typedef struct table_row {
+	int lower, upper;
+	double share;
+} table_row;
+
+/* energy.cpp:255 rowOf: the place of the indices' ratio among the rows */
+static table_row row_of(double near, double far) {
+	const double ratio = maxd(near, far) / mind(near, far);
+	const double place = (mind(ratio, DENSEST_RATIO) - 1) / (DENSEST_RATIO - 1) * (RATIOS - 1);
+	int lower = (int) floor(place);
+	lower = lower < 0 ? 0 : (lower > RATIOS - 1 ? RATIOS - 1 : lower);
+	table_row r;
+	r.lower = lower;
+	r.upper = lower + 1 < RATIOS - 1 ? lower + 1 : RATIOS - 1;
+	r.share = clampd(place - lower, 0, 1);
+	return r;
+}
+
+static double blended_row(const double* values, table_row r) { return values[r.lower] * (1 - r.share) + values[r.upper] * r.share; }
+
+typedef struct loss {
+	double near_average, far_average, back, through, share;
+} loss;
+
+/* energy.cpp:284 lossAt */
+static loss loss_at(const double* b, double near, double far) {
+	const table_row row = row_of(near, far);
+	const double rarer = blended_row(b + 2 * RATIOS * VIEWS, row);
+	const double denser = blended_row(b + 2 * RATIOS * VIEWS + RATIOS, row);
+	const double share = blended_row(b + 2 * RATIOS * VIEWS + 2 * RATIOS, row);
+	const int from_rarer = near <= far;
+	loss l;
+	l.near_average = from_rarer ? rarer : denser;
+	l.far_average = from_rarer ? denser : rarer;
+	l.back = l.through = l.share = 0;
+	const double near_lost = 1 - l.near_average, denser_lost = 1 - denser;
+	if (!(near_lost > 1e-9) || !(denser_lost > 1e-9)) return l;
+	const double turned = (far / near) * (far / near);
+	l.through = from_rarer ? share / denser_lost : share / denser_lost * turned;
+	const double given = mind(l.through * (1 - l.far_average), 1.0);
+	l.back = (1 - given) / near_lost;
+	l.share = given;
+	return l;
+}
+
+/* energy.cpp:309 rowAt, :317 boundaryAt */
+static double row_at(const double* table, int row, double c) {
+	const double place = clampd(c, 0, 1) * VIEWS - 0.5;
+	int lower = (int) floor(place);
+	lower = lower < 0 ? 0 : (lower > VIEWS - 1 ? VIEWS - 1 : lower);
+	const int upper = lower + 1 < VIEWS - 1 ? lower + 1 : VIEWS - 1;
+	const double share = clampd(place - lower, 0, 1);
+	return table[row * VIEWS + lower] * (1 - share) + table[row * VIEWS + upper] * share;
+}
+
+static double boundary_at(const double* b, double near, double far, double c) {
+	const table_row row = row_of(near, far);
+	const double* table = near <= far ? b : b + RATIOS * VIEWS;
+	return row_at(table, row.lower, c) * (1 - row.share) + row_at(table, row.upper, c) * row.share;
+}
+
+/* material.cpp:780 lossLeft */
+static double loss_left(const double* b, double near, double far, double c) { return maxd(1 - boundary_at(b, near, far, c), 0.0); }
+
+typedef struct broad {
+	double share, through;
+} broad;
+
+/* material.cpp:789 broadOf, over the hero lane's indices */
+static broad broad_of(const shading* s, double leaving) {
+	broad w = { 0, 0 };
+	if (s->m->loses_much) {
+		w.share = clampd(loss_left(s->m->boundary, s->within.v[0], s->beyond.v[0], leaving), 0.0, 1.0);
+		w.through = loss_at(s->m->boundary, s->within.v[0], s->beyond.v[0]).share;
+	}
+	return w;
+}
+
+/* material.cpp:797 laneReflectance (no film), :814 laneReflectances, :821 reflectChance */
+static double lane_reflectance(const shading* s, double c, int k) { return dielectric(c, s->within.v[k] / s->beyond.v[k]); }
+
+static spec lane_reflectances(const shading* s, double c) {
+	if (!s->parted) return flat(lane_reflectance(s, c, 0));
+	spec r;
+	for (int k = 0; k < 4; ++k) r.v[k] = lane_reflectance(s, c, k);
+	return r;
+}
+
+static double reflect_chance(const shading* s, double c) {
+	if (!s->parted) return lane_reflectance(s, c, 0);
+	const spec r = lane_reflectances(s, c);
+	return 0.25 * (r.v[0] + r.v[1] + r.v[2] + r.v[3]);
+}
+
+/* material.cpp:836 reflectanceAcross: seen from the denser side, Fresnel of the arriving cosine */
+static double reflectance_across(const shading* s, double leaving, double arriving, int k) {
+	const double within = s->within.v[k], beyond = s->beyond.v[k];
+	if (within <= beyond) return lane_reflectance(s, leaving, k);
+	return dielectric(arriving, beyond / within);
+}
+
+/* material.cpp:846 backLoss, :850 throughLoss, :859 givenBack */
+static spec given_back(const shading* s, double leaving, double arriving, int through) {
+	if (!s->m->loses_much) return flat(0);
+	const int lanes_n = s->parted ? 4 : 1;
+	spec g = flat(0);
+	for (int k = 0; k < lanes_n; ++k) {
+		const double near = s->within.v[k], far = s->beyond.v[k];
+		const loss l = loss_at(s->m->boundary, near, far);
+		g.v[k] = through ? l.through * loss_left(s->m->boundary, near, far, leaving) * loss_left(s->m->boundary, far, near, -arriving) / PI
+		                 : l.back * loss_left(s->m->boundary, near, far, leaving) * loss_left(s->m->boundary, near, far, arriving) / PI;
+	}
+	return s->parted ? g : flat(g.v[0]);
+}
+
+/* material.cpp:884 glassReflection */
+static response glass_reflection(const shading* s, v3 out, v3 in, double leaving, double arriving) {
+	const double width = s->m->width;
+	const v3 facet = halfway(out, in, s->normal);
+	const double onto = dotv(out, facet);
+	const spec each = lane_reflectances(s, maxd(onto, 0.0));
+	const double lobe = onto > 0 ? facet_distribution(dotv(s->normal, facet), width) : 0;
+	const double back = s->parted ? 0.25 * (each.v[0] + each.v[1] + each.v[2] + each.v[3]) : each.v[0];
+	const double facets = lobe * smith_masking(leaving, width) / (4 * leaving);
+	const broad wide = broad_of(s, leaving);
+	response r;
+	r.value = sadd(sscale(each, lobe * smith_visibility(leaving, arriving, width)), given_back(s, leaving, arriving, 0));
+	r.density = (1 - wide.share) * back * facets + wide.share * (1 - wide.through) * arriving / PI;
+	return r;
+}
+
+/* material.cpp:947 lanePassage over :925 bentFacet */
+static void lane_passage(const shading* s, v3 out, v3 in, double leaving, double arriving, int k, double* sent, double* facets) {
+	const double width = s->m->width;
+	const double near = s->within.v[k], far = s->beyond.v[k];
+	*sent = *facets = 0;
+	const v3 sum = add(scl(out, near), scl(in, far));
+	const double size = len(sum);
+	if (!(size > 1e-12)) return;
+	const v3 facet = scl(sum, (dotv(sum, s->normal) < 0 ? -1 : 1) / size);
+	const double into = dotv(in, facet);
+	if (dotv(out, facet) <= 0 || into >= 0) return;
+	const double stretch = far * far * -into / (size * size);
+	if (stretch <= 0) return;
+	const double onto = dotv(out, facet);
+	const double lobe = facet_distribution(dotv(s->normal, facet), width) * onto * stretch;
+	const double kept = 1 - reflectance_across(s, onto, -dotv(in, facet), k);
+	*sent = kept * lobe * 4 * smith_visibility(leaving, -arriving, width);
+	*facets = (1 - reflect_chance(s, onto)) * lobe * smith_masking(leaving, width) / leaving;
+}
+
+/* material.cpp:986 glassPassage */
+static response glass_passage(const shading* s, v3 out, v3 in, double leaving, double arriving) {
+	const int lanes_n = s->parted ? 4 : 1;
+	spec sent = flat(0);
+	double facets = 0;
+	for (int k = 0; k < lanes_n; ++k) {
+		double f;
+		lane_passage(s, out, in, leaving, arriving, k, &sent.v[k], &f);
+		if (k == 0) facets = f;
+	}
+	const broad wide = broad_of(s, leaving);
+	response r;
+	r.value = sadd(s->parted ? sent : flat(sent.v[0]), given_back(s, leaving, arriving, 1));
+	r.density = (1 - wide.share) * facets + wide.share * wide.through * -arriving / PI;
+	return r;
+}
+
 static response respond(const shading* s, v3 out, v3 in, const lanes* w) {
 	response r;
 	r.value = flat(0);
@@ -443,8 +617,10 @@ static response respond(const shading* s, v3 out, v3 in, const lanes* w) {
 		return r;
 	}
 	if (m->kind == 3) {
+		/* material.cpp:1002 glassResponse */
 		r.density = 0;
-		return r;
+		if (s->leaving <= 0 || m->exact) return r;
+		return arriving < 0 ? glass_passage(s, out, in, s->leaving, arriving) : glass_reflection(s, out, in, s->leaving, arriving);
 	}
 	const double cosd = maxd(arriving, 0) / PI;
 	if (s->leaving <= 0 || arriving <= 0) {
@@ -518,6 +694,47 @@ static scatter sample(const shading* s, v3 out, const lanes* w, double lobe, dou
 		o.weight = sscale(r.value, fabs(arriving) / r.density);
 		return o;
 	}
+	if (!m->exact) {
+		/* material.cpp:1328 glassScatter: the broad lobe (cosine about
+		 * either side, :1236 broadChoice) or a visible facet, mirrored or
+		 * bent by the hero lane (:1246 facetChoice) */
+		const double leaving = s->leaving;
+		if (leaving <= 0) return o;
+		const broad wide = broad_of(s, leaving);
+		int found = 1, reflected;
+		v3 in;
+		if (lobe < wide.share) {
+			reflected = side >= wide.through;
+			const basis around = basis_around(reflected ? s->normal : scl(s->normal, -1));
+			const double reach = sqrt(u), angle = 2 * PI * v, height = sqrt(maxd(1 - u, 0));
+			in = to_world(around, mk(reach * cos(angle), reach * sin(angle), height));
+		} else {
+			const v3 facet = visible_facet(s->frame, out, m->width, u, v);
+			const double onto = dotv(out, facet);
+			if (onto <= 0) return o;
+			reflected = side < reflect_chance(s, onto);
+			if (reflected) {
+				in = mirrored(out, facet);
+			} else {
+				const double ratio = s->within.v[0] / s->beyond.v[0];
+				const double leftover = 1 - ratio * ratio * (1 - onto * onto);
+				found = leftover > 0;
+				in = found ? sub(scl(sub(scl(facet, onto), out), ratio), scl(facet, sqrt(leftover))) : mk(0, 0, 0);
+			}
+		}
+		const double arriving = dotv(s->normal, in);
+		if (!found || (reflected ? arriving <= 0 : arriving >= 0)) return o;
+		const response r = reflected ? glass_reflection(s, out, in, leaving, arriving) : glass_passage(s, out, in, leaving, arriving);
+		if (r.density <= 0) return o;
+		o.found = 1;
+		o.incoming = in;
+		o.density = r.density;
+		o.weight = sscale(r.value, fabs(arriving) / r.density);
+		o.through = !reflected;
+		o.dispersed = o.through && s->parted && s->within.v[0] != s->beyond.v[0];
+		o.medium_after = o.through ? (medium != NO_MATERIAL ? NO_MATERIAL : material) : NO_MATERIAL;
+		return o;
+	}
 	/* material.cpp:1300 exactGlassScatter */
 	if (s->leaving <= 0) return o;
 	double refl[4];
@@ -558,6 +775,7 @@ typedef struct job {
 	double reach, aspect;
 	uint64_t seed_mix;
 	int absorbs; /* absorption.cpp:18 sceneAbsorbs: some glass absorbs */
+	const double* placements; /* 12 a leaf, or none */
 } job;
 
 /* trace.cpp:179 keptOnLeg with absorption.cpp:28 keptThrough: what a leg of
@@ -595,17 +813,85 @@ static void sky_colour(const kp_view* view, v3 d, double out[3]) {
 
 /* material.cpp:345 bsdfAt: the leaf's albedo, mixed with the other leaf's by
  * the hit's share where a blend joins two leaves */
-static const kp_material* material_of_leaf(const job* J, uint32_t leaf) {
-	const uint32_t material = leaf != 0xFFFFFFFFu ? J->leaf_material[leaf] : 0;
-	return &J->materials[material < J->view->material_count ? material : 0];
+static const kp_material* material_in(const kp_material* materials, uint32_t count, const uint32_t* leaf_material, uint32_t leaf) {
+	const uint32_t material = leaf != 0xFFFFFFFFu ? leaf_material[leaf] : 0;
+	return &materials[material < count ? material : 0];
 }
 
-static void albedo_at(const job* J, const kp_hit* hit, double rgb[3]) {
-	const kp_material* m = material_of_leaf(J, hit->leaf);
-	for (int c = 0; c < 3; ++c) rgb[c] = m->albedo[c];
+/* material.cpp:281 rampAt: the stops spread evenly over 0..1 */
+static void ramp_at(const kp_material* m, double value, double rgb[3]) {
+	const uint32_t n = m->stop_count;
+	if (n <= 1) {
+		for (int c = 0; c < 3; ++c) rgb[c] = m->stops ? m->stops[c] : m->albedo[c];
+		return;
+	}
+	const double place = clampd(value, 0, 1) * (double) (n - 1);
+	size_t lower = (size_t) place;
+	if (lower > n - 2) lower = n - 2;
+	const double share = place - (double) lower;
+	for (int c = 0; c < 3; ++c) rgb[c] = m->stops[3 * lower + c] * (1 - share) + m->stops[3 * lower + 3 + c] * share;
+}
+
+/* material.cpp:292 placedVector: linear x (v - origin), or linear x v */
+static v3 placed(const double* pl, v3 v, int offset) {
+	const v3 d = offset ? sub(v, mk(pl[9], pl[10], pl[11])) : v;
+	return mk(pl[0] * d.x + pl[1] * d.y + pl[2] * d.z, pl[3] * d.x + pl[4] * d.y + pl[5] * d.z, pl[6] * d.x + pl[7] * d.y + pl[8] * d.z);
+}
+
+/* material.cpp:314 albedoAt over :299 patternAt: a flat colour, or the ramp
+ * at the pattern's value at the point and normal, in the painted leaf's
+ * space unless the pattern is read in world space */
+static void colour_at(const kp_material* m, const double* placements, uint32_t leaf, v3 point, v3 normal, double rgb[3]) {
+	if (m->pattern.count == 0) {
+		for (int c = 0; c < 3; ++c) rgb[c] = m->albedo[c];
+		return;
+	}
+	const int local = !m->world && leaf != 0xFFFFFFFFu && placements != NULL;
+	v3 p = point, n = normal;
+	if (local) {
+		const double* pl = placements + 12 * (size_t) leaf;
+		p = placed(pl, point, 1);
+		const v3 turned = placed(pl, normal, 0);
+		const double size = len(turned);
+		n = size > 0 ? scl(turned, 1 / size) : turned;
+	}
+	const double pt[3] = { p.x, p.y, p.z }, nv[3] = { n.x, n.y, n.z };
+	double* regs = (double*) malloc(sizeof(double) * m->pattern.count);
+	const double value = kp_eval_inputs(&m->pattern, pt, nv, m->pattern_arguments, regs);
+	free(regs);
+	ramp_at(m, value, rgb);
+}
+
+static void albedo_in(const kp_material* materials, uint32_t count, const uint32_t* leaf_material, const double* placements, const kp_hit* hit,
+                      v3 normal, double rgb[3]) {
+	const v3 point = mk(hit->point[0], hit->point[1], hit->point[2]);
+	colour_at(material_in(materials, count, leaf_material, hit->leaf), placements, hit->leaf, point, normal, rgb);
 	if (hit->other != 0xFFFFFFFFu && hit->share > 0) {
-		const kp_material* o = material_of_leaf(J, hit->other);
-		for (int c = 0; c < 3; ++c) rgb[c] = rgb[c] * (1 - (double) hit->share) + o->albedo[c] * (double) hit->share;
+		double o[3];
+		colour_at(material_in(materials, count, leaf_material, hit->other), placements, hit->other, point, normal, o);
+		for (int c = 0; c < 3; ++c) rgb[c] = rgb[c] * (1 - (double) hit->share) + o[c] * (double) hit->share;
+	}
+}
+
+static const kp_material* material_of_leaf(const job* J, uint32_t leaf) {
+	return material_in(J->materials, J->view->material_count, J->leaf_material, leaf);
+}
+
+static void albedo_at(const job* J, const kp_hit* hit, v3 normal, double rgb[3]) {
+	albedo_in(J->materials, J->view->material_count, J->leaf_material, J->placements, hit, normal, rgb);
+}
+
+void kp_albedos(const kp_material* materials, uint32_t material_count, const uint32_t* leaf_material, uint32_t leaf_count, const double* placements,
+                uint32_t n, const uint32_t* leaf, const uint32_t* other, const float* share, const double* point, const double* normal, double* rgb) {
+	(void) leaf_count;
+	for (uint32_t i = 0; i < n; ++i) {
+		kp_hit hit;
+		memset(&hit, 0, sizeof hit);
+		hit.leaf = leaf[i];
+		hit.other = other[i];
+		hit.share = share[i];
+		for (int c = 0; c < 3; ++c) hit.point[c] = (float) point[3 * i + c];
+		albedo_in(materials, material_count, leaf_material, placements, &hit, mk(normal[3 * i], normal[3 * i + 1], normal[3 * i + 2]), rgb + 3 * i);
 	}
 }
 
@@ -673,9 +959,15 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 		const int capped = depth + 1 >= V->surfaces;
 		const v3 out = scl(heading, -1);
 		double rgb[3];
-		albedo_at(J, &hit, rgb);
+		albedo_at(J, &hit, normal, rgb);
 		const shading s = shading_of(m, rgb, J->materials, normal, out, &w, medium);
-		if (!m->exact && V->lamp_count > 0) {
+		/* trace.cpp:583 aimable: from outside every body, or from inside
+		 * the glass being crossed where it bends; trace.cpp:590 openSide:
+		 * the side the line leaves by */
+		const int bends = m->kind == 3 && s.within.v[0] != s.beyond.v[0];
+		const int aimable = medium == NO_MATERIAL || (medium == material && bends);
+		const v3 open = s.inside ? scl(normal, -1) : normal;
+		if (!m->exact && aimable && V->lamp_count > 0) {
 			const double u0 = number(stream, index, depth, LIGHT_U), v0 = number(stream, index, depth, LIGHT_V);
 			double choice = number(stream, index, depth, PICK);
 			double total = 0, picked = 0, chosen_dist = 0;
@@ -684,7 +976,7 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 			for (uint32_t k = 0; k < V->lamp_count; ++k) {
 				const aim a = aim_lamp(&J->lamps[k], point, u0, v0);
 				if (!a.found) continue;
-				const double facing = dotv(normal, a.toward);
+				const double facing = dotv(open, a.toward);
 				if (facing <= 0 || a.distance <= 0) continue;
 				const response f = respond(&s, out, a.toward, &w);
 				double wgt = 1;
@@ -708,7 +1000,7 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 				}
 			}
 			if (picked > 0) {
-				const kp_ray line = ray_of(add(point, scl(normal, lift)), chosen_dir, chosen_dist - lift, NO_MATERIAL);
+				const kp_ray line = ray_of(add(point, scl(open, lift)), chosen_dir, chosen_dist - lift, NO_MATERIAL);
 				kp_hit blocked;
 				kp_tracer_trace(tracer, &line, &blocked);
 				if (blocked.kind == 0) R = sadd(R, sscale(chosen, total / picked));
@@ -730,9 +1022,13 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 			if (!(number(stream, index, depth, SURVIVAL) < survival)) break;
 			carried = sscale(carried, 1 / survival);
 		}
+		/* trace.cpp:956 aimedAlong: the next leg's meets are weighed against
+		 * aiming where the scatter left by the open side of an aimable vertex */
+		const int left_open = sc.through == (medium != NO_MATERIAL);
+		const int aimed = !sc.delta && sc.density > 0 && left_open && aimable;
 		if (sc.through) medium = sc.medium_after;
 		T = carried;
-		drawn = sc.delta ? 0 : sc.density;
+		drawn = aimed ? sc.density : 0;
 		camera = 0;
 		from = point;
 		ray = ray_of(add(point, scl(normal, side_of > 0 ? lift : -lift)), sc.incoming, INFINITY, medium);
@@ -771,7 +1067,7 @@ static void* worker(void* arg) {
 }
 
 void kp_render_band(const kp_octree* tree, const uint32_t* leaf_material, const kp_material* materials, const kp_lamp* lamps, const kp_view* view,
-                    int row0, int rows, int threads, double* sums) {
+                    const double* placements, int row0, int rows, int threads, double* sums) {
 	job J;
 	memset(&J, 0, sizeof J);
 	J.tree = tree;
@@ -782,6 +1078,7 @@ void kp_render_band(const kp_octree* tree, const uint32_t* leaf_material, const 
 	J.row0 = row0;
 	J.rows = rows;
 	J.sums = sums;
+	J.placements = placements;
 	pthread_mutex_init(&J.lock, NULL);
 	/* core/camera.cpp:9 lensOf */
 	J.eye = vd(view->eye);

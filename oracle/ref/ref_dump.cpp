@@ -74,6 +74,16 @@ int dumpScene(const char* sdf, const char* out) {
 	for (std::size_t i = 0; i < file.scene.leaves.size(); ++i) {
 		std::fprintf(f, "%s%u", i ? "," : "", file.scene.leaves[i].material);
 	}
+	// sdf/scene.h Placement of each leaf: linear (row by row), then origin
+	std::fprintf(f, "],\n\"placements\":[");
+	for (std::size_t i = 0; i < file.scene.leaves.size(); ++i) {
+		const Placement& pl = file.scene.leaves[i].placement;
+		std::fprintf(f, "%s[", i ? "," : "");
+		for (int r = 0; r < 3; ++r) {
+			for (int c = 0; c < 3; ++c) std::fprintf(f, "%.17g,", pl.linear[r][c]);
+		}
+		std::fprintf(f, "%.17g,%.17g,%.17g]", pl.origin[0], pl.origin[1], pl.origin[2]);
+	}
 	std::fprintf(f, "],\n\"materials\":[");
 	for (std::size_t i = 0; i < file.looks.materials.size(); ++i) {
 		const Material& m = file.looks.materials[i];
@@ -85,7 +95,25 @@ int dumpScene(const char* sdf, const char* out) {
 		putColour(f, m.absorb);
 		std::fprintf(f, ",\"glow\":");
 		putColour(f, m.glow);
-		std::fprintf(f, ",\"strength\":%.9g,\"film\":[%.9g,%.9g],\"coats\":%zu}", double(m.strength), double(m.film[0]), double(m.film[1]), file.looks.coats.size());
+		std::fprintf(f, ",\"strength\":%.9g,\"film\":[%.9g,%.9g],\"coats\":%zu", double(m.strength), double(m.film[0]), double(m.film[1]), file.looks.coats.size());
+		// sdf/scene.h Albedo: the pattern's program (Scene::programs), the
+		// arguments it reads (Scene::arguments from Albedo::arguments), and
+		// whether it is read in world space
+		std::fprintf(f, ",\"world\":%d", int(m.albedo.world));
+		if (m.albedo.program >= 0) {
+			const Program& program = file.scene.programs[std::size_t(m.albedo.program)];
+			std::fprintf(f, ",\"patternResult\":%u,\"patternSteps\":[", program.result);
+			for (std::size_t s = 0; s < program.steps.size(); ++s) {
+				const Step& step = program.steps[s];
+				std::fprintf(f, "%s[%d,%u,%u,%u,%.17g,%u]", s ? "," : "", int(step.opcode), step.a, step.b, step.c, step.value, step.leaf);
+			}
+			std::fprintf(f, "],\"patternArguments\":[");
+			for (std::uint32_t k = 0; k < program.arguments; ++k) {
+				std::fprintf(f, "%s%.17g", k ? "," : "", file.scene.arguments[m.albedo.arguments + k]);
+			}
+			std::fprintf(f, "]");
+		}
+		std::fprintf(f, "}");
 	}
 	std::fprintf(f, "],\n\"lights\":[");
 	for (std::size_t i = 0; i < file.lighting.lights.size(); ++i) {
@@ -113,7 +141,26 @@ int dumpScene(const char* sdf, const char* out) {
 		for (int k = 0; k < energyViews; ++k) {
 			std::fprintf(f, "%s%.17g", k ? "," : "", fin.escape.table[std::size_t(k)]);
 		}
-		std::fprintf(f, "]}");
+		std::fprintf(f, "]");
+		// material/energy.h Boundary of a glass: rarer, denser (a row of
+		// views per ratio), rarerAverage, denserAverage, rarerThrough
+		if (fin.kind == MaterialKind::Glass) {
+			std::fprintf(f, ",\"boundary\":[");
+			bool first = true;
+			const auto put = [&](const double* v, std::size_t n) {
+				for (std::size_t k = 0; k < n; ++k) {
+					std::fprintf(f, "%s%.17g", first ? "" : ",", v[k]);
+					first = false;
+				}
+			};
+			put(fin.boundary.rarer.data(), fin.boundary.rarer.size());
+			put(fin.boundary.denser.data(), fin.boundary.denser.size());
+			put(fin.boundary.rarerAverage.data(), fin.boundary.rarerAverage.size());
+			put(fin.boundary.denserAverage.data(), fin.boundary.denserAverage.size());
+			put(fin.boundary.rarerThrough.data(), fin.boundary.rarerThrough.size());
+			std::fprintf(f, "]");
+		}
+		std::fprintf(f, "}");
 	}
 	const Sky& sky = file.lighting.sky;
 	std::fprintf(f, "],\n\"sky\":{\"kind\":%d,\"zenith\":", int(sky.kind));

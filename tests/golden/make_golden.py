@@ -37,13 +37,22 @@ REFERENCE_FLAGS = ["--threads", "8", "--use", "stopping=fixed_count", "--use", "
 
 # The image fixtures are drawn on the reference's sphere-traced geometry
 # (plugins/geometry/sphere_trace, sphereTraced), the geometry the oracle and
-# the device restate; the reference's default tree geometry (face-fitted
-# leaves) lands hits a little differently and its frames differ from the
-# sphere-traced ones by up to ~0.7% on scenes with close contacts.
+# the device restate, over the region the tree would be built over
+# (--region, the scene's sceneRegion) rather than the sphere tracer's own
+# reach around the target; the reference's default tree geometry
+# (face-fitted leaves) lands hits a little differently and its frames
+# differ from the sphere-traced ones by up to ~0.7% on scenes with close
+# contacts.
 IMAGE_FLAGS = REFERENCE_FLAGS + ["--use", "geometry=sphere_trace"]
 
+
+def region_flags(scene: Scene) -> list[str]:
+    lower = np.asarray(scene.region_lower, np.float64)
+    upper = lower + np.asarray(scene.region_size, np.float64)
+    return ["--region"] + [repr(float(x)) for x in lower] + [repr(float(x)) for x in upper]
+
 # name -> (seeds, spp per seed) of the reference frames kept as image fixtures
-IMAGES = {"room_small": (16, 64), "c1_small": (16, 64), "c2_small": (16, 64), "glow_small": (16, 64), "glass_small": (16, 64)}
+IMAGES = {"room_small": (16, 64), "c1_small": (16, 64), "c2_small": (16, 64), "glow_small": (16, 64), "glass_small": (16, 64), "patterns_small": (16, 64), "rough_small": (16, 64)}
 
 # name -> (generator, kwargs, trace rays, cut depth)
 SCENES = {
@@ -55,6 +64,8 @@ SCENES = {
     "c2_small": (scenegen.scene_config2, dict(seed=3, width=64, height=36, samples=64, groups=24), 0, 0),
     "glow_small": (scenegen.scene_glow, dict(seed=5, width=48, height=48, samples=64), 0, 0),
     "glass_small": (scenegen.scene_glass, dict(seed=6, width=48, height=48, samples=64), 0, 0),
+    "patterns_small": (scenegen.scene_patterns, dict(seed=7, width=48, height=48, samples=64), 0, 0),
+    "rough_small": (scenegen.scene_glass, dict(seed=8, width=48, height=48, samples=64, rough=True), 0, 0),
 }
 
 
@@ -137,7 +148,7 @@ def read_pfm(path: str) -> np.ndarray:
     return a[::-1].copy()
 
 
-def reference_images(render: str, sdf: str, name: str, tmp: str) -> None:
+def reference_images(render: str, sdf: str, name: str, tmp: str, scene: Scene) -> None:
     """Frames of the reference renderer at fixed spp under independent seeds:
     their per-pixel mean and the standard error of one seed's frame."""
     seeds, spp = IMAGES[name]
@@ -145,7 +156,7 @@ def reference_images(render: str, sdf: str, name: str, tmp: str) -> None:
     for k in range(seeds):
         pfm = os.path.join(tmp, f"{name}_{k}.pfm")
         subprocess.run([render, sdf, "--out", os.path.join(tmp, f"{name}_{k}.ppm"), "--pfm", pfm, "--seed", str(1000 + k),
-                        "--samples", str(spp)] + IMAGE_FLAGS, check=True, capture_output=True)
+                        "--samples", str(spp)] + IMAGE_FLAGS + region_flags(scene), check=True, capture_output=True)
         frames.append(read_pfm(pfm))
     f = np.stack(frames)
     np.savez_compressed(os.path.join(HERE, f"image_{name}.npz"), frames=f.astype(np.float32), spp=spp, seeds=np.arange(1000, 1000 + seeds))
@@ -348,7 +359,7 @@ def main() -> None:
         scene.save(os.path.join(HERE, "scenes", name + ".npz"))
         print(name, "programs", scene.program_count, "steps", len(scene.steps))
         if name in IMAGES:
-            reference_images(render, sdf, name, tmp)
+            reference_images(render, sdf, name, tmp, scene)
         if nrays:
             rng = np.random.default_rng(1234)
             rays = np.concatenate([camera_rays(scene, nrays // 2, rng), scattered_rays(scene, nrays - nrays // 2, rng)])

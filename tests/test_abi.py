@@ -51,6 +51,32 @@ def test_block_checks():
     b.close()
 
 
+def test_pattern_blocks():
+    """A scene with patterned albedos carries the looks.patterns,
+    pattern_steps, pattern_arguments, stops and placements blocks, each
+    with the reference's element size."""
+    b = host_backend()
+    sc = scene("patterns_small")
+    blocks = K.scene_blocks(sc)
+    for name in ("looks.patterns", "looks.pattern_steps", "looks.pattern_arguments", "looks.stops", "looks.placements"):
+        assert name in blocks
+    assert blocks["looks.patterns"].dtype.itemsize == 32
+    assert blocks["looks.placements"].dtype.itemsize == 96
+    pats = blocks["looks.patterns"]
+    patterned = np.asarray(sc.materials["patterned"]) != 0
+    assert np.all((pats["count"] > 0) == patterned)
+    assert np.all(pats["count"][patterned] <= 64)
+    assert len(blocks["looks.placements"]) == len(sc.leaf_material)
+    b.load(sc)
+    with pytest.raises(K.KdnError) as e:
+        b.upload("looks.patterns", np.zeros(4, np.uint32))
+    assert e.value.status == K.KDN_BAD_ARG
+    with pytest.raises(K.KdnError) as e:
+        b.upload("looks.placements", np.zeros((2, 12), np.float32))
+    assert e.value.status == K.KDN_BAD_ARG
+    b.close()
+
+
 def test_bad_program_is_refused():
     b = host_backend()
     sc = scene("c1")

@@ -48,7 +48,7 @@ def compare(a, b):
     return (np.abs(z) > 3).mean(), cz, ca.mean(0), cb.mean(0)
 
 
-@pytest.mark.parametrize("name", ["room_small", "c1_small", "c2_small", "glow_small", "glass_small"])
+@pytest.mark.parametrize("name", ["room_small", "c1_small", "c2_small", "glow_small", "glass_small", "patterns_small", "rough_small"])
 def test_frame_matches_oracle_and_reference(backend, name):
     import oracle.port as op
     sc = scene(name)
@@ -101,10 +101,43 @@ def test_unsupported_material_is_refused(backend):
     backend.load(sc)
     backend.build(5, 10, 64)
     blocks = K.scene_blocks(sc)
-    mats = blocks["looks.materials"].copy()
-    mats["flags"][0] = 1  # a patterned albedo
-    backend.upload("looks.materials", mats)
+    finishes = blocks["transport.finishes"].copy()
+    finishes["film"][0] = (0.5, 1.4)  # a thin film
+    backend.upload("transport.finishes", finishes)
     with pytest.raises(K.KdnError) as e:
         backend.render(8, 8, 1)
     assert e.value.status == K.KDN_BAD_ARG
-    backend.upload("looks.materials", blocks["looks.materials"])
+    backend.upload("transport.finishes", blocks["transport.finishes"])
+
+
+def test_bad_patterns_are_refused(backend):
+    """kdn_render checks each patterned albedo before drawing: a step that
+    reads past its program or more than 64 steps is KDN_BAD_ARG, placements
+    that do not cover every leaf KDN_NOT_READY."""
+    import kodanuki_gb300 as K
+    sc = scene("patterns_small")
+    backend.load(sc)
+    backend.build(5, 10, 64)
+    blocks = K.scene_blocks(sc)
+    backend.render(8, 8, 1)
+    steps = blocks["looks.pattern_steps"].copy()
+    k = int(np.nonzero(steps["opcode"] >= 8)[0][0])
+    steps["a"][k] = 1000
+    backend.upload("looks.pattern_steps", steps)
+    with pytest.raises(K.KdnError) as e:
+        backend.render(8, 8, 1)
+    assert e.value.status == K.KDN_BAD_ARG
+    backend.upload("looks.pattern_steps", blocks["looks.pattern_steps"])
+    pats = blocks["looks.patterns"].copy()
+    pats["count"][pats["count"] > 0] = 65
+    backend.upload("looks.patterns", pats)
+    with pytest.raises(K.KdnError) as e:
+        backend.render(8, 8, 1)
+    assert e.value.status == K.KDN_BAD_ARG
+    backend.upload("looks.patterns", blocks["looks.patterns"])
+    backend.upload("looks.placements", blocks["looks.placements"][:1])
+    with pytest.raises(K.KdnError) as e:
+        backend.render(8, 8, 1)
+    assert e.value.status == K.KDN_NOT_READY
+    backend.upload("looks.placements", blocks["looks.placements"])
+    assert np.isfinite(backend.render(8, 8, 1)).all()

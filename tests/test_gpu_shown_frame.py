@@ -62,7 +62,7 @@ def check(name, shown, want):
     assert np.median(err) <= 1e-4
 
 
-@pytest.mark.parametrize("name", ["c2_small", "room_small"])
+@pytest.mark.parametrize("name", ["c2_small", "room_small", "patterns_small"])
 def test_surfaces_match_oracle(backend, name):
     import oracle.port as op
     sc = scene(name)
