@@ -247,6 +247,20 @@ const char* kdn_last_error(const kdn_ctx* ctx);
 kdn_status kdn_open(int device, kdn_ctx** out);
 kdn_status kdn_close(kdn_ctx* ctx);
 
+/* A context that draws frames of `scene`'s built world without a copy of
+ * it: the world's device buffers are borrowed, the blocks copied, the frame
+ * buffers, streams (created at `priority`, as cudaStreamCreateWithPriority:
+ * lower is more urgent, clamped to the device's range) and counters its
+ * own, so frames of one scene run side by side on several such contexts.
+ * The scene may be neither rebuilt nor closed while a sharing context is
+ * open (KDN_BAD_ARG).  A host-only scene gives a host-only context. */
+kdn_status kdn_open_sharing(kdn_ctx* scene, int priority, kdn_ctx** out);
+
+/* The most device bytes a frame's path buffers may take on this context
+ * (0, the default: half the free device memory); a frame larger than that
+ * is drawn in more chunks. */
+kdn_status kdn_set_frame_budget(kdn_ctx* ctx, uint64_t bytes);
+
 /*
  * Copy one block into the context (core/block.h:565 Block {name, data,
  * count, size}).  Names and element sizes:
@@ -418,6 +432,80 @@ kdn_status kdn_temporal_device(kdn_ctx* ctx, const kdn_temporal_frame* frame, co
 /* Write a buffer larger than the L2 cache on the context's stream, so that
  * the next launch starts with a cold cache. */
 kdn_status kdn_flush_l2(kdn_ctx* ctx);
+
+/*
+ * The serving loop (the render host's request loop, core/plugin.h:241
+ * hostRenderer, as continuous batching): resident scenes, requests of any
+ * scene, size and spp submitted as they arrive and drawn side by side on
+ * the device, progressive sessions whose accumulation and denoiser history
+ * stay resident, admission against a device-memory budget, and the
+ * latency of every request.
+ *
+ * Each request runs on a context sharing its scene's world
+ * (kdn_open_sharing) from a pool per scene; a session keeps its own until
+ * it ends.  Up to `slots` requests are on the device at once, each on its
+ * own streams; a request is admitted, interactive requests first and each
+ * kind oldest first, when a slot is free (with more than one slot, one is
+ * kept for interactive requests) and its path buffers (its paths x 364
+ * bytes, capped at budget / slots) fit in what the running requests leave
+ * of the budget.  Interactive requests (KDN_REQUEST_INTERACTIVE) run on
+ * high-priority streams.  Latency percentiles count the requests that
+ * completed.  A frame's result
+ * equals the same request drawn alone (kdn_render on a context of the same
+ * scene).
+ */
+typedef struct kdn_server kdn_server;
+
+typedef struct kdn_serve_options {
+	int32_t device;        /* CUDA device, or KDN_HOST_ONLY (requests then end in KDN_NO_DEVICE) */
+	uint32_t slots;        /* requests on the device at once, 1..64 */
+	uint64_t budget_bytes; /* device bytes the running requests' path buffers may take; 0: 120 GB */
+} kdn_serve_options;
+
+#define KDN_REQUEST_INTERACTIVE 4u /* drawn on high-priority streams */
+
+typedef struct kdn_request {
+	uint32_t scene;   /* from kdn_serve_add_scene */
+	int32_t width, height;
+	int32_t samples;  /* a pixel, this request */
+	int32_t surfaces;
+	int32_t seed;
+	uint32_t flags;   /* KDN_FRAME_DENOISE, KDN_REQUEST_INTERACTIVE */
+	uint32_t pad_;
+	uint64_t session; /* 0: a single frame; else a progressive session: its
+	                     frames accumulate in order onto one resident frame
+	                     (and denoiser history) until kdn_serve_end_session */
+} kdn_request;
+
+typedef struct kdn_served {
+	kdn_status status;
+	uint32_t frame;     /* the session's frame index (0 for a single frame) */
+	double queued_ms;   /* submit to start */
+	double render_ms;   /* start to the result in host memory */
+	double latency_ms;  /* submit to the result */
+} kdn_served;
+
+kdn_status kdn_serve_open(const kdn_serve_options* options, kdn_server** out);
+/* Register a built scene context (it stays the caller's; close it after the server). */
+kdn_status kdn_serve_add_scene(kdn_server* server, kdn_ctx* scene, uint32_t* id);
+/* Queue a request; out_rgb (width x height x 3 floats, host) is written
+ * before kdn_serve_wait returns for its ticket. */
+kdn_status kdn_serve_submit(kdn_server* server, const kdn_request* request, float* out_rgb, uint64_t* ticket);
+/* Wait for a request (each ticket once). */
+kdn_status kdn_serve_wait(kdn_server* server, uint64_t ticket, kdn_served* out);
+/* Drop every queued request not yet started: its wait returns
+ * KDN_NOT_READY at once (requests on the device finish). */
+kdn_status kdn_serve_cancel_queued(kdn_server* server, uint64_t* cancelled);
+/* End a session: its context goes back when its frames are done. */
+kdn_status kdn_serve_end_session(kdn_server* server, uint64_t session);
+/* Latency percentiles over the requests waited for so far (all, or only
+ * the interactive ones). */
+kdn_status kdn_serve_latency(kdn_server* server, int interactive_only, double* p50_ms, double* p99_ms, uint64_t* count);
+const char* kdn_serve_last_error(const kdn_server* server);
+/* Stop the workers (after the requests on the device finish), drop what is
+ * still queued and close the server's contexts; call it once every ticket
+ * that will be waited for has been. */
+kdn_status kdn_serve_close(kdn_server* server);
 
 #ifdef __cplusplus
 }

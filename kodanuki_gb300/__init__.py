@@ -84,7 +84,26 @@ EXPORTS = [
     "kdn_status_string", "kdn_last_error", "kdn_open", "kdn_close", "kdn_upload_block", "kdn_build", "kdn_world_stats",
     "kdn_world_cell", "kdn_extend", "kdn_extend_device", "kdn_render", "kdn_render_device", "kdn_frame_stats_get", "kdn_flush_l2",
     "kdn_frame_surfaces", "kdn_frame_record", "kdn_world_march", "kdn_world_locate", "kdn_temporal_device", "kdn_denoise", "kdn_denoise_device", "kdn_denoise_static",
+    "kdn_open_sharing", "kdn_set_frame_budget", "kdn_serve_open", "kdn_serve_add_scene", "kdn_serve_submit", "kdn_serve_wait", "kdn_serve_end_session",
+    "kdn_serve_latency", "kdn_serve_last_error", "kdn_serve_close", "kdn_serve_cancel_queued",
 ]
+
+REQUEST_INTERACTIVE = 4
+
+
+class ServeOptions(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("slots", ctypes.c_uint32), ("budget_bytes", ctypes.c_uint64)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("scene", ctypes.c_uint32), ("width", ctypes.c_int32), ("height", ctypes.c_int32), ("samples", ctypes.c_int32),
+                ("surfaces", ctypes.c_int32), ("seed", ctypes.c_int32), ("flags", ctypes.c_uint32), ("pad", ctypes.c_uint32),
+                ("session", ctypes.c_uint64)]
+
+
+class Served(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("frame", ctypes.c_uint32), ("queued_ms", ctypes.c_double), ("render_ms", ctypes.c_double),
+                ("latency_ms", ctypes.c_double)]
 
 
 class DenoiseFrame(ctypes.Structure):
@@ -144,9 +163,21 @@ def library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.kdn_denoise.argtypes = [P, ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P]
     L.kdn_denoise_device.argtypes = [P, ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P, P]
     L.kdn_denoise_static.argtypes = [ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P, P]
+    L.kdn_open_sharing.argtypes = [P, ctypes.c_int, ctypes.POINTER(P)]
+    L.kdn_set_frame_budget.argtypes = [P, ctypes.c_uint64]
+    L.kdn_serve_open.argtypes = [ctypes.POINTER(ServeOptions), ctypes.POINTER(P)]
+    L.kdn_serve_add_scene.argtypes = [P, P, ctypes.POINTER(ctypes.c_uint32)]
+    L.kdn_serve_submit.argtypes = [P, ctypes.POINTER(Request), P, ctypes.POINTER(ctypes.c_uint64)]
+    L.kdn_serve_wait.argtypes = [P, ctypes.c_uint64, ctypes.POINTER(Served)]
+    L.kdn_serve_end_session.argtypes = [P, ctypes.c_uint64]
+    L.kdn_serve_latency.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64)]
+    L.kdn_serve_last_error.restype = ctypes.c_char_p
+    L.kdn_serve_last_error.argtypes = [P]
+    L.kdn_serve_close.argtypes = [P]
+    L.kdn_serve_cancel_queued.argtypes = [P, ctypes.POINTER(ctypes.c_uint64)]
     for name in EXPORTS:
         fn = getattr(L, name)
-        if name not in ("kdn_status_string", "kdn_last_error"):
+        if name not in ("kdn_status_string", "kdn_last_error", "kdn_serve_last_error"):
             fn.restype = ctypes.c_int
     _lib = L
     return L
@@ -329,6 +360,19 @@ class Backend:
         self._check(self.lib.kdn_render(self.handle, ctypes.byref(f), _ptr(out)))
         return out
 
+    def share(self, priority: int = 0) -> "Backend":
+        """A context drawing this one's world (include/kdn.h kdn_open_sharing);
+        close it before this one."""
+        b = Backend.__new__(Backend)
+        b.lib = self.lib
+        b.handle = ctypes.c_void_p()
+        self._check(self.lib.kdn_open_sharing(self.handle, priority, ctypes.byref(b.handle)))
+        b.scene = self.scene
+        return b
+
+    def set_frame_budget(self, nbytes: int) -> None:
+        self._check(self.lib.kdn_set_frame_budget(self.handle, nbytes))
+
     def frame_stats(self) -> FrameStats:
         s = FrameStats()
         self._check(self.lib.kdn_frame_stats_get(self.handle, ctypes.byref(s)))
@@ -393,3 +437,71 @@ class Backend:
         out = np.zeros((width * height, 3), np.float32)
         self._check(self.lib.kdn_denoise(self.handle, ctypes.byref(f), *[_ptr(a) for a in arrs], _ptr(out)))
         return out
+
+
+class Server:
+    """The serving loop (include/kdn.h kdn_serve_*): resident scenes,
+    requests submitted as they arrive and drawn side by side, progressive
+    sessions, latency percentiles."""
+
+    def __init__(self, device: int = 0, slots: int = 4, budget_bytes: int = 0):
+        self.lib = library()
+        self.handle = ctypes.c_void_p()
+        o = ServeOptions(device, slots, budget_bytes)
+        st = self.lib.kdn_serve_open(ctypes.byref(o), ctypes.byref(self.handle))
+        if st != KDN_OK:
+            raise KdnError(st, "kdn_serve_open")
+        self.outputs: dict[int, np.ndarray] = {}
+        self.scenes: list[Backend] = []
+
+    def _check(self, st: int) -> None:
+        if st != KDN_OK:
+            raise KdnError(st, self.lib.kdn_serve_last_error(self.handle).decode())
+
+    def add_scene(self, backend: "Backend") -> int:
+        """Register a built scene (the Backend stays open until the server closes)."""
+        sid = ctypes.c_uint32()
+        self._check(self.lib.kdn_serve_add_scene(self.handle, backend.handle, ctypes.byref(sid)))
+        self.scenes.append(backend)
+        return int(sid.value)
+
+    def submit(self, scene: int, width: int, height: int, samples: int, surfaces: int = 8, seed: int = 1, denoise: bool = False,
+               interactive: bool = False, session: int = 0) -> int:
+        r = Request(scene, width, height, samples, surfaces, seed, (FRAME_DENOISE if denoise else 0) | (REQUEST_INTERACTIVE if interactive else 0), 0, session)
+        out = np.zeros((height, width, 3), np.float32)
+        ticket = ctypes.c_uint64()
+        self._check(self.lib.kdn_serve_submit(self.handle, ctypes.byref(r), _ptr(out), ctypes.byref(ticket)))
+        self.outputs[int(ticket.value)] = out
+        return int(ticket.value)
+
+    def wait(self, ticket: int) -> tuple[int, dict, np.ndarray]:
+        """(status, {frame, queued_ms, render_ms, latency_ms}, image)."""
+        served = Served()
+        self.lib.kdn_serve_wait(self.handle, ticket, ctypes.byref(served))
+        out = self.outputs.pop(ticket)
+        return int(served.status), {"frame": int(served.frame), "queued_ms": served.queued_ms, "render_ms": served.render_ms,
+                                    "latency_ms": served.latency_ms}, out
+
+    def end_session(self, session: int) -> None:
+        self._check(self.lib.kdn_serve_end_session(self.handle, session))
+
+    def cancel_queued(self) -> int:
+        n = ctypes.c_uint64()
+        self._check(self.lib.kdn_serve_cancel_queued(self.handle, ctypes.byref(n)))
+        return int(n.value)
+
+    def latency(self, interactive_only: bool = False) -> dict:
+        p50, p99, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_uint64()
+        self._check(self.lib.kdn_serve_latency(self.handle, 1 if interactive_only else 0, ctypes.byref(p50), ctypes.byref(p99), ctypes.byref(n)))
+        return {"p50_ms": p50.value, "p99_ms": p99.value, "count": int(n.value)}
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.kdn_serve_close(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __enter__(self) -> "Server":
+        return self
+
+    def __exit__(self, *exc) -> None:
+        self.close()

@@ -109,9 +109,46 @@ kdn_status kdn_open(int device, kdn_ctx** out) {
 	return KDN_OK;
 }
 
+kdn_status kdn_open_sharing(kdn_ctx* scene, int priority, kdn_ctx** out) {
+	if (scene == nullptr || out == nullptr) return KDN_BAD_ARG;
+	*out          = nullptr;
+	Context* from = reinterpret_cast<Context*>(scene);
+	std::lock_guard<std::mutex> guard(from->lock);
+	if (!from->built) return from->fail(KDN_NOT_READY, "kdn_open_sharing: the scene has no world built (kdn_build)");
+	if (from->source != nullptr) return from->fail(KDN_BAD_ARG, "kdn_open_sharing: the scene itself shares another context's world");
+	Context* ctx = new (std::nothrow) Context();
+	if (ctx == nullptr) return KDN_OOM;
+	ctx->device   = from->device;
+	ctx->priority = priority;
+	if (ctx->device >= 0) {
+		int least = 0, greatest = 0;
+		cudaDeviceGetStreamPriorityRange(&least, &greatest);
+		ctx->priority = std::min(std::max(priority, greatest), least);
+		const kdn_status s = ctx->open();
+		if (s != KDN_OK) {
+			from->error = ctx->error;
+			ctx->release();
+			delete ctx;
+			return s;
+		}
+	}
+	ctx->share(from);
+	*out = reinterpret_cast<kdn_ctx*>(ctx);
+	return KDN_OK;
+}
+
+kdn_status kdn_set_frame_budget(kdn_ctx* handle, uint64_t bytes) {
+	if (handle == nullptr) return KDN_BAD_ARG;
+	Context* ctx = reinterpret_cast<Context*>(handle);
+	std::lock_guard<std::mutex> guard(ctx->lock);
+	ctx->frameBudget = bytes;
+	return KDN_OK;
+}
+
 kdn_status kdn_close(kdn_ctx* handle) {
 	if (handle == nullptr) return KDN_BAD_ARG;
 	Context* ctx = reinterpret_cast<Context*>(handle);
+	if (ctx->sharers.load() > 0) return ctx->fail(KDN_BAD_ARG, "kdn_close: other contexts still draw this one's world (close them first)");
 	{
 		std::lock_guard<std::mutex> guard(ctx->lock);
 		ctx->release();
@@ -141,6 +178,8 @@ kdn_status kdn_build(kdn_ctx* handle, const kdn_build_options* options) {
 	if (handle == nullptr) return KDN_BAD_ARG;
 	Context* ctx = reinterpret_cast<Context*>(handle);
 	std::lock_guard<std::mutex> guard(ctx->lock);
+	if (ctx->sharers.load() > 0) return ctx->fail(KDN_BAD_ARG, "kdn_build: other contexts draw this one's world (close them first)");
+	if (ctx->source != nullptr) return ctx->fail(KDN_BAD_ARG, "kdn_build: this context draws another's world");
 	kdn::BuildOptions o;
 	if (options != nullptr) {
 		if (options->min_depth < 0 || options->max_depth < options->min_depth || options->max_depth > 24) return ctx->fail(KDN_BAD_ARG, "kdn_build: depths out of range");
@@ -154,6 +193,7 @@ kdn_status kdn_build(kdn_ctx* handle, const kdn_build_options* options) {
 kdn_status kdn_world_stats(kdn_ctx* handle, uint64_t out[4]) {
 	if (handle == nullptr || out == nullptr) return KDN_BAD_ARG;
 	Context* ctx = reinterpret_cast<Context*>(handle);
+	if (ctx->source != nullptr) ctx = ctx->source; // a sharing context reads its scene's world
 	std::lock_guard<std::mutex> guard(ctx->lock);
 	if (!ctx->built) return ctx->fail(KDN_NOT_READY, "kdn_world_stats: no world built");
 	out[0] = ctx->octree.cells.size();
@@ -166,6 +206,7 @@ kdn_status kdn_world_stats(kdn_ctx* handle, uint64_t out[4]) {
 kdn_status kdn_world_cell(kdn_ctx* handle, uint64_t i, uint32_t head[6], uint32_t* objects, uint32_t* results, uint32_t* counts, kdn_step* steps, size_t capacity) {
 	if (handle == nullptr || head == nullptr) return KDN_BAD_ARG;
 	Context* ctx = reinterpret_cast<Context*>(handle);
+	if (ctx->source != nullptr) ctx = ctx->source; // a sharing context reads its scene's world
 	std::lock_guard<std::mutex> guard(ctx->lock);
 	if (!ctx->built) return ctx->fail(KDN_NOT_READY, "kdn_world_cell: no world built");
 	const int64_t at = ctx->preorderCell(i);

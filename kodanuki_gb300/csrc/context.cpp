@@ -11,19 +11,39 @@ kdn_status Context::open() {
 	if (!check(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties")) return KDN_NO_DEVICE;
 	smCount = prop.multiProcessorCount;
 	if (!check(setTraceAttributes(), "the trace kernel is not built for this device")) return KDN_NO_DEVICE;
-	if (!check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate")) return KDN_CUDA_ERROR;
+	if (!check(cudaStreamCreateWithPriority(&stream, cudaStreamNonBlocking, priority), "cudaStreamCreate")) return KDN_CUDA_ERROR;
 	kdn_status s = ensure(counters, 8 * sizeof(unsigned long long));
 	if (s != KDN_OK) return s;
 	return ensure(fetch, 256);
 }
 
+// Draw frames of `from`'s built world: its world buffers are borrowed (not
+// copied, not freed here), its blocks copied; the frame buffers, streams and
+// counters are this context's own.
+kdn_status Context::share(Context* from) {
+	blocks = from->blocks;
+	world  = from->world;
+	for (auto pair : { std::make_pair(&leafMaterial, &from->leafMaterial), std::make_pair(&objectMaterial, &from->objectMaterial) }) {
+		*pair.first          = *pair.second;
+		pair.first->borrowed = true;
+	}
+	built        = from->built;
+	sceneChanged = false;
+	source       = from;
+	from->sharers.fetch_add(1);
+	return KDN_OK;
+}
+
 static void freeBuffer(DeviceBuffer& b) {
-	if (b.ptr) cudaFree(b.ptr);
-	b.ptr   = nullptr;
-	b.bytes = 0;
+	if (b.ptr && !b.borrowed) cudaFree(b.ptr);
+	b.ptr      = nullptr;
+	b.bytes    = 0;
+	b.borrowed = false;
 }
 
 void Context::release() {
+	if (source) source->sharers.fetch_sub(1);
+	source = nullptr;
 	if (device < 0) return;
 	cudaSetDevice(device);
 	if (stream) cudaStreamSynchronize(stream);

@@ -7,6 +7,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -17,8 +18,9 @@ namespace kdn {
 
 // A device allocation that grows on demand and is freed with the context.
 struct DeviceBuffer {
-	void* ptr    = nullptr;
-	size_t bytes = 0;
+	void* ptr     = nullptr;
+	size_t bytes  = 0;
+	bool borrowed = false; // another context's: not freed with this one
 };
 
 struct FrameState; // render.cpp
@@ -27,6 +29,12 @@ struct Context {
 	int device          = 0;
 	int smCount         = 0;
 	cudaStream_t stream = nullptr;
+	int priority        = 0; // of this context's streams (cudaStreamCreateWithPriority)
+	// a context that draws frames of another's world (kdn_open_sharing)
+	Context* source = nullptr;
+	std::atomic<int> sharers { 0 }; // contexts drawing this one's world
+	// the most device bytes a frame's path buffers may take (0: half the free memory)
+	uint64_t frameBudget = 0;
 	std::mutex lock;
 	std::string error;
 	std::map<std::string, std::vector<uint8_t>> blocks;
@@ -46,6 +54,7 @@ struct Context {
 	FrameState* frame = nullptr;
 
 	kdn_status open();
+	kdn_status share(Context* from);
 	void release();
 	kdn_status fail(kdn_status status, const std::string& message);
 	bool check(cudaError_t e, const char* what);

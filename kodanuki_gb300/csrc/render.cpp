@@ -258,8 +258,10 @@ uint64_t chunkPaths(Context* ctx, uint64_t framePaths) {
 	size_t freeBytes = 0, totalBytes = 0;
 	if (cudaMemGetInfo(&freeBytes, &totalBytes) != cudaSuccess) freeBytes = 0;
 	const uint64_t held = ctx->frame ? uint64_t(ctx->frame->capacity) * kLanes * kPathBytes : 0;
-	const uint64_t room = (uint64_t(freeBytes) + held) / 2 / kPathBytes;
-	return std::min<uint64_t>(framePaths, std::min<uint64_t>(uint64_t(1) << 28, std::max<uint64_t>(room, uint64_t(1) << 20)));
+	uint64_t room = (uint64_t(freeBytes) + held) / 2 / kPathBytes;
+	if (ctx->frameBudget > 0) room = std::min<uint64_t>(room, ctx->frameBudget / kPathBytes);
+	const uint64_t least = ctx->frameBudget > 0 ? uint64_t(1) << 16 : uint64_t(1) << 20;
+	return std::min<uint64_t>(framePaths, std::min<uint64_t>(uint64_t(1) << 28, std::max<uint64_t>(room, least)));
 }
 
 // The path buffers for a chunk of `capacity` paths on each lane.
@@ -433,7 +435,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	if (!ctx->check(cudaMemsetAsync(counts, 0, kLanes * 4 * sizeof(uint32_t), stream), "clear counts")) return KDN_CUDA_ERROR;
 	cudaStream_t lanes[kLanes] = { stream };
 	for (int l = 1; l < kLanes; ++l) {
-		if (f.side[l - 1] == nullptr && !ctx->check(cudaStreamCreateWithFlags(&f.side[l - 1], cudaStreamNonBlocking), "cudaStreamCreate")) return KDN_CUDA_ERROR;
+		if (f.side[l - 1] == nullptr && !ctx->check(cudaStreamCreateWithPriority(&f.side[l - 1], cudaStreamNonBlocking, ctx->priority), "cudaStreamCreate")) return KDN_CUDA_ERROR;
 		if (f.ended[l - 1] == nullptr && !ctx->check(cudaEventCreateWithFlags(&f.ended[l - 1], cudaEventDisableTiming), "cudaEventCreate")) return KDN_CUDA_ERROR;
 		lanes[l] = f.side[l - 1];
 	}

@@ -11,6 +11,7 @@ using kdn::Context;
 extern "C" kdn_status kdn_world_march(kdn_ctx* handle, uint64_t i, const float* points, uint32_t n, float* values, size_t capacity, uint32_t* programs) {
 	if (handle == nullptr || programs == nullptr || (n > 0 && (points == nullptr || values == nullptr))) return KDN_BAD_ARG;
 	Context* ctx = reinterpret_cast<Context*>(handle);
+	if (ctx->source != nullptr) ctx = ctx->source; // a sharing context reads its scene's world
 	std::lock_guard<std::mutex> guard(ctx->lock);
 	if (!ctx->built) return ctx->fail(KDN_NOT_READY, "kdn_world_march: no world built");
 	if (ctx->flat.nodes.empty()) return ctx->fail(KDN_NOT_READY, "kdn_world_march: no device layout: " + ctx->flatError);
@@ -39,6 +40,7 @@ extern "C" kdn_status kdn_world_march(kdn_ctx* handle, uint64_t i, const float* 
 extern "C" kdn_status kdn_world_locate(kdn_ctx* handle, const float* points, uint32_t n, uint32_t* by_grid, uint32_t* by_descent) {
 	if (handle == nullptr || (n > 0 && (points == nullptr || by_grid == nullptr || by_descent == nullptr))) return KDN_BAD_ARG;
 	Context* ctx = reinterpret_cast<Context*>(handle);
+	if (ctx->source != nullptr) ctx = ctx->source; // a sharing context reads its scene's world
 	std::lock_guard<std::mutex> guard(ctx->lock);
 	if (!ctx->built) return ctx->fail(KDN_NOT_READY, "kdn_world_locate: no world built");
 	if (ctx->flat.nodes.empty()) return ctx->fail(KDN_NOT_READY, "kdn_world_locate: no device layout: " + ctx->flatError);
