@@ -293,10 +293,100 @@ def run_gpu(args) -> None:
                 line["cpu_baseline"] = cpu_baseline(scene)
             except Exception as e:  # the oracle is test infrastructure; report why it could not run
                 line["cpu_baseline"] = {"value": None, "unit": "Msamples/s", "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {e}"}
+        if not (args.no_cpu or args.no_serve):
+            try:
+                line["serving"] = serving(b)
+            except Exception as e:  # report why the serving run could not finish
+                line["serving"] = {"failed": str(e)}
         print(json.dumps(line), flush=True)
     b.close()
     if dist:
         dist.destroy_process_group()
+
+
+# The serving run (bounded): Poisson arrivals over four
+# resident scenes for a fixed window; 70% single frames of a uniform
+# resolution in {320x240, 640x480, 1280x720, 1920x1080} and spp in
+# {1, 4, 16, 64}, 30% frames of four progressive 1280x720 sessions at 1 spp
+# with the denoiser's history (interactive).  What is still queued when the
+# window closes is cancelled; latency is over the completed requests.
+SERVE_SCENES = ["c1", "room", "glow_small"]  # beside config 2, already resident
+SERVE_RATE, SERVE_WINDOW_S, SERVE_SLOTS, SERVE_SESSIONS = 200.0, 5.0, 4, 4
+SERVE_SIZES = [(320, 240), (640, 480), (1280, 720), (1920, 1080)]
+SERVE_SPP = [1, 4, 16, 64]
+
+
+def serving(main_backend) -> dict:
+    import kodanuki_gb300 as K
+    from kodanuki_gb300.scene import Scene
+    rng = np.random.default_rng(2024)
+    backends = [main_backend]
+    for name in SERVE_SCENES:
+        b = K.Backend(0)
+        b.load(Scene.load(os.path.join(ROOT, "tests", "golden", "scenes", name + ".npz")))
+        b.build(min_depth=6, max_depth=10, split_steps=64)
+        backends.append(b)
+    srv = K.Server(0, slots=SERVE_SLOTS)
+    ids = [srv.add_scene(b) for b in backends]
+    session_scene = [ids[k % len(ids)] for k in range(SERVE_SESSIONS)]
+    # warm-up (not counted): each session's first frame and a frame of each
+    # scene, which open the contexts and their buffers
+    warm = [srv.submit(session_scene[k], 1280, 720, 1, surfaces=8, seed=7 + k, denoise=True, interactive=True, session=k + 1) for k in range(SERVE_SESSIONS)]
+    warm += [srv.submit(i, 640, 480, 1, surfaces=8, seed=1) for i in ids]
+    for t in warm:
+        srv.wait(t)
+    srv.reset_latency()
+    tickets, kinds = [], []
+    t0 = time.perf_counter()
+    next_at = 0.0
+    samples_of = {}
+    while True:
+        next_at += rng.exponential(1.0 / SERVE_RATE)
+        if next_at > SERVE_WINDOW_S:
+            break
+        delay = t0 + next_at - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        if rng.random() < 0.3:
+            k = int(rng.integers(SERVE_SESSIONS))
+            t = srv.submit(session_scene[k], 1280, 720, 1, surfaces=8, seed=7 + k, denoise=True, interactive=True, session=k + 1)
+            kinds.append("interactive")
+            samples_of[t] = 1280 * 720
+        else:
+            w, h = SERVE_SIZES[int(rng.integers(4))]
+            spp = SERVE_SPP[int(rng.integers(4))]
+            t = srv.submit(ids[int(rng.integers(len(ids)))], w, h, spp, surfaces=8, seed=int(rng.integers(1 << 30)))
+            kinds.append("batch")
+            samples_of[t] = w * h * spp
+        tickets.append(t)
+    cancelled = srv.cancel_queued()
+    done_samples, completed, statuses = 0, {"interactive": 0, "batch": 0}, []
+    for t, kind in zip(tickets, kinds):
+        st, served, _ = srv.wait(t)
+        statuses.append(st)
+        if st == K.KDN_OK:
+            completed[kind] += 1
+            done_samples += samples_of[t]
+    wall = time.perf_counter() - t0
+    inter, every = srv.latency(True), srv.latency(False)
+    for k in range(SERVE_SESSIONS):
+        try:
+            srv.end_session(k + 1)
+        except K.KdnError:
+            pass
+    srv.close()
+    for b in backends[1:]:
+        b.close()
+    return {
+        "workload": f"Poisson {SERVE_RATE:.0f}/s for {SERVE_WINDOW_S:.0f} s over {len(ids)} resident scenes (config 2, {', '.join(SERVE_SCENES)}); "
+                    f"70% frames of {{320x240,640x480,1280x720,1920x1080}} x {{1,4,16,64}} spp, 30% frames of {SERVE_SESSIONS} progressive "
+                    f"1280x720 1-spp denoised interactive sessions; {SERVE_SLOTS} slots, 120 GB budget; queued requests cancelled at the window's end",
+        "submitted": len(tickets), "completed": completed, "cancelled": int(cancelled),
+        "failed": int(sum(1 for st in statuses if st not in (K.KDN_OK, K.KDN_NOT_READY))),
+        "msamples_per_s": done_samples / wall / 1e6, "wall_s": wall,
+        "interactive_720p_1spp_ms": {"p50": inter["p50_ms"], "p99": inter["p99_ms"], "count": inter["count"]},
+        "all_ms": {"p50": every["p50_ms"], "p99": every["p99_ms"], "count": every["count"]},
+    }
 
 
 def main() -> None:
@@ -309,7 +399,8 @@ def main() -> None:
     ap.add_argument("--width", type=int, default=WIDTH, help="a smaller frame for profiling captures only")
     ap.add_argument("--height", type=int, default=HEIGHT)
     ap.add_argument("--spp", type=int, default=SPP)
-    ap.add_argument("--no-cpu", action="store_true", help="leave out the CPU baseline (profiling captures)")
+    ap.add_argument("--no-cpu", action="store_true", help="leave out the CPU baseline and the serving run (profiling captures)")
+    ap.add_argument("--no-serve", action="store_true", help="leave out the serving run")
     args = ap.parse_args()
     WIDTH, HEIGHT, SPP = args.width, args.height, args.spp
     if args.impl == "reference":

@@ -261,6 +261,10 @@ kdn_status kdn_open_sharing(kdn_ctx* scene, int priority, kdn_ctx** out);
  * is drawn in more chunks. */
 kdn_status kdn_set_frame_budget(kdn_ctx* ctx, uint64_t bytes);
 
+/* Size this context's kernel grids for `sms` SMs (0: all of the device's),
+ * so its frames leave the other SMs to work on other streams. */
+kdn_status kdn_set_sm_limit(kdn_ctx* ctx, int sms);
+
 /*
  * Copy one block into the context (core/block.h:565 Block {name, data,
  * count, size}).  Names and element sizes:
@@ -449,7 +453,9 @@ kdn_status kdn_flush_l2(kdn_ctx* ctx);
  * kept for interactive requests) and its path buffers (its paths x 364
  * bytes, capped at budget / slots) fit in what the running requests leave
  * of the budget.  Interactive requests (KDN_REQUEST_INTERACTIVE) run on
- * high-priority streams.  Latency percentiles count the requests that
+ * high-priority streams; with more than one slot the others' grids are
+ * sized for three quarters of the SMs, so an interactive frame finds SMs
+ * free.  Latency percentiles count the requests that
  * completed.  A frame's result
  * equals the same request drawn alone (kdn_render on a context of the same
  * scene).
@@ -501,6 +507,8 @@ kdn_status kdn_serve_end_session(kdn_server* server, uint64_t session);
 /* Latency percentiles over the requests waited for so far (all, or only
  * the interactive ones). */
 kdn_status kdn_serve_latency(kdn_server* server, int interactive_only, double* p50_ms, double* p99_ms, uint64_t* count);
+/* Forget the latencies counted so far (after a warm-up). */
+kdn_status kdn_serve_reset_latency(kdn_server* server);
 const char* kdn_serve_last_error(const kdn_server* server);
 /* Stop the workers (after the requests on the device finish), drop what is
  * still queued and close the server's contexts; call it once every ticket

@@ -85,7 +85,7 @@ EXPORTS = [
     "kdn_world_cell", "kdn_extend", "kdn_extend_device", "kdn_render", "kdn_render_device", "kdn_frame_stats_get", "kdn_flush_l2",
     "kdn_frame_surfaces", "kdn_frame_record", "kdn_world_march", "kdn_world_locate", "kdn_temporal_device", "kdn_denoise", "kdn_denoise_device", "kdn_denoise_static",
     "kdn_open_sharing", "kdn_set_frame_budget", "kdn_serve_open", "kdn_serve_add_scene", "kdn_serve_submit", "kdn_serve_wait", "kdn_serve_end_session",
-    "kdn_serve_latency", "kdn_serve_last_error", "kdn_serve_close", "kdn_serve_cancel_queued",
+    "kdn_serve_latency", "kdn_serve_last_error", "kdn_serve_close", "kdn_serve_cancel_queued", "kdn_set_sm_limit", "kdn_serve_reset_latency",
 ]
 
 REQUEST_INTERACTIVE = 4
@@ -165,6 +165,8 @@ def library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.kdn_denoise_static.argtypes = [ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P, P]
     L.kdn_open_sharing.argtypes = [P, ctypes.c_int, ctypes.POINTER(P)]
     L.kdn_set_frame_budget.argtypes = [P, ctypes.c_uint64]
+    L.kdn_set_sm_limit.argtypes = [P, ctypes.c_int]
+    L.kdn_serve_reset_latency.argtypes = [P]
     L.kdn_serve_open.argtypes = [ctypes.POINTER(ServeOptions), ctypes.POINTER(P)]
     L.kdn_serve_add_scene.argtypes = [P, P, ctypes.POINTER(ctypes.c_uint32)]
     L.kdn_serve_submit.argtypes = [P, ctypes.POINTER(Request), P, ctypes.POINTER(ctypes.c_uint64)]
@@ -484,6 +486,9 @@ class Server:
 
     def end_session(self, session: int) -> None:
         self._check(self.lib.kdn_serve_end_session(self.handle, session))
+
+    def reset_latency(self) -> None:
+        self._check(self.lib.kdn_serve_reset_latency(self.handle))
 
     def cancel_queued(self) -> int:
         n = ctypes.c_uint64()

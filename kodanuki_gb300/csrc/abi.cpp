@@ -145,6 +145,14 @@ kdn_status kdn_set_frame_budget(kdn_ctx* handle, uint64_t bytes) {
 	return KDN_OK;
 }
 
+kdn_status kdn_set_sm_limit(kdn_ctx* handle, int sms) {
+	if (handle == nullptr || sms < 0) return KDN_BAD_ARG;
+	Context* ctx = reinterpret_cast<Context*>(handle);
+	std::lock_guard<std::mutex> guard(ctx->lock);
+	if (ctx->device >= 0) ctx->smCount = sms == 0 ? ctx->deviceSms : std::min(sms, ctx->deviceSms);
+	return KDN_OK;
+}
+
 kdn_status kdn_close(kdn_ctx* handle) {
 	if (handle == nullptr) return KDN_BAD_ARG;
 	Context* ctx = reinterpret_cast<Context*>(handle);

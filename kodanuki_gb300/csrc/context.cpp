@@ -9,7 +9,8 @@ kdn_status Context::open() {
 	if (!check(cudaSetDevice(device), "cudaSetDevice")) return KDN_NO_DEVICE;
 	cudaDeviceProp prop;
 	if (!check(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties")) return KDN_NO_DEVICE;
-	smCount = prop.multiProcessorCount;
+	smCount   = prop.multiProcessorCount;
+	deviceSms = prop.multiProcessorCount;
 	if (!check(setTraceAttributes(), "the trace kernel is not built for this device")) return KDN_NO_DEVICE;
 	if (!check(cudaStreamCreateWithPriority(&stream, cudaStreamNonBlocking, priority), "cudaStreamCreate")) return KDN_CUDA_ERROR;
 	kdn_status s = ensure(counters, 8 * sizeof(unsigned long long));

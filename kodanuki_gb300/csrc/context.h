@@ -27,7 +27,8 @@ struct FrameState; // render.cpp
 
 struct Context {
 	int device          = 0;
-	int smCount         = 0;
+	int smCount         = 0; // SMs the kernels' grids are sized for (kdn_set_sm_limit)
+	int deviceSms       = 0; // the device's
 	cudaStream_t stream = nullptr;
 	int priority        = 0; // of this context's streams (cudaStreamCreateWithPriority)
 	// a context that draws frames of another's world (kdn_open_sharing)

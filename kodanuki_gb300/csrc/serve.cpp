@@ -10,6 +10,8 @@
 // it draws one frame at a time, this one as many as there are slots.
 #include "kdn.h"
 
+#include <cuda_runtime.h>
+
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -68,6 +70,7 @@ struct kdn_server {
 	uint32_t slots    = 1;
 	uint64_t budget   = 0;
 	uint64_t slotCap  = 0; // the most path-buffer bytes one request takes
+	int sms           = 0; // the device's SMs
 	std::mutex m;
 	std::condition_variable work, finished;
 	std::vector<Scene> scenes;
@@ -183,6 +186,8 @@ void serveLoop(kdn_server* S) {
 		if (fresh) {
 			status = kdn_open_sharing(sceneCtx, interactive ? kInteractivePriority : 0, &ctx);
 			if (status == KDN_OK) status = kdn_set_frame_budget(ctx, S->slotCap);
+			// the batch frames leave a quarter of the SMs to interactive ones
+			if (status == KDN_OK && !interactive && S->slots > 1 && S->sms > 0) status = kdn_set_sm_limit(ctx, S->sms * 3 / 4);
 			if (status != KDN_OK) why = kdn_last_error(sceneCtx);
 		}
 		if (status == KDN_OK) {
@@ -247,6 +252,10 @@ kdn_status kdn_serve_open(const kdn_serve_options* options, kdn_server** out) {
 	S->slots   = options->slots;
 	S->budget  = options->budget_bytes ? options->budget_bytes : uint64_t(120) << 30;
 	S->slotCap = std::max<uint64_t>(S->budget / S->slots, uint64_t(64) << 20);
+	if (S->device >= 0 && cudaDeviceGetAttribute(&S->sms, cudaDevAttrMultiProcessorCount, S->device) != cudaSuccess) {
+		cudaGetLastError();
+		S->sms = 0;
+	}
 	for (uint32_t k = 0; k < S->slots; ++k) S->workers.emplace_back(serveLoop, S);
 	*out = S;
 	return KDN_OK;
@@ -356,6 +365,14 @@ kdn_status kdn_serve_latency(kdn_server* S, int interactive_only, double* p50_ms
 	*p50_ms = percentile(v, 0.50);
 	*p99_ms = percentile(v, 0.99);
 	*count  = v.size();
+	return KDN_OK;
+}
+
+kdn_status kdn_serve_reset_latency(kdn_server* S) {
+	if (S == nullptr) return KDN_BAD_ARG;
+	std::lock_guard<std::mutex> guard(S->m);
+	S->latencies.clear();
+	S->interactiveLatencies.clear();
 	return KDN_OK;
 }
 
