@@ -86,6 +86,7 @@ struct Looks {
 	const PatternStep* patternSteps;
 	const float* stops;
 	const float* boundaries;
+	uint32_t materialCount;
 };
 
 struct FrameConstants {
@@ -160,14 +161,13 @@ struct SurfaceArgs {
 	uint32_t* leaf;
 };
 
-cudaError_t uploadFrameConstants(const FrameConstants& c, cudaStream_t stream);
-cudaError_t launchCamera(const PathBuffers& paths, const QueueBuffers& queue, uint32_t firstPixel, uint32_t n, cudaStream_t stream, int smCount);
-cudaError_t launchShade(const ShadeArgs& args, cudaStream_t stream, int smCount);
+cudaError_t launchCamera(const FrameConstants& frame, const PathBuffers& paths, const QueueBuffers& queue, uint32_t firstPixel, uint32_t n, cudaStream_t stream, int smCount);
+cudaError_t launchShade(const FrameConstants& frame, const ShadeArgs& args, cudaStream_t stream, int smCount);
 cudaError_t launchLines(const PathBuffers& paths, const ShadowBuffers& shadow, uint32_t capacity, cudaStream_t stream, int smCount);
 // light (may be null): each pixel's mean of this call's samples, RGB float
-cudaError_t launchFold(const PathBuffers& paths, uint32_t firstPixel, uint32_t pixels, uint32_t spp, double* sums, float* light, cudaStream_t stream, int smCount);
+cudaError_t launchFold(const FrameConstants& frame, const PathBuffers& paths, uint32_t firstPixel, uint32_t pixels, uint32_t spp, double* sums, float* light, cudaStream_t stream, int smCount);
 cudaError_t launchMeans(const double* sums, uint32_t pixels, double taken, float* out, cudaStream_t stream, int smCount);
-cudaError_t launchSurfaceRays(const QueueBuffers& queue, uint32_t firstPixel, uint32_t n, cudaStream_t stream, int smCount);
+cudaError_t launchSurfaceRays(const FrameConstants& frame, const QueueBuffers& queue, uint32_t firstPixel, uint32_t n, cudaStream_t stream, int smCount);
 cudaError_t launchSurfaces(const SurfaceArgs& args, uint32_t n, cudaStream_t stream, int smCount);
 
 } // namespace kdn

@@ -375,7 +375,6 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		put(c.ground, v3(skies[0].ground));
 	}
 	buildSpectralTables(c.spectral);
-	if (!ctx->check(uploadFrameConstants(c, stream), "frame constants")) return KDN_CUDA_ERROR;
 	std::vector<DeviceMaterial> dm;
 	for (size_t k = 0; k < mats.size(); ++k) dm.push_back(materialOf(mats[k], finishes[k]));
 	// material/energy.h Boundary of each rough glass that loses much
@@ -414,6 +413,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	looks.patternSteps   = static_cast<const PatternStep*>(f.patternSteps.ptr);
 	looks.stops          = static_cast<const float*>(f.stops.ptr);
 	looks.boundaries     = static_cast<const float*>(f.boundaries.ptr);
+	looks.materialCount  = uint32_t(dm.size());
 	if ((s = ctx->ensure(ctx->counters, 8 * sizeof(unsigned long long))) != KDN_OK) return s;
 	if (!ctx->check(cudaMemsetAsync(ctx->counters.ptr, 0, 8 * sizeof(unsigned long long), stream), "clear counters")) return KDN_CUDA_ERROR;
 
@@ -500,7 +500,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		const Lane& L = lane[0];
 		for (uint32_t first = 0; first < pixels; first += capacity) {
 			const uint32_t n = std::min(capacity, pixels - first);
-			if (!ctx->check(launchSurfaceRays(L.Q[0], first, n, stream, ctx->smCount), "surface rays kernel")) return KDN_CUDA_ERROR;
+			if (!ctx->check(launchSurfaceRays(c, L.Q[0], first, n, stream, ctx->smCount), "surface rays kernel")) return KDN_CUDA_ERROR;
 			TraceArgs t;
 			t.world          = ctx->world;
 			t.rays           = L.Q[0].rays;
@@ -545,7 +545,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		const uint32_t chunk     = std::min(chunkPixels, pixels - first);
 		const uint32_t n         = chunk * spp;
 		const PathBuffers& LP    = L.P;
-		if (!ctx->check(launchCamera(LP, L.Q[0], first, n, on, ctx->smCount), "camera kernel")) return KDN_CUDA_ERROR;
+		if (!ctx->check(launchCamera(c, LP, L.Q[0], first, n, on, ctx->smCount), "camera kernel")) return KDN_CUDA_ERROR;
 		++launches;
 		if (!ctx->check(cudaMemsetAsync(L.S.count, 0, 4, on), "clear lines")) return KDN_CUDA_ERROR;
 		int q = 0;
@@ -605,11 +605,11 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 			a.firstNormal   = denoised ? static_cast<uint16_t*>(f.firstNormal.ptr) : nullptr;
 			a.firstAlbedo   = denoised ? static_cast<uint16_t*>(f.firstAlbedo.ptr) : nullptr;
 			a.firstLeaf     = denoised ? static_cast<uint32_t*>(f.firstLeaf.ptr) : nullptr;
-			if (!ctx->check(launchShade(a, on, ctx->smCount), "shade kernel")) return KDN_CUDA_ERROR;
+			if (!ctx->check(launchShade(c, a, on, ctx->smCount), "shade kernel")) return KDN_CUDA_ERROR;
 			++launches;
 			q = nxt;
 		}
-		if (!ctx->check(launchFold(LP, first, chunk, spp, static_cast<double*>(f.sums.ptr), denoised ? static_cast<float*>(f.frameLight.ptr) : nullptr, on, ctx->smCount), "fold kernel")) return KDN_CUDA_ERROR;
+		if (!ctx->check(launchFold(c, LP, first, chunk, spp, static_cast<double*>(f.sums.ptr), denoised ? static_cast<float*>(f.frameLight.ptr) : nullptr, on, ctx->smCount), "fold kernel")) return KDN_CUDA_ERROR;
 		++launches;
 	}
 	// the first lane goes on once the others are done

@@ -23,7 +23,10 @@
 
 namespace kdn {
 
-__constant__ FrameConstants cFrame;
+// The frame's constants travel with each launch as a kernel parameter
+// (__grid_constant__, read through the constant bank), so frames of
+// several contexts can run at once without one's constants overwriting
+// another's.
 
 namespace {
 
@@ -47,7 +50,7 @@ __device__ __forceinline__ float number(uint64_t stream, uint32_t index, int eve
 }
 
 // plugins/transport/paths/trace.cpp:66 pixelNumbers
-__device__ __forceinline__ uint64_t streamOf(uint32_t x, uint32_t y) {
+__device__ __forceinline__ uint64_t streamOf(const FrameConstants& cFrame, uint32_t x, uint32_t y) {
 	return cFrame.seedMix ^ mixedBits((uint64_t(x) << 32) | uint64_t(y));
 }
 
@@ -76,7 +79,7 @@ __device__ __forceinline__ float tableAt(const float* curve, float nm) {
 }
 
 // math/colour.cpp:213 colourOf
-__device__ float3 colourOf(float4 nm, float4 density, float4 spectrum) {
+__device__ float3 colourOf(const FrameConstants& cFrame, float4 nm, float4 density, float4 spectrum) {
 	const float lanes[4] = { nm.x, nm.y, nm.z, nm.w };
 	const float dens[4]  = { density.x, density.y, density.z, density.w };
 	const float spec[4]  = { spectrum.x, spectrum.y, spectrum.z, spectrum.w };
@@ -280,7 +283,7 @@ __device__ bool meetLamp(const DeviceLamp& l, float3 origin, float3 dir, float l
 }
 
 // light.cpp:575 gradientColour
-__device__ float3 skyColour(float3 dir) {
+__device__ float3 skyColour(const FrameConstants& cFrame, float3 dir) {
 	const float height = dir.z;
 	const float3 far   = height >= 0.0f ? f3(cFrame.zenith) : f3(cFrame.ground);
 	const float share  = sqrtf(fabsf(height));
@@ -316,14 +319,14 @@ __device__ __forceinline__ uint32_t warpSlot(uint32_t* count, bool want) {
 }
 
 // ---- K-cam: camera rays and hero wavelengths (trace.cpp:116 startedPathIn) ----
-__global__ void __launch_bounds__(kBlock) cameraKernel(PathBuffers P, QueueBuffers Q, uint32_t firstPixel, uint32_t n) {
+__global__ void __launch_bounds__(kBlock) cameraKernel(const __grid_constant__ FrameConstants cFrame, PathBuffers P, QueueBuffers Q, uint32_t firstPixel, uint32_t n) {
 	if (blockIdx.x == 0 && threadIdx.x == 0) *Q.count = n;
 	for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
 		const uint32_t pixel  = firstPixel + p / cFrame.spp;
 		const uint32_t sample = cFrame.firstSample + p % cFrame.spp;
 		const uint32_t x      = pixel % uint32_t(cFrame.width);
 		const uint32_t y      = pixel / uint32_t(cFrame.width);
-		const uint64_t stream = streamOf(x, y);
+		const uint64_t stream = streamOf(cFrame, x, y);
 		// math/colour.cpp:236 sampledWavelengths of the pixel's golden-ratio share
 		const double start  = double(hashedBits(stream, ~uint64_t(0), 0)) * 0x1p-53;
 		const double turned = double(sample) * 0.6180339887498949 + start;
@@ -360,7 +363,7 @@ __global__ void __launch_bounds__(kBlock) cameraKernel(PathBuffers P, QueueBuffe
 
 __device__ __forceinline__ const DeviceMaterial& materialOfLeaf(uint32_t leaf, const Looks& L) {
 	const uint32_t m = leaf < L.leafCount ? L.leafMaterial[leaf] : 0u;
-	return L.materials[m < cFrame.materialCount ? m : 0u];
+	return L.materials[m < L.materialCount ? m : 0u];
 }
 
 // sdf/program.cpp evaluate over a pattern program's steps, with the point
@@ -421,7 +424,7 @@ __device__ __forceinline__ float3 albedoAt(const kdn_hit& hit, float3 normal, co
 }
 
 // ---- the surfaces pass: one ray through each pixel's centre (core/surfaces.cpp:39 surfaceRay) ----
-__global__ void __launch_bounds__(kBlock) surfaceRaysKernel(QueueBuffers Q, uint32_t firstPixel, uint32_t n) {
+__global__ void __launch_bounds__(kBlock) surfaceRaysKernel(const __grid_constant__ FrameConstants cFrame, QueueBuffers Q, uint32_t firstPixel, uint32_t n) {
 	if (blockIdx.x == 0 && threadIdx.x == 0) *Q.count = n;
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 		const uint32_t pixel = firstPixel + i;
@@ -469,7 +472,7 @@ __global__ void __launch_bounds__(kBlock) surfacesKernel(SurfaceArgs A) {
 }
 
 // ---- K-shade ----
-__global__ void __launch_bounds__(kBlock) shadeKernel(ShadeArgs A) {
+__global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ FrameConstants cFrame, ShadeArgs A) {
 	const uint32_t n = *A.in.count;
 	for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
 		const uint32_t q = base + threadIdx.x;
@@ -548,7 +551,7 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(ShadeArgs A) {
 				A.firstAlbedo[3 * px + 2] = __half_as_ushort(__float2half_rn(albedo.z));
 			}
 			if (!found) {
-				const float3 sky = skyColour(heading);
+				const float3 sky = skyColour(cFrame, heading);
 				R                = add4(R, mul4(mul4(T, keptOver(__int_as_float(0x7f800000))), spectrumOf(sky.x, sky.y, sky.z, nm)));
 			} else {
 				const uint32_t material = hit.leaf < A.looks.leafCount ? A.looks.leafMaterial[hit.leaf] : 0u;
@@ -576,7 +579,7 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(ShadeArgs A) {
 				const float lift        = kBias + 2.0f * hit.loosened;
 				const uint32_t x        = A.paths.pixel[p] % uint32_t(cFrame.width);
 				const uint32_t y        = A.paths.pixel[p] / uint32_t(cFrame.width);
-				const uint64_t stream   = streamOf(x, y);
+				const uint64_t stream   = streamOf(cFrame, x, y);
 				const uint32_t index    = A.paths.sample[p];
 				const bool capped       = depth + 1 >= cFrame.surfaces;
 				const float3 outgoing   = heading * -1.0f;
@@ -696,12 +699,12 @@ __global__ void __launch_bounds__(kBlock) linesKernel(PathBuffers P, ShadowBuffe
 
 // ---- K-fold: per pixel, the samples' colours (frame.cpp:273 foldPixels) ----
 // With light, also this call's mean a pixel (the frame record's light).
-__global__ void __launch_bounds__(kBlock) foldKernel(PathBuffers P, uint32_t firstPixel, uint32_t pixels, uint32_t spp, double* sums, float* light) {
+__global__ void __launch_bounds__(kBlock) foldKernel(const __grid_constant__ FrameConstants cFrame, PathBuffers P, uint32_t firstPixel, uint32_t pixels, uint32_t spp, double* sums, float* light) {
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < pixels; i += gridDim.x * blockDim.x) {
 		double r = 0.0, g = 0.0, b = 0.0;
 		for (uint32_t k = 0; k < spp; ++k) {
 			const uint32_t p = i * spp + k;
-			const float3 c   = colourOf(P.nanometres[p], P.density[p], P.radiance[p]);
+			const float3 c   = colourOf(cFrame, P.nanometres[p], P.density[p], P.radiance[p]);
 			r += double(c.x);
 			g += double(c.y);
 			b += double(c.z);
@@ -732,17 +735,13 @@ uint32_t gridFor(uint64_t n, int smCount) {
 
 } // namespace
 
-cudaError_t uploadFrameConstants(const FrameConstants& c, cudaStream_t stream) {
-	return cudaMemcpyToSymbolAsync(cFrame, &c, sizeof(FrameConstants), 0, cudaMemcpyHostToDevice, stream);
-}
-
-cudaError_t launchCamera(const PathBuffers& paths, const QueueBuffers& queue, uint32_t firstPixel, uint32_t n, cudaStream_t stream, int smCount) {
-	cameraKernel<<<gridFor(n, smCount), kBlock, 0, stream>>>(paths, queue, firstPixel, n);
+cudaError_t launchCamera(const FrameConstants& frame, const PathBuffers& paths, const QueueBuffers& queue, uint32_t firstPixel, uint32_t n, cudaStream_t stream, int smCount) {
+	cameraKernel<<<gridFor(n, smCount), kBlock, 0, stream>>>(frame, paths, queue, firstPixel, n);
 	return cudaGetLastError();
 }
 
-cudaError_t launchShade(const ShadeArgs& args, cudaStream_t stream, int smCount) {
-	shadeKernel<<<gridFor(args.capacity, smCount), kBlock, 0, stream>>>(args);
+cudaError_t launchShade(const FrameConstants& frame, const ShadeArgs& args, cudaStream_t stream, int smCount) {
+	shadeKernel<<<gridFor(args.capacity, smCount), kBlock, 0, stream>>>(frame, args);
 	return cudaGetLastError();
 }
 
@@ -751,13 +750,13 @@ cudaError_t launchLines(const PathBuffers& paths, const ShadowBuffers& shadow, u
 	return cudaGetLastError();
 }
 
-cudaError_t launchFold(const PathBuffers& paths, uint32_t firstPixel, uint32_t pixels, uint32_t spp, double* sums, float* light, cudaStream_t stream, int smCount) {
-	foldKernel<<<gridFor(pixels, smCount), kBlock, 0, stream>>>(paths, firstPixel, pixels, spp, sums, light);
+cudaError_t launchFold(const FrameConstants& frame, const PathBuffers& paths, uint32_t firstPixel, uint32_t pixels, uint32_t spp, double* sums, float* light, cudaStream_t stream, int smCount) {
+	foldKernel<<<gridFor(pixels, smCount), kBlock, 0, stream>>>(frame, paths, firstPixel, pixels, spp, sums, light);
 	return cudaGetLastError();
 }
 
-cudaError_t launchSurfaceRays(const QueueBuffers& queue, uint32_t firstPixel, uint32_t n, cudaStream_t stream, int smCount) {
-	surfaceRaysKernel<<<gridFor(n, smCount), kBlock, 0, stream>>>(queue, firstPixel, n);
+cudaError_t launchSurfaceRays(const FrameConstants& frame, const QueueBuffers& queue, uint32_t firstPixel, uint32_t n, cudaStream_t stream, int smCount) {
+	surfaceRaysKernel<<<gridFor(n, smCount), kBlock, 0, stream>>>(frame, queue, firstPixel, n);
 	return cudaGetLastError();
 }
 
