@@ -311,12 +311,12 @@ def run_gpu(args) -> None:
 # with the denoiser's history (interactive).  What is still queued when the
 # window closes is cancelled; latency is over the completed requests.
 SERVE_SCENES = ["c1", "room", "glow_small"]  # beside config 2, already resident
-SERVE_RATE, SERVE_WINDOW_S, SERVE_SLOTS, SERVE_SESSIONS = 200.0, 5.0, 4, 4
+SERVE_RATE, SERVE_WINDOW_S, SERVE_SLOTS, SERVE_SESSIONS = 200.0, 5.0, 8, 4
 SERVE_SIZES = [(320, 240), (640, 480), (1280, 720), (1920, 1080)]
 SERVE_SPP = [1, 4, 16, 64]
 
 
-def serving(main_backend) -> dict:
+def serving(main_backend, **options) -> dict:
     import kodanuki_gb300 as K
     from kodanuki_gb300.scene import Scene
     rng = np.random.default_rng(2024)
@@ -326,7 +326,7 @@ def serving(main_backend) -> dict:
         b.load(Scene.load(os.path.join(ROOT, "tests", "golden", "scenes", name + ".npz")))
         b.build(min_depth=6, max_depth=10, split_steps=64)
         backends.append(b)
-    srv = K.Server(0, slots=SERVE_SLOTS)
+    srv = K.Server(0, slots=options.pop("slots", SERVE_SLOTS), **options)
     ids = [srv.add_scene(b) for b in backends]
     session_scene = [ids[k % len(ids)] for k in range(SERVE_SESSIONS)]
     # warm-up (not counted): each session's first frame and a frame of each

@@ -449,13 +449,14 @@ kdn_status kdn_flush_l2(kdn_ctx* ctx);
  * (kdn_open_sharing) from a pool per scene; a session keeps its own until
  * it ends.  Up to `slots` requests are on the device at once, each on its
  * own streams; a request is admitted, interactive requests first and each
- * kind oldest first, when a slot is free (with more than one slot, one is
- * kept for interactive requests) and its path buffers (its paths x 364
- * bytes, capped at budget / slots) fit in what the running requests leave
- * of the budget.  Interactive requests (KDN_REQUEST_INTERACTIVE) run on
- * high-priority streams; with more than one slot the others' grids are
- * sized for three quarters of the SMs, so an interactive frame finds SMs
- * free.  Latency percentiles count the requests that
+ * kind oldest first, when a slot is free (at most batch_slots of them
+ * holding requests that are not interactive) and its path buffers (its
+ * paths x 364 bytes, capped at budget / slots, or at batch_frame_bytes for
+ * a batch request) fit in what the running requests leave of the budget.
+ * Interactive requests (KDN_REQUEST_INTERACTIVE) run on high-priority
+ * streams over every SM; batch requests run in short chunks on grids sized
+ * for batch_sm_percent of the SMs between them, so an interactive frame
+ * finds SMs free and a batch launch gives its SMs back soon.  Latency percentiles count the requests that
  * completed.  A frame's result
  * equals the same request drawn alone (kdn_render on a context of the same
  * scene).
@@ -463,9 +464,12 @@ kdn_status kdn_flush_l2(kdn_ctx* ctx);
 typedef struct kdn_server kdn_server;
 
 typedef struct kdn_serve_options {
-	int32_t device;        /* CUDA device, or KDN_HOST_ONLY (requests then end in KDN_NO_DEVICE) */
-	uint32_t slots;        /* requests on the device at once, 1..64 */
-	uint64_t budget_bytes; /* device bytes the running requests' path buffers may take; 0: 120 GB */
+	int32_t device;             /* CUDA device, or KDN_HOST_ONLY (requests then end in KDN_NO_DEVICE) */
+	uint32_t slots;             /* requests on the device at once, 1..64 */
+	uint64_t budget_bytes;      /* device bytes the running requests' path buffers may take; 0: 120 GB */
+	uint32_t batch_slots;       /* of the slots, the most that hold requests not interactive; 0: a quarter (at least 1) */
+	uint32_t batch_sm_percent;  /* the SMs the batch requests' grids are sized for together; 0: 50 */
+	uint64_t batch_frame_bytes; /* a batch request's path buffers, larger frames drawn in more chunks (short launches); 0: 1 GiB */
 } kdn_serve_options;
 
 #define KDN_REQUEST_INTERACTIVE 4u /* drawn on high-priority streams */

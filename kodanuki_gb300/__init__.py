@@ -92,7 +92,8 @@ REQUEST_INTERACTIVE = 4
 
 
 class ServeOptions(ctypes.Structure):
-    _fields_ = [("device", ctypes.c_int32), ("slots", ctypes.c_uint32), ("budget_bytes", ctypes.c_uint64)]
+    _fields_ = [("device", ctypes.c_int32), ("slots", ctypes.c_uint32), ("budget_bytes", ctypes.c_uint64), ("batch_slots", ctypes.c_uint32),
+                ("batch_sm_percent", ctypes.c_uint32), ("batch_frame_bytes", ctypes.c_uint64)]
 
 
 class Request(ctypes.Structure):
@@ -446,10 +447,11 @@ class Server:
     requests submitted as they arrive and drawn side by side, progressive
     sessions, latency percentiles."""
 
-    def __init__(self, device: int = 0, slots: int = 4, budget_bytes: int = 0):
+    def __init__(self, device: int = 0, slots: int = 4, budget_bytes: int = 0, batch_slots: int = 0, batch_sm_percent: int = 0,
+                 batch_frame_bytes: int = 0):
         self.lib = library()
         self.handle = ctypes.c_void_p()
-        o = ServeOptions(device, slots, budget_bytes)
+        o = ServeOptions(device, slots, budget_bytes, batch_slots, batch_sm_percent, batch_frame_bytes)
         st = self.lib.kdn_serve_open(ctypes.byref(o), ctypes.byref(self.handle))
         if st != KDN_OK:
             raise KdnError(st, "kdn_serve_open")

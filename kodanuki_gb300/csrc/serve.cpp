@@ -69,7 +69,10 @@ struct kdn_server {
 	int device        = 0;
 	uint32_t slots    = 1;
 	uint64_t budget   = 0;
-	uint64_t slotCap  = 0; // the most path-buffer bytes one request takes
+	uint64_t slotCap  = 0; // the most path-buffer bytes one interactive request takes
+	uint32_t batchSlots   = 1;
+	uint32_t batchSms     = 0; // SMs a batch request's grids are sized for
+	uint64_t batchCap     = 0; // the most path-buffer bytes one batch request takes
 	int sms           = 0; // the device's SMs
 	std::mutex m;
 	std::condition_variable work, finished;
@@ -104,7 +107,7 @@ bool interactiveOf(const Job* j) { return (j->request.flags & KDN_REQUEST_INTERA
 // budget (one request is always let in).
 Job* admitted(kdn_server* S) {
 	if (S->running >= S->slots) return nullptr;
-	const bool batchRoom = S->slots == 1 || S->runningBatch + 1 < S->slots;
+	const bool batchRoom = S->runningBatch < S->batchSlots;
 	for (int pass = 0; pass < 2; ++pass) {
 		const bool wantInteractive = pass == 0;
 		if (!wantInteractive && !batchRoom) break;
@@ -186,8 +189,9 @@ void serveLoop(kdn_server* S) {
 		if (fresh) {
 			status = kdn_open_sharing(sceneCtx, interactive ? kInteractivePriority : 0, &ctx);
 			if (status == KDN_OK) status = kdn_set_frame_budget(ctx, S->slotCap);
-			// the batch frames leave a quarter of the SMs to interactive ones
-			if (status == KDN_OK && !interactive && S->slots > 1 && S->sms > 0) status = kdn_set_sm_limit(ctx, S->sms * 3 / 4);
+			// batch frames: short chunks on their share of the SMs
+			if (status == KDN_OK && !interactive) status = kdn_set_frame_budget(ctx, S->batchCap);
+			if (status == KDN_OK && !interactive && S->slots > 1 && S->batchSms > 0) status = kdn_set_sm_limit(ctx, int(S->batchSms));
 			if (status != KDN_OK) why = kdn_last_error(sceneCtx);
 		}
 		if (status == KDN_OK) {
@@ -252,10 +256,14 @@ kdn_status kdn_serve_open(const kdn_serve_options* options, kdn_server** out) {
 	S->slots   = options->slots;
 	S->budget  = options->budget_bytes ? options->budget_bytes : uint64_t(120) << 30;
 	S->slotCap = std::max<uint64_t>(S->budget / S->slots, uint64_t(64) << 20);
+	S->batchSlots = options->batch_slots ? std::min(options->batch_slots, S->slots) : std::max<uint32_t>(1, S->slots / 4);
+	S->batchCap   = std::min<uint64_t>(S->slotCap, options->batch_frame_bytes ? options->batch_frame_bytes : uint64_t(1) << 30);
 	if (S->device >= 0 && cudaDeviceGetAttribute(&S->sms, cudaDevAttrMultiProcessorCount, S->device) != cudaSuccess) {
 		cudaGetLastError();
 		S->sms = 0;
 	}
+	const uint32_t percent = options->batch_sm_percent ? std::min<uint32_t>(options->batch_sm_percent, 100) : 50;
+	S->batchSms = std::max<uint32_t>(1, uint32_t(S->sms) * percent / 100 / S->batchSlots);
 	for (uint32_t k = 0; k < S->slots; ++k) S->workers.emplace_back(serveLoop, S);
 	*out = S;
 	return KDN_OK;
@@ -280,7 +288,8 @@ kdn_status kdn_serve_submit(kdn_server* S, const kdn_request* request, float* ou
 	job->out       = out_rgb;
 	job->submitted = Clock::now();
 	const uint64_t pixels = uint64_t(request->width) * uint64_t(request->height);
-	job->need = std::min<uint64_t>(pixels * uint64_t(request->samples) * kPathBytes, S->slotCap) + pixels * kPixelBytes;
+	const uint64_t cap = (request->flags & KDN_REQUEST_INTERACTIVE) ? S->slotCap : S->batchCap;
+	job->need = std::min<uint64_t>(pixels * uint64_t(request->samples) * kPathBytes, cap) + pixels * kPixelBytes;
 	std::lock_guard<std::mutex> guard(S->m);
 	if (S->closing) return S->fail(KDN_BAD_ARG, "kdn_serve_submit: the server is closing");
 	if (request->scene >= S->scenes.size()) return S->fail(KDN_BAD_ARG, "kdn_serve_submit: no scene " + std::to_string(request->scene));
