@@ -519,6 +519,66 @@ const char* kdn_serve_last_error(const kdn_server* server);
  * that will be waited for has been. */
 kdn_status kdn_serve_close(kdn_server* server);
 
+/*
+ * The learned guide (an added form: the reference's guides are the highlight
+ * guide, plugins/sampler/highlight_guide/mixture.cpp:113 mixtureDirection,
+ * and the plain BSDF sampling of the default sampler, paths/sampler.cpp:93
+ * drawDirection; this is the guiding plugin point's learned proposal).
+ *
+ * A multiresolution hash-grid encoding of the position (16 levels, 2
+ * features a level, 2^table_log2 entries a level, FP16 table) and the
+ * vertex's faced normal feed a 3 x 64 ReLU network whose 40 outputs are a
+ * mixture of eight von Mises-Fisher lobes over directions.  It is trained
+ * online, on the device, on the radiance the tracer carries back to each
+ * recorded vertex (loss mean(-w log q(direction)), Adam), and a frame
+ * samples with it by one-sample MIS with the BSDF (kdn_set_guide), so the
+ * estimate stays unbiased.  Both the training and the inference run on
+ * the tensor cores (BF16 operands, FP32 accumulation).
+ */
+typedef struct kdn_guide kdn_guide;
+
+typedef struct kdn_guide_options {
+	uint32_t table_log2;      /* entries a level, log2: 19 for the full grid; 8..22 */
+	uint32_t seed;            /* of the initial weights and table */
+	float learning_rate;      /* Adam, 1e-2 */
+	float region_lo[3];       /* the box positions are encoded over (clamped to it) */
+	float region_hi[3];
+	uint32_t batch;           /* samples an Adam step (0: 16384) */
+	uint32_t max_steps;       /* Adam steps a training frame at most (0: 256) */
+	uint32_t sample_capacity; /* training samples a frame keeps (0: 2^22) */
+} kdn_guide_options;
+
+kdn_status kdn_guide_open(int device, const kdn_guide_options* options, kdn_guide** out);
+kdn_status kdn_guide_close(kdn_guide* guide);
+const char* kdn_guide_last_error(void);
+/* floats of the weights (14336: W0 64x48, W1 64x64, W2 64x64, W3 48x64, row
+ * major, out x in) and of the table (16 << table_log2 entries x 2) */
+kdn_status kdn_guide_sizes(const kdn_guide* guide, uint64_t* weights, uint64_t* table);
+kdn_status kdn_guide_get_params(kdn_guide* guide, float* weights, float* table);
+kdn_status kdn_guide_set_params(kdn_guide* guide, const float* weights, const float* table);
+/* samples: n x 10 floats (point, faced normal, direction, weight = the
+ * integrand's estimate over the density the direction was drawn with).
+ * The loss and its gradients over the n samples, no step taken. */
+kdn_status kdn_guide_gradients(kdn_guide* guide, const float* samples, uint32_t n, float* loss, float* dweights, float* dtable);
+/* steps Adam steps of batch samples each over the n samples (0 steps: one
+ * pass); last_loss: the last step's loss */
+kdn_status kdn_guide_train(kdn_guide* guide, const float* samples, uint32_t n, uint32_t batch, uint32_t steps, float* last_loss);
+/* rows: n x 6 floats (point, faced normal) -> lobes: n x 40 floats, lobe j
+ * at 5j: weight, concentration, mean direction */
+kdn_status kdn_guide_query(kdn_guide* guide, const float* rows, uint32_t n, float* lobes);
+kdn_status kdn_guide_clear_samples(kdn_guide* guide);
+int kdn_guide_ready(const kdn_guide* guide);
+
+/* Frames of ctx use the guide (null: none).  flags: KDN_GUIDE_SAMPLE draws
+ * the first kGuideDepth (3) vertices' directions on matte and plastic
+ * surfaces from share x guide + (1 - share) x BSDF once the guide is
+ * trained; KDN_GUIDE_TRAIN records those vertices and trains the guide on
+ * them after each frame.  The guide must live on the context's device and
+ * must not be used by two contexts' frames at once. */
+#define KDN_GUIDE_SAMPLE 1u
+#define KDN_GUIDE_TRAIN 2u
+kdn_status kdn_set_guide(kdn_ctx* ctx, kdn_guide* guide, float share, uint32_t flags);
+
 #ifdef __cplusplus
 }
 #endif

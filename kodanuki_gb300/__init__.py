@@ -86,6 +86,8 @@ EXPORTS = [
     "kdn_frame_surfaces", "kdn_frame_record", "kdn_world_march", "kdn_world_locate", "kdn_temporal_device", "kdn_denoise", "kdn_denoise_device", "kdn_denoise_static",
     "kdn_open_sharing", "kdn_set_frame_budget", "kdn_serve_open", "kdn_serve_add_scene", "kdn_serve_submit", "kdn_serve_wait", "kdn_serve_end_session",
     "kdn_serve_latency", "kdn_serve_last_error", "kdn_serve_close", "kdn_serve_cancel_queued", "kdn_set_sm_limit", "kdn_serve_reset_latency",
+    "kdn_guide_open", "kdn_guide_close", "kdn_guide_last_error", "kdn_guide_sizes", "kdn_guide_get_params", "kdn_guide_set_params",
+    "kdn_guide_gradients", "kdn_guide_train", "kdn_guide_query", "kdn_guide_clear_samples", "kdn_guide_ready", "kdn_set_guide",
 ]
 
 REQUEST_INTERACTIVE = 4
@@ -178,9 +180,22 @@ def library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.kdn_serve_last_error.argtypes = [P]
     L.kdn_serve_close.argtypes = [P]
     L.kdn_serve_cancel_queued.argtypes = [P, ctypes.POINTER(ctypes.c_uint64)]
+    L.kdn_guide_open.argtypes = [ctypes.c_int, P, ctypes.POINTER(P)]
+    L.kdn_guide_close.argtypes = [P]
+    L.kdn_guide_last_error.restype = ctypes.c_char_p
+    L.kdn_guide_last_error.argtypes = []
+    L.kdn_guide_sizes.argtypes = [P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
+    L.kdn_guide_get_params.argtypes = [P, P, P]
+    L.kdn_guide_set_params.argtypes = [P, P, P]
+    L.kdn_guide_gradients.argtypes = [P, P, ctypes.c_uint32, P, P, P]
+    L.kdn_guide_train.argtypes = [P, P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, P]
+    L.kdn_guide_query.argtypes = [P, P, ctypes.c_uint32, P]
+    L.kdn_guide_clear_samples.argtypes = [P]
+    L.kdn_guide_ready.argtypes = [P]
+    L.kdn_set_guide.argtypes = [P, P, ctypes.c_float, ctypes.c_uint32]
     for name in EXPORTS:
         fn = getattr(L, name)
-        if name not in ("kdn_status_string", "kdn_last_error", "kdn_serve_last_error"):
+        if name not in ("kdn_status_string", "kdn_last_error", "kdn_serve_last_error", "kdn_guide_last_error"):
             fn.restype = ctypes.c_int
     _lib = L
     return L
@@ -512,3 +527,81 @@ class Server:
 
     def __exit__(self, *exc) -> None:
         self.close()
+
+
+GUIDE_SAMPLE = 1
+GUIDE_TRAIN = 2
+
+
+class GuideOptions(ctypes.Structure):
+    _fields_ = [("table_log2", ctypes.c_uint32), ("seed", ctypes.c_uint32), ("learning_rate", ctypes.c_float),
+                ("region_lo", ctypes.c_float * 3), ("region_hi", ctypes.c_float * 3), ("batch", ctypes.c_uint32),
+                ("max_steps", ctypes.c_uint32), ("sample_capacity", ctypes.c_uint32)]
+
+
+class Guide:
+    """The learned guide (kdn_guide_*): a hash-grid encoding and a 3 x 64
+    network whose outputs are eight vMF lobes, trained and queried on the
+    device's tensor cores."""
+
+    def __init__(self, device: int = 0, table_log2: int = 19, seed: int = 1, learning_rate: float = 1e-2,
+                 region=((-1.0, -1.0, -1.0), (1.0, 1.0, 1.0)), batch: int = 0, max_steps: int = 0, sample_capacity: int = 0):
+        self.lib = library()
+        o = GuideOptions()
+        o.table_log2, o.seed, o.learning_rate = table_log2, seed, learning_rate
+        for k in range(3):
+            o.region_lo[k], o.region_hi[k] = float(region[0][k]), float(region[1][k])
+        o.batch, o.max_steps, o.sample_capacity = batch, max_steps, sample_capacity
+        self.options = o
+        self.handle = ctypes.c_void_p()
+        self._check(self.lib.kdn_guide_open(device, ctypes.byref(o), ctypes.byref(self.handle)))
+        w, t = ctypes.c_uint64(), ctypes.c_uint64()
+        self._check(self.lib.kdn_guide_sizes(self.handle, ctypes.byref(w), ctypes.byref(t)))
+        self.weight_count, self.table_count = w.value, t.value
+        self.table_log2 = table_log2
+
+    def _check(self, status: int) -> None:
+        if status != KDN_OK:
+            raise KdnError(status, self.lib.kdn_guide_last_error().decode())
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.kdn_guide_close(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def params(self):
+        w = np.zeros(self.weight_count, np.float32)
+        t = np.zeros(self.table_count, np.float32)
+        self._check(self.lib.kdn_guide_get_params(self.handle, _ptr(w), _ptr(t)))
+        return w, t
+
+    def set_params(self, w: np.ndarray, t: np.ndarray) -> None:
+        w = np.ascontiguousarray(w, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        self._check(self.lib.kdn_guide_set_params(self.handle, _ptr(w), _ptr(t)))
+
+    def gradients(self, samples: np.ndarray):
+        s = np.ascontiguousarray(samples, np.float32)
+        loss = np.zeros(1, np.float32)
+        dw = np.zeros(self.weight_count, np.float32)
+        dt = np.zeros(self.table_count, np.float32)
+        self._check(self.lib.kdn_guide_gradients(self.handle, _ptr(s), len(s), _ptr(loss), _ptr(dw), _ptr(dt)))
+        return float(loss[0]), dw, dt
+
+    def train(self, samples: np.ndarray, batch: int = 16384, steps: int = 0) -> float:
+        s = np.ascontiguousarray(samples, np.float32)
+        loss = np.zeros(1, np.float32)
+        self._check(self.lib.kdn_guide_train(self.handle, _ptr(s), len(s), batch, steps, _ptr(loss)))
+        return float(loss[0])
+
+    def query(self, rows: np.ndarray) -> np.ndarray:
+        r = np.ascontiguousarray(rows, np.float32)
+        out = np.zeros((len(r), 40), np.float32)
+        self._check(self.lib.kdn_guide_query(self.handle, _ptr(r), len(r), _ptr(out)))
+        return out

@@ -145,6 +145,17 @@ kdn_status kdn_set_frame_budget(kdn_ctx* handle, uint64_t bytes) {
 	return KDN_OK;
 }
 
+kdn_status kdn_set_guide(kdn_ctx* handle, kdn_guide* guide, float share, uint32_t flags) {
+	if (handle == nullptr || (guide != nullptr && !(share > 0.0f && share < 1.0f)) || (flags & ~(KDN_GUIDE_SAMPLE | KDN_GUIDE_TRAIN)) != 0) return KDN_BAD_ARG;
+	Context* ctx = reinterpret_cast<Context*>(handle);
+	std::lock_guard<std::mutex> guard(ctx->lock);
+	if (guide != nullptr && kdn::guideDevice(guide) != ctx->device) return ctx->fail(KDN_BAD_ARG, "kdn_set_guide: the guide lives on another device");
+	ctx->guide      = guide;
+	ctx->guideShare = share;
+	ctx->guideFlags = guide != nullptr ? flags : 0u;
+	return KDN_OK;
+}
+
 kdn_status kdn_set_sm_limit(kdn_ctx* handle, int sms) {
 	if (handle == nullptr || sms < 0) return KDN_BAD_ARG;
 	Context* ctx = reinterpret_cast<Context*>(handle);

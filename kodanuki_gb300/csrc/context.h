@@ -53,6 +53,10 @@ struct Context {
 	DeviceBuffer extendRays, extendHits, extendStates, counters, l2;
 	DeviceBuffer denoiseScratch, denoiseIo, fetch;
 	FrameState* frame = nullptr;
+	// the learned guide frames use (kdn_set_guide): KDN_GUIDE_SAMPLE, KDN_GUIDE_TRAIN
+	kdn_guide* guide    = nullptr;
+	float guideShare    = 0.5f;
+	uint32_t guideFlags = 0;
 
 	kdn_status open();
 	kdn_status share(Context* from);
@@ -77,6 +81,9 @@ struct Context {
 	kdn_status flushL2();
 	void releaseFrame();
 };
+
+// guide.cu: the device a learned guide lives on
+int guideDevice(const kdn_guide* guide);
 
 // denoise_abi.cpp: the denoiser over device buffers with the context's scratch.
 kdn_status denoiseOnDevice(Context* ctx, const kdn_denoise_frame* frame, const float* colour, const float* moment, const float* length, const uint16_t* distance,
