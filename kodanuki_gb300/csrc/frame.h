@@ -147,6 +147,12 @@ struct ShadeArgs {
 	uint16_t* firstNormal;
 	uint16_t* firstAlbedo;
 	uint32_t* firstLeaf;
+	// the learned guide: where set, each queue entry's lobes (kGuideLobeFloats
+	// floats, written for guidable hits), and the share of guided draws; the
+	// records of a training frame (kGuideDepth a path)
+	const float* lobes;
+	float guideShare;
+	struct GuideRecord* records;
 };
 
 // The surfaces pass: the first surface through each pixel's centre, as the

@@ -16,7 +16,7 @@
 // packed BF16 weight images come into shared memory by one bulk TMA copy.
 //
 // The reference has no learned guide: this is the backend's added form.
-#include "guide.h"
+#include "guide_mix.cuh"
 
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -264,12 +264,13 @@ __device__ __forceinline__ void lobesOf(const float* o, float* L) {
 #pragma unroll
 	for (int j = 0; j < kGuideLobes; ++j) {
 		const float* m  = o + 5 * j + 2;
-		const float nrm = fmaxf(sqrtf(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]), 1e-6f);
+		const float nrm = sqrtf(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+		const bool flat = !(nrm > 1e-6f); // read as +z
 		L[5 * j]        = e[j] / sum;
 		L[5 * j + 1]    = expf(fminf(fmaxf(o[5 * j + 1], kKappaLo), kKappaHi));
-		L[5 * j + 2]    = m[0] / nrm;
-		L[5 * j + 3]    = m[1] / nrm;
-		L[5 * j + 4]    = m[2] / nrm;
+		L[5 * j + 2]    = flat ? 0.0f : m[0] / nrm;
+		L[5 * j + 3]    = flat ? 0.0f : m[1] / nrm;
+		L[5 * j + 4]    = flat ? 1.0f : m[2] / nrm;
 	}
 }
 
@@ -294,10 +295,12 @@ __device__ void lossRow(const float* o, float3 d, float w, float invN, float* g,
 		live[j]       = c > kKappaLo && c < kKappaHi;
 		kap[j]        = expf(fminf(fmaxf(c, kKappaLo), kKappaHi));
 		const float* m = o + 5 * j + 2;
-		nrm[j]        = fmaxf(sqrtf(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]), 1e-6f);
-		mu[j][0]      = m[0] / nrm[j];
-		mu[j][1]      = m[1] / nrm[j];
-		mu[j][2]      = m[2] / nrm[j];
+		nrm[j]        = sqrtf(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+		const bool flat = !(nrm[j] > 1e-6f); // read as +z, no gradient
+		mu[j][0]      = flat ? 0.0f : m[0] / nrm[j];
+		mu[j][1]      = flat ? 0.0f : m[1] / nrm[j];
+		mu[j][2]      = flat ? 1.0f : m[2] / nrm[j];
+		if (flat) nrm[j] = __int_as_float(0x7f800000);
 		cs[j]         = mu[j][0] * d.x + mu[j][1] * d.y + mu[j][2] * d.z;
 		const float lv = logf(kap[j]) - 1.8378770664093453f - log1pf(-expf(-2.0f * kap[j])) + kap[j] * (cs[j] - 1.0f);
 		pv[j]         = pi[j] * expf(lv);

@@ -3,12 +3,16 @@
 #pragma once
 
 #include "frame.h"
-#include "guide_mix.cuh"
 #include "kdn.h"
 
 #include <cuda_runtime.h>
 
 namespace kdn {
+
+constexpr int kGuideLobes        = 8;
+constexpr int kGuideLobeFloats   = 5 * kGuideLobes;
+constexpr int kGuideDepth        = 3;  // vertices 0, 1, 2 of a path are guided and recorded
+constexpr int kGuideSampleFloats = 10; // point, normal, direction, weight
 
 // One vertex of a path that a training frame records: where it stood, its
 // faced normal, the direction it left by, the throughput that reached it

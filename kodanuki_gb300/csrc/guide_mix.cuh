@@ -5,14 +5,11 @@
 // distribution on S2"): v(w) = k / (2 pi (1 - e^-2k)) exp(k (mu . w - 1)).
 #pragma once
 
+#include "guide.h"
+
 #include <cuda_runtime.h>
 
 namespace kdn {
-
-constexpr int kGuideLobes       = 8;
-constexpr int kGuideLobeFloats  = 5 * kGuideLobes;
-constexpr int kGuideDepth       = 3;   // vertices 0, 1, 2 of a path are guided and recorded
-constexpr int kGuideSampleFloats = 10; // point, normal, direction, weight
 
 __device__ __forceinline__ float vmfDensity(float kappa, float cosine) {
 	return kappa / (6.283185307179586f * (1.0f - __expf(-2.0f * kappa))) * __expf(kappa * (cosine - 1.0f));

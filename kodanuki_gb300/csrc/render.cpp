@@ -9,6 +9,7 @@
 #include "context.h"
 #include "temporal.h"
 #include "frame.h"
+#include "guide.h"
 
 #include <algorithm>
 #include <cmath>
@@ -33,6 +34,7 @@ struct FrameState {
 	DeviceBuffer frameLight, firstDistance, firstNormal, firstAlbedo, firstLeaf;
 	DeviceBuffer gDistance[2], gNormal[2], gAlbedo[2], gLeaf[2];
 	DeviceBuffer tColour[2], tMoment[2], tLength[2];
+	DeviceBuffer guideLobes, guideRecords; // the learned guide's, a lane's capacity each
 	uint32_t capacity = 0;
 	int32_t width = 0, height = 0;
 	double taken = 0;
@@ -52,7 +54,7 @@ struct FrameState {
 void Context::releaseFrame() {
 	if (frame == nullptr) return;
 	FrameState& f = *frame;
-	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.hits, &f.states, &f.counts, &f.shadowPaths, &f.shadowContribution, &f.sums, &f.out, &f.materials, &f.patternSteps, &f.stops, &f.placements, &f.boundaries, &f.frameLight, &f.firstDistance, &f.firstNormal, &f.firstAlbedo, &f.firstLeaf, &f.gDistance[0], &f.gDistance[1], &f.gNormal[0], &f.gNormal[1], &f.gAlbedo[0], &f.gAlbedo[1], &f.gLeaf[0], &f.gLeaf[1], &f.tColour[0], &f.tColour[1], &f.tMoment[0], &f.tMoment[1], &f.tLength[0], &f.tLength[1] }) {
+	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.hits, &f.states, &f.counts, &f.shadowPaths, &f.shadowContribution, &f.sums, &f.out, &f.materials, &f.patternSteps, &f.stops, &f.placements, &f.boundaries, &f.frameLight, &f.firstDistance, &f.firstNormal, &f.firstAlbedo, &f.firstLeaf, &f.gDistance[0], &f.gDistance[1], &f.gNormal[0], &f.gNormal[1], &f.gAlbedo[0], &f.gAlbedo[1], &f.gLeaf[0], &f.gLeaf[1], &f.tColour[0], &f.tColour[1], &f.tMoment[0], &f.tMoment[1], &f.tLength[0], &f.tLength[1], &f.guideLobes, &f.guideRecords }) {
 		if (b->ptr) cudaFree(b->ptr);
 		b->ptr   = nullptr;
 		b->bytes = 0;
@@ -254,12 +256,17 @@ static_assert(kPathBytes == 364, "path bytes");
 // every launch has a large share of the frame's rays to spread over the GPU
 // and the slow rays of a launch hold back one thread each, not a small
 // chunk's whole tail.
+// with the learned guide, a path also holds its queue entry's lobes and its
+// training records
+constexpr size_t kGuidePathBytes = kdn::kGuideLobeFloats * sizeof(float) + kdn::kGuideDepth * sizeof(kdn::GuideRecord);
+
 uint64_t chunkPaths(Context* ctx, uint64_t framePaths) {
 	size_t freeBytes = 0, totalBytes = 0;
 	if (cudaMemGetInfo(&freeBytes, &totalBytes) != cudaSuccess) freeBytes = 0;
-	const uint64_t held = ctx->frame ? uint64_t(ctx->frame->capacity) * kLanes * kPathBytes : 0;
-	uint64_t room = (uint64_t(freeBytes) + held) / 2 / kPathBytes;
-	if (ctx->frameBudget > 0) room = std::min<uint64_t>(room, ctx->frameBudget / kPathBytes);
+	const size_t pathBytes = kPathBytes + (ctx->guideFlags != 0 ? kGuidePathBytes : 0);
+	const uint64_t held = ctx->frame ? uint64_t(ctx->frame->capacity) * kLanes * kPathBytes + ctx->frame->guideLobes.bytes + ctx->frame->guideRecords.bytes : 0;
+	uint64_t room = (uint64_t(freeBytes) + held) / 2 / pathBytes;
+	if (ctx->frameBudget > 0) room = std::min<uint64_t>(room, ctx->frameBudget / pathBytes);
 	const uint64_t least = ctx->frameBudget > 0 ? uint64_t(1) << 16 : uint64_t(1) << 20;
 	return std::min<uint64_t>(framePaths, std::min<uint64_t>(uint64_t(1) << 28, std::max<uint64_t>(room, least)));
 }
@@ -321,6 +328,11 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	kdn_status s = ensureFrame(ctx, capacity);
 	if (s != KDN_OK) return s;
 	FrameState& f = *ctx->frame;
+	// the learned guide: draws from it once it is trained, records for training
+	const bool guiding = ctx->guide != nullptr && (ctx->guideFlags & KDN_GUIDE_SAMPLE) && kdn_guide_ready(ctx->guide);
+	const bool training = ctx->guide != nullptr && (ctx->guideFlags & KDN_GUIDE_TRAIN);
+	if (guiding && (s = ctx->ensure(f.guideLobes, size_t(f.capacity) * kLanes * kGuideLobeFloats * sizeof(float))) != KDN_OK) return s;
+	if (training && (s = ctx->ensure(f.guideRecords, size_t(f.capacity) * kLanes * kGuideDepth * sizeof(GuideRecord))) != KDN_OK) return s;
 	// pixel sums: fresh unless accumulating onto a frame of the same size
 	const bool fresh = !fr->accumulate || f.width != fr->width || f.height != fr->height || f.sums.ptr == nullptr;
 	if ((s = ctx->ensure(f.sums, size_t(pixels) * 3 * sizeof(double))) != KDN_OK) return s;
@@ -448,6 +460,8 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		kdn_hit* hits;
 		uint32_t* none;
 		uint32_t* fetch;
+		float* lobes;
+		GuideRecord* records;
 	};
 	Lane lane[kLanes];
 	for (int l = 0; l < kLanes; ++l) {
@@ -480,6 +494,8 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		L.S.states       = L.states + capacity;
 		L.none           = counts + 4 * l + 3;
 		L.fetch          = static_cast<uint32_t*>(ctx->fetch.ptr) + l;
+		L.lobes          = guiding ? static_cast<float*>(f.guideLobes.ptr) + base * kGuideLobeFloats : nullptr;
+		L.records        = training ? static_cast<GuideRecord*>(f.guideRecords.ptr) + base * kGuideDepth : nullptr;
 	}
 
 	// timing: one event pair around the frame, one around each trace launch
@@ -545,6 +561,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		const uint32_t chunk     = std::min(chunkPixels, pixels - first);
 		const uint32_t n         = chunk * spp;
 		const PathBuffers& LP    = L.P;
+		if (training && !ctx->check(cudaMemsetAsync(L.records, 0xFF, size_t(n) * kGuideDepth * sizeof(GuideRecord), on), "clear guide records")) return KDN_CUDA_ERROR;
 		if (!ctx->check(launchCamera(c, LP, L.Q[0], first, n, on, ctx->smCount), "camera kernel")) return KDN_CUDA_ERROR;
 		++launches;
 		if (!ctx->check(cudaMemsetAsync(L.S.count, 0, 4, on), "clear lines")) return KDN_CUDA_ERROR;
@@ -580,6 +597,17 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 				h.count  = L.Q[q].count;
 				if (!ctx->check(launchHits(h, on, ctx->smCount), "hit kernel")) return KDN_CUDA_ERROR;
 				++launches;
+				if (guiding && bounce < kGuideDepth) {
+					GuideQueue gq;
+					gq.hits          = L.hits;
+					gq.rays          = L.Q[q].rays;
+					gq.count         = L.Q[q].count;
+					gq.looks         = looks;
+					gq.materialCount = looks.materialCount;
+					gq.lobes         = L.lobes;
+					if (!ctx->check(guideQueryQueue(ctx->guide, gq, n, on, ctx->smCount), "guide query kernel")) return KDN_CUDA_ERROR;
+					++launches;
+				}
 			}
 			if (bounce > 0) {
 				// the bounce before's lines that reached their lamps
@@ -605,17 +633,25 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 			a.firstNormal   = denoised ? static_cast<uint16_t*>(f.firstNormal.ptr) : nullptr;
 			a.firstAlbedo   = denoised ? static_cast<uint16_t*>(f.firstAlbedo.ptr) : nullptr;
 			a.firstLeaf     = denoised ? static_cast<uint32_t*>(f.firstLeaf.ptr) : nullptr;
+			a.lobes         = (guiding && bounce < kGuideDepth) ? L.lobes : nullptr;
+			a.guideShare    = ctx->guideShare;
+			a.records       = L.records;
 			if (!ctx->check(launchShade(c, a, on, ctx->smCount), "shade kernel")) return KDN_CUDA_ERROR;
 			++launches;
 			q = nxt;
 		}
 		if (!ctx->check(launchFold(c, LP, first, chunk, spp, static_cast<double*>(f.sums.ptr), denoised ? static_cast<float*>(f.frameLight.ptr) : nullptr, on, ctx->smCount), "fold kernel")) return KDN_CUDA_ERROR;
 		++launches;
+		if (training) {
+			if (!ctx->check(guideGather(ctx->guide, L.records, LP.radiance, n, on, ctx->smCount), "guide gather kernel")) return KDN_CUDA_ERROR;
+			++launches;
+		}
 	}
 	// the first lane goes on once the others are done
 	for (int l = 1; l < kLanes; ++l) {
 		if (!ctx->check(cudaEventRecord(f.ended[l - 1], lanes[l]), "event") || !ctx->check(cudaStreamWaitEvent(stream, f.ended[l - 1], 0), "stream wait")) return KDN_CUDA_ERROR;
 	}
+	if (training && (s = guideTrainGathered(ctx->guide, stream)) != KDN_OK) return ctx->fail(s, std::string("kdn_render: guide training: ") + kdn_guide_last_error());
 	f.taken += double(spp);
 	f.last_denoised = denoised;
 	if (!denoised) f.shown = -1; // a frame without the shown chain drops the temporal history

@@ -15,6 +15,7 @@
 // Throughput and radiance are four hero-wavelength lanes in FP32 (the
 // reference carries them in double).
 #include "frame.h"
+#include "guide_mix.cuh"
 #include "materials.cuh"
 #include "program.cuh"
 
@@ -495,6 +496,9 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 			float4 R            = A.paths.radiance[p];
 			const float4 nm     = A.paths.nanometres[p];
 			const float drawnDensity = A.paths.drawn[p];
+			// a training frame: the radiance held on reaching this vertex is
+			// what the vertex before held once its own aim was answered
+			if (A.records != nullptr && depth >= 1 && depth <= kGuideDepth) A.records[size_t(p) * kGuideDepth + depth - 1].before = R.x + R.y + R.z + R.w;
 			const float3 heading = make_float3(ray.direction[0], ray.direction[1], ray.direction[2]);
 			const float3 origin  = make_float3(ray.origin[0], ray.origin[1], ray.origin[2]);
 			const bool found     = hit.kind != 0;
@@ -576,6 +580,7 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 					if (glow.x > 0.0f || glow.y > 0.0f || glow.z > 0.0f) R = add4(R, mul4(T, spectrumOf(glow.x, glow.y, glow.z, nm)));
 				}
 				if (dot3(normal, heading) >= 0.0f) normal = normal * -1.0f;
+				const float4 T0         = T; // what reached this vertex
 				const float lift        = kBias + 2.0f * hit.loosened;
 				const uint32_t x        = A.paths.pixel[p] % uint32_t(cFrame.width);
 				const uint32_t y        = A.paths.pixel[p] / uint32_t(cFrame.width);
@@ -589,6 +594,9 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 				// the glass being crossed where it bends; trace.cpp:590
 				// openSide: the side a line leaves by
 				const bool aimable = medium == kNoMaterial || (medium == material && m.kind == 3 && surf.within.x != surf.beyond.x);
+				// the learned guide's lobes at this vertex (one-sample MIS with the BSDF)
+				const float* lobes = (A.lobes != nullptr && depth < kGuideDepth && guidable(m.kind)) ? A.lobes + size_t(q) * kGuideLobeFloats : nullptr;
+				const float share  = A.guideShare;
 				const float3 open  = surf.inside ? normal * -1.0f : normal;
 				// aim: offer every lamp, trace one offer drawn by its lane mean
 				if (!m.exact && aimable && cFrame.lampCount > 0) {
@@ -607,7 +615,7 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 						const Response f = respond(surf, m, outgoing, a.toward, nm);
 						float w          = 1.0f;
 						if (a.density > 0.0f) {
-							const float pm = capped ? 0.0f : f.density;
+							const float pm = capped ? 0.0f : (lobes ? share * mixtureDensity(lobes, a.toward) + (1.0f - share) * f.density : f.density);
 							w              = a.density * a.density / (a.density * a.density + pm * pm);
 						}
 						const float4 offer = scale4(mul4(mul4(T, f.value), spectrumOf(a.arriving.x, a.arriving.y, a.arriving.z, nm)), facing * w);
@@ -633,11 +641,31 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 				}
 				// scatter (trace.cpp:1020 scatteredFrom)
 				if (!capped) {
-					const float lobe = number(stream, index, depth, Lobe);
+					float lobe       = number(stream, index, depth, Lobe);
 					const float side = number(stream, index, depth, Side);
 					const float du   = number(stream, index, depth, DirectionU);
 					const float dv   = number(stream, index, depth, DirectionV);
-					Scatter s        = sampleSurface(surf, m, outgoing, nm, lobe, side, du, dv, material, medium);
+					Scatter s;
+					if (lobes != nullptr && lobe < share) {
+						// drawn from the guide: weighed by the mixture's density
+						s               = noScatter();
+						s.incoming      = mixtureSample(lobes, lobe / share, du, dv);
+						const Response f = respond(surf, m, outgoing, s.incoming, nm);
+						s.density       = share * mixtureDensity(lobes, s.incoming) + (1.0f - share) * f.density;
+						const float cosine = fabsf(dot3(s.incoming, normal));
+						s.found         = s.density > 0.0f && max4(f.value) > 0.0f;
+						s.weight        = scale4(f.value, cosine / fmaxf(s.density, 1e-30f));
+					} else {
+						if (lobes != nullptr) lobe = (lobe - share) / (1.0f - share);
+						s = sampleSurface(surf, m, outgoing, nm, lobe, side, du, dv, material, medium);
+						if (lobes != nullptr && s.found && !s.delta) {
+							// the BSDF's draw weighed by the mixture's density
+							const Response f   = respond(surf, m, outgoing, s.incoming, nm);
+							s.density          = share * mixtureDensity(lobes, s.incoming) + (1.0f - share) * f.density;
+							const float cosine = fabsf(dot3(s.incoming, normal));
+							s.weight           = scale4(f.value, cosine / fmaxf(s.density, 1e-30f));
+						}
+					}
 					const float sideOf = dot3(s.incoming, normal);
 					const bool below   = s.through ? sideOf >= 0.0f : sideOf <= 0.0f;
 					if (s.found && !below) {
@@ -662,6 +690,13 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 							const float off       = sideOf > 0.0f ? lift : -lift;
 							next                  = makeRay(point + normal * off, s.incoming, __int_as_float(0x7f800000), medium);
 							A.paths.drawn[p]      = aimed ? s.density : 0.0f;
+							if (A.records != nullptr && depth < kGuideDepth && guidable(m.kind)) {
+								GuideRecord& r = A.records[size_t(p) * kGuideDepth + depth];
+								r.point[0] = point.x, r.point[1] = point.y, r.point[2] = point.z;
+								r.normal[0] = normal.x, r.normal[1] = normal.y, r.normal[2] = normal.z;
+								r.direction[0] = s.incoming.x, r.direction[1] = s.incoming.y, r.direction[2] = s.incoming.z;
+								r.reached = T0.x + T0.y + T0.z + T0.w;
+							}
 							A.paths.from[p]       = make_float4(point.x, point.y, point.z, 0.0f);
 							uint32_t stNext       = uint32_t(depth + 1) | (medium == kNoMaterial ? 0u : ((medium + 1u) << 16));
 							if (s.dispersed || ((st >> 9) & 1u)) stNext |= 1u << 9;

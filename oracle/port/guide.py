@@ -147,8 +147,10 @@ def mixture(out):
     kappa = np.exp(np.clip(c, KAPPA_LO, KAPPA_HI))
     m = o[:, :, 2:5]
     norm = np.sqrt((m * m).sum(axis=2))
-    safe = np.maximum(norm, 1e-6)
-    mu = m / safe[:, :, None]
+    # a mean of length under 1e-6 is read as +z, and passes no gradient
+    flat = norm <= 1e-6
+    safe = np.where(flat, np.inf, norm)
+    mu = np.where(flat[:, :, None], np.array([0.0, 0.0, 1.0]), m / np.maximum(norm, 1e-6)[:, :, None])
     return pi, kappa, mu, safe, live
 
 
