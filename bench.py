@@ -293,6 +293,11 @@ def run_gpu(args) -> None:
                 line["cpu_baseline"] = cpu_baseline(scene)
             except Exception as e:  # the oracle is test infrastructure; report why it could not run
                 line["cpu_baseline"] = {"value": None, "unit": "Msamples/s", "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {e}"}
+        if not (args.no_cpu or args.no_guide):
+            try:
+                line["guided"] = guided(local)
+            except Exception as e:  # report why the guided run could not finish
+                line["guided"] = {"failed": str(e)}
         if not (args.no_cpu or args.no_serve):
             try:
                 line["serving"] = serving(b)
@@ -302,6 +307,109 @@ def run_gpu(args) -> None:
     b.close()
     if dist:
         dist.destroy_process_group()
+
+
+# The learned-guide run (config 4's scene: the config-1 primitives in a
+# closed room lit through a 5% aperture): plain BSDF sampling against the
+# learned guide at equal wall time, training included, in relative MSE
+# against a high-sample plain frame.  The frame is 480x270 (a quarter of
+# 1080p a side) so that the reference frame of 4096 spp stays within
+# seconds; the guide is config 4's (2^19 entries a level, Adam lr 1e-2,
+# trained on the first 8 spp).
+GUIDE_SCENE = os.path.join(ROOT, "tests", "golden", "scenes", "room.npz")
+GUIDE_W, GUIDE_H, GUIDE_SURFACES, GUIDE_REF_SPP, GUIDE_PLAIN_SPP, GUIDE_TRAIN_SPP = 480, 270, 8, 4096, 64, 8
+
+
+def guided(device: int) -> dict:
+    import kodanuki_gb300 as K
+    from kodanuki_gb300.scene import Scene
+
+    sc = Scene.load(GUIDE_SCENE)
+
+    def rel(img, ref):
+        return float(np.mean((img - ref) ** 2 / (ref ** 2 + 0.01)))
+
+    def timed(fn):
+        t0 = time.perf_counter()
+        out = fn()
+        return out, time.perf_counter() - t0
+
+    with K.Backend(device) as b:
+        b.load(sc)
+        b.build(5, 10, 64)
+        b.render(GUIDE_W, GUIDE_H, 4, surfaces=GUIDE_SURFACES, seed=9)  # warm-up
+        ref, ref_s = timed(lambda: b.render(GUIDE_W, GUIDE_H, GUIDE_REF_SPP, surfaces=GUIDE_SURFACES, seed=101))
+        plain, plain_s = timed(lambda: b.render(GUIDE_W, GUIDE_H, GUIDE_PLAIN_SPP, surfaces=GUIDE_SURFACES, seed=7))
+        lo = np.asarray(sc.region_lower, np.float64)
+        hi = lo + np.asarray(sc.region_size, np.float64)
+        with K.Guide(device, table_log2=19, seed=2, region=(lo, hi), learning_rate=1e-2, batch=16384, max_steps=256) as g:
+            b.set_guide(g, 0.5, K.GUIDE_TRAIN)
+            t0 = time.perf_counter()
+            for k in range(GUIDE_TRAIN_SPP):
+                b.render(GUIDE_W, GUIDE_H, 1, surfaces=GUIDE_SURFACES, seed=2000 + k)
+            train_s = time.perf_counter() - t0
+            b.set_guide(g, 0.5, K.GUIDE_SAMPLE)
+            _, pilot_s = timed(lambda: b.render(GUIDE_W, GUIDE_H, 8, surfaces=GUIDE_SURFACES, seed=3))
+            spp = max(1, int((plain_s - train_s) / (pilot_s / 8)))
+            img, guided_s = timed(lambda: b.render(GUIDE_W, GUIDE_H, spp, surfaces=GUIDE_SURFACES, seed=7))
+            # equal samples too, to separate the sampling gain from the cost
+            same, _ = timed(lambda: b.render(GUIDE_W, GUIDE_H, GUIDE_PLAIN_SPP, surfaces=GUIDE_SURFACES, seed=7))
+            b.set_guide(None)
+            # the network's kernels alone: a training step and a query launch
+            rng = np.random.default_rng(5)
+            n = 1 << 16
+            p = rng.uniform(lo, hi, size=(n, 3))
+            nv = rng.normal(size=(n, 3))
+            nv /= np.linalg.norm(nv, axis=1, keepdims=True)
+            d = rng.normal(size=(n, 3))
+            d /= np.linalg.norm(d, axis=1, keepdims=True)
+            samples = np.concatenate([p, nv, d, np.ones((n, 1))], axis=1).astype(np.float32)
+            g.train(samples, batch=16384, steps=4)
+            _, t_train = timed(lambda: g.train(samples, batch=16384, steps=64))
+            rows = samples[:, :6].copy()
+            g.query(rows)
+            _, t_query = timed(lambda: g.query(rows))
+    rp, rg, rs = rel(plain, ref), rel(img, ref), rel(same, ref)
+    flops = 2 * (48 * 64 + 64 * 64 * 2 + 64 * 48)  # a sample's forward pass
+    return {
+        "workload": f"config-4 room scene (64 primitives in a closed room, 5% aperture), {GUIDE_W}x{GUIDE_H}, {GUIDE_SURFACES} surfaces; "
+                    f"reference {GUIDE_REF_SPP} spp plain",
+        "reference_s": ref_s,
+        "plain": {"spp": GUIDE_PLAIN_SPP, "seconds": plain_s, "relmse": rp},
+        "guided": {"train_spp": GUIDE_TRAIN_SPP, "train_s": train_s, "spp": spp, "seconds": train_s + guided_s, "relmse": rg},
+        "equal_time_gain": rp / rg if rg > 0 else None,
+        "equal_spp_gain": rp / rs if rs > 0 else None,
+        "train_samples_per_s": 64 * 16384 / t_train,
+        "train_tflops": 3 * flops * 64 * 16384 / t_train / 1e12,
+        "query_rows_per_s": n / t_query,
+        "note": "train and query rates are host-timed around whole calls (with copies); the network is 3 x 64 wide, so its tensor work is small beside the encoding's gathers",
+    }
+
+
+def guide_profile(device: int) -> None:
+    """Two training frames (each ends in Adam steps of 16384 samples) and one
+    guided frame of the room scene at 480x270: a short run for profilers."""
+    import kodanuki_gb300 as K
+    from kodanuki_gb300.scene import Scene
+
+    sc = Scene.load(GUIDE_SCENE)
+    with K.Backend(device) as b:
+        b.load(sc)
+        b.build(5, 10, 64)
+        lo = np.asarray(sc.region_lower, np.float64)
+        hi = lo + np.asarray(sc.region_size, np.float64)
+        with K.Guide(device, table_log2=19, seed=2, region=(lo, hi), batch=16384, max_steps=16) as g:
+            b.set_guide(g, 0.5, K.GUIDE_TRAIN)
+            t0 = time.perf_counter()
+            for k in range(2):
+                b.render(GUIDE_W, GUIDE_H, 1, surfaces=GUIDE_SURFACES, seed=2000 + k)
+            train_s = time.perf_counter() - t0
+            b.set_guide(g, 0.5, K.GUIDE_SAMPLE)
+            t0 = time.perf_counter()
+            img = b.render(GUIDE_W, GUIDE_H, 4, surfaces=GUIDE_SURFACES, seed=7)
+            guided_s = time.perf_counter() - t0
+            b.set_guide(None)
+    print(json.dumps({"guide_profile": True, "train_s": train_s, "guided_s": guided_s, "finite": bool(np.isfinite(img).all())}), flush=True)
 
 
 # The serving run (bounded): Poisson arrivals over four
@@ -401,10 +509,14 @@ def main() -> None:
     ap.add_argument("--spp", type=int, default=SPP)
     ap.add_argument("--no-cpu", action="store_true", help="leave out the CPU baseline and the serving run (profiling captures)")
     ap.add_argument("--no-serve", action="store_true", help="leave out the serving run")
+    ap.add_argument("--no-guide", action="store_true", help="leave out the learned-guide run")
+    ap.add_argument("--guide-profile", action="store_true", help="a short learned-guide run alone (profiling captures): two training frames and one guided frame of the room scene")
     args = ap.parse_args()
     WIDTH, HEIGHT, SPP = args.width, args.height, args.spp
     if args.impl == "reference":
         run_reference(args)
+    elif args.guide_profile:
+        guide_profile(env_int("LOCAL_RANK", 0))
     else:
         run_gpu(args)
 

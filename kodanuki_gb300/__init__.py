@@ -365,6 +365,12 @@ class Backend:
         self._check(self.lib.kdn_extend(self.handle, _ptr(r), r.shape[0], _ptr(hits)))
         return hits
 
+    def set_guide(self, guide, share: float = 0.5, flags: int = 3) -> None:
+        """Frames draw with the learned guide (GUIDE_SAMPLE, once trained)
+        and train it on their paths (GUIDE_TRAIN); None: plain frames."""
+        h = guide.handle if guide is not None else None
+        self._check(self.lib.kdn_set_guide(self.handle, h, share, flags if guide is not None else 0))
+
     def render(self, width: int, height: int, samples: int, surfaces: int | None = None, seed: int | None = None,
                first: int = 0, accumulate: bool = False, denoise: bool = False, restart: bool = False) -> np.ndarray:
         """Draw `samples` samples a pixel and return the pixel means
