@@ -578,6 +578,12 @@ int kdn_guide_ready(const kdn_guide* guide);
 #define KDN_GUIDE_SAMPLE 1u
 #define KDN_GUIDE_TRAIN 2u
 kdn_status kdn_set_guide(kdn_ctx* ctx, kdn_guide* guide, float share, uint32_t flags);
+/* Keeps the guide's sampling only where it pays: draws two pilot frames
+ * plain and two guided (the pilot's size, samples, surfaces and seeds seed,
+ * seed + 1), measures each method's relative variance times its frame time,
+ * and sets or clears KDN_GUIDE_SAMPLE on ctx by the lower; *guided says
+ * which.  The costs are written where the pointers are not null. */
+kdn_status kdn_guide_select(kdn_ctx* ctx, const kdn_frame* pilot, int* guided, double* plain_cost, double* guided_cost);
 
 #ifdef __cplusplus
 }

@@ -88,6 +88,7 @@ EXPORTS = [
     "kdn_serve_latency", "kdn_serve_last_error", "kdn_serve_close", "kdn_serve_cancel_queued", "kdn_set_sm_limit", "kdn_serve_reset_latency",
     "kdn_guide_open", "kdn_guide_close", "kdn_guide_last_error", "kdn_guide_sizes", "kdn_guide_get_params", "kdn_guide_set_params",
     "kdn_guide_gradients", "kdn_guide_train", "kdn_guide_query", "kdn_guide_clear_samples", "kdn_guide_ready", "kdn_set_guide",
+    "kdn_guide_select",
 ]
 
 REQUEST_INTERACTIVE = 4
@@ -193,6 +194,7 @@ def library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.kdn_guide_clear_samples.argtypes = [P]
     L.kdn_guide_ready.argtypes = [P]
     L.kdn_set_guide.argtypes = [P, P, ctypes.c_float, ctypes.c_uint32]
+    L.kdn_guide_select.argtypes = [P, ctypes.POINTER(Frame), ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
     for name in EXPORTS:
         fn = getattr(L, name)
         if name not in ("kdn_status_string", "kdn_last_error", "kdn_serve_last_error", "kdn_guide_last_error"):
@@ -370,6 +372,15 @@ class Backend:
         and train it on their paths (GUIDE_TRAIN); None: plain frames."""
         h = guide.handle if guide is not None else None
         self._check(self.lib.kdn_set_guide(self.handle, h, share, flags if guide is not None else 0))
+
+    def guide_select(self, width: int, height: int, samples: int, surfaces: int | None = None, seed: int = 1):
+        """Pilot frames decide whether the attached guide's sampling stays on
+        (kdn_guide_select): returns (guided, plain cost, guided cost)."""
+        sc = self.scene
+        f = Frame(width, height, samples, surfaces if surfaces is not None else int(sc.render["surfaces"]), seed, 0, 0, 0)
+        g, pc, gc = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
+        self._check(self.lib.kdn_guide_select(self.handle, ctypes.byref(f), ctypes.byref(g), ctypes.byref(pc), ctypes.byref(gc)))
+        return bool(g.value), pc.value, gc.value
 
     def render(self, width: int, height: int, samples: int, surfaces: int | None = None, seed: int | None = None,
                first: int = 0, accumulate: bool = False, denoise: bool = False, restart: bool = False) -> np.ndarray:

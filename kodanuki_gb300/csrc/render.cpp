@@ -12,6 +12,7 @@
 #include "guide.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 
@@ -770,6 +771,56 @@ kdn_status kdn_render(kdn_ctx* handle, const kdn_frame* frame, float* out_rgb) {
 	std::lock_guard<std::mutex> guard(ctx->lock);
 	if (ctx->device < 0) return ctx->fail(KDN_NO_DEVICE, "kdn_render: a host-only context has no device");
 	return renderFrame(ctx, frame, out_rgb, ctx->stream, true);
+}
+
+// Keep the learned guide where it pays: two independent pilot frames drawn
+// plain and two drawn guided give each method's relative variance,
+// mean((A - B)^2 / (((A + B) / 2)^2 + 0.01)) / 2, and, times its frame time,
+// its cost at equal time; the guide's sampling stays on only where its cost
+// is the lower.  Training (KDN_GUIDE_TRAIN) is left as it was, and off
+// during the pilots.
+kdn_status kdn_guide_select(kdn_ctx* handle, const kdn_frame* pilot, int* guided, double* plain_cost, double* guided_cost) {
+	if (handle == nullptr || pilot == nullptr || guided == nullptr) return KDN_BAD_ARG;
+	Context* ctx = reinterpret_cast<Context*>(handle);
+	std::lock_guard<std::mutex> guard(ctx->lock);
+	if (ctx->device < 0) return ctx->fail(KDN_NO_DEVICE, "kdn_guide_select: a host-only context has no device");
+	if (ctx->guide == nullptr || !kdn_guide_ready(ctx->guide)) return ctx->fail(KDN_NOT_READY, "kdn_guide_select: no trained guide on this context");
+	const uint32_t flags = ctx->guideFlags;
+	const size_t n       = size_t(pilot->width) * size_t(pilot->height) * 3;
+	std::vector<float> img[4];
+	double seconds[2]    = { 0.0, 0.0 };
+	kdn_frame fr         = *pilot;
+	fr.accumulate        = 0;
+	fr.flags             = 0;
+	for (int k = 0; k < 4; ++k) {
+		const bool useGuide = k >= 2;
+		ctx->guideFlags     = useGuide ? KDN_GUIDE_SAMPLE : 0u;
+		fr.seed             = pilot->seed + uint32_t(k % 2);
+		img[k].assign(n, 0.0f);
+		const auto t0 = std::chrono::steady_clock::now();
+		kdn_status s  = renderFrame(ctx, &fr, img[k].data(), ctx->stream, true);
+		seconds[useGuide ? 1 : 0] += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+		if (s != KDN_OK) {
+			ctx->guideFlags = flags;
+			return s;
+		}
+	}
+	double cost[2];
+	for (int m = 0; m < 2; ++m) {
+		const std::vector<float>& A = img[2 * m];
+		const std::vector<float>& B = img[2 * m + 1];
+		double sum = 0.0;
+		for (size_t i = 0; i < n; ++i) {
+			const double d = double(A[i]) - double(B[i]), mean = 0.5 * (double(A[i]) + double(B[i]));
+			sum += d * d / (mean * mean + 0.01);
+		}
+		cost[m] = sum / double(n) / 2.0 * (seconds[m] / 2.0);
+	}
+	*guided         = cost[1] < cost[0] ? 1 : 0;
+	ctx->guideFlags = (flags & ~KDN_GUIDE_SAMPLE) | (*guided ? KDN_GUIDE_SAMPLE : 0u);
+	if (plain_cost) *plain_cost = cost[0];
+	if (guided_cost) *guided_cost = cost[1];
+	return KDN_OK;
 }
 
 kdn_status kdn_render_device(kdn_ctx* handle, const kdn_frame* frame, float* out_rgb, void* stream) {

@@ -75,3 +75,31 @@ def test_training_while_guided_and_plain_frames_unchanged(room):
         g.close()
     after = b.render(32, 24, 4, surfaces=SURFACES, seed=5)
     assert np.array_equal(before, after)
+
+
+def test_select_keeps_a_useful_guide_and_drops_a_harmful_one(room):
+    """kdn_guide_select's pilots keep the trained guide on the room (it
+    gains there) and turn off a guide trained to point into the surfaces."""
+    import kodanuki_gb300 as K
+    b, sc, _ = room
+    g = trained_guide(b, sc)
+    try:
+        b.set_guide(g, 0.5, K.GUIDE_SAMPLE)
+        keep, pc, gc = b.guide_select(W, H, 16, surfaces=SURFACES, seed=21)
+        assert keep and gc < pc, (pc, gc)
+    finally:
+        b.set_guide(None)
+        g.close()
+    lo = np.asarray(sc.region_lower, np.float64)
+    hi = lo + np.asarray(sc.region_size, np.float64)
+    with K.Guide(0, table_log2=16, seed=4, region=(lo, hi)) as bad:
+        rng = np.random.default_rng(1)
+        n = 1 << 15
+        p = rng.uniform(lo, hi, size=(n, 3))
+        nv = np.tile([0.0, 0.0, 1.0], (n, 1))
+        d = np.tile([0.0, 0.0, -1.0], (n, 1))  # straight into the surface
+        bad.train(np.concatenate([p, nv, d, np.ones((n, 1))], axis=1).astype(np.float32), batch=4096, steps=200)
+        b.set_guide(bad, 0.9, K.GUIDE_SAMPLE)
+        keep, pc, gc = b.guide_select(W, H, 16, surfaces=SURFACES, seed=21)
+        assert not keep and gc > pc, (pc, gc)
+        b.set_guide(None)
