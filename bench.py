@@ -310,14 +310,15 @@ def run_gpu(args) -> None:
 
 
 # The learned-guide run (config 4's scene: the config-1 primitives in a
-# closed room lit through a 5% aperture): plain BSDF sampling against the
-# learned guide at equal wall time, training included, in relative MSE
-# against a high-sample plain frame.  The frame is 480x270 (a quarter of
-# 1080p a side) so that the reference frame of 4096 spp stays within
-# seconds; the guide is config 4's (2^19 entries a level, Adam lr 1e-2,
-# trained on the first 8 spp).
+# closed room lit through a 5% aperture) at 1920x1080: plain BSDF sampling
+# against the learned guide at equal wall time, training included, in
+# relative MSE against a plain frame of 512 spp (8x the plain frame's: its
+# own noise adds about an eighth of the plain frame's relMSE to both
+# figures).  The guide is config 4's (2^19 entries a level, Adam lr 1e-2,
+# trained on the first 8 spp: one training frame of 8 spp).
 GUIDE_SCENE = os.path.join(ROOT, "tests", "golden", "scenes", "room.npz")
-GUIDE_W, GUIDE_H, GUIDE_SURFACES, GUIDE_REF_SPP, GUIDE_PLAIN_SPP, GUIDE_TRAIN_SPP = 480, 270, 8, 4096, 64, 8
+GUIDE_W, GUIDE_H, GUIDE_SURFACES, GUIDE_REF_SPP, GUIDE_PLAIN_SPP, GUIDE_TRAIN_SPP = 1920, 1080, 8, 512, 64, 8
+PROFILE_W, PROFILE_H = 480, 270
 
 
 def guided(device: int) -> dict:
@@ -345,8 +346,7 @@ def guided(device: int) -> dict:
         with K.Guide(device, table_log2=19, seed=2, region=(lo, hi), learning_rate=1e-2, batch=16384, max_steps=256) as g:
             b.set_guide(g, 0.5, K.GUIDE_TRAIN)
             t0 = time.perf_counter()
-            for k in range(GUIDE_TRAIN_SPP):
-                b.render(GUIDE_W, GUIDE_H, 1, surfaces=GUIDE_SURFACES, seed=2000 + k)
+            b.render(GUIDE_W, GUIDE_H, GUIDE_TRAIN_SPP, surfaces=GUIDE_SURFACES, seed=2000)
             train_s = time.perf_counter() - t0
             b.set_guide(g, 0.5, K.GUIDE_SAMPLE)
             _, pilot_s = timed(lambda: b.render(GUIDE_W, GUIDE_H, 8, surfaces=GUIDE_SURFACES, seed=3))
@@ -376,7 +376,8 @@ def guided(device: int) -> dict:
                     f"reference {GUIDE_REF_SPP} spp plain",
         "reference_s": ref_s,
         "plain": {"spp": GUIDE_PLAIN_SPP, "seconds": plain_s, "relmse": rp},
-        "guided": {"train_spp": GUIDE_TRAIN_SPP, "train_s": train_s, "spp": spp, "seconds": train_s + guided_s, "relmse": rg},
+        "guided": {"train_spp": GUIDE_TRAIN_SPP, "train_s": train_s, "spp": spp, "seconds": train_s + guided_s, "relmse": rg,
+                   "seconds_per_spp": pilot_s / 8, "plain_seconds_per_spp": plain_s / GUIDE_PLAIN_SPP},
         "equal_time_gain": rp / rg if rg > 0 else None,
         "equal_spp_gain": rp / rs if rs > 0 else None,
         "train_samples_per_s": 64 * 16384 / t_train,
@@ -388,7 +389,7 @@ def guided(device: int) -> dict:
 
 def guide_profile(device: int) -> None:
     """Two training frames (each ends in Adam steps of 16384 samples) and one
-    guided frame of the room scene at 480x270: a short run for profilers."""
+    guided frame of the room scene at PROFILE_W x PROFILE_H: a short run for profilers."""
     import kodanuki_gb300 as K
     from kodanuki_gb300.scene import Scene
 
@@ -402,11 +403,11 @@ def guide_profile(device: int) -> None:
             b.set_guide(g, 0.5, K.GUIDE_TRAIN)
             t0 = time.perf_counter()
             for k in range(2):
-                b.render(GUIDE_W, GUIDE_H, 1, surfaces=GUIDE_SURFACES, seed=2000 + k)
+                b.render(PROFILE_W, PROFILE_H, 1, surfaces=GUIDE_SURFACES, seed=2000 + k)
             train_s = time.perf_counter() - t0
             b.set_guide(g, 0.5, K.GUIDE_SAMPLE)
             t0 = time.perf_counter()
-            img = b.render(GUIDE_W, GUIDE_H, 4, surfaces=GUIDE_SURFACES, seed=7)
+            img = b.render(PROFILE_W, PROFILE_H, 4, surfaces=GUIDE_SURFACES, seed=7)
             guided_s = time.perf_counter() - t0
             b.set_guide(None)
     print(json.dumps({"guide_profile": True, "train_s": train_s, "guided_s": guided_s, "finite": bool(np.isfinite(img).all())}), flush=True)

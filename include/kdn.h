@@ -545,7 +545,7 @@ typedef struct kdn_guide_options {
 	float region_hi[3];
 	uint32_t batch;           /* samples an Adam step (0: 16384) */
 	uint32_t max_steps;       /* Adam steps a training frame at most (0: 256) */
-	uint32_t sample_capacity; /* training samples a frame keeps (0: 2^22) */
+	uint32_t sample_capacity; /* training samples a frame keeps (0: 2^24), an even share of its records */
 } kdn_guide_options;
 
 kdn_status kdn_guide_open(int device, const kdn_guide_options* options, kdn_guide** out);

@@ -617,7 +617,10 @@ __global__ void packKernel(const float* w, uint8_t* packed) {
 }
 
 // a chunk's records into samples; the warp's finds compacted by ballot and prefix
-__global__ void gatherKernel(const GuideRecord* rec, const float4* radiance, uint32_t paths, float* samples, uint32_t* count, uint32_t capacity) {
+// A record is kept where a hash of its path and vertex falls under keep (of
+// 2^24): a frame with more records than the samples hold keeps an even share
+// of every part of the frame, not its first pixels.
+__global__ void gatherKernel(const GuideRecord* rec, const float4* radiance, uint32_t paths, float* samples, uint32_t* count, uint32_t capacity, uint32_t keepShare, uint32_t salt) {
 	const uint32_t lane = threadIdx.x & 31u;
 	for (uint32_t base = blockIdx.x * blockDim.x; base < paths; base += gridDim.x * blockDim.x) {
 		const uint32_t p = base + threadIdx.x;
@@ -635,6 +638,11 @@ __global__ void gatherKernel(const GuideRecord* rec, const float4* radiance, uin
 				r    = rec[size_t(p) * kGuideDepth + v];
 				w    = (total - r.before) / r.reached;
 				keep = isfinite(r.direction[0]) && isfinite(r.before) && r.reached > 0.0f && w > 0.0f && isfinite(w);
+				uint32_t h = ((p * uint32_t(kGuideDepth) + uint32_t(v)) ^ salt) * 0x9E3779B1u;
+				h ^= h >> 15;
+				h *= 0x2C1B3C6Du;
+				h ^= h >> 12;
+				keep = keep && (h & 0xFFFFFFu) < keepShare;
 			}
 			const uint32_t mask = __ballot_sync(0xFFFFFFFFu, keep);
 			if (mask == 0) continue;
@@ -787,9 +795,12 @@ cudaError_t guideQueryQueue(kdn_guide* g, const GuideQueue& queue, uint32_t capa
 	return launchQuery(a, capacity, stream, smCount);
 }
 
-cudaError_t guideGather(kdn_guide* g, const GuideRecord* records, const float4* radiance, uint32_t paths, cudaStream_t stream, int smCount) {
+cudaError_t guideGather(kdn_guide* g, const GuideRecord* records, const float4* radiance, uint32_t paths, uint64_t framePaths, uint32_t salt, cudaStream_t stream, int smCount) {
 	const uint32_t blocks = std::min((paths + 255u) / 256u, uint32_t(std::max(1, smCount)) * 8u);
-	gatherKernel<<<std::max(1u, blocks), 256, 0, stream>>>(records, radiance, paths, g->samples, g->count, g->capacity);
+	// about half the vertices leave a record: keep an even share that fills the samples
+	const double share    = std::min(1.0, double(g->capacity) / (0.5 * double(framePaths) * kGuideDepth));
+	const uint32_t keep   = share >= 1.0 ? (1u << 24) : uint32_t(share * double(1u << 24));
+	gatherKernel<<<std::max(1u, blocks), 256, 0, stream>>>(records, radiance, paths, g->samples, g->count, g->capacity, keep, salt);
 	return cudaGetLastError();
 }
 
@@ -837,7 +848,7 @@ kdn_status kdn_guide_open(int device, const kdn_guide_options* o, kdn_guide** ou
 	          grab((void**)&g->wV, kWeights * 4) && grab((void**)&g->table, tf * 4) && grab((void**)&g->tGrad, tf * 4) && grab((void**)&g->tM, tf * 4) &&
 	          grab((void**)&g->tV, tf * 4) && grab((void**)&g->tHalf, tf * 2) && grab((void**)&g->packed, kPacked) && grab((void**)&g->loss, 4) &&
 	          grab((void**)&g->error, 4) && grab((void**)&g->count, 4) && cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) == cudaSuccess;
-	const uint32_t cap = o->sample_capacity ? o->sample_capacity : (1u << 22);
+	const uint32_t cap = o->sample_capacity ? o->sample_capacity : (1u << 24);
 	if (ok) ok = ensureSamples(g, cap) == KDN_OK;
 	if (!ok) {
 		tError = "guide: device allocation failed";

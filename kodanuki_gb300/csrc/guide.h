@@ -44,7 +44,7 @@ __host__ __device__ __forceinline__ bool guidable(uint32_t kind) { return kind =
 // inference over a bounce's queue (no launch where the guide is not ready)
 cudaError_t guideQueryQueue(kdn_guide* guide, const GuideQueue& queue, uint32_t capacity, cudaStream_t stream, int smCount);
 // the records of a chunk's paths into the guide's training samples
-cudaError_t guideGather(kdn_guide* guide, const GuideRecord* records, const float4* radiance, uint32_t paths, cudaStream_t stream, int smCount);
+cudaError_t guideGather(kdn_guide* guide, const GuideRecord* records, const float4* radiance, uint32_t paths, uint64_t framePaths, uint32_t salt, cudaStream_t stream, int smCount);
 // one training pass over the samples gathered so far (reads their count:
 // synchronises the stream), then clears them
 kdn_status guideTrainGathered(kdn_guide* guide, cudaStream_t stream);

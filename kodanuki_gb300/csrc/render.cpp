@@ -644,7 +644,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		if (!ctx->check(launchFold(c, LP, first, chunk, spp, static_cast<double*>(f.sums.ptr), denoised ? static_cast<float*>(f.frameLight.ptr) : nullptr, on, ctx->smCount), "fold kernel")) return KDN_CUDA_ERROR;
 		++launches;
 		if (training) {
-			if (!ctx->check(guideGather(ctx->guide, L.records, LP.radiance, n, on, ctx->smCount), "guide gather kernel")) return KDN_CUDA_ERROR;
+			if (!ctx->check(guideGather(ctx->guide, L.records, LP.radiance, n, uint64_t(pixels) * spp, uint32_t(fr->seed) * 0x85EBCA6Bu + first, on, ctx->smCount), "guide gather kernel")) return KDN_CUDA_ERROR;
 			++launches;
 		}
 	}
