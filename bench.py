@@ -349,6 +349,7 @@ def guided(device: int) -> dict:
             b.render(GUIDE_W, GUIDE_H, GUIDE_TRAIN_SPP, surfaces=GUIDE_SURFACES, seed=2000)
             train_s = time.perf_counter() - t0
             b.set_guide(g, 0.5, K.GUIDE_SAMPLE)
+            b.render(GUIDE_W, GUIDE_H, 1, surfaces=GUIDE_SURFACES, seed=4)  # the guided path's buffers, allocated once
             _, pilot_s = timed(lambda: b.render(GUIDE_W, GUIDE_H, 8, surfaces=GUIDE_SURFACES, seed=3))
             spp = max(1, int((plain_s - train_s) / (pilot_s / 8)))
             img, guided_s = timed(lambda: b.render(GUIDE_W, GUIDE_H, spp, surfaces=GUIDE_SURFACES, seed=7))
