@@ -104,9 +104,12 @@ def test_training_fits_a_field_of_directions():
         return np.concatenate([p, nv, d, np.ones((n, 1), np.float32)], axis=1)
 
     with _guide(seed=5) as g:
-        train = draw(1 << 17)
+        # online, as the renderer trains: ~2 passes over many samples, not
+        # many passes over few (the fine levels would learn the samples
+        # themselves and lose the held-out ones)
+        train = draw(1 << 20)
         first = g.train(train, batch=8192, steps=1)
-        last = g.train(train, batch=8192, steps=800)
+        last = g.train(train, batch=8192, steps=300)
         held = draw(4096)
         lobes = g.query(held[:, 0:6])
         q = G.density(_lobes_as_outputs(lobes), held[:, 6:9].astype(np.float64))
