@@ -355,9 +355,11 @@ def guided(device: int) -> dict:
             img, guided_s = timed(lambda: b.render(GUIDE_W, GUIDE_H, spp, surfaces=GUIDE_SURFACES, seed=7))
             # equal samples too, to separate the sampling gain from the cost
             same, _ = timed(lambda: b.render(GUIDE_W, GUIDE_H, GUIDE_PLAIN_SPP, surfaces=GUIDE_SURFACES, seed=7))
-            # the fallback: pilot frames (a quarter of the frame a side, 16 spp)
-            # keep the guide's sampling only where it costs less at equal time
-            (keep, plain_cost, guided_cost), select_s = timed(lambda: b.guide_select(GUIDE_W // 4, GUIDE_H // 4, 16, surfaces=GUIDE_SURFACES, seed=41))
+            # the fallback: pilot frames (the frame's own size, 4 spp) keep the
+            # guide's sampling only where it costs less at equal time; a pilot
+            # of another size misjudges it, since a frame's time per sample
+            # depends on its size
+            (keep, plain_cost, guided_cost), select_s = timed(lambda: b.guide_select(GUIDE_W, GUIDE_H, 4, surfaces=GUIDE_SURFACES, seed=41))
             b.set_guide(None)
             # the network's kernels alone: a training step and a query launch
             rng = np.random.default_rng(5)
@@ -383,7 +385,7 @@ def guided(device: int) -> dict:
         "guided": {"train_spp": GUIDE_TRAIN_SPP, "train_s": train_s, "spp": spp, "seconds": train_s + guided_s, "relmse": rg,
                    "seconds_per_spp": pilot_s / 8, "plain_seconds_per_spp": plain_s / GUIDE_PLAIN_SPP},
         "select": {"kept_guide": keep, "plain_cost": plain_cost, "guided_cost": guided_cost, "seconds": select_s,
-                   "pilot": f"2 plain + 2 guided frames of {GUIDE_W // 4}x{GUIDE_H // 4} at 16 spp"},
+                   "pilot": f"2 plain + 2 guided frames of {GUIDE_W}x{GUIDE_H} at 4 spp"},
         "equal_time_gain": rp / rg if rg > 0 else None,
         "equal_spp_gain": rp / rs if rs > 0 else None,
         "train_samples_per_s": 64 * 16384 / t_train,
