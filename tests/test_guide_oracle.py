@@ -57,3 +57,26 @@ def test_corner_weights_sum_to_one_and_stay_in_table():
     idx, w = G.corners(pos, -1.0, 1.0, 12)
     assert np.allclose(w.sum(axis=2), 1.0, atol=1e-5)
     assert idx.min() >= 0 and idx.max() < (1 << 12)
+
+
+def test_set_guide_checks_its_arguments_without_a_device():
+    """kdn_set_guide on a host-only context: no guide detaches (OK), unknown
+    flags and a share outside (0, 1) with a guide are refused; the guide
+    entry points refuse null handles."""
+    import ctypes
+
+    import kodanuki_gb300 as K
+    from helpers import host_backend
+
+    b = host_backend()
+    L = b.lib
+    assert L.kdn_set_guide(b.handle, None, ctypes.c_float(0.5), 0) == K.KDN_OK
+    assert L.kdn_set_guide(b.handle, None, ctypes.c_float(0.5), 8) == K.KDN_BAD_ARG
+    fake = ctypes.c_void_p(1)  # never dereferenced: the share is refused first
+    assert L.kdn_set_guide(b.handle, fake, ctypes.c_float(1.5), K.GUIDE_SAMPLE) == K.KDN_BAD_ARG
+    assert L.kdn_guide_close(None) == K.KDN_BAD_ARG
+    assert L.kdn_guide_ready(None) == 0
+    o = K.GuideOptions()
+    o.table_log2 = 30  # past the limit: refused before any device call
+    h = ctypes.c_void_p()
+    assert L.kdn_guide_open(0, ctypes.byref(o), ctypes.byref(h)) == K.KDN_BAD_ARG
