@@ -578,11 +578,16 @@ int kdn_guide_ready(const kdn_guide* guide);
 #define KDN_GUIDE_SAMPLE 1u
 #define KDN_GUIDE_TRAIN 2u
 kdn_status kdn_set_guide(kdn_ctx* ctx, kdn_guide* guide, float share, uint32_t flags);
-/* Keeps the guide's sampling only where it pays: draws two pilot frames
- * plain and two guided (the pilot's size, samples, surfaces and seeds seed,
- * seed + 1), measures each method's relative variance times its frame time,
- * and sets or clears KDN_GUIDE_SAMPLE on ctx by the lower; *guided says
- * which.  The costs are written where the pointers are not null. */
+/* Keeps the guide's sampling only where it pays: after one untimed frame
+ * of each method, draws pairs of pilot frames plain and guided (the pilot's
+ * size, samples and surfaces; seeds seed + 1 ...), measures each method's
+ * relative variance of a frame times its device frame time (the frame's
+ * CUDA events), and keeps KDN_GUIDE_SAMPLE on ctx only where the guided
+ * cost is more than 5% below the plain one; *guided says which.  Pairs are
+ * drawn (3 to 16) until the cost ratio lies two standard errors from that
+ * margin.  The costs (relative variance x seconds) are written where the
+ * pointers are not null.  KDN_BAD_ARG for a pilot of no or too many pixels
+ * (2^26), samples (2^20) or surfaces (255). */
 kdn_status kdn_guide_select(kdn_ctx* ctx, const kdn_frame* pilot, int* guided, double* plain_cost, double* guided_cost);
 
 #ifdef __cplusplus

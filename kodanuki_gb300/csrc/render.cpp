@@ -12,7 +12,6 @@
 #include "guide.h"
 
 #include <algorithm>
-#include <chrono>
 #include <cmath>
 #include <cstring>
 
@@ -773,50 +772,107 @@ kdn_status kdn_render(kdn_ctx* handle, const kdn_frame* frame, float* out_rgb) {
 	return renderFrame(ctx, frame, out_rgb, ctx->stream, true);
 }
 
-// Keep the learned guide where it pays: two independent pilot frames drawn
-// plain and two drawn guided give each method's relative variance,
-// mean((A - B)^2 / (((A + B) / 2)^2 + 0.01)) / 2, and, times its frame time,
-// its cost at equal time; the guide's sampling stays on only where its cost
-// is the lower.  Training (KDN_GUIDE_TRAIN) is left as it was, and off
-// during the pilots.
+// Keep the learned guide where it pays.  Each method (plain, guided) draws
+// pairs of independent pilot frames; a pair (A, B) gives the method's
+// relative variance of one frame, mean((A - B)^2 / (((A + B) / 2)^2 + 0.01))
+// / 2, and the mean of those times the mean device time of its frames (the
+// frame's own CUDA events, kdn_frame_stats.total_ms, launch to last kernel)
+// is its cost at equal time.  One untimed frame of each method comes first,
+// so the guided path's buffers are allocated and both paths' kernels warm
+// before any pilot is timed, and the methods' frames alternate so a drift in
+// the GPU's clocks falls on both.  A frame's time varies far more than its
+// variance (on small frames it is set by the few slowest rays), so pairs are
+// drawn until the log of the cost ratio lies more than two standard errors
+// (from the spread of the pairs' variances and of the frames' times) from
+// the margin, kSelectLeastPairs at least and kSelectMostPairs at most.  The
+// guide's sampling stays on only where its cost is below the plain cost by
+// more than kSelectMargin.  Training (KDN_GUIDE_TRAIN) is left as it was,
+// and off during the pilots.
+constexpr int kSelectLeastPairs = 3;
+constexpr int kSelectMostPairs  = 16;
+constexpr double kSelectMargin  = 0.05;
+
+namespace {
+
+// Mean and squared relative standard error of the mean of n values from
+// their sum and sum of squares.
+struct Moments {
+	double sum = 0.0, squares = 0.0;
+	int n      = 0;
+	void add(double v) {
+		sum += v;
+		squares += v * v;
+		++n;
+	}
+	double mean() const { return n > 0 ? sum / n : 0.0; }
+	double relativeError2() const {
+		if (n < 2 || sum <= 0.0) return 0.0;
+		const double m = sum / n, var = std::max(0.0, (squares - n * m * m) / (n - 1));
+		return var / (n * m * m);
+	}
+};
+
+} // namespace
+
 kdn_status kdn_guide_select(kdn_ctx* handle, const kdn_frame* pilot, int* guided, double* plain_cost, double* guided_cost) {
 	if (handle == nullptr || pilot == nullptr || guided == nullptr) return KDN_BAD_ARG;
 	Context* ctx = reinterpret_cast<Context*>(handle);
 	std::lock_guard<std::mutex> guard(ctx->lock);
+	if (pilot->width <= 0 || pilot->height <= 0 || pilot->samples <= 0 || pilot->samples > (1 << 20) || pilot->surfaces <= 0 || pilot->surfaces > 255 ||
+	    uint64_t(pilot->width) * uint64_t(pilot->height) > (uint64_t(1) << 26))
+		return ctx->fail(KDN_BAD_ARG, "kdn_guide_select: the pilot's width and height (at most 2^26 pixels), samples (1..2^20) and surfaces (1..255) must be positive");
 	if (ctx->device < 0) return ctx->fail(KDN_NO_DEVICE, "kdn_guide_select: a host-only context has no device");
 	if (ctx->guide == nullptr || !kdn_guide_ready(ctx->guide)) return ctx->fail(KDN_NOT_READY, "kdn_guide_select: no trained guide on this context");
 	const uint32_t flags = ctx->guideFlags;
 	const size_t n       = size_t(pilot->width) * size_t(pilot->height) * 3;
-	std::vector<float> img[4];
-	double seconds[2]    = { 0.0, 0.0 };
-	kdn_frame fr         = *pilot;
-	fr.accumulate        = 0;
-	fr.flags             = 0;
-	for (int k = 0; k < 4; ++k) {
-		const bool useGuide = k >= 2;
-		ctx->guideFlags     = useGuide ? KDN_GUIDE_SAMPLE : 0u;
-		fr.seed             = pilot->seed + uint32_t(k % 2);
-		img[k].assign(n, 0.0f);
-		const auto t0 = std::chrono::steady_clock::now();
-		kdn_status s  = renderFrame(ctx, &fr, img[k].data(), ctx->stream, true);
-		seconds[useGuide ? 1 : 0] += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-		if (s != KDN_OK) {
-			ctx->guideFlags = flags;
-			return s;
-		}
+	std::vector<float> img[2][2];
+	for (auto& m : img) {
+		for (auto& v : m) v.assign(n, 0.0f);
 	}
-	double cost[2];
-	for (int m = 0; m < 2; ++m) {
-		const std::vector<float>& A = img[2 * m];
-		const std::vector<float>& B = img[2 * m + 1];
-		double sum = 0.0;
-		for (size_t i = 0; i < n; ++i) {
-			const double d = double(A[i]) - double(B[i]), mean = 0.5 * (double(A[i]) + double(B[i]));
-			sum += d * d / (mean * mean + 0.01);
-		}
-		cost[m] = sum / double(n) / 2.0 * (seconds[m] / 2.0);
+	Moments ms[2], variance[2];
+	kdn_frame fr       = *pilot;
+	fr.accumulate      = 0;
+	fr.flags           = 0;
+	kdn_status s       = KDN_OK;
+	// warm-up: one untimed frame a method
+	for (int m = 0; m < 2 && s == KDN_OK; ++m) {
+		ctx->guideFlags = m == 1 ? KDN_GUIDE_SAMPLE : 0u;
+		fr.seed         = pilot->seed;
+		s               = renderFrame(ctx, &fr, img[m][0].data(), ctx->stream, true);
 	}
-	*guided         = cost[1] < cost[0] ? 1 : 0;
+	const double threshold = -std::log(1.0 - kSelectMargin); // log(plain cost / guided cost) past which the guide pays
+	double logRatio        = 0.0;
+	for (int p = 0; p < kSelectMostPairs && s == KDN_OK; ++p) {
+		for (int k = 0; k < 2 && s == KDN_OK; ++k) {
+			for (int m = 0; m < 2 && s == KDN_OK; ++m) {
+				ctx->guideFlags = m == 1 ? KDN_GUIDE_SAMPLE : 0u;
+				fr.seed         = pilot->seed + uint32_t(2 * p + k + 1);
+				s               = renderFrame(ctx, &fr, img[m][k].data(), ctx->stream, true);
+				if (s == KDN_OK) ms[m].add(double(ctx->frame->stats.total_ms) * 1e-3);
+			}
+		}
+		if (s != KDN_OK) break;
+		for (int m = 0; m < 2; ++m) {
+			const std::vector<float>& A = img[m][0];
+			const std::vector<float>& B = img[m][1];
+			double sum = 0.0;
+			for (size_t i = 0; i < n; ++i) {
+				const double d = double(A[i]) - double(B[i]), mean = 0.5 * (double(A[i]) + double(B[i]));
+				sum += d * d / (mean * mean + 0.01);
+			}
+			variance[m].add(sum / double(n) / 2.0);
+		}
+		const double cp = variance[0].mean() * ms[0].mean(), cg = variance[1].mean() * ms[1].mean();
+		logRatio        = cp > 0.0 && cg > 0.0 ? std::log(cp / cg) : 0.0;
+		const double se = std::sqrt(variance[0].relativeError2() + variance[1].relativeError2() + ms[0].relativeError2() + ms[1].relativeError2());
+		if (p + 1 >= kSelectLeastPairs && std::fabs(logRatio - threshold) > 2.0 * se) break;
+	}
+	if (s != KDN_OK) {
+		ctx->guideFlags = flags;
+		return s;
+	}
+	const double cost[2] = { variance[0].mean() * ms[0].mean(), variance[1].mean() * ms[1].mean() };
+	*guided              = logRatio > threshold ? 1 : 0;
 	ctx->guideFlags = (flags & ~KDN_GUIDE_SAMPLE) | (*guided ? KDN_GUIDE_SAMPLE : 0u);
 	if (plain_cost) *plain_cost = cost[0];
 	if (guided_cost) *guided_cost = cost[1];

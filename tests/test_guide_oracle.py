@@ -80,3 +80,9 @@ def test_set_guide_checks_its_arguments_without_a_device():
     o.table_log2 = 30  # past the limit: refused before any device call
     h = ctypes.c_void_p()
     assert L.kdn_guide_open(0, ctypes.byref(o), ctypes.byref(h)) == K.KDN_BAD_ARG
+    # pilot frames of no or of too many pixels, samples or surfaces are refused
+    # before any host buffer is sized for them
+    g, pc, gc = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
+    for w, h_, spp, surf in [(-1, 64, 4, 6), (64, 0, 4, 6), (1 << 20, 1 << 20, 4, 6), (64, 64, 0, 6), (64, 64, 1 << 21, 6), (64, 64, 4, 0), (64, 64, 4, 256)]:
+        f = K.Frame(w, h_, spp, surf, 1, 0, 0, 0)
+        assert L.kdn_guide_select(b.handle, ctypes.byref(f), ctypes.byref(g), ctypes.byref(pc), ctypes.byref(gc)) == K.KDN_BAD_ARG, (w, h_, spp, surf)
