@@ -232,7 +232,7 @@ typedef struct kdn_frame_stats {
 	uint32_t longest_march; /* the most march steps one ray took */
 	uint64_t capped_rays;   /* rays that ran out of march steps (65536) */
 	uint32_t trace_launches; /* launches of the sphere-trace kernel in trace_ms */
-	uint32_t pad_;
+	uint32_t carried_rays;   /* marches carried to a later launch (kdn_set_march_budget) */
 } kdn_frame_stats;
 
 const char* kdn_status_string(kdn_status status);
@@ -264,6 +264,17 @@ kdn_status kdn_set_frame_budget(kdn_ctx* ctx, uint64_t bytes);
 /* Size this context's kernel grids for `sms` SMs (0: all of the device's),
  * so its frames leave the other SMs to work on other streams. */
 kdn_status kdn_set_sm_limit(kdn_ctx* ctx, int sms);
+
+/* March steps a ray may take in one trace launch of this context's frames
+ * (0, the default, or 65536 and above: no limit).  A ray past it stops with
+ * its march state (distance and step count) and goes on in the next launch,
+ * so no launch waits for the few rays that skim a surface for thousands of
+ * steps (the reference marches each ray to its end in one call,
+ * plugins/geometry/sphere_trace/sphere_trace.cpp:203, at most 65536 steps,
+ * sphere_trace.h:20); a path whose shadow line is still marching waits for
+ * it before its next vertex is shaded.  Frames are the same to the bit with
+ * any budget.  Frames sampling the learned guide march without a budget. */
+kdn_status kdn_set_march_budget(kdn_ctx* ctx, uint32_t steps);
 
 /*
  * Copy one block into the context (core/block.h:565 Block {name, data,

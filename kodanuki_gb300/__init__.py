@@ -70,7 +70,7 @@ class FrameStats(ctypes.Structure):
     _fields_ = [("total_ms", ctypes.c_double), ("trace_ms", ctypes.c_double), ("shade_ms", ctypes.c_double), ("other_ms", ctypes.c_double),
                 ("segments", ctypes.c_uint64), ("march_steps", ctypes.c_uint64), ("program_steps", ctypes.c_uint64),
                 ("launches", ctypes.c_uint32), ("longest_march", ctypes.c_uint32), ("capped_rays", ctypes.c_uint64),
-                ("trace_launches", ctypes.c_uint32), ("pad", ctypes.c_uint32)]
+                ("trace_launches", ctypes.c_uint32), ("carried_rays", ctypes.c_uint32)]
 
 
 class KdnError(RuntimeError):
@@ -88,7 +88,7 @@ EXPORTS = [
     "kdn_serve_latency", "kdn_serve_last_error", "kdn_serve_close", "kdn_serve_cancel_queued", "kdn_set_sm_limit", "kdn_serve_reset_latency",
     "kdn_guide_open", "kdn_guide_close", "kdn_guide_last_error", "kdn_guide_sizes", "kdn_guide_get_params", "kdn_guide_set_params",
     "kdn_guide_gradients", "kdn_guide_train", "kdn_guide_query", "kdn_guide_clear_samples", "kdn_guide_ready", "kdn_set_guide",
-    "kdn_guide_select",
+    "kdn_guide_select", "kdn_set_march_budget",
 ]
 
 REQUEST_INTERACTIVE = 4
@@ -170,6 +170,7 @@ def library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.kdn_open_sharing.argtypes = [P, ctypes.c_int, ctypes.POINTER(P)]
     L.kdn_set_frame_budget.argtypes = [P, ctypes.c_uint64]
     L.kdn_set_sm_limit.argtypes = [P, ctypes.c_int]
+    L.kdn_set_march_budget.argtypes = [P, ctypes.c_uint32]
     L.kdn_serve_reset_latency.argtypes = [P]
     L.kdn_serve_open.argtypes = [ctypes.POINTER(ServeOptions), ctypes.POINTER(P)]
     L.kdn_serve_add_scene.argtypes = [P, P, ctypes.POINTER(ctypes.c_uint32)]
@@ -407,6 +408,12 @@ class Backend:
 
     def set_frame_budget(self, nbytes: int) -> None:
         self._check(self.lib.kdn_set_frame_budget(self.handle, nbytes))
+
+    def set_march_budget(self, steps: int) -> None:
+        """March steps a ray may take in one trace launch of this context's
+        frames before it goes on in the next (kdn_set_march_budget; 0: none).
+        Frames are the same to the bit with any budget."""
+        self._check(self.lib.kdn_set_march_budget(self.handle, steps))
 
     def frame_stats(self) -> FrameStats:
         s = FrameStats()

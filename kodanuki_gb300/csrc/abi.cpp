@@ -145,6 +145,14 @@ kdn_status kdn_set_frame_budget(kdn_ctx* handle, uint64_t bytes) {
 	return KDN_OK;
 }
 
+kdn_status kdn_set_march_budget(kdn_ctx* handle, uint32_t steps) {
+	if (handle == nullptr) return KDN_BAD_ARG;
+	Context* ctx = reinterpret_cast<Context*>(handle);
+	std::lock_guard<std::mutex> guard(ctx->lock);
+	ctx->marchBudget = steps >= kdn::kMarchSteps ? 0u : steps;
+	return KDN_OK;
+}
+
 kdn_status kdn_set_guide(kdn_ctx* handle, kdn_guide* guide, float share, uint32_t flags) {
 	if (handle == nullptr || (guide != nullptr && !(share > 0.0f && share < 1.0f)) || (flags & ~(KDN_GUIDE_SAMPLE | KDN_GUIDE_TRAIN)) != 0) return KDN_BAD_ARG;
 	Context* ctx = reinterpret_cast<Context*>(handle);

@@ -36,6 +36,9 @@ struct Context {
 	std::atomic<int> sharers { 0 }; // contexts drawing this one's world
 	// the most device bytes a frame's path buffers may take (0: half the free memory)
 	uint64_t frameBudget = 0;
+	// march steps a ray takes in one trace launch of a frame before it is
+	// carried to the next (0: no budget; kdn_set_march_budget)
+	uint32_t marchBudget = 0;
 	std::mutex lock;
 	std::string error;
 	std::map<std::string, std::vector<uint8_t>> blocks;

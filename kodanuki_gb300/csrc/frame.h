@@ -114,14 +114,21 @@ struct PathBuffers {
 	float4* nanometres;
 	float4* density;
 	float* drawn;         // density of the last scattered direction, 0 when exact
-	uint32_t* state;      // depth (bits 0-7), camera leg (bit 8), dispersed (bit 9), medium + 1 (bits 16-31)
+	uint32_t* state;      // depth (bits 0-7), camera leg (bit 8), dispersed (bit 9), line pending (bit 10), medium + 1 (bits 16-31)
 	float4* from;         // xyz: where the leg was drawn from
 };
+
+// PathBuffers::state bit 10: the path's shadow line was carried to a later
+// trace launch and is not answered yet, so the path's next vertex waits
+// (its radiance takes the line's share before the next vertex's meets, in
+// the order of a frame without a march budget).
+constexpr uint32_t kLinePending = 1u << 10;
 
 struct QueueBuffers {
 	uint32_t* paths;      // path index of each queued ray
 	kdn_ray* rays;
 	uint32_t* count;      // device count
+	uint2* carry;         // resume data of each ray slot (TraceArgs::carry)
 };
 
 struct ShadowBuffers {
@@ -130,6 +137,7 @@ struct ShadowBuffers {
 	float4* contribution;
 	uint32_t* count;
 	HitState* states;
+	uint2* carry;         // resume data of each line slot
 };
 
 struct ShadeArgs {
@@ -138,6 +146,7 @@ struct ShadeArgs {
 	QueueBuffers out;
 	ShadowBuffers shadow;
 	const kdn_hit* hits;
+	const HitState* states; // where each ray's march ended (a held path resumes there)
 	Looks looks;
 	uint32_t capacity;
 	uint32_t* error;
@@ -169,7 +178,8 @@ struct SurfaceArgs {
 
 cudaError_t launchCamera(const FrameConstants& frame, const PathBuffers& paths, const QueueBuffers& queue, uint32_t firstPixel, uint32_t n, cudaStream_t stream, int smCount);
 cudaError_t launchShade(const FrameConstants& frame, const ShadeArgs& args, cudaStream_t stream, int smCount);
-cudaError_t launchLines(const PathBuffers& paths, const ShadowBuffers& shadow, uint32_t capacity, cudaStream_t stream, int smCount);
+// Answers the lines traced in a launch (in); carried lines go on in out.
+cudaError_t launchLines(const PathBuffers& paths, const ShadowBuffers& in, const ShadowBuffers& out, uint32_t capacity, cudaStream_t stream, int smCount);
 // light (may be null): each pixel's mean of this call's samples, RGB float
 cudaError_t launchFold(const FrameConstants& frame, const PathBuffers& paths, uint32_t firstPixel, uint32_t pixels, uint32_t spp, double* sums, float* light, cudaStream_t stream, int smCount);
 cudaError_t launchMeans(const double* sums, uint32_t pixels, double taken, float* out, cudaStream_t stream, int smCount);

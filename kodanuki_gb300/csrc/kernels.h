@@ -13,7 +13,10 @@ namespace kdn {
 
 // Where a ray's march ended: kind 0 none, 1 surface at distance, 2 a crossing
 // into a solid of another material (read past the point); first/index name
-// the kept program that is least there.
+// the kept program that is least there.  Kind kCarried: the ray used up its
+// march budget for this launch and goes on in a later one from distance,
+// after steps march steps (its resume data, TraceArgs::carry).
+constexpr uint32_t kCarried = 3;
 struct HitState {
 	uint32_t kind;
 	float distance;
@@ -36,7 +39,23 @@ struct TraceArgs {
 	// count read on the device (null: none); traced in the same launch
 	const uint32_t* secondCount = nullptr;
 	uint32_t second             = 0;
+	// Carried rays (null: none).  A ray whose pad_[0] has bit 0 set resumes
+	// its march where carry[ray] says (x: distance bits, y: march steps so
+	// far) instead of at the region's edge; with budget > 0 a ray that has
+	// taken budget march steps in this launch stops as kCarried.  The march
+	// is deterministic, so a carried ray ends where it would have in one launch.
+	const uint2* carry = nullptr;
+	uint32_t budget    = 0;
+	// where set, a count that must be zero (path rays left after a frame's
+	// last round): added to counters[6], which the host checks
+	const uint32_t* left = nullptr;
 };
+
+// kdn_hit.kind of a carried ray: distance is where its march stands, cell
+// its march steps so far.
+constexpr uint8_t kHitCarried = 0xFE;
+// kdn_ray.pad_[0] bit 0: the ray resumes a carried march.
+constexpr uint8_t kRayResumes = 1;
 
 struct HitArgs {
 	DeviceWorld world;

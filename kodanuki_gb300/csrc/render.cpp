@@ -23,8 +23,12 @@ static_assert(kLanes >= 1 && kLanes <= 64, "a lane takes one of the context's 64
 
 struct FrameState {
 	DeviceBuffer pixel, sample, throughput, radiance, nanometres, density, drawn, state, from;
-	DeviceBuffer queuePaths[2], queueRays[2], hits, states, counts;
-	DeviceBuffer shadowPaths, shadowContribution;
+	DeviceBuffer queuePaths[2], queueRays[2], queueCarry[2], hits, states, counts;
+	DeviceBuffer shadowPaths[2], shadowContribution[2];
+	// the surfaces pass's own queue, states and hits, so it runs beside the
+	// lanes' chunks on its own stream
+	DeviceBuffer surfacePaths, surfaceRays, surfaceStates, surfaceHits;
+	uint32_t surfaceCapacity = 0;
 	DeviceBuffer sums, out, materials;
 	DeviceBuffer patternSteps, stops, placements; // what patterned albedos read (Looks)
 	DeviceBuffer boundaries;                      // rough glasses' boundary tables (Looks)
@@ -48,13 +52,15 @@ struct FrameState {
 	cudaStream_t side[kLanes - 1] = {};   // the streams of the lanes after the first
 	cudaEvent_t started           = nullptr; // the first lane's work before the chunks
 	cudaEvent_t ended[kLanes - 1] = {};   // each other lane's end of the chunks
+	cudaStream_t surfaceStream    = nullptr; // the surfaces pass
+	cudaEvent_t surfacesDone      = nullptr; // its end
 	kdn_frame_stats stats {};
 };
 
 void Context::releaseFrame() {
 	if (frame == nullptr) return;
 	FrameState& f = *frame;
-	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.hits, &f.states, &f.counts, &f.shadowPaths, &f.shadowContribution, &f.sums, &f.out, &f.materials, &f.patternSteps, &f.stops, &f.placements, &f.boundaries, &f.frameLight, &f.firstDistance, &f.firstNormal, &f.firstAlbedo, &f.firstLeaf, &f.gDistance[0], &f.gDistance[1], &f.gNormal[0], &f.gNormal[1], &f.gAlbedo[0], &f.gAlbedo[1], &f.gLeaf[0], &f.gLeaf[1], &f.tColour[0], &f.tColour[1], &f.tMoment[0], &f.tMoment[1], &f.tLength[0], &f.tLength[1], &f.guideLobes, &f.guideRecords }) {
+	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.queueCarry[0], &f.queueCarry[1], &f.hits, &f.states, &f.counts, &f.shadowPaths[0], &f.shadowPaths[1], &f.shadowContribution[0], &f.shadowContribution[1], &f.surfacePaths, &f.surfaceRays, &f.surfaceStates, &f.surfaceHits, &f.sums, &f.out, &f.materials, &f.patternSteps, &f.stops, &f.placements, &f.boundaries, &f.frameLight, &f.firstDistance, &f.firstNormal, &f.firstAlbedo, &f.firstLeaf, &f.gDistance[0], &f.gDistance[1], &f.gNormal[0], &f.gNormal[1], &f.gAlbedo[0], &f.gAlbedo[1], &f.gLeaf[0], &f.gLeaf[1], &f.tColour[0], &f.tColour[1], &f.tMoment[0], &f.tMoment[1], &f.tLength[0], &f.tLength[1], &f.guideLobes, &f.guideRecords }) {
 		if (b->ptr) cudaFree(b->ptr);
 		b->ptr   = nullptr;
 		b->bytes = 0;
@@ -69,6 +75,11 @@ void Context::releaseFrame() {
 		cudaStreamSynchronize(side);
 		cudaStreamDestroy(side);
 	}
+	if (f.surfaceStream) {
+		cudaStreamSynchronize(f.surfaceStream);
+		cudaStreamDestroy(f.surfaceStream);
+	}
+	if (f.surfacesDone) cudaEventDestroy(f.surfacesDone);
 	delete frame;
 	frame = nullptr;
 }
@@ -245,11 +256,15 @@ namespace {
 
 // Device bytes one path of a chunk holds (the buffers ensureFrame sizes).
 // pixel, sample, drawn, state; throughput, radiance, nanometres, density,
-// from; the two queues' path indices and rays (a path ray and a shadow line
-// each); hits; hit states of a path ray and a line; the lines' path indices
-// and contributions.
-constexpr size_t kPathBytes = 4 * 4 + 5 * 16 + 2 * 4 + 2 * 2 * sizeof(kdn_ray) + sizeof(kdn_hit) + 2 * sizeof(kdn::HitState) + 4 + 16;
-static_assert(kPathBytes == 364, "path bytes");
+// from; the two queues' path indices, rays and resume data (a path ray and
+// a shadow line each); hits; hit states of a path ray and a line; the two
+// line queues' path indices and contributions.
+constexpr size_t kPathBytes = 4 * 4 + 5 * 16 + 2 * 4 + 2 * 2 * (sizeof(kdn_ray) + sizeof(uint2)) + sizeof(kdn_hit) + 2 * sizeof(kdn::HitState) + 2 * (4 + 16);
+static_assert(kPathBytes == 416, "path bytes");
+
+// A lane's device counts: [0], [1] the two ray queues, [2], [3] the two
+// line queues, [4] zero; the first lane's [6]: the surfaces pass's queue.
+constexpr int kCountsPerLane = 8;
 
 // The paths the lanes' chunks hold together: the whole frame where the
 // device has room for it (at most 2^28 paths, half the free memory), so
@@ -288,8 +303,9 @@ kdn_status ensureFrame(Context* ctx, uint32_t capacity) {
 		// a queue holds a bounce's path rays in [0, n) and the shadow lines of
 		// the bounce before in [n, 2n): one trace launch takes both
 		{ &f.queuePaths[0], n * 4 }, { &f.queuePaths[1], n * 4 }, { &f.queueRays[0], 2 * n * sizeof(kdn_ray) }, { &f.queueRays[1], 2 * n * sizeof(kdn_ray) },
-		{ &f.hits, n * sizeof(kdn_hit) }, { &f.states, 2 * n * sizeof(kdn::HitState) }, { &f.counts, kLanes * 4 * sizeof(uint32_t) },
-		{ &f.shadowPaths, n * 4 }, { &f.shadowContribution, n * 16 },
+		{ &f.queueCarry[0], 2 * n * sizeof(uint2) }, { &f.queueCarry[1], 2 * n * sizeof(uint2) },
+		{ &f.hits, n * sizeof(kdn_hit) }, { &f.states, 2 * n * sizeof(kdn::HitState) }, { &f.counts, kLanes * kCountsPerLane * sizeof(uint32_t) },
+		{ &f.shadowPaths[0], n * 4 }, { &f.shadowPaths[1], n * 4 }, { &f.shadowContribution[0], n * 16 }, { &f.shadowContribution[1], n * 16 },
 	};
 	for (const Want& w : wants) {
 		if ((s = ctx->ensure(*w.b, w.bytes)) != KDN_OK) return s;
@@ -443,8 +459,8 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	// share of the path buffers, queues and counters, so one chunk's work
 	// fills the SMs another chunk's launch leaves idle in its tail (the
 	// slowest rays of a trace launch).
-	uint32_t* counts = static_cast<uint32_t*>(f.counts.ptr); // a lane: [0],[1] ray queues, [2] lines, [3] zero
-	if (!ctx->check(cudaMemsetAsync(counts, 0, kLanes * 4 * sizeof(uint32_t), stream), "clear counts")) return KDN_CUDA_ERROR;
+	uint32_t* counts = static_cast<uint32_t*>(f.counts.ptr); // kCountsPerLane a lane
+	if (!ctx->check(cudaMemsetAsync(counts, 0, kLanes * kCountsPerLane * sizeof(uint32_t), stream), "clear counts")) return KDN_CUDA_ERROR;
 	cudaStream_t lanes[kLanes] = { stream };
 	for (int l = 1; l < kLanes; ++l) {
 		if (f.side[l - 1] == nullptr && !ctx->check(cudaStreamCreateWithPriority(&f.side[l - 1], cudaStreamNonBlocking, ctx->priority), "cudaStreamCreate")) return KDN_CUDA_ERROR;
@@ -454,8 +470,8 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	if (f.started == nullptr && !ctx->check(cudaEventCreateWithFlags(&f.started, cudaEventDisableTiming), "cudaEventCreate")) return KDN_CUDA_ERROR;
 	struct Lane {
 		PathBuffers P;
-		QueueBuffers Q[2];
-		ShadowBuffers S;
+		QueueBuffers Q[2];   // a bounce's path rays in [0, capacity) of rays and carry
+		ShadowBuffers S[2];  // the shadow lines traced with Q[k], in [capacity, 2 capacity)
 		HitState* states;
 		kdn_hit* hits;
 		uint32_t* none;
@@ -467,6 +483,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	for (int l = 0; l < kLanes; ++l) {
 		const size_t base = size_t(l) * capacity;
 		Lane& L           = lane[l];
+		uint32_t* lc      = counts + kCountsPerLane * l;
 		L.P               = P;
 		L.P.pixel         = P.pixel + base;
 		L.P.sample        = P.sample + base;
@@ -477,30 +494,40 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		L.P.drawn         = P.drawn + base;
 		L.P.state         = P.state + base;
 		L.P.from          = P.from + base;
+		// a queue's path rays and hit states in [0, capacity), the shadow lines
+		// traced with them in [capacity, 2 capacity): one trace launch takes both
+		L.states = static_cast<HitState*>(f.states.ptr) + 2 * base;
+		L.hits   = static_cast<kdn_hit*>(f.hits.ptr) + base;
 		for (int k = 0; k < 2; ++k) {
-			L.Q[k].paths = static_cast<uint32_t*>(f.queuePaths[k].ptr) + base;
-			L.Q[k].rays  = static_cast<kdn_ray*>(f.queueRays[k].ptr) + 2 * base;
-			L.Q[k].count = counts + 4 * l + k;
+			L.Q[k].paths        = static_cast<uint32_t*>(f.queuePaths[k].ptr) + base;
+			L.Q[k].rays         = static_cast<kdn_ray*>(f.queueRays[k].ptr) + 2 * base;
+			L.Q[k].carry        = static_cast<uint2*>(f.queueCarry[k].ptr) + 2 * base;
+			L.Q[k].count        = lc + k;
+			L.S[k].rays         = L.Q[k].rays + capacity;
+			L.S[k].carry        = L.Q[k].carry + capacity;
+			L.S[k].paths        = static_cast<uint32_t*>(f.shadowPaths[k].ptr) + base;
+			L.S[k].contribution = static_cast<float4*>(f.shadowContribution[k].ptr) + base;
+			L.S[k].count        = lc + 2 + k;
+			L.S[k].states       = L.states + capacity;
 		}
-		// the shadow lines a shade writes go to the second half of the next
-		// queue's rays (and of the hit states), so the next bounce's trace
-		// launch takes them with its path rays
-		L.states         = static_cast<HitState*>(f.states.ptr) + 2 * base;
-		L.hits           = static_cast<kdn_hit*>(f.hits.ptr) + base;
-		L.S.rays         = nullptr; // set a bounce: the second half of the next queue
-		L.S.paths        = static_cast<uint32_t*>(f.shadowPaths.ptr) + base;
-		L.S.contribution = static_cast<float4*>(f.shadowContribution.ptr) + base;
-		L.S.count        = counts + 4 * l + 2;
-		L.S.states       = L.states + capacity;
-		L.none           = counts + 4 * l + 3;
-		L.fetch          = static_cast<uint32_t*>(ctx->fetch.ptr) + l;
-		L.lobes          = guiding ? static_cast<float*>(f.guideLobes.ptr) + base * kGuideLobeFloats : nullptr;
-		L.records        = training ? static_cast<GuideRecord*>(f.guideRecords.ptr) + base * kGuideDepth : nullptr;
+		L.none    = lc + 4;
+		L.fetch   = static_cast<uint32_t*>(ctx->fetch.ptr) + l;
+		L.lobes   = guiding ? static_cast<float*>(f.guideLobes.ptr) + base * kGuideLobeFloats : nullptr;
+		L.records = training ? static_cast<GuideRecord*>(f.guideRecords.ptr) + base * kGuideDepth : nullptr;
 	}
+
+	// Rounds a chunk: surfaces + 1 (each traces the bounce's path rays and
+	// the lines of the bounce before; the last, the last lines).  With a
+	// march budget a path waits a round each time its ray or its line is
+	// carried, at most once a round, so surfaces + 1 more rounds without a
+	// budget finish every path that waited.
+	const bool budgeted     = ctx->marchBudget > 0 && ctx->marchBudget < kMarchSteps && !guiding;
+	const int mainRounds    = fr->surfaces + 1;
+	const int rounds        = budgeted ? 2 * mainRounds : mainRounds;
 
 	// timing: one event pair around the frame, one around each trace launch
 	const uint32_t chunks = (pixels + chunkPixels - 1) / chunkPixels;
-	const size_t traceEvents = size_t(chunks) * size_t(fr->surfaces + 1) * 2;
+	const size_t traceEvents = size_t(chunks) * size_t(rounds) * 2;
 	const size_t needEvents  = 2 + traceEvents;
 	while (f.events.size() < needEvents) {
 		cudaEvent_t e;
@@ -510,48 +537,66 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	size_t ev = 2;
 	if (!ctx->check(cudaEventRecord(f.events[0], stream), "event")) return KDN_CUDA_ERROR;
 	uint32_t launches = 0;
+	// the other lanes (and the surfaces pass) start after what the first holds so far
+	if (!ctx->check(cudaEventRecord(f.started, stream), "event")) return KDN_CUDA_ERROR;
+	for (int l = 1; l < kLanes; ++l) {
+		if (!ctx->check(cudaStreamWaitEvent(lanes[l], f.started, 0), "stream wait")) return KDN_CUDA_ERROR;
+	}
 	if (denoised) {
-		// core/surfaces.cpp:133 tracedSurfaces: the denoiser's features, on the
-		// first lane before its chunks
-		const Lane& L = lane[0];
-		for (uint32_t first = 0; first < pixels; first += capacity) {
-			const uint32_t n = std::min(capacity, pixels - first);
-			if (!ctx->check(launchSurfaceRays(c, L.Q[0], first, n, stream, ctx->smCount), "surface rays kernel")) return KDN_CUDA_ERROR;
+		// core/surfaces.cpp:133 tracedSurfaces: the denoiser's features, on a
+		// stream of its own beside the chunks, its own queue and hits
+		if (f.surfaceStream == nullptr && !ctx->check(cudaStreamCreateWithPriority(&f.surfaceStream, cudaStreamNonBlocking, ctx->priority), "cudaStreamCreate")) return KDN_CUDA_ERROR;
+		if (f.surfacesDone == nullptr && !ctx->check(cudaEventCreateWithFlags(&f.surfacesDone, cudaEventDisableTiming), "cudaEventCreate")) return KDN_CUDA_ERROR;
+		const uint32_t sc = std::min<uint32_t>(pixels, 1u << 22);
+		const struct {
+			DeviceBuffer* b;
+			size_t bytes;
+		} wants[] = { { &f.surfacePaths, size_t(sc) * 4 }, { &f.surfaceRays, size_t(sc) * sizeof(kdn_ray) }, { &f.surfaceStates, size_t(sc) * sizeof(HitState) },
+			          { &f.surfaceHits, size_t(sc) * sizeof(kdn_hit) } };
+		for (const auto& w : wants) {
+			if ((s = ctx->ensure(*w.b, w.bytes)) != KDN_OK) return s;
+		}
+		const cudaStream_t on = f.surfaceStream;
+		if (!ctx->check(cudaStreamWaitEvent(on, f.started, 0), "stream wait")) return KDN_CUDA_ERROR;
+		QueueBuffers sq;
+		sq.paths = static_cast<uint32_t*>(f.surfacePaths.ptr);
+		sq.rays  = static_cast<kdn_ray*>(f.surfaceRays.ptr);
+		sq.count = counts + kCountsPerLane * 0 + 6; // lane 0's spare count
+		sq.carry = nullptr;
+		for (uint32_t first = 0; first < pixels; first += sc) {
+			const uint32_t n = std::min(sc, pixels - first);
+			if (!ctx->check(launchSurfaceRays(c, sq, first, n, on, ctx->smCount), "surface rays kernel")) return KDN_CUDA_ERROR;
 			TraceArgs t;
 			t.world          = ctx->world;
-			t.rays           = L.Q[0].rays;
+			t.rays           = sq.rays;
 			t.n              = n;
-			t.states         = L.states;
+			t.states         = static_cast<HitState*>(f.surfaceStates.ptr);
 			t.objectMaterial = static_cast<const uint32_t*>(ctx->objectMaterial.ptr);
 			t.maxSteps       = kMarchSteps;
 			t.counters       = nullptr;
-			t.count          = L.Q[0].count;
-			t.fetch          = L.fetch;
-			if (!ctx->check(launchTrace(t, stream, ctx->smCount), "surface trace kernel")) return KDN_CUDA_ERROR;
+			t.count          = sq.count;
+			t.fetch          = static_cast<uint32_t*>(ctx->fetch.ptr) + kLanes;
+			if (!ctx->check(launchTrace(t, on, ctx->smCount), "surface trace kernel")) return KDN_CUDA_ERROR;
 			HitArgs h;
 			h.world  = ctx->world;
-			h.rays   = L.Q[0].rays;
+			h.rays   = sq.rays;
 			h.states = t.states;
 			h.n      = n;
-			h.hits   = L.hits;
-			h.count  = L.Q[0].count;
-			if (!ctx->check(launchHits(h, stream, ctx->smCount), "surface hit kernel")) return KDN_CUDA_ERROR;
+			h.hits   = static_cast<kdn_hit*>(f.surfaceHits.ptr);
+			h.count  = sq.count;
+			if (!ctx->check(launchHits(h, on, ctx->smCount), "surface hit kernel")) return KDN_CUDA_ERROR;
 			SurfaceArgs g;
-			g.rays         = L.Q[0];
+			g.rays         = sq;
 			g.hits         = h.hits;
 			g.looks        = looks;
 			g.distance     = static_cast<uint16_t*>(f.gDistance[cur].ptr);
 			g.normal       = static_cast<uint16_t*>(f.gNormal[cur].ptr);
 			g.albedo       = static_cast<uint16_t*>(f.gAlbedo[cur].ptr);
 			g.leaf         = static_cast<uint32_t*>(f.gLeaf[cur].ptr);
-			if (!ctx->check(launchSurfaces(g, n, stream, ctx->smCount), "surfaces kernel")) return KDN_CUDA_ERROR;
+			if (!ctx->check(launchSurfaces(g, n, on, ctx->smCount), "surfaces kernel")) return KDN_CUDA_ERROR;
 			launches += 4;
 		}
-	}
-	// the other lanes start after what the first holds so far
-	if (!ctx->check(cudaEventRecord(f.started, stream), "event")) return KDN_CUDA_ERROR;
-	for (int l = 1; l < kLanes; ++l) {
-		if (!ctx->check(cudaStreamWaitEvent(lanes[l], f.started, 0), "stream wait")) return KDN_CUDA_ERROR;
+		if (!ctx->check(cudaEventRecord(f.surfacesDone, on), "event")) return KDN_CUDA_ERROR;
 	}
 	uint32_t chunkIndex = 0;
 	for (uint32_t first = 0; first < pixels; first += chunkPixels, ++chunkIndex) {
@@ -564,12 +609,12 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		if (training && !ctx->check(cudaMemsetAsync(L.records, 0xFF, size_t(n) * kGuideDepth * sizeof(GuideRecord), on), "clear guide records")) return KDN_CUDA_ERROR;
 		if (!ctx->check(launchCamera(c, LP, L.Q[0], first, n, on, ctx->smCount), "camera kernel")) return KDN_CUDA_ERROR;
 		++launches;
-		if (!ctx->check(cudaMemsetAsync(L.S.count, 0, 4, on), "clear lines")) return KDN_CUDA_ERROR;
+		if (!ctx->check(cudaMemsetAsync(L.S[0].count, 0, 4, on), "clear lines")) return KDN_CUDA_ERROR;
 		int q = 0;
 		// each round traces the bounce's path rays and the bounce before's
 		// shadow lines in one launch; a last round traces the last lines alone
-		for (int bounce = 0; bounce <= fr->surfaces; ++bounce) {
-			const bool last = bounce == fr->surfaces;
+		for (int round = 0; round < rounds; ++round) {
+			const bool last = round == rounds - 1;
 			const int nxt   = 1 - q;
 			TraceArgs t;
 			t.world          = ctx->world;
@@ -581,8 +626,11 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 			t.counters       = static_cast<unsigned long long*>(ctx->counters.ptr);
 			t.count          = last ? L.none : L.Q[q].count;
 			t.fetch          = L.fetch;
-			t.secondCount    = L.S.count;
+			t.secondCount    = L.S[q].count;
 			t.second         = capacity;
+			t.carry          = L.Q[q].carry;
+			t.budget         = budgeted && round < mainRounds ? ctx->marchBudget : 0u;
+			t.left           = last ? L.Q[q].count : nullptr;
 			cudaEventRecord(f.events[ev++], on);
 			if (!ctx->check(launchTrace(t, on, ctx->smCount), "trace kernel")) return KDN_CUDA_ERROR;
 			cudaEventRecord(f.events[ev++], on);
@@ -597,7 +645,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 				h.count  = L.Q[q].count;
 				if (!ctx->check(launchHits(h, on, ctx->smCount), "hit kernel")) return KDN_CUDA_ERROR;
 				++launches;
-				if (guiding && bounce < kGuideDepth) {
+				if (guiding && round < kGuideDepth) {
 					GuideQueue gq;
 					gq.hits          = L.hits;
 					gq.rays          = L.Q[q].rays;
@@ -609,23 +657,22 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 					++launches;
 				}
 			}
-			if (bounce > 0) {
-				// the bounce before's lines that reached their lamps
-				ShadowBuffers lines = L.S;
-				lines.rays          = L.Q[q].rays + capacity;
-				if (!ctx->check(launchLines(LP, lines, capacity, on, ctx->smCount), "lines kernel")) return KDN_CUDA_ERROR;
+			if (!ctx->check(cudaMemsetAsync(L.S[nxt].count, 0, 4, on), "clear lines")) return KDN_CUDA_ERROR;
+			if (round > 0) {
+				// the bounce before's lines that reached their lamps; lines still
+				// marching go on with the next round's
+				if (!ctx->check(launchLines(LP, L.S[q], L.S[nxt], capacity, on, ctx->smCount), "lines kernel")) return KDN_CUDA_ERROR;
 				++launches;
 			}
 			if (last) break;
 			if (!ctx->check(cudaMemsetAsync(L.Q[nxt].count, 0, 4, on), "clear queue")) return KDN_CUDA_ERROR;
-			if (!ctx->check(cudaMemsetAsync(L.S.count, 0, 4, on), "clear lines")) return KDN_CUDA_ERROR;
 			ShadeArgs a;
 			a.paths         = LP;
 			a.in            = L.Q[q];
 			a.out           = L.Q[nxt];
-			a.shadow        = L.S;
-			a.shadow.rays   = L.Q[nxt].rays + capacity;
+			a.shadow        = L.S[nxt];
 			a.hits          = L.hits;
+			a.states        = L.states;
 			a.looks         = looks;
 			a.capacity      = capacity;
 			a.error         = nullptr;
@@ -633,7 +680,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 			a.firstNormal   = denoised ? static_cast<uint16_t*>(f.firstNormal.ptr) : nullptr;
 			a.firstAlbedo   = denoised ? static_cast<uint16_t*>(f.firstAlbedo.ptr) : nullptr;
 			a.firstLeaf     = denoised ? static_cast<uint32_t*>(f.firstLeaf.ptr) : nullptr;
-			a.lobes         = (guiding && bounce < kGuideDepth) ? L.lobes : nullptr;
+			a.lobes         = (guiding && round < kGuideDepth) ? L.lobes : nullptr;
 			a.guideShare    = ctx->guideShare;
 			a.records       = L.records;
 			if (!ctx->check(launchShade(c, a, on, ctx->smCount), "shade kernel")) return KDN_CUDA_ERROR;
@@ -647,10 +694,11 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 			++launches;
 		}
 	}
-	// the first lane goes on once the others are done
+	// the first lane goes on once the others and the surfaces pass are done
 	for (int l = 1; l < kLanes; ++l) {
 		if (!ctx->check(cudaEventRecord(f.ended[l - 1], lanes[l]), "event") || !ctx->check(cudaStreamWaitEvent(stream, f.ended[l - 1], 0), "stream wait")) return KDN_CUDA_ERROR;
 	}
+	if (denoised && !ctx->check(cudaStreamWaitEvent(stream, f.surfacesDone, 0), "stream wait")) return KDN_CUDA_ERROR;
 	if (training && (s = guideTrainGathered(ctx->guide, stream)) != KDN_OK) return ctx->fail(s, std::string("kdn_render: guide training: ") + kdn_guide_last_error());
 	f.taken += double(spp);
 	f.last_denoised = denoised;
@@ -753,6 +801,10 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	st.longest_march = uint32_t(host[2]);
 	st.capped_rays   = host[3];
 	st.segments      = host[4];
+	st.carried_rays  = uint32_t(std::min<unsigned long long>(host[5], 0xFFFFFFFFull));
+	// the rounds cover the longest wait a march budget can give a path: a
+	// path ray left after the last round would be a fault of this backend
+	if (host[6] != 0) return ctx->fail(KDN_CUDA_ERROR, "kdn_render: " + std::to_string(host[6]) + " path rays were left after the frame's last round");
 	st.trace_launches = uint32_t((ev - 2) / 2);
 	st.launches      = launches;
 	st.other_ms      = st.total_ms - st.trace_ms;

@@ -171,12 +171,16 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 	const uint32_t stride = blockDim.x;
 	float* slots          = slotMemory + threadIdx.x;
 	setConstants(slots, stride);
-	uint32_t marchSteps = 0, programSteps = 0, traced = 0, capped = 0, longest = 0;
+	uint32_t marchSteps = 0, programSteps = 0, traced = 0, capped = 0, longest = 0, carried = 0;
 	// the rays: [0, n1) and, after them in the fetch order, [second, second + n2)
 	const uint32_t n1 = args.count ? *args.count : args.n;
 	const uint32_t n  = n1 + (args.secondCount ? *args.secondCount : 0u);
 	const unsigned lane = threadIdx.x & 31u;
 
+	if (args.left != nullptr && args.counters != nullptr && blockIdx.x == 0 && threadIdx.x == 0) {
+		const uint32_t left = *args.left;
+		if (left) atomicAdd(&args.counters[6], (unsigned long long) left);
+	}
 	uint32_t mode = Fetch;
 	uint32_t ray  = 0;
 	float o[3], d[3], inv[3];
@@ -184,6 +188,7 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 	bool inside      = false;
 	uint32_t medium  = kNoLeaf;
 	uint32_t step    = 0;
+	uint32_t startStep = 0, stepLimit = 0; // the ray's steps when this launch took it, and where its budget ends
 	Located cell;
 	cell.leaf = kNoLeaf;
 	float exitT = 0.0f;
@@ -198,9 +203,10 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 	// a ray ends: its state, the step counts, and the next ray
 	auto done = [&](HitState h) {
 		args.states[ray] = h;
-		marchSteps += h.steps;
+		marchSteps += h.steps - startStep;
 		longest = max(longest, h.steps);
-		capped += h.steps >= args.maxSteps ? 1u : 0u;
+		capped += h.kind != kCarried && h.steps >= args.maxSteps ? 1u : 0u;
+		carried += h.kind == kCarried ? 1u : 0u;
 		mode = Fetch;
 	};
 
@@ -219,7 +225,6 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 					mode = Finished;
 				} else {
 					if (ray >= n1) ray = args.second + (ray - n1);
-					++traced;
 					const kdn_ray r = args.rays[ray];
 					for (int a = 0; a < 3; ++a) {
 						o[a]   = r.origin[a];
@@ -238,9 +243,19 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 					inside    = r.inside != 0;
 					medium    = r.within;
 					step      = 0;
+					// a carried ray goes on where its march stood
+					if (args.carry != nullptr && (r.pad_[0] & kRayResumes)) {
+						const uint2 c = args.carry[ray];
+						t             = __uint_as_float(c.x);
+						step          = c.y;
+					} else {
+						++traced; // a segment is counted once, in the launch that starts it
+					}
+					startStep = step;
+					stepLimit = args.budget > 0 ? step + args.budget : 0xFFFFFFFFu;
 					cell.leaf = kNoLeaf;
 					if (up < lo) {
-						done(HitState { 0, 0.0f, kNoLeaf, 0, 0 });
+						done(HitState { 0, t, kNoLeaf, 0, step });
 					} else {
 						mode = Locating;
 					}
@@ -252,8 +267,14 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 		// find the cell of the point, skipping empty cells, and start its first program
 		if (mode == Locating) {
 			for (uint32_t skipped = 0;;) {
+				// a miss keeps where its march stopped, so a held path can resume it
 				if (!(step < args.maxSteps && t <= up)) {
-					done(HitState { 0, 0.0f, kNoLeaf, 0, step });
+					done(HitState { 0, t, kNoLeaf, 0, step });
+					break;
+				}
+				// out of this launch's budget: the march's whole state is (t, step) here
+				if (step >= stepLimit) {
+					done(HitState { kCarried, t, 0, 0, step });
 					break;
 				}
 				for (int a = 0; a < 3; ++a) p[a] = o[a] + d[a] * t;
@@ -354,6 +375,7 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 			programSteps += __shfl_down_sync(0xFFFFFFFFu, programSteps, o);
 			traced += __shfl_down_sync(0xFFFFFFFFu, traced, o);
 			capped += __shfl_down_sync(0xFFFFFFFFu, capped, o);
+			carried += __shfl_down_sync(0xFFFFFFFFu, carried, o);
 			longest = max(longest, __shfl_down_sync(0xFFFFFFFFu, longest, o));
 		}
 		if ((threadIdx.x & 31) == 0) {
@@ -362,6 +384,7 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 			atomicMax(&args.counters[2], (unsigned long long) longest);
 			atomicAdd(&args.counters[3], (unsigned long long) capped);
 			atomicAdd(&args.counters[4], (unsigned long long) traced);
+			if (carried) atomicAdd(&args.counters[5], (unsigned long long) carried);
 		}
 	}
 }
@@ -387,7 +410,12 @@ __global__ void __launch_bounds__(kTraceBlock) hitKernel(HitArgs args) {
 		out.leaf_kind = 0;
 		out.pad1_[0] = out.pad1_[1] = out.pad1_[2] = 0;
 		out.cell      = kNoLeaf;
-		if (h.kind != 0) {
+		if (h.kind == kCarried) {
+			// the march goes on in a later launch: where it stands and its steps
+			out.kind     = kHitCarried;
+			out.distance = h.distance;
+			out.cell     = h.steps;
+		} else if (h.kind != 0) {
 			const float d[3]  = { ray.direction[0], ray.direction[1], ray.direction[2] };
 			const float t     = h.distance;
 			const float p[3]  = { ray.origin[0] + d[0] * t, ray.origin[1] + d[1] * t, ray.origin[2] + d[2] * t };

@@ -484,8 +484,25 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 		kdn_ray line {};
 		float4 lineRadiance = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 		uint32_t p = 0;
+		// a ray whose march was carried, or a path whose shadow line is still
+		// marching, waits a launch: its ray goes on from where its march stands
+		bool resumes   = false;
+		uint2 carryOut = make_uint2(0u, 0u);
 		if (live) {
-			p                   = A.in.paths[q];
+			p = A.in.paths[q];
+			const uint8_t kind = A.hits[q].kind;
+			if (kind == kHitCarried || (A.paths.state[p] & kLinePending)) {
+				const HitState h = A.states[q];
+				// a landed march resumes a step before its landing and lands again
+				const bool landed = h.kind == 1u || h.kind == 2u;
+				next              = A.in.rays[q];
+				next.pad_[0] |= kRayResumes;
+				carryOut = make_uint2(__float_as_uint(h.distance), landed ? h.steps - 1u : h.steps);
+				onward = resumes = true;
+				live             = false;
+			}
+		}
+		if (live) {
 			const kdn_hit hit   = A.hits[q];
 			const kdn_ray ray   = A.in.rays[q];
 			const uint32_t st   = A.paths.state[p];
@@ -712,6 +729,7 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 		if (onward && slot < A.capacity) {
 			A.out.paths[slot] = p;
 			A.out.rays[slot]  = next;
+			if (resumes) A.out.carry[slot] = carryOut;
 		}
 		const uint32_t lineSlot = warpSlot(A.shadow.count, lined);
 		if (lined && lineSlot < A.capacity) {
@@ -723,12 +741,36 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 }
 
 // ---- K-line: add each shadow line that reached its lamp (trace.cpp:1294 lineAnswered) ----
-__global__ void __launch_bounds__(kBlock) linesKernel(PathBuffers P, ShadowBuffers S) {
+// A line whose march was carried goes on in the next launch (out) and its
+// path waits for it (kLinePending); an answered line that had been carried
+// lets its path go on.  A path has at most one line in flight.
+__global__ void __launch_bounds__(kBlock) linesKernel(PathBuffers P, ShadowBuffers S, ShadowBuffers out, uint32_t capacity) {
 	const uint32_t n = *S.count;
-	for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
-		if (S.states[s].kind != 0) continue;
-		const uint32_t p = S.paths[s];
-		P.radiance[p]    = add4(P.radiance[p], S.contribution[s]);
+	for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+		const uint32_t s = base + threadIdx.x;
+		bool carried     = false;
+		HitState h {};
+		uint32_t p = 0;
+		if (s < n) {
+			h       = S.states[s];
+			p       = S.paths[s];
+			carried = h.kind == kCarried;
+			if (!carried) {
+				if (h.kind == 0) P.radiance[p] = add4(P.radiance[p], S.contribution[s]);
+				if (S.rays[s].pad_[0] & kRayResumes) P.state[p] &= ~kLinePending;
+			} else {
+				P.state[p] |= kLinePending;
+			}
+		}
+		const uint32_t slot = warpSlot(out.count, carried);
+		if (carried && slot < capacity) {
+			kdn_ray r = S.rays[s];
+			r.pad_[0] |= kRayResumes;
+			out.rays[slot]         = r;
+			out.carry[slot]        = make_uint2(__float_as_uint(h.distance), h.steps);
+			out.paths[slot]        = p;
+			out.contribution[slot] = S.contribution[s];
+		}
 	}
 }
 
@@ -780,8 +822,8 @@ cudaError_t launchShade(const FrameConstants& frame, const ShadeArgs& args, cuda
 	return cudaGetLastError();
 }
 
-cudaError_t launchLines(const PathBuffers& paths, const ShadowBuffers& shadow, uint32_t capacity, cudaStream_t stream, int smCount) {
-	linesKernel<<<gridFor(capacity, smCount), kBlock, 0, stream>>>(paths, shadow);
+cudaError_t launchLines(const PathBuffers& paths, const ShadowBuffers& in, const ShadowBuffers& out, uint32_t capacity, cudaStream_t stream, int smCount) {
+	linesKernel<<<gridFor(capacity, smCount), kBlock, 0, stream>>>(paths, in, out, capacity);
 	return cudaGetLastError();
 }
 
