@@ -171,7 +171,10 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 	const uint32_t stride = blockDim.x;
 	float* slots          = slotMemory + threadIdx.x;
 	setConstants(slots, stride);
-	uint32_t marchSteps = 0, programSteps = 0, traced = 0, capped = 0, longest = 0, carried = 0;
+	// capped rays in the low 16 bits, carried ones in the high: one register
+	uint32_t marchSteps = 0, programSteps = 0, traced = 0, cappedCarried = 0, longest = 0;
+	// the steps a ray may take in this launch: a launch's budget, or the cap
+	const uint32_t allowance = args.budget > 0 ? args.budget : kMarchSteps;
 	// the rays: [0, n1) and, after them in the fetch order, [second, second + n2)
 	const uint32_t n1 = args.count ? *args.count : args.n;
 	const uint32_t n  = n1 + (args.secondCount ? *args.secondCount : 0u);
@@ -188,7 +191,8 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 	bool inside      = false;
 	uint32_t medium  = kNoLeaf;
 	uint32_t step    = 0;
-	uint32_t startStep = 0, stepLimit = 0; // the ray's steps when this launch took it, and where its budget ends
+	// where the ray's march stops in this launch: the cap, or sooner its budget
+	uint32_t stepLimit = 0;
 	Located cell;
 	cell.leaf = kNoLeaf;
 	float exitT = 0.0f;
@@ -203,10 +207,9 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 	// a ray ends: its state, the step counts, and the next ray
 	auto done = [&](HitState h) {
 		args.states[ray] = h;
-		marchSteps += h.steps - startStep;
+		marchSteps += h.steps; // less the steps it had when taken (at the fetch)
 		longest = max(longest, h.steps);
-		capped += h.kind != kCarried && h.steps >= args.maxSteps ? 1u : 0u;
-		carried += h.kind == kCarried ? 1u : 0u;
+		cappedCarried += h.kind == kCarried ? 0x10000u : (h.steps >= args.maxSteps ? 1u : 0u);
 		mode = Fetch;
 	};
 
@@ -251,8 +254,8 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 					} else {
 						++traced; // a segment is counted once, in the launch that starts it
 					}
-					startStep = step;
-					stepLimit = args.budget > 0 ? step + args.budget : 0xFFFFFFFFu;
+					stepLimit = min(args.maxSteps, step + allowance);
+					marchSteps -= step;
 					cell.leaf = kNoLeaf;
 					if (up < lo) {
 						done(HitState { 0, t, kNoLeaf, 0, step });
@@ -267,14 +270,12 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 		// find the cell of the point, skipping empty cells, and start its first program
 		if (mode == Locating) {
 			for (uint32_t skipped = 0;;) {
-				// a miss keeps where its march stopped, so a held path can resume it
-				if (!(step < args.maxSteps && t <= up)) {
-					done(HitState { 0, t, kNoLeaf, 0, step });
-					break;
-				}
-				// out of this launch's budget: the march's whole state is (t, step) here
-				if (step >= stepLimit) {
-					done(HitState { kCarried, t, 0, 0, step });
+				// past the cap or the region: a miss, which keeps where its march
+				// stopped (a held path resumes it); out of this launch's budget
+				// before either: carried, the march's whole state being (t, step)
+				if (!(step < stepLimit && t <= up)) {
+					const bool carried = step < args.maxSteps && t <= up;
+					done(HitState { carried ? kCarried : 0u, t, kNoLeaf, 0, step });
 					break;
 				}
 				for (int a = 0; a < 3; ++a) p[a] = o[a] + d[a] * t;
@@ -374,17 +375,16 @@ __global__ void __launch_bounds__(kTraceBlock) traceKernel(TraceArgs args) {
 			marchSteps += __shfl_down_sync(0xFFFFFFFFu, marchSteps, o);
 			programSteps += __shfl_down_sync(0xFFFFFFFFu, programSteps, o);
 			traced += __shfl_down_sync(0xFFFFFFFFu, traced, o);
-			capped += __shfl_down_sync(0xFFFFFFFFu, capped, o);
-			carried += __shfl_down_sync(0xFFFFFFFFu, carried, o);
+			cappedCarried += __shfl_down_sync(0xFFFFFFFFu, cappedCarried, o);
 			longest = max(longest, __shfl_down_sync(0xFFFFFFFFu, longest, o));
 		}
 		if ((threadIdx.x & 31) == 0) {
 			atomicAdd(&args.counters[0], (unsigned long long) marchSteps);
 			atomicAdd(&args.counters[1], (unsigned long long) programSteps);
 			atomicMax(&args.counters[2], (unsigned long long) longest);
-			atomicAdd(&args.counters[3], (unsigned long long) capped);
+			atomicAdd(&args.counters[3], (unsigned long long) (cappedCarried & 0xFFFFu));
 			atomicAdd(&args.counters[4], (unsigned long long) traced);
-			if (carried) atomicAdd(&args.counters[5], (unsigned long long) carried);
+			if (cappedCarried >> 16) atomicAdd(&args.counters[5], (unsigned long long) (cappedCarried >> 16));
 		}
 	}
 }
