@@ -47,7 +47,7 @@ WIDTH, HEIGHT, SPP, SURFACES = 1920, 1080, 64, 16
 DENOISE = True  # the temporal member and the a-trous denoiser on the frame's FP16 features
 # DRAM bytes the trace kernel moves a ray (read + write): every trace
 # launch of a 960x540x8 config-2 frame captured by ncu (cold L2 a launch),
-# over the rays the kernel counted (profiles/trace_kernel_config2_960x540.md)
+# over the rays the kernel counted
 TRACE_DRAM_BYTES_PER_RAY = 229.9
 BUILD = dict(min_depth=7, max_depth=11, split_steps=32)
 

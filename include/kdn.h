@@ -322,7 +322,15 @@ kdn_status kdn_world_march(kdn_ctx* ctx, uint64_t i, const float* points, uint32
 kdn_status kdn_world_locate(kdn_ctx* ctx, const float* points, uint32_t n, uint32_t* by_grid, uint32_t* by_descent);
 
 /* ExtendRays (core/step.cpp:132): the first hit of each ray, host arrays in
- * and out (a host-to-device and device-to-host copy each call). */
+ * and out (a host-to-device and device-to-host copy each call).  The
+ * caller passes only the pool slots that wait on a ray (core/batch.h:360
+ * waitsOnRay) and marks them answered, as execution/single does
+ * (plugins/execution/single/plugin.cpp:28-36); the pool's ray kinds are not
+ * passed because the geometry traces every kind alike (the reference's
+ * intersect takes none) and the kinds only feed the caller's ray counters
+ * (kodanuki_gb300/reference_plugin/backend_gb300.cpp keeps them).  A hit's
+ * cell holds the device's object index; the binding clears it, as the
+ * reference's sphere-traced hits carry no tree cell. */
 kdn_status kdn_extend(kdn_ctx* ctx, const kdn_ray* rays, uint32_t n, kdn_hit* hits);
 /* The same over device arrays, on the given CUDA stream (0: the context's). */
 kdn_status kdn_extend_device(kdn_ctx* ctx, const kdn_ray* rays, uint32_t n, kdn_hit* hits, void* stream);

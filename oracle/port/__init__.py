@@ -61,6 +61,7 @@ def lib():
         L.kp_octree_cell.argtypes = [_P, ctypes.c_uint64, _P]
         L.kp_octree_cell_program.argtypes = [_P, ctypes.c_uint64, ctypes.c_uint32, _P, ctypes.POINTER(Program)]
         L.kp_sphere_trace.argtypes = [_P, ctypes.c_uint32, _P, _P, _P, _P, ctypes.c_uint32, _P]
+        L.kp_sphere_trace_rule.argtypes = [_P, ctypes.c_uint32, _P, _P, _P, _P, ctypes.c_uint32, _P, ctypes.c_int]
         L.kp_octree_trace.argtypes = [_P, _P, _P, ctypes.c_uint32, _P]
         L.kp_mixed_bits.restype = ctypes.c_uint64
         L.kp_mixed_bits.argtypes = [ctypes.c_uint64]
@@ -93,13 +94,17 @@ class Programs:
         self.count = scene.program_count
 
 
-def sphere_trace(scene, rays: np.ndarray, lower, size) -> np.ndarray:
+def sphere_trace(scene, rays: np.ndarray, lower, size, rule: int = 0) -> np.ndarray:
+    """sphere_trace.cpp:216 sphereTraced over the scene's object programs in
+    double; rule 1 stops by the FP32 device march's tolerance instead of the
+    reference's (kp_sphere_trace_rule)."""
     progs = Programs(scene)
     hits = np.zeros(len(rays), HIT_DTYPE)
     lo = np.asarray(lower, np.float64)
     sz = np.asarray(size, np.float64)
     mat = np.ascontiguousarray(scene.leaf_material, np.uint32)
-    lib().kp_sphere_trace(ctypes.addressof(progs.array), progs.count, _ptr(mat), _ptr(lo), _ptr(sz), _ptr(rays), len(rays), _ptr(hits))
+    rays = np.ascontiguousarray(rays, RAY_DTYPE)
+    lib().kp_sphere_trace_rule(ctypes.addressof(progs.array), progs.count, _ptr(mat), _ptr(lo), _ptr(sz), _ptr(rays), len(rays), _ptr(hits), rule)
     return hits
 
 

@@ -876,7 +876,20 @@ typedef struct march {
 	kp_program* storage;
 	cand_list* cand;
 	cand_list* cand2;
+	int rule; /* stopping rule: 0 the reference's (SPHERE_TOL), 1 the device's (tolerance_at) */
 } march;
+
+/* The stopping tolerance at t: the reference's 1e-6 (sphere_trace.h:14
+ * sphereTolerance), or, as a sensitivity check of the reference's own
+ * answer, the FP32 device march's 2e-6 max(1, |p|_inf / 4). */
+static double tolerance_at(const march* m, double t) {
+	if (m->rule == 0) return SPHERE_TOL;
+	const double p0 = fabs((double) m->ray->origin[0] + (double) m->ray->direction[0] * t);
+	const double p1 = fabs((double) m->ray->origin[1] + (double) m->ray->direction[1] * t);
+	const double p2 = fabs((double) m->ray->origin[2] + (double) m->ray->direction[2] * t);
+	const double big = p0 > p1 ? (p0 > p2 ? p0 : p2) : (p1 > p2 ? p1 : p2);
+	return 2e-6 * (big * 0.25 > 1.0 ? big * 0.25 : 1.0);
+}
 
 static void values_at(march* m, double t, cand_list* c, double* values) {
 	double p[3];
@@ -940,7 +953,7 @@ static void landed(march* m, const double* values, uint32_t n, double t, kp_hit*
 	for (uint32_t k = 0; k < n; ++k) tied |= k != first && values[k] - values[first] <= band;
 	if (tied) {
 		double q[3];
-		point_at(m->ray, t + SPHERE_INSET, q);
+		point_at(m->ray, t + 2 * tolerance_at(m, t), q);
 		double on[4096];
 		for (uint32_t k = 0; k < n; ++k) on[k] = kp_eval(m->cand->progs[k], q, m->regs);
 		for (uint32_t k = 0; k < n; ++k) winner = values[k] - values[first] <= band && on[k] < on[winner] ? k : winner;
@@ -972,6 +985,7 @@ static void trace_one(march* m, const double lower[3], const double size[3], kp_
 	for (int step = 0; step < SPHERE_STEPS && t <= up; ++step) {
 		values_at(m, t, m->cand, values);
 		hit->steps = (uint32_t) step + 1;
+		const double tol = tolerance_at(m, t), inset = 2 * tol;
 		if (m->cand->empty) {
 			t = dmax(m->cand->exit_t, t) + SPHERE_TOL;
 			continue;
@@ -979,7 +993,7 @@ static void trace_one(march* m, const double lower[3], const double size[3], kp_
 		if (m->cand->n == 0) return;
 		if (!ray->inside) {
 			const double least = values[least_of(values, m->cand->n)];
-			if (least < SPHERE_TOL) {
+			if (least < tol) {
 				landed(m, values, m->cand->n, t, hit);
 				return;
 			}
@@ -989,9 +1003,9 @@ static void trace_one(march* m, const double lower[3], const double size[3], kp_
 		/* sphereFromInside (sphere_trace.cpp:188) */
 		double nearest = fabs(values[0]);
 		for (uint32_t k = 0; k < m->cand->n; ++k) nearest = dmin(nearest, fabs(values[k]));
-		if (nearest < SPHERE_TOL) {
+		if (nearest < tol) {
 			double past[4096];
-			values_at(m, t + SPHERE_INSET, m->cand2, past);
+			values_at(m, t + inset, m->cand2, past);
 			const int past_empty = m->cand2->empty || m->cand2->n == 0;
 			const uint32_t least = past_empty ? 0 : least_of(past, m->cand2->n);
 			if (past_empty || past[least] > 0) {
@@ -1000,7 +1014,7 @@ static void trace_one(march* m, const double lower[3], const double size[3], kp_
 				return;
 			}
 			kp_hit there;
-			field_hit(m, t + SPHERE_INSET, m->cand2->progs[least], m->cand2->objects[least], &there);
+			field_hit(m, t + inset, m->cand2->progs[least], m->cand2->objects[least], &there);
 			if (there.leaf != NO_LEAF && m->leaf_material && m->leaf_material[there.leaf] != ray->within) {
 				double p[3];
 				point_at(ray, t, p);
@@ -1011,12 +1025,12 @@ static void trace_one(march* m, const double lower[3], const double size[3], kp_
 				return;
 			}
 		}
-		t = nearest < SPHERE_TOL ? t + SPHERE_INSET : dmin(t + nearest, dmax(m->cand->exit_t, t) + SPHERE_TOL);
+		t = nearest < tol ? t + inset : dmin(t + nearest, dmax(m->cand->exit_t, t) + SPHERE_TOL);
 	}
 	missed(hit);
 }
 
-static void trace_all(const kp_octree* tree, const kp_program* programs, uint32_t count, const uint32_t* leaf_material, const double lower[3], const double size[3], const kp_ray* rays, uint32_t n, kp_hit* hits) {
+static void trace_all(const kp_octree* tree, const kp_program* programs, uint32_t count, const uint32_t* leaf_material, const double lower[3], const double size[3], const kp_ray* rays, uint32_t n, kp_hit* hits, int rule) {
 	uint32_t longest = 1;
 	if (tree) {
 		for (uint64_t i = 0; i < tree->ncells; ++i)
@@ -1034,6 +1048,7 @@ static void trace_all(const kp_octree* tree, const kp_program* programs, uint32_
 	m.storage = (kp_program*) malloc(sizeof(kp_program) * 8192);
 	m.cand = (cand_list*) malloc(sizeof(cand_list));
 	m.cand2 = (cand_list*) malloc(sizeof(cand_list));
+	m.rule = rule;
 	for (uint32_t i = 0; i < n; ++i) {
 		m.ray = &rays[i];
 		trace_one(&m, lower, size, &hits[i]);
@@ -1085,9 +1100,13 @@ void kp_tracer_free(kp_tracer* t) {
 }
 
 void kp_sphere_trace(const kp_program* programs, uint32_t count, const uint32_t* leaf_material, const double lower[3], const double size[3], const kp_ray* rays, uint32_t n, kp_hit* hits) {
-	trace_all(NULL, programs, count, leaf_material, lower, size, rays, n, hits);
+	trace_all(NULL, programs, count, leaf_material, lower, size, rays, n, hits, 0);
+}
+
+void kp_sphere_trace_rule(const kp_program* programs, uint32_t count, const uint32_t* leaf_material, const double lower[3], const double size[3], const kp_ray* rays, uint32_t n, kp_hit* hits, int rule) {
+	trace_all(NULL, programs, count, leaf_material, lower, size, rays, n, hits, rule);
 }
 
 void kp_octree_trace(const kp_octree* tree, const uint32_t* leaf_material, const kp_ray* rays, uint32_t n, kp_hit* hits) {
-	trace_all(tree, NULL, 0, leaf_material, tree->lower, tree->size, rays, n, hits);
+	trace_all(tree, NULL, 0, leaf_material, tree->lower, tree->size, rays, n, hits, 0);
 }

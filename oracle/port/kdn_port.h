@@ -105,6 +105,10 @@ typedef struct kp_hit {
 
 /* sphereTraced (sphere_trace.cpp:216) over every object, in double. */
 void kp_sphere_trace(const kp_program* programs, uint32_t count, const uint32_t* leaf_material, const double lower[3], const double size[3], const kp_ray* rays, uint32_t n, kp_hit* hits);
+/* The same march with a stopping rule: 0 the reference's tolerance, 1 the
+ * FP32 device march's 2e-6 max(1, |p|_inf / 4) (a sensitivity check of the
+ * reference's answer: which rays move when the tolerance does). */
+void kp_sphere_trace_rule(const kp_program* programs, uint32_t count, const uint32_t* leaf_material, const double lower[3], const double size[3], const kp_ray* rays, uint32_t n, kp_hit* hits, int rule);
 /* The same march with each step's field read from the cut programs of the
  * octree cell the point lies in, and empty cells skipped to their exit. */
 void kp_octree_trace(const kp_octree* tree, const uint32_t* leaf_material, const kp_ray* rays, uint32_t n, kp_hit* hits);

@@ -5,6 +5,7 @@
 //
 //   kdn_ref_dump scene  <file.sdf> <out.json>            compiled scene as JSON
 //   kdn_ref_dump trace  <file.sdf> <rays.f32> <hits.bin>  sphereTraced per ray
+//   kdn_ref_dump cells  <file.sdf> <targets.u32> <out.bin> cutCell of chosen cells
 //   kdn_ref_dump cut    <file.sdf> <depth> <out.bin>      cutCell down an octree
 //   kdn_ref_dump denoise  <in.bin> <out.f32>              denoisedFrame
 //   kdn_ref_dump temporal <in.bin> <out.bin>              temporalFrame
@@ -267,6 +268,74 @@ int dumpCut(const char* sdf, int depth, const char* outPath) {
 	return 0;
 }
 
+// The reference's cut of chosen cells: each target (level, place) is reached
+// from the root by cutting every cell on its path (a child is cut from its
+// parent's cut, as writeCell does), the paths' common cells cut once.
+struct Target {
+	std::uint32_t level, place[3];
+	std::size_t index;
+};
+
+void cutTargets(const CellPrograms& programs, const Box& box, std::uint32_t level, const std::uint32_t place[3], std::vector<Target> targets,
+                std::vector<std::vector<std::uint8_t>>& records) {
+	const CellCut cut = cutCell(programs, box);
+	std::vector<Target> below;
+	for (const Target& t : targets) {
+		if (t.level != level) {
+			below.push_back(t);
+			continue;
+		}
+		std::vector<std::uint8_t>& rec = records[t.index];
+		auto put = [&](const void* p, std::size_t n) { rec.insert(rec.end(), static_cast<const std::uint8_t*>(p), static_cast<const std::uint8_t*>(p) + n); };
+		const std::uint32_t h[] = { level, place[0], place[1], place[2], std::uint32_t(cut.occupancy), std::uint32_t(cut.programs.objects.size()) };
+		put(h, sizeof h);
+		for (std::size_t i = 0; i < cut.programs.objects.size(); ++i) {
+			const Program& program  = *cut.programs.programs[i];
+			const std::uint32_t o[] = { cut.programs.objects[i], program.result, std::uint32_t(program.steps.size()) };
+			put(o, sizeof o);
+			for (const Step& step : program.steps) {
+				const std::uint32_t st[] = { std::uint32_t(step.opcode), step.a, step.b, step.c };
+				put(st, sizeof st);
+				put(&step.value, 8);
+				put(&step.leaf, 4);
+			}
+		}
+	}
+	for (int octant = 0; octant < 8; ++octant) {
+		const std::uint32_t child[3] = { place[0] * 2 + (octant & 1), place[1] * 2 + ((octant >> 1) & 1), place[2] * 2 + ((octant >> 2) & 1) };
+		std::vector<Target> mine;
+		for (const Target& t : below) {
+			const std::uint32_t shift = t.level - level - 1;
+			if ((t.place[0] >> shift) == child[0] && (t.place[1] >> shift) == child[1] && (t.place[2] >> shift) == child[2]) mine.push_back(t);
+		}
+		if (!mine.empty()) cutTargets(cut.programs, octantBox(box, octant), level + 1, child, mine, records);
+	}
+}
+
+// targets file: u32 count, then (level, x, y, z) u32 each; output: one
+// writeCell record a target, in the targets' order (no recursion below it).
+int dumpCells(const char* sdf, const char* targetsPath, const char* outPath) {
+	const SceneFile file = loaded(sdf);
+	const Region region  = sceneRegion(file.scene, file.shot, 8);
+	FILE* in             = std::fopen(targetsPath, "rb");
+	std::uint32_t count  = 0;
+	if (std::fread(&count, 4, 1, in) != 1) return 1;
+	std::vector<Target> targets(count);
+	for (std::uint32_t i = 0; i < count; ++i) {
+		std::uint32_t v[4];
+		if (std::fread(v, 4, 4, in) != 4) return 1;
+		targets[i] = Target { v[0], { v[1], v[2], v[3] }, i };
+	}
+	std::fclose(in);
+	std::vector<std::vector<std::uint8_t>> records(count);
+	const std::uint32_t root[3] = { 0, 0, 0 };
+	cutTargets(rootPrograms(file.scene), regionBox(region), 0, root, targets, records);
+	FILE* out = std::fopen(outPath, "wb");
+	for (const auto& r : records) std::fwrite(r.data(), 1, r.size(), out);
+	std::fclose(out);
+	return 0;
+}
+
 // Feature buffers in, the reference's denoised frame out
 // (plugins/reconstruction/atrous/atrous.cpp:513 denoisedFrame).  Input: int32
 // width, height, demodulated; doubles eye[3], forward[3], right[3], up[3],
@@ -477,6 +546,9 @@ int main(int argc, char** argv) {
 	if (argc >= 5 && std::strcmp(argv[1], "cut") == 0) {
 		return dumpCut(argv[2], std::atoi(argv[3]), argv[4]);
 	}
-	std::fprintf(stderr, "usage: kdn_ref_dump scene|trace|cut ...\n");
+	if (argc >= 5 && std::strcmp(argv[1], "cells") == 0) {
+		return dumpCells(argv[2], argv[3], argv[4]);
+	}
+	std::fprintf(stderr, "usage: kdn_ref_dump scene|trace|cut|cells ...\n");
 	return 2;
 }

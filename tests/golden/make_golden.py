@@ -2,14 +2,16 @@
 
 Run only where the reference checkout and its oracle build exist:
 
-    make -C oracle/ref REF=/root/reference -j8
+    make -C oracle/ref REF=<the reference checkout> -j8
     python tests/golden/make_golden.py [--ref-bin oracle/_ref] [--only NAME]
 
 It writes, under tests/golden/:
   scenes/<name>.npz      the compiled scene (kodanuki_gb300.scene.Scene)
   trace_<name>.npz       seeded rays and the reference's sphereTraced hits
   cut_<name>.npz         cutCell results down a fixed-depth octree
-  image_<name>.npz       reference frames (fixed spp, two seeds)
+  cutdeep_c2.npz         cutCell of a sample of the benchmark octree's cells
+  image_<name>.npz       reference frames (fixed spp, several seeds; config 1 at
+                         its own size as per-pixel mean and variance)
 Every input is seeded; rerunning gives the same files.
 """
 from __future__ import annotations
@@ -161,6 +163,32 @@ def reference_images(render: str, sdf: str, name: str, tmp: str, scene: Scene) -
     f = np.stack(frames)
     np.savez_compressed(os.path.join(HERE, f"image_{name}.npz"), frames=f.astype(np.float32), spp=spp, seeds=np.arange(1000, 1000 + seeds))
     print(" image", f.shape, "mean", f.mean(axis=(0, 1, 2)))
+
+
+# name -> (seeds, spp, octree depth) of reference frames drawn at the scene's
+# own size on the reference's default geometry (geometry/tree), kept as the
+# per-pixel mean and variance over the seeds
+TREE_IMAGES = {"c1": (12, 16, 6)}
+TREE_FLAGS = ["--threads", str(os.cpu_count() or 8), "--use", "stopping=fixed_count", "--use", "execution=single", "--use", "detail=none",
+              "--use", "build=none", "--use", "strategy=none", "--use", "sampler=none", "--use", "observer=none", "--use", "geometry=tree"]
+
+
+def reference_tree_images(render: str, sdf: str, name: str, tmp: str) -> None:
+    """Frames of the reference renderer on its own fast path (the tree
+    geometry at the config's octree depth), at the scene's size and spp,
+    under independent seeds: the per-pixel mean and the variance of one
+    seed's frame."""
+    seeds, spp, depth = TREE_IMAGES[name]
+    frames = []
+    for k in range(seeds):
+        pfm = os.path.join(tmp, f"{name}_tree_{k}.pfm")
+        subprocess.run([render, sdf, "--out", os.path.join(tmp, f"{name}_tree_{k}.ppm"), "--pfm", pfm, "--seed", str(2000 + k),
+                        "--samples", str(spp), "--depth", str(depth)] + TREE_FLAGS, check=True, capture_output=True)
+        frames.append(read_pfm(pfm).astype(np.float64))
+    f = np.stack(frames)
+    np.savez_compressed(os.path.join(HERE, f"image_{name}.npz"), mean=f.mean(0).astype(np.float32), var=f.var(0, ddof=1).astype(np.float32),
+                        seeds=seeds, spp=spp, depth=depth)
+    print(" tree image", f.shape, "mean", f.mean(axis=(0, 1, 2)))
 
 
 def denoise_fields(width: int = 64, height: int = 48):
@@ -335,6 +363,56 @@ def temporal_fixture(dump: str, tmp: str) -> None:
     np.savez_compressed(os.path.join(HERE, "temporal.npz"), **out)
 
 
+# The benchmark's own octree of config 2 and the cells sampled from it for
+# tests/golden/cutdeep_c2.npz
+DEEP_BUILD = (7, 11, 32)
+DEEP_SAMPLE = 2000
+
+
+def deep_cut_fixture(dump: str, tmp: str) -> None:
+    """tests/golden/cutdeep_c2.npz: the reference's cutCell of a seeded
+    sample of the cells of the octree the benchmark builds over config 2
+    (down to level 11), each cut from the root along its path as the
+    reference's own recursion does; the product's host build must hold the
+    same programs there."""
+    import ctypes
+
+    import kodanuki_gb300 as K
+    sc = Scene.load(os.path.join(HERE, "scenes", "c2.npz"))
+    L = K.library()
+    h = ctypes.c_void_p()
+    assert L.kdn_open(-1, ctypes.byref(h)) == K.KDN_OK
+    b = K.Backend.__new__(K.Backend)
+    b.lib, b.handle, b.scene = L, h, None
+    b.load(sc)
+    b.build(*DEEP_BUILD)
+    n = b.world_stats()["cells"]
+    index = np.sort(np.random.default_rng(77).choice(n, DEEP_SAMPLE, replace=False)).astype(np.uint64)
+    targets = np.array([(lvl, *place) for lvl, place, _, _ in (b.world_cell(int(i)) for i in index)], np.uint32)
+    b.close()
+    tp = os.path.join(tmp, "deep.targets")
+    with open(tp, "wb") as fh:
+        fh.write(struct.pack("<I", len(targets)))
+        fh.write(targets.astype("<u4").tobytes())
+    sdf = os.path.join(tmp, "c2_deep.sdf")
+    gen, kw, _, _ = SCENES["c2"]
+    open(sdf, "w").write(gen(**kw))
+    cp = os.path.join(tmp, "deep.cut")
+    subprocess.run([dump, "cells", sdf, tp, cp], check=True)
+    cells = read_cut(cp)
+    head = np.array([(c[0], *c[1], c[2], len(c[3])) for c in cells], np.uint32)
+    objects, results, counts, digests = [], [], [], []
+    for c in cells:
+        for obj, res, steps in c[3]:
+            objects.append(obj)
+            results.append(res)
+            counts.append(len(steps))
+            digests.append(step_digest(steps))
+    np.savez_compressed(os.path.join(HERE, "cutdeep_c2.npz"), build=np.array(DEEP_BUILD), index=index, head=head, objects=np.array(objects, np.uint32),
+                        results=np.array(results, np.uint32), counts=np.array(counts, np.uint32), digests=np.array(digests, np.uint64))
+    print(" deep cut cells", len(cells), "of", n, "levels", np.bincount(head[:, 0]).tolist(), "programs", len(objects))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref-bin", default=os.path.join(ROOT, "oracle", "_ref"))
@@ -348,6 +426,8 @@ def main() -> None:
         denoise_fixture(dump, tmp)
     if args.only in (None, "temporal"):
         temporal_fixture(dump, tmp)
+    if args.only in (None, "cutdeep"):
+        deep_cut_fixture(dump, tmp)
     for name, (gen, kw, nrays, depth) in SCENES.items():
         if args.only and name != args.only:
             continue
@@ -360,6 +440,8 @@ def main() -> None:
         print(name, "programs", scene.program_count, "steps", len(scene.steps))
         if name in IMAGES:
             reference_images(render, sdf, name, tmp, scene)
+        if name in TREE_IMAGES:
+            reference_tree_images(render, sdf, name, tmp)
         if nrays:
             rng = np.random.default_rng(1234)
             rays = np.concatenate([camera_rays(scene, nrays // 2, rng), scattered_rays(scene, nrays - nrays // 2, rng)])

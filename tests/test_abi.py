@@ -113,6 +113,22 @@ def test_world_build_matches_reference_cut(name):
     b.close()
 
 
+def test_bench_world_cells_match_reference_cut():
+    """The octree the benchmark builds over config 2 (levels 7 to 11, split
+    while a cell's programs pass 32 steps): a seeded sample of its cells,
+    every level down to 11, holds exactly the programs the reference's
+    cutCell gives those cells when cut from the root along their paths
+    (tests/golden/cutdeep_c2.npz)."""
+    fx = np.load(os.path.join(GOLDEN, "cutdeep_c2.npz"))
+    b = host_backend()
+    b.load(scene("c2"))
+    b.build(*[int(x) for x in fx["build"]])
+    index = fx["index"]
+    assert compare_cells(lambda k: b.world_cell(int(index[k])), fx) == 0
+    assert int(fx["head"][:, 0].max()) == 11
+    b.close()
+
+
 def test_world_build_matches_oracle_adaptive():
     """The adaptive build (split while a cell's programs are long) agrees
     with the oracle's build cell for cell."""
