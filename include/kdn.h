@@ -398,8 +398,10 @@ kdn_status kdn_denoise_device(kdn_ctx* ctx, const kdn_denoise_frame* frame, cons
  * are refused with KDN_BAD_ARG.  It runs on the current device, on the given
  * stream; the arrays are device pointers as for kdn_denoise_device.  The
  * first call on a device looks the array's device address up; make that
- * first call before any stream capture.  All calls share the array: calls
- * whose work overlaps on the GPU race.  Nothing in it has to start at zero.
+ * first call before any stream capture.  A call copies nothing from host
+ * memory: the lens travels in the kernels' parameters.  All calls share the
+ * array: calls whose work overlaps on the GPU race.  Nothing in it has to
+ * start at zero.
  * The message of a failed call is kdn_last_error(NULL) on the calling thread.
  */
 kdn_status kdn_denoise_static(const kdn_denoise_frame* frame, const float* colour, const float* moment, const float* length, const uint16_t* distance,

@@ -18,10 +18,6 @@ LIB = os.path.join(OUT, "libkdn_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 EXACT_FLOAT = {"denoise.cu"}
-# the march's square roots by the hardware's approximate square root (a few
-# ulp), not the correctly rounded sequence: sphere tracing stops within
-# 2e-6 of a surface, far above either's error
-FAST_SQRT = {"trace.cu"}
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc")
 
 

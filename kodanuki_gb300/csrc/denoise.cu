@@ -37,7 +37,7 @@ __device__ __forceinline__ float luma(float r, float g, float b) { return 0.2126
 
 __device__ __forceinline__ double divisorOf(double a) { return a < 1e-3 ? 1.0 : a; }
 
-__global__ void prepKernel(DenoiseArgs a) {
+__global__ void prepKernel(const __grid_constant__ DenoiseArgs a) {
 	const int x = blockIdx.x * blockDim.x + threadIdx.x;
 	const int y = blockIdx.y * blockDim.y + threadIdx.y;
 	if (x >= a.width || y >= a.height) return;
@@ -95,7 +95,7 @@ __device__ __forceinline__ float tapWeight(float4 pa, float4 pb, float psky, flo
 	return kernel * power * quickExp(-plane - apart);
 }
 
-__global__ void varianceKernel(DenoiseArgs a) {
+__global__ void varianceKernel(const __grid_constant__ DenoiseArgs a) {
 	const int x = blockIdx.x * blockDim.x + threadIdx.x;
 	const int y = blockIdx.y * blockDim.y + threadIdx.y;
 	if (x >= a.width || y >= a.height) return;
@@ -138,7 +138,7 @@ __global__ void varianceKernel(DenoiseArgs a) {
 __constant__ float cSpline[5] = { 1.0f / 16, 1.0f / 4, 3.0f / 8, 1.0f / 4, 1.0f / 16 };
 __constant__ float cGauss[3]  = { 0.25f, 0.5f, 0.25f };
 
-__global__ void atrousKernel(DenoiseArgs a, const float4* __restrict__ in, float4* __restrict__ out, int step) {
+__global__ void atrousKernel(const __grid_constant__ DenoiseArgs a, const float4* __restrict__ in, float4* __restrict__ out, int step) {
 	const int x = blockIdx.x * blockDim.x + threadIdx.x;
 	const int y = blockIdx.y * blockDim.y + threadIdx.y;
 	if (x >= a.width || y >= a.height) return;
@@ -187,7 +187,7 @@ __global__ void atrousKernel(DenoiseArgs a, const float4* __restrict__ in, float
 	out[p] = o;
 }
 
-__global__ void remodulateKernel(DenoiseArgs a, const float4* __restrict__ light) {
+__global__ void remodulateKernel(const __grid_constant__ DenoiseArgs a, const float4* __restrict__ light) {
 	const int x = blockIdx.x * blockDim.x + threadIdx.x;
 	const int y = blockIdx.y * blockDim.y + threadIdx.y;
 	if (x >= a.width || y >= a.height) return;

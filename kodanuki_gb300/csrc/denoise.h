@@ -10,7 +10,7 @@ namespace kdn {
 struct DenoiseArgs {
 	int width, height;
 	int demodulated;
-	const double* lens;      // device: eye[3], forward[3], right[3], up[3], reach, aspect
+	double lens[14];         // eye[3], forward[3], right[3], up[3], reach, aspect: by value, in the kernels' parameters
 	const float* colour;     // RGB a pixel
 	const float* moment;
 	const float* length;

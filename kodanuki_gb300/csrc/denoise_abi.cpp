@@ -29,12 +29,10 @@ void lensOf(const kdn_denoise_frame* f, double lens[14]) {
 
 // The context's scratch for n pixels, carved from one allocation.
 kdn_status scratch(Context* ctx, size_t n, kdn::DenoiseArgs& a) {
-	const kdn_status s = ctx->ensure(ctx->denoiseScratch, n * kdn::kDenoiseScratchPerPixel + 16 * sizeof(double));
+	const kdn_status s = ctx->ensure(ctx->denoiseScratch, n * kdn::kDenoiseScratchPerPixel);
 	if (s != KDN_OK) return s;
 	char* base = static_cast<char*>(ctx->denoiseScratch.ptr);
-	a.lens     = reinterpret_cast<const double*>(base);
-	base += 16 * sizeof(double);
-	a.guideA = reinterpret_cast<float4*>(base);
+	a.guideA   = reinterpret_cast<float4*>(base);
 	a.guideB = a.guideA + n;
 	a.lightA = a.guideB + n;
 	a.lightB = a.lightA + n;
@@ -43,9 +41,7 @@ kdn_status scratch(Context* ctx, size_t n, kdn::DenoiseArgs& a) {
 }
 
 kdn_status run(Context* ctx, const kdn_denoise_frame* f, kdn::DenoiseArgs& a, cudaStream_t stream) {
-	double lens[14];
-	lensOf(f, lens);
-	if (!ctx->check(cudaMemcpyAsync(const_cast<double*>(a.lens), lens, sizeof(lens), cudaMemcpyHostToDevice, stream), "kdn_denoise lens")) return KDN_CUDA_ERROR;
+	lensOf(f, a.lens);
 	a.width       = f->width;
 	a.height      = f->height;
 	a.demodulated = f->demodulated ? 1 : 0;

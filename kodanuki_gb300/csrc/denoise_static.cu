@@ -23,11 +23,11 @@ namespace kdn {
 
 void setThreadError(const std::string& message); // abi.cpp: kdn_last_error(NULL)
 
-// The largest frame the static scratch holds: 512 x 512 pixels.
+// The largest frame the static scratch holds: 512 x 512 pixels.  The lens
+// travels by value in the kernels' parameters, so the scratch is the
+// per-pixel guides and light alone.
 constexpr size_t kStaticDenoisePixels = size_t(512) * 512;
-// The lens (14 doubles, rounded up to 256 bytes), then the per-pixel scratch.
-constexpr size_t kStaticLensBytes     = 256;
-constexpr size_t kStaticDenoiseBytes  = kStaticLensBytes + kStaticDenoisePixels * kDenoiseScratchPerPixel;
+constexpr size_t kStaticDenoiseBytes  = kStaticDenoisePixels * kDenoiseScratchPerPixel;
 
 // File-scope device scratch: 17 MiB on every device that loads the library.
 static __device__ __align__(256) unsigned char staticDenoiseScratch[kStaticDenoiseBytes];
@@ -84,23 +84,18 @@ kdn_status kdn_denoise_static(const kdn_denoise_frame* frame, const float* colou
 	const kdn_status s = scratchAddress(device, &base);
 	if (s != KDN_OK) return s;
 	const cudaStream_t on = static_cast<cudaStream_t>(stream);
-	double lens[14];
+	DenoiseArgs a {};
 	for (int k = 0; k < 3; ++k) {
-		lens[k]     = frame->eye[k];
-		lens[3 + k] = frame->forward[k];
-		lens[6 + k] = frame->right[k];
-		lens[9 + k] = frame->up[k];
+		a.lens[k]     = frame->eye[k];
+		a.lens[3 + k] = frame->forward[k];
+		a.lens[6 + k] = frame->right[k];
+		a.lens[9 + k] = frame->up[k];
 	}
-	lens[12] = frame->reach;
-	lens[13] = frame->aspect;
-	e = cudaMemcpyAsync(base, lens, sizeof(lens), cudaMemcpyHostToDevice, on);
-	if (e != cudaSuccess) return failed(KDN_CUDA_ERROR, std::string("kdn_denoise_static: lens copy: ") + cudaGetErrorString(e));
+	a.lens[12] = frame->reach;
+	a.lens[13] = frame->aspect;
 	// Every kernel writes each pixel's guides and light before any reads
 	// them, so nothing in the scratch has to start at zero.
-	char* bytes = static_cast<char*>(base);
-	DenoiseArgs a {};
-	a.lens        = reinterpret_cast<const double*>(bytes);
-	a.guideA      = reinterpret_cast<float4*>(bytes + kStaticLensBytes);
+	a.guideA      = static_cast<float4*>(base);
 	a.guideB      = a.guideA + n;
 	a.lightA      = a.guideB + n;
 	a.lightB      = a.lightA + n;

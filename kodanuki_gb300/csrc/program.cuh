@@ -42,6 +42,19 @@ KDN_HD float smoothMinF(float a, float b, float r) {
 
 KDN_HD float truthF(bool b) { return b ? 1.0f : 0.0f; }
 
+// The march's square root: the hardware's approximate one on the device
+// (PTX sqrt.approx.f32, relative error within 2^-22), correctly rounded on
+// the host.
+KDN_HD float marchSqrt(float x) {
+#ifdef __CUDA_ARCH__
+	float r;
+	asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+	return r;
+#else
+	return sqrtf(x);
+#endif
+}
+
 KDN_HD float stepValue(uint8_t op, float a, float b, float c, float value, const float p[3]) {
 	switch (op) {
 		case OpConstant: return value;
@@ -114,7 +127,7 @@ KDN_HD float marchStep(const MarchStep& s, float* slots, uint32_t stride) {
 		// the smooth minimum of radius r = value: min - max(r - |f - w|, 0)^2 * 0.25 / r
 		const float m = fmaxf(s.value - fabsf(f - w), 0.0f);
 		r             = f;
-		r             = s.op == PostSqrt ? sqrtf(f) : r;
+		r             = s.op == PostSqrt ? marchSqrt(f) : r;
 		r             = s.op == PostAbs ? fabsf(f) : r;
 		r             = s.op == PostPosSq ? q * q : r;
 		r             = s.op == PostMin ? (w < f ? w : f) : r;
