@@ -385,7 +385,7 @@ def guided(device: int) -> dict:
         "guided": {"train_spp": GUIDE_TRAIN_SPP, "train_s": train_s, "spp": spp, "seconds": train_s + guided_s, "relmse": rg,
                    "seconds_per_spp": pilot_s / 8, "plain_seconds_per_spp": plain_s / GUIDE_PLAIN_SPP},
         "select": {"kept_guide": keep, "plain_cost": plain_cost, "guided_cost": guided_cost, "seconds": select_s,
-                   "pilot": f"2 plain + 2 guided frames of {GUIDE_W}x{GUIDE_H} at 4 spp"},
+                   "pilot": f"pairs of plain and guided frames of {GUIDE_W}x{GUIDE_H} at 4 spp, 3 to 16 pairs (until the cost ratio is 2 standard errors from a 5% margin), after one untimed frame of each"},
         "equal_time_gain": rp / rg if rg > 0 else None,
         "equal_spp_gain": rp / rs if rs > 0 else None,
         "train_samples_per_s": 64 * 16384 / t_train,
@@ -421,13 +421,14 @@ def guide_profile(device: int) -> None:
     print(json.dumps({"guide_profile": True, "train_s": train_s, "guided_s": guided_s, "finite": bool(np.isfinite(img).all())}), flush=True)
 
 
-# The serving run (bounded): Poisson arrivals over four
-# resident scenes for a fixed window; 70% single frames of a uniform
-# resolution in {320x240, 640x480, 1280x720, 1920x1080} and spp in
-# {1, 4, 16, 64}, 30% frames of four progressive 1280x720 sessions at 1 spp
-# with the denoiser's history (interactive).  What is still queued when the
-# window closes is cancelled; latency is over the completed requests.
-SERVE_SCENES = ["c1", "room", "glow_small"]  # beside config 2, already resident
+# The serving run (config 3, bounded): Poisson arrivals at 200 requests a
+# second over eight resident seeded scenes of 256 to 16384 config-1-style
+# primitives for a fixed window; 70% single frames of a uniform resolution in
+# {320x240, 640x480, 1280x720, 1920x1080} and spp in {1, 4, 16, 64}, 30%
+# frames of four progressive 1280x720 sessions at 1 spp with the denoiser's
+# history (interactive).  What is still queued when the window closes is
+# cancelled; latency is over the completed requests.
+SERVE_SCENES = [f"serve_{n}" for n in (256, 512, 1024, 2048, 4096, 6144, 10240, 16384)]
 SERVE_RATE, SERVE_WINDOW_S, SERVE_SLOTS, SERVE_SESSIONS = 200.0, 5.0, 8, 4
 SERVE_SIZES = [(320, 240), (640, 480), (1280, 720), (1920, 1080)]
 SERVE_SPP = [1, 4, 16, 64]
@@ -437,7 +438,7 @@ def serving(main_backend, **options) -> dict:
     import kodanuki_gb300 as K
     from kodanuki_gb300.scene import Scene
     rng = np.random.default_rng(2024)
-    backends = [main_backend]
+    backends = []
     for name in SERVE_SCENES:
         b = K.Backend(0)
         b.load(Scene.load(os.path.join(ROOT, "tests", "golden", "scenes", name + ".npz")))
@@ -492,10 +493,10 @@ def serving(main_backend, **options) -> dict:
         except K.KdnError:
             pass
     srv.close()
-    for b in backends[1:]:
+    for b in backends:
         b.close()
     return {
-        "workload": f"Poisson {SERVE_RATE:.0f}/s for {SERVE_WINDOW_S:.0f} s over {len(ids)} resident scenes (config 2, {', '.join(SERVE_SCENES)}); "
+        "workload": f"config 3: Poisson {SERVE_RATE:.0f}/s for {SERVE_WINDOW_S:.0f} s over {len(ids)} resident scenes of 256 to 16384 primitives ({', '.join(SERVE_SCENES)}); "
                     f"70% frames of {{320x240,640x480,1280x720,1920x1080}} x {{1,4,16,64}} spp, 30% frames of {SERVE_SESSIONS} progressive "
                     f"1280x720 1-spp denoised interactive sessions; {SERVE_SLOTS} slots, 120 GB budget; queued requests cancelled at the window's end",
         "submitted": len(tickets), "completed": completed, "cancelled": int(cancelled),

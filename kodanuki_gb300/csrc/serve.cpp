@@ -30,12 +30,17 @@ namespace {
 using Clock = std::chrono::steady_clock;
 
 // Device bytes a path takes in a frame's buffers (render.cpp kPathBytes),
-// and a pixel's (sums, record, G-buffer, temporal state, image).
-constexpr uint64_t kPathBytes  = 364;
-constexpr uint64_t kPixelBytes = 128;
+// and a pixel's (sums, record, G-buffer, temporal state, image: 128; the
+// surfaces pass's own queue, states and hits: 116).
+constexpr uint64_t kPathBytes  = 416;
+constexpr uint64_t kPixelBytes = 128 + 116;
 // Stream priority of interactive requests (lower is more urgent; clamped
 // to the device's range by kdn_open_sharing).
 constexpr int kInteractivePriority = -8;
+// March steps a ray takes in one trace launch (kdn_set_march_budget) of an
+// interactive and of a batch request's frames
+constexpr uint32_t kInteractiveMarchBudget = 64;
+constexpr uint32_t kBatchMarchBudget       = 1024;
 
 struct Job {
 	uint64_t ticket = 0;
@@ -192,6 +197,10 @@ void serveLoop(kdn_server* S) {
 			// batch frames: short chunks on their share of the SMs
 			if (status == KDN_OK && !interactive) status = kdn_set_frame_budget(ctx, S->batchCap);
 			if (status == KDN_OK && !interactive && S->slots > 1 && S->batchSms > 0) status = kdn_set_sm_limit(ctx, int(S->batchSms));
+			// short trace launches: an interactive frame waits on no ray that
+			// skims a surface, and a batch frame hands its SMs back often
+			// (frames are the same to the bit with any budget)
+			if (status == KDN_OK) status = kdn_set_march_budget(ctx, interactive ? kInteractiveMarchBudget : kBatchMarchBudget);
 			if (status != KDN_OK) why = kdn_last_error(sceneCtx);
 		}
 		if (status == KDN_OK) {

@@ -58,14 +58,16 @@ class Scene:
         return self.steps[self.program_first[i]:self.program_first[i + 1]], int(self.program_result[i])
 
     def save(self, path: str) -> None:
-        arrays = {
-            "steps": self.steps,
+        # the steps field by field: a column of opcodes, of operands, of
+        # values compresses far better than the interleaved records
+        arrays = {f"steps_{f}": np.ascontiguousarray(self.steps[f]) for f in STEP_DTYPE.names}
+        arrays.update({
             "program_first": self.program_first,
             "program_result": self.program_result,
             "leaf_material": self.leaf_material,
             "region_lower": self.region_lower,
             "region_size": self.region_size,
-        }
+        })
         for k, v in self.materials.items():
             arrays["material_" + k] = v
         for k, v in self.lights.items():
@@ -85,7 +87,13 @@ class Scene:
         lights = {k[len("light_"):]: z[k] for k in z.files if k.startswith("light_")}
         patterns = {k[len("pattern_"):]: z[k] for k in z.files if k.startswith("pattern_")}
         placement = z["leaf_placement"] if "leaf_placement" in z.files else None
-        return Scene(z["steps"], z["program_first"], z["program_result"], z["leaf_material"], mats, lights,
+        if "steps" in z.files:
+            steps = z["steps"]
+        else:
+            steps = np.zeros(len(z["steps_opcode"]), STEP_DTYPE)
+            for f in STEP_DTYPE.names:
+                steps[f] = z[f"steps_{f}"]
+        return Scene(steps, z["program_first"], z["program_result"], z["leaf_material"], mats, lights,
                      meta["sky"], meta["camera"], meta["render"], z["region_lower"], z["region_size"], placement, patterns)
 
     @staticmethod

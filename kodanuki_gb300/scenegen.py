@@ -340,7 +340,10 @@ def scene_serving(seed: int, count: int, width: int = 640, height: int = 480, sa
         for _ in range(min(64, count - g)):
             albedo = [rng.uniform(0.2, 0.8) for _ in range(3)]
             pos = [rng.uniform(-reach, reach) for _ in range(3)]
-            mat = f"plastic({_v(albedo)}, roughness = {_f(rng.uniform(0.05, 0.5))})"
+            # roughness on a 0.01 grid: the compiled scene's finish tables
+            # (one per material, derived from the roughness) repeat and
+            # compress, which keeps the 16384-primitive scene small
+            mat = f"plastic({_v(albedo)}, roughness = {_f(round(rng.uniform(0.05, 0.5), 2))})"
             if rng.random() < 0.5:
                 shape = f"sphere({_f(rng.uniform(0.1, 0.5))})"
             else:

@@ -62,6 +62,7 @@ def lib():
         L.kp_octree_cell_program.argtypes = [_P, ctypes.c_uint64, ctypes.c_uint32, _P, ctypes.POINTER(Program)]
         L.kp_sphere_trace.argtypes = [_P, ctypes.c_uint32, _P, _P, _P, _P, ctypes.c_uint32, _P]
         L.kp_sphere_trace_rule.argtypes = [_P, ctypes.c_uint32, _P, _P, _P, _P, ctypes.c_uint32, _P, ctypes.c_int]
+        L.kp_normal_at.argtypes = [_P, _P, ctypes.c_double, _P, _P]
         L.kp_octree_trace.argtypes = [_P, _P, _P, ctypes.c_uint32, _P]
         L.kp_mixed_bits.restype = ctypes.c_uint64
         L.kp_mixed_bits.argtypes = [ctypes.c_uint64]
@@ -106,6 +107,21 @@ def sphere_trace(scene, rays: np.ndarray, lower, size, rule: int = 0) -> np.ndar
     rays = np.ascontiguousarray(rays, RAY_DTYPE)
     lib().kp_sphere_trace_rule(ctypes.addressof(progs.array), progs.count, _ptr(mat), _ptr(lo), _ptr(sz), _ptr(rays), len(rays), _ptr(hits), rule)
     return hits
+
+
+def normal_at(scene, rays: np.ndarray, objects: np.ndarray, ts: np.ndarray):
+    """sphereNormal of each ray's object program at p(t): (normals n x 3,
+    gradient lengths n) in double (kp_normal_at)."""
+    progs = Programs(scene)
+    rays = np.ascontiguousarray(rays, RAY_DTYPE)
+    out = np.zeros((len(rays), 3), np.float64)
+    grad = np.zeros(len(rays), np.float64)
+    L = lib()
+    base = ctypes.addressof(progs.array)
+    size = ctypes.sizeof(Program)
+    for i in range(len(rays)):
+        L.kp_normal_at(base + size * int(objects[i]), rays[i:i + 1].ctypes.data, float(ts[i]), out[i].ctypes.data, grad[i:i + 1].ctypes.data)
+    return out, grad
 
 
 class Octree:

@@ -1107,6 +1107,25 @@ void kp_sphere_trace_rule(const kp_program* programs, uint32_t count, const uint
 	trace_all(NULL, programs, count, leaf_material, lower, size, rays, n, hits, rule);
 }
 
+void kp_normal_at(const kp_program* program, const kp_ray* ray, double t, double normal[3], double* gradient_length) {
+	kp_dual* dregs = (kp_dual*) malloc(sizeof(kp_dual) * (program->count ? program->count : 1));
+	double* regs   = (double*) malloc(sizeof(double) * (program->count ? program->count : 1));
+	march m;
+	memset(&m, 0, sizeof m);
+	m.ray   = ray;
+	m.regs  = regs;
+	m.dregs = dregs;
+	kp_hit hit;
+	field_hit(&m, t, program, 0, &hit);
+	double p[3];
+	point_at(ray, t, p);
+	const kp_dual d = kp_eval_dual(program, p, dregs);
+	*gradient_length = sqrt(d.g[0] * d.g[0] + d.g[1] * d.g[1] + d.g[2] * d.g[2]);
+	for (int a = 0; a < 3; ++a) normal[a] = hit.normal[a];
+	free(dregs);
+	free(regs);
+}
+
 void kp_octree_trace(const kp_octree* tree, const uint32_t* leaf_material, const kp_ray* rays, uint32_t n, kp_hit* hits) {
 	trace_all(tree, NULL, 0, leaf_material, tree->lower, tree->size, rays, n, hits, 0);
 }

@@ -112,6 +112,10 @@ void kp_sphere_trace_rule(const kp_program* programs, uint32_t count, const uint
 /* The same march with each step's field read from the cut programs of the
  * octree cell the point lies in, and empty cells skipped to their exit. */
 void kp_octree_trace(const kp_octree* tree, const uint32_t* leaf_material, const kp_ray* rays, uint32_t n, kp_hit* hits);
+/* sphere_trace.cpp:140 sphereNormal of one program at p(t) along a ray, and
+ * the length of the program's gradient there (a hit's normal anywhere along
+ * the stretch its stopping tolerance admits). */
+void kp_normal_at(const kp_program* program, const kp_ray* ray, double t, double normal[3], double* gradient_length);
 
 /* One tracer per thread: the same march, one ray at a time. */
 typedef struct kp_tracer kp_tracer;
