@@ -45,10 +45,15 @@ METRIC = "Msamples/s @1080p vs CPU; equal-time relMSE guided vs plain; p50/p99 l
 SCENE = os.path.join(ROOT, "tests", "golden", "scenes", "c2.npz")
 WIDTH, HEIGHT, SPP, SURFACES = 1920, 1080, 64, 16
 DENOISE = True  # the temporal member and the a-trous denoiser on the frame's FP16 features
-# DRAM bytes the trace kernel moves a ray (read + write): every trace
-# launch of a 960x540x8 config-2 frame captured by ncu (cold L2 a launch),
-# over the rays the kernel counted
-TRACE_DRAM_BYTES_PER_RAY = 229.9
+# The trace kernel's roof is FP32 issue (divergent SIMT work: neither HBM
+# nor the tensor pipe bounds it).  From one ncu pass over every trace launch
+# of a 960x540x8 config-2 frame (smsp__thread_inst_executed.sum and
+# smsp__inst_executed.sum, with the frame's own program-step counters): the
+# lane instructions the kernel issues a march-form program step, and the
+# warp execution efficiency (active lanes an instruction / 32).
+TRACE_LANE_INST_PER_PROGRAM_STEP = 156.9
+TRACE_WARP_EFFICIENCY = 0.249
+SM_COUNT, LANES_PER_SM = 152, 128
 BUILD = dict(min_depth=7, max_depth=11, split_steps=32)
 
 
@@ -102,14 +107,6 @@ class Clocks:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k].lower().startswith("active")})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(self.samples)}
-
-
-def peaks() -> dict:
-    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(path):
-        d = json.load(open(path))
-        return {"hbm_gbs": d.get("hbm_gbs", 6800.0), "source": "measured"}
-    return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
 WORKLOAD = "config-2: 4096 primitives, 1920x1080, 64 spp, 16 surfaces, FP32, temporal + a-trous denoiser on FP16 features"
@@ -243,13 +240,17 @@ def run_gpu(args) -> None:
     e_dt = time.perf_counter() - e0
     e2e = samples * world / e_dt / 1e6
 
-    # roofline of the dominant kernel, the sphere-trace kernel: its
-    # algorithmic bytes are the rays it reads (36 B) and the end states it
-    # writes (20 B); the world it walks (programs, octree) stays in L2.
-    pk = peaks()
-    ray_bytes = 36 + 20
-    achieved_gbs = segments * ray_bytes / (trace_ms / 1e3) / 1e9 if trace_ms else None
+    # roofline of the dominant kernel, the sphere-trace kernel (90% of the
+    # frame's launch time): FP32 issue.  Its lane instructions a second are
+    # the march-form program steps it ran in the timed frames, counted live,
+    # times the lane instructions a step, over the frames' device time (its
+    # launches on the four render lanes overlap and cover the frame); the
+    # peak is every SM's 128 FP32 lanes at the SM clock sampled meanwhile.
     rays_per_launch = segments / trace_launches if trace_launches else None
+    clock_summary = clocks.summary()
+    sm_hz = (clock_summary.get("sm_mhz") or 2070.0) * 1e6
+    lane_inst_per_s = program * TRACE_LANE_INST_PER_PROGRAM_STEP / (device_ms / 1e3) if device_ms else None
+    issue_peak = SM_COUNT * LANES_PER_SM * sm_hz
     line = {
         "metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": device_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -259,7 +260,7 @@ def run_gpu(args) -> None:
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
-        "clocks": clocks.summary(),
+        "clocks": clock_summary,
         "wall_s": wall,
         "march_steps_per_sample": march / samples,
         "segments_per_sample": segments / samples,
@@ -272,12 +273,15 @@ def run_gpu(args) -> None:
     }
     if rank == 0:
         line["roofline"] = {
-            "bound": "hbm", "achieved": achieved_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
-            "frac": achieved_gbs / pk["hbm_gbs"] if achieved_gbs else None,
-            "traffic": TRACE_DRAM_BYTES_PER_RAY * rays_per_launch if (rays_per_launch and TRACE_DRAM_BYTES_PER_RAY) else None,
-            "kernel": "traceKernel", "peak_source": pk["source"],
-            "algorithmic": f"{ray_bytes} B a ray (ray in, end state out) x {rays_per_launch:.0f} rays a launch" if rays_per_launch else None,
-            "note": "the trace kernel is bound by FP32 issue and latency, not HBM; traffic = DRAM bytes a ray from the ncu capture in profiles/ (cold L2) x rays a launch",
+            "bound": "fp32-issue", "achieved": lane_inst_per_s / 1e12 if lane_inst_per_s else None, "peak": issue_peak / 1e12,
+            "unit": "Tlane-inst/s", "frac": lane_inst_per_s / issue_peak if lane_inst_per_s else None,
+            "traffic": None,
+            "kernel": "traceKernel", "peak_source": f"computed: {SM_COUNT} SMs x {LANES_PER_SM} FP32 lanes x the sampled SM clock",
+            "warp_efficiency": TRACE_WARP_EFFICIENCY,
+            "algorithmic": f"{program / max(1, segments):.0f} march-form program steps a ray x {TRACE_LANE_INST_PER_PROGRAM_STEP} lane instructions a step (ncu); "
+                           f"{rays_per_launch:.0f} rays a launch" if rays_per_launch else None,
+            "note": "traffic: none against this roof (the kernel's DRAM bytes, from an ncu capture of one launch, are in the trace kernel's "
+                    "profile); the kernel issues at ~8 of 32 lanes (warp_efficiency), so its issue slots bind long before its FP32 lanes",
         }
         # over the frame's device time: the two render lanes' trace
         # launches overlap, so their summed launch time exceeds it
