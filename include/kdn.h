@@ -135,7 +135,7 @@ typedef struct kdn_finish {
 	uint32_t kind;
 	uint32_t sharp;
 	uint32_t exact;      /* a smooth glass answered exactly */
-	uint32_t loses_much; /* a rough glass that needs its boundary tables (not drawn by this build) */
+	uint32_t loses_much; /* a rough glass that gives back what single scattering loses (its boundary tables in transport.boundaries) */
 	double width;
 	double facet_share;
 	double body;
@@ -143,7 +143,7 @@ typedef struct kdn_finish {
 	double coat_front, coat_twice, coat_room;
 	double escape_average;
 	double escape[32];
-	double film[2];      /* thickness (nm), index; a thickness above 0 is not drawn by this build */
+	double film[2];      /* the thin film (material.cpp:106 filmOf): thickness in nm (0: none), index */
 } kdn_finish;
 
 /* sdf/scene.h Light, 136 bytes. kind: sdf/scene.h LightKind (2 sphere, 3 quad). */
@@ -337,7 +337,11 @@ kdn_status kdn_extend_device(kdn_ctx* ctx, const kdn_ray* rays, uint32_t n, kdn_
 
 /* Render samples of one frame into the context's pixel sums and write the
  * pixel means, linear RGB float, row-major, 3 floats a pixel.  out is a host
- * pointer (kdn_render) or a device pointer (kdn_render_device). */
+ * pointer (kdn_render) or a device pointer (kdn_render_device).  Matte,
+ * plastic, metal and glass (smooth or rough, dispersive, absorbing, under a
+ * thin film or not) are drawn; a scene with a medium (a scattering body) or
+ * a passable glass (refraction 1 without dispersion or film) is refused
+ * with KDN_BAD_ARG. */
 kdn_status kdn_render(kdn_ctx* ctx, const kdn_frame* frame, float* out_rgb);
 kdn_status kdn_render_device(kdn_ctx* ctx, const kdn_frame* frame, float* out_rgb, void* stream);
 kdn_status kdn_frame_stats_get(kdn_ctx* ctx, kdn_frame_stats* stats);

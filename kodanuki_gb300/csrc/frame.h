@@ -55,7 +55,9 @@ struct DeviceMaterial {
 	// a rough glass: gives back what single scattering loses, read off its
 	// boundary tables (kBoundaryFloats floats at boundaryFirst of Looks::boundaries)
 	uint32_t losesMuch, boundaryFirst;
-	uint32_t pad;
+	// material.cpp:106 filmOf: the thin film a metal, plastic or glass wears
+	// (thickness in nanometres, 0 for none; its index)
+	float filmThickness, filmIndex;
 };
 
 // material/energy.h Boundary as floats: rarer and denser (17 ratios x 32
@@ -100,6 +102,7 @@ struct FrameConstants {
 	uint32_t lampCount;
 	uint32_t materialCount;
 	uint32_t absorbs; // absorption.cpp:18 sceneAbsorbs: some glass absorbs
+	uint32_t films;   // some metal, plastic or glass wears a thin film
 	float zenith[3], horizon[3], ground[3];
 	DeviceLamp lamps[kMaxLamps];
 	SpectralTables spectral;

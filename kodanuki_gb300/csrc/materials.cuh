@@ -25,7 +25,8 @@
 namespace kdn {
 
 constexpr float kPiF     = 3.14159265358979f;
-constexpr float kCoatRatio = 1.0f / 1.5f; // material.cpp:10 coatIndex
+constexpr float kCoatIndex = 1.5f;        // material.cpp:10 coatIndex
+constexpr float kCoatRatio = 1.0f / kCoatIndex;
 
 struct Frame {
 	float3 t, b, n;
@@ -119,6 +120,106 @@ __device__ __forceinline__ float dielectricReflectance(float cosine, float ratio
 	return 0.5f * (perp * perp + par * par);
 }
 
+// ---- thin films: a layer `thickness` nm deep of index `index` between an
+// outside and a beneath index, thin enough that the light off its two faces
+// interferes (material.cpp:106-172) ----
+
+// material.cpp:143 bentCosine: the cosine past a crossing from index
+// `before` into `after`, -1 where the crossing reflects totally
+__device__ __forceinline__ float bentCosine(float before, float facing, float after) {
+	const float sine = before / after * sqrtf(fmaxf(1.0f - facing * facing, 0.0f));
+	return sine >= 1.0f ? -1.0f : sqrtf(1.0f - sine * sine);
+}
+
+// material.cpp:136 airySum: the reflectance of the two faces' amplitudes
+// summed over every round trip inside the layer, `shift` the cosine of the
+// phase one round trip adds
+__device__ __forceinline__ float airySum(float front, float back, float shift) {
+	const float both   = front * back;
+	const float top    = front * front + back * back + 2.0f * both * shift;
+	const float bottom = 1.0f + both * both + 2.0f * both * shift;
+	return bottom > 0.0f ? fminf(fmaxf(top / bottom, 0.0f), 1.0f) : 1.0f;
+}
+
+// material.cpp:148 filmReflectance at one wavelength: the mean of the two
+// polarisations' Airy sums over the front face (outside into the layer) and
+// the back face (the layer into beneath), their amplitudes as
+// material.cpp:129 faceAmplitude; 1 where either face reflects totally.
+// The film functions are called, not inlined, so that the shading of
+// unfilmed surfaces keeps its registers.
+__device__ __noinline__ float filmReflectance(float thickness, float index, float facing, float nm, float outside, float beneath) {
+	const float inside = bentCosine(outside, facing, index);
+	const float beyond = inside < 0.0f ? -1.0f : bentCosine(index, inside, beneath);
+	if (inside < 0.0f || beyond < 0.0f) return 1.0f;
+	const float nearPerp = (outside * facing - index * inside) / (outside * facing + index * inside);
+	const float nearPar  = (index * facing - outside * inside) / (index * facing + outside * inside);
+	const float farPerp  = (index * inside - beneath * beyond) / (index * inside + beneath * beyond);
+	const float farPar   = (beneath * inside - index * beyond) / (beneath * inside + index * beyond);
+	const float shift    = cosf(4.0f * kPiF * index * thickness * inside / nm);
+	return 0.5f * (airySum(nearPerp, farPerp, shift) + airySum(nearPar, farPar, shift));
+}
+
+// material.cpp:515 stackedFilm: a film in air over a reflector of
+// reflectance `under` (a metal's facets), the light held between them
+// summed
+__device__ __forceinline__ float stackedFilm(float thickness, float index, float facing, float nm, float under) {
+	if (!(thickness > 0.0f)) return under;
+	const float front = filmReflectance(thickness, index, facing, nm, 1.0f, 1.0f);
+	const float held  = fminf(fmaxf(under, 0.0f), 1.0f);
+	const float room  = 1.0f - front * held;
+	if (!(room > 1e-9f)) return 1.0f;
+	return front + (1.0f - front) * (1.0f - front) * held / room;
+}
+
+// material.cpp:528 coatFacing: a plastic's coat at the cosine `onto` under
+// its film (the film in air over the coat's index)
+__device__ __forceinline__ float filmedCoatFacing(float thickness, float index, float onto, float nm) {
+	return filmReflectance(thickness, index, onto, nm, 1.0f, kCoatIndex);
+}
+
+// material.cpp:592 metalTwice under a film: microfacet.cpp:116
+// averagedFresnel `average` at the lanes, under the film facing straight on
+__device__ __noinline__ float4 filmedMetalTwice(float4 average, float escapeAverage, float thickness, float index, float4 nm) {
+	float t[4];
+	for (int k = 0; k < 4; ++k) {
+		const float flat = stackedFilm(thickness, index, 1.0f, lane4(nm, k), lane4(average, k));
+		t[k]             = flat * flat * escapeAverage / (1.0f - flat * (1.0f - escapeAverage));
+	}
+	return make_float4(t[0], t[1], t[2], t[3]);
+}
+
+// material.cpp:651 viewedMetal's facet colour under a film: `face` (Schlick
+// at the lanes) under the film at the cosine `onto`
+__device__ __noinline__ float4 filmedMetalFace(float4 face, float onto, float thickness, float index, float4 nm) {
+	return make_float4(stackedFilm(thickness, index, onto, nm.x, face.x), stackedFilm(thickness, index, onto, nm.y, face.y),
+	                   stackedFilm(thickness, index, onto, nm.z, face.z), stackedFilm(thickness, index, onto, nm.w, face.w));
+}
+
+// material.cpp:661 viewedPlastic under a filmed coat: each lane's coat
+// (:543 filmCoating, :604 laneCoats) at its own wavelength; `albedo` the
+// body's colour at the lanes, `left`/`came` the escapes of the two
+// directions, `facets` the facet term, `lost` material.cpp:620 lostOf
+__device__ __noinline__ float4 filmedPlastic(float4 albedo, float left, float came, float escapeAverage, float onto, float facets, float lost, float thickness,
+                                             float index, float4 nm) {
+	float v[4];
+	for (int k = 0; k < 4; ++k) {
+		const float nmk     = lane4(nm, k);
+		const float faced   = filmedCoatFacing(thickness, index, 1.0f, nmk);
+		const float front   = faced + (1.0f - faced) / 21.0f;
+		const float twice   = front * front * escapeAverage / (1.0f - front * (1.0f - escapeAverage));
+		const float room    = 1.0f - front * escapeAverage;
+		const float through = room > 1e-6f ? (1.0f - front * left) * (1.0f - front * came) / room : 0.0f;
+		v[k] = lane4(albedo, k) / kPiF * through + filmedCoatFacing(thickness, index, onto, nmk) * facets + twice * lost;
+	}
+	return make_float4(v[0], v[1], v[2], v[3]);
+}
+
+// material.cpp:797 laneReflectance of a filmed glass at the four lanes
+__device__ __noinline__ float4 filmedLanes(float thickness, float index, float cosine, float4 nm, float4 within, float4 beyond) {
+	return make_float4(filmReflectance(thickness, index, cosine, nm.x, within.x, beyond.x), filmReflectance(thickness, index, cosine, nm.y, within.y, beyond.y),
+	                   filmReflectance(thickness, index, cosine, nm.z, within.z, beyond.z), filmReflectance(thickness, index, cosine, nm.w, within.w, beyond.w));
+}
+
 // energy.cpp:120 escapeAt
 __device__ __forceinline__ float escapeAt(const float* table, float cosine) {
 	const float place = fminf(fmaxf(cosine, 0.0f), 1.0f) * 32.0f - 0.5f;
@@ -141,10 +242,12 @@ struct Shading {
 	float masking;   // smithMasking(leaving)
 	float4 twice;    // metal: the colour light keeps over many bounces
 	float4 within, beyond; // glass: index on either side, per lane
-	bool parted;     // the lanes bend apart (a dispersing glass)
+	bool parted;     // the lanes answer apart (a dispersing or filmed glass)
 	bool inside;     // glass: the vertex is seen from inside the body
 	float width;     // glass: GGX width of the facets
 	const float* boundary; // rough glass that loses much: its boundary tables
+	float filmThickness, filmIndex; // the film it wears (thickness 0: none)
+	float4 nm;       // the lanes' wavelengths
 };
 
 struct Response {
@@ -208,7 +311,10 @@ __device__ __forceinline__ float plasticShare(const DeviceMaterial& m, float lea
 	return fminf(fmaxf(share, 0.25f), 0.9f);
 }
 
-// rgb: the albedo at the hit (the material's, or mixed across a blend seam)
+// rgb: the albedo at the hit (the material's, or mixed across a blend seam).
+// Films: the frame's scene wears a thin film somewhere; without, the film
+// fields are the constant 0 and every film branch folds away.
+template <bool Films>
 __device__ __forceinline__ Shading surfaceOf(const DeviceMaterial& m, float3 rgb, float3 normal, float3 outgoing, float4 nm, uint32_t medium, const DeviceMaterial* all,
                                              const float* boundaries) {
 	Shading s;
@@ -227,21 +333,31 @@ __device__ __forceinline__ Shading surfaceOf(const DeviceMaterial& m, float3 rgb
 	s.inside  = medium != kNoMaterial;
 	s.width   = m.width;
 	s.boundary = (m.kind == 3 && m.losesMuch && boundaries != nullptr) ? boundaries + size_t(m.boundaryFirst) * kBoundaryFloats : nullptr;
+	s.filmThickness = Films ? m.filmThickness : 0.0f;
+	s.filmIndex     = Films ? m.filmIndex : 1.0f;
+	s.nm            = nm;
 	if (m.kind == 1 || m.kind == 2) {
 		s.left    = escapeAt(m.escape, s.leaving);
 		s.share   = m.kind == 2 ? m.facetShare : (s.leaving <= 0.0f ? 0.0f : plasticShare(m, s.leaving));
 		s.masking = smithMasking(s.leaving, m.width);
 		if (m.kind == 2) {
-			// microfacet.cpp:116 averagedFresnel, then material.cpp:567 metalTwice
+			// microfacet.cpp:116 averagedFresnel under the film facing
+			// straight on, then material.cpp:592 metalTwice
 			const float4 avg = lin4(s.albedo, 1.0f - 1.0f / 21.0f, flat4(1.0f), 1.0f / 21.0f);
 			const float e    = m.escapeAverage;
-			const float a[4] = { avg.x, avg.y, avg.z, avg.w };
-			float t[4];
-			for (int k = 0; k < 4; ++k) t[k] = a[k] * a[k] * e / (1.0f - a[k] * (1.0f - e));
-			s.twice = make_float4(t[0], t[1], t[2], t[3]);
+			if (s.filmThickness > 0.0f) {
+				s.twice = filmedMetalTwice(avg, e, s.filmThickness, s.filmIndex, nm);
+			} else {
+				const float a[4] = { avg.x, avg.y, avg.z, avg.w };
+				float t[4];
+				for (int k = 0; k < 4; ++k) t[k] = a[k] * a[k] * e / (1.0f - a[k] * (1.0f - e));
+				s.twice = make_float4(t[0], t[1], t[2], t[3]);
+			}
 		}
 	} else if (m.kind == 3) {
-		// material.cpp:328 sidesOf with feature/dispersion's per-lane indices
+		// material.cpp:328 sidesOf with feature/dispersion's per-lane
+		// indices (dispersion.cpp:60 dispersedSides); a filmed glass answers
+		// each lane at its own wavelength (dispersion.cpp:38 filmedSides)
 		if (medium != kNoMaterial) {
 			const DeviceMaterial& body = all[medium];
 			s.within = laneIndices(body, nm);
@@ -250,6 +366,7 @@ __device__ __forceinline__ Shading surfaceOf(const DeviceMaterial& m, float3 rgb
 			s.beyond = laneIndices(m, nm);
 			s.parted = m.dispersion != 0.0f;
 		}
+		s.parted = s.parted || s.filmThickness > 0.0f;
 	}
 	return s;
 }
@@ -335,10 +452,16 @@ __device__ __forceinline__ Broad broadOf(const Shading& s, float leaving) {
 	return w;
 }
 
-// material.cpp:797 laneReflectance (no film), :814 laneReflectances, :821 reflectChance
-__device__ __forceinline__ float laneReflectance(const Shading& s, float cosine, int k) { return dielectricReflectance(cosine, lane4(s.within, k) / lane4(s.beyond, k)); }
+// material.cpp:797 laneReflectance (Fresnel, or the film between the two
+// sides at lane k's wavelength), :814 laneReflectances, :821 reflectChance
+__device__ __forceinline__ float laneReflectance(const Shading& s, float cosine, int k) {
+	const float within = lane4(s.within, k), beyond = lane4(s.beyond, k);
+	if (!(s.filmThickness > 0.0f)) return dielectricReflectance(cosine, within / beyond);
+	return filmReflectance(s.filmThickness, s.filmIndex, cosine, lane4(s.nm, k), within, beyond);
+}
 
 __device__ __forceinline__ float4 laneReflectances(const Shading& s, float cosine) {
+	if (s.filmThickness > 0.0f) return filmedLanes(s.filmThickness, s.filmIndex, cosine, s.nm, s.within, s.beyond); // a filmed glass is parted
 	if (!s.parted) return flat4(laneReflectance(s, cosine, 0));
 	return make_float4(laneReflectance(s, cosine, 0), laneReflectance(s, cosine, 1), laneReflectance(s, cosine, 2), laneReflectance(s, cosine, 3));
 }
@@ -349,10 +472,12 @@ __device__ __forceinline__ float reflectChance(const Shading& s, float cosine) {
 	return 0.25f * (r.x + r.y + r.z + r.w);
 }
 
-// material.cpp:836 reflectanceAcross: from the denser side, Fresnel of the arriving cosine
+// material.cpp:836 reflectanceAcross: from the denser side, Fresnel (or the
+// film, :825 filmedFromDenser) of the arriving cosine
 __device__ __forceinline__ float reflectanceAcross(const Shading& s, float leaving, float arriving, int k) {
 	const float within = lane4(s.within, k), beyond = lane4(s.beyond, k);
 	if (within <= beyond) return laneReflectance(s, leaving, k);
+	if (s.filmThickness > 0.0f) return filmReflectance(s.filmThickness, s.filmIndex, arriving, lane4(s.nm, k), beyond, within);
 	return dielectricReflectance(arriving, beyond / within);
 }
 
@@ -457,14 +582,19 @@ __device__ __forceinline__ Response respond(const Shading& s, const DeviceMateri
 	const float facets = D * smithVisibility(s.leaving, arriving, m.width);
 	const float lost   = lostOf(m, s.left, came);
 	if (s.kind == 2) {
-		// Schlick per channel, then to lanes: spectrumOf is linear in a shift toward white
+		// material.cpp:651 viewedMetal: Schlick per channel, then to lanes
+		// (spectrumOf is linear in a shift toward white), under the film
 		const float rest = powf(fminf(fmaxf(1.0f - onto, 0.0f), 1.0f), 5.0f);
-		const float4 face = lin4(s.albedo, 1.0f - rest, flat4(1.0f), rest);
-		r.value           = lin4(face, facets, s.twice, lost);
-	} else {
+		float4 face      = lin4(s.albedo, 1.0f - rest, flat4(1.0f), rest);
+		if (s.filmThickness > 0.0f) face = filmedMetalFace(face, onto, s.filmThickness, s.filmIndex, s.nm);
+		r.value = lin4(face, facets, s.twice, lost);
+	} else if (!(s.filmThickness > 0.0f)) {
+		// material.cpp:661 viewedPlastic
 		const float through = m.coatRoom > 1e-6f ? (1.0f - m.coatFront * s.left) * (1.0f - m.coatFront * came) / m.coatRoom : 0.0f;
 		const float coated  = dielectricReflectance(onto, kCoatRatio) * facets + m.coatTwice * lost;
 		r.value             = lin4(s.albedo, through / kPiF, flat4(1.0f), coated);
+	} else {
+		r.value = filmedPlastic(s.albedo, s.left, came, m.escapeAverage, onto, facets, lost, s.filmThickness, s.filmIndex, s.nm);
 	}
 	const float facetDensity = ontoRaw <= 0.0f ? 0.0f : D * s.masking / (4.0f * s.leaving);
 	r.density                = s.share * facetDensity + (1.0f - s.share) * cosineDensity;
@@ -567,8 +697,13 @@ __device__ __forceinline__ Scatter sampleSurface(const Shading& s, const DeviceM
 	// material.cpp:1300 exactGlassScatter
 	if (s.leaving <= 0.0f) return out;
 	float refl[4];
-	for (int k = 0; k < 4; ++k) refl[k] = dielectricReflectance(s.leaving, lane4(s.within, k) / lane4(s.beyond, k));
-	if (!s.parted) refl[1] = refl[2] = refl[3] = refl[0];
+	if (s.filmThickness > 0.0f) {
+		const float4 r = filmedLanes(s.filmThickness, s.filmIndex, s.leaving, s.nm, s.within, s.beyond);
+		refl[0] = r.x, refl[1] = r.y, refl[2] = r.z, refl[3] = r.w;
+	} else {
+		for (int k = 0; k < 4; ++k) refl[k] = dielectricReflectance(s.leaving, lane4(s.within, k) / lane4(s.beyond, k));
+		if (!s.parted) refl[1] = refl[2] = refl[3] = refl[0];
+	}
 	const float chance   = s.parted ? 0.25f * (refl[0] + refl[1] + refl[2] + refl[3]) : refl[0];
 	const float ratio    = s.within.x / s.beyond.x;
 	const float leftover = 1.0f - ratio * ratio * (1.0f - s.leaving * s.leaving);

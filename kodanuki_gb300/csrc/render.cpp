@@ -162,6 +162,8 @@ DeviceMaterial materialOf(const kdn_material& m, const kdn_finish& f) {
 	d.coatTwice     = float(f.coat_twice);
 	d.coatRoom      = float(f.coat_room);
 	d.losesMuch     = m.kind == 3 && !f.exact && f.loses_much ? 1u : 0u;
+	d.filmThickness = m.kind == 0 ? 0.0f : float(f.film[0]);
+	d.filmIndex     = float(f.film[1]);
 	for (int k = 0; k < 32; ++k) d.escape[k] = float(f.escape[k]);
 	return d;
 }
@@ -239,8 +241,7 @@ kdn_status patternTables(Context* ctx, const std::vector<kdn_material>& mats, st
 // Why a material cannot be drawn by these kernels, or null.
 const char* unsupported(const kdn_material& m, const kdn_finish& f) {
 	if (m.kind > 3) return "a medium (scattering body)";
-	if (f.film[0] > 0) return "a thin film";
-	if (m.kind == 3 && m.refraction == 1.0f && m.dispersion == 0.0f) return "a passable glass";
+	if (m.kind == 3 && m.refraction == 1.0f && m.dispersion == 0.0f && !(f.film[0] > 0)) return "a passable glass";
 	return nullptr;
 }
 
@@ -404,7 +405,10 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	}
 	buildSpectralTables(c.spectral);
 	std::vector<DeviceMaterial> dm;
-	for (size_t k = 0; k < mats.size(); ++k) dm.push_back(materialOf(mats[k], finishes[k]));
+	for (size_t k = 0; k < mats.size(); ++k) {
+		dm.push_back(materialOf(mats[k], finishes[k]));
+		if (dm.back().filmThickness > 0.0f) c.films = 1;
+	}
 	// material/energy.h Boundary of each rough glass that loses much
 	std::vector<float> boundaryTables;
 	{

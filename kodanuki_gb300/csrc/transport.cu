@@ -473,6 +473,9 @@ __global__ void __launch_bounds__(kBlock) surfacesKernel(SurfaceArgs A) {
 }
 
 // ---- K-shade ----
+// Films: built twice, so that a frame without thin films runs a kernel with
+// no film code (the frame's FrameConstants::films picks one)
+template <bool Films>
 __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ FrameConstants cFrame, ShadeArgs A) {
 	const uint32_t n = *A.in.count;
 	for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -606,7 +609,7 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 				const bool capped       = depth + 1 >= cFrame.surfaces;
 				const float3 outgoing   = heading * -1.0f;
 				const float3 rgb        = albedoAt(hit, normal, A.looks);
-				const Shading surf      = surfaceOf(m, rgb, normal, outgoing, nm, medium, A.looks.materials, A.looks.boundaries);
+				const Shading surf      = surfaceOf<Films>(m, rgb, normal, outgoing, nm, medium, A.looks.materials, A.looks.boundaries);
 				// trace.cpp:583 aimable: from outside every body, or from inside
 				// the glass being crossed where it bends; trace.cpp:590
 				// openSide: the side a line leaves by
@@ -818,7 +821,11 @@ cudaError_t launchCamera(const FrameConstants& frame, const PathBuffers& paths, 
 }
 
 cudaError_t launchShade(const FrameConstants& frame, const ShadeArgs& args, cudaStream_t stream, int smCount) {
-	shadeKernel<<<gridFor(args.capacity, smCount), kBlock, 0, stream>>>(frame, args);
+	if (frame.films) {
+		shadeKernel<true><<<gridFor(args.capacity, smCount), kBlock, 0, stream>>>(frame, args);
+	} else {
+		shadeKernel<false><<<gridFor(args.capacity, smCount), kBlock, 0, stream>>>(frame, args);
+	}
 	return cudaGetLastError();
 }
 

@@ -281,6 +281,58 @@ def scene_glass(seed: int = 1, width: int = 256, height: int = 256, samples: int
     return "".join(out)
 
 
+def scene_films(seed: int = 1, width: int = 256, height: int = 256, samples: int = 16, surfaces: int = 12, count: int = 12) -> str:
+    """Thin films (``film = [thickness, index]``): ``count`` bodies cycling
+    through a filmed metal (oxide-like, 250-600 nm of index 1.8-2.4), a
+    filmed plastic (300-700 nm of 1.3-1.6), a filmed glass of refraction
+    1.5 (smooth, rough, or dispersive), and a soap bubble (a glass of
+    refraction 1 under 250-550 nm of index 1.33, which bends nothing but is
+    no passable glass), over a plastic ground; one quad light, a dim sky.
+    The bodies neither touch one another nor reach the ground (bounding
+    spheres kept 0.05 apart): a path in a body that does not absorb, in a
+    scene where another glass does, that leaves its body through a touching
+    one's surface or the ground's open half-space and escapes to the sky
+    would be kept exp(-0 x inf), a NaN, in the reference
+    (absorption.cpp:28 keptThrough) as here."""
+    rng = random.Random(seed)
+    out = [_header(width, height, samples, surfaces, seed, [0.0, -8.5, 3.2], [0.0, 0.0, -0.6], 0.75)]
+    out.append(_sky([0.1, 0.1, 0.12]))
+    out.append(_quad([-1.25, 1.25, 4.5], [2.5, 0.0, 0.0], [0.0, -2.5, 0.0], blackbody_rgb(5000.0, 60.0)))
+    out.append("paint(plastic([0.5, 0.5, 0.5], roughness = 0.5)) plane([0, 0, 1], -2.2);\n\n")
+    placed = []
+    for k in range(count):
+        role = k % 4
+        if role == 0:
+            film = _v([round(rng.uniform(250.0, 600.0)), rng.uniform(1.8, 2.4)])
+            mat = f"metal({_v([rng.uniform(0.5, 0.95) for _ in range(3)])}, roughness = {_f(rng.uniform(0.05, 0.4))}, film = {film})"
+        elif role == 1:
+            film = _v([round(rng.uniform(300.0, 700.0)), rng.uniform(1.3, 1.6)])
+            mat = f"plastic({_v([rng.uniform(0.2, 0.8) for _ in range(3)])}, roughness = {_f(rng.uniform(0.05, 0.4))}, film = {film})"
+        elif role == 2:
+            film = _v([round(rng.uniform(250.0, 600.0)), rng.uniform(1.3, 2.0)])
+            variant = (k // 4) % 3
+            extra = [", roughness = 0", f", roughness = {_f(rng.uniform(0.05, 0.3))}", ", roughness = 0, dispersion = 0.01"][variant]
+            mat = f"glass(refraction = 1.5{extra}, absorb = {_v([rng.uniform(0.1, 1.0) for _ in range(3)])}, film = {film})"
+        else:
+            film = _v([round(rng.uniform(250.0, 550.0)), 1.33])
+            mat = f"glass(refraction = 1, roughness = 0, film = {film})"
+        if role == 3 or rng.random() < 0.6:
+            radius = rng.uniform(0.3, 0.7)
+            shape, bound = f"sphere({_f(radius)})", radius
+        else:
+            size = [2 * rng.uniform(0.2, 0.5) for _ in range(3)]
+            shape, bound = f"box({_v(size)}, 0.05)", 0.5 * math.sqrt(sum(x * x for x in size))
+        for _ in range(1000):
+            pos = [rng.uniform(-2.4, 2.4), rng.uniform(-2.2, 2.2), rng.uniform(-1.3, 1.2)]
+            if pos[2] - bound > -2.15 and all(math.dist(pos, q) > bound + b + 0.05 for q, b in placed):
+                break
+        else:
+            continue
+        placed.append((pos, bound))
+        out.append(f"paint({mat}) at({_v(pos)}) {shape};\n")
+    return "".join(out)
+
+
 _PATTERNS = """function bands(count) {
 	return 0.5 + 0.5 * sin(p.z * count);
 }

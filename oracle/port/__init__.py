@@ -173,7 +173,7 @@ class Material(ctypes.Structure):
                 ("escape_average", ctypes.c_double), ("escape", ctypes.c_double * 32), ("glow", ctypes.c_double * 3),
                 ("absorb", ctypes.c_double * 3), ("pattern", Program), ("pattern_arguments", ctypes.c_void_p),
                 ("stops", ctypes.c_void_p), ("stop_count", ctypes.c_uint32), ("world", ctypes.c_uint32),
-                ("loses_much", ctypes.c_uint32), ("boundary", ctypes.c_void_p)]
+                ("loses_much", ctypes.c_uint32), ("boundary", ctypes.c_void_p), ("film", ctypes.c_double * 2)]
 
 
 def _materials(scene):
@@ -202,6 +202,9 @@ def _materials(scene):
             mats[i].escape_average = float(m["finish_escape_average"][i])
             for k in range(32):
                 mats[i].escape[k] = float(m["finish_escape"][i][k])
+        if "finish_film" in m and int(m["kind"][i]) != 0:
+            # material.cpp:106 filmOf: thickness (nm, 0 for none) and index
+            mats[i].film[0], mats[i].film[1] = (float(x) for x in m["finish_film"][i])
         if "finish_boundary" in m and int(m["kind"][i]) == 3:
             boundary = np.ascontiguousarray(m["finish_boundary"][i], np.float64)
             keep.append(boundary)
@@ -360,6 +363,25 @@ def albedos(scene, leaf, other, share, point, normal) -> np.ndarray:
     L.kp_albedos.argtypes = [_P, ctypes.c_uint32, _P, ctypes.c_uint32, _P, ctypes.c_uint32, _P, _P, _P, _P, _P, _P]
     L.kp_albedos(ctypes.addressof(mats), len(mats), _ptr(leaf_material), len(leaf_material), _ptr(placements) if placements is not None else None,
                  len(leaf), _ptr(leaf), _ptr(other), _ptr(share), _ptr(point), _ptr(normal), _ptr(out))
+    del keep
+    return out
+
+
+def bsdf_answers(scene, ids, records) -> dict:
+    """material.cpp:1076 respondBsdf and :1366 sampleBsdf at n vertices of
+    the scene's materials: ids (n x 2 uint32: material, medium or
+    0xFFFFFFFF), records (n x 17 double: albedo[3], normal[3], outgoing[3],
+    incoming[3], wavelength share, draw numbers u, v, lobe, side)."""
+    mats, keep = _materials(scene)
+    ids = np.ascontiguousarray(ids, np.uint32).reshape(-1, 2)
+    records = np.ascontiguousarray(records, np.float64).reshape(-1, 17)
+    n = len(ids)
+    out = {"value": np.zeros((n, 4)), "density": np.zeros(n), "seen": np.zeros((n, 2), np.uint32), "incoming": np.zeros((n, 3)),
+           "weight": np.zeros((n, 4)), "drawn_density": np.zeros(n)}
+    L = lib()
+    L.kp_bsdf_answers.argtypes = [_P, ctypes.c_uint32, ctypes.c_uint32] + [_P] * 8
+    L.kp_bsdf_answers(ctypes.addressof(mats), len(mats), n, _ptr(ids), _ptr(records), _ptr(out["value"]), _ptr(out["density"]), _ptr(out["seen"]),
+                      _ptr(out["incoming"]), _ptr(out["weight"]), _ptr(out["drawn_density"]))
     del keep
     return out
 

@@ -147,6 +147,9 @@ typedef struct kp_material {
 	 * rarer-through shares) */
 	uint32_t loses_much;
 	const double* boundary;
+	/* material.cpp:106 filmOf: the thin film a metal, plastic or glass
+	 * wears, thickness in nanometres (0: none) and index */
+	double film[2];
 } kp_material;
 
 /* A lamp (light.cpp:78 lampOf): kind 2 sphere, 3 quad. */
@@ -176,6 +179,11 @@ void kp_render_band(const kp_octree* tree, const uint32_t* leaf_material, const 
  * the normal facing the ray): the leaf's material's colour or ramp over its
  * pattern, mixed with the other leaf's across a blend seam.  placements: 12
  * doubles a leaf (sdf/scene.h Placement: linear row by row, origin). */
+/* respondBsdf and sampleBsdf at chosen vertices (transport.c, the
+ * known-answer test against the reference's own) */
+void kp_bsdf_answers(const kp_material* materials, uint32_t count, uint32_t n, const uint32_t* ids, const double* d, double* value, double* density,
+                     uint32_t* seen, double* incoming, double* weight, double* drawn_density);
+
 void kp_albedos(const kp_material* materials, uint32_t material_count, const uint32_t* leaf_material, uint32_t leaf_count, const double* placements,
                 uint32_t n, const uint32_t* leaf, const uint32_t* other, const float* share, const double* point, const double* normal, double* rgb);
 

@@ -345,6 +345,60 @@ static double dielectric(double c, double ratio) {
 	const double pa = (ratio * on - c) / (ratio * on + c);
 	return 0.5 * (pe * pe + pa * pa);
 }
+/* ---- thin films (material.cpp:106-172): a layer `thickness` nm deep of
+ * index `index` between an outside and a beneath index, the light off its
+ * two faces interfering ---- */
+
+/* material.cpp:143 bentCosine: the cosine past a crossing from `before`
+ * into `after`, -1 where it reflects totally */
+static double bent_cosine(double before, double facing, double after) {
+	const double sine = before / after * sqrt(maxd(1 - facing * facing, 0));
+	return sine >= 1 ? -1 : sqrt(1 - sine * sine);
+}
+
+/* material.cpp:136 airySum */
+static double airy_sum(double front, double back, double shift) {
+	const double both = front * back;
+	const double top = front * front + back * back + 2 * both * shift;
+	const double bottom = 1 + both * both + 2 * both * shift;
+	return bottom > 0 ? clampd(top / bottom, 0, 1) : 1;
+}
+
+/* material.cpp:129 faceAmplitude: the perpendicular [0] and parallel [1]
+ * amplitudes of a face from index `before` into `after` */
+static void face_amplitude(double before, double after, double facing, double onward, double a[2]) {
+	a[0] = (before * facing - after * onward) / (before * facing + after * onward);
+	a[1] = (after * facing - before * onward) / (after * facing + before * onward);
+}
+
+/* material.cpp:148 filmReflectance at one wavelength */
+static double film_reflectance(const double film[2], double facing, double nm, double outside, double beneath) {
+	const double inside = bent_cosine(outside, facing, film[1]);
+	const double beyond = inside < 0 ? -1 : bent_cosine(film[1], inside, beneath);
+	if (inside < 0 || beyond < 0) return 1;
+	double near[2], far[2];
+	face_amplitude(outside, film[1], facing, inside, near);
+	face_amplitude(film[1], beneath, inside, beyond, far);
+	const double shift = cos(4 * PI * film[1] * film[0] * inside / nm);
+	return 0.5 * (airy_sum(near[0], far[0], shift) + airy_sum(near[1], far[1], shift));
+}
+
+/* material.cpp:515 stackedFilm over material.cpp:506 filmOver (air on both sides) */
+static double stacked_film(const double film[2], double facing, double nm, double under) {
+	if (!(film[0] > 0)) return under;
+	const double front = film_reflectance(film, facing, nm, 1, 1);
+	const double held = clampd(under, 0, 1);
+	const double room = 1 - front * held;
+	if (!(room > 1e-9)) return 1;
+	return front + (1 - front) * (1 - front) * held / room;
+}
+
+/* material.cpp:528 coatFacing */
+static double coat_facing(const double film[2], double onto, double nm) {
+	if (!(film[0] > 0)) return dielectric(onto, 1 / 1.5);
+	return film_reflectance(film, onto, nm, 1, 1.5);
+}
+
 static double escape_at(const double* table, double c) {
 	const double place = clampd(c, 0, 1) * 32 - 0.5;
 	int lower = (int) floor(place);
@@ -375,6 +429,7 @@ typedef struct shading {
 	spec albedo, twice, within, beyond;
 	double rgb[3]; /* the albedo at the hit, blended across a shared seam */
 	double leaving, left, share, masking;
+	double nm[4]; /* the lanes' wavelengths */
 	int parted, inside;
 } shading;
 
@@ -398,6 +453,7 @@ static shading shading_of(const kp_material* m, const double* rgb, const kp_mate
 	s.leaving = dotv(n, out);
 	s.within = flat(1);
 	s.beyond = flat(1);
+	for (int k = 0; k < 4; ++k) s.nm[k] = w->nm[k];
 	if (m->kind == 1 || m->kind == 2) {
 		s.left = escape_at(m->escape, s.leaving);
 		if (m->kind == 2) {
@@ -409,11 +465,15 @@ static shading shading_of(const kp_material* m, const double* rgb, const kp_mate
 		}
 		s.masking = smith_masking(s.leaving, m->width);
 		if (m->kind == 2) {
-			/* material.cpp:567 metalTwice over microfacet.cpp:116 averagedFresnel */
+			/* material.cpp:592 metalTwice over microfacet.cpp:116
+			 * averagedFresnel under the film facing straight on */
 			double avg[3];
 			for (int c = 0; c < 3; ++c) avg[c] = s.rgb[c] + (1 - s.rgb[c]) * (1.0 / 21);
 			const spec a = spectrum(avg, w);
-			for (int k = 0; k < 4; ++k) s.twice.v[k] = a.v[k] * a.v[k] * m->escape_average / (1 - a.v[k] * (1 - m->escape_average));
+			for (int k = 0; k < 4; ++k) {
+				const double f = stacked_film(m->film, 1, w->nm[k], a.v[k]);
+				s.twice.v[k] = f * f * m->escape_average / (1 - f * (1 - m->escape_average));
+			}
 		}
 	} else if (m->kind == 3) {
 		s.inside = medium != NO_MATERIAL;
@@ -424,6 +484,8 @@ static shading shading_of(const kp_material* m, const double* rgb, const kp_mate
 			s.beyond = lane_indices(m, w);
 			s.parted = m->dispersion != 0;
 		}
+		/* dispersion.cpp:38 filmedSides: a filmed glass answers each lane apart */
+		s.parted = s.parted || m->film[0] > 0;
 	}
 	return s;
 }
@@ -516,8 +578,12 @@ static broad broad_of(const shading* s, double leaving) {
 	return w;
 }
 
-/* material.cpp:797 laneReflectance (no film), :814 laneReflectances, :821 reflectChance */
-static double lane_reflectance(const shading* s, double c, int k) { return dielectric(c, s->within.v[k] / s->beyond.v[k]); }
+/* material.cpp:797 laneReflectance (Fresnel, or the film between the
+ * sides at lane k's wavelength), :814 laneReflectances, :821 reflectChance */
+static double lane_reflectance(const shading* s, double c, int k) {
+	if (!(s->m->film[0] > 0)) return dielectric(c, s->within.v[k] / s->beyond.v[k]);
+	return film_reflectance(s->m->film, c, s->nm[k], s->within.v[k], s->beyond.v[k]);
+}
 
 static spec lane_reflectances(const shading* s, double c) {
 	if (!s->parted) return flat(lane_reflectance(s, c, 0));
@@ -536,6 +602,8 @@ static double reflect_chance(const shading* s, double c) {
 static double reflectance_across(const shading* s, double leaving, double arriving, int k) {
 	const double within = s->within.v[k], beyond = s->beyond.v[k];
 	if (within <= beyond) return lane_reflectance(s, leaving, k);
+	/* material.cpp:825 filmedFromDenser */
+	if (s->m->film[0] > 0) return film_reflectance(s->m->film, arriving, s->nm[k], beyond, within);
 	return dielectric(arriving, beyond / within);
 }
 
@@ -640,12 +708,26 @@ static response respond(const shading* s, v3 out, v3 in, const lanes* w) {
 		const double rest = pow(clampd(1 - onto, 0, 1), 5.0);
 		double face[3];
 		for (int c = 0; c < 3; ++c) face[c] = s->rgb[c] + (1 - s->rgb[c]) * rest;
-		r.value = sadd(sscale(spectrum(face, w), facets), sscale(s->twice, lost));
-	} else {
+		spec lanes_face = spectrum(face, w);
+		for (int k = 0; k < 4; ++k) lanes_face.v[k] = stacked_film(m->film, onto, w->nm[k], lanes_face.v[k]);
+		r.value = sadd(sscale(lanes_face, facets), sscale(s->twice, lost));
+	} else if (!(m->film[0] > 0)) {
 		/* material.cpp:661 viewedPlastic */
 		const double through = m->coat_room > 1e-6 ? (1 - m->coat_front * s->left) * (1 - m->coat_front * came) / m->coat_room : 0;
 		const double coated = dielectric(onto, 1 / 1.5) * facets + m->coat_twice * lost;
 		r.value = sadd(sscale(s->albedo, through / PI), flat(coated));
+	} else {
+		/* material.cpp:661 viewedPlastic under a filmed coat: each lane's
+		 * coat (:543 filmCoating, :604 laneCoats) at its wavelength */
+		for (int k = 0; k < 4; ++k) {
+			const double faced = coat_facing(m->film, 1, w->nm[k]);
+			const double front = faced + (1 - faced) / 21;
+			const double e = m->escape_average;
+			const double twice = front * front * e / (1 - front * (1 - e));
+			const double room_k = 1 - front * e;
+			const double through = room_k > 1e-6 ? (1 - front * s->left) * (1 - front * came) / room_k : 0;
+			r.value.v[k] = s->albedo.v[k] / PI * through + coat_facing(m->film, onto, w->nm[k]) * facets + twice * lost;
+		}
 	}
 	const double fd = onto_raw <= 0 ? 0 : D * s->masking / (4 * s->leaving);
 	r.density = s->share * fd + (1 - s->share) * cosd;
@@ -738,7 +820,7 @@ static scatter sample(const shading* s, v3 out, const lanes* w, double lobe, dou
 	/* material.cpp:1300 exactGlassScatter */
 	if (s->leaving <= 0) return o;
 	double refl[4];
-	for (int k = 0; k < 4; ++k) refl[k] = dielectric(s->leaving, s->within.v[k] / s->beyond.v[k]);
+	for (int k = 0; k < 4; ++k) refl[k] = lane_reflectance(s, s->leaving, k);
 	if (!s->parted) refl[1] = refl[2] = refl[3] = refl[0];
 	const double chance = s->parted ? 0.25 * (refl[0] + refl[1] + refl[2] + refl[3]) : refl[0];
 	const double ratio = s->within.v[0] / s->beyond.v[0];
@@ -759,6 +841,36 @@ static scatter sample(const shading* s, v3 out, const lanes* w, double lobe, dou
 	o.dispersed = s->parted && s->within.v[0] != s->beyond.v[0];
 	o.medium_after = medium != NO_MATERIAL ? NO_MATERIAL : material;
 	return o;
+}
+
+/* respondBsdf and sampleBsdf (material.cpp:1076, :1366) at chosen
+ * vertices, for the known-answer test against the reference's own: per
+ * record ids (material, medium) and 17 doubles (albedo[3], normal[3],
+ * outgoing[3], incoming[3], the wavelength share, draw numbers u, v, lobe,
+ * side); out per record value[4], density, seen (found, through),
+ * incoming[3], weight[4], drawn density. */
+void kp_bsdf_answers(const kp_material* materials, uint32_t count, uint32_t n, const uint32_t* ids, const double* d, double* value, double* density,
+                     uint32_t* seen, double* incoming, double* weight, double* drawn_density) {
+	for (uint32_t i = 0; i < n; ++i) {
+		const double* r = d + 17 * (size_t) i;
+		const uint32_t material = ids[2 * i] < count ? ids[2 * i] : 0;
+		const uint32_t medium = ids[2 * i + 1];
+		lanes w;
+		kp_sampled_wavelengths(r[12], w.nm, w.density, w.basis);
+		const v3 normal = mk(r[3], r[4], r[5]), out = mk(r[6], r[7], r[8]), in = mk(r[9], r[10], r[11]);
+		const shading s = shading_of(&materials[material], r, materials, normal, out, &w, medium);
+		const response a = respond(&s, out, in, &w);
+		for (int k = 0; k < 4; ++k) value[4 * i + k] = a.value.v[k];
+		density[i] = a.density;
+		const scatter o = sample(&s, out, &w, r[15], r[16], r[13], r[14], material, medium);
+		seen[2 * i] = (uint32_t) o.found;
+		seen[2 * i + 1] = (uint32_t) o.through;
+		incoming[3 * i] = o.incoming.x;
+		incoming[3 * i + 1] = o.incoming.y;
+		incoming[3 * i + 2] = o.incoming.z;
+		for (int k = 0; k < 4; ++k) weight[4 * i + k] = o.weight.v[k];
+		drawn_density[i] = o.density;
+	}
 }
 
 /* ---- the band renderer ---- */

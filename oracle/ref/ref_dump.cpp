@@ -9,11 +9,13 @@
 //   kdn_ref_dump cut    <file.sdf> <depth> <out.bin>      cutCell down an octree
 //   kdn_ref_dump denoise  <in.bin> <out.f32>              denoisedFrame
 //   kdn_ref_dump temporal <in.bin> <out.bin>              temporalFrame
+//   kdn_ref_dump bsdf  <file.sdf> <in.bin> <out.bin>      respondBsdf, sampleBsdf
 //
 // Reference entry points used: loadScene (syntax/evaluator.cpp:2898),
 // sceneRegion (plugins/geometry/tree/build.cpp:405), sphereTraced
 // (plugins/geometry/sphere_trace/sphere_trace.cpp:216), rootPrograms/cutCell/
 // octantBox/regionBox (plugins/geometry/tree/cut.cpp:463 ff).
+#include "plugins/feature/dispersion/dispersion.h"
 #include "plugins/geometry/sphere_trace/sphere_trace.h"
 #include "plugins/geometry/tree/build.h"
 #include "plugins/geometry/tree/cut.h"
@@ -32,6 +34,12 @@
 #include <vector>
 
 using namespace kodanuki;
+
+namespace kodanuki {
+// plugins/transport/paths/material/material.cpp:329, defined with external
+// linkage there but declared in no header
+Sides sidesOf(const Materials& materials, std::uint32_t material, std::uint32_t medium);
+}
 
 namespace {
 
@@ -530,9 +538,89 @@ int dumpTemporal(const char* inPath, const char* outPath) {
 
 } // namespace
 
+// respondBsdf and sampleBsdf (plugins/transport/paths/material/material.cpp
+// :1076, :1366) at chosen vertices of a scene's materials, built as the
+// renderer builds them (materialsOf with exact smooth glass, no coats), the
+// sides set as its trace sets them (material.cpp:328 sidesOf, then
+// feature/dispersion dispersedSides and filmedSides), the wavelengths drawn
+// by math/colour.cpp sampledWavelengths.  Input records: uint32 material,
+// medium (0xFFFFFFFF: outside every body); double albedo[3], normal[3],
+// outgoing[3], incoming[3], wavelength share, draw numbers u, v, lobe, side.
+// Output per record: double value[4], density (respondBsdf of outgoing and
+// incoming); uint32 found, through; double incoming[3], weight[4], density
+// (sampleBsdf from the eye with the numbers).
+int dumpBsdf(const char* sdf, const char* inPath, const char* outPath) {
+	const SceneFile file   = loaded(sdf);
+	const Materials made   = materialsOf(file.looks, SmoothGlass::Exact);
+	const Dispersion bends = dispersionOf(file.looks);
+	FILE* in               = std::fopen(inPath, "rb");
+	FILE* out              = std::fopen(outPath, "wb");
+	if (in == nullptr || out == nullptr) {
+		return 1;
+	}
+	for (;;) {
+		std::uint32_t ids[2];
+		double d[17];
+		if (std::fread(ids, 4, 2, in) != 2 || std::fread(d, 8, 17, in) != 17) {
+			break;
+		}
+		const std::uint32_t material = ids[0];
+		const std::uint32_t medium   = ids[1] == 0xFFFFFFFFu ? noMaterial : ids[1];
+		const Wavelengths lanes      = sampledWavelengths(d[12]);
+		Sides sides                  = sidesOf(made, material, medium);
+		const DispersedQuery query   = {
+			  .material    = material,
+			  .medium      = medium,
+			  .sides       = sides,
+			  .wavelengths = lanes,
+        };
+		sides                      = dispersedSides(bends, query);
+		const DispersedQuery again = {
+			.material    = material,
+			.medium      = medium,
+			.sides       = sides,
+			.wavelengths = lanes,
+		};
+		sides           = filmedSides(bends, again);
+		const Bsdf bsdf = {
+			.material = material,
+			.albedo   = FloatColour(d[0], d[1], d[2]),
+			.normal   = math::FloatVector(d[3], d[4], d[5]),
+			.sides    = sides,
+		};
+		const BsdfPair pair = {
+			.outgoing    = { d[6], d[7], d[8] },
+			.incoming    = { d[9], d[10], d[11] },
+			.wavelengths = lanes,
+		};
+		const Response answer = respondBsdf(made, bsdf, pair);
+		const BsdfDraw draw   = {
+			  .outgoing    = { d[6], d[7], d[8] },
+			  .travel      = Travel::FromEye,
+			  .numbers     = { .pair = { .u = d[13], .v = d[14] }, .lobe = d[15], .side = d[16] },
+			  .wavelengths = lanes,
+        };
+		const Scatter drawn        = sampleBsdf(made, bsdf, draw);
+		const std::uint32_t seen[2] = { drawn.found ? 1u : 0u, drawn.through ? 1u : 0u };
+		const double incoming[3]   = { drawn.incoming.x, drawn.incoming.y, drawn.incoming.z };
+		std::fwrite(answer.value.values, 8, 4, out);
+		std::fwrite(&answer.density, 8, 1, out);
+		std::fwrite(seen, 4, 2, out);
+		std::fwrite(incoming, 8, 3, out);
+		std::fwrite(drawn.weight.values, 8, 4, out);
+		std::fwrite(&drawn.density, 8, 1, out);
+	}
+	std::fclose(in);
+	std::fclose(out);
+	return 0;
+}
+
 int main(int argc, char** argv) {
 	if (argc >= 4 && std::strcmp(argv[1], "temporal") == 0) {
 		return dumpTemporal(argv[2], argv[3]);
+	}
+	if (argc >= 5 && std::strcmp(argv[1], "bsdf") == 0) {
+		return dumpBsdf(argv[2], argv[3], argv[4]);
 	}
 	if (argc >= 4 && std::strcmp(argv[1], "denoise") == 0) {
 		return dumpDenoise(argv[2], argv[3]);
@@ -549,6 +637,6 @@ int main(int argc, char** argv) {
 	if (argc >= 5 && std::strcmp(argv[1], "cells") == 0) {
 		return dumpCells(argv[2], argv[3], argv[4]);
 	}
-	std::fprintf(stderr, "usage: kdn_ref_dump scene|trace|cut|cells ...\n");
+	std::fprintf(stderr, "usage: kdn_ref_dump scene|trace|cut|cells|bsdf|denoise|temporal ...\n");
 	return 2;
 }

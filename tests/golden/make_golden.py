@@ -54,7 +54,8 @@ def region_flags(scene: Scene) -> list[str]:
     return ["--region"] + [repr(float(x)) for x in lower] + [repr(float(x)) for x in upper]
 
 # name -> (seeds, spp per seed) of the reference frames kept as image fixtures
-IMAGES = {"room_small": (16, 64), "c1_small": (16, 64), "c2_small": (16, 64), "glow_small": (16, 64), "glass_small": (16, 64), "patterns_small": (16, 64), "rough_small": (16, 64)}
+IMAGES = {"room_small": (16, 64), "c1_small": (16, 64), "c2_small": (16, 64), "glow_small": (16, 64), "glass_small": (16, 64), "patterns_small": (16, 64), "rough_small": (16, 64),
+          "films_small": (16, 64)}
 
 # name -> (generator, kwargs, trace rays, cut depth)
 SCENES = {
@@ -68,6 +69,7 @@ SCENES = {
     "glass_small": (scenegen.scene_glass, dict(seed=6, width=48, height=48, samples=64), 0, 0),
     "patterns_small": (scenegen.scene_patterns, dict(seed=7, width=48, height=48, samples=64), 0, 0),
     "rough_small": (scenegen.scene_glass, dict(seed=8, width=48, height=48, samples=64, rough=True), 0, 0),
+    "films_small": (scenegen.scene_films, dict(seed=9, width=48, height=48, samples=64), 0, 0),
 }
 # config 3: the eight resident scenes of the serving run, 256 to 16384
 # config-1-style primitives (merge(0.05) groups of 64)

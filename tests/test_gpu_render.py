@@ -48,7 +48,7 @@ def compare(a, b):
     return (np.abs(z) > 3).mean(), cz, ca.mean(0), cb.mean(0)
 
 
-@pytest.mark.parametrize("name", ["room_small", "c1_small", "c2_small", "glow_small", "glass_small", "patterns_small", "rough_small"])
+@pytest.mark.parametrize("name", ["room_small", "c1_small", "c2_small", "glow_small", "glass_small", "patterns_small", "rough_small", "films_small"])
 def test_frame_matches_oracle_and_reference(backend, name):
     import oracle.port as op
     sc = scene(name)
@@ -95,19 +95,23 @@ def test_progressive_accumulation(backend):
     assert np.allclose(one, two, rtol=1e-5, atol=1e-6)
 
 
-def test_unsupported_material_is_refused(backend):
+@pytest.mark.parametrize("kind, refraction", [(4, 1.0), (3, 1.0)])
+def test_unsupported_material_is_refused(backend, kind, refraction):
+    """A medium (a scattering body) and a passable glass (refraction 1, no
+    dispersion, no film) are refused with KDN_BAD_ARG; a glass of
+    refraction 1 under a film is drawn (the films_small frames)."""
     import kodanuki_gb300 as K
     sc = scene("room_small")
     backend.load(sc)
     backend.build(5, 10, 64)
     blocks = K.scene_blocks(sc)
-    finishes = blocks["transport.finishes"].copy()
-    finishes["film"][0] = (0.5, 1.4)  # a thin film
-    backend.upload("transport.finishes", finishes)
+    mats = blocks["looks.materials"].copy()
+    mats["kind"][0], mats["refraction"][0], mats["dispersion"][0] = kind, refraction, 0.0
+    backend.upload("looks.materials", mats)
     with pytest.raises(K.KdnError) as e:
         backend.render(8, 8, 1)
     assert e.value.status == K.KDN_BAD_ARG
-    backend.upload("transport.finishes", blocks["transport.finishes"])
+    backend.upload("looks.materials", blocks["looks.materials"])
 
 
 def test_bad_patterns_are_refused(backend):
