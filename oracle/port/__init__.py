@@ -10,7 +10,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(os.path.dirname(HERE), "_build")
 LIB = os.path.join(OUT, "libkdn_oracle.so")
-SOURCES = ["geometry.c", "spectral.c", "transport.c", "denoise.c", "temporal.c"]
+SOURCES = ["geometry.c", "spectral.c", "transport.c", "denoise.c", "temporal.c", "upscale.c"]
 
 _lib = None
 
@@ -367,6 +367,37 @@ def albedos(scene, leaf, other, share, point, normal) -> np.ndarray:
     return out
 
 
+def upscale(width: int, height: int, factor: int, phase: int, moved: bool, kept: bool, settling: bool, lens_now, lens_before, internal,
+            distance=None, before_colour=None, before_depth=None):
+    """The oracle's upscale member over one frame (kp_upscale): the drawn
+    frame `internal` (drawn size x 3) to the shown size, with the G-buffer's
+    distances at the drawn size (or none: every sample sky) and the state
+    before (shown size; read when kept).  Returns the state after (colour n
+    x 3 double, depth n float) and the image (n x 3 float)."""
+    L = lib()
+    L.kp_upscale.argtypes = [ctypes.c_int] * 7 + [_P] * 9
+    n = width * height
+    internal = np.ascontiguousarray(internal, np.float32)
+    dist = None if distance is None else np.ascontiguousarray(distance, np.float32)
+    bc = np.zeros((n, 3)) if before_colour is None else np.ascontiguousarray(before_colour, np.float64)
+    bd = np.zeros(n, np.float32) if before_depth is None else np.ascontiguousarray(before_depth, np.float32)
+    colour = np.zeros((n, 3))
+    depth = np.zeros(n, np.float32)
+    image = np.zeros((n, 3), np.float32)
+    ln = np.ascontiguousarray(lens_now, np.float64)
+    lb = np.ascontiguousarray(lens_before, np.float64)
+    L.kp_upscale(width, height, factor, phase, int(moved), int(kept), int(settling), _ptr(ln), _ptr(lb), _ptr(internal),
+                 _ptr(dist) if dist is not None else None, _ptr(bc), _ptr(bd), _ptr(colour), _ptr(depth), _ptr(image))
+    return colour, depth, image
+
+
+def upscale_settling(kept: bool, moved: bool, before_moved: bool, before_settling: int) -> tuple[bool, int]:
+    """upscale.cpp:557 settlingFrames and the count the state keeps: whether
+    this frame settles (blends at alpha 1) and the count after."""
+    settling = (0 if moved else (4 if before_moved else before_settling)) if kept else 0
+    return settling > 0, max(settling - 1, 0)
+
+
 def bsdf_answers(scene, ids, records) -> dict:
     """material.cpp:1076 respondBsdf and :1366 sampleBsdf at n vertices of
     the scene's materials: ids (n x 2 uint32: material, medium or
@@ -410,11 +441,13 @@ def surfaces_array(surf: dict) -> np.ndarray:
 
 
 def temporal(width: int, height: int, moved: bool, recounted: bool, kept: bool, lens_now, lens_before, light, first: dict, centre: dict,
-             before: np.ndarray | None):
-    """The oracle's temporal member over one frame (kp_temporal): the state
-    after (TPIXEL_DTYPE) and the image."""
+             before: np.ndarray | None, film=(1, 0, 1, 0)):
+    """The oracle's temporal member over one frame (kp_temporal) on the drawn
+    grid: the state after (TPIXEL_DTYPE) and the image.  film: this frame's
+    film factor and phase, then the state before's."""
     L = lib()
-    L.kp_temporal.argtypes = [ctypes.c_int] * 5 + [_P] * 8
+    L.kp_temporal.argtypes = [ctypes.c_int] * 5 + [_P] * 9
+    film_arr = np.ascontiguousarray(film, np.int32)
     n = width * height
     prev = np.zeros(n, TPIXEL_DTYPE) if before is None else np.ascontiguousarray(before, TPIXEL_DTYPE)
     after = np.zeros(n, TPIXEL_DTYPE)
@@ -424,6 +457,6 @@ def temporal(width: int, height: int, moved: bool, recounted: bool, kept: bool, 
     li = np.ascontiguousarray(light, np.float64)
     fs = surfaces_array(first)
     cs = surfaces_array(centre)
-    L.kp_temporal(width, height, int(moved), int(recounted), int(kept), _ptr(ln), _ptr(lb), _ptr(li), _ptr(fs), _ptr(cs), _ptr(prev), _ptr(after),
-                  _ptr(image))
+    L.kp_temporal(width, height, int(moved), int(recounted), int(kept), _ptr(film_arr), _ptr(ln), _ptr(lb), _ptr(li), _ptr(fs), _ptr(cs), _ptr(prev),
+                  _ptr(after), _ptr(image))
     return after, image

@@ -219,10 +219,19 @@ typedef struct kp_tpixel {
 	double albedo[3];
 } kp_tpixel;
 
-void kp_temporal(int width, int height, int moved, int recounted, int kept, const double lens_now[14], const double lens_before[14], const double* light,
+void kp_temporal(int width, int height, int moved, int recounted, int kept, const int film[4], const double lens_now[14], const double lens_before[14], const double* light,
                  const kp_surface* first, const kp_surface* centre, const kp_tpixel* before, kp_tpixel* after, float* image);
 
 /* ---- numbers, wavelengths and colour (math/random.cpp, math/colour.cpp) ---- */
+/* The upscale member (upscale.c; plugins/reconstruction/upscale/upscale.cpp
+ * upscaledFrame) for one frame at a film factor above 1: width, height the
+ * shown size; internal the drawn frame (RGB float, drawn size); distance the
+ * G-buffer's distances at the drawn size or NULL; kept: the state before is
+ * read; settling: the frame settles after movement (alpha 1). */
+void kp_upscale(int width, int height, int factor, int phase, int moved, int kept, int settling, const double lens_now[14], const double lens_before[14],
+                const float* internal, const float* distance, const double* before_colour, const float* before_depth, double* colour, float* depth,
+                float* image);
+
 uint64_t kp_mixed_bits(uint64_t v);
 double kp_unit_of(uint64_t bits);
 double kp_hashed(uint64_t stream, uint64_t index, uint64_t coordinate);

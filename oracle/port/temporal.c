@@ -194,9 +194,16 @@ static int place_before(const camera* before, vec along, double* x, double* y) {
 	return *x >= 0 && *x < before->width && *y >= 0 && *y < before->height;
 }
 
+/* core/camera.cpp:51 filmCentre of this frame's film and of the state
+ * before's (temporal.cpp:187 temporalCentre): where in a grid pixel its
+ * G-buffer ray passes */
+typedef struct centres {
+	double now_x, now_y, before_x, before_y;
+} centres;
+
 /* :378 lastPlane */
-static plane last_plane(const camera* before, const kp_tpixel* last, int x, int y) {
-	const vec heading = film_heading(before, x + 0.5, y + 0.5);
+static plane last_plane(const camera* before, const centres* c, const kp_tpixel* last, int x, int y) {
+	const vec heading = film_heading(before, x + c->before_x, y + c->before_y);
 	if (last->leaf == NO_LEAF || !isfinite(last->distance)) return sky_plane();
 	plane p;
 	p.leaf = last->leaf;
@@ -208,16 +215,16 @@ static plane last_plane(const camera* before, const kp_tpixel* last, int x, int 
 
 /* :584 surfacedHistory with :495 fetchedHistory (bilinear taps over the
  * pixels before whose surface lies on this pixel's plane) */
-static history surfaced_history(const camera* now, const camera* before, const kp_tpixel* last, const kp_surface* centre, int x, int y, int w, int h,
-                                int recounted) {
+static history surfaced_history(const camera* now, const camera* before, const centres* c, const kp_tpixel* last, const kp_surface* centre, int x, int y,
+                                int w, int h, int recounted) {
 	history out;
 	memset(&out, 0, sizeof out);
-	const vec heading = film_heading(now, x + 0.5, y + 0.5);
+	const vec heading = film_heading(now, x + c->now_x, y + c->now_y);
 	const plane p = plane_through(&centre[(size_t) y * (size_t) w + (size_t) x], now->eye, heading);
 	const vec along = p.leaf == NO_LEAF ? heading : sub(p.point, before->eye);
 	double px, py;
 	if (!place_before(before, along, &px, &py)) return out;
-	const double ax = px - 0.5, ay = py - 0.5;
+	const double ax = px - c->before_x, ay = py - c->before_y;
 	const int lx = (int) floor(ax), ly = (int) floor(ay);
 	const double tx = ax - lx, ty = ay - ly;
 	double sum[3] = { 0, 0, 0 }, albedo[3] = { 0, 0, 0 }, moment = 0, weight = 0;
@@ -228,7 +235,7 @@ static history surfaced_history(const camera* now, const camera* before, const k
 			const double wt = (i == 0 ? 1 - tx : tx) * (j == 0 ? 1 - ty : ty);
 			if (!(wt > 0 && cx >= 0 && cx < w && cy >= 0 && cy < h)) continue;
 			const kp_tpixel* l = &last[(size_t) cy * (size_t) w + (size_t) cx];
-			const plane lp = last_plane(before, l, cx, cy);
+			const plane lp = last_plane(before, c, l, cx, cy);
 			if (!(l->length > 0 && on_plane(&p, &lp, recounted))) continue;
 			for (int c = 0; c < 3; ++c) {
 				sum[c] += l->colour[c] * wt;
@@ -251,19 +258,19 @@ static history surfaced_history(const camera* now, const camera* before, const k
 }
 
 /* :711 fillShare against a sample's plane along its pixel centre */
-static int sample_on_plane(const plane* p, const camera* now, const kp_surface* first, size_t k, int w) {
+static int sample_on_plane(const plane* p, const camera* now, const centres* c, const kp_surface* first, size_t k, int w) {
 	const int x = (int) (k % (size_t) w), y = (int) (k / (size_t) w);
-	const plane sp = plane_through(&first[k], now->eye, film_heading(now, x + 0.5, y + 0.5));
+	const plane sp = plane_through(&first[k], now->eye, film_heading(now, x + c->now_x, y + c->now_y));
 	return on_plane(p, &sp, 0);
 }
 
 /* :754 jointFilled: the pixel's own light if its sample lies on the
  * G-buffer's plane, else those of the 3x3 that do, else its own */
-static void joint_filled(const camera* now, const double* light, const kp_surface* first, const kp_surface* centre, int x, int y, int w, int h,
-                         double out[3]) {
+static void joint_filled(const camera* now, const centres* c, const double* light, const kp_surface* first, const kp_surface* centre, int x, int y, int w,
+                         int h, double out[3]) {
 	const size_t k = (size_t) y * (size_t) w + (size_t) x;
-	const plane p = plane_through(&centre[k], now->eye, film_heading(now, x + 0.5, y + 0.5));
-	if (sample_on_plane(&p, now, first, k, w)) {
+	const plane p = plane_through(&centre[k], now->eye, film_heading(now, x + c->now_x, y + c->now_y));
+	if (sample_on_plane(&p, now, c, first, k, w)) {
 		sample_light(light, first, k, out);
 		return;
 	}
@@ -271,7 +278,7 @@ static void joint_filled(const camera* now, const double* light, const kp_surfac
 	for (int dy = -1; dy <= 1; ++dy) {
 		for (int dx = -1; dx <= 1; ++dx) {
 			const size_t j = clamped(x + dx, y + dy, w, h);
-			if (!sample_on_plane(&p, now, first, j, w)) continue;
+			if (!sample_on_plane(&p, now, c, first, j, w)) continue;
 			double c[3];
 			sample_light(light, first, j, c);
 			for (int i = 0; i < 3; ++i) sum[i] += c[i];
@@ -285,10 +292,14 @@ static void joint_filled(const camera* now, const double* light, const kp_surfac
 	sample_light(light, first, k, out);
 }
 
-void kp_temporal(int width, int height, int moved, int recounted, int kept, const double lens_now[14], const double lens_before[14], const double* light,
-                 const kp_surface* first, const kp_surface* centre, const kp_tpixel* before, kp_tpixel* after, float* image) {
+void kp_temporal(int width, int height, int moved, int recounted, int kept, const int film[4], const double lens_now[14], const double lens_before[14],
+                 const double* light, const kp_surface* first, const kp_surface* centre, const kp_tpixel* before, kp_tpixel* after, float* image) {
 	const camera now = camera_of(lens_now, width, height);
 	const camera prev = camera_of(lens_before, width, height);
+	/* core/camera.cpp:51 filmCentre: film = factor, phase now; factor, phase before */
+	const int fn = film[0] > 1 ? film[0] : 1, fb = film[2] > 1 ? film[2] : 1;
+	const centres cs = { ((fn > 1 ? film[1] % fn : 0) + 0.5) / fn, ((fn > 1 ? film[1] / fn : 0) + 0.5) / fn, ((fb > 1 ? film[3] % fb : 0) + 0.5) / fb,
+		                 ((fb > 1 ? film[3] / fb : 0) + 0.5) / fb };
 	const double cap = moved ? MOVING_CAP : STILL_CAP;
 	for (int y = 0; y < height; ++y) {
 		for (int x = 0; x < width; ++x) {
@@ -311,7 +322,7 @@ void kp_temporal(int width, int height, int moved, int recounted, int kept, cons
 						memcpy(hist.albedo, l->albedo, sizeof hist.albedo);
 					}
 				} else {
-					hist = surfaced_history(&now, &prev, before, centre, x, y, width, height, recounted);
+					hist = surfaced_history(&now, &prev, &cs, before, centre, x, y, width, height, recounted);
 				}
 			}
 			double colour[3], moment;
@@ -319,7 +330,7 @@ void kp_temporal(int width, int height, int moved, int recounted, int kept, cons
 			if (!hist.found) {
 				/* :796 freshBlend */
 				if (aimed) sample_light(light, first, k, colour);
-				else joint_filled(&now, light, first, centre, x, y, width, height, colour);
+				else joint_filled(&now, &cs, light, first, centre, x, y, width, height, colour);
 				const double l = luminance(colour);
 				moment = l * l;
 				length = aimed ? 1.0f : 0.0f;

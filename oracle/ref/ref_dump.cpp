@@ -10,6 +10,7 @@
 //   kdn_ref_dump denoise  <in.bin> <out.f32>              denoisedFrame
 //   kdn_ref_dump temporal <in.bin> <out.bin>              temporalFrame
 //   kdn_ref_dump bsdf  <file.sdf> <in.bin> <out.bin>      respondBsdf, sampleBsdf
+//   kdn_ref_dump upscale  <in.bin> <out.bin>              upscaledFrame
 //
 // Reference entry points used: loadScene (syntax/evaluator.cpp:2898),
 // sceneRegion (plugins/geometry/tree/build.cpp:405), sphereTraced
@@ -21,6 +22,7 @@
 #include "plugins/geometry/tree/cut.h"
 #include "plugins/reconstruction/atrous/atrous.h"
 #include "plugins/reconstruction/temporal/temporal.h"
+#include "plugins/reconstruction/upscale/upscale.h"
 #include "plugins/transport/paths/material/material.h"
 #include "sdf/program.h"
 #include "sdf/scene.h"
@@ -475,8 +477,9 @@ void writePixel(FILE* out, const TemporalPixel& p) {
 
 // One frame of the temporal member (plugins/reconstruction/temporal/
 // temporal.cpp:1001 temporalFrame) at a film factor of 1.  Input: int32
-// width, height, moved, recounted, kept (the state before holds a frame),
-// demodulated (the state before's flag); doubles lens now[14], lens
+// width, height (the drawn grid), moved, recounted, kept (the state before
+// holds a frame), demodulated (the state before's flag), film factor and
+// phase, the state before's film factor and phase; doubles lens now[14], lens
 // before[14] (eye, forward, right, up, reach, aspect); then per pixel the
 // record's light (3 f64), the record's surface and the G-buffer's surface
 // (each distance f32, normal 3 f32, leaf u32, albedo 3 f32), and the state
@@ -485,10 +488,12 @@ void writePixel(FILE* out, const TemporalPixel& p) {
 // (the same layout), then the image, RGB f32.
 int dumpTemporal(const char* inPath, const char* outPath) {
 	FILE* in = std::fopen(inPath, "rb");
-	std::int32_t head[6];
+	std::int32_t head[10];
 	double now[14], before[14];
-	if (std::fread(head, 4, 6, in) != 6 || std::fread(now, 8, 14, in) != 14 || std::fread(before, 8, 14, in) != 14) return 1;
+	if (std::fread(head, 4, 10, in) != 10 || std::fread(now, 8, 14, in) != 14 || std::fread(before, 8, 14, in) != 14) return 1;
 	const int width = head[0], height = head[1];
+	const FilmPlan film       = { .factor = head[6], .phase = head[7] };
+	const FilmPlan filmBefore = { .factor = head[8], .phase = head[9] };
 	const std::size_t n = std::size_t(width) * std::size_t(height);
 	FrameRecord record  = emptyFrameRecord();
 	record.width        = width;
@@ -498,7 +503,7 @@ int dumpTemporal(const char* inPath, const char* outPath) {
 	state.width         = head[4] ? width : 0;
 	state.height        = head[4] ? height : 0;
 	state.demodulated   = head[5] != 0;
-	state.film          = { .factor = 1, .phase = 0 };
+	state.film          = filmBefore;
 	for (std::size_t k = 0; k < n; ++k) {
 		double light[3];
 		Surface first, centre;
@@ -510,15 +515,16 @@ int dumpTemporal(const char* inPath, const char* outPath) {
 		if (head[4]) state.pixels.push_back(last);
 	}
 	std::fclose(in);
-	const Lens lensNow    = lensOf14(now, width, height);
-	const Lens lensBefore = lensOf14(before, width, height);
+	// the shown frame: the drawn grid times the factor (core/shown.cpp:7 shownLens)
+	const Lens lensNow    = lensOf14(now, width * film.factor, height * film.factor);
+	const Lens lensBefore = lensOf14(before, width * film.factor, height * film.factor);
 	static const std::vector<PixelSum> estimates;
 	const ShownFrame frame = {
-		.width     = width,
-		.height    = height,
+		.width     = width * film.factor,
+		.height    = height * film.factor,
 		.lens      = lensNow,
 		.before    = lensBefore,
-		.film      = { .factor = 1, .phase = 0 },
+		.film      = film,
 		.moved     = head[2] != 0,
 		.restarted = false,
 		.recounted = head[3] != 0,
@@ -531,6 +537,85 @@ int dumpTemporal(const char* inPath, const char* outPath) {
 	const Temporal next = temporalFrame(state, frame);
 	FILE* out           = std::fopen(outPath, "wb");
 	for (const TemporalPixel& p : next.state.pixels) writePixel(out, p);
+	std::fwrite(next.image.rgb.data(), 4, next.image.rgb.size(), out);
+	std::fclose(out);
+	return 0;
+}
+
+// The upscale member (plugins/reconstruction/upscale/upscale.cpp
+// upscaledFrame) for one frame.  Input: int32 shown width, height, film
+// factor, phase, moved, restarted, kept (a state before is given), the state
+// before's moved flag and settling count, surfaces (the G-buffer's
+// distances are given); doubles lens now[14], lens before[14] (eye,
+// forward, right, up, reach, aspect); the internal image at the drawn size
+// (RGB f32); the G-buffer's distance a drawn pixel (f32) where given; the
+// state before's pixels at the shown size (colour 3 f64, depth f32) where
+// kept.  Output: the state after's moved flag and settling count (int32),
+// its pixels (the same layout), then the image, RGB f32.
+int dumpUpscale(const char* inPath, const char* outPath) {
+	FILE* in = std::fopen(inPath, "rb");
+	std::int32_t head[10];
+	double now[14], before[14];
+	if (in == nullptr || std::fread(head, 4, 10, in) != 10 || std::fread(now, 8, 14, in) != 14 || std::fread(before, 8, 14, in) != 14) return 1;
+	const int width = head[0], height = head[1];
+	const FilmPlan film = { .factor = head[2], .phase = head[3] };
+	const int drawnWidth = width / film.factor, drawnHeight = height / film.factor;
+	const std::size_t drawn = std::size_t(drawnWidth) * std::size_t(drawnHeight);
+	const std::size_t shown = std::size_t(width) * std::size_t(height);
+	Image internal          = blankImage(drawnWidth, drawnHeight);
+	if (std::fread(internal.rgb.data(), 4, drawn * 3, in) != drawn * 3) return 1;
+	std::vector<Surface> surfaces;
+	if (head[9]) {
+		for (std::size_t k = 0; k < drawn; ++k) {
+			Surface s = missedSurface();
+			if (std::fread(&s.distance, 4, 1, in) != 1) return 1;
+			surfaces.push_back(s);
+		}
+	}
+	UpscaleState state = emptyUpscale();
+	if (head[6]) {
+		state.width  = width;
+		state.height = height;
+		for (std::size_t k = 0; k < shown; ++k) {
+			double colour[3];
+			float depth;
+			if (std::fread(colour, 8, 3, in) != 3 || std::fread(&depth, 4, 1, in) != 1) return 1;
+			state.pixels.push_back(UpscalePixel { .colour = { colour[0], colour[1], colour[2] }, .depth = depth });
+		}
+	}
+	state.moved    = head[7] != 0;
+	state.settling = head[8];
+	std::fclose(in);
+	const Lens lensNow    = lensOf14(now, width, height);
+	const Lens lensBefore = lensOf14(before, width, height);
+	FrameRecord record    = emptyFrameRecord();
+	record.width          = drawnWidth;
+	record.height         = drawnHeight;
+	static const std::vector<PixelSum> estimates;
+	const ShownFrame frame = {
+		.width     = width,
+		.height    = height,
+		.lens      = lensNow,
+		.before    = lensBefore,
+		.film      = film,
+		.moved     = head[4] != 0,
+		.restarted = head[5] != 0,
+		.recounted = false,
+		.still     = head[4] ? 1u : 2u,
+		.record    = record,
+		.estimates = estimates,
+		.surfaces  = surfaces,
+		.threads   = 4,
+	};
+	const Upscaled next = upscaledFrame(state, internal, frame);
+	FILE* out           = std::fopen(outPath, "wb");
+	const std::int32_t tail[2] = { next.state.moved ? 1 : 0, next.state.settling };
+	std::fwrite(tail, 4, 2, out);
+	for (const UpscalePixel& p : next.state.pixels) {
+		const double colour[3] = { p.colour.red, p.colour.green, p.colour.blue };
+		std::fwrite(colour, 8, 3, out);
+		std::fwrite(&p.depth, 4, 1, out);
+	}
 	std::fwrite(next.image.rgb.data(), 4, next.image.rgb.size(), out);
 	std::fclose(out);
 	return 0;
@@ -619,6 +704,9 @@ int main(int argc, char** argv) {
 	if (argc >= 4 && std::strcmp(argv[1], "temporal") == 0) {
 		return dumpTemporal(argv[2], argv[3]);
 	}
+	if (argc >= 4 && std::strcmp(argv[1], "upscale") == 0) {
+		return dumpUpscale(argv[2], argv[3]);
+	}
 	if (argc >= 5 && std::strcmp(argv[1], "bsdf") == 0) {
 		return dumpBsdf(argv[2], argv[3], argv[4]);
 	}
@@ -637,6 +725,6 @@ int main(int argc, char** argv) {
 	if (argc >= 5 && std::strcmp(argv[1], "cells") == 0) {
 		return dumpCells(argv[2], argv[3], argv[4]);
 	}
-	std::fprintf(stderr, "usage: kdn_ref_dump scene|trace|cut|cells|bsdf|denoise|temporal ...\n");
+	std::fprintf(stderr, "usage: kdn_ref_dump scene|trace|cut|cells|bsdf|denoise|temporal|upscale ...\n");
 	return 2;
 }

@@ -294,11 +294,18 @@ def _fp16_surfaces(surf: dict) -> dict:
             "albedo": surf["albedo"].astype(np.float16).astype(np.float32), "leaf": surf["leaf"].astype(np.uint32)}
 
 
-def temporal_frames(scene: Scene, rng: np.random.Generator):
+# core/shown.cpp bayerPhase: the order a film factor's phases are drawn in
+BAYER = {1: [0], 2: [0, 3, 1, 2], 3: [0, 7, 5, 2, 6, 4, 3, 1, 8], 4: [0, 10, 2, 8, 5, 15, 7, 13, 1, 11, 3, 9, 4, 14, 6, 12]}
+
+
+def temporal_frames(scene: Scene, rng: np.random.Generator, factor: int = 1):
     """A seeded sequence of frames over config 2's small scene, the camera
     still, then moving, then still again: per frame the lens now and before,
-    the record's light and first surfaces (each pixel's last sample, jittered)
-    and the G-buffer (pixel centres)."""
+    the record's light and first surfaces (each pixel's last sample, jittered
+    within the shown pixel its phase aims at) and the G-buffer (through that
+    shown pixel's centre, core/camera.cpp:51 filmCentre), on the drawn grid
+    of TEMPORAL_SIZE at a film factor of `factor`, the phases in Bayer
+    order."""
     import oracle.port as op
     w, h = TEMPORAL_SIZE
     build = dict(min_depth=5, max_depth=9, split_steps=64)
@@ -320,32 +327,39 @@ def temporal_frames(scene: Scene, rng: np.random.Generator):
     frames = []
     for f, (kept, move) in enumerate(plan):
         lens = lenses[f]
-        gbuffer = _fp16_surfaces(op.traced_surfaces(scene, w, h, build, lens=lens))
-        first = _fp16_surfaces(op.traced_surfaces(scene, w, h, build, lens=lens, offsets=rng.random((w * h, 2))))
+        phase = BAYER[factor][f % (factor * factor)]
+        column, row = phase % factor, phase // factor
+        centre = np.tile([(column + 0.5) / factor, (row + 0.5) / factor], (w * h, 1))
+        jitter = (np.array([column, row]) + rng.random((w * h, 2))) / factor
+        gbuffer = _fp16_surfaces(op.traced_surfaces(scene, w, h, build, lens=lens, offsets=None if factor == 1 else centre))
+        first = _fp16_surfaces(op.traced_surfaces(scene, w, h, build, lens=lens, offsets=jitter))
         hit = first["leaf"] != 0xFFFFFFFF
         shade = 0.3 + 0.7 * np.clip(first["normal"].astype(np.float64) @ sun, 0, None)
         light = np.where(hit[:, None], first["albedo"].astype(np.float64) * shade[:, None], np.array([0.4, 0.5, 0.7]))
         light = light * (1 + 0.3 * rng.normal(size=light.shape))
         light = np.clip(light, 0, None)
-        frames.append(dict(lens=lens, before=lenses[max(f - 1, 0)], kept=kept, moved=move, light=light, first=first, gbuffer=gbuffer))
+        frames.append(dict(lens=lens, before=lenses[max(f - 1, 0)], kept=kept, moved=move, light=light, first=first, gbuffer=gbuffer,
+                           factor=factor, phase=phase))
     return frames
 
 
-def temporal_fixture(dump: str, tmp: str) -> None:
-    """tests/golden/temporal.npz: the reference's temporalFrame over a
-    sequence of frames, each fed the state the one before left."""
+def temporal_fixture(dump: str, tmp: str, factor: int = 1) -> None:
+    """tests/golden/temporal.npz (a film factor of 1) and
+    temporal_factor<k>.npz: the reference's temporalFrame over a sequence of
+    frames, each fed the state the one before left."""
     scene = Scene.load(os.path.join(HERE, "scenes", "c2_small.npz"))
     w, h = TEMPORAL_SIZE
     n = w * h
-    frames = temporal_frames(scene, np.random.default_rng(2024))
+    frames = temporal_frames(scene, np.random.default_rng(2024 + factor - 1), factor)
     state = None
-    out = {"width": w, "height": h, "frames": len(frames)}
+    out = {"width": w, "height": h, "frames": len(frames), "factor": factor}
     pixel = np.dtype([("colour", "<f8", 3), ("moment", "<f8"), ("length", "<f4"), ("distance", "<f4"), ("normal", "<f8", 3), ("leaf", "<u4"),
                       ("albedo", "<f8", 3)])
     for f, fr in enumerate(frames):
         path = os.path.join(tmp, f"temporal_{f}.bin")
+        before_phase = frames[f - 1]["phase"] if f else 0
         with open(path, "wb") as fh:
-            fh.write(struct.pack("<6i", w, h, fr["moved"], 0, fr["kept"], 1))
+            fh.write(struct.pack("<10i", w, h, fr["moved"], 0, fr["kept"], 1, factor, fr["phase"], factor, before_phase))
             fh.write(fr["lens"].astype("<f8").tobytes())
             fh.write(fr["before"].astype("<f8").tobytes())
             before = state if state is not None else np.zeros(n, pixel)
@@ -359,8 +373,9 @@ def temporal_fixture(dump: str, tmp: str) -> None:
         raw = open(res, "rb").read()
         after = np.frombuffer(raw[: n * pixel.itemsize], pixel).copy()
         image = np.frombuffer(raw[n * pixel.itemsize:], "<f4").reshape(n, 3).copy()
-        for key in ("lens", "before", "kept", "moved", "light"):
+        for key in ("lens", "before", "kept", "moved", "light", "phase"):
             out[f"{f}.{key}"] = fr[key]
+        out[f"{f}.before_phase"] = before_phase
         for part in ("first", "gbuffer"):
             for key, v in fr[part].items():
                 out[f"{f}.{part}.{key}"] = v
@@ -368,8 +383,76 @@ def temporal_fixture(dump: str, tmp: str) -> None:
             out[f"{f}.state.{key}"] = after[key]
         out[f"{f}.image"] = image
         state = after
-        print(" temporal frame", f, "kept", fr["kept"], "moved", fr["moved"], "held", float((after["length"] > 1).mean()), "image", image.mean(0))
-    np.savez_compressed(os.path.join(HERE, "temporal.npz"), **out)
+        print(" temporal frame", f, "factor", factor, "phase", fr["phase"], "kept", fr["kept"], "moved", fr["moved"], "held",
+              float((after["length"] > 1).mean()), "image", image.mean(0))
+    np.savez_compressed(os.path.join(HERE, "temporal.npz" if factor == 1 else f"temporal_factor{factor}.npz"), **out)
+
+
+def upscale_fixture(dump: str, tmp: str) -> None:
+    """tests/golden/upscale.npz: the reference's upscaledFrame
+    (plugins/reconstruction/upscale/upscale.cpp) over a sequence of frames
+    at a film factor of 2, each fed the state the one before left: the
+    temporal fixture's factor-2 frames (their lenses, FP16 G-buffer
+    distances and the reference's own temporal images as the drawn frames),
+    then three still frames that settle, a restart, and two frames at a film
+    factor of 4 without a G-buffer (every sample sky)."""
+    import oracle.port as op
+    t = np.load(os.path.join(HERE, "temporal_factor2.npz"))
+    dw, dh = int(t["width"]), int(t["height"])
+    rng = np.random.default_rng(77)
+    seq = []
+    for f in range(int(t["frames"])):
+        seq.append(dict(factor=2, phase=int(t[f"{f}.phase"]), moved=int(t[f"{f}.moved"]), restarted=0, lens=t[f"{f}.lens"], before=t[f"{f}.before"],
+                        internal=t[f"{f}.image"].reshape(-1, 3), distance=t[f"{f}.gbuffer.distance"]))
+    last = seq[-1]
+    for k in range(3):
+        seq.append(dict(last, phase=BAYER[2][(len(seq)) % 4], moved=0, before=last["lens"],
+                        internal=np.clip(last["internal"] * (1 + 0.05 * rng.normal(size=last["internal"].shape)), 0, None).astype(np.float32)))
+    seq.append(dict(seq[-1], phase=BAYER[2][len(seq) % 4], restarted=1))
+    small = (dw // 2, dh // 2)
+    for k in range(2):
+        internal = (0.5 + 0.4 * np.sin(np.arange(small[0] * small[1] * 3) * 0.37)).astype(np.float32).reshape(-1, 3)
+        seq.append(dict(factor=4, phase=BAYER[4][k], moved=0, restarted=0, lens=last["lens"], before=last["lens"], internal=internal, distance=None))
+    out = {"frames": len(seq)}
+    state = None  # (width, height, colour, depth, moved, settling)
+    for f, fr in enumerate(seq):
+        factor = fr["factor"]
+        ddw, ddh = (dw, dh) if factor == 2 else small
+        w, h = ddw * factor, ddh * factor
+        kept = int(state is not None and state[0] == w and state[1] == h and not fr["restarted"])
+        before_moved = state[4] if state is not None else 0
+        before_settling = state[5] if state is not None else 0
+        path = os.path.join(tmp, f"upscale_{f}.bin")
+        with open(path, "wb") as fh:
+            fh.write(struct.pack("<10i", w, h, factor, fr["phase"], fr["moved"], fr["restarted"], 1 if state is not None and kept else 0,
+                                 before_moved, before_settling, 0 if fr["distance"] is None else 1))
+            fh.write(np.asarray(fr["lens"], "<f8").tobytes())
+            fh.write(np.asarray(fr["before"], "<f8").tobytes())
+            fh.write(np.asarray(fr["internal"], "<f4").tobytes())
+            if fr["distance"] is not None:
+                fh.write(np.asarray(fr["distance"], "<f4").tobytes())
+            if state is not None and kept:
+                rec = np.zeros(w * h, [("c", "<f8", 3), ("d", "<f4")])
+                rec["c"], rec["d"] = state[2], state[3]
+                fh.write(rec.tobytes())
+        res = os.path.join(tmp, f"upscale_{f}.out")
+        subprocess.run([dump, "upscale", path, res], check=True)
+        raw = open(res, "rb").read()
+        moved_after, settling_after = struct.unpack("<2i", raw[:8])
+        px = np.frombuffer(raw[8:8 + w * h * 28], [("c", "<f8", 3), ("d", "<f4")])
+        image = np.frombuffer(raw[8 + w * h * 28:], "<f4").reshape(-1, 3)
+        for key in ("factor", "phase", "moved", "restarted", "lens", "before", "internal"):
+            out[f"{f}.{key}"] = fr[key]
+        if fr["distance"] is not None:
+            out[f"{f}.distance"] = fr["distance"]
+        out[f"{f}.kept"] = kept
+        out[f"{f}.before_moved"], out[f"{f}.before_settling"] = before_moved, before_settling
+        out[f"{f}.colour"], out[f"{f}.depth"], out[f"{f}.image"] = px["c"].copy(), px["d"].copy(), image.copy()
+        out[f"{f}.moved_after"], out[f"{f}.settling_after"] = moved_after, settling_after
+        state = (w, h, px["c"].copy(), px["d"].copy(), moved_after, settling_after)
+        print(" upscale frame", f, "factor", factor, "phase", fr["phase"], "kept", kept, "moved", fr["moved"], "settling after", settling_after,
+              "image", image.mean(0))
+    np.savez_compressed(os.path.join(HERE, "upscale.npz"), **out)
 
 
 # The benchmark's own octree of config 2 and the cells sampled from it for
@@ -435,6 +518,9 @@ def main() -> None:
         denoise_fixture(dump, tmp)
     if args.only in (None, "temporal"):
         temporal_fixture(dump, tmp)
+        temporal_fixture(dump, tmp, factor=2)
+    if args.only in (None, "temporal", "upscale"):
+        upscale_fixture(dump, tmp)
     if args.only in (None, "cutdeep"):
         deep_cut_fixture(dump, tmp)
     for name, (gen, kw, nrays, depth) in SCENES.items():
