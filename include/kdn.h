@@ -201,6 +201,16 @@ typedef struct kdn_frame {
 	uint32_t first;   /* sample index of this call's first sample of every pixel */
 	uint32_t accumulate; /* 1: add to the pixel sums of the previous call */
 	uint32_t flags;      /* KDN_FRAME_DENOISE: return the denoised frame */
+	/* core/camera.h:65 FilmPlan: with a factor of 2 to 4 (0 or 1: none) the
+	 * frame is drawn at width / factor x height / factor, each drawn pixel's
+	 * samples aimed at the shown pixel (x * factor + phase % factor,
+	 * y * factor + phase / factor) (plugins/transport/paths/trace.cpp:93
+	 * phasedDraw), and shown at width x height through the reconstruction
+	 * chain temporal + a-trous + upscale: KDN_FRAME_DENOISE is needed and
+	 * the size must be a multiple of the factor.  The pixel sums, the record
+	 * and the G-buffer are at the drawn size. */
+	uint32_t factor;
+	uint32_t phase; /* 0 .. factor^2 - 1: core/shown.cpp bayerFilm gives the order */
 } kdn_frame;
 
 /* With KDN_FRAME_DENOISE a frame returns what the reference shows through
@@ -413,9 +423,12 @@ kdn_status kdn_denoise_static(const kdn_denoise_frame* frame, const float* colou
 
 /*
  * The temporal member (plugins/reconstruction/temporal/temporal.cpp:1001
- * temporalFrame) for one frame at a film factor of 1 with a G-buffer: the
- * grid the reference runs before the a-trous denoiser, each pixel's light
- * divided by the albedo of its sample's first surface.  Each pixel blends
+ * temporalFrame) for one frame with a G-buffer: the drawn grid the
+ * reference runs before the a-trous denoiser, each pixel's light divided by
+ * the albedo of its sample's first surface.  At a film factor above 1 a
+ * grid pixel's rays pass through the centre of the shown pixel its phase
+ * aims at (core/camera.cpp:51 filmCentre), this frame's and, for the
+ * history, the state before's.  Each pixel blends
  * this frame's light into its history: its own on a still camera, else the
  * frame before's pixels around where its G-buffer point was seen whose
  * surface lies on its plane (bilinear), clamped to this frame's 3x3
@@ -425,10 +438,14 @@ kdn_status kdn_denoise_static(const kdn_denoise_frame* frame, const float* colou
  * frame and the a-trous denoiser; kdn_temporal_device runs it alone.
  */
 typedef struct kdn_temporal_frame {
-	int32_t width, height;
+	int32_t width, height; /* the drawn grid */
 	uint32_t moved;     /* the camera moved since the frame before */
 	uint32_t recounted; /* the scene's shapes changed: leaves compare as hit or sky alone */
 	uint32_t kept;      /* the state before holds a frame of this size */
+	uint32_t factor;    /* this frame's film factor (0 or 1: none) and phase */
+	uint32_t phase;
+	uint32_t before_factor; /* the state before's film factor and phase */
+	uint32_t before_phase;
 	uint32_t pad_;
 	double now[14], before[14]; /* lenses: eye, forward, right, up, reach, aspect */
 } kdn_temporal_frame;
@@ -457,6 +474,39 @@ typedef struct kdn_temporal_buffers {
 } kdn_temporal_buffers;
 
 kdn_status kdn_temporal_device(kdn_ctx* ctx, const kdn_temporal_frame* frame, const kdn_temporal_buffers* buffers, void* stream);
+
+/*
+ * The upscale member (plugins/reconstruction/upscale/upscale.cpp
+ * upscaledFrame) for one frame at a film factor of 2 to 4: a frame drawn at
+ * 1/factor of the shown size, each drawn pixel's samples aimed at one
+ * phase of the factor^2 shown pixels it covers, gathered to the shown size.
+ * Each shown pixel takes the 3x3 drawn pixels around it (Gaussian and
+ * Catmull-Rom weights) and blends them into the shown pixels of the frame
+ * before where its nearest surface was seen there and the depth matches,
+ * the history clamped to the 3x3's mean and deviation.  kdn_render with
+ * KDN_FRAME_DENOISE at a film factor above 1 runs it after the a-trous
+ * denoiser; kdn_upscale_device runs it alone.  Its answers are the
+ * reference's to the bit.
+ */
+typedef struct kdn_upscale_frame {
+	int32_t width, height; /* the shown size: the drawn size times the factor */
+	uint32_t factor;       /* 2, 3 or 4 */
+	uint32_t phase;        /* the phase this frame's draws aimed at, 0 .. factor^2 - 1 */
+	uint32_t kept;         /* the state before is of this size and the sequence goes on */
+	uint32_t settling;     /* upscale.cpp:557 settlingFrames is above 0: blend at alpha 1 */
+	double now[14], before[14]; /* lenses at the shown size: eye, forward, right, up, reach, aspect */
+} kdn_upscale_frame;
+
+/* Device arrays, row-major. */
+typedef struct kdn_upscale_buffers {
+	const float* internal;    /* x3 at the drawn size: the reconstructed frame (temporal + a-trous) */
+	const uint16_t* distance; /* FP16 bits at the drawn size: the G-buffer's distances; null: every sample sky */
+	const float* before;      /* x4 at the shown size: the state before, colour and depth (read when kept) */
+	float* after;             /* x4: the state after */
+	float* image;             /* x3: the shown frame */
+} kdn_upscale_buffers;
+
+kdn_status kdn_upscale_device(kdn_ctx* ctx, const kdn_upscale_frame* frame, const kdn_upscale_buffers* buffers, void* stream);
 
 /* Write a buffer larger than the L2 cache on the context's stream, so that
  * the next launch starts with a cold cache. */

@@ -59,7 +59,12 @@ class BuildOptions(ctypes.Structure):
 
 class Frame(ctypes.Structure):
     _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("samples", ctypes.c_int32), ("surfaces", ctypes.c_int32),
-                ("seed", ctypes.c_int32), ("first", ctypes.c_uint32), ("accumulate", ctypes.c_uint32), ("flags", ctypes.c_uint32)]
+                ("seed", ctypes.c_int32), ("first", ctypes.c_uint32), ("accumulate", ctypes.c_uint32), ("flags", ctypes.c_uint32),
+                ("factor", ctypes.c_uint32), ("phase", ctypes.c_uint32)]
+
+
+# core/shown.cpp bayerPhase: the order a film factor's phases are drawn in
+BAYER = {1: [0], 2: [0, 3, 1, 2], 3: [0, 7, 5, 2, 6, 4, 3, 1, 8], 4: [0, 10, 2, 8, 5, 15, 7, 13, 1, 11, 3, 9, 4, 14, 6, 12]}
 
 
 FRAME_DENOISE = 1  # include/kdn.h KDN_FRAME_DENOISE
@@ -88,7 +93,7 @@ EXPORTS = [
     "kdn_serve_latency", "kdn_serve_last_error", "kdn_serve_close", "kdn_serve_cancel_queued", "kdn_set_sm_limit", "kdn_serve_reset_latency",
     "kdn_guide_open", "kdn_guide_close", "kdn_guide_last_error", "kdn_guide_sizes", "kdn_guide_get_params", "kdn_guide_set_params",
     "kdn_guide_gradients", "kdn_guide_train", "kdn_guide_query", "kdn_guide_clear_samples", "kdn_guide_ready", "kdn_set_guide",
-    "kdn_guide_select", "kdn_set_march_budget",
+    "kdn_guide_select", "kdn_set_march_budget", "kdn_upscale_device",
 ]
 
 REQUEST_INTERACTIVE = 4
@@ -119,7 +124,19 @@ class DenoiseFrame(ctypes.Structure):
 
 class TemporalFrame(ctypes.Structure):
     _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("moved", ctypes.c_uint32), ("recounted", ctypes.c_uint32),
-                ("kept", ctypes.c_uint32), ("pad", ctypes.c_uint32), ("now", ctypes.c_double * 14), ("before", ctypes.c_double * 14)]
+                ("kept", ctypes.c_uint32), ("factor", ctypes.c_uint32), ("phase", ctypes.c_uint32), ("before_factor", ctypes.c_uint32),
+                ("before_phase", ctypes.c_uint32), ("pad", ctypes.c_uint32), ("now", ctypes.c_double * 14), ("before", ctypes.c_double * 14)]
+
+
+class UpscaleFrame(ctypes.Structure):
+    """include/kdn.h kdn_upscale_frame."""
+    _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("factor", ctypes.c_uint32), ("phase", ctypes.c_uint32),
+                ("kept", ctypes.c_uint32), ("settling", ctypes.c_uint32), ("now", ctypes.c_double * 14), ("before", ctypes.c_double * 14)]
+
+
+class UpscaleBuffers(ctypes.Structure):
+    """include/kdn.h kdn_upscale_buffers: device pointers."""
+    _fields_ = [(name, ctypes.c_void_p) for name in ("internal", "distance", "before", "after", "image")]
 
 
 class TemporalBuffers(ctypes.Structure):
@@ -164,6 +181,7 @@ def library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.kdn_world_march.argtypes = [P, ctypes.c_uint64, P, ctypes.c_uint32, P, ctypes.c_size_t, P]
     L.kdn_world_locate.argtypes = [P, P, ctypes.c_uint32, P, P]
     L.kdn_temporal_device.argtypes = [P, ctypes.POINTER(TemporalFrame), ctypes.POINTER(TemporalBuffers), P]
+    L.kdn_upscale_device.argtypes = [P, ctypes.POINTER(UpscaleFrame), ctypes.POINTER(UpscaleBuffers), P]
     L.kdn_denoise.argtypes = [P, ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P]
     L.kdn_denoise_device.argtypes = [P, ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P, P]
     L.kdn_denoise_static.argtypes = [ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P, P]
@@ -384,14 +402,17 @@ class Backend:
         return bool(g.value), pc.value, gc.value
 
     def render(self, width: int, height: int, samples: int, surfaces: int | None = None, seed: int | None = None,
-               first: int = 0, accumulate: bool = False, denoise: bool = False, restart: bool = False) -> np.ndarray:
+               first: int = 0, accumulate: bool = False, denoise: bool = False, restart: bool = False, factor: int = 1,
+               phase: int = 0) -> np.ndarray:
         """Draw `samples` samples a pixel and return the pixel means
         (linear RGB, float32, height x width x 3), or with `denoise` the
-        means filtered by the a-trous denoiser over the first surfaces."""
+        means through the reconstruction chain (temporal + a-trous, and at a
+        film `factor` of 2 to 4 the upscale member: the frame is drawn at
+        1/factor of the size, aimed at `phase`)."""
         sc = self.scene
         f = Frame(width, height, samples, surfaces if surfaces is not None else int(sc.render["surfaces"]),
                   seed if seed is not None else int(sc.render["seed"]), first, 1 if accumulate else 0,
-                  (FRAME_DENOISE if denoise else 0) | (FRAME_RESTART if restart else 0))
+                  (FRAME_DENOISE if denoise else 0) | (FRAME_RESTART if restart else 0), factor, phase)
         out = np.zeros((height, width, 3), np.float32)
         self._check(self.lib.kdn_render(self.handle, ctypes.byref(f), _ptr(out)))
         return out

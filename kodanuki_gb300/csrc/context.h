@@ -25,6 +25,16 @@ struct DeviceBuffer {
 
 struct FrameState; // render.cpp
 
+// The upscale member's scratch: the drawn frame's tones and depths, and the
+// axes of every phase of a film factor over a shown size (columns of each
+// place across, then rows of each place down), kept while the factor and
+// size stay.
+struct UpscaleScratch {
+	DeviceBuffer samples, axes;
+	uint32_t factor = 0;
+	int32_t width = 0, height = 0;
+};
+
 struct Context {
 	int device          = 0;
 	int smCount         = 0; // SMs the kernels' grids are sized for (kdn_set_sm_limit)
@@ -55,6 +65,7 @@ struct Context {
 	DeviceBuffer nodes, leaves, programs, steps, march, ssa, leafMaterial, objectMaterial, grid, gridWalls;
 	DeviceBuffer extendRays, extendHits, extendStates, counters, l2;
 	DeviceBuffer denoiseScratch, denoiseIo, fetch;
+	UpscaleScratch upscale; // kdn_upscale_device's
 	FrameState* frame = nullptr;
 	// the learned guide frames use (kdn_set_guide): KDN_GUIDE_SAMPLE, KDN_GUIDE_TRAIN
 	kdn_guide* guide    = nullptr;
@@ -87,6 +98,10 @@ struct Context {
 
 // guide.cu: the device a learned guide lives on
 int guideDevice(const kdn_guide* guide);
+
+// denoise_abi.cpp: the upscale member over device buffers (kdn_upscale_device
+// and a frame's chain), with the scratch of its caller.
+kdn_status upscaleOnDevice(Context* ctx, UpscaleScratch& scratch, const kdn_upscale_frame* frame, const kdn_upscale_buffers* io, cudaStream_t stream);
 
 // denoise_abi.cpp: the denoiser over device buffers with the context's scratch.
 kdn_status denoiseOnDevice(Context* ctx, const kdn_denoise_frame* frame, const float* colour, const float* moment, const float* length, const uint16_t* distance,

@@ -2,7 +2,9 @@
 #include "context.h"
 #include "denoise.h"
 
+#include <algorithm>
 #include <cstring>
+#include <vector>
 
 using kdn::Context;
 
@@ -130,6 +132,7 @@ kdn_status kdn_denoise(kdn_ctx* handle, const kdn_denoise_frame* frame, const fl
 } // extern "C"
 
 #include "temporal.h"
+#include "upscale.h"
 
 extern "C" kdn_status kdn_temporal_device(kdn_ctx* handle, const kdn_temporal_frame* frame, const kdn_temporal_buffers* io, void* stream) {
 	if (handle == nullptr || frame == nullptr || io == nullptr) return KDN_BAD_ARG;
@@ -138,6 +141,9 @@ extern "C" kdn_status kdn_temporal_device(kdn_ctx* handle, const kdn_temporal_fr
 	if (ctx->device < 0) return ctx->fail(KDN_NO_DEVICE, "kdn_temporal_device: a host-only context has no device");
 	if (frame->width <= 0 || frame->height <= 0 || int64_t(frame->width) * int64_t(frame->height) > (int64_t(1) << 26))
 		return ctx->fail(KDN_BAD_ARG, "kdn_temporal_device: frame size out of range");
+	if (frame->factor > 4 || frame->before_factor > 4 || frame->phase >= std::max(frame->factor, 1u) * std::max(frame->factor, 1u) ||
+	    frame->before_phase >= std::max(frame->before_factor, 1u) * std::max(frame->before_factor, 1u))
+		return ctx->fail(KDN_BAD_ARG, "kdn_temporal_device: a film factor of 1 to 4 and a phase below its square are needed");
 	const bool reads = frame->kept != 0;
 	if (!io->light || !io->first_distance || !io->first_normal || !io->first_albedo || !io->first_leaf || !io->centre_distance || !io->centre_normal ||
 	    !io->centre_albedo || !io->centre_leaf || !io->colour || !io->moment || !io->length ||
@@ -152,7 +158,70 @@ extern "C" kdn_status kdn_temporal_device(kdn_ctx* handle, const kdn_temporal_fr
 	a.kept      = frame->kept;
 	a.now       = kdn::temporalCameraOf(frame->now, frame->width, frame->height);
 	a.before    = kdn::temporalCameraOf(frame->before, frame->width, frame->height);
+	kdn::filmCentreOf(frame->factor, frame->phase, a.centre);
+	kdn::filmCentreOf(frame->before_factor, frame->before_phase, a.centreBefore);
 	a.io        = *io;
 	if (!ctx->check(kdn::launchTemporal(a, stream ? static_cast<cudaStream_t>(stream) : ctx->stream), "temporal kernel")) return KDN_CUDA_ERROR;
 	return KDN_OK;
+}
+
+namespace kdn {
+
+kdn_status upscaleOnDevice(Context* ctx, UpscaleScratch& scratch, const kdn_upscale_frame* frame, const kdn_upscale_buffers* io, cudaStream_t stream) {
+	const int factor = int(frame->factor);
+	const int dw = frame->width / factor, dh = frame->height / factor;
+	kdn_status s;
+	if ((s = ctx->ensure(scratch.samples, size_t(dw) * size_t(dh) * sizeof(float4))) != KDN_OK) return s;
+	if (scratch.factor != frame->factor || scratch.width != frame->width || scratch.height != frame->height) {
+		// upscale.cpp:568 upscaleAxis of every place of the factor, on the host
+		std::vector<UpscaleAxis> axes(size_t(factor) * size_t(frame->width + frame->height));
+		for (int place = 0; place < factor; ++place) {
+			upscaleAxes(factor, place, dw, frame->width, axes.data() + size_t(place) * size_t(frame->width));
+			upscaleAxes(factor, place, dh, frame->height, axes.data() + size_t(factor) * size_t(frame->width) + size_t(place) * size_t(frame->height));
+		}
+		scratch.factor = 0;
+		if ((s = ctx->ensure(scratch.axes, axes.size() * sizeof(UpscaleAxis))) != KDN_OK) return s;
+		if (!ctx->check(cudaMemcpyAsync(scratch.axes.ptr, axes.data(), axes.size() * sizeof(UpscaleAxis), cudaMemcpyHostToDevice, stream), "upscale axes")) return KDN_CUDA_ERROR;
+		if (!ctx->check(cudaStreamSynchronize(stream), "upscale axes")) return KDN_CUDA_ERROR;
+		scratch.factor = frame->factor;
+		scratch.width  = frame->width;
+		scratch.height = frame->height;
+	}
+	const UpscaleAxis* axes = static_cast<const UpscaleAxis*>(scratch.axes.ptr);
+	UpscaleArgs a {};
+	a.width       = frame->width;
+	a.height      = frame->height;
+	a.drawnWidth  = dw;
+	a.drawnHeight = dh;
+	a.kept        = frame->kept;
+	a.settling    = frame->settling;
+	std::memcpy(a.now, frame->now, sizeof a.now);
+	std::memcpy(a.before, frame->before, sizeof a.before);
+	a.internal     = io->internal;
+	a.distance     = io->distance;
+	a.columns      = axes + size_t(frame->phase % frame->factor) * size_t(frame->width);
+	a.rows         = axes + size_t(factor) * size_t(frame->width) + size_t(frame->phase / frame->factor) * size_t(frame->height);
+	a.before_state = reinterpret_cast<const float4*>(io->before);
+	a.after_state  = reinterpret_cast<float4*>(io->after);
+	a.image        = io->image;
+	a.samples      = static_cast<float4*>(scratch.samples.ptr);
+	if (!ctx->check(launchUpscale(a, stream, ctx->smCount), "upscale kernels")) return KDN_CUDA_ERROR;
+	return KDN_OK;
+}
+
+} // namespace kdn
+
+extern "C" kdn_status kdn_upscale_device(kdn_ctx* handle, const kdn_upscale_frame* frame, const kdn_upscale_buffers* io, void* stream) {
+	if (handle == nullptr || frame == nullptr || io == nullptr) return KDN_BAD_ARG;
+	Context* ctx = reinterpret_cast<Context*>(handle);
+	std::lock_guard<std::mutex> guard(ctx->lock);
+	if (ctx->device < 0) return ctx->fail(KDN_NO_DEVICE, "kdn_upscale_device: a host-only context has no device");
+	if (frame->factor < 2 || frame->factor > 4) return ctx->fail(KDN_BAD_ARG, "kdn_upscale_device: the film factor must be 2, 3 or 4");
+	if (frame->phase >= frame->factor * frame->factor) return ctx->fail(KDN_BAD_ARG, "kdn_upscale_device: the phase must be below the factor's square");
+	if (frame->width <= 0 || frame->height <= 0 || frame->width % int32_t(frame->factor) != 0 || frame->height % int32_t(frame->factor) != 0 ||
+	    int64_t(frame->width) * int64_t(frame->height) > (int64_t(1) << 26))
+		return ctx->fail(KDN_BAD_ARG, "kdn_upscale_device: the shown size must be positive, a multiple of the factor and at most 2^26 pixels");
+	if (!io->internal || !io->after || !io->image || (frame->kept && !io->before)) return ctx->fail(KDN_BAD_ARG, "kdn_upscale_device: a buffer is missing");
+	if (!ctx->check(cudaSetDevice(ctx->device), "cudaSetDevice")) return KDN_CUDA_ERROR;
+	return kdn::upscaleOnDevice(ctx, ctx->upscale, frame, io, stream ? static_cast<cudaStream_t>(stream) : ctx->stream);
 }

@@ -103,6 +103,12 @@ struct FrameConstants {
 	uint32_t materialCount;
 	uint32_t absorbs; // absorption.cpp:18 sceneAbsorbs: some glass absorbs
 	uint32_t films;   // some metal, plastic or glass wears a thin film
+	// core/camera.h:65 FilmPlan: a drawn pixel's samples aim at the shown
+	// pixel (x * factor + phase % factor, y * factor + phase / factor); its
+	// G-buffer ray passes through that pixel's centre (core/camera.cpp:51
+	// filmCentre, in drawn pixels)
+	uint32_t factor, phase;
+	float centre[2];
 	float zenith[3], horizon[3], ground[3];
 	DeviceLamp lamps[kMaxLamps];
 	SpectralTables spectral;

@@ -38,6 +38,10 @@ struct FrameState {
 	DeviceBuffer frameLight, firstDistance, firstNormal, firstAlbedo, firstLeaf;
 	DeviceBuffer gDistance[2], gNormal[2], gAlbedo[2], gLeaf[2];
 	DeviceBuffer tColour[2], tMoment[2], tLength[2];
+	// at a film factor above 1: the drawn frame the a-trous filter leaves,
+	// and the upscale member's state twice (colour and depth a shown pixel)
+	DeviceBuffer internal, upState[2];
+	UpscaleScratch upscale;
 	DeviceBuffer guideLobes, guideRecords; // the learned guide's, a lane's capacity each
 	uint32_t capacity = 0;
 	int32_t width = 0, height = 0;
@@ -46,6 +50,13 @@ struct FrameState {
 	int shown      = -1;    // which of them the last denoised frame wrote; -1: none
 	double lens[14] = {};   // the last denoised frame's lens
 	int32_t stateWidth = 0, stateHeight = 0;
+	uint32_t stateFactor = 1, statePhase = 0; // the film the temporal state was drawn at
+	// the upscale state: which of upState the last frame wrote (-1: none),
+	// its shown size, and upscale.cpp's moved flag and settling count
+	int upShown = -1;
+	int32_t upWidth = 0, upHeight = 0;
+	bool upMoved = false;
+	int upSettling = 0;
 	bool last_denoised = false; // the last frame drawn was a denoised one
 	bool surfaced() const { return last_denoised && shown >= 0; }
 	std::vector<cudaEvent_t> events;
@@ -60,7 +71,7 @@ struct FrameState {
 void Context::releaseFrame() {
 	if (frame == nullptr) return;
 	FrameState& f = *frame;
-	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.queueCarry[0], &f.queueCarry[1], &f.hits, &f.states, &f.counts, &f.shadowPaths[0], &f.shadowPaths[1], &f.shadowContribution[0], &f.shadowContribution[1], &f.surfacePaths, &f.surfaceRays, &f.surfaceStates, &f.surfaceHits, &f.sums, &f.out, &f.materials, &f.patternSteps, &f.stops, &f.placements, &f.boundaries, &f.frameLight, &f.firstDistance, &f.firstNormal, &f.firstAlbedo, &f.firstLeaf, &f.gDistance[0], &f.gDistance[1], &f.gNormal[0], &f.gNormal[1], &f.gAlbedo[0], &f.gAlbedo[1], &f.gLeaf[0], &f.gLeaf[1], &f.tColour[0], &f.tColour[1], &f.tMoment[0], &f.tMoment[1], &f.tLength[0], &f.tLength[1], &f.guideLobes, &f.guideRecords }) {
+	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.queueCarry[0], &f.queueCarry[1], &f.hits, &f.states, &f.counts, &f.shadowPaths[0], &f.shadowPaths[1], &f.shadowContribution[0], &f.shadowContribution[1], &f.surfacePaths, &f.surfaceRays, &f.surfaceStates, &f.surfaceHits, &f.sums, &f.out, &f.materials, &f.patternSteps, &f.stops, &f.placements, &f.boundaries, &f.frameLight, &f.firstDistance, &f.firstNormal, &f.firstAlbedo, &f.firstLeaf, &f.gDistance[0], &f.gDistance[1], &f.gNormal[0], &f.gNormal[1], &f.gAlbedo[0], &f.gAlbedo[1], &f.gLeaf[0], &f.gLeaf[1], &f.tColour[0], &f.tColour[1], &f.tMoment[0], &f.tMoment[1], &f.tLength[0], &f.tLength[1], &f.internal, &f.upState[0], &f.upState[1], &f.upscale.samples, &f.upscale.axes, &f.guideLobes, &f.guideRecords }) {
 		if (b->ptr) cudaFree(b->ptr);
 		b->ptr   = nullptr;
 		b->bytes = 0;
@@ -321,6 +332,15 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	if (fr->width <= 0 || fr->height <= 0 || fr->samples <= 0 || fr->surfaces <= 0 || fr->surfaces > 255) return ctx->fail(KDN_BAD_ARG, "kdn_render: width, height, samples and surfaces (1..255) must be positive");
 	if (uint64_t(fr->width) * uint64_t(fr->height) > (uint64_t(1) << 26)) return ctx->fail(KDN_BAD_ARG, "kdn_render: frame larger than 2^26 pixels");
 	if (fr->samples > (1 << 20)) return ctx->fail(KDN_BAD_ARG, "kdn_render: more than 2^20 samples a pixel in one call (accumulate over calls)");
+	// core/camera.h:65 FilmPlan: the frame is drawn at 1/factor of its size
+	const uint32_t factor = fr->factor > 1 ? fr->factor : 1u;
+	if (factor > 4) return ctx->fail(KDN_BAD_ARG, "kdn_render: the film factor must be 1 to 4");
+	if (factor > 1) {
+		if (!(fr->flags & KDN_FRAME_DENOISE)) return ctx->fail(KDN_BAD_ARG, "kdn_render: a film factor above 1 needs the reconstruction chain (KDN_FRAME_DENOISE)");
+		if (fr->width % int32_t(factor) != 0 || fr->height % int32_t(factor) != 0) return ctx->fail(KDN_BAD_ARG, "kdn_render: the size must be a multiple of the film factor");
+		if (fr->phase >= factor * factor) return ctx->fail(KDN_BAD_ARG, "kdn_render: the phase must be below the film factor's square");
+	}
+	const int32_t drawnWidth = fr->width / int32_t(factor), drawnHeight = fr->height / int32_t(factor);
 	if (!ctx->has("shot.camera") || !ctx->has("looks.materials")) return ctx->fail(KDN_NOT_READY, "kdn_render: the shot.camera and looks.materials blocks are needed");
 	if (!ctx->check(cudaSetDevice(ctx->device), "cudaSetDevice")) return KDN_CUDA_ERROR;
 	const kdn_camera cam                     = ctx->block<kdn_camera>("shot.camera")[0];
@@ -335,8 +355,9 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		const char* why = unsupported(mats[k], finishes[k]);
 		if (why) return ctx->fail(KDN_BAD_ARG, "kdn_render: material " + std::to_string(k) + " is " + why + ", which this build does not draw");
 	}
-	const uint32_t pixels = uint32_t(fr->width) * uint32_t(fr->height);
-	const uint32_t spp    = uint32_t(fr->samples);
+	const uint32_t pixels      = uint32_t(drawnWidth) * uint32_t(drawnHeight); // drawn
+	const uint32_t shownPixels = uint32_t(fr->width) * uint32_t(fr->height);
+	const uint32_t spp         = uint32_t(fr->samples);
 	// a chunk a lane: the frame's paths halved where they fit, else as many as
 	// the lanes' share of the room holds
 	const uint64_t want        = chunkPaths(ctx, uint64_t(pixels) * spp) / kLanes;
@@ -351,7 +372,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	if (guiding && (s = ctx->ensure(f.guideLobes, size_t(f.capacity) * kLanes * kGuideLobeFloats * sizeof(float))) != KDN_OK) return s;
 	if (training && (s = ctx->ensure(f.guideRecords, size_t(f.capacity) * kLanes * kGuideDepth * sizeof(GuideRecord))) != KDN_OK) return s;
 	// pixel sums: fresh unless accumulating onto a frame of the same size
-	const bool fresh = !fr->accumulate || f.width != fr->width || f.height != fr->height || f.sums.ptr == nullptr;
+	const bool fresh = !fr->accumulate || f.width != drawnWidth || f.height != drawnHeight || f.sums.ptr == nullptr;
 	if ((s = ctx->ensure(f.sums, size_t(pixels) * 3 * sizeof(double))) != KDN_OK) return s;
 	const bool denoised = (fr->flags & KDN_FRAME_DENOISE) != 0;
 	if (denoised) {
@@ -367,14 +388,20 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		for (const auto& w : wants) {
 			if ((s = ctx->ensure(*w.b, w.bytes)) != KDN_OK) return s;
 		}
+		if (factor > 1) {
+			for (DeviceBuffer* b : { &f.upState[0], &f.upState[1] }) {
+				if ((s = ctx->ensure(*b, size_t(shownPixels) * 16)) != KDN_OK) return s;
+			}
+			if ((s = ctx->ensure(f.internal, px * 12)) != KDN_OK) return s;
+		}
 	}
 	if (fresh) {
 		if (!ctx->check(cudaMemsetAsync(f.sums.ptr, 0, size_t(pixels) * 3 * sizeof(double), stream), "clear sums")) return KDN_CUDA_ERROR;
 		f.taken = 0;
 	}
 	const int cur = f.current; // the G-buffer and state pair this frame writes
-	f.width  = fr->width;
-	f.height = fr->height;
+	f.width  = drawnWidth;
+	f.height = drawnHeight;
 	// constants
 	FrameConstants c {};
 	const V3 eye = v3(cam.eye), target = v3(cam.target), up = v3(cam.up);
@@ -385,9 +412,12 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	put(c.right, right);
 	put(c.up, cross(right, forward));
 	c.reach         = float(std::tan(cam.fov / 2));
-	c.aspect        = float(double(fr->width) / double(fr->height));
-	c.width         = fr->width;
-	c.height        = fr->height;
+	c.aspect        = float(double(drawnWidth) / double(drawnHeight));
+	c.width         = drawnWidth;
+	c.height        = drawnHeight;
+	c.factor        = factor;
+	c.phase         = factor > 1 ? fr->phase : 0u;
+	filmCentreOf(factor, c.phase, c.centre);
 	c.seedMix       = mixedBits(uint64_t(int64_t(fr->seed)));
 	c.surfaces      = fr->surfaces;
 	c.spp           = spp;
@@ -706,11 +736,14 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	if (training && (s = guideTrainGathered(ctx->guide, stream)) != KDN_OK) return ctx->fail(s, std::string("kdn_render: guide training: ") + kdn_guide_last_error());
 	f.taken += double(spp);
 	f.last_denoised = denoised;
-	if (!denoised) f.shown = -1; // a frame without the shown chain drops the temporal history
+	if (!denoised) { // a frame without the shown chain drops the temporal and upscale histories
+		f.shown   = -1;
+		f.upShown = -1;
+	}
 
 	float* image = out;
 	if (hostOut) {
-		if ((s = ctx->ensure(f.out, size_t(pixels) * 3 * sizeof(float))) != KDN_OK) return s;
+		if ((s = ctx->ensure(f.out, size_t(shownPixels) * 3 * sizeof(float))) != KDN_OK) return s;
 		image = static_cast<float*>(f.out.ptr);
 	}
 	if (!denoised) {
@@ -732,18 +765,23 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 			lens[3 * k + 2] = parts[k]->z;
 		}
 		lens[12]        = std::tan(cam.fov / 2);
-		lens[13]        = double(fr->width) / double(fr->height);
+		lens[13]        = double(drawnWidth) / double(drawnHeight);
 		const int prev  = 1 - cur;
-		const bool kept = f.shown == prev && f.stateWidth == fr->width && f.stateHeight == fr->height && !(fr->flags & KDN_FRAME_RESTART);
+		const bool restarted = (fr->flags & KDN_FRAME_RESTART) != 0;
+		const bool kept = f.shown == prev && f.stateWidth == drawnWidth && f.stateHeight == drawnHeight && !restarted;
 		const bool moved = kept && std::memcmp(lens, f.lens, sizeof lens) != 0;
 		TemporalArgs ta {};
-		ta.width                  = fr->width;
-		ta.height                 = fr->height;
+		ta.width                  = drawnWidth;
+		ta.height                 = drawnHeight;
 		ta.moved                  = moved ? 1u : 0u;
 		ta.recounted              = 0;
 		ta.kept                   = kept ? 1u : 0u;
-		ta.now                    = temporalCameraOf(lens, fr->width, fr->height);
-		ta.before                 = temporalCameraOf(kept ? f.lens : lens, fr->width, fr->height);
+		ta.now                    = temporalCameraOf(lens, drawnWidth, drawnHeight);
+		ta.before                 = temporalCameraOf(kept ? f.lens : lens, drawnWidth, drawnHeight);
+		// temporal.cpp:187 temporalCentre: the grid read through the film each was drawn at
+		filmCentreOf(factor, c.phase, ta.centre);
+		if (kept) filmCentreOf(f.stateFactor, f.statePhase, ta.centreBefore);
+		else filmCentreOf(factor, c.phase, ta.centreBefore);
 		ta.io.light               = static_cast<const float*>(f.frameLight.ptr);
 		ta.io.first_distance      = static_cast<const uint16_t*>(f.firstDistance.ptr);
 		ta.io.first_normal        = static_cast<const uint16_t*>(f.firstNormal.ptr);
@@ -765,8 +803,8 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		ta.io.image               = nullptr;
 		if (!ctx->check(launchTemporal(ta, stream), "temporal kernel")) return KDN_CUDA_ERROR;
 		kdn_denoise_frame df {};
-		df.width  = fr->width;
-		df.height = fr->height;
+		df.width  = drawnWidth;
+		df.height = drawnHeight;
 		for (int k = 0; k < 3; ++k) {
 			df.eye[k]     = lens[k];
 			df.forward[k] = lens[3 + k];
@@ -776,18 +814,56 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		df.reach       = lens[12];
 		df.aspect      = lens[13];
 		df.demodulated = 1;
+		float* drawnImage = factor > 1 ? static_cast<float*>(f.internal.ptr) : image;
 		if ((s = denoiseOnDevice(ctx, &df, ta.io.colour, ta.io.moment, ta.io.length, ta.io.centre_distance, ta.io.centre_normal, ta.io.centre_albedo,
-		                         ta.io.centre_leaf, image, stream)) != KDN_OK)
+		                         ta.io.centre_leaf, drawnImage, stream)) != KDN_OK)
 			return s;
 		launches += 8;
+		if (factor > 1) {
+			// plugins/reconstruction/upscale/upscale.cpp upscaledFrame: the
+			// denoised drawn frame to the shown size, its history kept where
+			// the last frame was upscaled to this size and the sequence goes on;
+			// :557 settlingFrames counts the still frames after a movement
+			const int upPrev     = f.upShown;
+			const bool upKept    = upPrev >= 0 && f.upWidth == fr->width && f.upHeight == fr->height && !restarted;
+			const bool lensMoved = f.upShown >= 0 && std::memcmp(lens, f.lens, sizeof lens) != 0;
+			const int settling   = upKept ? (lensMoved ? 0 : (f.upMoved ? 4 : f.upSettling)) : 0;
+			kdn_upscale_frame uf {};
+			uf.width    = fr->width;
+			uf.height   = fr->height;
+			uf.factor   = factor;
+			uf.phase    = c.phase;
+			uf.kept     = upKept ? 1u : 0u;
+			uf.settling = settling > 0 ? 1u : 0u;
+			std::memcpy(uf.now, lens, sizeof lens);
+			std::memcpy(uf.before, f.upShown >= 0 ? f.lens : lens, sizeof lens);
+			const int upCur = upPrev >= 0 ? 1 - upPrev : 0;
+			kdn_upscale_buffers ub {};
+			ub.internal = drawnImage;
+			ub.distance = ta.io.centre_distance;
+			ub.before   = upKept ? static_cast<const float*>(f.upState[upPrev].ptr) : nullptr;
+			ub.after    = static_cast<float*>(f.upState[upCur].ptr);
+			ub.image    = image;
+			if ((s = upscaleOnDevice(ctx, f.upscale, &uf, &ub, stream)) != KDN_OK) return s;
+			launches += 2;
+			f.upShown    = upCur;
+			f.upWidth    = fr->width;
+			f.upHeight   = fr->height;
+			f.upMoved    = lensMoved;
+			f.upSettling = std::max(settling - 1, 0);
+		} else {
+			f.upShown = -1;
+		}
 		std::memcpy(f.lens, lens, sizeof lens);
-		f.stateWidth  = fr->width;
-		f.stateHeight = fr->height;
+		f.stateWidth  = drawnWidth;
+		f.stateHeight = drawnHeight;
+		f.stateFactor = factor;
+		f.statePhase  = c.phase;
 		f.shown       = cur;
 		f.current     = prev;
 	}
 	if (!ctx->check(cudaEventRecord(f.events[1], stream), "event")) return KDN_CUDA_ERROR;
-	if (hostOut && !ctx->check(cudaMemcpyAsync(out, image, size_t(pixels) * 3 * sizeof(float), cudaMemcpyDeviceToHost, stream), "copy frame")) return KDN_CUDA_ERROR;
+	if (hostOut && !ctx->check(cudaMemcpyAsync(out, image, size_t(shownPixels) * 3 * sizeof(float), cudaMemcpyDeviceToHost, stream), "copy frame")) return KDN_CUDA_ERROR;
 	if (!ctx->check(cudaStreamSynchronize(stream), "kdn_render")) return KDN_CUDA_ERROR;
 	kdn_frame_stats st {};
 	float ms = 0;

@@ -1,6 +1,10 @@
-// The temporal member on the device, one thread a pixel, in FP32
-// (plugins/reconstruction/temporal/temporal.cpp, at a film factor of 1 with
-// a G-buffer).  Per pixel:
+// The temporal member on the device, one thread a pixel: the geometry
+// (headings, planes, where a point was seen before, the bilinear weights)
+// in double as the reference computes it, the light in FP32
+// (plugins/reconstruction/temporal/temporal.cpp, with a G-buffer, on the
+// drawn grid: at a film factor above 1 a grid pixel's rays pass through the
+// centre of the shown pixel its phase aims at, core/camera.cpp:51
+// filmCentre, this frame's and the state before's).  Per pixel:
 //   - the 3x3 neighbourhood of this frame's demodulated light (:903
 //     neighbourhoodOf): mean, deviation;
 //   - whether the pixel's sample met the G-buffer's surface (:244
@@ -26,7 +30,8 @@ namespace {
 
 constexpr float kMovingCap = 32.0f, kStillCap = 256.0f, kYoungLength = 8.0f;
 constexpr float kMovingSpread = 1.25f, kStillSpread = 6.0f;
-constexpr float kDepthShare = 0.03f, kNormalCosine = 0.9f, kAlbedoFloor = 1e-3f;
+constexpr double kDepthShare = 0.03, kNormalCosine = 0.9;
+constexpr float kAlbedoFloor = 1e-3f;
 constexpr uint32_t kSky = 0xFFFFFFFFu;
 
 struct V {
@@ -36,34 +41,45 @@ __device__ __forceinline__ V v3(const float* a) { return { a[0], a[1], a[2] }; }
 __device__ __forceinline__ V operator+(V a, V b) { return { a.x + b.x, a.y + b.y, a.z + b.z }; }
 __device__ __forceinline__ V operator-(V a, V b) { return { a.x - b.x, a.y - b.y, a.z - b.z }; }
 __device__ __forceinline__ V operator*(V a, float s) { return { a.x * s, a.y * s, a.z * s }; }
-__device__ __forceinline__ float dotV(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+// the geometry's vectors, in double
+struct D {
+	double x, y, z;
+};
+__device__ __forceinline__ D d3(const double* a) { return { a[0], a[1], a[2] }; }
+__device__ __forceinline__ D operator+(D a, D b) { return { a.x + b.x, a.y + b.y, a.z + b.z }; }
+__device__ __forceinline__ D operator-(D a, D b) { return { a.x - b.x, a.y - b.y, a.z - b.z }; }
+__device__ __forceinline__ D operator*(D a, double s) { return { a.x * s, a.y * s, a.z * s }; }
+__device__ __forceinline__ double dotD(D a, D b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 
 __device__ __forceinline__ float half(const uint16_t* p, size_t i) { return __half2float(__ushort_as_half(p[i])); }
 
 struct Surf {
 	float distance;
-	V normal;
+	D normal;
 	uint32_t leaf;
 };
 
 __device__ __forceinline__ Surf surfAt(const uint16_t* distance, const uint16_t* normal, const uint32_t* leaf, size_t k) {
-	return { half(distance, k), { half(normal, 3 * k), half(normal, 3 * k + 1), half(normal, 3 * k + 2) }, leaf[k] };
+	return { half(distance, k), { double(half(normal, 3 * k)), double(half(normal, 3 * k + 1)), double(half(normal, 3 * k + 2)) }, leaf[k] };
 }
 
 __device__ __forceinline__ bool skyOf(const Surf& s) { return s.leaf == kSky || !isfinite(s.distance); }
 
 struct Plane {
 	uint32_t leaf;
-	V point, normal;
-	float reach;
+	D point, normal;
+	double reach;
 };
 
-__device__ __forceinline__ V filmHeading(const TemporalCamera& c, float x, float y) { return v3(c.corner) + v3(c.across) * x + v3(c.down) * y; }
+// :324 filmHeading
+__device__ __forceinline__ D filmHeading(const TemporalCamera& c, double x, double y) { return d3(c.corner) + d3(c.across) * x + d3(c.down) * y; }
 
-// :358 planeThrough
-__device__ __forceinline__ Plane planeThrough(const Surf& s, V eye, V heading, float reach) {
-	if (skyOf(s)) return { kSky, { 0, 0, 0 }, { 0, 0, 0 }, 0.0f };
-	return { s.leaf, eye + heading * (s.distance / sqrtf(dotV(heading, heading))), s.normal, reach * s.distance };
+// :358 planeThrough over :345 surfacePointAlong
+__device__ __forceinline__ Plane planeThrough(const Surf& s, D eye, D heading, double share) {
+	if (skyOf(s)) return { kSky, { 0, 0, 0 }, { 0, 0, 0 }, 0.0 };
+	const double distance = double(s.distance);
+	return { s.leaf, eye + heading * (distance / sqrt(dotD(heading, heading))), s.normal, share * distance };
 }
 
 __device__ __forceinline__ bool sameLeaf(uint32_t a, uint32_t b, bool recounted) { return recounted ? ((a == kSky) == (b == kSky)) : a == b; }
@@ -72,8 +88,8 @@ __device__ __forceinline__ bool sameLeaf(uint32_t a, uint32_t b, bool recounted)
 __device__ __forceinline__ bool onPlane(const Plane& p, const Plane& other, bool recounted) {
 	if (!sameLeaf(other.leaf, p.leaf, recounted)) return false;
 	if (p.leaf == kSky) return true;
-	if (dotV(other.normal, p.normal) < kNormalCosine) return false;
-	return fabsf(dotV(other.point - p.point, p.normal)) <= p.reach;
+	if (dotD(other.normal, p.normal) < kNormalCosine) return false;
+	return fabs(dotD(other.point - p.point, p.normal)) <= p.reach;
 }
 
 __device__ __forceinline__ float divisorOf(float albedo) { return albedo < kAlbedoFloor ? 1.0f : albedo; }
@@ -95,7 +111,7 @@ __device__ __forceinline__ size_t clampedPixel(int x, int y, int w, int h) {
 __device__ __forceinline__ bool sampleOnPlane(const TemporalArgs& a, const Plane& p, size_t k) {
 	const int x = int(k % size_t(a.width)), y = int(k / size_t(a.width));
 	const Surf s = surfAt(a.io.first_distance, a.io.first_normal, a.io.first_leaf, k);
-	return onPlane(p, planeThrough(s, v3(a.now.eye), filmHeading(a.now, float(x) + 0.5f, float(y) + 0.5f), kDepthShare), false);
+	return onPlane(p, planeThrough(s, d3(a.now.eye), filmHeading(a.now, double(x) + double(a.centre[0]), double(y) + double(a.centre[1])), kDepthShare), false);
 }
 
 __global__ void temporalKernel(TemporalArgs a) {
@@ -118,8 +134,8 @@ __global__ void temporalKernel(TemporalArgs a) {
 		const Surf first  = surfAt(io.first_distance, io.first_normal, io.first_leaf, k);
 		const Surf centre = surfAt(io.centre_distance, io.centre_normal, io.centre_leaf, k);
 		const bool aimed  = (skyOf(first) ? kSky : first.leaf) == (skyOf(centre) ? kSky : centre.leaf);
-		const V heading   = filmHeading(a.now, float(x) + 0.5f, float(y) + 0.5f);
-		const Plane plane = planeThrough(centre, v3(a.now.eye), heading, kDepthShare);
+		const D heading   = filmHeading(a.now, double(x) + double(a.centre[0]), double(y) + double(a.centre[1]));
+		const Plane plane = planeThrough(centre, d3(a.now.eye), heading, kDepthShare);
 		// the history
 		bool found = false;
 		V history  = { 0, 0, 0 };
@@ -134,40 +150,45 @@ __global__ void temporalKernel(TemporalArgs a) {
 					historyLength = length;
 				}
 			} else {
-				const V along     = plane.leaf == kSky ? heading : plane.point - v3(a.before.eye);
-				const float ahead = dotV(along, v3(a.before.forward));
-				if (ahead > 0.0f) {
-					const float scale = 1.0f / ahead;
-					const float px    = dotV(along, v3(a.before.acrossInverse)) * scale + 0.5f * a.before.width;
-					const float py    = dotV(along, v3(a.before.downInverse)) * scale + 0.5f * a.before.height;
-					if (px >= 0.0f && px < a.before.width && py >= 0.0f && py < a.before.height) {
-						const float ax = px - 0.5f, ay = py - 0.5f;
-						const int lx = int(floorf(ax)), ly = int(floorf(ay));
-						const float tx = ax - float(lx), ty = ay - float(ly);
-						V colour = { 0, 0, 0 };
-						float moment = 0.0f, length = 0.0f, weight = 0.0f;
+				// :584 surfacedHistory, :418 placeBefore, :495 fetchedHistory
+				const D along      = plane.leaf == kSky ? heading : plane.point - d3(a.before.eye);
+				const double ahead = dotD(along, d3(a.before.forward));
+				if (ahead > 0) {
+					const double scale = 1 / ahead;
+					const double px    = dotD(along, d3(a.before.acrossInverse)) * scale + 0.5 * a.before.width;
+					const double py    = dotD(along, d3(a.before.downInverse)) * scale + 0.5 * a.before.height;
+					if (px >= 0 && px < a.before.width && py >= 0 && py < a.before.height) {
+						const double ax = px - double(a.centreBefore[0]), ay = py - double(a.centreBefore[1]);
+						const int lx = int(floor(ax)), ly = int(floor(ay));
+						const double tx = ax - double(lx), ty = ay - double(ly);
+						D colour = { 0, 0, 0 };
+						double moment = 0.0, weight = 0.0;
+						float length  = 0.0f;
 						for (int j = 0; j < 2; ++j) {
 							for (int i = 0; i < 2; ++i) {
 								const int cx = lx + i, cy = ly + j;
-								const float w = (i == 0 ? 1.0f - tx : tx) * (j == 0 ? 1.0f - ty : ty);
-								if (!(w > 0.0f && cx >= 0 && cx < a.width && cy >= 0 && cy < a.height)) continue;
+								const double w = (i == 0 ? 1 - tx : tx) * (j == 0 ? 1 - ty : ty);
+								if (!(w > 0 && cx >= 0 && cx < a.width && cy >= 0 && cy < a.height)) continue;
 								const size_t c = size_t(cy) * size_t(a.width) + size_t(cx);
 								const float lastLength = io.before_length[c];
 								if (!(lastLength > 0.0f)) continue;
 								const Surf last = surfAt(io.before_distance, io.before_normal, io.before_leaf, c);
-								const Plane lastPlane = planeThrough(last, v3(a.before.eye), filmHeading(a.before, float(cx) + 0.5f, float(cy) + 0.5f), 0.0f);
+								const Plane lastPlane = planeThrough(last, d3(a.before.eye),
+								                                     filmHeading(a.before, double(cx) + double(a.centreBefore[0]), double(cy) + double(a.centreBefore[1])), 0.0);
 								if (!onPlane(plane, lastPlane, a.recounted != 0)) continue;
-								colour = colour + v3(io.before_colour + 3 * c) * w;
-								moment += io.before_moment[c] * w;
-								length += lastLength * w;
+								const float* lc = io.before_colour + 3 * c;
+								colour = colour + D { double(lc[0]), double(lc[1]), double(lc[2]) } * w;
+								moment += double(io.before_moment[c]) * w;
+								length += float(double(lastLength) * w);
 								weight += w;
 							}
 						}
-						if (weight > 0.0f) {
+						if (weight > 0) {
+							// :470 summedHistory
 							found         = true;
-							history       = colour * (1.0f / weight);
-							historyMoment = moment / weight;
-							historyLength = length / weight;
+							history       = { float(colour.x * (1 / weight)), float(colour.y * (1 / weight)), float(colour.z * (1 / weight)) };
+							historyMoment = float(moment / weight);
+							historyLength = float(double(length) / weight);
 						}
 					}
 				}
@@ -234,6 +255,12 @@ __global__ void temporalKernel(TemporalArgs a) {
 
 } // namespace
 
+void filmCentreOf(uint32_t factor, uint32_t phase, float centre[2]) {
+	const uint32_t f = factor > 1 ? factor : 1;
+	centre[0]        = float((double(f > 1 ? phase % f : 0) + 0.5) / double(f));
+	centre[1]        = float((double(f > 1 ? phase / f : 0) + 0.5) / double(f));
+}
+
 TemporalCamera temporalCameraOf(const double l[14], int width, int height) {
 	const double sideways = l[12] * l[13], reach = l[12];
 	double across[3], down[3], corner[3];
@@ -246,17 +273,18 @@ TemporalCamera temporalCameraOf(const double l[14], int width, int height) {
 		dd += down[a] * down[a];
 	}
 	TemporalCamera c {};
+	const double acrossScale = 1 / aa, downScale = 1 / dd;
 	for (int a = 0; a < 3; ++a) {
-		c.eye[a]           = float(l[a]);
-		c.forward[a]       = float(l[3 + a]);
-		c.corner[a]        = float(corner[a]);
-		c.across[a]        = float(across[a]);
-		c.down[a]          = float(down[a]);
-		c.acrossInverse[a] = float(across[a] / aa);
-		c.downInverse[a]   = float(down[a] / dd);
+		c.eye[a]           = l[a];
+		c.forward[a]       = l[3 + a];
+		c.corner[a]        = corner[a];
+		c.across[a]        = across[a];
+		c.down[a]          = down[a];
+		c.acrossInverse[a] = across[a] * acrossScale;
+		c.downInverse[a]   = down[a] * downScale;
 	}
-	c.width  = float(width);
-	c.height = float(height);
+	c.width  = double(width);
+	c.height = double(height);
 	return c;
 }
 

@@ -343,8 +343,16 @@ __global__ void __launch_bounds__(kBlock) cameraKernel(const __grid_constant__ F
 			nm[lane]            = float(fmin(value, 699.9999999999999));
 			dens[lane]          = float(1.0 / (kCuts * width));
 		}
-		const float px = float(x) + number(stream, sample, 0, PixelX);
-		const float py = float(y) + number(stream, sample, 0, PixelY);
+		// trace.cpp:105 filmDraw, :93 phasedDraw at a film factor above 1
+		float px, py;
+		if (cFrame.factor > 1) {
+			const float factor = float(cFrame.factor);
+			px = float(x) + (float(cFrame.phase % cFrame.factor) + number(stream, sample, 0, PixelX)) / factor;
+			py = float(y) + (float(cFrame.phase / cFrame.factor) + number(stream, sample, 0, PixelY)) / factor;
+		} else {
+			px = float(x) + number(stream, sample, 0, PixelX);
+			py = float(y) + number(stream, sample, 0, PixelY);
+		}
 		const float u  = 2.0f * px / float(cFrame.width) - 1.0f;
 		const float v  = 1.0f - 2.0f * py / float(cFrame.height);
 		const float3 heading = normalizedOf(f3(cFrame.forward) + f3(cFrame.right) * (u * cFrame.reach * cFrame.aspect) + f3(cFrame.up) * (v * cFrame.reach));
@@ -424,15 +432,15 @@ __device__ __forceinline__ float3 albedoAt(const kdn_hit& hit, float3 normal, co
 	return a;
 }
 
-// ---- the surfaces pass: one ray through each pixel's centre (core/surfaces.cpp:39 surfaceRay) ----
+// ---- the surfaces pass: one ray through each pixel's film centre (core/surfaces.cpp:39 surfaceRay) ----
 __global__ void __launch_bounds__(kBlock) surfaceRaysKernel(const __grid_constant__ FrameConstants cFrame, QueueBuffers Q, uint32_t firstPixel, uint32_t n) {
 	if (blockIdx.x == 0 && threadIdx.x == 0) *Q.count = n;
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 		const uint32_t pixel = firstPixel + i;
 		const uint32_t x     = pixel % uint32_t(cFrame.width);
 		const uint32_t y     = pixel / uint32_t(cFrame.width);
-		const float u        = 2.0f * (float(x) + 0.5f) / float(cFrame.width) - 1.0f;
-		const float v        = 1.0f - 2.0f * (float(y) + 0.5f) / float(cFrame.height);
+		const float u        = 2.0f * (float(x) + cFrame.centre[0]) / float(cFrame.width) - 1.0f;
+		const float v        = 1.0f - 2.0f * (float(y) + cFrame.centre[1]) / float(cFrame.height);
 		const float3 heading = normalizedOf(f3(cFrame.forward) + f3(cFrame.right) * (u * cFrame.reach * cFrame.aspect) + f3(cFrame.up) * (v * cFrame.reach));
 		Q.paths[i]           = pixel;
 		Q.rays[i]            = makeRay(f3(cFrame.eye), heading, __int_as_float(0x7f800000), kNoMaterial);

@@ -240,7 +240,8 @@ class View(ctypes.Structure):
     _fields_ = [("eye", ctypes.c_double * 3), ("target", ctypes.c_double * 3), ("up", ctypes.c_double * 3), ("fov", ctypes.c_double),
                 ("zenith", ctypes.c_double * 3), ("horizon", ctypes.c_double * 3), ("ground", ctypes.c_double * 3),
                 ("width", ctypes.c_int32), ("height", ctypes.c_int32), ("spp", ctypes.c_int32), ("surfaces", ctypes.c_int32),
-                ("seed", ctypes.c_int32), ("lamp_count", ctypes.c_uint32), ("material_count", ctypes.c_uint32)]
+                ("seed", ctypes.c_int32), ("lamp_count", ctypes.c_uint32), ("material_count", ctypes.c_uint32),
+                ("factor", ctypes.c_uint32), ("phase", ctypes.c_uint32)]
 
 
 _trees: dict = {}
@@ -254,9 +255,11 @@ def _octree_for(scene, build: dict) -> "Octree":
 
 
 def render_band(scene, width: int, height: int, spp: int, surfaces: int, seed: int, row0: int, rows: int, threads: int,
-                build: dict | None = None) -> np.ndarray:
+                build: dict | None = None, factor: int = 1, phase: int = 0) -> np.ndarray:
     """The oracle renderer over rows [row0, row0 + rows) of a frame: summed
-    RGB per pixel (rows x width x 3, divide by spp for the means)."""
+    RGB per pixel (rows x width x 3, divide by spp for the means).  With a
+    film factor above 1, width x height is the drawn frame and each pixel's
+    samples aim at the shown pixel of `phase`."""
     build = build or dict(min_depth=6, max_depth=10, split_steps=96)
     tree = _octree_for(scene, build)
     mats, keep = _materials(scene)
@@ -283,6 +286,7 @@ def render_band(scene, width: int, height: int, spp: int, surfaces: int, seed: i
     v.fov = scene.camera["fov"]
     v.width, v.height, v.spp, v.surfaces, v.seed = width, height, spp, surfaces, seed
     v.lamp_count, v.material_count = nl, n
+    v.factor, v.phase = factor, phase
     sums = np.zeros((rows, width, 3), np.float64)
     mat_leaf = np.ascontiguousarray(scene.leaf_material, np.uint32)
     L = lib()

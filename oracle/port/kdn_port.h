@@ -163,6 +163,10 @@ typedef struct kp_view {
 	double zenith[3], horizon[3], ground[3];
 	int32_t width, height, spp, surfaces, seed;
 	uint32_t lamp_count, material_count;
+	/* core/camera.h:65 FilmPlan: width x height is the drawn frame; with a
+	 * factor above 1 each pixel's samples aim at the shown pixel of the
+	 * phase (plugins/transport/paths/trace.cpp:93 phasedDraw) */
+	uint32_t factor, phase;
 } kp_view;
 
 /*

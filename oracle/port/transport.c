@@ -1012,8 +1012,11 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 	const uint64_t stream = J->seed_mix ^ kp_mixed_bits(((uint64_t) (uint32_t) x << 32) | (uint64_t) (uint32_t) y);
 	lanes w;
 	kp_sampled_wavelengths(kp_wavelength_share(kp_hashed(stream, ~(uint64_t) 0, 0), index), w.nm, w.density, w.basis);
-	const double px = x + number(stream, index, 0, PIXEL_X);
-	const double py = y + number(stream, index, 0, PIXEL_Y);
+	/* trace.cpp:105 filmDraw, :93 phasedDraw */
+	const int factor = V->factor > 1 ? (int) V->factor : 1;
+	const double column = factor > 1 ? (double) (V->phase % (uint32_t) factor) : 0, row = factor > 1 ? (double) (V->phase / (uint32_t) factor) : 0;
+	const double px = factor > 1 ? x + (column + number(stream, index, 0, PIXEL_X)) / factor : x + number(stream, index, 0, PIXEL_X);
+	const double py = factor > 1 ? y + (row + number(stream, index, 0, PIXEL_Y)) / factor : y + number(stream, index, 0, PIXEL_Y);
 	const double u = 2 * px / V->width - 1, v = 1 - 2 * py / V->height;
 	v3 heading = unit(add(add(J->forward, scl(J->right, u * J->reach * J->aspect)), scl(J->up, v * J->reach)));
 	kp_ray ray = ray_of(J->eye, heading, INFINITY, NO_MATERIAL);
