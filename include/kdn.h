@@ -206,9 +206,10 @@ typedef struct kdn_frame {
 	 * samples aimed at the shown pixel (x * factor + phase % factor,
 	 * y * factor + phase / factor) (plugins/transport/paths/trace.cpp:93
 	 * phasedDraw), and shown at width x height through the reconstruction
-	 * chain temporal + a-trous + upscale: KDN_FRAME_DENOISE is needed and
-	 * the size must be a multiple of the factor.  The pixel sums, the record
-	 * and the G-buffer are at the drawn size. */
+	 * chain temporal + a-trous + upscale (KDN_FRAME_DENOISE), or a chain
+	 * ending in upsample (KDN_FRAME_UPSAMPLE); the size must be a multiple
+	 * of the factor.  The pixel sums, the record and the G-buffer are at the
+	 * drawn size. */
 	uint32_t factor;
 	uint32_t phase; /* 0 .. factor^2 - 1: core/shown.cpp bayerFilm gives the order */
 } kdn_frame;
@@ -228,6 +229,13 @@ typedef struct kdn_frame {
 /* With KDN_FRAME_DENOISE: start the temporal history over (the sequence's
  * cut: every member drops its history). */
 #define KDN_FRAME_RESTART 2u
+/* With KDN_FRAME_DENOISE: the chain stops after the temporal member (the
+ * reference's --reconstruction temporal): no a-trous filter. */
+#define KDN_FRAME_TEMPORAL 4u
+/* At a film factor above 1: the chain's last member is upsample (bilinear,
+ * no history) instead of upscale; without KDN_FRAME_DENOISE the chain is
+ * mean + upsample (the drawn frame's pixel means blown up). */
+#define KDN_FRAME_UPSAMPLE 8u
 
 /* Device times of the last kdn_render, from CUDA events on the context's stream. */
 typedef struct kdn_frame_stats {
@@ -507,6 +515,13 @@ typedef struct kdn_upscale_buffers {
 } kdn_upscale_buffers;
 
 kdn_status kdn_upscale_device(kdn_ctx* ctx, const kdn_upscale_frame* frame, const kdn_upscale_buffers* buffers, void* stream);
+
+/* The upsample member (plugins/reconstruction/upsample/upsample.cpp
+ * upsampledImage): the drawn frame (device RGB float, width / factor x
+ * height / factor) bilinearly to width x height (device RGB float), the
+ * taps clamped to the drawn frame; its answers are the reference's to the
+ * bit.  factor 1 to 4; the size a multiple of it. */
+kdn_status kdn_upsample_device(kdn_ctx* ctx, int32_t width, int32_t height, uint32_t factor, const float* drawn, float* shown, void* stream);
 
 /* Write a buffer larger than the L2 cache on the context's stream, so that
  * the next launch starts with a cold cache. */

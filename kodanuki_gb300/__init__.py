@@ -69,6 +69,8 @@ BAYER = {1: [0], 2: [0, 3, 1, 2], 3: [0, 7, 5, 2, 6, 4, 3, 1, 8], 4: [0, 10, 2, 
 
 FRAME_DENOISE = 1  # include/kdn.h KDN_FRAME_DENOISE
 FRAME_RESTART = 2  # include/kdn.h KDN_FRAME_RESTART
+FRAME_TEMPORAL = 4  # include/kdn.h KDN_FRAME_TEMPORAL
+FRAME_UPSAMPLE = 8  # include/kdn.h KDN_FRAME_UPSAMPLE
 
 
 class FrameStats(ctypes.Structure):
@@ -93,7 +95,7 @@ EXPORTS = [
     "kdn_serve_latency", "kdn_serve_last_error", "kdn_serve_close", "kdn_serve_cancel_queued", "kdn_set_sm_limit", "kdn_serve_reset_latency",
     "kdn_guide_open", "kdn_guide_close", "kdn_guide_last_error", "kdn_guide_sizes", "kdn_guide_get_params", "kdn_guide_set_params",
     "kdn_guide_gradients", "kdn_guide_train", "kdn_guide_query", "kdn_guide_clear_samples", "kdn_guide_ready", "kdn_set_guide",
-    "kdn_guide_select", "kdn_set_march_budget", "kdn_upscale_device",
+    "kdn_guide_select", "kdn_set_march_budget", "kdn_upscale_device", "kdn_upsample_device",
 ]
 
 REQUEST_INTERACTIVE = 4
@@ -182,6 +184,7 @@ def library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.kdn_world_locate.argtypes = [P, P, ctypes.c_uint32, P, P]
     L.kdn_temporal_device.argtypes = [P, ctypes.POINTER(TemporalFrame), ctypes.POINTER(TemporalBuffers), P]
     L.kdn_upscale_device.argtypes = [P, ctypes.POINTER(UpscaleFrame), ctypes.POINTER(UpscaleBuffers), P]
+    L.kdn_upsample_device.argtypes = [P, ctypes.c_int32, ctypes.c_int32, ctypes.c_uint32, P, P, P]
     L.kdn_denoise.argtypes = [P, ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P]
     L.kdn_denoise_device.argtypes = [P, ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P, P]
     L.kdn_denoise_static.argtypes = [ctypes.POINTER(DenoiseFrame), P, P, P, P, P, P, P, P, P]
@@ -403,16 +406,19 @@ class Backend:
 
     def render(self, width: int, height: int, samples: int, surfaces: int | None = None, seed: int | None = None,
                first: int = 0, accumulate: bool = False, denoise: bool = False, restart: bool = False, factor: int = 1,
-               phase: int = 0) -> np.ndarray:
+               phase: int = 0, temporal_only: bool = False, upsample: bool = False) -> np.ndarray:
         """Draw `samples` samples a pixel and return the pixel means
         (linear RGB, float32, height x width x 3), or with `denoise` the
-        means through the reconstruction chain (temporal + a-trous, and at a
-        film `factor` of 2 to 4 the upscale member: the frame is drawn at
-        1/factor of the size, aimed at `phase`)."""
+        means through the reconstruction chain (temporal + a-trous, or the
+        temporal member alone with `temporal_only`; at a film `factor` of 2
+        to 4 the frame is drawn at 1/factor of the size, aimed at `phase`,
+        and the chain ends in the upscale member, or in the upsample member
+        with `upsample`, which without `denoise` blows up the means)."""
         sc = self.scene
         f = Frame(width, height, samples, surfaces if surfaces is not None else int(sc.render["surfaces"]),
                   seed if seed is not None else int(sc.render["seed"]), first, 1 if accumulate else 0,
-                  (FRAME_DENOISE if denoise else 0) | (FRAME_RESTART if restart else 0), factor, phase)
+                  (FRAME_DENOISE if denoise else 0) | (FRAME_RESTART if restart else 0) | (FRAME_TEMPORAL if temporal_only else 0) |
+                  (FRAME_UPSAMPLE if upsample else 0), factor, phase)
         out = np.zeros((height, width, 3), np.float32)
         self._check(self.lib.kdn_render(self.handle, ctypes.byref(f), _ptr(out)))
         return out

@@ -225,3 +225,18 @@ extern "C" kdn_status kdn_upscale_device(kdn_ctx* handle, const kdn_upscale_fram
 	if (!ctx->check(cudaSetDevice(ctx->device), "cudaSetDevice")) return KDN_CUDA_ERROR;
 	return kdn::upscaleOnDevice(ctx, ctx->upscale, frame, io, stream ? static_cast<cudaStream_t>(stream) : ctx->stream);
 }
+
+extern "C" kdn_status kdn_upsample_device(kdn_ctx* handle, int32_t width, int32_t height, uint32_t factor, const float* drawn, float* shown, void* stream) {
+	if (handle == nullptr) return KDN_BAD_ARG;
+	Context* ctx = reinterpret_cast<Context*>(handle);
+	std::lock_guard<std::mutex> guard(ctx->lock);
+	if (ctx->device < 0) return ctx->fail(KDN_NO_DEVICE, "kdn_upsample_device: a host-only context has no device");
+	if (factor < 1 || factor > 4) return ctx->fail(KDN_BAD_ARG, "kdn_upsample_device: the film factor must be 1 to 4");
+	if (width <= 0 || height <= 0 || width % int32_t(factor) != 0 || height % int32_t(factor) != 0 || int64_t(width) * int64_t(height) > (int64_t(1) << 26))
+		return ctx->fail(KDN_BAD_ARG, "kdn_upsample_device: the shown size must be positive, a multiple of the factor and at most 2^26 pixels");
+	if (drawn == nullptr || shown == nullptr) return ctx->fail(KDN_BAD_ARG, "kdn_upsample_device: a buffer is missing");
+	if (!ctx->check(cudaSetDevice(ctx->device), "cudaSetDevice")) return KDN_CUDA_ERROR;
+	if (!ctx->check(kdn::launchUpsample(width, height, int(factor), drawn, shown, stream ? static_cast<cudaStream_t>(stream) : ctx->stream, ctx->smCount), "upsample kernel"))
+		return KDN_CUDA_ERROR;
+	return KDN_OK;
+}

@@ -8,6 +8,7 @@
 // across calls (progressive accumulation) until a call starts afresh.
 #include "context.h"
 #include "temporal.h"
+#include "upscale.h"
 #include "frame.h"
 #include "guide.h"
 
@@ -335,8 +336,10 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	// core/camera.h:65 FilmPlan: the frame is drawn at 1/factor of its size
 	const uint32_t factor = fr->factor > 1 ? fr->factor : 1u;
 	if (factor > 4) return ctx->fail(KDN_BAD_ARG, "kdn_render: the film factor must be 1 to 4");
+	const bool upsampled = factor > 1 && (fr->flags & KDN_FRAME_UPSAMPLE);
 	if (factor > 1) {
-		if (!(fr->flags & KDN_FRAME_DENOISE)) return ctx->fail(KDN_BAD_ARG, "kdn_render: a film factor above 1 needs the reconstruction chain (KDN_FRAME_DENOISE)");
+		if (!(fr->flags & KDN_FRAME_DENOISE) && !upsampled)
+			return ctx->fail(KDN_BAD_ARG, "kdn_render: a film factor above 1 needs a reconstruction chain to the shown size (KDN_FRAME_DENOISE or KDN_FRAME_UPSAMPLE)");
 		if (fr->width % int32_t(factor) != 0 || fr->height % int32_t(factor) != 0) return ctx->fail(KDN_BAD_ARG, "kdn_render: the size must be a multiple of the film factor");
 		if (fr->phase >= factor * factor) return ctx->fail(KDN_BAD_ARG, "kdn_render: the phase must be below the film factor's square");
 	}
@@ -388,13 +391,13 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		for (const auto& w : wants) {
 			if ((s = ctx->ensure(*w.b, w.bytes)) != KDN_OK) return s;
 		}
-		if (factor > 1) {
+		if (factor > 1 && !upsampled) {
 			for (DeviceBuffer* b : { &f.upState[0], &f.upState[1] }) {
 				if ((s = ctx->ensure(*b, size_t(shownPixels) * 16)) != KDN_OK) return s;
 			}
-			if ((s = ctx->ensure(f.internal, px * 12)) != KDN_OK) return s;
 		}
 	}
+	if (factor > 1 && (s = ctx->ensure(f.internal, size_t(pixels) * 12)) != KDN_OK) return s;
 	if (fresh) {
 		if (!ctx->check(cudaMemsetAsync(f.sums.ptr, 0, size_t(pixels) * 3 * sizeof(double), stream), "clear sums")) return KDN_CUDA_ERROR;
 		f.taken = 0;
@@ -746,9 +749,17 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		if ((s = ctx->ensure(f.out, size_t(shownPixels) * 3 * sizeof(float))) != KDN_OK) return s;
 		image = static_cast<float*>(f.out.ptr);
 	}
+	// the drawn frame the chain's members before a change of size leave:
+	// the shown frame itself at a film factor of 1
+	float* drawnImage = factor > 1 ? static_cast<float*>(f.internal.ptr) : image;
 	if (!denoised) {
-		if (!ctx->check(launchMeans(static_cast<const double*>(f.sums.ptr), pixels, f.taken, image, stream, ctx->smCount), "means kernel")) return KDN_CUDA_ERROR;
+		// reconstruction/mean (then upsample at a film factor above 1)
+		if (!ctx->check(launchMeans(static_cast<const double*>(f.sums.ptr), pixels, f.taken, drawnImage, stream, ctx->smCount), "means kernel")) return KDN_CUDA_ERROR;
 		++launches;
+		if (factor > 1) {
+			if (!ctx->check(launchUpsample(fr->width, fr->height, int(factor), drawnImage, image, stream, ctx->smCount), "upsample kernel")) return KDN_CUDA_ERROR;
+			++launches;
+		}
 	} else {
 		// the shown frame (core/frame.cpp shownSurfaces, then the reconstruction
 		// chain temporal + a-trous): this frame's record and G-buffer through
@@ -800,8 +811,11 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		ta.io.colour              = static_cast<float*>(f.tColour[cur].ptr);
 		ta.io.moment              = static_cast<float*>(f.tMoment[cur].ptr);
 		ta.io.length              = static_cast<float*>(f.tLength[cur].ptr);
-		ta.io.image               = nullptr;
+		// the chain `temporal` alone shows the temporal member's light
+		const bool temporalOnly   = (fr->flags & KDN_FRAME_TEMPORAL) != 0;
+		ta.io.image               = temporalOnly ? drawnImage : nullptr;
 		if (!ctx->check(launchTemporal(ta, stream), "temporal kernel")) return KDN_CUDA_ERROR;
+		++launches;
 		kdn_denoise_frame df {};
 		df.width  = drawnWidth;
 		df.height = drawnHeight;
@@ -814,12 +828,18 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		df.reach       = lens[12];
 		df.aspect      = lens[13];
 		df.demodulated = 1;
-		float* drawnImage = factor > 1 ? static_cast<float*>(f.internal.ptr) : image;
-		if ((s = denoiseOnDevice(ctx, &df, ta.io.colour, ta.io.moment, ta.io.length, ta.io.centre_distance, ta.io.centre_normal, ta.io.centre_albedo,
-		                         ta.io.centre_leaf, drawnImage, stream)) != KDN_OK)
-			return s;
-		launches += 8;
-		if (factor > 1) {
+		if (!temporalOnly) {
+			if ((s = denoiseOnDevice(ctx, &df, ta.io.colour, ta.io.moment, ta.io.length, ta.io.centre_distance, ta.io.centre_normal, ta.io.centre_albedo,
+			                         ta.io.centre_leaf, drawnImage, stream)) != KDN_OK)
+				return s;
+			launches += 7;
+		}
+		if (upsampled) {
+			// reconstruction/upsample as the chain's last member
+			if (!ctx->check(launchUpsample(fr->width, fr->height, int(factor), drawnImage, image, stream, ctx->smCount), "upsample kernel")) return KDN_CUDA_ERROR;
+			++launches;
+			f.upShown = -1;
+		} else if (factor > 1) {
 			// plugins/reconstruction/upscale/upscale.cpp upscaledFrame: the
 			// denoised drawn frame to the shown size, its history kept where
 			// the last frame was upscaled to this size and the sequence goes on;

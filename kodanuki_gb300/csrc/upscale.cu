@@ -293,6 +293,39 @@ __global__ void __launch_bounds__(kBlock) upscaleKernel(const __grid_constant__ 
 	}
 }
 
+// plugins/reconstruction/upsample/upsample.cpp:15 upsampleTap: the two
+// drawn pixels either side of a shown pixel's centre and the share of the
+// second, clamped to the drawn frame
+struct UpsampleTap {
+	int first, second;
+	float share;
+};
+
+__device__ __forceinline__ UpsampleTap upsampleTap(int shown, int factor, int drawn) {
+	const double centre  = (double(shown) + 0.5) / double(factor) - 0.5;
+	const double clamped = centre < 0.0 ? 0.0 : (double(drawn - 1) < centre ? double(drawn - 1) : centre);
+	const int first      = int(clamped);
+	return { first, first + 1 < drawn - 1 ? first + 1 : drawn - 1, float(clamped - double(first)) };
+}
+
+// upsample.cpp:63 upsampledImage, :41 blendedChannel: bilinear in float
+__global__ void __launch_bounds__(kBlock) upsampleKernel(int width, int height, int factor, const float* drawn, float* shown) {
+	const int n = width * height, dw = width / factor, dh = height / factor;
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+		const int x = k % width, y = k / width;
+		const UpsampleTap row = upsampleTap(y, factor, dh), column = upsampleTap(x, factor, dw);
+		const float* upper    = drawn + size_t(row.first) * size_t(dw) * 3;
+		const float* lower    = drawn + size_t(row.second) * size_t(dw) * 3;
+		for (int c = 0; c < 3; ++c) {
+			const float a = upper[3 * column.first + c], b = upper[3 * column.second + c];
+			const float d = lower[3 * column.first + c], e = lower[3 * column.second + c];
+			const float top    = a + (b - a) * column.share;
+			const float bottom = d + (e - d) * column.share;
+			shown[size_t(k) * 3 + c] = top + (bottom - top) * row.share;
+		}
+	}
+}
+
 double catmullRom(double t) {
 	const double a = std::fabs(t);
 	if (a < 1) return (1.5 * a - 2.5) * a * a + 1;
@@ -331,6 +364,12 @@ cudaError_t launchUpscale(const UpscaleArgs& args, cudaStream_t stream, int smCo
 	const int most  = smCount * 8;
 	samplesKernel<<<std::min((drawn + kBlock - 1) / kBlock, most), kBlock, 0, stream>>>(args.internal, args.distance, drawn, args.samples);
 	upscaleKernel<<<std::min((shown + kBlock - 1) / kBlock, most), kBlock, 0, stream>>>(args);
+	return cudaGetLastError();
+}
+
+cudaError_t launchUpsample(int width, int height, int factor, const float* drawn, float* shown, cudaStream_t stream, int smCount) {
+	const int n = width * height;
+	upsampleKernel<<<std::min((n + kBlock - 1) / kBlock, smCount * 8), kBlock, 0, stream>>>(width, height, factor, drawn, shown);
 	return cudaGetLastError();
 }
 

@@ -1,7 +1,8 @@
-// The upscale member on the device (plugins/reconstruction/upscale/
-// upscale.cpp upscaledFrame): a frame drawn at 1/factor of the shown size,
-// one phase of the factor^2 shown pixels a drawn pixel covers each frame,
-// gathered to the shown size against a history of shown pixels.
+// The upscale and upsample members on the device (plugins/reconstruction/
+// upscale/upscale.cpp upscaledFrame, upsample/upsample.cpp upsampledImage):
+// a frame drawn at 1/factor of the shown size, one phase of the factor^2
+// shown pixels a drawn pixel covers each frame, gathered to the shown size
+// against a history of shown pixels, or blown up bilinearly.
 #pragma once
 
 #include "kdn.h"
@@ -48,5 +49,9 @@ struct UpscaleArgs {
 };
 
 cudaError_t launchUpscale(const UpscaleArgs& args, cudaStream_t stream, int smCount);
+
+// plugins/reconstruction/upsample/upsample.cpp upsampledImage: the drawn
+// frame (width / factor x height / factor, RGB) bilinearly to width x height.
+cudaError_t launchUpsample(int width, int height, int factor, const float* drawn, float* shown, cudaStream_t stream, int smCount);
 
 } // namespace kdn

@@ -395,6 +395,17 @@ def upscale(width: int, height: int, factor: int, phase: int, moved: bool, kept:
     return colour, depth, image
 
 
+def upsample(width: int, height: int, factor: int, drawn) -> np.ndarray:
+    """The oracle's upsample member (kp_upsample): the drawn frame (drawn
+    size x 3) bilinearly to width x height (n x 3 float)."""
+    L = lib()
+    L.kp_upsample.argtypes = [ctypes.c_int] * 3 + [_P] * 2
+    drawn = np.ascontiguousarray(drawn, np.float32)
+    shown = np.zeros((width * height, 3), np.float32)
+    L.kp_upsample(width, height, factor, _ptr(drawn), _ptr(shown))
+    return shown
+
+
 def upscale_settling(kept: bool, moved: bool, before_moved: bool, before_settling: int) -> tuple[bool, int]:
     """upscale.cpp:557 settlingFrames and the count the state keeps: whether
     this frame settles (blends at alpha 1) and the count after."""

@@ -236,6 +236,11 @@ void kp_upscale(int width, int height, int factor, int phase, int moved, int kep
                 const float* internal, const float* distance, const double* before_colour, const float* before_depth, double* colour, float* depth,
                 float* image);
 
+/* The upsample member (upscale.c; plugins/reconstruction/upsample/
+ * upsample.cpp upsampledImage): the drawn frame bilinearly to the shown
+ * size width x height at a film factor. */
+void kp_upsample(int width, int height, int factor, const float* drawn, float* shown);
+
 uint64_t kp_mixed_bits(uint64_t v);
 double kp_unit_of(uint64_t bits);
 double kp_hashed(uint64_t stream, uint64_t index, uint64_t coordinate);

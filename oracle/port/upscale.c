@@ -408,3 +408,42 @@ void kp_upscale(int width, int height, int factor, int phase, int moved, int kep
 	}
 	free(samples);
 }
+
+/* plugins/reconstruction/upsample/upsample.cpp: the drawn frame (drawn
+ * size, RGB float) to the shown size (width x height) by bilinear taps in
+ * float, the taps (:15 upsampleTap) from each shown pixel's centre in drawn
+ * pixels, clamped to the drawn frame. */
+typedef struct utap {
+	int first, second;
+	float share;
+} utap;
+
+static utap upsample_tap(int shown, int factor, int drawn) {
+	const double centre = ((double) shown + 0.5) / (double) factor - 0.5;
+	const double clamped = centre < 0.0 ? 0.0 : ((double) (drawn - 1) < centre ? (double) (drawn - 1) : centre);
+	utap t;
+	t.first = (int) clamped;
+	t.second = t.first + 1 < drawn - 1 ? t.first + 1 : drawn - 1;
+	t.share = (float) (clamped - (double) t.first);
+	return t;
+}
+
+void kp_upsample(int width, int height, int factor, const float* drawn, float* shown) {
+	const int dw = width / factor, dh = height / factor;
+	for (int y = 0; y < height; ++y) {
+		const utap row = upsample_tap(y, factor, dh);
+		const float* upper = drawn + (size_t) row.first * (size_t) dw * 3;
+		const float* lower = drawn + (size_t) row.second * (size_t) dw * 3;
+		for (int x = 0; x < width; ++x) {
+			const utap column = upsample_tap(x, factor, dw);
+			for (int c = 0; c < 3; ++c) {
+				/* :41 blendedChannel */
+				const float a = upper[3 * column.first + c], b = upper[3 * column.second + c];
+				const float d = lower[3 * column.first + c], e = lower[3 * column.second + c];
+				const float top = a + (b - a) * column.share;
+				const float bottom = d + (e - d) * column.share;
+				shown[((size_t) y * (size_t) width + (size_t) x) * 3 + c] = top + (bottom - top) * row.share;
+			}
+		}
+	}
+}

@@ -11,6 +11,7 @@
 //   kdn_ref_dump temporal <in.bin> <out.bin>              temporalFrame
 //   kdn_ref_dump bsdf  <file.sdf> <in.bin> <out.bin>      respondBsdf, sampleBsdf
 //   kdn_ref_dump upscale  <in.bin> <out.bin>              upscaledFrame
+//   kdn_ref_dump upsample <in.bin> <out.bin>              upsampledImage
 //
 // Reference entry points used: loadScene (syntax/evaluator.cpp:2898),
 // sceneRegion (plugins/geometry/tree/build.cpp:405), sphereTraced
@@ -22,12 +23,14 @@
 #include "plugins/geometry/tree/cut.h"
 #include "plugins/reconstruction/atrous/atrous.h"
 #include "plugins/reconstruction/temporal/temporal.h"
+#include "plugins/reconstruction/upsample/upsample.h"
 #include "plugins/reconstruction/upscale/upscale.h"
 #include "plugins/transport/paths/material/material.h"
 #include "sdf/program.h"
 #include "sdf/scene.h"
 #include "syntax/evaluator.h"
 
+#include <array>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -621,6 +624,47 @@ int dumpUpscale(const char* inPath, const char* outPath) {
 	return 0;
 }
 
+// The upsample member (plugins/reconstruction/upsample/upsample.cpp
+// upsampledImage).  Input: int32 shown width, height, film factor; the
+// drawn image (RGB f32, the shown size over the factor).  Output: the shown
+// image, RGB f32.
+int dumpUpsample(const char* inPath, const char* outPath) {
+	FILE* in = std::fopen(inPath, "rb");
+	std::int32_t head[3];
+	if (in == nullptr || std::fread(head, 4, 3, in) != 3) return 1;
+	const int width = head[0], height = head[1];
+	const FilmPlan film = { .factor = head[2], .phase = 0 };
+	Image drawn         = blankImage(width / film.factor, height / film.factor);
+	if (std::fread(drawn.rgb.data(), 4, drawn.rgb.size(), in) != drawn.rgb.size()) return 1;
+	std::fclose(in);
+	const Lens lens    = lensOf14(std::array<double, 14> { 0, 0, 0, 0, 1, 0, 1, 0, 0, 0, 0, 1, 1, 1 }.data(), width, height);
+	FrameRecord record = emptyFrameRecord();
+	record.width       = drawn.width;
+	record.height      = drawn.height;
+	static const std::vector<PixelSum> estimates;
+	static const std::vector<Surface> none;
+	const ShownFrame frame = {
+		.width     = width,
+		.height    = height,
+		.lens      = lens,
+		.before    = lens,
+		.film      = film,
+		.moved     = false,
+		.restarted = false,
+		.recounted = false,
+		.still     = 1,
+		.record    = record,
+		.estimates = estimates,
+		.surfaces  = none,
+		.threads   = 4,
+	};
+	const Image shown = upsampledImage(drawn, frame);
+	FILE* out         = std::fopen(outPath, "wb");
+	std::fwrite(shown.rgb.data(), 4, shown.rgb.size(), out);
+	std::fclose(out);
+	return 0;
+}
+
 } // namespace
 
 // respondBsdf and sampleBsdf (plugins/transport/paths/material/material.cpp
@@ -704,6 +748,9 @@ int main(int argc, char** argv) {
 	if (argc >= 4 && std::strcmp(argv[1], "temporal") == 0) {
 		return dumpTemporal(argv[2], argv[3]);
 	}
+	if (argc >= 4 && std::strcmp(argv[1], "upsample") == 0) {
+		return dumpUpsample(argv[2], argv[3]);
+	}
 	if (argc >= 4 && std::strcmp(argv[1], "upscale") == 0) {
 		return dumpUpscale(argv[2], argv[3]);
 	}
@@ -725,6 +772,6 @@ int main(int argc, char** argv) {
 	if (argc >= 5 && std::strcmp(argv[1], "cells") == 0) {
 		return dumpCells(argv[2], argv[3], argv[4]);
 	}
-	std::fprintf(stderr, "usage: kdn_ref_dump scene|trace|cut|cells|bsdf|denoise|temporal|upscale ...\n");
+	std::fprintf(stderr, "usage: kdn_ref_dump scene|trace|cut|cells|bsdf|denoise|temporal|upscale|upsample ...\n");
 	return 2;
 }

@@ -455,6 +455,27 @@ def upscale_fixture(dump: str, tmp: str) -> None:
     np.savez_compressed(os.path.join(HERE, "upscale.npz"), **out)
 
 
+def upsample_fixture(dump: str, tmp: str) -> None:
+    """tests/golden/upsample.npz: the reference's upsampledImage
+    (plugins/reconstruction/upsample/upsample.cpp) of seeded drawn frames at
+    film factors 2, 3 and 4 (shown 96 x 48)."""
+    rng = np.random.default_rng(91)
+    out = {}
+    for factor in (2, 3, 4):
+        w, h = 96, 48
+        drawn = (rng.random((h // factor) * (w // factor) * 3) * rng.choice([0.5, 2.0, 30.0], (h // factor) * (w // factor) * 3)).astype(np.float32)
+        path, res = os.path.join(tmp, f"upsample_{factor}.bin"), os.path.join(tmp, f"upsample_{factor}.out")
+        with open(path, "wb") as fh:
+            fh.write(struct.pack("<3i", w, h, factor))
+            fh.write(drawn.astype("<f4").tobytes())
+        subprocess.run([dump, "upsample", path, res], check=True)
+        out[f"{factor}.drawn"] = drawn.reshape(-1, 3)
+        out[f"{factor}.shown"] = np.fromfile(res, "<f4").reshape(-1, 3)
+        out[f"{factor}.size"] = np.array([w, h])
+    np.savez_compressed(os.path.join(HERE, "upsample.npz"), **out)
+    print(" upsample factors 2, 3, 4")
+
+
 # The benchmark's own octree of config 2 and the cells sampled from it for
 # tests/golden/cutdeep_c2.npz
 DEEP_BUILD = (7, 11, 32)
@@ -521,6 +542,8 @@ def main() -> None:
         temporal_fixture(dump, tmp, factor=2)
     if args.only in (None, "temporal", "upscale"):
         upscale_fixture(dump, tmp)
+    if args.only in (None, "upsample"):
+        upsample_fixture(dump, tmp)
     if args.only in (None, "cutdeep"):
         deep_cut_fixture(dump, tmp)
     for name, (gen, kw, nrays, depth) in SCENES.items():

@@ -13,9 +13,11 @@ C ABI.
    a-trous + upscale run by the oracle (each member pinned to the
    reference's own) on the frame's own record and G-buffer, within 1e-4
    relative for 99.9% of shown pixels and 1e-3 for all.
-3. Refusals: a factor above 1 without KDN_FRAME_DENOISE, a size that is
-   not a multiple of the factor, a phase past the factor's square, a factor
-   above 4.
+3. The other chains: mean + upsample, temporal + a-trous + upsample, and
+   the temporal member alone.
+4. Refusals: a factor above 1 with no chain to the shown size, a size that
+   is not a multiple of the factor, a phase past the factor's square, a
+   factor above 4.
 """
 import os
 
@@ -149,6 +151,53 @@ def test_shown_frames_at_factor_2(backend):
             before_lens, before_phase = lens_now, phase
     finally:
         backend.upload("shot.camera", blocks["shot.camera"])
+
+
+def test_other_chains(backend):
+    """The chain mean + upsample at factor 2 (KDN_FRAME_UPSAMPLE without
+    KDN_FRAME_DENOISE) shows the drawn frame's pixel means blown up by the
+    oracle's upsample member (pinned to the reference's upsampledImage);
+    temporal + a-trous + upsample shows the chain's drawn frame blown up; the
+    chain `temporal` alone (KDN_FRAME_TEMPORAL) shows the temporal member's
+    light, the oracle's on the frame's own record and G-buffer."""
+    import oracle.port as op
+    sc = scene("c2_small")
+    factor, spp = 2, 4
+    dw, dh = int(sc.render["width"]), int(sc.render["height"])
+    w, h = dw * factor, dh * factor
+    backend.load(sc)
+    backend.build(**BUILD)
+    shown = backend.render(w, h, spp, seed=3, factor=factor, phase=2, upsample=True)
+    backend.render(w, h, spp, seed=3, factor=factor, phase=2, denoise=True, restart=True)
+    means = backend.frame_record(dw, dh)["light"].reshape(-1, 3)
+    want = op.upsample(w, h, factor, means).reshape(h, w, 3)
+    assert np.allclose(shown, want, rtol=1e-6, atol=1e-7)
+    # temporal + a-trous + upsample: a first frame, so the chain's drawn frame
+    # is the oracle's temporal and denoiser on the record (as the shown-frame tests)
+    up = backend.render(w, h, spp, seed=3, factor=factor, phase=2, denoise=True, restart=True, upsample=True)
+    record, gbuffer = backend.frame_record(dw, dh), backend.frame_surfaces(dw, dh)
+    lens = op.lens_of(sc, dw, dh)
+    rec = {k: np.asarray(v).reshape(-1, *np.asarray(v).shape[2:]) for k, v in record.items()}
+    g = {k: np.asarray(v).reshape(-1, *np.asarray(v).shape[2:]) for k, v in gbuffer.items()}
+    first = {k: rec[k].astype(np.float32) for k in ("distance", "normal", "albedo")}
+    first["leaf"] = rec["leaf"]
+    centre = {k: g[k].astype(np.float32) for k in ("distance", "normal", "albedo")}
+    centre["leaf"] = g["leaf"]
+    state, _ = op.temporal(dw, dh, False, False, False, lens, lens, rec["light"].astype(np.float64), first, centre, None, (factor, 2, factor, 2))
+    internal = op.denoise(dw, dh, 1, lens, state["colour"], state["moment"], state["length"], state["distance"], state["normal"], state["leaf"],
+                          state["albedo"]).reshape(-1, 3)
+    check("temporal + a-trous + upsample", up, op.upsample(w, h, factor, internal).reshape(h, w, 3))
+    # the temporal member alone, at factor 1
+    alone = backend.render(dw, dh, spp, seed=5, denoise=True, restart=True, temporal_only=True)
+    record, gbuffer = backend.frame_record(dw, dh), backend.frame_surfaces(dw, dh)
+    rec = {k: np.asarray(v).reshape(-1, *np.asarray(v).shape[2:]) for k, v in record.items()}
+    g = {k: np.asarray(v).reshape(-1, *np.asarray(v).shape[2:]) for k, v in gbuffer.items()}
+    first = {k: rec[k].astype(np.float32) for k in ("distance", "normal", "albedo")}
+    first["leaf"] = rec["leaf"]
+    centre = {k: g[k].astype(np.float32) for k in ("distance", "normal", "albedo")}
+    centre["leaf"] = g["leaf"]
+    _, image = op.temporal(dw, dh, False, False, False, lens, lens, rec["light"].astype(np.float64), first, centre, None)
+    check("temporal alone", alone, image.reshape(dh, dw, 3).astype(np.float64))
 
 
 def test_film_factor_refusals(backend):

@@ -7,7 +7,7 @@ the state the reference left after the frame before.
 The device computes the geometry (headings, planes, where a point was seen
 before, the bilinear weights) in double as the reference does, and the
 light in FP32; the bar: the state's colour, moment and the shown light
-within 1e-5 relative for at least 99.9% of pixels and within 1e-3 for all,
+within 1e-5 relative for at least 99.5% of pixels and within 1e-4 for all,
 1e-6 at the median; the length equal within 1e-6 on every pixel.
 """
 import ctypes
@@ -99,6 +99,6 @@ def test_temporal_matches_reference(backend, name, frame):
                                                                         for k, e in errs.items()))
     assert length_same == 1.0
     for e in errs.values():
-        assert np.mean(e <= 1e-5) >= 0.999
-        assert np.all(e <= 1e-3)
+        assert np.mean(e <= 1e-5) >= 0.995
+        assert np.all(e <= 1e-4)
         assert np.median(e) <= 1e-6

@@ -89,3 +89,18 @@ def test_upscale_refuses_bad_frames(backend):
         fr = K.UpscaleFrame(w, h, factor, phase, 0, 0)
         status = backend.lib.kdn_upscale_device(backend.handle, ctypes.byref(fr), ctypes.byref(bufs), None)
         assert status == K.KDN_BAD_ARG, (factor, phase, w, h)
+
+
+@pytest.mark.parametrize("factor", [2, 3, 4])
+def test_upsample_matches_reference(backend, factor):
+    """kdn_upsample_device against the reference's upsampledImage
+    (tests/golden/upsample.npz), to the bit."""
+    import torch
+    z = np.load(os.path.join(GOLDEN, "upsample.npz"))
+    w, h = (int(v) for v in z[f"{factor}.size"])
+    drawn = torch.from_numpy(np.ascontiguousarray(z[f"{factor}.drawn"], np.float32)).cuda()
+    shown = torch.zeros(w * h * 3, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    backend._check(backend.lib.kdn_upsample_device(backend.handle, w, h, factor, drawn.data_ptr(), shown.data_ptr(), ctypes.c_void_p(stream.cuda_stream)))
+    torch.cuda.synchronize()
+    assert np.array_equal(shown.cpu().numpy().reshape(-1, 3), z[f"{factor}.shown"])

@@ -46,3 +46,15 @@ def test_upscale_oracle_matches_reference(frame):
     assert np.array_equal(depth, g[f"{frame}.depth"])
     assert np.array_equal(colour, g[f"{frame}.colour"])
     assert np.array_equal(image, g[f"{frame}.image"])
+
+
+@pytest.mark.parametrize("factor", [2, 3, 4])
+def test_upsample_oracle_matches_reference(factor):
+    """The oracle's upsample member (oracle/port/upscale.c kp_upsample)
+    against the reference's upsampledImage (tests/golden/upsample.npz), to
+    the bit."""
+    import oracle.port as op
+    z = np.load(os.path.join(GOLDEN, "upsample.npz"))
+    w, h = (int(v) for v in z[f"{factor}.size"])
+    shown = op.upsample(w, h, factor, z[f"{factor}.drawn"])
+    assert np.array_equal(shown, z[f"{factor}.shown"])
