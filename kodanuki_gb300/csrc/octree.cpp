@@ -889,53 +889,113 @@ std::string marchCode(const Prog& p, std::vector<MarchStep>& steps, GpuProgram& 
 std::string flattenOctree(const Octree& tree, FlatWorld& flat) {
 	flat = FlatWorld();
 	flat.nodes.resize(tree.cells.size());
+	// the distinct programs, in the order the leaves first name them
 	std::unordered_map<const Prog*, uint32_t> made;
+	std::vector<const Prog*> order;
+	std::vector<uint32_t> named; // each leaf's programs, in leaf order
+	for (size_t i = 0; i < tree.cells.size(); ++i) {
+		const Cell& c = tree.cells[i];
+		if (c.firstChild >= 0) continue;
+		if (c.programs.size() > kMaxLeafProgs) return "a leaf keeps more than " + std::to_string(kMaxLeafProgs) + " programs";
+		for (const ProgPtr& p : c.programs) {
+			auto found = made.find(p.get());
+			if (found == made.end()) {
+				found = made.emplace(p.get(), uint32_t(order.size())).first;
+				order.push_back(p.get());
+			}
+			named.push_back(found->second);
+		}
+	}
+	// Compile them on every core: contiguous runs of the order, each into
+	// its own buffers (offsets from the run's start), then laid end to end
+	// in order, so the layout is the one a single thread would make.
+	struct Run {
+		size_t first, end;
+		std::vector<GpuProgram> programs;
+		std::vector<GpuStep> steps;
+		std::vector<SsaOps> ssa;
+		std::vector<MarchStep> march;
+		std::string error;
+		size_t failed = SIZE_MAX;
+	};
+	const int threads = std::max(1, std::min(32, int(std::thread::hardware_concurrency())));
+	const size_t runCount = std::max<size_t>(1, std::min<size_t>(order.size() / 256 + 1, size_t(threads) * 8));
+	std::vector<Run> runs(runCount);
+	for (size_t r = 0; r < runCount; ++r) {
+		runs[r].first = order.size() * r / runCount;
+		runs[r].end   = order.size() * (r + 1) / runCount;
+	}
+	parallelFor(runCount, runCount < 64 ? 1 : threads, [&](size_t r, Scratch&) {
+		Run& run = runs[r];
+		run.programs.reserve(run.end - run.first);
+		for (size_t k = run.first; k < run.end; ++k) {
+			GpuProgram g = {};
+			std::string error = slotted(*order[k], run.steps, run.ssa, g);
+			if (error.empty()) error = marchCode(*order[k], run.march, g);
+			if (!error.empty()) {
+				run.error  = error;
+				run.failed = k;
+				return;
+			}
+			run.programs.push_back(g);
+		}
+	});
+	for (const Run& run : runs) {
+		if (!run.error.empty()) return run.error;
+	}
+	std::vector<size_t> stepBase(runCount), marchBase(runCount);
+	size_t stepTotal = 0, marchTotal = 0;
+	for (size_t r = 0; r < runCount; ++r) {
+		stepBase[r]  = stepTotal;
+		marchBase[r] = marchTotal;
+		stepTotal += runs[r].steps.size();
+		marchTotal += runs[r].march.size();
+	}
+	std::vector<GpuProgram> programs(order.size());
+	flat.steps.resize(stepTotal);
+	flat.ssa.resize(stepTotal);
+	flat.march.resize(marchTotal);
+	parallelFor(runCount, runCount < 64 ? 1 : threads, [&](size_t r, Scratch&) {
+		const Run& run = runs[r];
+		std::copy(run.steps.begin(), run.steps.end(), flat.steps.begin() + std::ptrdiff_t(stepBase[r]));
+		std::copy(run.ssa.begin(), run.ssa.end(), flat.ssa.begin() + std::ptrdiff_t(stepBase[r]));
+		std::copy(run.march.begin(), run.march.end(), flat.march.begin() + std::ptrdiff_t(marchBase[r]));
+		for (size_t k = 0; k < run.programs.size(); ++k) {
+			GpuProgram g = run.programs[k];
+			g.code += uint32_t(stepBase[r]);
+			g.march += uint32_t(marchBase[r]);
+			programs[run.first + k] = g;
+		}
+	});
+	// the leaves; each names its programs through an indirection, and the
+	// kernel reads them as one run, so the GpuPrograms are laid out per leaf
+	flat.programs.reserve(named.size());
+	size_t at = 0;
 	for (size_t i = 0; i < tree.cells.size(); ++i) {
 		const Cell& c = tree.cells[i];
 		if (c.firstChild >= 0) {
 			flat.nodes[i] = int32_t(c.firstChild);
 			continue;
 		}
-		if (c.programs.size() > kMaxLeafProgs) return "a leaf keeps more than " + std::to_string(kMaxLeafProgs) + " programs";
 		GpuLeaf leaf   = {};
 		leaf.occupancy = c.occupancy;
 		leaf.count     = uint16_t(c.programs.size());
-		leaf.first     = uint32_t(flat.leafPrograms.size());
+		leaf.first     = uint32_t(flat.programs.size());
 		uint32_t slots = 1;
-		for (const ProgPtr& p : c.programs) {
-			auto found = made.find(p.get());
-			uint32_t index;
-			if (found == made.end()) {
-				GpuProgram g     = {};
-				std::string error = slotted(*p, flat.steps, flat.ssa, g);
-				if (!error.empty()) return error;
-				error = marchCode(*p, flat.march, g);
-				if (!error.empty()) return error;
-				index = uint32_t(flat.programs.size());
-				flat.programs.push_back(g);
-				made.emplace(p.get(), index);
-			} else {
-				index = found->second;
-			}
-			slots = std::max<uint32_t>(slots, flat.programs[index].slots);
-			flat.leafPrograms.push_back(index);
+		for (size_t k = 0; k < c.programs.size(); ++k) {
+			const GpuProgram& g = programs[named[at++]];
+			slots               = std::max<uint32_t>(slots, g.slots);
+			flat.programs.push_back(g);
 		}
-		leaf.slots    = uint8_t(slots);
+		leaf.slots = uint8_t(slots);
+		if (leaf.count > 0) {
+			const GpuProgram& g = flat.programs[leaf.first];
+			leaf.march          = g.march;
+			leaf.marchCount     = g.marchCount;
+			leaf.marchSlot      = g.marchSlot;
+		}
 		flat.nodes[i] = ~int32_t(flat.leaves.size());
 		flat.leaves.push_back(leaf);
-	}
-	// Each leaf names its programs through an indirection; the kernel reads
-	// them as one run, so lay the GpuPrograms out per leaf.
-	std::vector<GpuProgram> runs;
-	runs.reserve(flat.leafPrograms.size());
-	for (uint32_t k : flat.leafPrograms) runs.push_back(flat.programs[k]);
-	flat.programs.swap(runs);
-	for (GpuLeaf& leaf : flat.leaves) {
-		if (leaf.count == 0) continue;
-		const GpuProgram& g = flat.programs[leaf.first];
-		leaf.march          = g.march;
-		leaf.marchCount     = g.marchCount;
-		leaf.marchSlot      = g.marchSlot;
 	}
 	return "";
 }

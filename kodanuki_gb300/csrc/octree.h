@@ -44,7 +44,6 @@ struct BuildOptions {
 struct FlatWorld {
 	std::vector<int32_t> nodes;
 	std::vector<GpuLeaf> leaves;
-	std::vector<uint32_t> leafPrograms;
 	std::vector<GpuProgram> programs; // one run per leaf
 	std::vector<GpuStep> steps;
 	std::vector<SsaOps> ssa;
