@@ -399,6 +399,78 @@ def guided(device: int) -> dict:
     }
 
 
+STRESS_SCENE = os.path.join(ROOT, "tests", "golden", "scenes", "c5.npz")
+STRESS_W, STRESS_H, STRESS_SPP, STRESS_SURFACES = 3840, 2160, 256, 32
+
+
+def stress(device: int) -> dict:
+    """Config 5, the stress configuration: the 65536-box city with its
+    dispersive sphere cluster at 3840x2160, 256 spp, 32 surfaces, on the
+    octree the benchmark builds at depth 11; then learned guiding on it;
+    then 4 progressive 1-spp sessions of it served alongside config-2
+    batch frames.  Device times from the frames' CUDA events."""
+    import kodanuki_gb300 as K
+    from kodanuki_gb300.scene import Scene
+    sc = Scene.load(STRESS_SCENE)
+    out = {"workload": f"config 5: {sc.program_count} objects (a 256 x 256 city of rounded boxes, heights 0.4 LogNormal(0, 0.5), "
+                       f"24 dispersive glass spheres), {STRESS_W}x{STRESS_H}, {STRESS_SPP} spp, {STRESS_SURFACES} surfaces, FP32"}
+    with K.Backend(device) as b:
+        b.load(sc)
+        t0 = time.perf_counter()
+        b.build(7, 11, 32)
+        out["build_s"] = time.perf_counter() - t0
+        out["world"] = b.world_stats()
+        b.render(STRESS_W, STRESS_H, 1, surfaces=STRESS_SURFACES, seed=9)  # warm-up
+        b.render(STRESS_W, STRESS_H, STRESS_SPP, surfaces=STRESS_SURFACES, seed=1)
+        st = b.frame_stats()
+        out["plain"] = {"ms": st.total_ms, "msamples_per_s": STRESS_W * STRESS_H * STRESS_SPP / st.total_ms / 1e3,
+                        "capped_rays": int(st.capped_rays), "longest_march": int(st.longest_march)}
+        lo = np.asarray(sc.region_lower, np.float64)
+        hi = lo + np.asarray(sc.region_size, np.float64)
+        with K.Guide(device, table_log2=19, seed=2, region=(lo, hi), learning_rate=1e-2, batch=16384, max_steps=256) as g:
+            b.set_guide(g, 0.5, K.GUIDE_TRAIN)
+            b.render(STRESS_W, STRESS_H, 8, surfaces=STRESS_SURFACES, seed=2000)
+            train_ms = b.frame_stats().total_ms
+            b.set_guide(g, 0.5, K.GUIDE_SAMPLE)
+            b.render(STRESS_W, STRESS_H, 1, surfaces=STRESS_SURFACES, seed=4)
+            b.render(STRESS_W, STRESS_H, 64, surfaces=STRESS_SURFACES, seed=3)
+            guided_ms = b.frame_stats().total_ms
+            b.set_guide(None)
+        out["guided"] = {"train_spp": 8, "train_ms": train_ms, "spp": 64, "ms": guided_ms,
+                         "msamples_per_s": STRESS_W * STRESS_H * 64 / guided_ms / 1e3}
+        # served: 4 progressive 1-spp sessions of the city, 8 frames each,
+        # beside config-2 batch frames (1080p, 64 spp)
+        with K.Backend(device) as c2:
+            c2.load(Scene.load(SCENE))
+            c2.build(7, 11, 32)
+            srv = K.Server(device, slots=8)
+            city, batch = srv.add_scene(b), srv.add_scene(c2)
+            warm = [srv.submit(city, STRESS_W, STRESS_H, 1, surfaces=STRESS_SURFACES, seed=5 + k, denoise=True, interactive=True, session=k + 1)
+                    for k in range(4)]
+            warm.append(srv.submit(batch, 640, 480, 1, surfaces=16, seed=1))
+            for t in warm:
+                srv.wait(t)
+            srv.reset_latency()
+            t0 = time.perf_counter()
+            jobs = [srv.submit(batch, 1920, 1080, 64, surfaces=16, seed=100 + k) for k in range(3)]
+            frames = 0
+            for _ in range(8):
+                tickets = [srv.submit(city, STRESS_W, STRESS_H, 1, surfaces=STRESS_SURFACES, seed=5 + k, denoise=True, interactive=True, session=k + 1)
+                           for k in range(4)]
+                for t in tickets:
+                    frames += int(srv.wait(t)[0] == K.KDN_OK)
+            done = sum(int(srv.wait(t)[0] == K.KDN_OK) for t in jobs)
+            wall = time.perf_counter() - t0
+            inter = srv.latency(True)
+            for k in range(4):
+                srv.end_session(k + 1)
+            srv.close()
+        out["served"] = {"sessions": 4, "session_frames": frames, "batch_frames": done, "wall_s": wall,
+                         "interactive_4k_1spp_ms": {"p50": inter["p50_ms"], "p99": inter["p99_ms"], "count": inter["count"]},
+                         "note": "each round submits the four sessions' next frames and waits for them; three config-2 batch frames run beside"}
+    return out
+
+
 def guide_profile(device: int) -> None:
     """Two training frames (each ends in Adam steps of 16384 samples) and one
     guided frame of the room scene at PROFILE_W x PROFILE_H: a short run for profilers."""
@@ -525,12 +597,15 @@ def main() -> None:
     ap.add_argument("--no-serve", action="store_true", help="leave out the serving run")
     ap.add_argument("--no-guide", action="store_true", help="leave out the learned-guide run")
     ap.add_argument("--guide-profile", action="store_true", help="a short learned-guide run alone (profiling captures): two training frames and one guided frame of the room scene")
+    ap.add_argument("--stress", action="store_true", help="config 5 alone (the 65536-box city at 3840x2160, 256 spp, guided, served): one JSON line, a few minutes")
     args = ap.parse_args()
     WIDTH, HEIGHT, SPP = args.width, args.height, args.spp
     if args.impl == "reference":
         run_reference(args)
     elif args.guide_profile:
         guide_profile(env_int("LOCAL_RANK", 0))
+    elif args.stress:
+        print(json.dumps(stress(env_int("LOCAL_RANK", 0))), flush=True)
     else:
         run_gpu(args)
 

@@ -333,6 +333,38 @@ def scene_films(seed: int = 1, width: int = 256, height: int = 256, samples: int
     return "".join(out)
 
 
+def scene_config5(seed: int = 1, width: int = 3840, height: int = 2160, samples: int = 256, surfaces: int = 32, side: int = 256) -> str:
+    """The stress scene: a city of side x side rounded boxes on a grid
+    (0.25 apart, footprints 0.16-0.2, heights 0.4 x LogNormal(0, 0.5)),
+    each its own object, plastics and metals; above its middle a cluster of
+    24 dispersive glass spheres (refraction 1.5, dispersion 0.02) that
+    throws caustics on the roofs; a warm quad light high over the centre and
+    a dim sky."""
+    rng = random.Random(seed)
+    span = 0.25 * side
+    out = [_header(width, height, samples, surfaces, seed, [0.0, -0.62 * span, 0.3 * span], [0.0, 0.0, 0.0], 0.9, far=1.6 * span)]
+    out.append(_sky([0.06, 0.07, 0.09]))
+    out.append(_quad([-0.1 * span, 0.1 * span, 0.45 * span], [0.2 * span, 0.0, 0.0], [0.0, -0.2 * span, 0.0], blackbody_rgb(5000.0, 40.0)))
+    out.append("paint(matte([0.35, 0.35, 0.35])) plane([0, 0, 1], 0);\n\n")
+    mats = [f"plastic({_v([rng.uniform(0.3, 0.8) for _ in range(3)])}, roughness = {_f(rng.uniform(0.1, 0.6))})" for _ in range(6)]
+    mats += [f"metal({_v([rng.uniform(0.6, 0.95) for _ in range(3)])}, roughness = {_f(rng.uniform(0.05, 0.3))})" for _ in range(2)]
+    for k, m in enumerate(mats):
+        out.append(f"let m{k} = {m};\n")
+    out.append("\n")
+    for i in range(side):
+        for j in range(side):
+            h = 0.4 * math.exp(rng.gauss(0.0, 0.5))
+            wx, wy = rng.uniform(0.16, 0.2), rng.uniform(0.16, 0.2)
+            pos = [(i - side / 2 + 0.5) * 0.25, (j - side / 2 + 0.5) * 0.25, h / 2]
+            out.append(f"paint(m{rng.randrange(len(mats))}) at({_v(pos)}) box({_v([wx, wy, h])}, 0.02);\n")
+    out.append("\nwith paint(glass(refraction = 1.5, dispersion = 0.02, roughness = 0)) {\n")
+    for _ in range(24):
+        pos = [rng.uniform(-1.5, 1.5), rng.uniform(-1.5, 1.5), rng.uniform(3.0, 4.5)]
+        out.append(f"\tat({_v(pos)}) sphere({_f(rng.uniform(0.2, 0.45))});\n")
+    out.append("}\n")
+    return "".join(out)
+
+
 _PATTERNS = """function bands(count) {
 	return 0.5 + 0.5 * sin(p.z * count);
 }

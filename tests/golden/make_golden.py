@@ -70,6 +70,8 @@ SCENES = {
     "patterns_small": (scenegen.scene_patterns, dict(seed=7, width=48, height=48, samples=64), 0, 0),
     "rough_small": (scenegen.scene_glass, dict(seed=8, width=48, height=48, samples=64, rough=True), 0, 0),
     "films_small": (scenegen.scene_films, dict(seed=9, width=48, height=48, samples=64), 0, 0),
+    # config 5, the stress scene (the benchmark's --stress run)
+    "c5": (scenegen.scene_config5, dict(seed=1), 0, 0),
 }
 # config 3: the eight resident scenes of the serving run, 256 to 16384
 # config-1-style primitives (merge(0.05) groups of 64)
