@@ -236,6 +236,11 @@ typedef struct kdn_frame {
  * no history) instead of upscale; without KDN_FRAME_DENOISE the chain is
  * mean + upsample (the drawn frame's pixel means blown up). */
 #define KDN_FRAME_UPSAMPLE 8u
+/* --use sampler=sobol (plugins/sampler/sobol): the first 28 dimensions of
+ * every path's draws from a Sobol sequence Owen-scrambled per pixel
+ * (plugins/transport/paths/sampler.cpp:16 numberAt), the rest hashed as
+ * without it. */
+#define KDN_FRAME_SOBOL 16u
 
 /* Device times of the last kdn_render, from CUDA events on the context's stream. */
 typedef struct kdn_frame_stats {

@@ -49,7 +49,7 @@ void Context::release() {
 	cudaSetDevice(device);
 	if (stream) cudaStreamSynchronize(stream);
 	releaseFrame();
-	for (DeviceBuffer* b : { &nodes, &leaves, &programs, &steps, &march, &ssa, &leafMaterial, &objectMaterial, &grid, &gridWalls, &extendRays, &extendHits, &extendStates, &counters, &l2, &denoiseScratch, &denoiseIo, &fetch, &upscale.samples, &upscale.axes }) freeBuffer(*b);
+	for (DeviceBuffer* b : { &nodes, &leaves, &programs, &steps, &march, &ssa, &leafMaterial, &objectMaterial, &grid, &gridWalls, &extendRays, &extendHits, &extendStates, &counters, &l2, &denoiseScratch, &denoiseIo, &fetch, &upscale.samples, &upscale.axes, &sobolTables }) freeBuffer(*b);
 	if (stream) cudaStreamDestroy(stream);
 	stream = nullptr;
 }

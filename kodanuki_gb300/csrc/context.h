@@ -66,6 +66,7 @@ struct Context {
 	DeviceBuffer extendRays, extendHits, extendStates, counters, l2;
 	DeviceBuffer denoiseScratch, denoiseIo, fetch;
 	UpscaleScratch upscale; // kdn_upscale_device's
+	DeviceBuffer sobolTables; // --use sampler=sobol's byte tables, built at the first frame that asks
 	FrameState* frame = nullptr;
 	// the learned guide frames use (kdn_set_guide): KDN_GUIDE_SAMPLE, KDN_GUIDE_TRAIN
 	kdn_guide* guide    = nullptr;

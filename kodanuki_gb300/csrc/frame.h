@@ -109,6 +109,9 @@ struct FrameConstants {
 	// filmCentre, in drawn pixels)
 	uint32_t factor, phase;
 	float centre[2];
+	// --use sampler=sobol: the Sobol byte tables (sobol.h), or null for
+	// independent numbers
+	const uint32_t* sobol;
 	float zenith[3], horizon[3], ground[3];
 	DeviceLamp lamps[kMaxLamps];
 	SpectralTables spectral;

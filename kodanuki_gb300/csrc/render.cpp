@@ -7,6 +7,7 @@
 // synchronisation.  Pixel sums are kept in double on the device and persist
 // across calls (progressive accumulation) until a call starts afresh.
 #include "context.h"
+#include "sobol.h"
 #include "temporal.h"
 #include "upscale.h"
 #include "frame.h"
@@ -421,6 +422,16 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	c.factor        = factor;
 	c.phase         = factor > 1 ? fr->phase : 0u;
 	filmCentreOf(factor, c.phase, c.centre);
+	c.sobol         = nullptr;
+	if (fr->flags & KDN_FRAME_SOBOL) {
+		if (ctx->sobolTables.ptr == nullptr) {
+			std::vector<uint32_t> tables(kSobolTableWords);
+			buildSobolTables(tables.data());
+			if ((s = ctx->upload(ctx->sobolTables, tables.data(), tables.size() * sizeof(uint32_t))) != KDN_OK) return s;
+			if (!ctx->check(cudaStreamSynchronize(ctx->stream), "sobol tables")) return KDN_CUDA_ERROR;
+		}
+		c.sobol = static_cast<const uint32_t*>(ctx->sobolTables.ptr);
+	}
 	c.seedMix       = mixedBits(uint64_t(int64_t(fr->seed)));
 	c.surfaces      = fr->surfaces;
 	c.spp           = spp;

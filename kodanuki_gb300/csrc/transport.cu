@@ -18,6 +18,7 @@
 #include "guide_mix.cuh"
 #include "materials.cuh"
 #include "program.cuh"
+#include "sobol.h"
 
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -46,8 +47,14 @@ __device__ __forceinline__ uint64_t dimensionOf(int event, int draw) {
 	return draw < LightU ? uint64_t(draw) : uint64_t(4 + event * 8 + (draw - LightU));
 }
 
-__device__ __forceinline__ float number(uint64_t stream, uint32_t index, int event, int draw) {
-	return unitFrom(hashedBits(stream, index, dimensionOf(event, draw)));
+// plugins/transport/paths/sampler.cpp:16 numberAt: a hashed number, or with
+// the Sobol tables the scrambled Sobol sequence's for the first 28
+// dimensions (a pixel's sample index and its group are the same at one
+// sample a split)
+__device__ __forceinline__ float number(const uint32_t* sobol, uint64_t stream, uint32_t index, int event, int draw) {
+	const uint64_t dimension = dimensionOf(event, draw);
+	if (sobol != nullptr && dimension < kSobolDimensions) return fminf(float(sobolBits(sobol, stream, index, uint32_t(dimension))) * 0x1p-32f, 0x1.fffffep-1f);
+	return unitFrom(hashedBits(stream, index, dimension));
 }
 
 // plugins/transport/paths/trace.cpp:66 pixelNumbers
@@ -347,11 +354,11 @@ __global__ void __launch_bounds__(kBlock) cameraKernel(const __grid_constant__ F
 		float px, py;
 		if (cFrame.factor > 1) {
 			const float factor = float(cFrame.factor);
-			px = float(x) + (float(cFrame.phase % cFrame.factor) + number(stream, sample, 0, PixelX)) / factor;
-			py = float(y) + (float(cFrame.phase / cFrame.factor) + number(stream, sample, 0, PixelY)) / factor;
+			px = float(x) + (float(cFrame.phase % cFrame.factor) + number(cFrame.sobol, stream, sample, 0, PixelX)) / factor;
+			py = float(y) + (float(cFrame.phase / cFrame.factor) + number(cFrame.sobol, stream, sample, 0, PixelY)) / factor;
 		} else {
-			px = float(x) + number(stream, sample, 0, PixelX);
-			py = float(y) + number(stream, sample, 0, PixelY);
+			px = float(x) + number(cFrame.sobol, stream, sample, 0, PixelX);
+			py = float(y) + number(cFrame.sobol, stream, sample, 0, PixelY);
 		}
 		const float u  = 2.0f * px / float(cFrame.width) - 1.0f;
 		const float v  = 1.0f - 2.0f * py / float(cFrame.height);
@@ -628,9 +635,9 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 				const float3 open  = surf.inside ? normal * -1.0f : normal;
 				// aim: offer every lamp, trace one offer drawn by its lane mean
 				if (!m.exact && aimable && cFrame.lampCount > 0) {
-					const float u0   = number(stream, index, depth, LightU);
-					const float v0   = number(stream, index, depth, LightV);
-					float choice     = number(stream, index, depth, Pick);
+					const float u0   = number(cFrame.sobol, stream, index, depth, LightU);
+					const float v0   = number(cFrame.sobol, stream, index, depth, LightV);
+					float choice     = number(cFrame.sobol, stream, index, depth, Pick);
 					float total      = 0.0f, picked = 0.0f;
 					float4 chosen    = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 					float3 chosenDir = make_float3(0.0f, 0.0f, 1.0f);
@@ -669,10 +676,10 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 				}
 				// scatter (trace.cpp:1020 scatteredFrom)
 				if (!capped) {
-					float lobe       = number(stream, index, depth, Lobe);
-					const float side = number(stream, index, depth, Side);
-					const float du   = number(stream, index, depth, DirectionU);
-					const float dv   = number(stream, index, depth, DirectionV);
+					float lobe       = number(cFrame.sobol, stream, index, depth, Lobe);
+					const float side = number(cFrame.sobol, stream, index, depth, Side);
+					const float du   = number(cFrame.sobol, stream, index, depth, DirectionU);
+					const float dv   = number(cFrame.sobol, stream, index, depth, DirectionV);
 					Scatter s;
 					if (lobes != nullptr && lobe < share) {
 						// drawn from the guide: weighed by the mixture's density
@@ -704,7 +711,7 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 						bool alive      = true;
 						if (depth >= 4) {
 							const float survival = fminf(0.95f, max4(carried));
-							if (!(number(stream, index, depth, Survival) < survival)) alive = false;
+							if (!(number(cFrame.sobol, stream, index, depth, Survival) < survival)) alive = false;
 							else carried = scale4(carried, 1.0f / survival);
 						}
 						if (alive) {

@@ -241,7 +241,7 @@ class View(ctypes.Structure):
                 ("zenith", ctypes.c_double * 3), ("horizon", ctypes.c_double * 3), ("ground", ctypes.c_double * 3),
                 ("width", ctypes.c_int32), ("height", ctypes.c_int32), ("spp", ctypes.c_int32), ("surfaces", ctypes.c_int32),
                 ("seed", ctypes.c_int32), ("lamp_count", ctypes.c_uint32), ("material_count", ctypes.c_uint32),
-                ("factor", ctypes.c_uint32), ("phase", ctypes.c_uint32)]
+                ("factor", ctypes.c_uint32), ("phase", ctypes.c_uint32), ("sobol", ctypes.c_uint32)]
 
 
 _trees: dict = {}
@@ -255,11 +255,11 @@ def _octree_for(scene, build: dict) -> "Octree":
 
 
 def render_band(scene, width: int, height: int, spp: int, surfaces: int, seed: int, row0: int, rows: int, threads: int,
-                build: dict | None = None, factor: int = 1, phase: int = 0) -> np.ndarray:
+                build: dict | None = None, factor: int = 1, phase: int = 0, sobol: bool = False) -> np.ndarray:
     """The oracle renderer over rows [row0, row0 + rows) of a frame: summed
     RGB per pixel (rows x width x 3, divide by spp for the means).  With a
     film factor above 1, width x height is the drawn frame and each pixel's
-    samples aim at the shown pixel of `phase`."""
+    samples aim at the shown pixel of `phase`.  `sobol`: --use sampler=sobol."""
     build = build or dict(min_depth=6, max_depth=10, split_steps=96)
     tree = _octree_for(scene, build)
     mats, keep = _materials(scene)
@@ -286,7 +286,7 @@ def render_band(scene, width: int, height: int, spp: int, surfaces: int, seed: i
     v.fov = scene.camera["fov"]
     v.width, v.height, v.spp, v.surfaces, v.seed = width, height, spp, surfaces, seed
     v.lamp_count, v.material_count = nl, n
-    v.factor, v.phase = factor, phase
+    v.factor, v.phase, v.sobol = factor, phase, int(sobol)
     sums = np.zeros((rows, width, 3), np.float64)
     mat_leaf = np.ascontiguousarray(scene.leaf_material, np.uint32)
     L = lib()
@@ -393,6 +393,18 @@ def upscale(width: int, height: int, factor: int, phase: int, moved: bool, kept:
     L.kp_upscale(width, height, factor, phase, int(moved), int(kept), int(settling), _ptr(ln), _ptr(lb), _ptr(internal),
                  _ptr(dist) if dist is not None else None, _ptr(bc), _ptr(bd), _ptr(colour), _ptr(depth), _ptr(image))
     return colour, depth, image
+
+
+def sobol_numbers(stream, index, dimension) -> np.ndarray:
+    """plugins/sampler/sobol/sobol.cpp sobolNumber of (stream, index,
+    dimension) triples (arrays; dimensions below 28)."""
+    L = lib()
+    L.kp_sobol_tables.argtypes = [_P]
+    L.kp_sobol_number.argtypes = [_P, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32]
+    L.kp_sobol_number.restype = ctypes.c_double
+    tables = np.zeros(28 * 512, np.uint32)
+    L.kp_sobol_tables(_ptr(tables))
+    return np.array([L.kp_sobol_number(_ptr(tables), int(s), int(i), int(d)) for s, i, d in zip(stream, index, dimension)])
 
 
 def upsample(width: int, height: int, factor: int, drawn) -> np.ndarray:

@@ -167,6 +167,8 @@ typedef struct kp_view {
 	 * factor above 1 each pixel's samples aim at the shown pixel of the
 	 * phase (plugins/transport/paths/trace.cpp:93 phasedDraw) */
 	uint32_t factor, phase;
+	/* 1: --use sampler=sobol */
+	uint32_t sobol;
 } kp_view;
 
 /*
@@ -240,6 +242,14 @@ void kp_upscale(int width, int height, int factor, int phase, int moved, int kep
  * upsample.cpp upsampledImage): the drawn frame bilinearly to the shown
  * size width x height at a film factor. */
 void kp_upsample(int width, int height, int factor, const float* drawn, float* shown);
+
+/* --use sampler=sobol (spectral.c; plugins/sampler/sobol/sobol.cpp): the
+ * byte tables of the 28 Sobol dimensions (28 x 512 words) and the number of
+ * a dimension below 28 of a pixel stream's sample. */
+#define KP_SOBOL_DIMENSIONS 28
+#define KP_SOBOL_SHARED 6
+void kp_sobol_tables(uint32_t* out);
+double kp_sobol_number(const uint32_t* tables, uint64_t stream, uint32_t index, uint32_t dimension);
 
 uint64_t kp_mixed_bits(uint64_t v);
 double kp_unit_of(uint64_t bits);

@@ -175,3 +175,84 @@ void kp_colour_of(const double nanometres[4], const double density[4], const dou
 	linear_of(x / 4, y / 4, z / 4, lin);
 	for (int c = 0; c < 3; ++c) rgb[c] = lin[c] / white[c];
 }
+
+/* ---- --use sampler=sobol (plugins/sampler/sobol/sobol.cpp): an
+ * Owen-scrambled Sobol sequence for the first 28 dimensions of a path's
+ * draws.  Direction numbers from Joe and Kuo's published primitive
+ * polynomials and initial numbers (dimension 0: van der Corput), the index
+ * shuffled and the points scrambled by the Laine-Karras permutation
+ * (Burley 2020), seeds hashed by Wellons' lowbias32. ---- */
+static uint32_t sobol_stirred(uint32_t v) {
+	v ^= v >> 16;
+	v *= 0x7FEB352DU;
+	v ^= v >> 15;
+	v *= 0x846CA68BU;
+	return v ^ (v >> 16);
+}
+
+static uint32_t sobol_reversed(uint32_t v) {
+	uint32_t r = 0;
+	for (int b = 0; b < 32; ++b) r |= ((v >> b) & 1U) << (31 - b);
+	return r;
+}
+
+static uint32_t sobol_reversed16(uint32_t v) { return sobol_reversed(v & 0xFFFFU) >> 16; }
+
+static uint32_t laine_karras(uint32_t v, uint32_t seed) {
+	v += seed;
+	v ^= v * 0x6C50B47CU;
+	v ^= v * 0xB82F1E52U;
+	v ^= v * 0xC7AFE638U;
+	return v ^ (v * 0x8D22F6E6U);
+}
+
+void kp_sobol_tables(uint32_t* out) {
+	static const int degree[KP_SOBOL_DIMENSIONS] = { 0, 1, 2, 3, 3, 4, 4, 5, 5, 5, 5, 5, 5, 6, 6, 6, 6, 6, 6, 7, 7, 7, 7, 7, 7, 7, 7, 7 };
+	static const int inner[KP_SOBOL_DIMENSIONS] = { 0, 0, 1, 1, 2, 1, 4, 2, 4, 7, 11, 13, 14, 1, 13, 16, 19, 22, 25, 1, 4, 7, 8, 14, 19, 21, 28, 31 };
+	static const uint32_t initial[KP_SOBOL_DIMENSIONS][7] = {
+		{ 1 }, { 1 }, { 1, 3 }, { 1, 3, 1 }, { 1, 1, 1 }, { 1, 1, 3, 3 }, { 1, 3, 5, 13 }, { 1, 1, 5, 5, 17 }, { 1, 1, 5, 5, 5 }, { 1, 1, 7, 11, 19 },
+		{ 1, 1, 5, 1, 1 }, { 1, 1, 1, 3, 11 }, { 1, 3, 5, 5, 31 }, { 1, 3, 3, 9, 7, 49 }, { 1, 1, 1, 15, 21, 21 }, { 1, 3, 1, 13, 27, 49 },
+		{ 1, 1, 1, 15, 7, 5 }, { 1, 3, 1, 15, 13, 25 }, { 1, 1, 5, 5, 19, 61 }, { 1, 3, 7, 11, 23, 15, 103 }, { 1, 3, 7, 13, 13, 15, 69 },
+		{ 1, 1, 3, 13, 7, 35, 63 }, { 1, 3, 5, 9, 1, 25, 53 }, { 1, 3, 1, 13, 9, 35, 107 }, { 1, 3, 1, 5, 27, 61, 31 }, { 1, 1, 5, 11, 19, 41, 61 },
+		{ 1, 3, 5, 3, 3, 13, 69 }, { 1, 1, 7, 13, 1, 19, 1 },
+	};
+	for (int d = 0; d < KP_SOBOL_DIMENSIONS; ++d) {
+		uint32_t m[16];
+		for (int bit = 0; bit < 16; ++bit) {
+			const int s = degree[d];
+			if (s == 0) {
+				m[bit] = 1;
+			} else if (bit < s) {
+				m[bit] = initial[d][bit];
+			} else {
+				/* Bratley and Fox's recurrence */
+				uint32_t v = m[bit - s] ^ (m[bit - s] << s);
+				for (int k = 1; k < s; ++k) {
+					if ((inner[d] >> (s - 1 - k)) & 1) v ^= m[bit - k] << k;
+				}
+				m[bit] = v;
+			}
+		}
+		for (uint32_t byte = 0; byte < 256; ++byte) {
+			uint32_t low = 0, high = 0;
+			for (int bit = 0; bit < 16; ++bit) {
+				const uint32_t column = sobol_reversed(m[bit] << (31 - bit));
+				if (((byte >> bit) & 1U) != 0) low ^= column;
+				if ((((byte << 8) >> bit) & 1U) != 0) high ^= column;
+			}
+			out[d * 512 + byte] = low;
+			out[d * 512 + 256 + byte] = high;
+		}
+	}
+}
+
+/* sobol.cpp:140 sobolNumber: the number of dimension `dimension` (below 28)
+ * of sample `index` of the pixel stream `stream` */
+double kp_sobol_number(const uint32_t* tables, uint64_t stream, uint32_t index, uint32_t dimension) {
+	const uint32_t own = dimension < KP_SOBOL_SHARED ? 0U : 0x68E31DA4U;
+	const uint32_t place = sobol_reversed16(laine_karras(sobol_reversed16(index), sobol_stirred((uint32_t) (stream >> 32) + own)) & 0xFFFFU);
+	const uint32_t seed = sobol_stirred((uint32_t) (stream >> 32) + dimension * 0xA136AAADU + 0x2545F491U);
+	const uint32_t* column = tables + (size_t) (dimension < KP_SOBOL_SHARED ? dimension : dimension - KP_SOBOL_SHARED) * 512;
+	const uint32_t value = column[place & 0xFFU] ^ column[256 + ((place >> 8) & 0xFFU)];
+	return (double) sobol_reversed(laine_karras(value, seed)) * 0x1p-32;
+}

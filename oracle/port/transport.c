@@ -106,8 +106,12 @@ static spec spectrum(const double rgb[3], const lanes* w) {
 /* ---- numbers (trace.cpp:47 drawnNumber, path.cpp:22 dimensionOf) ---- */
 enum { PIXEL_X, PIXEL_Y, LENS_U, LENS_V, LIGHT_U, LIGHT_V, DIRECTION_U, DIRECTION_V, LOBE, SIDE, SURVIVAL, PICK };
 
-static double number(uint64_t stream, uint32_t index, int event, int draw) {
+/* sampler.cpp:16 numberAt: hashed, or with the Sobol tables the scrambled
+ * Sobol sequence's for the first 28 dimensions (a sample's index and its
+ * group are the same at one sample a split) */
+static double number(const uint32_t* sobol, uint64_t stream, uint32_t index, int event, int draw) {
 	const uint64_t dim = draw < LIGHT_U ? (uint64_t) draw : (uint64_t) (4 + event * 8 + (draw - LIGHT_U));
+	if (sobol != NULL && dim < KP_SOBOL_DIMENSIONS) return kp_sobol_number(sobol, stream, index, (uint32_t) dim);
 	return kp_hashed(stream, index, dim);
 }
 
@@ -888,6 +892,7 @@ typedef struct job {
 	uint64_t seed_mix;
 	int absorbs; /* absorption.cpp:18 sceneAbsorbs: some glass absorbs */
 	const double* placements; /* 12 a leaf, or none */
+	const uint32_t* sobol;    /* --use sampler=sobol's tables, or none */
 } job;
 
 /* trace.cpp:179 keptOnLeg with absorption.cpp:28 keptThrough: what a leg of
@@ -1015,8 +1020,8 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 	/* trace.cpp:105 filmDraw, :93 phasedDraw */
 	const int factor = V->factor > 1 ? (int) V->factor : 1;
 	const double column = factor > 1 ? (double) (V->phase % (uint32_t) factor) : 0, row = factor > 1 ? (double) (V->phase / (uint32_t) factor) : 0;
-	const double px = factor > 1 ? x + (column + number(stream, index, 0, PIXEL_X)) / factor : x + number(stream, index, 0, PIXEL_X);
-	const double py = factor > 1 ? y + (row + number(stream, index, 0, PIXEL_Y)) / factor : y + number(stream, index, 0, PIXEL_Y);
+	const double px = factor > 1 ? x + (column + number(J->sobol, stream, index, 0, PIXEL_X)) / factor : x + number(J->sobol, stream, index, 0, PIXEL_X);
+	const double py = factor > 1 ? y + (row + number(J->sobol, stream, index, 0, PIXEL_Y)) / factor : y + number(J->sobol, stream, index, 0, PIXEL_Y);
 	const double u = 2 * px / V->width - 1, v = 1 - 2 * py / V->height;
 	v3 heading = unit(add(add(J->forward, scl(J->right, u * J->reach * J->aspect)), scl(J->up, v * J->reach)));
 	kp_ray ray = ray_of(J->eye, heading, INFINITY, NO_MATERIAL);
@@ -1083,8 +1088,8 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 		const int aimable = medium == NO_MATERIAL || (medium == material && bends);
 		const v3 open = s.inside ? scl(normal, -1) : normal;
 		if (!m->exact && aimable && V->lamp_count > 0) {
-			const double u0 = number(stream, index, depth, LIGHT_U), v0 = number(stream, index, depth, LIGHT_V);
-			double choice = number(stream, index, depth, PICK);
+			const double u0 = number(J->sobol, stream, index, depth, LIGHT_U), v0 = number(J->sobol, stream, index, depth, LIGHT_V);
+			double choice = number(J->sobol, stream, index, depth, PICK);
 			double total = 0, picked = 0, chosen_dist = 0;
 			spec chosen = flat(0);
 			v3 chosen_dir = mk(0, 0, 1);
@@ -1122,7 +1127,7 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 			}
 		}
 		if (capped) break;
-		const scatter sc = sample(&s, out, &w, number(stream, index, depth, LOBE), number(stream, index, depth, SIDE), number(stream, index, depth, DIRECTION_U), number(stream, index, depth, DIRECTION_V), material, medium);
+		const scatter sc = sample(&s, out, &w, number(J->sobol, stream, index, depth, LOBE), number(J->sobol, stream, index, depth, SIDE), number(J->sobol, stream, index, depth, DIRECTION_U), number(J->sobol, stream, index, depth, DIRECTION_V), material, medium);
 		const double side_of = dotv(sc.incoming, normal);
 		const int below = sc.through ? side_of >= 0 : side_of <= 0;
 		if (!sc.found || below) break;
@@ -1134,7 +1139,7 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 		}
 		if (depth >= 4) {
 			const double survival = mind(0.95, smax(carried));
-			if (!(number(stream, index, depth, SURVIVAL) < survival)) break;
+			if (!(number(J->sobol, stream, index, depth, SURVIVAL) < survival)) break;
 			carried = sscale(carried, 1 / survival);
 		}
 		/* trace.cpp:956 aimedAlong: the next leg's meets are weighed against
@@ -1207,10 +1212,17 @@ void kp_render_band(const kp_octree* tree, const uint32_t* leaf_material, const 
 		const kp_material* m = &materials[k];
 		if (m->kind == 3 && (m->absorb[0] > 0 || m->absorb[1] > 0 || m->absorb[2] > 0)) J.absorbs = 1;
 	}
+	uint32_t* sobol = NULL;
+	if (view->sobol) {
+		sobol = (uint32_t*) malloc(sizeof(uint32_t) * KP_SOBOL_DIMENSIONS * 512);
+		kp_sobol_tables(sobol);
+	}
+	J.sobol = sobol;
 	if (threads < 1) threads = 1;
 	pthread_t* pool = (pthread_t*) malloc(sizeof(pthread_t) * (size_t) threads);
 	for (int t = 0; t < threads; ++t) pthread_create(&pool[t], NULL, worker, &J);
 	for (int t = 0; t < threads; ++t) pthread_join(pool[t], NULL);
 	free(pool);
+	free(sobol);
 	pthread_mutex_destroy(&J.lock);
 }

@@ -12,6 +12,7 @@
 //   kdn_ref_dump bsdf  <file.sdf> <in.bin> <out.bin>      respondBsdf, sampleBsdf
 //   kdn_ref_dump upscale  <in.bin> <out.bin>              upscaledFrame
 //   kdn_ref_dump upsample <in.bin> <out.bin>              upsampledImage
+//   kdn_ref_dump sobol    <in.bin> <out.f64>              sobolNumber, sobolPair
 //
 // Reference entry points used: loadScene (syntax/evaluator.cpp:2898),
 // sceneRegion (plugins/geometry/tree/build.cpp:405), sphereTraced
@@ -24,6 +25,7 @@
 #include "plugins/reconstruction/atrous/atrous.h"
 #include "plugins/reconstruction/temporal/temporal.h"
 #include "plugins/reconstruction/upsample/upsample.h"
+#include "plugins/sampler/sobol/sobol.h"
 #include "plugins/reconstruction/upscale/upscale.h"
 #include "plugins/transport/paths/material/material.h"
 #include "sdf/program.h"
@@ -665,6 +667,30 @@ int dumpUpsample(const char* inPath, const char* outPath) {
 	return 0;
 }
 
+// plugins/sampler/sobol/sobol.cpp sobolNumber and sobolPair of keys.
+// Input records: uint64 stream, uint32 index, uint32 coordinate (below
+// sobolDimensions).  Output per record: double sobolNumber, then the pair
+// of the coordinate rounded down to even (its first and second number).
+int dumpSobol(const char* inPath, const char* outPath) {
+	FILE* in  = std::fopen(inPath, "rb");
+	FILE* out = std::fopen(outPath, "wb");
+	if (in == nullptr || out == nullptr) return 1;
+	for (;;) {
+		std::uint64_t stream;
+		std::uint32_t index[2];
+		if (std::fread(&stream, 8, 1, in) != 1 || std::fread(index, 4, 2, in) != 2) break;
+		const math::Key key = { .stream = stream, .index = index[0], .coordinate = index[1] };
+		const math::Key even = { .stream = stream, .index = index[0], .coordinate = index[1] & ~std::uint64_t(1) };
+		const double number       = sobolNumber(key);
+		const math::UnitPair pair = sobolPair(even);
+		const double values[3]    = { number, pair.u, pair.v };
+		std::fwrite(values, 8, 3, out);
+	}
+	std::fclose(in);
+	std::fclose(out);
+	return 0;
+}
+
 } // namespace
 
 // respondBsdf and sampleBsdf (plugins/transport/paths/material/material.cpp
@@ -748,6 +774,9 @@ int main(int argc, char** argv) {
 	if (argc >= 4 && std::strcmp(argv[1], "temporal") == 0) {
 		return dumpTemporal(argv[2], argv[3]);
 	}
+	if (argc >= 4 && std::strcmp(argv[1], "sobol") == 0) {
+		return dumpSobol(argv[2], argv[3]);
+	}
 	if (argc >= 4 && std::strcmp(argv[1], "upsample") == 0) {
 		return dumpUpsample(argv[2], argv[3]);
 	}
@@ -772,6 +801,6 @@ int main(int argc, char** argv) {
 	if (argc >= 5 && std::strcmp(argv[1], "cells") == 0) {
 		return dumpCells(argv[2], argv[3], argv[4]);
 	}
-	std::fprintf(stderr, "usage: kdn_ref_dump scene|trace|cut|cells|bsdf|denoise|temporal|upscale|upsample ...\n");
+	std::fprintf(stderr, "usage: kdn_ref_dump scene|trace|cut|cells|bsdf|denoise|temporal|upscale|upsample|sobol ...\n");
 	return 2;
 }

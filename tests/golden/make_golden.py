@@ -57,6 +57,9 @@ def region_flags(scene: Scene) -> list[str]:
 IMAGES = {"room_small": (16, 64), "c1_small": (16, 64), "c2_small": (16, 64), "glow_small": (16, 64), "glass_small": (16, 64), "patterns_small": (16, 64), "rough_small": (16, 64),
           "films_small": (16, 64)}
 
+# the scenes whose reference frames are also drawn with --use sampler=sobol
+SOBOL_IMAGES = ("c1_small", "glass_small")
+
 # name -> (generator, kwargs, trace rays, cut depth)
 SCENES = {
     "c1": (scenegen.scene_config1, dict(seed=1), 2000, 4),
@@ -159,19 +162,22 @@ def read_pfm(path: str) -> np.ndarray:
     return a[::-1].copy()
 
 
-def reference_images(render: str, sdf: str, name: str, tmp: str, scene: Scene) -> None:
+def reference_images(render: str, sdf: str, name: str, tmp: str, scene: Scene, sampler: str = "none") -> None:
     """Frames of the reference renderer at fixed spp under independent seeds:
-    their per-pixel mean and the standard error of one seed's frame."""
+    their per-pixel mean and the standard error of one seed's frame; with
+    `sampler` "sobol", drawn with --use sampler=sobol (image_<name>_sobol.npz)."""
     seeds, spp = IMAGES[name]
+    flags = [f if f != "sampler=none" else f"sampler={sampler}" for f in IMAGE_FLAGS]
+    suffix = "" if sampler == "none" else f"_{sampler}"
     frames = []
     for k in range(seeds):
         pfm = os.path.join(tmp, f"{name}_{k}.pfm")
         subprocess.run([render, sdf, "--out", os.path.join(tmp, f"{name}_{k}.ppm"), "--pfm", pfm, "--seed", str(1000 + k),
-                        "--samples", str(spp)] + IMAGE_FLAGS + region_flags(scene), check=True, capture_output=True)
+                        "--samples", str(spp)] + flags + region_flags(scene), check=True, capture_output=True)
         frames.append(read_pfm(pfm))
     f = np.stack(frames)
-    np.savez_compressed(os.path.join(HERE, f"image_{name}.npz"), frames=f.astype(np.float32), spp=spp, seeds=np.arange(1000, 1000 + seeds))
-    print(" image", f.shape, "mean", f.mean(axis=(0, 1, 2)))
+    np.savez_compressed(os.path.join(HERE, f"image_{name}{suffix}.npz"), frames=f.astype(np.float32), spp=spp, seeds=np.arange(1000, 1000 + seeds))
+    print(" image", suffix, f.shape, "mean", f.mean(axis=(0, 1, 2)))
 
 
 # name -> (seeds, spp) of reference frames drawn at the scene's own size on
@@ -457,6 +463,26 @@ def upscale_fixture(dump: str, tmp: str) -> None:
     np.savez_compressed(os.path.join(HERE, "upscale.npz"), **out)
 
 
+def sobol_fixture(dump: str, tmp: str) -> None:
+    """tests/golden/sobol.npz: the reference's sobolNumber and sobolPair
+    (plugins/sampler/sobol/sobol.cpp) of 20000 seeded keys: streams of 64
+    random bits, sample indices below 2^17 (past the 16 bits the sequence's
+    place keeps), coordinates below 28."""
+    rng = np.random.default_rng(28)
+    n = 20000
+    keys = np.zeros(n, [("stream", "<u8"), ("index", "<u4"), ("coordinate", "<u4")])
+    keys["stream"] = rng.integers(0, 2 ** 63, n, dtype=np.uint64) * 2 + rng.integers(0, 2, n, dtype=np.uint64)
+    keys["index"] = rng.integers(0, 1 << 17, n)
+    keys["coordinate"] = rng.integers(0, 28, n)
+    path, res = os.path.join(tmp, "sobol.bin"), os.path.join(tmp, "sobol.out")
+    keys.tofile(path)
+    subprocess.run([dump, "sobol", path, res], check=True)
+    values = np.fromfile(res, "<f8").reshape(n, 3)
+    np.savez_compressed(os.path.join(HERE, "sobol.npz"), stream=keys["stream"], index=keys["index"], coordinate=keys["coordinate"],
+                        number=values[:, 0], pair=values[:, 1:])
+    print(" sobol keys", n)
+
+
 def upsample_fixture(dump: str, tmp: str) -> None:
     """tests/golden/upsample.npz: the reference's upsampledImage
     (plugins/reconstruction/upsample/upsample.cpp) of seeded drawn frames at
@@ -546,6 +572,8 @@ def main() -> None:
         upscale_fixture(dump, tmp)
     if args.only in (None, "upsample"):
         upsample_fixture(dump, tmp)
+    if args.only in (None, "sobol"):
+        sobol_fixture(dump, tmp)
     if args.only in (None, "cutdeep"):
         deep_cut_fixture(dump, tmp)
     for name, (gen, kw, nrays, depth) in SCENES.items():
@@ -560,6 +588,8 @@ def main() -> None:
         print(name, "programs", scene.program_count, "steps", len(scene.steps))
         if name in IMAGES:
             reference_images(render, sdf, name, tmp, scene)
+        if name in SOBOL_IMAGES:
+            reference_images(render, sdf, name, tmp, scene, sampler="sobol")
         if name in SIZED_IMAGES:
             reference_sized_images(render, sdf, name, tmp, scene)
         if nrays:

@@ -145,3 +145,30 @@ def test_bad_patterns_are_refused(backend):
     assert e.value.status == K.KDN_NOT_READY
     backend.upload("looks.placements", blocks["looks.placements"])
     assert np.isfinite(backend.render(8, 8, 1)).all()
+
+
+@pytest.mark.parametrize("name", ["c1_small", "glass_small"])
+def test_sobol_frame_matches_oracle_and_reference(backend, name):
+    """KDN_FRAME_SOBOL (--use sampler=sobol): the GPU's frames against the
+    oracle's drawn with the same Sobol numbers and against the reference's
+    own frames drawn so (tests/golden/image_<name>_sobol.npz), to the bars
+    of the frame test above."""
+    import oracle.port as op
+    sc = scene(name)
+    ref = np.load(os.path.join(GOLDEN, f"image_{name}_sobol.npz"))
+    frames = ref["frames"].astype(np.float64)
+    spp = int(ref["spp"])
+    surfaces = int(sc.render["surfaces"])
+    build = dict(min_depth=5, max_depth=10, split_steps=64)
+    backend.load(sc)
+    backend.build(**build)
+    h, w = sc.render["height"], sc.render["width"]
+    got = np.stack([backend.render(w, h, spp, surfaces=surfaces, seed=s, sobol=True) for s in SEEDS]).astype(np.float64)
+    oracle = np.stack([op.render_band(sc, w, h, spp, surfaces, s, 0, h, os.cpu_count() or 4, build, sobol=True) / spp for s in SEEDS])
+    far_o, cz_o, g_mean, o_mean = compare(got, oracle)
+    far_r, cz_r, _, r_mean = compare(got, frames)
+    print(f"{name} sobol: gpu {g_mean} oracle {o_mean} reference {r_mean}; vs oracle z {cz_o} px {far_o:.4f}; vs reference rel {g_mean / r_mean - 1} px {far_r:.4f}")
+    assert far_o <= 0.01
+    assert np.all(np.abs(cz_o) < 3)
+    assert np.all(np.abs(g_mean / r_mean - 1) < 0.005)
+    assert far_r <= 0.015

@@ -124,3 +124,42 @@ def test_bsdf_matches_reference_answers(name):
         kinds = np.asarray(scene(name).materials["kind"])[d["ids"][:, 0]]
         spread = d["weight"].max(1) - d["weight"].min(1)
         assert (spread[(kinds == 3) & drawn] > 1e-2).sum() > 200
+
+
+def test_sobol_numbers_match_reference():
+    """plugins/sampler/sobol/sobol.cpp sobolNumber of 20000 seeded keys
+    (tests/golden/sobol.npz: the reference's own numbers, streams of 64
+    bits, indices past 2^16, every coordinate below 28), and its pairs,
+    to the bit."""
+    z = np.load(os.path.join(GOLDEN, "sobol.npz"))
+    got = op.sobol_numbers(z["stream"], z["index"], z["coordinate"])
+    assert np.array_equal(got, z["number"])
+    even = z["coordinate"] & np.uint32(0xFFFFFFFE)
+    assert np.array_equal(op.sobol_numbers(z["stream"], z["index"], even), z["pair"][:, 0])
+    assert np.array_equal(op.sobol_numbers(z["stream"], z["index"], even + 1), z["pair"][:, 1])
+
+
+@pytest.mark.parametrize("name", ["c1_small", "glass_small"])
+def test_sobol_frames_match_reference(name):
+    """The oracle drawing with --use sampler=sobol against the reference's
+    own frames drawn so (tests/golden/image_<name>_sobol.npz, 16 seeds at 64
+    spp), to the bar of the other frame tests; and the scrambled sequence
+    does what it is for: the frames' variance across seeds is below the
+    independent numbers' (the reference's frames of each kind)."""
+    sc = scene(name)
+    ref = np.load(os.path.join(GOLDEN, f"image_{name}_sobol.npz"))
+    frames = ref["frames"].astype(np.float64)
+    spp = int(ref["spp"])
+    h, w = sc.render["height"], sc.render["width"]
+    build = dict(min_depth=5, max_depth=10, split_steps=64)
+    got = np.stack([op.render_band(sc, w, h, spp, int(sc.render["surfaces"]), s, 0, h, os.cpu_count() or 4, build, sobol=True) / spp
+                    for s in range(1, 9)])
+    z = (got.mean(0) - frames.mean(0)) / np.sqrt(got.var(0, ddof=1) / len(got) + frames.var(0, ddof=1) / len(frames) + 1e-12)
+    ca, cb = got.mean(axis=(1, 2)), frames.mean(axis=(1, 2))
+    cz = (ca.mean(0) - cb.mean(0)) / np.sqrt(ca.var(0, ddof=1) / len(ca) + cb.var(0, ddof=1) / len(cb))
+    plain = np.load(os.path.join(GOLDEN, f"image_{name}.npz"))["frames"].astype(np.float64)
+    gain = plain.var(0, ddof=1).mean() / frames.var(0, ddof=1).mean()
+    print(f"{name} sobol: oracle {ca.mean(0)} reference {cb.mean(0)} z {cz} far px {(np.abs(z) > 3).mean():.4f}; variance gain over independent {gain:.2f}")
+    assert np.all(np.abs(cz) < 4)
+    assert (np.abs(z) > 3).mean() <= 0.015
+    assert gain > 1.0
