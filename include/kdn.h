@@ -241,6 +241,12 @@ typedef struct kdn_frame {
  * (plugins/transport/paths/sampler.cpp:16 numberAt), the rest hashed as
  * without it. */
 #define KDN_FRAME_SOBOL 16u
+/* --use sampler=sky_map (plugins/sampler/sky_map): the sky aimed at as a
+ * light after the lamps, by a chart of its brightness (64 x 128 cells of
+ * equal solid angle, a tenth of the draws uniform), unless the lamps
+ * outshine it five times over at the region's middle; a path that meets
+ * the sky weighs it against that aim. */
+#define KDN_FRAME_SKY_MAP 32u
 
 /* Device times of the last kdn_render, from CUDA events on the context's stream. */
 typedef struct kdn_frame_stats {

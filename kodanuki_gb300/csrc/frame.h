@@ -112,6 +112,9 @@ struct FrameConstants {
 	// --use sampler=sobol: the Sobol byte tables (sobol.h), or null for
 	// independent numbers
 	const uint32_t* sobol;
+	// --use sampler=sky_map: the sky's chart (skymap.h), or null where the
+	// sky is only met
+	const double* skyChart;
 	float zenith[3], horizon[3], ground[3];
 	DeviceLamp lamps[kMaxLamps];
 	SpectralTables spectral;

@@ -7,6 +7,7 @@
 // synchronisation.  Pixel sums are kept in double on the device and persist
 // across calls (progressive accumulation) until a call starts afresh.
 #include "context.h"
+#include "skymap.h"
 #include "sobol.h"
 #include "temporal.h"
 #include "upscale.h"
@@ -44,6 +45,7 @@ struct FrameState {
 	// and the upscale member's state twice (colour and depth a shown pixel)
 	DeviceBuffer internal, upState[2];
 	UpscaleScratch upscale;
+	DeviceBuffer skyChart; // --use sampler=sky_map's chart of the frame
 	DeviceBuffer guideLobes, guideRecords; // the learned guide's, a lane's capacity each
 	uint32_t capacity = 0;
 	int32_t width = 0, height = 0;
@@ -73,7 +75,7 @@ struct FrameState {
 void Context::releaseFrame() {
 	if (frame == nullptr) return;
 	FrameState& f = *frame;
-	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.queueCarry[0], &f.queueCarry[1], &f.hits, &f.states, &f.counts, &f.shadowPaths[0], &f.shadowPaths[1], &f.shadowContribution[0], &f.shadowContribution[1], &f.surfacePaths, &f.surfaceRays, &f.surfaceStates, &f.surfaceHits, &f.sums, &f.out, &f.materials, &f.patternSteps, &f.stops, &f.placements, &f.boundaries, &f.frameLight, &f.firstDistance, &f.firstNormal, &f.firstAlbedo, &f.firstLeaf, &f.gDistance[0], &f.gDistance[1], &f.gNormal[0], &f.gNormal[1], &f.gAlbedo[0], &f.gAlbedo[1], &f.gLeaf[0], &f.gLeaf[1], &f.tColour[0], &f.tColour[1], &f.tMoment[0], &f.tMoment[1], &f.tLength[0], &f.tLength[1], &f.internal, &f.upState[0], &f.upState[1], &f.upscale.samples, &f.upscale.axes, &f.guideLobes, &f.guideRecords }) {
+	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.queueCarry[0], &f.queueCarry[1], &f.hits, &f.states, &f.counts, &f.shadowPaths[0], &f.shadowPaths[1], &f.shadowContribution[0], &f.shadowContribution[1], &f.surfacePaths, &f.surfaceRays, &f.surfaceStates, &f.surfaceHits, &f.sums, &f.out, &f.materials, &f.patternSteps, &f.stops, &f.placements, &f.boundaries, &f.frameLight, &f.firstDistance, &f.firstNormal, &f.firstAlbedo, &f.firstLeaf, &f.gDistance[0], &f.gDistance[1], &f.gNormal[0], &f.gNormal[1], &f.gAlbedo[0], &f.gAlbedo[1], &f.gLeaf[0], &f.gLeaf[1], &f.tColour[0], &f.tColour[1], &f.tMoment[0], &f.tMoment[1], &f.tLength[0], &f.tLength[1], &f.internal, &f.upState[0], &f.upState[1], &f.upscale.samples, &f.upscale.axes, &f.skyChart, &f.guideLobes, &f.guideRecords }) {
 		if (b->ptr) cudaFree(b->ptr);
 		b->ptr   = nullptr;
 		b->bytes = 0;
@@ -431,6 +433,40 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 			if (!ctx->check(cudaStreamSynchronize(ctx->stream), "sobol tables")) return KDN_CUDA_ERROR;
 		}
 		c.sobol = static_cast<const uint32_t*>(ctx->sobolTables.ptr);
+	}
+	c.skyChart = nullptr;
+	if (fr->flags & KDN_FRAME_SKY_MAP) {
+		// plugins/sampler/sky_map/plugin.cpp:15 chartedSkyPrepared: charted
+		// each frame from the sky, the lamps and the region's middle
+		SkyGradient g {};
+		if (!skies.empty()) {
+			for (int k = 0; k < 3; ++k) {
+				g.zenith[k]  = skies[0].zenith[k];
+				g.horizon[k] = skies[0].horizon[k];
+				g.ground[k]  = skies[0].ground[k];
+			}
+		}
+		std::vector<ChartLamp> chartLamps(lights.size());
+		for (size_t k = 0; k < lights.size(); ++k) {
+			chartLamps[k].kind = lights[k].kind;
+			for (int a = 0; a < 3; ++a) {
+				chartLamps[k].at[a]     = lights[k].at[a];
+				chartLamps[k].along[a]  = lights[k].along[a];
+				chartLamps[k].across[a] = lights[k].across[a];
+				chartLamps[k].power[a]  = lights[k].power[a];
+			}
+		}
+		const std::vector<kdn_region> region = ctx->block<kdn_region>("geometry.region");
+		double middle[3] = { 0, 0, 0 };
+		if (!region.empty()) {
+			for (int a = 0; a < 3; ++a) middle[a] = region[0].lower[a] + 0.5 * region[0].size[a];
+		}
+		std::vector<double> chart(kChartDoubles);
+		if (buildSkyChart(g, chartLamps.data(), uint32_t(chartLamps.size()), middle, chart.data())) {
+			if ((s = ctx->upload(f.skyChart, chart.data(), chart.size() * sizeof(double))) != KDN_OK) return s;
+			if (!ctx->check(cudaStreamSynchronize(ctx->stream), "sky chart")) return KDN_CUDA_ERROR;
+			c.skyChart = static_cast<const double*>(f.skyChart.ptr);
+		}
 	}
 	c.seedMix       = mixedBits(uint64_t(int64_t(fr->seed)));
 	c.surfaces      = fr->surfaces;

@@ -18,6 +18,7 @@
 #include "guide_mix.cuh"
 #include "materials.cuh"
 #include "program.cuh"
+#include "skymap.h"
 #include "sobol.h"
 
 #include <cuda_fp16.h>
@@ -55,6 +56,15 @@ __device__ __forceinline__ float number(const uint32_t* sobol, uint64_t stream, 
 	const uint64_t dimension = dimensionOf(event, draw);
 	if (sobol != nullptr && dimension < kSobolDimensions) return fminf(float(sobolBits(sobol, stream, index, uint32_t(dimension))) * 0x1p-32f, 0x1.fffffep-1f);
 	return unitFrom(hashedBits(stream, index, dimension));
+}
+
+// the hashed number of a dimension past the per-event draws: path.cpp:22
+// dimensionOf's plain draws, five an event from 2^20 (MixturePart,
+// MixtureLump, AimPart, AimJitterU, AimJitterV)
+constexpr uint64_t kPlainFirst = uint64_t(1) << 20;
+enum PlainDraw : int { AimPart = 2, AimJitterU = 3, AimJitterV = 4 };
+__device__ __forceinline__ float plainNumber(uint64_t stream, uint32_t index, int event, int draw) {
+	return unitFrom(hashedBits(stream, index, kPlainFirst + uint64_t(event) * 5u + uint64_t(draw)));
 }
 
 // plugins/transport/paths/trace.cpp:66 pixelNumbers
@@ -291,6 +301,37 @@ __device__ bool meetLamp(const DeviceLamp& l, float3 origin, float3 dir, float l
 }
 
 // light.cpp:575 gradientColour
+__device__ float3 skyColour(const FrameConstants& cFrame, float3 dir);
+
+// sky_map.cpp:138 chartedDirection, :144 chartAim: a direction drawn from the
+// sky's chart (or, a tenth of the time, uniformly), its density and the
+// sky's radiance there over it
+__device__ Aim aimSky(const FrameConstants& cFrame, float u, float v, float part, float jitterU, float jitterV) {
+	const double* chart = cFrame.skyChart;
+	float height, turn;
+	if (double(part) < kChartEven) {
+		height = 1.0f - 2.0f * u;
+		turn   = 2.0f * 3.14159265358979f * v;
+	} else {
+		const int row    = chartFound(chart, kChartRows, double(u));
+		const int column = chartFound(chart + kChartRows + 1 + row * kChartCells, kChartColumns, double(v));
+		height           = -1.0f + (float(row) + jitterU) * (2.0f / kChartRows);
+		turn             = (float(column) + jitterV) * (2.0f * 3.14159265358979f / kChartColumns);
+	}
+	const float across = sqrtf(fmaxf(1.0f - height * height, 0.0f));
+	float3 toward      = make_float3(across * cosf(turn), across * sinf(turn), height);
+	const float size   = sqrtf(toward.x * toward.x + toward.y * toward.y + toward.z * toward.z);
+	toward             = make_float3(toward.x / size, toward.y / size, toward.z / size);
+	Aim a;
+	a.toward         = toward;
+	a.distance       = __int_as_float(0x7f800000);
+	a.density        = float(chartDensity(chart, toward.x, toward.y, toward.z));
+	a.found          = a.density > 0.0f;
+	const float3 sky = skyColour(cFrame, toward);
+	a.arriving       = a.found ? make_float3(sky.x / a.density, sky.y / a.density, sky.z / a.density) : make_float3(0.0f, 0.0f, 0.0f);
+	return a;
+}
+
 __device__ float3 skyColour(const FrameConstants& cFrame, float3 dir) {
 	const float height = dir.z;
 	const float3 far   = height >= 0.0f ? f3(cFrame.zenith) : f3(cFrame.ground);
@@ -590,8 +631,15 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 				A.firstAlbedo[3 * px + 2] = __half_as_ushort(__float2half_rn(albedo.z));
 			}
 			if (!found) {
+				// the sky met, weighed against aiming at it by its chart
+				// (trace.cpp:294 meetAimDensity, sampler.cpp:344 aimDensityAt)
 				const float3 sky = skyColour(cFrame, heading);
-				R                = add4(R, mul4(mul4(T, keptOver(__int_as_float(0x7f800000))), spectrumOf(sky.x, sky.y, sky.z, nm)));
+				float w          = 1.0f;
+				if (drawnDensity > 0.0f && cFrame.skyChart != nullptr) {
+					const float pa = float(chartDensity(cFrame.skyChart, heading.x, heading.y, heading.z));
+					w              = drawnDensity * drawnDensity / (drawnDensity * drawnDensity + pa * pa);
+				}
+				R = add4(R, scale4(mul4(mul4(T, keptOver(__int_as_float(0x7f800000))), spectrumOf(sky.x, sky.y, sky.z, nm)), w));
 			} else {
 				const uint32_t material = hit.leaf < A.looks.leafCount ? A.looks.leafMaterial[hit.leaf] : 0u;
 				const DeviceMaterial& m = A.looks.materials[material < cFrame.materialCount ? material : 0u];
@@ -633,8 +681,10 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 				const float* lobes = (A.lobes != nullptr && depth < kGuideDepth && guidable(m.kind)) ? A.lobes + size_t(q) * kGuideLobeFloats : nullptr;
 				const float share  = A.guideShare;
 				const float3 open  = surf.inside ? normal * -1.0f : normal;
-				// aim: offer every lamp, trace one offer drawn by its lane mean
-				if (!m.exact && aimable && cFrame.lampCount > 0) {
+				// aim: offer every lamp and a charted sky (the light after the
+				// lamps, sampler.cpp:312 skyAim), trace one offer drawn by its
+				// lane mean
+				if (!m.exact && aimable && (cFrame.lampCount > 0 || cFrame.skyChart != nullptr)) {
 					const float u0   = number(cFrame.sobol, stream, index, depth, LightU);
 					const float v0   = number(cFrame.sobol, stream, index, depth, LightV);
 					float choice     = number(cFrame.sobol, stream, index, depth, Pick);
@@ -642,8 +692,10 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 					float4 chosen    = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 					float3 chosenDir = make_float3(0.0f, 0.0f, 1.0f);
 					float chosenDist = 0.0f;
-					for (uint32_t k = 0; k < cFrame.lampCount; ++k) {
-						const Aim a = aimLamp(cFrame.lamps[k], point, u0, v0);
+					for (uint32_t k = 0; k < cFrame.lampCount + (cFrame.skyChart != nullptr ? 1u : 0u); ++k) {
+						const Aim a = k < cFrame.lampCount ? aimLamp(cFrame.lamps[k], point, u0, v0)
+						                                   : aimSky(cFrame, u0, v0, plainNumber(stream, index, depth, AimPart), plainNumber(stream, index, depth, AimJitterU),
+						                                            plainNumber(stream, index, depth, AimJitterV));
 						if (!a.found) continue;
 						const float facing = dot3(open, a.toward);
 						if (facing <= 0.0f || a.distance <= 0.0f) continue;

@@ -365,6 +365,32 @@ def scene_config5(seed: int = 1, width: int = 3840, height: int = 2160, samples:
     return "".join(out)
 
 
+def scene_skylit(seed: int = 1, width: int = 256, height: int = 256, samples: int = 16, surfaces: int = 8, count: int = 12) -> str:
+    """Lit by the sky: config-1 primitives (plastics and metals) on a
+    plastic ground under a bright gradient sky (blue zenith, white horizon,
+    dark ground) and one dim quad lamp that does not outshine it, so that
+    --use sampler=sky_map charts the sky."""
+    rng = random.Random(seed)
+    out = [_header(width, height, samples, surfaces, seed, [0.0, -8.5, 3.2], [0.0, 0.0, -0.6], 0.75)]
+    out.append("sky gradient {\n\tzenith  = [0.6, 0.8, 1.4];\n\thorizon = [1.0, 1.0, 1.0];\n\tground  = [0.15, 0.13, 0.1];\n}\n\n")
+    out.append(_quad([-0.5, 0.5, 4.5], [1.0, 0.0, 0.0], [0.0, -1.0, 0.0], blackbody_rgb(5000.0, 8.0)))
+    out.append("paint(plastic([0.5, 0.5, 0.5], roughness = 0.5)) plane([0, 0, 1], -2.2);\n\n")
+    out.append("merge(0.05) {\n")
+    for k in range(count):
+        pos = [rng.uniform(-2.0, 2.0) for _ in range(3)]
+        if k % 3 == 2:
+            mat = f"metal({_v([rng.uniform(0.5, 0.95) for _ in range(3)])}, roughness = {_f(rng.uniform(0.1, 0.4))})"
+        else:
+            mat = f"plastic({_v([rng.uniform(0.2, 0.8) for _ in range(3)])}, roughness = {_f(rng.uniform(0.1, 0.5))})"
+        if rng.random() < 0.5:
+            shape = f"sphere({_f(rng.uniform(0.25, 0.6))})"
+        else:
+            shape = f"box({_v([2 * rng.uniform(0.15, 0.45) for _ in range(3)])}, 0.02)"
+        out.append(f"\tpaint({mat}) at({_v(pos)}) {shape};\n")
+    out.append("}\n")
+    return "".join(out)
+
+
 _PATTERNS = """function bands(count) {
 	return 0.5 + 0.5 * sin(p.z * count);
 }

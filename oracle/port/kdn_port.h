@@ -169,6 +169,10 @@ typedef struct kp_view {
 	uint32_t factor, phase;
 	/* 1: --use sampler=sobol */
 	uint32_t sobol;
+	/* 1: --use sampler=sky_map, charted against the lamps at `middle`, the
+	 * middle of the scene's region */
+	uint32_t sky_map;
+	double middle[3];
 } kp_view;
 
 /*

@@ -847,6 +847,95 @@ static scatter sample(const shading* s, v3 out, const lanes* w, double lobe, dou
 	return o;
 }
 
+/* ---- --use sampler=sky_map (plugins/sampler/sky_map/sky_map.cpp): the
+ * sky aimed at by a chart of its brightness, 64 rows of equal height by
+ * 128 columns of equal turn (the sky's up is +z, so level and aside are +x
+ * and +y), a tenth of the draws uniform; uncharted where the lamps outshine
+ * it five times over at the region's middle ---- */
+#define CHART_ROWS 64
+#define CHART_COLUMNS 128
+#define CHART_EVEN 0.1
+#define CHART_DOUBLES (CHART_ROWS + 1 + CHART_ROWS * (CHART_COLUMNS + 1))
+
+/* light.cpp:582 gradientColour's channel mean at a height */
+static double sky_brightness(const kp_view* V, double height) {
+	const double* far = height >= 0 ? V->zenith : V->ground;
+	const double share = sqrt(fabs(height));
+	double mean = 0;
+	for (int c = 0; c < 3; ++c) mean += V->horizon[c] * (1 - share) + far[c] * share;
+	return maxd(mean / 3, 0.0);
+}
+
+/* sky_map.cpp:99 chartedSky; 0 where the sky stays uncharted */
+static int sky_chart(const kp_view* V, const kp_lamp* lamps, double* chart) {
+	const double row_height = 2.0 / CHART_ROWS;
+	double* weights = (double*) malloc(sizeof(double) * CHART_ROWS * CHART_COLUMNS);
+	double total = 0;
+	for (int row = 0; row < CHART_ROWS; ++row) {
+		const double height = -1 + (row + 0.5) * row_height;
+		for (int column = 0; column < CHART_COLUMNS; ++column) weights[row * CHART_COLUMNS + column] = sky_brightness(V, height);
+	}
+	for (int k = 0; k < CHART_ROWS * CHART_COLUMNS; ++k) total += weights[k];
+	if (!(total > 0)) {
+		free(weights);
+		return 0;
+	}
+	double* rows = chart;
+	double* cells = chart + CHART_ROWS + 1;
+	rows[0] = 0;
+	for (int row = 0; row < CHART_ROWS; ++row) {
+		double* run = cells + row * (CHART_COLUMNS + 1);
+		run[0] = 0;
+		for (int column = 0; column < CHART_COLUMNS; ++column) run[column + 1] = run[column] + weights[row * CHART_COLUMNS + column];
+		const double held = run[CHART_COLUMNS];
+		for (int column = 1; column <= CHART_COLUMNS; ++column) run[column] = held > 0 ? run[column] / held : (double) column / CHART_COLUMNS;
+		rows[row + 1] = rows[row] + held / total;
+	}
+	rows[CHART_ROWS] = 1;
+	free(weights);
+	const double brightness = total / (double) (CHART_ROWS * CHART_COLUMNS);
+	/* sky_map.cpp:83 lampSent, :94 outshone */
+	double lit = 0;
+	for (uint32_t k = 0; k < V->lamp_count; ++k) {
+		const kp_lamp* l = &lamps[k];
+		double apart = 0;
+		for (int a = 0; a < 3; ++a) {
+			const double place = l->kind == 3 ? l->at[a] + (l->along[a] + l->across[a]) * 0.5 : l->at[a];
+			const double d = place - V->middle[a];
+			apart += d * d;
+		}
+		const double mean = maxd((l->power[0] + l->power[1] + l->power[2]) / 3, 0.0);
+		const double emitted = (l->kind == 3 ? PI : 4 * PI) * mean;
+		lit += emitted / (4 * PI * maxd(apart, 1e-12));
+	}
+	return !(lit > 5 * 4 * PI * brightness);
+}
+
+/* sky_map.cpp:153 chartDensity */
+static double chart_density(const double* chart, v3 t) {
+	const double row_height = 2.0 / CHART_ROWS, column_width = 2 * PI / CHART_COLUMNS;
+	const double height = clampd(t.z, -1.0, 1.0);
+	const double angle = atan2(t.y, t.x);
+	const double turn = angle < 0 ? angle + 2 * PI : angle;
+	size_t row = (size_t) ((height + 1) / row_height), column = (size_t) (turn / column_width);
+	if (row > CHART_ROWS - 1) row = CHART_ROWS - 1;
+	if (column > CHART_COLUMNS - 1) column = CHART_COLUMNS - 1;
+	const double* run = chart + CHART_ROWS + 1 + row * (CHART_COLUMNS + 1);
+	const double held = (chart[row + 1] - chart[row]) * (run[column + 1] - run[column]);
+	return CHART_EVEN / (4 * PI) + (1 - CHART_EVEN) * held / (row_height * column_width);
+}
+
+/* sky_map.cpp:131 foundIn (std::upper_bound over run[1..count]) */
+static int chart_found(const double* run, int count, double target) {
+	int lo = 0, hi = count;
+	while (lo < hi) {
+		const int mid = (lo + hi) / 2;
+		if (target < run[1 + mid]) hi = mid;
+		else lo = mid + 1;
+	}
+	return lo < count - 1 ? lo : count - 1;
+}
+
 /* respondBsdf and sampleBsdf (material.cpp:1076, :1366) at chosen
  * vertices, for the known-answer test against the reference's own: per
  * record ids (material, medium) and 17 doubles (albedo[3], normal[3],
@@ -893,6 +982,7 @@ typedef struct job {
 	int absorbs; /* absorption.cpp:18 sceneAbsorbs: some glass absorbs */
 	const double* placements; /* 12 a leaf, or none */
 	const uint32_t* sobol;    /* --use sampler=sobol's tables, or none */
+	const double* chart;      /* --use sampler=sky_map's chart, or none (the sky only met) */
 } job;
 
 /* trace.cpp:179 keptOnLeg with absorption.cpp:28 keptThrough: what a leg of
@@ -926,6 +1016,35 @@ static void sky_colour(const kp_view* view, v3 d, double out[3]) {
 	const double* far = h >= 0 ? view->zenith : view->ground;
 	const double share = sqrt(fabs(h));
 	for (int c = 0; c < 3; ++c) out[c] = view->horizon[c] * (1 - share) + far[c] * share;
+}
+
+/* sky_map.cpp:138 chartedDirection, :144 chartAim: a direction from the
+ * sky's chart (or a tenth of the time uniformly), its density and the sky's
+ * radiance there over it */
+static aim aim_sky(const kp_view* V, const double* chart, double u, double v, double part, double jitter_u, double jitter_v) {
+	const double row_height = 2.0 / CHART_ROWS, column_width = 2 * PI / CHART_COLUMNS;
+	double height, turn;
+	if (part < CHART_EVEN) {
+		height = 1 - 2 * u;
+		turn = 2 * PI * v;
+	} else {
+		const int row = chart_found(chart, CHART_ROWS, u);
+		const int column = chart_found(chart + CHART_ROWS + 1 + row * (CHART_COLUMNS + 1), CHART_COLUMNS, v);
+		height = -1 + (row + jitter_u) * row_height;
+		turn = (column + jitter_v) * column_width;
+	}
+	const double across = sqrt(maxd(1 - height * height, 0.0));
+	/* sky_map.cpp:30 chartDirection with level +x, aside +y, up +z */
+	const v3 toward = unit(add(add(scl(mk(1, 0, 0), across * cos(turn)), scl(mk(0, 1, 0), across * sin(turn))), scl(mk(0, 0, 1), height)));
+	aim a;
+	a.toward = toward;
+	a.distance = INFINITY;
+	a.density = chart_density(chart, toward);
+	a.found = a.density > 0;
+	double sky[3];
+	sky_colour(V, toward, sky);
+	for (int c = 0; c < 3; ++c) a.arriving[c] = a.found ? sky[c] / a.density : 0;
+	return a;
 }
 
 /* material.cpp:345 bsdfAt: the leaf's albedo, mixed with the other leaf's by
@@ -1050,9 +1169,16 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 			}
 		}
 		if (!found) {
+			/* the sky met, weighed against aiming at it by its chart
+			 * (trace.cpp:294 meetAimDensity, sampler.cpp:344 aimDensityAt) */
 			double sky[3];
 			sky_colour(V, heading, sky);
-			R = sadd(R, smul(smul(T, kept_along(J, medium, INFINITY, &w)), spectrum(sky, &w)));
+			double wgt = 1;
+			if (drawn > 0 && J->chart != NULL) {
+				const double pa = chart_density(J->chart, heading);
+				wgt = drawn * drawn / (drawn * drawn + pa * pa);
+			}
+			R = sadd(R, sscale(smul(smul(T, kept_along(J, medium, INFINITY, &w)), spectrum(sky, &w)), wgt));
 			break;
 		}
 		const uint32_t material = hit.leaf != 0xFFFFFFFFu ? J->leaf_material[hit.leaf] : 0;
@@ -1087,14 +1213,20 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 		const int bends = m->kind == 3 && s.within.v[0] != s.beyond.v[0];
 		const int aimable = medium == NO_MATERIAL || (medium == material && bends);
 		const v3 open = s.inside ? scl(normal, -1) : normal;
-		if (!m->exact && aimable && V->lamp_count > 0) {
+		if (!m->exact && aimable && (V->lamp_count > 0 || J->chart != NULL)) {
 			const double u0 = number(J->sobol, stream, index, depth, LIGHT_U), v0 = number(J->sobol, stream, index, depth, LIGHT_V);
 			double choice = number(J->sobol, stream, index, depth, PICK);
 			double total = 0, picked = 0, chosen_dist = 0;
 			spec chosen = flat(0);
 			v3 chosen_dir = mk(0, 0, 1);
-			for (uint32_t k = 0; k < V->lamp_count; ++k) {
-				const aim a = aim_lamp(&J->lamps[k], point, u0, v0);
+			/* the lamps, then a charted sky (sampler.cpp:312 skyAim) with its
+			 * own draws past the per-event ones (path.cpp:22 dimensionOf:
+			 * AimPart, AimJitterU, AimJitterV at 2^20 + 5 x event + 2, 3, 4) */
+			for (uint32_t k = 0; k < V->lamp_count + (J->chart != NULL ? 1u : 0u); ++k) {
+				const uint64_t plain = ((uint64_t) 1 << 20) + 5 * (uint64_t) depth;
+				const aim a = k < V->lamp_count ? aim_lamp(&J->lamps[k], point, u0, v0)
+				                                : aim_sky(V, J->chart, u0, v0, kp_hashed(stream, index, plain + 2), kp_hashed(stream, index, plain + 3),
+				                                          kp_hashed(stream, index, plain + 4));
 				if (!a.found) continue;
 				const double facing = dotv(open, a.toward);
 				if (facing <= 0 || a.distance <= 0) continue;
@@ -1212,6 +1344,15 @@ void kp_render_band(const kp_octree* tree, const uint32_t* leaf_material, const 
 		const kp_material* m = &materials[k];
 		if (m->kind == 3 && (m->absorb[0] > 0 || m->absorb[1] > 0 || m->absorb[2] > 0)) J.absorbs = 1;
 	}
+	double* chart = NULL;
+	if (view->sky_map) {
+		chart = (double*) malloc(sizeof(double) * CHART_DOUBLES);
+		if (!sky_chart(view, lamps, chart)) {
+			free(chart);
+			chart = NULL;
+		}
+	}
+	J.chart = chart;
 	uint32_t* sobol = NULL;
 	if (view->sobol) {
 		sobol = (uint32_t*) malloc(sizeof(uint32_t) * KP_SOBOL_DIMENSIONS * 512);
@@ -1224,5 +1365,6 @@ void kp_render_band(const kp_octree* tree, const uint32_t* leaf_material, const 
 	for (int t = 0; t < threads; ++t) pthread_join(pool[t], NULL);
 	free(pool);
 	free(sobol);
+	free(chart);
 	pthread_mutex_destroy(&J.lock);
 }

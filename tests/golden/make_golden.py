@@ -55,10 +55,12 @@ def region_flags(scene: Scene) -> list[str]:
 
 # name -> (seeds, spp per seed) of the reference frames kept as image fixtures
 IMAGES = {"room_small": (16, 64), "c1_small": (16, 64), "c2_small": (16, 64), "glow_small": (16, 64), "glass_small": (16, 64), "patterns_small": (16, 64), "rough_small": (16, 64),
-          "films_small": (16, 64)}
+          "films_small": (16, 64), "skylit_small": (16, 64)}
 
 # the scenes whose reference frames are also drawn with --use sampler=sobol
 SOBOL_IMAGES = ("c1_small", "glass_small")
+# ... and with --use sampler=sky_map
+SKY_MAP_IMAGES = ("skylit_small",)
 
 # name -> (generator, kwargs, trace rays, cut depth)
 SCENES = {
@@ -75,6 +77,7 @@ SCENES = {
     "films_small": (scenegen.scene_films, dict(seed=9, width=48, height=48, samples=64), 0, 0),
     # config 5, the stress scene (the benchmark's --stress run)
     "c5": (scenegen.scene_config5, dict(seed=1), 0, 0),
+    "skylit_small": (scenegen.scene_skylit, dict(seed=10, width=48, height=48, samples=64), 0, 0),
 }
 # config 3: the eight resident scenes of the serving run, 256 to 16384
 # config-1-style primitives (merge(0.05) groups of 64)
@@ -590,6 +593,8 @@ def main() -> None:
             reference_images(render, sdf, name, tmp, scene)
         if name in SOBOL_IMAGES:
             reference_images(render, sdf, name, tmp, scene, sampler="sobol")
+        if name in SKY_MAP_IMAGES:
+            reference_images(render, sdf, name, tmp, scene, sampler="sky_map")
         if name in SIZED_IMAGES:
             reference_sized_images(render, sdf, name, tmp, scene)
         if nrays:

@@ -48,7 +48,8 @@ def compare(a, b):
     return (np.abs(z) > 3).mean(), cz, ca.mean(0), cb.mean(0)
 
 
-@pytest.mark.parametrize("name", ["room_small", "c1_small", "c2_small", "glow_small", "glass_small", "patterns_small", "rough_small", "films_small"])
+@pytest.mark.parametrize("name", ["room_small", "c1_small", "c2_small", "glow_small", "glass_small", "patterns_small", "rough_small", "films_small",
+                                  "skylit_small"])
 def test_frame_matches_oracle_and_reference(backend, name):
     import oracle.port as op
     sc = scene(name)
@@ -147,15 +148,16 @@ def test_bad_patterns_are_refused(backend):
     assert np.isfinite(backend.render(8, 8, 1)).all()
 
 
-@pytest.mark.parametrize("name", ["c1_small", "glass_small"])
-def test_sobol_frame_matches_oracle_and_reference(backend, name):
-    """KDN_FRAME_SOBOL (--use sampler=sobol): the GPU's frames against the
-    oracle's drawn with the same Sobol numbers and against the reference's
-    own frames drawn so (tests/golden/image_<name>_sobol.npz), to the bars
-    of the frame test above."""
+@pytest.mark.parametrize("name, sampler", [("c1_small", "sobol"), ("glass_small", "sobol"), ("skylit_small", "sky_map")])
+def test_sampler_frame_matches_oracle_and_reference(backend, name, sampler):
+    """KDN_FRAME_SOBOL (--use sampler=sobol) and KDN_FRAME_SKY_MAP (--use
+    sampler=sky_map): the GPU's frames against the oracle's drawn with the
+    same sampler and against the reference's own frames drawn so
+    (tests/golden/image_<name>_<sampler>.npz), to the bars of the frame test
+    above."""
     import oracle.port as op
     sc = scene(name)
-    ref = np.load(os.path.join(GOLDEN, f"image_{name}_sobol.npz"))
+    ref = np.load(os.path.join(GOLDEN, f"image_{name}_{sampler}.npz"))
     frames = ref["frames"].astype(np.float64)
     spp = int(ref["spp"])
     surfaces = int(sc.render["surfaces"])
@@ -163,11 +165,11 @@ def test_sobol_frame_matches_oracle_and_reference(backend, name):
     backend.load(sc)
     backend.build(**build)
     h, w = sc.render["height"], sc.render["width"]
-    got = np.stack([backend.render(w, h, spp, surfaces=surfaces, seed=s, sobol=True) for s in SEEDS]).astype(np.float64)
-    oracle = np.stack([op.render_band(sc, w, h, spp, surfaces, s, 0, h, os.cpu_count() or 4, build, sobol=True) / spp for s in SEEDS])
+    got = np.stack([backend.render(w, h, spp, surfaces=surfaces, seed=s, **{sampler: True}) for s in SEEDS]).astype(np.float64)
+    oracle = np.stack([op.render_band(sc, w, h, spp, surfaces, s, 0, h, os.cpu_count() or 4, build, **{sampler: True}) / spp for s in SEEDS])
     far_o, cz_o, g_mean, o_mean = compare(got, oracle)
     far_r, cz_r, _, r_mean = compare(got, frames)
-    print(f"{name} sobol: gpu {g_mean} oracle {o_mean} reference {r_mean}; vs oracle z {cz_o} px {far_o:.4f}; vs reference rel {g_mean / r_mean - 1} px {far_r:.4f}")
+    print(f"{name} {sampler}: gpu {g_mean} oracle {o_mean} reference {r_mean}; vs oracle z {cz_o} px {far_o:.4f}; vs reference rel {g_mean / r_mean - 1} px {far_r:.4f}")
     assert far_o <= 0.01
     assert np.all(np.abs(cz_o) < 3)
     assert np.all(np.abs(g_mean / r_mean - 1) < 0.005)
