@@ -247,6 +247,12 @@ typedef struct kdn_frame {
  * outshine it five times over at the region's middle; a path that meets
  * the sky weighs it against that aim. */
 #define KDN_FRAME_SKY_MAP 32u
+/* --use sampler=each_lamp_first (plugins/sampler/each_lamp_first): at a
+ * path's first vertex each of the first four lamps whose offer is bright
+ * traces a shadow line of its own, outside the one-offer reservoir
+ * (plugins/transport/paths/trace.cpp:935); the aim densities, so the MIS
+ * weights, are those without it. */
+#define KDN_FRAME_EACH_LAMP 64u
 
 /* Device times of the last kdn_render, from CUDA events on the context's stream. */
 typedef struct kdn_frame_stats {

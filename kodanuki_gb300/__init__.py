@@ -73,6 +73,7 @@ FRAME_TEMPORAL = 4  # include/kdn.h KDN_FRAME_TEMPORAL
 FRAME_UPSAMPLE = 8  # include/kdn.h KDN_FRAME_UPSAMPLE
 FRAME_SOBOL = 16  # include/kdn.h KDN_FRAME_SOBOL
 FRAME_SKY_MAP = 32  # include/kdn.h KDN_FRAME_SKY_MAP
+FRAME_EACH_LAMP = 64  # include/kdn.h KDN_FRAME_EACH_LAMP
 
 
 class FrameStats(ctypes.Structure):
@@ -409,7 +410,7 @@ class Backend:
     def render(self, width: int, height: int, samples: int, surfaces: int | None = None, seed: int | None = None,
                first: int = 0, accumulate: bool = False, denoise: bool = False, restart: bool = False, factor: int = 1,
                phase: int = 0, temporal_only: bool = False, upsample: bool = False, sobol: bool = False,
-               sky_map: bool = False) -> np.ndarray:
+               sky_map: bool = False, each_lamp_first: bool = False) -> np.ndarray:
         """Draw `samples` samples a pixel and return the pixel means
         (linear RGB, float32, height x width x 3), or with `denoise` the
         means through the reconstruction chain (temporal + a-trous, or the
@@ -419,12 +420,14 @@ class Backend:
         with `upsample`, which without `denoise` blows up the means).
         `sobol`: the first 28 dimensions of the draws from the scrambled
         Sobol sequence (--use sampler=sobol); `sky_map`: the sky aimed at by
-        its chart (--use sampler=sky_map)."""
+        its chart (--use sampler=sky_map); `each_lamp_first`: the first four
+        lamps' own lines at the first vertex (--use sampler=each_lamp_first)."""
         sc = self.scene
         f = Frame(width, height, samples, surfaces if surfaces is not None else int(sc.render["surfaces"]),
                   seed if seed is not None else int(sc.render["seed"]), first, 1 if accumulate else 0,
                   (FRAME_DENOISE if denoise else 0) | (FRAME_RESTART if restart else 0) | (FRAME_TEMPORAL if temporal_only else 0) |
-                  (FRAME_UPSAMPLE if upsample else 0) | (FRAME_SOBOL if sobol else 0) | (FRAME_SKY_MAP if sky_map else 0), factor, phase)
+                  (FRAME_UPSAMPLE if upsample else 0) | (FRAME_SOBOL if sobol else 0) | (FRAME_SKY_MAP if sky_map else 0) |
+                  (FRAME_EACH_LAMP if each_lamp_first else 0), factor, phase)
         out = np.zeros((height, width, 3), np.float32)
         self._check(self.lib.kdn_render(self.handle, ctypes.byref(f), _ptr(out)))
         return out

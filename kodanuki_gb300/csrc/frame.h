@@ -115,6 +115,9 @@ struct FrameConstants {
 	// --use sampler=sky_map: the sky's chart (skymap.h), or null where the
 	// sky is only met
 	const double* skyChart;
+	// --use sampler=each_lamp_first: at the first vertex each of the first
+	// kOwnLines lamps whose offer is bright traces a line of its own
+	uint32_t eachLamp;
 	float zenith[3], horizon[3], ground[3];
 	DeviceLamp lamps[kMaxLamps];
 	SpectralTables spectral;
@@ -129,15 +132,25 @@ struct PathBuffers {
 	float4* nanometres;
 	float4* density;
 	float* drawn;         // density of the last scattered direction, 0 when exact
-	uint32_t* state;      // depth (bits 0-7), camera leg (bit 8), dispersed (bit 9), line pending (bit 10), medium + 1 (bits 16-31)
+	uint32_t* state;      // depth (bits 0-7), camera leg (bit 8), dispersed (bit 9), lines pending (bits 10-12), medium + 1 (bits 16-31)
 	float4* from;         // xyz: where the leg was drawn from
+	// with --use sampler=each_lamp_first: what each own line of the first
+	// vertex brought (kOwnLines a path, in the lamps' order; zero where none
+	// or blocked), added to the radiance at the next vertex or at the fold
+	float4* held;
 };
 
-// PathBuffers::state bit 10: the path's shadow line was carried to a later
-// trace launch and is not answered yet, so the path's next vertex waits
-// (its radiance takes the line's share before the next vertex's meets, in
-// the order of a frame without a march budget).
-constexpr uint32_t kLinePending = 1u << 10;
+// PathBuffers::state bits 10-12: how many of the path's shadow lines were
+// carried to a later trace launch and are not answered yet; while any is,
+// the path's next vertex waits (its radiance takes the lines' shares before
+// the next vertex's meets, in the order of a frame without a march budget).
+constexpr uint32_t kLineWaiting  = 1u << 10;
+constexpr uint32_t kLinesPending = 7u << 10;
+
+// plugins/sampler/each_lamp_first/each_lamp_first.cpp:5 lampsWithOwnRay:
+// the lamps that trace a line of their own at the first vertex; a path
+// holds at most this many lines beside the reservoir's one.
+constexpr uint32_t kOwnLines = 4;
 
 struct QueueBuffers {
 	uint32_t* paths;      // path index of each queued ray
@@ -164,6 +177,7 @@ struct ShadeArgs {
 	const HitState* states; // where each ray's march ended (a held path resumes there)
 	Looks looks;
 	uint32_t capacity;
+	uint32_t lineCapacity; // the shadow queue's room: capacity, or (1 + kOwnLines) capacity with own lines
 	uint32_t* error;
 	// where set (a denoised frame), the first surface of each pixel's last
 	// sample (core/frame.cpp record surfaces): FP16 bits, the leaf

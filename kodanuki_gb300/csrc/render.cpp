@@ -28,6 +28,7 @@ struct FrameState {
 	DeviceBuffer pixel, sample, throughput, radiance, nanometres, density, drawn, state, from;
 	DeviceBuffer queuePaths[2], queueRays[2], queueCarry[2], hits, states, counts;
 	DeviceBuffer shadowPaths[2], shadowContribution[2];
+	DeviceBuffer held; // the own lines' answers (--use sampler=each_lamp_first)
 	// the surfaces pass's own queue, states and hits, so it runs beside the
 	// lanes' chunks on its own stream
 	DeviceBuffer surfacePaths, surfaceRays, surfaceStates, surfaceHits;
@@ -48,6 +49,7 @@ struct FrameState {
 	DeviceBuffer skyChart; // --use sampler=sky_map's chart of the frame
 	DeviceBuffer guideLobes, guideRecords; // the learned guide's, a lane's capacity each
 	uint32_t capacity = 0;
+	uint32_t lineRoom = 1; // the shadow queues' room, in capacities (1 + kOwnLines with own lines)
 	int32_t width = 0, height = 0;
 	double taken = 0;
 	int current    = 0;     // which of the pairs the next denoised frame writes
@@ -75,7 +77,7 @@ struct FrameState {
 void Context::releaseFrame() {
 	if (frame == nullptr) return;
 	FrameState& f = *frame;
-	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.queueCarry[0], &f.queueCarry[1], &f.hits, &f.states, &f.counts, &f.shadowPaths[0], &f.shadowPaths[1], &f.shadowContribution[0], &f.shadowContribution[1], &f.surfacePaths, &f.surfaceRays, &f.surfaceStates, &f.surfaceHits, &f.sums, &f.out, &f.materials, &f.patternSteps, &f.stops, &f.placements, &f.boundaries, &f.frameLight, &f.firstDistance, &f.firstNormal, &f.firstAlbedo, &f.firstLeaf, &f.gDistance[0], &f.gDistance[1], &f.gNormal[0], &f.gNormal[1], &f.gAlbedo[0], &f.gAlbedo[1], &f.gLeaf[0], &f.gLeaf[1], &f.tColour[0], &f.tColour[1], &f.tMoment[0], &f.tMoment[1], &f.tLength[0], &f.tLength[1], &f.internal, &f.upState[0], &f.upState[1], &f.upscale.samples, &f.upscale.axes, &f.skyChart, &f.guideLobes, &f.guideRecords }) {
+	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.queueCarry[0], &f.queueCarry[1], &f.hits, &f.states, &f.counts, &f.shadowPaths[0], &f.shadowPaths[1], &f.shadowContribution[0], &f.shadowContribution[1], &f.held, &f.surfacePaths, &f.surfaceRays, &f.surfaceStates, &f.surfaceHits, &f.sums, &f.out, &f.materials, &f.patternSteps, &f.stops, &f.placements, &f.boundaries, &f.frameLight, &f.firstDistance, &f.firstNormal, &f.firstAlbedo, &f.firstLeaf, &f.gDistance[0], &f.gDistance[1], &f.gNormal[0], &f.gNormal[1], &f.gAlbedo[0], &f.gAlbedo[1], &f.gLeaf[0], &f.gLeaf[1], &f.tColour[0], &f.tColour[1], &f.tMoment[0], &f.tMoment[1], &f.tLength[0], &f.tLength[1], &f.internal, &f.upState[0], &f.upState[1], &f.upscale.samples, &f.upscale.axes, &f.skyChart, &f.guideLobes, &f.guideRecords }) {
 		if (b->ptr) cudaFree(b->ptr);
 		b->ptr   = nullptr;
 		b->bytes = 0;
@@ -277,6 +279,9 @@ namespace {
 // line queues' path indices and contributions.
 constexpr size_t kPathBytes = 4 * 4 + 5 * 16 + 2 * 4 + 2 * 2 * (sizeof(kdn_ray) + sizeof(uint2)) + sizeof(kdn_hit) + 2 * sizeof(kdn::HitState) + 2 * (4 + 16);
 static_assert(kPathBytes == 416, "path bytes");
+// ... and with own lines (--use sampler=each_lamp_first) kOwnLines more
+// lines a path in each queue, their hit states and their held answers
+constexpr size_t kOwnPathBytes = kdn::kOwnLines * (2 * (sizeof(kdn_ray) + sizeof(uint2)) + sizeof(kdn::HitState) + 2 * (4 + 16) + 16);
 
 // A lane's device counts: [0], [1] the two ray queues, [2], [3] the two
 // line queues, [4] zero; the first lane's [6]: the surfaces pass's queue.
@@ -291,23 +296,29 @@ constexpr int kCountsPerLane = 8;
 // training records
 constexpr size_t kGuidePathBytes = kdn::kGuideLobeFloats * sizeof(float) + kdn::kGuideDepth * sizeof(kdn::GuideRecord);
 
-uint64_t chunkPaths(Context* ctx, uint64_t framePaths) {
+uint64_t chunkPaths(Context* ctx, uint64_t framePaths, bool ownLines) {
 	size_t freeBytes = 0, totalBytes = 0;
 	if (cudaMemGetInfo(&freeBytes, &totalBytes) != cudaSuccess) freeBytes = 0;
-	const size_t pathBytes = kPathBytes + (ctx->guideFlags != 0 ? kGuidePathBytes : 0);
-	const uint64_t held = ctx->frame ? uint64_t(ctx->frame->capacity) * kLanes * kPathBytes + ctx->frame->guideLobes.bytes + ctx->frame->guideRecords.bytes : 0;
+	const size_t pathBytes = kPathBytes + (ctx->guideFlags != 0 ? kGuidePathBytes : 0) + (ownLines ? kOwnPathBytes : 0);
+	const uint64_t held = ctx->frame ? uint64_t(ctx->frame->capacity) * kLanes * (kPathBytes + (ctx->frame->lineRoom > 1 ? kOwnPathBytes : 0)) + ctx->frame->guideLobes.bytes +
+	                                       ctx->frame->guideRecords.bytes
+	                                 : 0;
 	uint64_t room = (uint64_t(freeBytes) + held) / 2 / pathBytes;
 	if (ctx->frameBudget > 0) room = std::min<uint64_t>(room, ctx->frameBudget / pathBytes);
 	const uint64_t least = ctx->frameBudget > 0 ? uint64_t(1) << 16 : uint64_t(1) << 20;
 	return std::min<uint64_t>(framePaths, std::min<uint64_t>(uint64_t(1) << 28, std::max<uint64_t>(room, least)));
 }
 
-// The path buffers for a chunk of `capacity` paths on each lane.
-kdn_status ensureFrame(Context* ctx, uint32_t capacity) {
+// The path buffers for a chunk of `capacity` paths on each lane, with
+// shadow queues of `lineRoom` capacities.
+kdn_status ensureFrame(Context* ctx, uint32_t capacity, uint32_t lineRoom) {
 	if (ctx->frame == nullptr) ctx->frame = new FrameState();
 	FrameState& f = *ctx->frame;
-	if (f.capacity >= capacity) return KDN_OK;
+	if (f.capacity >= capacity && f.lineRoom >= lineRoom) return KDN_OK;
+	capacity       = std::max(capacity, f.capacity);
+	lineRoom       = std::max(lineRoom, f.lineRoom);
 	const size_t n = size_t(capacity) * kLanes;
+	const size_t m = n * lineRoom;
 	kdn_status s;
 	struct Want {
 		kdn::DeviceBuffer* b;
@@ -316,17 +327,20 @@ kdn_status ensureFrame(Context* ctx, uint32_t capacity) {
 	const Want wants[] = {
 		{ &f.pixel, n * 4 }, { &f.sample, n * 4 }, { &f.throughput, n * 16 }, { &f.radiance, n * 16 }, { &f.nanometres, n * 16 },
 		{ &f.density, n * 16 }, { &f.drawn, n * 4 }, { &f.state, n * 4 }, { &f.from, n * 16 },
-		// a queue holds a bounce's path rays in [0, n) and the shadow lines of
-		// the bounce before in [n, 2n): one trace launch takes both
-		{ &f.queuePaths[0], n * 4 }, { &f.queuePaths[1], n * 4 }, { &f.queueRays[0], 2 * n * sizeof(kdn_ray) }, { &f.queueRays[1], 2 * n * sizeof(kdn_ray) },
-		{ &f.queueCarry[0], 2 * n * sizeof(uint2) }, { &f.queueCarry[1], 2 * n * sizeof(uint2) },
-		{ &f.hits, n * sizeof(kdn_hit) }, { &f.states, 2 * n * sizeof(kdn::HitState) }, { &f.counts, kLanes * kCountsPerLane * sizeof(uint32_t) },
-		{ &f.shadowPaths[0], n * 4 }, { &f.shadowPaths[1], n * 4 }, { &f.shadowContribution[0], n * 16 }, { &f.shadowContribution[1], n * 16 },
+		// a lane's queue holds a bounce's path rays in [0, capacity) and the
+		// shadow lines of the bounce before in [capacity, (1 + lineRoom)
+		// capacity): one trace launch takes both
+		{ &f.queuePaths[0], n * 4 }, { &f.queuePaths[1], n * 4 }, { &f.queueRays[0], (n + m) * sizeof(kdn_ray) }, { &f.queueRays[1], (n + m) * sizeof(kdn_ray) },
+		{ &f.queueCarry[0], (n + m) * sizeof(uint2) }, { &f.queueCarry[1], (n + m) * sizeof(uint2) },
+		{ &f.hits, n * sizeof(kdn_hit) }, { &f.states, (n + m) * sizeof(kdn::HitState) }, { &f.counts, kLanes * kCountsPerLane * sizeof(uint32_t) },
+		{ &f.shadowPaths[0], m * 4 }, { &f.shadowPaths[1], m * 4 }, { &f.shadowContribution[0], m * 16 }, { &f.shadowContribution[1], m * 16 },
+		{ &f.held, lineRoom > 1 ? n * kdn::kOwnLines * 16 : 0 },
 	};
 	for (const Want& w : wants) {
 		if ((s = ctx->ensure(*w.b, w.bytes)) != KDN_OK) return s;
 	}
 	f.capacity = capacity;
+	f.lineRoom = lineRoom;
 	return KDN_OK;
 }
 
@@ -366,10 +380,14 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	const uint32_t spp         = uint32_t(fr->samples);
 	// a chunk a lane: the frame's paths halved where they fit, else as many as
 	// the lanes' share of the room holds
-	const uint64_t want        = chunkPaths(ctx, uint64_t(pixels) * spp) / kLanes;
+	// with own lines a path holds up to 1 + kOwnLines lines at its first vertex
+	const bool ownLines        = (fr->flags & KDN_FRAME_EACH_LAMP) != 0 && !lights.empty();
+	const uint32_t lineRoom    = ownLines ? 1u + kOwnLines : 1u;
+	const uint64_t want        = chunkPaths(ctx, uint64_t(pixels) * spp, ownLines) / kLanes;
 	const uint32_t chunkPixels = uint32_t(std::max<uint64_t>(1, (want + spp - 1) / spp));
 	const uint32_t capacity    = chunkPixels * spp;
-	kdn_status s = ensureFrame(ctx, capacity);
+	const uint32_t lineCapacity = capacity * lineRoom;
+	kdn_status s = ensureFrame(ctx, capacity, lineRoom);
 	if (s != KDN_OK) return s;
 	FrameState& f = *ctx->frame;
 	// the learned guide: draws from it once it is trained, records for training
@@ -468,6 +486,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 			c.skyChart = static_cast<const double*>(f.skyChart.ptr);
 		}
 	}
+	c.eachLamp      = ownLines ? 1u : 0u;
 	c.seedMix       = mixedBits(uint64_t(int64_t(fr->seed)));
 	c.surfaces      = fr->surfaces;
 	c.spp           = spp;
@@ -539,6 +558,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	P.drawn      = static_cast<float*>(f.drawn.ptr);
 	P.state      = static_cast<uint32_t*>(f.state.ptr);
 	P.from       = static_cast<float4*>(f.from.ptr);
+	P.held       = ownLines ? static_cast<float4*>(f.held.ptr) : nullptr;
 	// Lanes: the frame's chunks go round kLanes streams, each lane with its own
 	// share of the path buffers, queues and counters, so one chunk's work
 	// fills the SMs another chunk's launch leaves idle in its tail (the
@@ -555,7 +575,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	struct Lane {
 		PathBuffers P;
 		QueueBuffers Q[2];   // a bounce's path rays in [0, capacity) of rays and carry
-		ShadowBuffers S[2];  // the shadow lines traced with Q[k], in [capacity, 2 capacity)
+		ShadowBuffers S[2];  // the shadow lines traced with Q[k], in [capacity, capacity + lineCapacity)
 		HitState* states;
 		kdn_hit* hits;
 		uint32_t* none;
@@ -578,19 +598,21 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		L.P.drawn         = P.drawn + base;
 		L.P.state         = P.state + base;
 		L.P.from          = P.from + base;
+		L.P.held          = ownLines ? P.held + base * kOwnLines : nullptr;
 		// a queue's path rays and hit states in [0, capacity), the shadow lines
-		// traced with them in [capacity, 2 capacity): one trace launch takes both
-		L.states = static_cast<HitState*>(f.states.ptr) + 2 * base;
+		// traced with them in [capacity, capacity + lineCapacity): one trace
+		// launch takes both
+		L.states = static_cast<HitState*>(f.states.ptr) + (1 + lineRoom) * base;
 		L.hits   = static_cast<kdn_hit*>(f.hits.ptr) + base;
 		for (int k = 0; k < 2; ++k) {
 			L.Q[k].paths        = static_cast<uint32_t*>(f.queuePaths[k].ptr) + base;
-			L.Q[k].rays         = static_cast<kdn_ray*>(f.queueRays[k].ptr) + 2 * base;
-			L.Q[k].carry        = static_cast<uint2*>(f.queueCarry[k].ptr) + 2 * base;
+			L.Q[k].rays         = static_cast<kdn_ray*>(f.queueRays[k].ptr) + (1 + lineRoom) * base;
+			L.Q[k].carry        = static_cast<uint2*>(f.queueCarry[k].ptr) + (1 + lineRoom) * base;
 			L.Q[k].count        = lc + k;
 			L.S[k].rays         = L.Q[k].rays + capacity;
 			L.S[k].carry        = L.Q[k].carry + capacity;
-			L.S[k].paths        = static_cast<uint32_t*>(f.shadowPaths[k].ptr) + base;
-			L.S[k].contribution = static_cast<float4*>(f.shadowContribution[k].ptr) + base;
+			L.S[k].paths        = static_cast<uint32_t*>(f.shadowPaths[k].ptr) + lineRoom * base;
+			L.S[k].contribution = static_cast<float4*>(f.shadowContribution[k].ptr) + lineRoom * base;
 			L.S[k].count        = lc + 2 + k;
 			L.S[k].states       = L.states + capacity;
 		}
@@ -745,7 +767,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 			if (round > 0) {
 				// the bounce before's lines that reached their lamps; lines still
 				// marching go on with the next round's
-				if (!ctx->check(launchLines(LP, L.S[q], L.S[nxt], capacity, on, ctx->smCount), "lines kernel")) return KDN_CUDA_ERROR;
+				if (!ctx->check(launchLines(LP, L.S[q], L.S[nxt], lineCapacity, on, ctx->smCount), "lines kernel")) return KDN_CUDA_ERROR;
 				++launches;
 			}
 			if (last) break;
@@ -759,6 +781,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 			a.states        = L.states;
 			a.looks         = looks;
 			a.capacity      = capacity;
+			a.lineCapacity  = lineCapacity;
 			a.error         = nullptr;
 			a.firstDistance = denoised ? static_cast<uint16_t*>(f.firstDistance.ptr) : nullptr;
 			a.firstNormal   = denoised ? static_cast<uint16_t*>(f.firstNormal.ptr) : nullptr;

@@ -413,6 +413,9 @@ __global__ void __launch_bounds__(kBlock) cameraKernel(const __grid_constant__ F
 		P.drawn[p]      = 0.0f;
 		P.state[p]      = 1u << 8;
 		P.from[p]       = make_float4(cFrame.eye[0], cFrame.eye[1], cFrame.eye[2], 0.0f);
+		if (P.held != nullptr) {
+			for (uint32_t k = 0; k < kOwnLines; ++k) P.held[size_t(p) * kOwnLines + k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+		}
 		Q.paths[p]      = p;
 		Q.rays[p]       = makeRay(f3(cFrame.eye), heading, __int_as_float(0x7f800000), kNoMaterial);
 	}
@@ -550,7 +553,7 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 		if (live) {
 			p = A.in.paths[q];
 			const uint8_t kind = A.hits[q].kind;
-			if (kind == kHitCarried || (A.paths.state[p] & kLinePending)) {
+			if (kind == kHitCarried || (A.paths.state[p] & kLinesPending)) {
 				const HitState h = A.states[q];
 				// a landed march resumes a step before its landing and lands again
 				const bool landed = h.kind == 1u || h.kind == 2u;
@@ -570,6 +573,13 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 			uint32_t medium     = (st >> 16) == 0 ? kNoMaterial : (st >> 16) - 1u;
 			float4 T            = A.paths.throughput[p];
 			float4 R            = A.paths.radiance[p];
+			// the first vertex's own lines, all answered by now
+			if (depth == 1 && A.paths.held != nullptr) {
+				for (uint32_t k = 0; k < kOwnLines; ++k) {
+					R                                        = add4(R, A.paths.held[size_t(p) * kOwnLines + k]);
+					A.paths.held[size_t(p) * kOwnLines + k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+				}
+			}
 			const float4 nm     = A.paths.nanometres[p];
 			const float drawnDensity = A.paths.drawn[p];
 			// a training frame: the radiance held on reaching this vertex is
@@ -683,8 +693,12 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 				const float3 open  = surf.inside ? normal * -1.0f : normal;
 				// aim: offer every lamp and a charted sky (the light after the
 				// lamps, sampler.cpp:312 skyAim), trace one offer drawn by its
-				// lane mean
+				// lane mean; with --use sampler=each_lamp_first each of the
+				// first kOwnLines lamps whose offer is bright traces a line of
+				// its own at the first vertex, outside the reservoir
+				// (trace.cpp:935, each_lamp_first.cpp:7 eachLampFirst)
 				if (!m.exact && aimable && (cFrame.lampCount > 0 || cFrame.skyChart != nullptr)) {
+					uint32_t owned   = 0;
 					const float u0   = number(cFrame.sobol, stream, index, depth, LightU);
 					const float v0   = number(cFrame.sobol, stream, index, depth, LightV);
 					float choice     = number(cFrame.sobol, stream, index, depth, Pick);
@@ -708,6 +722,18 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 						const float4 offer = scale4(mul4(mul4(T, f.value), spectrumOf(a.arriving.x, a.arriving.y, a.arriving.z, nm)), facing * w);
 						const float weight = mean4(offer);
 						if (!(weight > 0.0f)) continue;
+						if (cFrame.eachLamp && depth == 0 && k < cFrame.lampCount && owned < kOwnLines) {
+							kdn_ray own    = makeRay(point + open * lift, a.toward, a.distance - lift, kNoMaterial);
+							own.pad_[1]    = uint8_t(owned + 1);
+							++owned;
+							const uint32_t ownSlot = warpSlot(A.shadow.count, true);
+							if (ownSlot < A.lineCapacity) {
+								A.shadow.rays[ownSlot]         = own;
+								A.shadow.paths[ownSlot]        = p;
+								A.shadow.contribution[ownSlot] = offer;
+							}
+							continue;
+						}
 						total           = total + weight;
 						const float keep = weight / total;
 						if (choice < keep) {
@@ -802,7 +828,7 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 			if (resumes) A.out.carry[slot] = carryOut;
 		}
 		const uint32_t lineSlot = warpSlot(A.shadow.count, lined);
-		if (lined && lineSlot < A.capacity) {
+		if (lined && lineSlot < A.lineCapacity) {
 			A.shadow.rays[lineSlot]         = line;
 			A.shadow.paths[lineSlot]        = p;
 			A.shadow.contribution[lineSlot] = lineRadiance;
@@ -812,8 +838,10 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 
 // ---- K-line: add each shadow line that reached its lamp (trace.cpp:1294 lineAnswered) ----
 // A line whose march was carried goes on in the next launch (out) and its
-// path waits for it (kLinePending); an answered line that had been carried
-// lets its path go on.  A path has at most one line in flight.
+// path waits for it (kLinesPending counts it in); an answered line that had
+// been carried counts out.  A path has at most one reservoir line in flight
+// and, at its first vertex with own lines, kOwnLines more: each own line
+// answers into its own held slot, so no two threads add to one path.
 __global__ void __launch_bounds__(kBlock) linesKernel(PathBuffers P, ShadowBuffers S, ShadowBuffers out, uint32_t capacity) {
 	const uint32_t n = *S.count;
 	for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -825,11 +853,17 @@ __global__ void __launch_bounds__(kBlock) linesKernel(PathBuffers P, ShadowBuffe
 			h       = S.states[s];
 			p       = S.paths[s];
 			carried = h.kind == kCarried;
+			const kdn_ray& r = S.rays[s];
+			const bool resumed = r.pad_[0] & kRayResumes;
 			if (!carried) {
-				if (h.kind == 0) P.radiance[p] = add4(P.radiance[p], S.contribution[s]);
-				if (S.rays[s].pad_[0] & kRayResumes) P.state[p] &= ~kLinePending;
-			} else {
-				P.state[p] |= kLinePending;
+				if (r.pad_[1] != 0) {
+					P.held[size_t(p) * kOwnLines + (r.pad_[1] - 1u)] = h.kind == 0 ? S.contribution[s] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+				} else if (h.kind == 0) {
+					P.radiance[p] = add4(P.radiance[p], S.contribution[s]);
+				}
+				if (resumed) atomicSub(&P.state[p], kLineWaiting);
+			} else if (!resumed) {
+				atomicAdd(&P.state[p], kLineWaiting);
 			}
 		}
 		const uint32_t slot = warpSlot(out.count, carried);
@@ -851,7 +885,12 @@ __global__ void __launch_bounds__(kBlock) foldKernel(const __grid_constant__ Fra
 		double r = 0.0, g = 0.0, b = 0.0;
 		for (uint32_t k = 0; k < spp; ++k) {
 			const uint32_t p = i * spp + k;
-			const float3 c   = colourOf(cFrame, P.nanometres[p], P.density[p], P.radiance[p]);
+			float4 radiance  = P.radiance[p];
+			// own lines of a path that ended at its first vertex
+			if (P.held != nullptr) {
+				for (uint32_t o = 0; o < kOwnLines; ++o) radiance = add4(radiance, P.held[size_t(p) * kOwnLines + o]);
+			}
+			const float3 c   = colourOf(cFrame, P.nanometres[p], P.density[p], radiance);
 			r += double(c.x);
 			g += double(c.y);
 			b += double(c.z);

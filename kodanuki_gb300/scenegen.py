@@ -391,6 +391,39 @@ def scene_skylit(seed: int = 1, width: int = 256, height: int = 256, samples: in
     return "".join(out)
 
 
+def scene_lamps(seed: int = 1, width: int = 256, height: int = 256, samples: int = 16, surfaces: int = 8, count: int = 12) -> str:
+    """Lit by many lamps: config-1 primitives (plastics and metals) on a
+    plastic ground under a black sky, lit by four small sphere lamps of
+    unlike colour and power around the scene and two quad lamps above it,
+    so that --use sampler=each_lamp_first gives the first four lamps a line
+    of their own at the first vertex and the reservoir the other two."""
+    rng = random.Random(seed)
+    out = [_header(width, height, samples, surfaces, seed, [0.0, -8.5, 3.2], [0.0, 0.0, -0.6], 0.75)]
+    out.append(_sky([0.0, 0.0, 0.0]))
+    for k in range(4):
+        turn = 2.0 * math.pi * (k + rng.uniform(0.1, 0.9)) / 4.0
+        at = [3.0 * math.cos(turn), 3.0 * math.sin(turn), rng.uniform(0.5, 3.0)]
+        power = blackbody_rgb(rng.uniform(2500.0, 9000.0), rng.uniform(6.0, 30.0))
+        out.append("light sphere {\n" + f"\tat     = {_v(at)};\n\tradius = {_f(rng.uniform(0.05, 0.3))};\n\tpower  = {_v(power)};\n}}\n\n")
+    out.append(_quad([-1.5, 1.0, 4.5], [1.0, 0.0, 0.0], [0.0, -1.0, 0.0], blackbody_rgb(5000.0, 25.0)))
+    out.append(_quad([0.5, 1.5, 4.0], [1.2, 0.0, 0.0], [0.0, -0.6, 0.0], blackbody_rgb(3500.0, 15.0)))
+    out.append("paint(plastic([0.5, 0.5, 0.5], roughness = 0.5)) plane([0, 0, 1], -2.2);\n\n")
+    out.append("merge(0.05) {\n")
+    for k in range(count):
+        pos = [rng.uniform(-2.0, 2.0) for _ in range(3)]
+        if k % 3 == 2:
+            mat = f"metal({_v([rng.uniform(0.5, 0.95) for _ in range(3)])}, roughness = {_f(rng.uniform(0.1, 0.4))})"
+        else:
+            mat = f"plastic({_v([rng.uniform(0.2, 0.8) for _ in range(3)])}, roughness = {_f(rng.uniform(0.1, 0.5))})"
+        if rng.random() < 0.5:
+            shape = f"sphere({_f(rng.uniform(0.25, 0.6))})"
+        else:
+            shape = f"box({_v([2 * rng.uniform(0.15, 0.45) for _ in range(3)])}, 0.02)"
+        out.append(f"\tpaint({mat}) at({_v(pos)}) {shape};\n")
+    out.append("}\n")
+    return "".join(out)
+
+
 _PATTERNS = """function bands(count) {
 	return 0.5 + 0.5 * sin(p.z * count);
 }

@@ -242,7 +242,7 @@ class View(ctypes.Structure):
                 ("width", ctypes.c_int32), ("height", ctypes.c_int32), ("spp", ctypes.c_int32), ("surfaces", ctypes.c_int32),
                 ("seed", ctypes.c_int32), ("lamp_count", ctypes.c_uint32), ("material_count", ctypes.c_uint32),
                 ("factor", ctypes.c_uint32), ("phase", ctypes.c_uint32), ("sobol", ctypes.c_uint32), ("sky_map", ctypes.c_uint32),
-                ("middle", ctypes.c_double * 3)]
+                ("each_lamp", ctypes.c_uint32), ("middle", ctypes.c_double * 3)]
 
 
 _trees: dict = {}
@@ -256,12 +256,14 @@ def _octree_for(scene, build: dict) -> "Octree":
 
 
 def render_band(scene, width: int, height: int, spp: int, surfaces: int, seed: int, row0: int, rows: int, threads: int,
-                build: dict | None = None, factor: int = 1, phase: int = 0, sobol: bool = False, sky_map: bool = False) -> np.ndarray:
+                build: dict | None = None, factor: int = 1, phase: int = 0, sobol: bool = False, sky_map: bool = False,
+                each_lamp_first: bool = False) -> np.ndarray:
     """The oracle renderer over rows [row0, row0 + rows) of a frame: summed
     RGB per pixel (rows x width x 3, divide by spp for the means).  With a
     film factor above 1, width x height is the drawn frame and each pixel's
     samples aim at the shown pixel of `phase`.  `sobol`: --use sampler=sobol;
-    `sky_map`: --use sampler=sky_map."""
+    `sky_map`: --use sampler=sky_map; `each_lamp_first`: --use
+    sampler=each_lamp_first."""
     build = build or dict(min_depth=6, max_depth=10, split_steps=96)
     tree = _octree_for(scene, build)
     mats, keep = _materials(scene)
@@ -288,7 +290,7 @@ def render_band(scene, width: int, height: int, spp: int, surfaces: int, seed: i
     v.fov = scene.camera["fov"]
     v.width, v.height, v.spp, v.surfaces, v.seed = width, height, spp, surfaces, seed
     v.lamp_count, v.material_count = nl, n
-    v.factor, v.phase, v.sobol, v.sky_map = factor, phase, int(sobol), int(sky_map)
+    v.factor, v.phase, v.sobol, v.sky_map, v.each_lamp = factor, phase, int(sobol), int(sky_map), int(each_lamp_first)
     lower = np.asarray(scene.region_lower, np.float64)
     size = np.asarray(scene.region_size, np.float64)
     for a in range(3):

@@ -172,6 +172,9 @@ typedef struct kp_view {
 	/* 1: --use sampler=sky_map, charted against the lamps at `middle`, the
 	 * middle of the scene's region */
 	uint32_t sky_map;
+	/* 1: --use sampler=each_lamp_first: at the first vertex each of the
+	 * first four lamps that offer light traces a line of its own */
+	uint32_t each_lamp;
 	double middle[3];
 } kp_view;
 

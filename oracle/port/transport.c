@@ -1222,6 +1222,11 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 			/* the lamps, then a charted sky (sampler.cpp:312 skyAim) with its
 			 * own draws past the per-event ones (path.cpp:22 dimensionOf:
 			 * AimPart, AimJitterU, AimJitterV at 2^20 + 5 x event + 2, 3, 4) */
+			/* sampler.cpp:171 selectLight, each_lamp_first.cpp:7: with
+			 * --use sampler=each_lamp_first, at the first vertex each of
+			 * the first four lamps whose offer is bright traces a line of
+			 * its own, outside the reservoir (trace.cpp:935) */
+			uint32_t owned = 0;
 			for (uint32_t k = 0; k < V->lamp_count + (J->chart != NULL ? 1u : 0u); ++k) {
 				const uint64_t plain = ((uint64_t) 1 << 20) + 5 * (uint64_t) depth;
 				const aim a = k < V->lamp_count ? aim_lamp(&J->lamps[k], point, u0, v0)
@@ -1239,6 +1244,14 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 				const spec offer = sscale(smul(smul(T, f.value), spectrum(a.arriving, &w)), facing * wgt);
 				const double weight = smean(offer);
 				if (!(weight > 0)) continue;
+				if (V->each_lamp && depth == 0 && k < V->lamp_count && owned < 4) {
+					++owned;
+					const kp_ray own = ray_of(add(point, scl(open, lift)), a.toward, a.distance - lift, NO_MATERIAL);
+					kp_hit blocked;
+					kp_tracer_trace(tracer, &own, &blocked);
+					if (blocked.kind == 0) R = sadd(R, offer);
+					continue;
+				}
 				total += weight;
 				const double keep = weight / total;
 				if (choice < keep) {

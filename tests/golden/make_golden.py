@@ -55,12 +55,14 @@ def region_flags(scene: Scene) -> list[str]:
 
 # name -> (seeds, spp per seed) of the reference frames kept as image fixtures
 IMAGES = {"room_small": (16, 64), "c1_small": (16, 64), "c2_small": (16, 64), "glow_small": (16, 64), "glass_small": (16, 64), "patterns_small": (16, 64), "rough_small": (16, 64),
-          "films_small": (16, 64), "skylit_small": (16, 64)}
+          "films_small": (16, 64), "skylit_small": (16, 64), "lamps_small": (16, 64)}
 
 # the scenes whose reference frames are also drawn with --use sampler=sobol
 SOBOL_IMAGES = ("c1_small", "glass_small")
 # ... and with --use sampler=sky_map
 SKY_MAP_IMAGES = ("skylit_small",)
+# ... and with --use sampler=each_lamp_first
+EACH_LAMP_IMAGES = ("lamps_small",)
 
 # name -> (generator, kwargs, trace rays, cut depth)
 SCENES = {
@@ -78,6 +80,7 @@ SCENES = {
     # config 5, the stress scene (the benchmark's --stress run)
     "c5": (scenegen.scene_config5, dict(seed=1), 0, 0),
     "skylit_small": (scenegen.scene_skylit, dict(seed=10, width=48, height=48, samples=64), 0, 0),
+    "lamps_small": (scenegen.scene_lamps, dict(seed=11, width=48, height=48, samples=64), 0, 0),
 }
 # config 3: the eight resident scenes of the serving run, 256 to 16384
 # config-1-style primitives (merge(0.05) groups of 64)
@@ -595,6 +598,8 @@ def main() -> None:
             reference_images(render, sdf, name, tmp, scene, sampler="sobol")
         if name in SKY_MAP_IMAGES:
             reference_images(render, sdf, name, tmp, scene, sampler="sky_map")
+        if name in EACH_LAMP_IMAGES:
+            reference_images(render, sdf, name, tmp, scene, sampler="each_lamp_first")
         if name in SIZED_IMAGES:
             reference_sized_images(render, sdf, name, tmp, scene)
         if nrays:

@@ -13,22 +13,26 @@ from helpers import scene
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("name", ["c2_small", "room_small", "glass_small", "rough_small"])
-def test_frames_with_a_budget_equal_frames_without(name):
+@pytest.mark.parametrize("name, sampler", [("c2_small", None), ("room_small", None), ("glass_small", None), ("rough_small", None),
+                                           ("lamps_small", "each_lamp_first")])
+def test_frames_with_a_budget_equal_frames_without(name, sampler):
+    """With --use sampler=each_lamp_first a path holds up to five lines at
+    its first vertex, each carried on its own."""
     import kodanuki_gb300 as K
     sc = scene(name)
+    extra = {sampler: True} if sampler else {}
     w, h = int(sc.render["width"]), int(sc.render["height"])
     surfaces = int(sc.render["surfaces"])
     with K.Backend(0) as b:
         b.load(sc)
         b.build(5, 10, 64)
         b.set_march_budget(0)
-        plain = b.render(w, h, 8, surfaces=surfaces, seed=3)
+        plain = b.render(w, h, 8, surfaces=surfaces, seed=3, **extra)
         st0 = b.frame_stats()
         assert st0.carried_rays == 0
         for budget in (1, 5, 64):
             b.set_march_budget(budget)
-            img = b.render(w, h, 8, surfaces=surfaces, seed=3)
+            img = b.render(w, h, 8, surfaces=surfaces, seed=3, **extra)
             st = b.frame_stats()
             assert np.array_equal(img, plain), (budget, np.abs(img - plain).max())
             assert st.carried_rays > 0, budget

@@ -49,7 +49,7 @@ def compare(a, b):
 
 
 @pytest.mark.parametrize("name", ["room_small", "c1_small", "c2_small", "glow_small", "glass_small", "patterns_small", "rough_small", "films_small",
-                                  "skylit_small"])
+                                  "skylit_small", "lamps_small"])
 def test_frame_matches_oracle_and_reference(backend, name):
     import oracle.port as op
     sc = scene(name)
@@ -148,10 +148,11 @@ def test_bad_patterns_are_refused(backend):
     assert np.isfinite(backend.render(8, 8, 1)).all()
 
 
-@pytest.mark.parametrize("name, sampler", [("c1_small", "sobol"), ("glass_small", "sobol"), ("skylit_small", "sky_map")])
+@pytest.mark.parametrize("name, sampler", [("c1_small", "sobol"), ("glass_small", "sobol"), ("skylit_small", "sky_map"), ("lamps_small", "each_lamp_first")])
 def test_sampler_frame_matches_oracle_and_reference(backend, name, sampler):
-    """KDN_FRAME_SOBOL (--use sampler=sobol) and KDN_FRAME_SKY_MAP (--use
-    sampler=sky_map): the GPU's frames against the oracle's drawn with the
+    """KDN_FRAME_SOBOL (--use sampler=sobol), KDN_FRAME_SKY_MAP (--use
+    sampler=sky_map) and KDN_FRAME_EACH_LAMP (--use
+    sampler=each_lamp_first): the GPU's frames against the oracle's drawn with the
     same sampler and against the reference's own frames drawn so
     (tests/golden/image_<name>_<sampler>.npz), to the bars of the frame test
     above."""

@@ -74,7 +74,7 @@ def test_denoiser_matches_reference():
 
 
 @pytest.mark.parametrize("name", ["room_small", "c1_small", "c2_small", "glow_small", "glass_small", "patterns_small", "rough_small", "films_small",
-                                  "skylit_small"])
+                                  "skylit_small", "lamps_small"])
 def test_renderer_matches_reference_frames(name):
     """The oracle's frames against the reference renderer's own
     (tests/golden/image_*.npz, 12 seeds at the scene's spp): both are
@@ -140,14 +140,16 @@ def test_sobol_numbers_match_reference():
     assert np.array_equal(op.sobol_numbers(z["stream"], z["index"], even + 1), z["pair"][:, 1])
 
 
-@pytest.mark.parametrize("name, sampler", [("c1_small", "sobol"), ("glass_small", "sobol"), ("skylit_small", "sky_map")])
+@pytest.mark.parametrize("name, sampler", [("c1_small", "sobol"), ("glass_small", "sobol"), ("skylit_small", "sky_map"), ("lamps_small", "each_lamp_first")])
 def test_sampler_frames_match_reference(name, sampler):
     """The oracle drawing with --use sampler=sobol (the scrambled Sobol
-    sequence) or sampler=sky_map (the sky aimed at by its chart) against the
-    reference's own frames drawn so (tests/golden/image_<name>_<sampler>.npz,
-    16 seeds at 64 spp), to the bar of the other frame tests.  The Sobol
-    sequence does what it is for: the reference's frames' variance across
-    seeds is below its plain frames'.  (The sky map does not on this scene:
+    sequence), sampler=sky_map (the sky aimed at by its chart) or
+    sampler=each_lamp_first (the first four lamps' own lines at the first
+    vertex) against the reference's own frames drawn so
+    (tests/golden/image_<name>_<sampler>.npz, 16 seeds at 64 spp), to the
+    bar of the other frame tests.  The Sobol sequence and the lamps' own
+    lines do what they are for: the reference's frames' variance across
+    seeds is below its plain frames'.  (The sky map does not on its scene:
     its smooth, bright sky is found as well by the BSDF's draws, and the
     reference's frames with the map vary 1.2x more than without.)"""
     sc = scene(name)
@@ -166,5 +168,5 @@ def test_sampler_frames_match_reference(name, sampler):
     print(f"{name} {sampler}: oracle {ca.mean(0)} reference {cb.mean(0)} z {cz} far px {(np.abs(z) > 3).mean():.4f}; variance gain over plain {gain:.2f}")
     assert np.all(np.abs(cz) < 4)
     assert (np.abs(z) > 3).mean() <= 0.015
-    if sampler == "sobol":
+    if sampler in ("sobol", "each_lamp_first"):
         assert gain > 1.0
