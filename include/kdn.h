@@ -146,7 +146,7 @@ typedef struct kdn_finish {
 	double film[2];      /* the thin film (material.cpp:106 filmOf): thickness in nm (0: none), index */
 } kdn_finish;
 
-/* sdf/scene.h Light, 136 bytes. kind: sdf/scene.h LightKind (2 sphere, 3 quad). */
+/* sdf/scene.h Light, 136 bytes. kind: sdf/scene.h LightKind (0 point, 1 directional, 2 sphere, 3 quad, 4 sun, 5 moon); direction: toward a directional light, a sun or a moon; angle: a sun's or a moon's disc, radians across. */
 typedef struct kdn_light {
 	uint32_t kind;
 	float radius;

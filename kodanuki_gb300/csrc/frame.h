@@ -19,13 +19,22 @@ constexpr uint32_t kNoMaterial = 0xFFFFFFFFu;
 // A lamp with what aiming at it and meeting it read, worked out once
 // (plugins/transport/paths/light/light.cpp:78 lampOf).
 struct DeviceLamp {
-	uint32_t kind;   // sdf/scene.h LightKind
+	uint32_t kind;   // sdf/scene.h LightKind: 0 point, 1 directional, 2 sphere, 3 quad, 4 sun, 5 moon
 	uint32_t square; // a quad whose edges are at right angles (light.cpp:145 squareQuad)
 	float at[3], along[3], across[3], facing[3], cross[3];
 	float ex[3], ey[3], raw[3];
 	float alongLength, acrossLength;
 	float radius, area;
 	float radiance[3], power[3];
+	// a directional light, a sun or a moon: the unit direction toward it;
+	// a sun or a moon: 1 - the cosine of its disc's half angle (the cone
+	// it is aimed in, kept apart from 1 so that a small disc keeps its size)
+	float direction[3];
+	float oneLess;
+	// a moon: its direction and the sine of its half angle in double, for
+	// the lit share of its disc (sky_layers.cpp:273 moonLit)
+	double disc[3];
+	double discRadius;
 };
 
 // What the transport reads of a material (sdf/scene.h Material and the
@@ -119,6 +128,10 @@ struct FrameConstants {
 	// kOwnLines lamps whose offer is bright traces a line of its own
 	uint32_t eachLamp;
 	float zenith[3], horizon[3], ground[3];
+	// sdf/scene.cpp:306 firstSun: the first sun's unit direction, where the
+	// scene has one (a moon's phase follows it)
+	double sunDirection[3];
+	uint32_t hasSun;
 	DeviceLamp lamps[kMaxLamps];
 	SpectralTables spectral;
 };

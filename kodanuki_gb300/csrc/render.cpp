@@ -150,6 +150,22 @@ DeviceLamp lampOf(const kdn_light& l) {
 	} else if (l.kind == 2) {
 		d.area = float(4 * pi * double(l.radius) * double(l.radius));
 		k      = l.radius > 0 ? 1.0 / (pi * double(l.radius) * double(l.radius)) : 0.0;
+	} else if (l.kind == 4 || l.kind == 5) {
+		// light.cpp:37 a far disc's radiance over its half angle's sine squared
+		const double half = 0.5 * double(l.angle);
+		const double sine = std::sin(half);
+		k                 = sine != 0 ? 1.0 / (pi * sine * sine) : 0.0;
+		// 1 - cos(half) as 2 sin^2(half / 2): exact for a small disc
+		const double quarter = std::sin(0.5 * half);
+		d.oneLess            = float(std::cos(half) < 1 ? 2 * quarter * quarter : 0.0);
+		d.discRadius         = sine;
+	}
+	// light.cpp:86 lampOf: the direction normalised
+	const V3 toward = v3(l.direction);
+	if (length(toward) > 0) {
+		put(d.direction, normalized(toward));
+		const V3 unit = normalized(toward);
+		d.disc[0] = unit.x, d.disc[1] = unit.y, d.disc[2] = unit.z;
 	}
 	for (int c = 0; c < 3; ++c) {
 		d.radiance[c] = float(l.power[c] * k);
@@ -497,6 +513,13 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		if (m.kind == 3 && (m.absorb[0] > 0 || m.absorb[1] > 0 || m.absorb[2] > 0)) c.absorbs = 1;
 	}
 	for (size_t k = 0; k < lights.size(); ++k) c.lamps[k] = lampOf(lights[k]);
+	for (size_t k = 0; k < lights.size(); ++k) {
+		if (lights[k].kind == 4) {
+			for (int a = 0; a < 3; ++a) c.sunDirection[a] = c.lamps[k].disc[a];
+			c.hasSun = length(v3(lights[k].direction)) > 0 ? 1u : 0u;
+			break;
+		}
+	}
 	if (!skies.empty()) {
 		put(c.zenith, v3(skies[0].zenith));
 		put(c.horizon, v3(skies[0].horizon));

@@ -56,6 +56,11 @@ bool buildSkyChart(const SkyGradient& sky, const ChartLamp* lamps, uint32_t lamp
 	double lit = 0;
 	for (uint32_t k = 0; k < lampCount; ++k) {
 		const ChartLamp& l = lamps[k];
+		// a directional light, a sun or a moon sends its power's mean from afar
+		if (l.kind == 1 || l.kind == 4 || l.kind == 5) {
+			lit += std::max((l.power[0] + l.power[1] + l.power[2]) / 3, 0.0);
+			continue;
+		}
 		double place[3], apart = 0;
 		for (int a = 0; a < 3; ++a) {
 			place[a]        = l.kind == 3 ? l.at[a] + (l.along[a] + l.across[a]) * 0.5 : l.at[a];

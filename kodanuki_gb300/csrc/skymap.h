@@ -31,7 +31,7 @@ struct SkyGradient {
 };
 
 struct ChartLamp {
-	uint32_t kind; // sdf/scene.h LightKind: 2 sphere, 3 quad
+	uint32_t kind; // sdf/scene.h LightKind
 	double at[3], along[3], across[3], power[3];
 };
 

@@ -186,10 +186,56 @@ __device__ __forceinline__ float coneDensity(float cosine) {
 	return cone > 1e-12f ? 1.0f / cone : 0.0f;
 }
 
-// aimLight (light.cpp:372) for a quad or a sphere lamp.
+// sky_layers.cpp:273 moonLit: the share of a moon's disc the first sun
+// lights where a direction meets it, eased (in double: the disc is small)
+__device__ float moonLit(const FrameConstants& c, const DeviceLamp& l, float3 toward) {
+	if (l.kind != 5 || !c.hasSun) return 1.0f;
+	const double d[3]   = { double(toward.x), double(toward.y), double(toward.z) };
+	const double along  = d[0] * l.disc[0] + d[1] * l.disc[1] + d[2] * l.disc[2];
+	const double aside  = fmax(1.0 - along * along, 0.0);
+	const double reach  = along - sqrt(fmax(l.discRadius * l.discRadius - aside, 0.0));
+	double facing       = 0.0;
+	for (int a = 0; a < 3; ++a) facing += (d[a] * reach - l.disc[a]) / l.discRadius * c.sunDirection[a];
+	const double lit    = fmin(fmax(facing / 0.1 + 0.5, 0.0), 1.0);
+	return float(lit * lit * (3.0 - 2.0 * lit));
+}
+
+// aimLight (light.cpp:372) for every kind of lamp.
 __device__ Aim aimLamp(const DeviceLamp& l, float3 from, float u, float v) {
 	Aim a;
 	a.found = false;
+	if (l.kind == 0) { // point (light.cpp:349 aimPoint): singular, density 0
+		const float3 off = f3(l.at) - from;
+		const float dist = lengthOf(off);
+		if (dist < 1e-9f) return a;
+		a.found    = true;
+		a.toward   = off * (1.0f / dist);
+		a.distance = dist;
+		a.arriving = f3(l.power) * (1.0f / (dist * dist));
+		a.density  = 0.0f;
+		return a;
+	}
+	if (l.kind == 1) { // directional (light.cpp:362): singular, from afar
+		a.found    = true;
+		a.toward   = f3(l.direction);
+		a.distance = __int_as_float(0x7f800000);
+		a.arriving = f3(l.power);
+		a.density  = 0.0f;
+		return a;
+	}
+	if (l.kind == 4 || l.kind == 5) { // sun or moon (light.cpp:334 aimSun): evenly in the disc's cone
+		if (!(l.oneLess > 0.0f)) return a;
+		const float drop   = u * l.oneLess; // 1 - the height in the cone
+		const float ring   = sqrtf(fmaxf(drop * (2.0f - drop), 0.0f));
+		const float angle  = 2.0f * 3.14159265358979f * v;
+		const Frame f      = frameAround(f3(l.direction));
+		a.found    = true;
+		a.toward   = f.toWorld(make_float3(ring * cosf(angle), ring * sinf(angle), 1.0f - drop));
+		a.distance = __int_as_float(0x7f800000);
+		a.density  = 1.0f / (2.0f * 3.14159265358979f * l.oneLess);
+		a.arriving = f3(l.radiance) * (2.0f * 3.14159265358979f * l.oneLess);
+		return a;
+	}
 	if (l.kind == 3) { // quad
 		if (l.area < 1e-12f || dot3(f3(l.facing), from - f3(l.at)) <= 0.0f) return a;
 		float3 spot;
@@ -251,8 +297,16 @@ __device__ Aim aimLamp(const DeviceLamp& l, float3 from, float u, float v) {
 	return a;
 }
 
+// Whether a unit direction lies in a far disc's cone: 1 - cos(apart) <=
+// 1 - cos(half), as half the squared distance between the unit vectors
+__device__ __forceinline__ bool inDisc(const DeviceLamp& l, float3 toward) {
+	const float3 apart = toward - f3(l.direction);
+	return l.oneLess > 0.0f && 0.5f * dot3(apart, apart) <= l.oneLess;
+}
+
 // aimDensity (light.cpp:463): the density aiming gives a direction.
 __device__ float aimDensityOf(const DeviceLamp& l, float3 from, float3 toward, float distance) {
+	if (l.kind == 4 || l.kind == 5) return inDisc(l, toward) ? 1.0f / (2.0f * 3.14159265358979f * l.oneLess) : 0.0f;
 	if (l.kind == 3) {
 		if (l.area < 1e-12f || dot3(f3(l.facing), from - f3(l.at)) <= 0.0f) return 0.0f;
 		if (l.square) {
@@ -272,8 +326,14 @@ __device__ float aimDensityOf(const DeviceLamp& l, float3 from, float3 toward, f
 	return 0.0f;
 }
 
-// meetLight (light.cpp:498) for a lamp: where a ray meets it before limit.
+// meetLight (light.cpp:498) for a lamp: where a ray meets it before limit
+// (a point or a directional light is never met; a sun or a moon only by a
+// ray that escaped, light.cpp:478 meetSun).
 __device__ bool meetLamp(const DeviceLamp& l, float3 origin, float3 dir, float limit, float& reach) {
+	if (l.kind == 4 || l.kind == 5) {
+		reach = __int_as_float(0x7f800000);
+		return limit >= 3.0e38f && inDisc(l, dir);
+	}
 	if (l.kind == 3) {
 		const float3 facing = f3(l.cross);
 		const float leaning = dot3(facing, dir);
@@ -614,7 +674,7 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 						const float pa = aimDensityOf(l, from, heading, reach);
 						w              = drawnDensity * drawnDensity / (drawnDensity * drawnDensity + pa * pa);
 					}
-					R = add4(R, scale4(mul4(mul4(T, keptOver(reach)), spectrumOf(l.radiance[0], l.radiance[1], l.radiance[2], nm)), w));
+					R = add4(R, scale4(mul4(mul4(T, keptOver(reach)), spectrumOf(l.radiance[0], l.radiance[1], l.radiance[2], nm)), w * moonLit(cFrame, l, heading)));
 				}
 			}
 			// the record's first surface of the pixel's last sample
@@ -707,10 +767,11 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 					float3 chosenDir = make_float3(0.0f, 0.0f, 1.0f);
 					float chosenDist = 0.0f;
 					for (uint32_t k = 0; k < cFrame.lampCount + (cFrame.skyChart != nullptr ? 1u : 0u); ++k) {
-						const Aim a = k < cFrame.lampCount ? aimLamp(cFrame.lamps[k], point, u0, v0)
+						Aim a = k < cFrame.lampCount ? aimLamp(cFrame.lamps[k], point, u0, v0)
 						                                   : aimSky(cFrame, u0, v0, plainNumber(stream, index, depth, AimPart), plainNumber(stream, index, depth, AimJitterU),
 						                                            plainNumber(stream, index, depth, AimJitterV));
 						if (!a.found) continue;
+						if (k < cFrame.lampCount) a.arriving = a.arriving * moonLit(cFrame, cFrame.lamps[k], a.toward);
 						const float facing = dot3(open, a.toward);
 						if (facing <= 0.0f || a.distance <= 0.0f) continue;
 						const Response f = respond(surf, m, outgoing, a.toward, nm);

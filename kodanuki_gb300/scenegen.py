@@ -424,6 +424,36 @@ def scene_lamps(seed: int = 1, width: int = 256, height: int = 256, samples: int
     return "".join(out)
 
 
+def scene_far_lights(seed: int = 1, width: int = 256, height: int = 256, samples: int = 16, surfaces: int = 8, count: int = 12) -> str:
+    """Lit by every kind of light but the area lamps: config-1 primitives
+    (plastics and rough metals) on a plastic ground under a dim gradient
+    sky, lit by a point light, a directional light, a sun (a disc 0.05
+    radians across) and a moon (0.06 radians, its lit share set by the
+    sun's direction)."""
+    rng = random.Random(seed)
+    out = [_header(width, height, samples, surfaces, seed, [0.0, -8.5, 3.2], [0.0, 0.0, -0.6], 0.75)]
+    out.append("sky gradient {\n\tzenith  = [0.04, 0.05, 0.09];\n\thorizon = [0.08, 0.08, 0.08];\n\tground  = [0.02, 0.02, 0.02];\n}\n\n")
+    out.append("light point {\n\tat    = [1.6, -1.8, 2.6];\n" + f"\tpower = {_v(blackbody_rgb(3200.0, 18.0))};\n}}\n\n")
+    out.append("light directional {\n\tdirection = [0.3, -0.6, 0.7];\n" + f"\tpower     = {_v(blackbody_rgb(7000.0, 0.6))};\n}}\n\n")
+    out.append("light sun {\n\tdirection = [-0.5, 0.3, 0.62];\n\tangle     = 0.05;\n" + f"\tpower     = {_v(blackbody_rgb(5500.0, 1.6))};\n}}\n\n")
+    out.append("light moon {\n\tdirection = [0.55, 0.45, 0.5];\n\tangle     = 0.06;\n" + f"\tpower     = {_v(blackbody_rgb(4500.0, 0.5))};\n}}\n\n")
+    out.append("paint(plastic([0.5, 0.5, 0.5], roughness = 0.5)) plane([0, 0, 1], -2.2);\n\n")
+    out.append("merge(0.05) {\n")
+    for k in range(count):
+        pos = [rng.uniform(-2.0, 2.0) for _ in range(3)]
+        if k % 3 == 2:
+            mat = f"metal({_v([rng.uniform(0.5, 0.95) for _ in range(3)])}, roughness = {_f(rng.uniform(0.15, 0.4))})"
+        else:
+            mat = f"plastic({_v([rng.uniform(0.2, 0.8) for _ in range(3)])}, roughness = {_f(rng.uniform(0.1, 0.5))})"
+        if rng.random() < 0.5:
+            shape = f"sphere({_f(rng.uniform(0.25, 0.6))})"
+        else:
+            shape = f"box({_v([2 * rng.uniform(0.15, 0.45) for _ in range(3)])}, 0.02)"
+        out.append(f"\tpaint({mat}) at({_v(pos)}) {shape};\n")
+    out.append("}\n")
+    return "".join(out)
+
+
 _PATTERNS = """function bands(count) {
 	return 0.5 + 0.5 * sin(p.z * count);
 }

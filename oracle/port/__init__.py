@@ -233,7 +233,8 @@ def _placements(scene):
 
 class Lamp(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_uint32), ("square", ctypes.c_uint32), ("at", ctypes.c_double * 3), ("along", ctypes.c_double * 3),
-                ("across", ctypes.c_double * 3), ("power", ctypes.c_double * 3), ("radius", ctypes.c_double)]
+                ("across", ctypes.c_double * 3), ("power", ctypes.c_double * 3), ("radius", ctypes.c_double),
+                ("direction", ctypes.c_double * 3), ("angle", ctypes.c_double)]
 
 
 class View(ctypes.Structure):
@@ -279,6 +280,9 @@ def render_band(scene, width: int, height: int, spp: int, surfaces: int, seed: i
             lamps[i].across[c] = float(l["across"][i][c])
             lamps[i].power[c] = float(l["power"][i][c])
         lamps[i].radius = float(l["radius"][i])
+        for c in range(3):
+            lamps[i].direction[c] = float(l["direction"][i][c])
+        lamps[i].angle = float(l["angle"][i])
     v = View()
     for c in range(3):
         v.eye[c] = scene.camera["eye"][c]

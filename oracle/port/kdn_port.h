@@ -152,10 +152,13 @@ typedef struct kp_material {
 	double film[2];
 } kp_material;
 
-/* A lamp (light.cpp:78 lampOf): kind 2 sphere, 3 quad. */
+/* A lamp (light.cpp:78 lampOf): kind 0 point, 1 directional, 2 sphere,
+ * 3 quad, 4 sun, 5 moon; direction toward a directional light, a sun or a
+ * moon; angle across a sun's or a moon's disc, radians. */
 typedef struct kp_lamp {
 	uint32_t kind, square;
 	double at[3], along[3], across[3], power[3], radius;
+	double direction[3], angle;
 } kp_lamp;
 
 typedef struct kp_view {

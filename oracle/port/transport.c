@@ -121,6 +121,10 @@ typedef struct lamp {
 	v3 at, along, across, facing, cross, ex, ey, raw;
 	double along_len, across_len, area, radius;
 	double radiance[3], power[3];
+	/* light.cpp:86: the direction normalised; the cosine of a far disc's
+	 * half angle; sky_layers.cpp:129: the sine of it */
+	v3 direction;
+	double cosine, disc_radius;
 } lamp;
 
 static lamp lamp_of(const kp_lamp* l) {
@@ -148,7 +152,14 @@ static lamp lamp_of(const kp_lamp* l) {
 	} else if (l->kind == 2) {
 		k = l->radius > 0 ? 1 / (PI * l->radius * l->radius) : 0;
 		d.area = 4 * PI * l->radius * l->radius;
+	} else if (l->kind == 4 || l->kind == 5) {
+		/* light.cpp:37: over pi sin^2 of the half angle */
+		const double s = sin(0.5 * l->angle);
+		k = 1 / (PI * s * s);
 	}
+	d.direction = unit(vd(l->direction));
+	d.cosine = cos(0.5 * l->angle);
+	d.disc_radius = sin(0.5 * l->angle);
 	for (int c = 0; c < 3; ++c) {
 		d.power[c] = l->power[c];
 		d.radiance[c] = l->power[c] * k;
@@ -217,10 +228,39 @@ typedef struct aim {
 	double arriving[3];
 } aim;
 
-/* light.cpp:372 aimLight for quads and spheres */
+/* light.cpp:372 aimLight for every kind of lamp */
 static aim aim_lamp(const lamp* l, v3 from, double u, double v) {
 	aim a;
 	memset(&a, 0, sizeof a);
+	if (l->kind == 0) { /* :349 aimPoint: singular, density 0 */
+		const v3 off = sub(l->at, from);
+		const double d = len(off);
+		if (d < 1e-9) return a;
+		a.found = 1;
+		a.toward = scl(off, 1 / d);
+		a.distance = d;
+		for (int c = 0; c < 3; ++c) a.arriving[c] = l->power[c] / (d * d);
+		return a;
+	}
+	if (l->kind == 1) { /* :362 a directional light: singular, from afar */
+		a.found = 1;
+		a.toward = l->direction;
+		a.distance = INFINITY;
+		for (int c = 0; c < 3; ++c) a.arriving[c] = l->power[c];
+		return a;
+	}
+	if (l->kind == 4 || l->kind == 5) { /* :334 aimSun: evenly in the disc's cone */
+		if (!(l->cosine < 1)) return a;
+		const double height = 1 - u * (1 - l->cosine);
+		const double ring = sqrt(maxd(1 - height * height, 0));
+		const double angle = 2 * PI * v;
+		a.found = 1;
+		a.toward = to_world(basis_around(l->direction), mk(ring * cos(angle), ring * sin(angle), height));
+		a.distance = INFINITY;
+		a.density = cone_density(l->cosine);
+		for (int c = 0; c < 3; ++c) a.arriving[c] = l->radiance[c] / a.density;
+		return a;
+	}
 	if (l->kind == 3) {
 		if (l->area < 1e-12 || dotv(l->facing, sub(from, l->at)) <= 0) return a;
 		if (l->square) {
@@ -275,6 +315,7 @@ static aim aim_lamp(const lamp* l, v3 from, double u, double v) {
 
 /* light.cpp:463 aimDensity */
 static double aim_density(const lamp* l, v3 from, v3 toward, double distance) {
+	if (l->kind == 4 || l->kind == 5) return l->cosine < 1 && dotv(toward, l->direction) >= l->cosine ? cone_density(l->cosine) : 0;
 	if (l->kind == 3) {
 		if (l->area < 1e-12 || dotv(l->facing, sub(from, l->at)) <= 0) return 0;
 		if (l->square) {
@@ -294,8 +335,26 @@ static double aim_density(const lamp* l, v3 from, v3 toward, double distance) {
 	return 0;
 }
 
-/* light.cpp:498 meetLight for a lamp */
+/* sky_layers.cpp:273 moonLit: the share of a moon's disc the first sun
+ * lights where a direction meets it, eased; 1 for every other lamp */
+static double moon_lit(const lamp* l, const v3* sun, v3 toward) {
+	if (l->kind != 5 || sun == NULL) return 1;
+	const double along = dotv(toward, l->direction);
+	const double aside = maxd(1 - along * along, 0);
+	const double reach = along - sqrt(maxd(l->disc_radius * l->disc_radius - aside, 0));
+	const v3 normal = scl(sub(scl(toward, reach), l->direction), 1 / l->disc_radius);
+	double lit = dotv(normal, *sun) / 0.1 + 0.5;
+	lit = lit < 0 ? 0 : (lit > 1 ? 1 : lit);
+	return lit * lit * (3 - 2 * lit);
+}
+
+/* light.cpp:498 meetLight for a lamp: a point or a directional light is
+ * never met, a sun or a moon only by a ray that escaped (:478 meetSun) */
 static int meet_lamp(const lamp* l, v3 origin, v3 dir, double limit, double* reach) {
+	if (l->kind == 4 || l->kind == 5) {
+		*reach = INFINITY;
+		return l->cosine < 1 && isinf(limit) && dotv(dir, l->direction) >= l->cosine;
+	}
 	if (l->kind == 3) {
 		const double leaning = dotv(l->cross, dir);
 		if (l->area < 1e-12 || leaning >= -1e-12) return 0;
@@ -898,6 +957,11 @@ static int sky_chart(const kp_view* V, const kp_lamp* lamps, double* chart) {
 	double lit = 0;
 	for (uint32_t k = 0; k < V->lamp_count; ++k) {
 		const kp_lamp* l = &lamps[k];
+		/* a directional light, a sun or a moon sends its power's mean from afar */
+		if (l->kind == 1 || l->kind == 4 || l->kind == 5) {
+			lit += maxd((l->power[0] + l->power[1] + l->power[2]) / 3, 0.0);
+			continue;
+		}
 		double apart = 0;
 		for (int a = 0; a < 3; ++a) {
 			const double place = l->kind == 3 ? l->at[a] + (l->along[a] + l->across[a]) * 0.5 : l->at[a];
@@ -983,6 +1047,8 @@ typedef struct job {
 	const double* placements; /* 12 a leaf, or none */
 	const uint32_t* sobol;    /* --use sampler=sobol's tables, or none */
 	const double* chart;      /* --use sampler=sky_map's chart, or none (the sky only met) */
+	v3 sun;                   /* sdf/scene.cpp:306 firstSun's direction ... */
+	const v3* has_sun;        /* ... or none */
 } job;
 
 /* trace.cpp:179 keptOnLeg with absorption.cpp:28 keptThrough: what a leg of
@@ -1165,7 +1231,7 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 					const double pa = aim_density(&J->lamps[k], from, heading, reach);
 					wgt = drawn * drawn / (drawn * drawn + pa * pa);
 				}
-				R = sadd(R, sscale(smul(smul(T, kept_along(J, medium, reach, &w)), spectrum(J->lamps[k].radiance, &w)), wgt));
+				R = sadd(R, sscale(smul(smul(T, kept_along(J, medium, reach, &w)), spectrum(J->lamps[k].radiance, &w)), wgt * moon_lit(&J->lamps[k], J->has_sun, heading)));
 			}
 		}
 		if (!found) {
@@ -1229,10 +1295,14 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 			uint32_t owned = 0;
 			for (uint32_t k = 0; k < V->lamp_count + (J->chart != NULL ? 1u : 0u); ++k) {
 				const uint64_t plain = ((uint64_t) 1 << 20) + 5 * (uint64_t) depth;
-				const aim a = k < V->lamp_count ? aim_lamp(&J->lamps[k], point, u0, v0)
+				aim a = k < V->lamp_count ? aim_lamp(&J->lamps[k], point, u0, v0)
 				                                : aim_sky(V, J->chart, u0, v0, kp_hashed(stream, index, plain + 2), kp_hashed(stream, index, plain + 3),
 				                                          kp_hashed(stream, index, plain + 4));
 				if (!a.found) continue;
+				if (k < V->lamp_count) {
+					const double lit = moon_lit(&J->lamps[k], J->has_sun, a.toward);
+					for (int c = 0; c < 3; ++c) a.arriving[c] *= lit;
+				}
 				const double facing = dotv(open, a.toward);
 				if (facing <= 0 || a.distance <= 0) continue;
 				const response f = respond(&s, out, a.toward, &w);
@@ -1339,6 +1409,14 @@ void kp_render_band(const kp_octree* tree, const uint32_t* leaf_material, const 
 	J.leaf_material = leaf_material;
 	J.materials = materials;
 	for (uint32_t k = 0; k < view->lamp_count && k < 16; ++k) J.lamps[k] = lamp_of(&lamps[k]);
+	J.has_sun = NULL;
+	for (uint32_t k = 0; k < view->lamp_count && k < 16; ++k) {
+		if (lamps[k].kind == 4) {
+			J.sun = J.lamps[k].direction;
+			if (len(vd(lamps[k].direction)) > 0) J.has_sun = &J.sun;
+			break;
+		}
+	}
 	J.view = view;
 	J.row0 = row0;
 	J.rows = rows;
