@@ -86,6 +86,8 @@ typedef struct kdn_material {
 	float glow[3];
 	float strength;
 	uint32_t flags_;    /* 1: the albedo is a ramp read off a pattern program ("looks.patterns") */
+	float scatter;      /* a glass: how much of a unit of travel its body turns aside (0: none) */
+	float lean;         /* Henyey-Greenstein's g of that scattering, in (-1, 1) */
 	uint32_t pad_;
 } kdn_material;
 
@@ -212,6 +214,10 @@ typedef struct kdn_frame {
 	 * drawn size. */
 	uint32_t factor;
 	uint32_t phase; /* 0 .. factor^2 - 1: core/shown.cpp bayerFilm gives the order */
+	/* render.collisions: the most collisions inside scattering bodies a path
+	 * stands on, apart from its surfaces (0: the reference's default, 256) */
+	int32_t collisions;
+	uint32_t pad_;
 } kdn_frame;
 
 /* With KDN_FRAME_DENOISE a frame returns what the reference shows through

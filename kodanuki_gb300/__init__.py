@@ -35,7 +35,8 @@ HIT_DTYPE = np.dtype([("kind", "u1"), ("pad0", "u1", 3), ("distance", "<f4"), ("
                       ("other", "<u4"), ("share", "<f4"), ("loosened", "<f4"), ("leaf_kind", "u1"), ("pad1", "u1", 3), ("cell", "<u4")])
 PROGRAM_REF_DTYPE = np.dtype([("first", "<u4"), ("count", "<u4"), ("result", "<u4")])
 MATERIAL_DTYPE = np.dtype([("kind", "<u4"), ("albedo", "<f4", 3), ("roughness", "<f4"), ("refraction", "<f4"), ("dispersion", "<f4"),
-                           ("absorb", "<f4", 3), ("glow", "<f4", 3), ("strength", "<f4"), ("flags", "<u4"), ("pad", "<u4")])
+                           ("absorb", "<f4", 3), ("glow", "<f4", 3), ("strength", "<f4"), ("flags", "<u4"),
+                           ("scatter", "<f4"), ("lean", "<f4"), ("pad", "<u4")])
 LIGHT_DTYPE = np.dtype([("kind", "<u4"), ("radius", "<f4"), ("angle", "<f4"), ("pad", "<f4"), ("at", "<f8", 3), ("direction", "<f8", 3),
                         ("along", "<f8", 3), ("across", "<f8", 3), ("power", "<f8", 3)])
 SKY_DTYPE = np.dtype([("zenith", "<f8", 3), ("horizon", "<f8", 3), ("ground", "<f8", 3)])
@@ -49,7 +50,7 @@ BOUNDARY_DTYPE = np.dtype([("rarer", "<f8", (17, 32)), ("denser", "<f8", (17, 32
 FINISH_DTYPE = np.dtype([("kind", "<u4"), ("sharp", "<u4"), ("exact", "<u4"), ("loses_much", "<u4"), ("width", "<f8"), ("facet_share", "<f8"),
                          ("body", "<f8"), ("index", "<f8"), ("coat_front", "<f8"), ("coat_twice", "<f8"), ("coat_room", "<f8"),
                          ("escape_average", "<f8"), ("escape", "<f8", 32), ("film", "<f8", 2)])
-assert RAY_DTYPE.itemsize == 36 and HIT_DTYPE.itemsize == 56 and MATERIAL_DTYPE.itemsize == 64 and LIGHT_DTYPE.itemsize == 136
+assert RAY_DTYPE.itemsize == 36 and HIT_DTYPE.itemsize == 56 and MATERIAL_DTYPE.itemsize == 72 and LIGHT_DTYPE.itemsize == 136
 assert FINISH_DTYPE.itemsize == 352
 
 
@@ -60,7 +61,7 @@ class BuildOptions(ctypes.Structure):
 class Frame(ctypes.Structure):
     _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("samples", ctypes.c_int32), ("surfaces", ctypes.c_int32),
                 ("seed", ctypes.c_int32), ("first", ctypes.c_uint32), ("accumulate", ctypes.c_uint32), ("flags", ctypes.c_uint32),
-                ("factor", ctypes.c_uint32), ("phase", ctypes.c_uint32)]
+                ("factor", ctypes.c_uint32), ("phase", ctypes.c_uint32), ("collisions", ctypes.c_int32), ("pad", ctypes.c_uint32)]
 
 
 # core/shown.cpp bayerPhase: the order a film factor's phases are drawn in
@@ -250,6 +251,8 @@ def scene_blocks(scene: Scene) -> dict[str, np.ndarray]:
     mats["glow"] = m["glow"]
     mats["strength"] = m["strength"]
     mats["flags"] = m["patterned"]
+    mats["scatter"] = m["scatter"] if "scatter" in m else 0
+    mats["lean"] = m["lean"] if "lean" in m else 0
     finishes = None
     if "finish_kind" in m:
         finishes = np.zeros(len(m["finish_kind"]), FINISH_DTYPE)
@@ -402,7 +405,8 @@ class Backend:
         """Pilot frames decide whether the attached guide's sampling stays on
         (kdn_guide_select): returns (guided, plain cost, guided cost)."""
         sc = self.scene
-        f = Frame(width, height, samples, surfaces if surfaces is not None else int(sc.render["surfaces"]), seed, 0, 0, 0)
+        f = Frame(width, height, samples, surfaces if surfaces is not None else int(sc.render["surfaces"]), seed, 0, 0, 0, 0, 0,
+                  int(sc.render.get("collisions", 0)))
         g, pc, gc = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
         self._check(self.lib.kdn_guide_select(self.handle, ctypes.byref(f), ctypes.byref(g), ctypes.byref(pc), ctypes.byref(gc)))
         return bool(g.value), pc.value, gc.value
@@ -427,7 +431,7 @@ class Backend:
                   seed if seed is not None else int(sc.render["seed"]), first, 1 if accumulate else 0,
                   (FRAME_DENOISE if denoise else 0) | (FRAME_RESTART if restart else 0) | (FRAME_TEMPORAL if temporal_only else 0) |
                   (FRAME_UPSAMPLE if upsample else 0) | (FRAME_SOBOL if sobol else 0) | (FRAME_SKY_MAP if sky_map else 0) |
-                  (FRAME_EACH_LAMP if each_lamp_first else 0), factor, phase)
+                  (FRAME_EACH_LAMP if each_lamp_first else 0), factor, phase, int(sc.render.get("collisions", 0)))
         out = np.zeros((height, width, 3), np.float32)
         self._check(self.lib.kdn_render(self.handle, ctypes.byref(f), _ptr(out)))
         return out

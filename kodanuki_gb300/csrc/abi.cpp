@@ -44,7 +44,7 @@ static_assert(sizeof(kdn_step) == 32, "kdn_step is the reference's 32-byte Step"
 static_assert(sizeof(kdn_ray) == 36, "kdn_ray is the reference's 36-byte Ray");
 static_assert(sizeof(kdn_hit) == 56, "kdn_hit is the reference's 56-byte Hit");
 static_assert(sizeof(kdn_program_ref) == 12, "kdn_program_ref is 12 bytes");
-static_assert(sizeof(kdn_material) == 64, "kdn_material is 64 bytes");
+static_assert(sizeof(kdn_material) == 72, "kdn_material is 72 bytes");
 static_assert(sizeof(kdn_light) == 136, "kdn_light is 136 bytes");
 static_assert(sizeof(kdn_finish) == 352, "kdn_finish is 352 bytes");
 static_assert(sizeof(kdn_sky) == 72, "kdn_sky is 72 bytes");

@@ -67,6 +67,9 @@ struct DeviceMaterial {
 	// material.cpp:106 filmOf: the thin film a metal, plastic or glass wears
 	// (thickness in nanometres, 0 for none; its index)
 	float filmThickness, filmIndex;
+	// scattering.cpp:7 scatters: a glass whose body turns aside `scatter` a
+	// unit of travel (0: none), by Henyey-Greenstein's phase of g = lean
+	float scatter, lean;
 };
 
 // material/energy.h Boundary as floats: rarer and denser (17 ratios x 32
@@ -127,6 +130,10 @@ struct FrameConstants {
 	// --use sampler=each_lamp_first: at the first vertex each of the first
 	// kOwnLines lamps whose offer is bright traces a line of its own
 	uint32_t eachLamp;
+	// scattering.cpp:29 sceneScatters: some glass body scatters; render.h
+	// collisions: the most collisions a path stands on (weight.cpp:23 atDepthCap)
+	uint32_t scatters;
+	uint32_t collisionCap;
 	float zenith[3], horizon[3], ground[3];
 	// sdf/scene.cpp:306 firstSun: the first sun's unit direction, where the
 	// scene has one (a moon's phase follows it)
@@ -151,6 +158,9 @@ struct PathBuffers {
 	// vertex brought (kOwnLines a path, in the lamps' order; zero where none
 	// or blocked), added to the radiance at the next vertex or at the fold
 	float4* held;
+	// where a body scatters: the collisions each path has stood on (the
+	// path's depth is state's surface count plus these)
+	uint32_t* collided;
 };
 
 // PathBuffers::state bits 10-12: how many of the path's shadow lines were

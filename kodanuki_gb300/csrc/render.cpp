@@ -28,7 +28,8 @@ struct FrameState {
 	DeviceBuffer pixel, sample, throughput, radiance, nanometres, density, drawn, state, from;
 	DeviceBuffer queuePaths[2], queueRays[2], queueCarry[2], hits, states, counts;
 	DeviceBuffer shadowPaths[2], shadowContribution[2];
-	DeviceBuffer held; // the own lines' answers (--use sampler=each_lamp_first)
+	DeviceBuffer held;     // the own lines' answers (--use sampler=each_lamp_first)
+	DeviceBuffer collided; // each path's collisions inside scattering bodies
 	// the surfaces pass's own queue, states and hits, so it runs beside the
 	// lanes' chunks on its own stream
 	DeviceBuffer surfacePaths, surfaceRays, surfaceStates, surfaceHits;
@@ -77,7 +78,7 @@ struct FrameState {
 void Context::releaseFrame() {
 	if (frame == nullptr) return;
 	FrameState& f = *frame;
-	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.queueCarry[0], &f.queueCarry[1], &f.hits, &f.states, &f.counts, &f.shadowPaths[0], &f.shadowPaths[1], &f.shadowContribution[0], &f.shadowContribution[1], &f.held, &f.surfacePaths, &f.surfaceRays, &f.surfaceStates, &f.surfaceHits, &f.sums, &f.out, &f.materials, &f.patternSteps, &f.stops, &f.placements, &f.boundaries, &f.frameLight, &f.firstDistance, &f.firstNormal, &f.firstAlbedo, &f.firstLeaf, &f.gDistance[0], &f.gDistance[1], &f.gNormal[0], &f.gNormal[1], &f.gAlbedo[0], &f.gAlbedo[1], &f.gLeaf[0], &f.gLeaf[1], &f.tColour[0], &f.tColour[1], &f.tMoment[0], &f.tMoment[1], &f.tLength[0], &f.tLength[1], &f.internal, &f.upState[0], &f.upState[1], &f.upscale.samples, &f.upscale.axes, &f.skyChart, &f.guideLobes, &f.guideRecords }) {
+	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.queueCarry[0], &f.queueCarry[1], &f.hits, &f.states, &f.counts, &f.shadowPaths[0], &f.shadowPaths[1], &f.shadowContribution[0], &f.shadowContribution[1], &f.held, &f.collided, &f.surfacePaths, &f.surfaceRays, &f.surfaceStates, &f.surfaceHits, &f.sums, &f.out, &f.materials, &f.patternSteps, &f.stops, &f.placements, &f.boundaries, &f.frameLight, &f.firstDistance, &f.firstNormal, &f.firstAlbedo, &f.firstLeaf, &f.gDistance[0], &f.gDistance[1], &f.gNormal[0], &f.gNormal[1], &f.gAlbedo[0], &f.gAlbedo[1], &f.gLeaf[0], &f.gLeaf[1], &f.tColour[0], &f.tColour[1], &f.tMoment[0], &f.tMoment[1], &f.tLength[0], &f.tLength[1], &f.internal, &f.upState[0], &f.upState[1], &f.upscale.samples, &f.upscale.axes, &f.skyChart, &f.guideLobes, &f.guideRecords }) {
 		if (b->ptr) cudaFree(b->ptr);
 		b->ptr   = nullptr;
 		b->bytes = 0;
@@ -197,6 +198,8 @@ DeviceMaterial materialOf(const kdn_material& m, const kdn_finish& f) {
 	d.losesMuch     = m.kind == 3 && !f.exact && f.loses_much ? 1u : 0u;
 	d.filmThickness = m.kind == 0 ? 0.0f : float(f.film[0]);
 	d.filmIndex     = float(f.film[1]);
+	d.scatter       = m.kind == 3 && m.scatter > 0.0f ? m.scatter : 0.0f;
+	d.lean          = m.lean;
 	for (int k = 0; k < 32; ++k) d.escape[k] = float(f.escape[k]);
 	return d;
 }
@@ -289,12 +292,12 @@ using kdn::kLanes;
 namespace {
 
 // Device bytes one path of a chunk holds (the buffers ensureFrame sizes).
-// pixel, sample, drawn, state; throughput, radiance, nanometres, density,
+// pixel, sample, drawn, state, collided; throughput, radiance, nanometres, density,
 // from; the two queues' path indices, rays and resume data (a path ray and
 // a shadow line each); hits; hit states of a path ray and a line; the two
 // line queues' path indices and contributions.
-constexpr size_t kPathBytes = 4 * 4 + 5 * 16 + 2 * 4 + 2 * 2 * (sizeof(kdn_ray) + sizeof(uint2)) + sizeof(kdn_hit) + 2 * sizeof(kdn::HitState) + 2 * (4 + 16);
-static_assert(kPathBytes == 416, "path bytes");
+constexpr size_t kPathBytes = 5 * 4 + 5 * 16 + 2 * 4 + 2 * 2 * (sizeof(kdn_ray) + sizeof(uint2)) + sizeof(kdn_hit) + 2 * sizeof(kdn::HitState) + 2 * (4 + 16);
+static_assert(kPathBytes == 420, "path bytes");
 // ... and with own lines (--use sampler=each_lamp_first) kOwnLines more
 // lines a path in each queue, their hit states and their held answers
 constexpr size_t kOwnPathBytes = kdn::kOwnLines * (2 * (sizeof(kdn_ray) + sizeof(uint2)) + sizeof(kdn::HitState) + 2 * (4 + 16) + 16);
@@ -341,7 +344,7 @@ kdn_status ensureFrame(Context* ctx, uint32_t capacity, uint32_t lineRoom) {
 		size_t bytes;
 	};
 	const Want wants[] = {
-		{ &f.pixel, n * 4 }, { &f.sample, n * 4 }, { &f.throughput, n * 16 }, { &f.radiance, n * 16 }, { &f.nanometres, n * 16 },
+		{ &f.pixel, n * 4 }, { &f.sample, n * 4 }, { &f.collided, n * 4 }, { &f.throughput, n * 16 }, { &f.radiance, n * 16 }, { &f.nanometres, n * 16 },
 		{ &f.density, n * 16 }, { &f.drawn, n * 4 }, { &f.state, n * 4 }, { &f.from, n * 16 },
 		// a lane's queue holds a bounce's path rays in [0, capacity) and the
 		// shadow lines of the bounce before in [capacity, (1 + lineRoom)
@@ -365,6 +368,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	if (!ctx->built) return ctx->fail(KDN_NOT_READY, "kdn_render: no world built (kdn_build)");
 	if (fr->width <= 0 || fr->height <= 0 || fr->samples <= 0 || fr->surfaces <= 0 || fr->surfaces > 255) return ctx->fail(KDN_BAD_ARG, "kdn_render: width, height, samples and surfaces (1..255) must be positive");
 	if (uint64_t(fr->width) * uint64_t(fr->height) > (uint64_t(1) << 26)) return ctx->fail(KDN_BAD_ARG, "kdn_render: frame larger than 2^26 pixels");
+	if (fr->collisions < 0 || fr->collisions > 4096) return ctx->fail(KDN_BAD_ARG, "kdn_render: collisions must be 0 (the default, 256) or 1..4096");
 	if (fr->samples > (1 << 20)) return ctx->fail(KDN_BAD_ARG, "kdn_render: more than 2^20 samples a pixel in one call (accumulate over calls)");
 	// core/camera.h:65 FilmPlan: the frame is drawn at 1/factor of its size
 	const uint32_t factor = fr->factor > 1 ? fr->factor : 1u;
@@ -503,6 +507,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		}
 	}
 	c.eachLamp      = ownLines ? 1u : 0u;
+	c.collisionCap  = fr->collisions > 0 ? uint32_t(fr->collisions) : 256u;
 	c.seedMix       = mixedBits(uint64_t(int64_t(fr->seed)));
 	c.surfaces      = fr->surfaces;
 	c.spp           = spp;
@@ -530,6 +535,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	for (size_t k = 0; k < mats.size(); ++k) {
 		dm.push_back(materialOf(mats[k], finishes[k]));
 		if (dm.back().filmThickness > 0.0f) c.films = 1;
+		if (dm.back().scatter > 0.0f) c.scatters = 1;
 	}
 	// material/energy.h Boundary of each rough glass that loses much
 	std::vector<float> boundaryTables;
@@ -582,6 +588,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	P.state      = static_cast<uint32_t*>(f.state.ptr);
 	P.from       = static_cast<float4*>(f.from.ptr);
 	P.held       = ownLines ? static_cast<float4*>(f.held.ptr) : nullptr;
+	P.collided   = c.scatters ? static_cast<uint32_t*>(f.collided.ptr) : nullptr;
 	// Lanes: the frame's chunks go round kLanes streams, each lane with its own
 	// share of the path buffers, queues and counters, so one chunk's work
 	// fills the SMs another chunk's launch leaves idle in its tail (the
@@ -622,6 +629,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		L.P.state         = P.state + base;
 		L.P.from          = P.from + base;
 		L.P.held          = ownLines ? P.held + base * kOwnLines : nullptr;
+		L.P.collided      = P.collided ? P.collided + base : nullptr;
 		// a queue's path rays and hit states in [0, capacity), the shadow lines
 		// traced with them in [capacity, capacity + lineCapacity): one trace
 		// launch takes both
@@ -645,13 +653,16 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		L.records = training ? static_cast<GuideRecord*>(f.guideRecords.ptr) + base * kGuideDepth : nullptr;
 	}
 
-	// Rounds a chunk: surfaces + 1 (each traces the bounce's path rays and
+	// Rounds a chunk: surfaces + 1 (+ the collision cap where a body
+	// scatters; each traces the bounce's path rays and
 	// the lines of the bounce before; the last, the last lines).  With a
 	// march budget a path waits a round each time its ray or its line is
 	// carried, at most once a round, so surfaces + 1 more rounds without a
 	// budget finish every path that waited.
 	const bool budgeted     = ctx->marchBudget > 0 && ctx->marchBudget < kMarchSteps && !guiding;
-	const int mainRounds    = fr->surfaces + 1;
+	// with scattering bodies a path also stands on up to collisionCap
+	// collisions, a round each
+	const int mainRounds    = fr->surfaces + 1 + (c.scatters ? int(c.collisionCap) : 0);
 	const int rounds        = budgeted ? 2 * mainRounds : mainRounds;
 
 	// timing: one event pair around the frame, one around each trace launch

@@ -32,7 +32,7 @@ using Clock = std::chrono::steady_clock;
 // Device bytes a path takes in a frame's buffers (render.cpp kPathBytes),
 // and a pixel's (sums, record, G-buffer, temporal state, image: 128; the
 // surfaces pass's own queue, states and hits: 116).
-constexpr uint64_t kPathBytes  = 416;
+constexpr uint64_t kPathBytes  = 420;
 constexpr uint64_t kPixelBytes = 128 + 116;
 // Stream priority of interactive requests (lower is more urgent; clamped
 // to the device's range by kdn_open_sharing).

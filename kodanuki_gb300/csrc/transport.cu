@@ -62,9 +62,30 @@ __device__ __forceinline__ float number(const uint32_t* sobol, uint64_t stream, 
 // dimensionOf's plain draws, five an event from 2^20 (MixturePart,
 // MixtureLump, AimPart, AimJitterU, AimJitterV)
 constexpr uint64_t kPlainFirst = uint64_t(1) << 20;
+// ... and path.cpp:13 collisionFirst: the Collision draw, one an event from 2^22
+constexpr uint64_t kCollisionFirst = uint64_t(1) << 22;
 enum PlainDraw : int { AimPart = 2, AimJitterU = 3, AimJitterV = 4 };
 __device__ __forceinline__ float plainNumber(uint64_t stream, uint32_t index, int event, int draw) {
 	return unitFrom(hashedBits(stream, index, kPlainFirst + uint64_t(event) * 5u + uint64_t(draw)));
+}
+
+// material.cpp:1051 phaseCosine, :1059 phaseScatter: a direction drawn
+// from Henyey-Greenstein's phase of g = lean about the heading, exactly
+// (its weight is 1 and its density the phase's value)
+__device__ __forceinline__ float phaseValue(float lean, float cosine) {
+	const float denominator = fmaxf(1.0f + lean * lean - 2.0f * lean * cosine, 0.0f);
+	return (1.0f - lean * lean) / (4.0f * 3.14159265358979f * denominator * sqrtf(denominator));
+}
+
+__device__ float3 phaseDirection(float lean, float3 heading, float u, float v) {
+	float cosine = 1.0f - 2.0f * u;
+	if (fabsf(lean) > 1e-3f) {
+		const float term = (1.0f - lean * lean) / (1.0f - lean + 2.0f * lean * u);
+		cosine           = fminf(fmaxf((1.0f + lean * lean - term * term) / (2.0f * lean), -1.0f), 1.0f);
+	}
+	const float reach = sqrtf(fmaxf(1.0f - cosine * cosine, 0.0f));
+	const float angle = 2.0f * 3.14159265358979f * v;
+	return frameAround(heading).toWorld(make_float3(reach * cosf(angle), reach * sinf(angle), cosine));
 }
 
 // plugins/transport/paths/trace.cpp:66 pixelNumbers
@@ -476,6 +497,7 @@ __global__ void __launch_bounds__(kBlock) cameraKernel(const __grid_constant__ F
 		if (P.held != nullptr) {
 			for (uint32_t k = 0; k < kOwnLines; ++k) P.held[size_t(p) * kOwnLines + k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 		}
+		if (P.collided != nullptr) P.collided[p] = 0u;
 		Q.paths[p]      = p;
 		Q.rays[p]       = makeRay(f3(cFrame.eye), heading, __int_as_float(0x7f800000), kNoMaterial);
 	}
@@ -592,9 +614,10 @@ __global__ void __launch_bounds__(kBlock) surfacesKernel(SurfaceArgs A) {
 }
 
 // ---- K-shade ----
-// Films: built twice, so that a frame without thin films runs a kernel with
-// no film code (the frame's FrameConstants::films picks one)
-template <bool Films>
+// Films, Scatters: built for each, so that a frame without thin films or
+// scattering bodies runs a kernel with no code for them (the frame's
+// FrameConstants::films and ::scatters pick one)
+template <bool Films, bool Scatters>
 __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ FrameConstants cFrame, ShadeArgs A) {
 	const uint32_t n = *A.in.count;
 	for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -628,7 +651,11 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 			const kdn_hit hit   = A.hits[q];
 			const kdn_ray ray   = A.in.rays[q];
 			const uint32_t st   = A.paths.state[p];
-			const int depth     = int(st & 0xFFu);
+			// the surfaces stood on, the collisions inside scattering bodies,
+			// and the path's depth (every vertex: the events its numbers follow)
+			const int surfaceDepth    = int(st & 0xFFu);
+			const uint32_t collisions = A.paths.collided != nullptr ? A.paths.collided[p] : 0u;
+			const int depth           = surfaceDepth + int(collisions);
 			const bool camera   = (st >> 8) & 1u;
 			uint32_t medium     = (st >> 16) == 0 ? kNoMaterial : (st >> 16) - 1u;
 			float4 T            = A.paths.throughput[p];
@@ -657,13 +684,38 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 				const DeviceMaterial& body = A.looks.materials[medium < cFrame.materialCount ? medium : 0u];
 				thickness                  = spectrumOf(body.absorb[0], body.absorb[1], body.absorb[2], nm);
 			}
+			// trace.cpp:250 stopOf: a leg inside a scattering body collides
+			// where a free flight drawn as -ln(1 - u) / scatter ends before its
+			// hit (scattering.cpp:61 scatteredAlong; u the event's Collision
+			// draw, trace.cpp:198 collisionNumber)
+			bool collided    = false;
+			float collidedAt = 0.0f;
+			float flight     = __int_as_float(0x7f800000);
+			if (Scatters && medium != kNoMaterial) {
+				const DeviceMaterial& body = A.looks.materials[medium < cFrame.materialCount ? medium : 0u];
+				if (body.scatter > 0.0f) {
+					const uint32_t px    = A.paths.pixel[p];
+					const uint64_t drawn = hashedBits(streamOf(cFrame, px % uint32_t(cFrame.width), px / uint32_t(cFrame.width)), A.paths.sample[p], kCollisionFirst + uint64_t(depth));
+					const double far     = -log(1.0 - double(drawn) * 0x1p-53) / double(body.scatter);
+					flight               = float(far);
+					const float3 leg     = make_float3(hit.point[0] - A.paths.from[p].x, hit.point[1] - A.paths.from[p].y, hit.point[2] - A.paths.from[p].z);
+					if (found && far < double(sqrtf(dot3(leg, leg)))) {
+						collided   = true;
+						collidedAt = flight;
+					}
+				}
+			}
+			// trace.cpp:218 keptAlong of the walked leg; a scattering body's
+			// absorption reaches only as far as the drawn flight
+			// (feature.cpp:358 mediumAlong over collisionAlong's `at`)
 			const auto keptOver = [&](float distance) {
-				return absorbing ? make_float4(expf(-thickness.x * distance), expf(-thickness.y * distance), expf(-thickness.z * distance), expf(-thickness.w * distance))
+				const float reach = fminf(distance, flight);
+				return absorbing ? make_float4(expf(-thickness.x * reach), expf(-thickness.y * reach), expf(-thickness.z * reach), expf(-thickness.w * reach))
 				                 : make_float4(1.0f, 1.0f, 1.0f, 1.0f);
 			};
 			// meet: lamps along the leg (not for camera legs) and the sky past it
 			if (!camera) {
-				const float limit = found ? hit.distance : 3.0e38f;
+				const float limit = collided ? collidedAt : (found ? hit.distance : 3.0e38f);
 				const float3 from = make_float3(A.paths.from[p].x, A.paths.from[p].y, A.paths.from[p].z);
 				for (uint32_t k = 0; k < cFrame.lampCount; ++k) {
 					const DeviceLamp& l = cFrame.lamps[k];
@@ -710,6 +762,39 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 					w              = drawnDensity * drawnDensity / (drawnDensity * drawnDensity + pa * pa);
 				}
 				R = add4(R, scale4(mul4(mul4(T, keptOver(__int_as_float(0x7f800000))), spectrumOf(sky.x, sky.y, sky.z, nm)), w));
+			} else if (Scatters && collided) {
+				// trace.cpp:502 collidedOn: the phase vertex (trace.cpp:474
+				// phaseVertex) at the collision, what the leg's body kept up
+				// to it; a bending body is not aimed from (trace.cpp:579
+				// aimsFromCollision), so the vertex only scatters
+				const DeviceMaterial& body = A.looks.materials[medium < cFrame.materialCount ? medium : 0u];
+				const float3 point         = make_float3(A.paths.from[p].x, A.paths.from[p].y, A.paths.from[p].z) + heading * collidedAt;
+				if (absorbing) T = mul4(T, keptOver(collidedAt));
+				const uint32_t stood = collisions + 1u;
+				// weight.cpp:23 atDepthCap: the surfaces stood on, or the collisions
+				if (surfaceDepth < cFrame.surfaces && stood < cFrame.collisionCap) {
+					const uint32_t px     = A.paths.pixel[p];
+					const uint64_t stream = streamOf(cFrame, px % uint32_t(cFrame.width), px / uint32_t(cFrame.width));
+					const uint32_t index  = A.paths.sample[p];
+					const float3 incoming = phaseDirection(body.lean, heading, number(cFrame.sobol, stream, index, depth, DirectionU),
+					                                       number(cFrame.sobol, stream, index, depth, DirectionV));
+					float4 carried        = T; // the phase's weight is 1
+					bool alive            = true;
+					if (depth >= 4) {
+						const float survival = fminf(0.95f, max4(carried));
+						if (!(number(cFrame.sobol, stream, index, depth, Survival) < survival)) alive = false;
+						else carried = scale4(carried, 1.0f / survival);
+					}
+					if (alive) {
+						onward              = true;
+						T                   = carried;
+						next                = makeRay(point, incoming, __int_as_float(0x7f800000), medium);
+						A.paths.drawn[p]    = 0.0f; // the next leg's meets take their light whole
+						A.paths.from[p]     = make_float4(point.x, point.y, point.z, 0.0f);
+						A.paths.collided[p] = stood;
+						A.paths.state[p]    = uint32_t(surfaceDepth) | (st & (1u << 9)) | ((medium + 1u) << 16);
+					}
+				}
 			} else {
 				const uint32_t material = hit.leaf < A.looks.leafCount ? A.looks.leafMaterial[hit.leaf] : 0u;
 				const DeviceMaterial& m = A.looks.materials[material < cFrame.materialCount ? material : 0u];
@@ -739,7 +824,7 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 				const uint32_t y        = A.paths.pixel[p] / uint32_t(cFrame.width);
 				const uint64_t stream   = streamOf(cFrame, x, y);
 				const uint32_t index    = A.paths.sample[p];
-				const bool capped       = depth + 1 >= cFrame.surfaces;
+				const bool capped       = surfaceDepth + 1 >= cFrame.surfaces || collisions >= cFrame.collisionCap;
 				const float3 outgoing   = heading * -1.0f;
 				const float3 rgb        = albedoAt(hit, normal, A.looks);
 				const Shading surf      = surfaceOf<Films>(m, rgb, normal, outgoing, nm, medium, A.looks.materials, A.looks.boundaries);
@@ -872,7 +957,7 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 								r.reached = T0.x + T0.y + T0.z + T0.w;
 							}
 							A.paths.from[p]       = make_float4(point.x, point.y, point.z, 0.0f);
-							uint32_t stNext       = uint32_t(depth + 1) | (medium == kNoMaterial ? 0u : ((medium + 1u) << 16));
+							uint32_t stNext       = uint32_t(surfaceDepth + 1) | (medium == kNoMaterial ? 0u : ((medium + 1u) << 16));
 							if (s.dispersed || ((st >> 9) & 1u)) stNext |= 1u << 9;
 							A.paths.state[p]      = stNext;
 						}
@@ -988,11 +1073,11 @@ cudaError_t launchCamera(const FrameConstants& frame, const PathBuffers& paths, 
 }
 
 cudaError_t launchShade(const FrameConstants& frame, const ShadeArgs& args, cudaStream_t stream, int smCount) {
-	if (frame.films) {
-		shadeKernel<true><<<gridFor(args.capacity, smCount), kBlock, 0, stream>>>(frame, args);
-	} else {
-		shadeKernel<false><<<gridFor(args.capacity, smCount), kBlock, 0, stream>>>(frame, args);
-	}
+	const uint32_t grid = gridFor(args.capacity, smCount);
+	if (frame.films && frame.scatters) shadeKernel<true, true><<<grid, kBlock, 0, stream>>>(frame, args);
+	else if (frame.films) shadeKernel<true, false><<<grid, kBlock, 0, stream>>>(frame, args);
+	else if (frame.scatters) shadeKernel<false, true><<<grid, kBlock, 0, stream>>>(frame, args);
+	else shadeKernel<false, false><<<grid, kBlock, 0, stream>>>(frame, args);
 	return cudaGetLastError();
 }
 

@@ -124,6 +124,8 @@ class Scene:
             "absorb": np.array([m["absorb"] for m in ms], np.float64).reshape(-1, 3),
             "glow": np.array([m["glow"] for m in ms], np.float64).reshape(-1, 3),
             "strength": np.array([m["strength"] for m in ms], np.float32),
+            "scatter": np.array([m.get("scatter", 0) for m in ms], np.float32),
+            "lean": np.array([m.get("lean", 0) for m in ms], np.float32),
         }
         fs = d.get("finishes", [])
         if fs:

@@ -454,6 +454,36 @@ def scene_far_lights(seed: int = 1, width: int = 256, height: int = 256, samples
     return "".join(out)
 
 
+def scene_scattering(seed: int = 1, width: int = 256, height: int = 256, samples: int = 16, surfaces: int = 8, count: int = 8) -> str:
+    """Scattering bodies: a rough glass ball that scatters forward (refraction
+    1.35, roughness 0.2, scatter 4, lean 0.3, a faint blue absorption), a
+    smooth glass box that scatters backward (refraction 1.5, scatter 2.5,
+    lean -0.2) and a smooth glass ball that scatters evenly (scatter 1.5),
+    among config-1 plastics on a plastic ground; one quad light, a dim sky."""
+    rng = random.Random(seed)
+    out = [_header(width, height, samples, surfaces, seed, [0.0, -8.5, 3.2], [0.0, 0.0, -0.6], 0.75)]
+    out.append(_sky([0.05, 0.05, 0.06]))
+    out.append(_quad([-1.25, 1.25, 4.5], [2.5, 0.0, 0.0], [0.0, -2.5, 0.0], blackbody_rgb(5000.0, 40.0)))
+    out.append("paint(plastic([0.5, 0.5, 0.5], roughness = 0.5)) plane([0, 0, 1], -2.2);\n\n")
+    out.append("paint(glass(refraction = 1.35, absorb = [0.05, 0.08, 0.2], roughness = 0.2, scatter = 4, lean = 0.3)) at([-1.1, 0.2, -1.2]) sphere(0.9);\n")
+    out.append("paint(glass(refraction = 1.5, scatter = 2.5, lean = -0.2)) at([1.2, -0.3, -1.5]) box([1.2, 1.2, 1.2], 0.05);\n")
+    out.append("paint(glass(refraction = 1.45, scatter = 1.5)) at([0.1, 1.4, -1.6]) sphere(0.6);\n\n")
+    # the plastics stay clear of the glass bodies (a body must not overlap another)
+    bodies = [([-1.1, 0.2, -1.2], 1.1), ([1.2, -0.3, -1.5], 1.1), ([0.1, 1.4, -1.6], 0.8)]
+    out.append("merge(0.05) {\n")
+    placed = 0
+    while placed < count:
+        pos = [rng.uniform(-2.5, 2.5), rng.uniform(-2.0, 2.5), rng.uniform(-1.9, 0.5)]
+        r = rng.uniform(0.2, 0.4)
+        if any(math.dist(pos, c) < rr + r + 0.1 for c, rr in bodies):
+            continue
+        albedo = [rng.uniform(0.2, 0.8) for _ in range(3)]
+        out.append(f"\tpaint(plastic({_v(albedo)}, roughness = {_f(rng.uniform(0.1, 0.5))})) at({_v(pos)}) sphere({_f(r)});\n")
+        placed += 1
+    out.append("}\n")
+    return "".join(out)
+
+
 _PATTERNS = """function bands(count) {
 	return 0.5 + 0.5 * sin(p.z * count);
 }

@@ -173,7 +173,8 @@ class Material(ctypes.Structure):
                 ("escape_average", ctypes.c_double), ("escape", ctypes.c_double * 32), ("glow", ctypes.c_double * 3),
                 ("absorb", ctypes.c_double * 3), ("pattern", Program), ("pattern_arguments", ctypes.c_void_p),
                 ("stops", ctypes.c_void_p), ("stop_count", ctypes.c_uint32), ("world", ctypes.c_uint32),
-                ("loses_much", ctypes.c_uint32), ("boundary", ctypes.c_void_p), ("film", ctypes.c_double * 2)]
+                ("loses_much", ctypes.c_uint32), ("boundary", ctypes.c_void_p), ("film", ctypes.c_double * 2),
+                ("scatter", ctypes.c_double), ("lean", ctypes.c_double)]
 
 
 def _materials(scene):
@@ -194,6 +195,9 @@ def _materials(scene):
             mats[i].absorb[c] = float(m["absorb"][i][c]) if "absorb" in m else 0.0
         mats[i].index = float(m["finish_index"][i]) if "finish_index" in m else 1.0
         mats[i].dispersion = float(m["dispersion"][i]) if int(m["kind"][i]) == 3 else 0.0
+        if "scatter" in m and int(m["kind"][i]) == 3:
+            mats[i].scatter = float(m["scatter"][i])
+            mats[i].lean = float(m["lean"][i])
         if "finish_width" in m:
             mats[i].width = float(m["finish_width"][i])
             mats[i].facet_share = float(m["finish_facet_share"][i])
@@ -243,7 +247,7 @@ class View(ctypes.Structure):
                 ("width", ctypes.c_int32), ("height", ctypes.c_int32), ("spp", ctypes.c_int32), ("surfaces", ctypes.c_int32),
                 ("seed", ctypes.c_int32), ("lamp_count", ctypes.c_uint32), ("material_count", ctypes.c_uint32),
                 ("factor", ctypes.c_uint32), ("phase", ctypes.c_uint32), ("sobol", ctypes.c_uint32), ("sky_map", ctypes.c_uint32),
-                ("each_lamp", ctypes.c_uint32), ("middle", ctypes.c_double * 3)]
+                ("each_lamp", ctypes.c_uint32), ("middle", ctypes.c_double * 3), ("collisions", ctypes.c_int32)]
 
 
 _trees: dict = {}
@@ -295,6 +299,7 @@ def render_band(scene, width: int, height: int, spp: int, surfaces: int, seed: i
     v.width, v.height, v.spp, v.surfaces, v.seed = width, height, spp, surfaces, seed
     v.lamp_count, v.material_count = nl, n
     v.factor, v.phase, v.sobol, v.sky_map, v.each_lamp = factor, phase, int(sobol), int(sky_map), int(each_lamp_first)
+    v.collisions = int(scene.render.get("collisions", 0)) or 256
     lower = np.asarray(scene.region_lower, np.float64)
     size = np.asarray(scene.region_size, np.float64)
     for a in range(3):

@@ -986,7 +986,9 @@ static void trace_one(march* m, const double lower[3], const double size[3], kp_
 		values_at(m, t, m->cand, values);
 		hit->steps = (uint32_t) step + 1;
 		const double tol = tolerance_at(m, t), inset = 2 * tol;
-		if (m->cand->empty) {
+		/* an empty cell, or from inside a body one it fills (no surface
+		 * passes through it: the full field's steps would cross it whole) */
+		if (m->cand->empty || (ray->inside && m->cand->n == 0)) {
 			t = dmax(m->cand->exit_t, t) + SPHERE_TOL;
 			continue;
 		}

@@ -150,6 +150,9 @@ typedef struct kp_material {
 	/* material.cpp:106 filmOf: the thin film a metal, plastic or glass
 	 * wears, thickness in nanometres (0: none) and index */
 	double film[2];
+	/* scattering.cpp:7 scatters: a glass whose body turns aside `scatter`
+	 * a unit of travel (0: none), by Henyey-Greenstein's phase of g = lean */
+	double scatter, lean;
 } kp_material;
 
 /* A lamp (light.cpp:78 lampOf): kind 0 point, 1 directional, 2 sphere,
@@ -179,6 +182,8 @@ typedef struct kp_view {
 	 * first four lamps that offer light traces a line of its own */
 	uint32_t each_lamp;
 	double middle[3];
+	/* render.collisions: the most collisions a path stands on */
+	int32_t collisions;
 } kp_view;
 
 /*

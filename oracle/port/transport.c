@@ -1213,7 +1213,7 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 	v3 from = J->eye;
 	spec T = flat(1), R = flat(0);
 	double drawn = 0;
-	int camera = 1, dispersed = 0;
+	int camera = 1, dispersed = 0, collisions = 0;
 	uint32_t medium = NO_MATERIAL;
 	for (int depth = 0;; ++depth) {
 		kp_hit hit;
@@ -1221,8 +1221,25 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 		const v3 origin = mk(ray.origin[0], ray.origin[1], ray.origin[2]);
 		heading = mk(ray.direction[0], ray.direction[1], ray.direction[2]);
 		const int found = hit.kind != 0;
+		/* trace.cpp:250 stopOf: a leg inside a scattering body collides where
+		 * a free flight -ln(1 - u) / scatter ends before its hit
+		 * (scattering.cpp:61 scatteredAlong; u the event's Collision draw,
+		 * path.cpp:28 dimensionOf: 2^22 + event) */
+		int collided = 0;
+		double collided_at = 0, flight = INFINITY;
+		if (medium != NO_MATERIAL && J->materials[medium].scatter > 0) {
+			flight = -log(1 - kp_hashed(stream, index, ((uint64_t) 1 << 22) + (uint64_t) depth)) / J->materials[medium].scatter;
+			if (found && flight < len(sub(mk(hit.point[0], hit.point[1], hit.point[2]), from))) {
+				collided = 1;
+				collided_at = flight;
+			}
+		}
+		/* trace.cpp:218 keptAlong of the walked leg: a scattering body's
+		 * absorption reaches only as far as the drawn flight
+		 * (feature.cpp:358 mediumAlong over collisionAlong's `at`) */
+#define KEPT(d) kept_along(J, medium, mind((d), flight), &w)
 		if (!camera) {
-			const double limit = found ? hit.distance : INFINITY;
+			const double limit = collided ? collided_at : (found ? hit.distance : INFINITY);
 			for (uint32_t k = 0; k < V->lamp_count; ++k) {
 				double reach;
 				if (!meet_lamp(&J->lamps[k], origin, heading, limit, &reach)) continue;
@@ -1231,7 +1248,7 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 					const double pa = aim_density(&J->lamps[k], from, heading, reach);
 					wgt = drawn * drawn / (drawn * drawn + pa * pa);
 				}
-				R = sadd(R, sscale(smul(smul(T, kept_along(J, medium, reach, &w)), spectrum(J->lamps[k].radiance, &w)), wgt * moon_lit(&J->lamps[k], J->has_sun, heading)));
+				R = sadd(R, sscale(smul(smul(T, KEPT(reach)), spectrum(J->lamps[k].radiance, &w)), wgt * moon_lit(&J->lamps[k], J->has_sun, heading)));
 			}
 		}
 		if (!found) {
@@ -1244,15 +1261,50 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 				const double pa = chart_density(J->chart, heading);
 				wgt = drawn * drawn / (drawn * drawn + pa * pa);
 			}
-			R = sadd(R, sscale(smul(smul(T, kept_along(J, medium, INFINITY, &w)), spectrum(sky, &w)), wgt));
+			R = sadd(R, sscale(smul(smul(T, KEPT(INFINITY)), spectrum(sky, &w)), wgt));
 			break;
+		}
+		if (collided) {
+			/* trace.cpp:502 collidedOn: the phase vertex at the collision
+			 * (:474 phaseVertex), what the body kept up to it; a bending body
+			 * is not aimed from (:579 aimsFromCollision), so it only scatters */
+			const kp_material* body = &J->materials[medium];
+			const v3 point = add(from, scl(heading, collided_at));
+			T = smul(T, KEPT(collided_at));
+			++collisions;
+			/* weight.cpp:23 atDepthCap */
+			if (depth + 1 - collisions >= V->surfaces || collisions >= V->collisions) break;
+			/* material.cpp:1051 phaseCosine, :1059 phaseScatter */
+			const double u = number(J->sobol, stream, index, depth, DIRECTION_U), v = number(J->sobol, stream, index, depth, DIRECTION_V);
+			const double g = body->lean;
+			double cosine = 1 - 2 * u;
+			if (fabs(g) > 1e-3) {
+				const double term = (1 - g * g) / (1 - g + 2 * g * u);
+				cosine = (1 + g * g - term * term) / (2 * g);
+				cosine = cosine < -1 ? -1 : (cosine > 1 ? 1 : cosine);
+			}
+			const double reach = sqrt(maxd(1 - cosine * cosine, 0)), angle = 2 * PI * v;
+			const v3 incoming = to_world(basis_around(heading), mk(reach * cos(angle), reach * sin(angle), cosine));
+			spec carried = T;
+			if (depth >= 4) {
+				const double survival = mind(0.95, smax(carried));
+				if (!(number(J->sobol, stream, index, depth, SURVIVAL) < survival)) break;
+				carried = sscale(carried, 1 / survival);
+			}
+			T = carried;
+			drawn = 0;
+			camera = 0;
+			from = point;
+			ray = ray_of(point, incoming, INFINITY, medium);
+			continue;
 		}
 		const uint32_t material = hit.leaf != 0xFFFFFFFFu ? J->leaf_material[hit.leaf] : 0;
 		const kp_material* m = &J->materials[material < V->material_count ? material : 0];
 		const v3 point = mk(hit.point[0], hit.point[1], hit.point[2]);
 		v3 normal = mk(hit.normal[0], hit.normal[1], hit.normal[2]);
 		/* trace.cpp:529 stoodOn: the leg's body keeps its share */
-		T = smul(T, kept_along(J, medium, sqrt(dotv(sub(point, origin), sub(point, origin))), &w));
+		T = smul(T, KEPT(sqrt(dotv(sub(point, origin), sub(point, origin)))));
+#undef KEPT
 		/* trace.cpp:415 metGlow at the vertex: the glow bsdfAt
 		 * (material.cpp:345) gives where the ray arrives from outside,
 		 * mixed across a blend seam; not aimed at by the plain sampler, so
@@ -1268,7 +1320,7 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 		}
 		if (dotv(normal, heading) >= 0) normal = scl(normal, -1);
 		const double lift = BIAS + 2 * 1e-6;
-		const int capped = depth + 1 >= V->surfaces;
+		const int capped = depth + 1 - collisions >= V->surfaces || collisions >= V->collisions;
 		const v3 out = scl(heading, -1);
 		double rgb[3];
 		albedo_at(J, &hit, normal, rgb);

@@ -111,7 +111,7 @@ int dumpScene(const char* sdf, const char* out) {
 		putColour(f, m.absorb);
 		std::fprintf(f, ",\"glow\":");
 		putColour(f, m.glow);
-		std::fprintf(f, ",\"strength\":%.9g,\"film\":[%.9g,%.9g],\"coats\":%zu", double(m.strength), double(m.film[0]), double(m.film[1]), file.looks.coats.size());
+		std::fprintf(f, ",\"strength\":%.9g,\"lean\":%.9g,\"film\":[%.9g,%.9g],\"coats\":%zu", double(m.strength), double(m.lean), double(m.film[0]), double(m.film[1]), file.looks.coats.size());
 		// sdf/scene.h Albedo: the pattern's program (Scene::programs), the
 		// arguments it reads (Scene::arguments from Albedo::arguments), and
 		// whether it is read in world space
@@ -194,7 +194,7 @@ int dumpScene(const char* sdf, const char* out) {
 	std::fprintf(f, ",\"up\":");
 	putVector(f, c.up);
 	std::fprintf(f, ",\"fov\":%.9g,\"aperture\":%.9g,\"focus\":%.9g},\n", double(c.fov), double(c.aperture), double(c.focus));
-	std::fprintf(f, "\"render\":{\"width\":%d,\"height\":%d,\"seed\":%d,\"samples\":%d,\"surfaces\":%d,\"far\":", r.width, r.height, r.seed, r.samples, r.surfaces);
+	std::fprintf(f, "\"render\":{\"width\":%d,\"height\":%d,\"seed\":%d,\"samples\":%d,\"surfaces\":%d,\"collisions\":%d,\"far\":", r.width, r.height, r.seed, r.samples, r.surfaces, r.collisions);
 	putDouble(f, r.far);
 	std::fprintf(f, "}}\n");
 	std::fclose(f);

@@ -14,10 +14,11 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("name, sampler", [("c2_small", None), ("room_small", None), ("glass_small", None), ("rough_small", None),
-                                           ("lamps_small", "each_lamp_first")])
+                                           ("lamps_small", "each_lamp_first"), ("scatter_small", None)])
 def test_frames_with_a_budget_equal_frames_without(name, sampler):
     """With --use sampler=each_lamp_first a path holds up to five lines at
-    its first vertex, each carried on its own."""
+    its first vertex, each carried on its own; in scatter_small paths stand
+    on collisions inside scattering bodies between their surfaces."""
     import kodanuki_gb300 as K
     sc = scene(name)
     extra = {sampler: True} if sampler else {}
