@@ -209,8 +209,7 @@ __device__ __forceinline__ float coneDensity(float cosine) {
 
 // sky_layers.cpp:273 moonLit: the share of a moon's disc the first sun
 // lights where a direction meets it, eased (in double: the disc is small)
-__device__ float moonLit(const FrameConstants& c, const DeviceLamp& l, float3 toward) {
-	if (l.kind != 5 || !c.hasSun) return 1.0f;
+__device__ __noinline__ float moonShare(const FrameConstants& c, const DeviceLamp& l, float3 toward) {
 	const double d[3]   = { double(toward.x), double(toward.y), double(toward.z) };
 	const double along  = d[0] * l.disc[0] + d[1] * l.disc[1] + d[2] * l.disc[2];
 	const double aside  = fmax(1.0 - along * along, 0.0);
@@ -221,8 +220,13 @@ __device__ float moonLit(const FrameConstants& c, const DeviceLamp& l, float3 to
 	return float(lit * lit * (3.0 - 2.0 * lit));
 }
 
-// aimLight (light.cpp:372) for every kind of lamp.
-__device__ Aim aimLamp(const DeviceLamp& l, float3 from, float u, float v) {
+__device__ __forceinline__ float moonLit(const FrameConstants& c, const DeviceLamp& l, float3 toward) {
+	return l.kind == 5 && c.hasSun ? moonShare(c, l, toward) : 1.0f;
+}
+
+// aimLight (light.cpp:372) for a point light, a directional light, a sun
+// or a moon (out of line: most scenes light by quads and spheres).
+__device__ __noinline__ Aim aimOther(const DeviceLamp& l, float3 from, float u, float v) {
 	Aim a;
 	a.found = false;
 	if (l.kind == 0) { // point (light.cpp:349 aimPoint): singular, density 0
@@ -257,6 +261,14 @@ __device__ Aim aimLamp(const DeviceLamp& l, float3 from, float u, float v) {
 		a.arriving = f3(l.radiance) * (2.0f * 3.14159265358979f * l.oneLess);
 		return a;
 	}
+	return a;
+}
+
+// aimLight (light.cpp:372) for every kind of lamp.
+__device__ Aim aimLamp(const DeviceLamp& l, float3 from, float u, float v) {
+	Aim a;
+	a.found = false;
+	if (l.kind != 2 && l.kind != 3) return aimOther(l, from, u, v);
 	if (l.kind == 3) { // quad
 		if (l.area < 1e-12f || dot3(f3(l.facing), from - f3(l.at)) <= 0.0f) return a;
 		float3 spot;
@@ -613,12 +625,26 @@ __global__ void __launch_bounds__(kBlock) surfacesKernel(SurfaceArgs A) {
 	}
 }
 
+// An own line of --use sampler=each_lamp_first (out of line: few frames
+// draw with it): the line and the slot it answers into (1 + its rank).
+__device__ __noinline__ void ownLine(const ShadowBuffers& S, uint32_t lineCapacity, uint32_t p, uint32_t rank, float3 from, float3 toward, float distance,
+                                     float4 offer) {
+	kdn_ray own    = makeRay(from, toward, distance, kNoMaterial);
+	own.pad_[1]    = uint8_t(rank + 1);
+	const uint32_t slot = warpSlot(S.count, true);
+	if (slot < lineCapacity) {
+		S.rays[slot]         = own;
+		S.paths[slot]        = p;
+		S.contribution[slot] = offer;
+	}
+}
+
 // ---- K-shade ----
 // Films, Scatters: built for each, so that a frame without thin films or
 // scattering bodies runs a kernel with no code for them (the frame's
 // FrameConstants::films and ::scatters pick one)
 template <bool Films, bool Scatters>
-__global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ FrameConstants cFrame, ShadeArgs A) {
+__global__ void __launch_bounds__(kBlock, 3) shadeKernel(const __grid_constant__ FrameConstants cFrame, ShadeArgs A) {
 	const uint32_t n = *A.in.count;
 	for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
 		const uint32_t q = base + threadIdx.x;
@@ -654,7 +680,7 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 			// the surfaces stood on, the collisions inside scattering bodies,
 			// and the path's depth (every vertex: the events its numbers follow)
 			const int surfaceDepth    = int(st & 0xFFu);
-			const uint32_t collisions = A.paths.collided != nullptr ? A.paths.collided[p] : 0u;
+			const uint32_t collisions = Scatters && A.paths.collided != nullptr ? A.paths.collided[p] : 0u;
 			const int depth           = surfaceDepth + int(collisions);
 			const bool camera   = (st >> 8) & 1u;
 			uint32_t medium     = (st >> 16) == 0 ? kNoMaterial : (st >> 16) - 1u;
@@ -869,15 +895,7 @@ __global__ void __launch_bounds__(kBlock) shadeKernel(const __grid_constant__ Fr
 						const float weight = mean4(offer);
 						if (!(weight > 0.0f)) continue;
 						if (cFrame.eachLamp && depth == 0 && k < cFrame.lampCount && owned < kOwnLines) {
-							kdn_ray own    = makeRay(point + open * lift, a.toward, a.distance - lift, kNoMaterial);
-							own.pad_[1]    = uint8_t(owned + 1);
-							++owned;
-							const uint32_t ownSlot = warpSlot(A.shadow.count, true);
-							if (ownSlot < A.lineCapacity) {
-								A.shadow.rays[ownSlot]         = own;
-								A.shadow.paths[ownSlot]        = p;
-								A.shadow.contribution[ownSlot] = offer;
-							}
+							ownLine(A.shadow, A.lineCapacity, p, owned++, point + open * lift, a.toward, a.distance - lift, offer);
 							continue;
 						}
 						total           = total + weight;
