@@ -161,11 +161,20 @@ typedef struct kdn_light {
 	double power[3]; /* linear RGB */
 } kdn_light;
 
-/* sdf/scene.h Sky, gradient kind: linear RGB zenith, horizon, ground. */
+/* sdf/scene.h Sky, 120 bytes: its kind (SkyKind: 0 gradient, 1 physical;
+ * a painted sky is refused); a gradient's linear RGB zenith, horizon and
+ * ground; a physical sky's haze and ground albedo (`ground`); the glow
+ * about the first sun (glow x strength, falling by e over `spread` radians:
+ * plugins/feature/sky_layers/sky_layers.cpp:181 glowSeen). */
 typedef struct kdn_sky {
 	double zenith[3];
 	double horizon[3];
 	double ground[3];
+	double glow[3];
+	double strength;
+	double spread;
+	uint32_t kind;
+	float haze;
 } kdn_sky;
 
 /* sdf/scene.h Camera and the Render fields a frame reads. */

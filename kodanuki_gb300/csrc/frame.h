@@ -139,6 +139,19 @@ struct FrameConstants {
 	// scene has one (a moon's phase follows it)
 	double sunDirection[3];
 	uint32_t hasSun;
+	// a physical sky lit by the first sun (atmosphere.h): the air's and the
+	// haze's tables (kAirTable floats each, null for none), the sky's frame,
+	// the sun's light thinned to the ground (`sunLamp` the lamp it thins) and
+	// what lands on the ground, the sunlight above the air and the ground's albedo
+	const float* airTables;
+	float airUp[3], airSun[3], airLevel[3], airAside[3];
+	float airPassed[33], airLanding[33];
+	float sunlight[3], airGround[3];
+	uint32_t sunLamp;
+	// sky_layers.cpp:181 glowSeen: the glow about the first sun (its colour
+	// times its strength, the angle it falls by e over, the sun's elevation)
+	uint32_t glows;
+	float glow[3], glowSpread, sunElevation;
 	DeviceLamp lamps[kMaxLamps];
 	SpectralTables spectral;
 };

@@ -7,6 +7,7 @@
 // synchronisation.  Pixel sums are kept in double on the device and persist
 // across calls (progressive accumulation) until a call starts afresh.
 #include "context.h"
+#include "atmosphere.h"
 #include "skymap.h"
 #include "sobol.h"
 #include "temporal.h"
@@ -48,6 +49,13 @@ struct FrameState {
 	DeviceBuffer internal, upState[2];
 	UpscaleScratch upscale;
 	DeviceBuffer skyChart; // --use sampler=sky_map's chart of the frame
+	// a physical sky's tables (air then haze, floats) and what they were
+	// marched for (the sun's direction and the haze), with the frame, passed
+	// and landing tables the constants take
+	DeviceBuffer airTables;
+	double airKey[4]   = { 0, 0, 0, -1 };
+	AirFrame airFrame  = {};
+	float airPassed[kAirColours] = {}, airLanding[kAirColours] = {};
 	DeviceBuffer guideLobes, guideRecords; // the learned guide's, a lane's capacity each
 	uint32_t capacity = 0;
 	uint32_t lineRoom = 1; // the shadow queues' room, in capacities (1 + kOwnLines with own lines)
@@ -78,7 +86,7 @@ struct FrameState {
 void Context::releaseFrame() {
 	if (frame == nullptr) return;
 	FrameState& f = *frame;
-	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.queueCarry[0], &f.queueCarry[1], &f.hits, &f.states, &f.counts, &f.shadowPaths[0], &f.shadowPaths[1], &f.shadowContribution[0], &f.shadowContribution[1], &f.held, &f.collided, &f.surfacePaths, &f.surfaceRays, &f.surfaceStates, &f.surfaceHits, &f.sums, &f.out, &f.materials, &f.patternSteps, &f.stops, &f.placements, &f.boundaries, &f.frameLight, &f.firstDistance, &f.firstNormal, &f.firstAlbedo, &f.firstLeaf, &f.gDistance[0], &f.gDistance[1], &f.gNormal[0], &f.gNormal[1], &f.gAlbedo[0], &f.gAlbedo[1], &f.gLeaf[0], &f.gLeaf[1], &f.tColour[0], &f.tColour[1], &f.tMoment[0], &f.tMoment[1], &f.tLength[0], &f.tLength[1], &f.internal, &f.upState[0], &f.upState[1], &f.upscale.samples, &f.upscale.axes, &f.skyChart, &f.guideLobes, &f.guideRecords }) {
+	for (DeviceBuffer* b : { &f.pixel, &f.sample, &f.throughput, &f.radiance, &f.nanometres, &f.density, &f.drawn, &f.state, &f.from, &f.queuePaths[0], &f.queuePaths[1], &f.queueRays[0], &f.queueRays[1], &f.queueCarry[0], &f.queueCarry[1], &f.hits, &f.states, &f.counts, &f.shadowPaths[0], &f.shadowPaths[1], &f.shadowContribution[0], &f.shadowContribution[1], &f.held, &f.collided, &f.surfacePaths, &f.surfaceRays, &f.surfaceStates, &f.surfaceHits, &f.sums, &f.out, &f.materials, &f.patternSteps, &f.stops, &f.placements, &f.boundaries, &f.frameLight, &f.firstDistance, &f.firstNormal, &f.firstAlbedo, &f.firstLeaf, &f.gDistance[0], &f.gDistance[1], &f.gNormal[0], &f.gNormal[1], &f.gAlbedo[0], &f.gAlbedo[1], &f.gLeaf[0], &f.gLeaf[1], &f.tColour[0], &f.tColour[1], &f.tMoment[0], &f.tMoment[1], &f.tLength[0], &f.tLength[1], &f.internal, &f.upState[0], &f.upState[1], &f.upscale.samples, &f.upscale.axes, &f.skyChart, &f.airTables, &f.guideLobes, &f.guideRecords }) {
 		if (b->ptr) cudaFree(b->ptr);
 		b->ptr   = nullptr;
 		b->bytes = 0;
@@ -389,6 +397,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	const std::vector<kdn_sky> skies         = ctx->block<kdn_sky>("lighting.sky");
 	if (lights.size() > kMaxLamps) return ctx->fail(KDN_BAD_ARG, "kdn_render: more than 16 lights");
 	if (mats.empty()) return ctx->fail(KDN_BAD_ARG, "kdn_render: no materials");
+	if (!skies.empty() && skies[0].kind > 1) return ctx->fail(KDN_BAD_ARG, "kdn_render: a painted sky, which this build does not draw");
 	const std::vector<kdn_finish> finishes = ctx->block<kdn_finish>("transport.finishes");
 	if (finishes.size() != mats.size()) return ctx->fail(KDN_NOT_READY, "kdn_render: the transport.finishes block needs one finish per material");
 	for (size_t k = 0; k < mats.size(); ++k) {
@@ -472,6 +481,65 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		}
 		c.sobol = static_cast<const uint32_t*>(ctx->sobolTables.ptr);
 	}
+	// the first sun (sdf/scene.cpp:306 firstSun)
+	uint32_t firstSun = uint32_t(lights.size());
+	for (size_t k = 0; k < lights.size(); ++k) {
+		if (lights[k].kind == 4) {
+			firstSun = uint32_t(k);
+			break;
+		}
+	}
+	const bool hasSun = firstSun < lights.size();
+	// a physical sky lit by a sun (atmosphere.cpp:308 atmosphereOf): its
+	// tables marched once a sun direction and haze
+	c.airTables = nullptr;
+	c.sunLamp   = 0xFFFFFFFFu;
+	if (!skies.empty() && skies[0].kind == 1 && hasSun) {
+		const kdn_light& sun = lights[firstSun];
+		const double key[4]  = { sun.direction[0], sun.direction[1], sun.direction[2], double(skies[0].haze) };
+		if (f.airTables.ptr == nullptr || !std::equal(key, key + 4, f.airKey)) {
+			std::vector<double> air(static_cast<size_t>(kAirTable)), haze(static_cast<size_t>(kAirTable)), passed(static_cast<size_t>(kAirColours)),
+			    landing(static_cast<size_t>(kAirColours));
+			buildAtmosphere(sun.direction, double(skies[0].haze), f.airFrame, air.data(), haze.data(), passed.data(), landing.data());
+			std::vector<float> tables(size_t(2) * kAirTable);
+			for (int k = 0; k < kAirTable; ++k) {
+				tables[size_t(k)]             = float(air[size_t(k)]);
+				tables[size_t(kAirTable + k)] = float(haze[size_t(k)]);
+			}
+			for (int k = 0; k < kAirColours; ++k) {
+				f.airPassed[k]  = float(passed[size_t(k)]);
+				f.airLanding[k] = float(landing[size_t(k)]);
+			}
+			if ((s = ctx->upload(f.airTables, tables.data(), tables.size() * sizeof(float))) != KDN_OK) return s;
+			if (!ctx->check(cudaStreamSynchronize(ctx->stream), "air tables")) return KDN_CUDA_ERROR;
+			std::copy(key, key + 4, f.airKey);
+		}
+		c.airTables = static_cast<const float*>(f.airTables.ptr);
+		for (int a = 0; a < 3; ++a) {
+			c.airUp[a]     = float(f.airFrame.up[a]);
+			c.airSun[a]    = float(f.airFrame.sun[a]);
+			c.airLevel[a]  = float(f.airFrame.level[a]);
+			c.airAside[a]  = float(f.airFrame.aside[a]);
+			c.sunlight[a]  = float(sun.power[a]);
+			c.airGround[a] = float(skies[0].ground[a]);
+		}
+		std::copy(f.airPassed, f.airPassed + kAirColours, c.airPassed);
+		std::copy(f.airLanding, f.airLanding + kAirColours, c.airLanding);
+		c.sunLamp = firstSun;
+	}
+	// sky_layers.cpp:164 skyGlows: a glow given and a sun
+	c.glows = 0;
+	if (!skies.empty() && hasSun) {
+		const double strength = skies[0].strength;
+		for (int a = 0; a < 3; ++a) c.glow[a] = float(skies[0].glow[a] * strength);
+		if (c.glow[0] > 0.0f || c.glow[1] > 0.0f || c.glow[2] > 0.0f) {
+			const V3 sun   = normalized(v3(lights[firstSun].direction));
+			c.glows        = 1;
+			c.glowSpread   = float(skies[0].spread);
+			c.sunElevation = float(std::asin(std::clamp(sun.z, -1.0, 1.0)));
+		}
+	}
+	if ((fr->flags & KDN_FRAME_SKY_MAP) && (c.airTables != nullptr || c.glows)) return ctx->fail(KDN_BAD_ARG, "kdn_render: the sky map charts a gradient sky without a glow only");
 	c.skyChart = nullptr;
 	if (fr->flags & KDN_FRAME_SKY_MAP) {
 		// plugins/sampler/sky_map/plugin.cpp:15 chartedSkyPrepared: charted

@@ -18,6 +18,7 @@
 #include "guide_mix.cuh"
 #include "materials.cuh"
 #include "program.cuh"
+#include "atmosphere.h"
 #include "skymap.h"
 #include "sobol.h"
 
@@ -432,6 +433,95 @@ __device__ float3 skyColour(const FrameConstants& cFrame, float3 dir) {
 	return f3(cFrame.horizon) * (1.0f - share) + far * share;
 }
 
+// math/spectrum.cpp:83 tablePlace, :88 spectrumTableAt: a 33-place table
+// over 380..700 nm read at each lane's wavelength
+__device__ __forceinline__ float tablePlaceOf(float nm) { return fminf(fmaxf((nm - 380.0f) / 320.0f, 0.0f), 1.0f) * 32.0f; }
+
+__device__ float4 tableSpectrum(const float* table, float4 nm) {
+	const float w[4] = { nm.x, nm.y, nm.z, nm.w };
+	float out[4];
+	for (int k = 0; k < 4; ++k) {
+		const float place = tablePlaceOf(w[k]);
+		const int low     = min(int(place), 31);
+		out[k]            = table[low] + (table[low + 1] - table[low]) * (place - float(low));
+	}
+	return make_float4(out[0], out[1], out[2], out[3]);
+}
+
+// atmosphere.cpp:206 airTableAt: trilinear in (row, column, colour)
+__device__ float airTableAt(const float* table, float row, float column, float colour) {
+	const int r = min(int(row), kAirHeights - 2), b = min(int(column), kAirBearings - 2), l = min(int(colour), kAirColours - 2);
+	const float fr = fminf(fmaxf(row - float(r), 0.0f), 1.0f), fb = fminf(fmaxf(column - float(b), 0.0f), 1.0f), fl = fminf(fmaxf(colour - float(l), 0.0f), 1.0f);
+	const float* t = table + (r * kAirBearings + b) * kAirColours + l;
+	const float lo = (1.0f - fb) * ((1.0f - fl) * t[0] + fl * t[1]) + fb * ((1.0f - fl) * t[kAirColours] + fl * t[kAirColours + 1]);
+	t += kAirBearings * kAirColours;
+	const float hi = (1.0f - fb) * ((1.0f - fl) * t[0] + fl * t[1]) + fb * ((1.0f - fl) * t[kAirColours] + fl * t[kAirColours + 1]);
+	return (1.0f - fr) * lo + fr * hi;
+}
+
+// atmosphere.cpp:312 airSeen: what the air shows along a direction (the
+// ground lit by the sun and the sky below the horizon), per lane
+__device__ __noinline__ float4 airSeen(const FrameConstants& c, float3 dir, float4 nm) {
+	const float4 sunlight = spectrumOf(c.sunlight[0], c.sunlight[1], c.sunlight[2], nm);
+	const float rise      = fminf(fmaxf(dot3(dir, f3(c.airUp)), -1.0f), 1.0f);
+	const float height    = asinf(rise);
+	if (height < 0.0f) {
+		return scale4(mul4(mul4(spectrumOf(c.airGround[0], c.airGround[1], c.airGround[2], nm), tableSpectrum(c.airLanding, nm)), sunlight), 1.0f / 3.14159265358979f);
+	}
+	const float bearing = fabsf(atan2f(dot3(dir, f3(c.airAside)), dot3(dir, f3(c.airLevel))));
+	const float row     = sqrtf(fmaxf(height, 0.0f) / (0.5f * 3.14159265358979f)) * float(kAirHeights - 1);
+	const float column  = bearing / 3.14159265358979f * float(kAirBearings - 1);
+	const float cosine  = dot3(dir, f3(c.airSun));
+	// the air's phase (Rayleigh) and the haze's (Cornette-Shanks, g = 0.76)
+	const float airPhase   = 3.0f / (16.0f * 3.14159265358979f) * (1.0f + cosine * cosine);
+	const float g          = 0.76f;
+	const float base       = fmaxf(1.0f + g * g - 2.0f * g * cosine, 1e-12f);
+	const float hazePhase  = 3.0f / (8.0f * 3.14159265358979f) * (1.0f - g * g) * (1.0f + cosine * cosine) / ((2.0f + g * g) * base * sqrtf(base));
+	const float w[4]       = { nm.x, nm.y, nm.z, nm.w };
+	float out[4];
+	for (int k = 0; k < 4; ++k) {
+		const float colour = tablePlaceOf(w[k]);
+		out[k] = airPhase * airTableAt(c.airTables, row, column, colour) + hazePhase * airTableAt(c.airTables + kAirTable, row, column, colour);
+	}
+	return mul4(make_float4(out[0], out[1], out[2], out[3]), sunlight);
+}
+
+// sky_layers.cpp:33 smoothShare
+__device__ __forceinline__ float smoothShare(float from, float to, float value) {
+	const float s = fminf(fmaxf((value - from) / (to - from), 0.0f), 1.0f);
+	return s * s * (3.0f - 2.0f * s);
+}
+
+// sky_layers.cpp:181 glowSeen: the glow about the first sun, falling by e
+// over `spread` radians from it, faded as the sun sinks 8 degrees below the
+// horizon and over the horizon, 0.02 either side
+__device__ __noinline__ float4 glowSeen(const FrameConstants& c, float3 dir, float4 nm) {
+	const float above   = smoothShare(-0.02f, 0.02f, dir.z);
+	const float apart   = acosf(fminf(fmaxf(float(double(dir.x) * c.sunDirection[0] + double(dir.y) * c.sunDirection[1] + double(dir.z) * c.sunDirection[2]), -1.0f), 1.0f));
+	const float fade    = smoothShare(-8.0f * 3.14159265358979f / 180.0f, 0.0f, c.sunElevation);
+	const float falling = expf(-apart / fmaxf(c.glowSpread, 1e-6f)) * fade * above;
+	return spectrumOf(c.glow[0] * falling, c.glow[1] * falling, c.glow[2] * falling, nm);
+}
+
+// feature.cpp:30 skyAt: the sky's radiance along a direction, per lane: the
+// gradient, or the air of a physical sky, and the glow about the sun
+__device__ __forceinline__ float4 skySpectrum(const FrameConstants& c, float3 dir, float4 nm) {
+	float4 sky;
+	if (c.airTables != nullptr) {
+		sky = airSeen(c, dir, nm);
+	} else {
+		const float3 rgb = skyColour(c, dir);
+		sky              = spectrumOf(rgb.x, rgb.y, rgb.z, nm);
+	}
+	return c.glows ? add4(sky, glowSeen(c, dir, nm)) : sky;
+}
+
+// feature.cpp:133 lampTint: what of a lamp's light the air lets through
+// (the first sun under a physical sky), per lane
+__device__ __forceinline__ float4 lampTint(const FrameConstants& c, uint32_t lamp, float4 nm) {
+	return c.airTables != nullptr && lamp == c.sunLamp ? tableSpectrum(c.airPassed, nm) : make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+}
+
 __device__ __forceinline__ kdn_ray makeRay(float3 o, float3 d, float far, uint32_t medium) {
 	kdn_ray r;
 	r.origin[0]    = o.x;
@@ -752,7 +842,8 @@ __global__ void __launch_bounds__(kBlock, 3) shadeKernel(const __grid_constant__
 						const float pa = aimDensityOf(l, from, heading, reach);
 						w              = drawnDensity * drawnDensity / (drawnDensity * drawnDensity + pa * pa);
 					}
-					R = add4(R, scale4(mul4(mul4(T, keptOver(reach)), spectrumOf(l.radiance[0], l.radiance[1], l.radiance[2], nm)), w * moonLit(cFrame, l, heading)));
+					R = add4(R, scale4(mul4(mul4(mul4(T, keptOver(reach)), spectrumOf(l.radiance[0], l.radiance[1], l.radiance[2], nm)), lampTint(cFrame, k, nm)),
+					                   w * moonLit(cFrame, l, heading)));
 				}
 			}
 			// the record's first surface of the pixel's last sample
@@ -781,13 +872,13 @@ __global__ void __launch_bounds__(kBlock, 3) shadeKernel(const __grid_constant__
 			if (!found) {
 				// the sky met, weighed against aiming at it by its chart
 				// (trace.cpp:294 meetAimDensity, sampler.cpp:344 aimDensityAt)
-				const float3 sky = skyColour(cFrame, heading);
+				const float4 sky = skySpectrum(cFrame, heading, nm);
 				float w          = 1.0f;
 				if (drawnDensity > 0.0f && cFrame.skyChart != nullptr) {
 					const float pa = float(chartDensity(cFrame.skyChart, heading.x, heading.y, heading.z));
 					w              = drawnDensity * drawnDensity / (drawnDensity * drawnDensity + pa * pa);
 				}
-				R = add4(R, scale4(mul4(mul4(T, keptOver(__int_as_float(0x7f800000))), spectrumOf(sky.x, sky.y, sky.z, nm)), w));
+				R = add4(R, scale4(mul4(mul4(T, keptOver(__int_as_float(0x7f800000))), sky), w));
 			} else if (Scatters && collided) {
 				// trace.cpp:502 collidedOn: the phase vertex (trace.cpp:474
 				// phaseVertex) at the collision, what the leg's body kept up
@@ -891,7 +982,9 @@ __global__ void __launch_bounds__(kBlock, 3) shadeKernel(const __grid_constant__
 							const float pm = capped ? 0.0f : (lobes ? share * mixtureDensity(lobes, a.toward) + (1.0f - share) * f.density : f.density);
 							w              = a.density * a.density / (a.density * a.density + pm * pm);
 						}
-						const float4 offer = scale4(mul4(mul4(T, f.value), spectrumOf(a.arriving.x, a.arriving.y, a.arriving.z, nm)), facing * w);
+						float4 arriving    = spectrumOf(a.arriving.x, a.arriving.y, a.arriving.z, nm);
+						if (k < cFrame.lampCount) arriving = mul4(arriving, lampTint(cFrame, k, nm));
+						const float4 offer = scale4(mul4(mul4(T, f.value), arriving), facing * w);
 						const float weight = mean4(offer);
 						if (!(weight > 0.0f)) continue;
 						if (cFrame.eachLamp && depth == 0 && k < cFrame.lampCount && owned < kOwnLines) {

@@ -484,6 +484,33 @@ def scene_scattering(seed: int = 1, width: int = 256, height: int = 256, samples
     return "".join(out)
 
 
+def scene_physical_sky(seed: int = 1, width: int = 256, height: int = 256, samples: int = 16, surfaces: int = 8, count: int = 12) -> str:
+    """Under a physical sky: config-1 primitives (plastics and metals) on a
+    plastic ground lit by a low sun (a disc 0.05 radians across) through
+    the air and haze of a physical sky with a glow about the sun; the camera
+    looks level enough to see the sky above the horizon."""
+    rng = random.Random(seed)
+    out = [_header(width, height, samples, surfaces, seed, [0.0, -8.5, 1.2], [0.0, 0.0, 0.2], 0.9)]
+    out.append("sky physical {\n\thaze     = 1.3;\n\tground   = [0.28, 0.30, 0.26];\n\tglow     = [1, 0.8, 0.55];\n"
+               "\tstrength = 0.5;\n\tspread   = 0.12;\n}\n\n")
+    out.append("light sun {\n\tdirection = [-0.5, 0.6, 0.35];\n\tangle     = 0.05;\n\tpower     = [3.1, 3, 2.8];\n}\n\n")
+    out.append("paint(plastic([0.5, 0.5, 0.5], roughness = 0.5)) plane([0, 0, 1], -2.2);\n\n")
+    out.append("merge(0.05) {\n")
+    for k in range(count):
+        pos = [rng.uniform(-2.0, 2.0), rng.uniform(-2.0, 2.0), rng.uniform(-2.0, 0.5)]
+        if k % 3 == 2:
+            mat = f"metal({_v([rng.uniform(0.5, 0.95) for _ in range(3)])}, roughness = {_f(rng.uniform(0.1, 0.4))})"
+        else:
+            mat = f"plastic({_v([rng.uniform(0.2, 0.8) for _ in range(3)])}, roughness = {_f(rng.uniform(0.1, 0.5))})"
+        if rng.random() < 0.5:
+            shape = f"sphere({_f(rng.uniform(0.25, 0.6))})"
+        else:
+            shape = f"box({_v([2 * rng.uniform(0.15, 0.45) for _ in range(3)])}, 0.02)"
+        out.append(f"\tpaint({mat}) at({_v(pos)}) {shape};\n")
+    out.append("}\n")
+    return "".join(out)
+
+
 _PATTERNS = """function bands(count) {
 	return 0.5 + 0.5 * sin(p.z * count);
 }

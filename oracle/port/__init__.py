@@ -247,7 +247,9 @@ class View(ctypes.Structure):
                 ("width", ctypes.c_int32), ("height", ctypes.c_int32), ("spp", ctypes.c_int32), ("surfaces", ctypes.c_int32),
                 ("seed", ctypes.c_int32), ("lamp_count", ctypes.c_uint32), ("material_count", ctypes.c_uint32),
                 ("factor", ctypes.c_uint32), ("phase", ctypes.c_uint32), ("sobol", ctypes.c_uint32), ("sky_map", ctypes.c_uint32),
-                ("each_lamp", ctypes.c_uint32), ("middle", ctypes.c_double * 3), ("collisions", ctypes.c_int32)]
+                ("each_lamp", ctypes.c_uint32), ("middle", ctypes.c_double * 3), ("collisions", ctypes.c_int32),
+                ("sky_kind", ctypes.c_uint32), ("haze", ctypes.c_double), ("glow", ctypes.c_double * 3), ("strength", ctypes.c_double),
+                ("spread", ctypes.c_double)]
 
 
 _trees: dict = {}
@@ -300,6 +302,12 @@ def render_band(scene, width: int, height: int, spp: int, surfaces: int, seed: i
     v.lamp_count, v.material_count = nl, n
     v.factor, v.phase, v.sobol, v.sky_map, v.each_lamp = factor, phase, int(sobol), int(sky_map), int(each_lamp_first)
     v.collisions = int(scene.render.get("collisions", 0)) or 256
+    v.sky_kind = int(scene.sky.get("kind", 0))
+    v.haze = float(np.float32(scene.sky.get("haze", 0)))
+    v.strength = float(np.float32(scene.sky.get("strength", 0)))
+    v.spread = float(np.float32(scene.sky.get("spread", 0)))
+    for c in range(3):
+        v.glow[c] = float(scene.sky.get("glow", [0, 0, 0])[c])
     lower = np.asarray(scene.region_lower, np.float64)
     size = np.asarray(scene.region_size, np.float64)
     for a in range(3):

@@ -184,6 +184,11 @@ typedef struct kp_view {
 	double middle[3];
 	/* render.collisions: the most collisions a path stands on */
 	int32_t collisions;
+	/* sdf/scene.h Sky: its kind (0 gradient, 1 physical), a physical sky's
+	 * haze (its ground albedo in `ground`), the glow about the first sun
+	 * (colour, strength, spread) */
+	uint32_t sky_kind;
+	double haze, glow[3], strength, spread;
 } kp_view;
 
 /*

@@ -1049,6 +1049,10 @@ typedef struct job {
 	const double* chart;      /* --use sampler=sky_map's chart, or none (the sky only met) */
 	v3 sun;                   /* sdf/scene.cpp:306 firstSun's direction ... */
 	const v3* has_sun;        /* ... or none */
+	struct air* sky_air;      /* a physical sky lit by the first sun, or none */
+	uint32_t sun_lamp;        /* the first sun, whose light the air thins */
+	int glows;                /* sky_layers.cpp:164 skyGlows */
+	double glow[3], sun_elevation;
 } job;
 
 /* trace.cpp:179 keptOnLeg with absorption.cpp:28 keptThrough: what a leg of
@@ -1082,6 +1086,202 @@ static void sky_colour(const kp_view* view, v3 d, double out[3]) {
 	const double* far = h >= 0 ? view->zenith : view->ground;
 	const double share = sqrt(fabs(h));
 	for (int c = 0; c < 3; ++c) out[c] = view->horizon[c] * (1 - share) + far[c] * share;
+}
+
+/* ---- a physical sky (plugins/feature/atmosphere/atmosphere.cpp) and the
+ * glow about the first sun (plugins/feature/sky_layers/sky_layers.cpp:181
+ * glowSeen): the air's and the haze's single scattering marched into tables
+ * of height, bearing and wavelength (48 x 32 x 33), their phases applied
+ * where the sky is met, the ground below the horizon lit by what lands on
+ * it, the sun's light thinned by what passes the air ---- */
+#define AIR_HEIGHTS 48
+#define AIR_BEARINGS 32
+#define AIR_COLOURS 33
+#define AIR_TABLE (AIR_HEIGHTS * AIR_BEARINGS * AIR_COLOURS)
+#define PLANET 6360.0
+#define AIR_TOP 6420.0
+
+typedef struct air {
+	v3 up, sun, level, aside;
+	double* air; /* AIR_TABLE, then the haze's AIR_TABLE */
+	double passed[AIR_COLOURS], landing[AIR_COLOURS];
+} air;
+
+static double air_wavelength(int colour) { return 380.0 + 320.0 * colour / (double) (AIR_COLOURS - 1); }
+static double air_scatter(double nm) { const double r = 440.0 / nm; return 33.1e-3 * r * r * r * r; }
+static double haze_scatter(double nm, double haze) { return 0.004 * haze * haze * pow(550.0 / nm, 1.3); }
+static double shell_leaving(v3 from, v3 d, double radius) {
+	const double along = dotv(from, d);
+	return -along + sqrt(maxd(along * along - (dotv(from, from) - radius * radius), 0.0));
+}
+static int ground_ahead(v3 from, v3 d) {
+	const double along = dotv(from, d), under = along * along - (dotv(from, from) - PLANET * PLANET);
+	return under >= 0.0 && -along - sqrt(under) > 0.0;
+}
+static void air_density(v3 at, double* a, double* h) {
+	const double height = maxd(len(at) - PLANET, 0.0);
+	*a = exp(-height / 8.0);
+	*h = exp(-height / 1.2);
+}
+static void sunward(v3 from, v3 sun, double* a, double* h) {
+	const double reach = shell_leaving(from, sun, AIR_TOP);
+	*a = *h = 0;
+	for (int k = 0; k < 12; ++k) {
+		const double n0 = k / 12.0, n1 = (k + 1) / 12.0, mid = (k + 0.5) / 12.0;
+		double da, dh;
+		air_density(add(from, scl(sun, reach * mid * mid)), &da, &dh);
+		*a += da * reach * (n1 * n1 - n0 * n0);
+		*h += dh * reach * (n1 * n1 - n0 * n0);
+	}
+}
+static double air_phase(double c) { return 3.0 / (16.0 * PI) * (1.0 + c * c); }
+static double haze_phase(double c) {
+	const double g = 0.76, g2 = g * g;
+	return 3.0 / (8.0 * PI) * (1.0 - g2) * (1.0 + c * c) / ((2.0 + g2) * pow(1.0 + g2 - 2.0 * g * c, 1.5));
+}
+static double air_lookup(const double* t, double row, double column, double colour) {
+	int r = (int) row, b = (int) column, l = (int) colour;
+	r = r < AIR_HEIGHTS - 2 ? r : AIR_HEIGHTS - 2;
+	b = b < AIR_BEARINGS - 2 ? b : AIR_BEARINGS - 2;
+	l = l < AIR_COLOURS - 2 ? l : AIR_COLOURS - 2;
+	double sum = 0;
+	for (int dr = 0; dr < 2; ++dr)
+		for (int db = 0; db < 2; ++db)
+			for (int dl = 0; dl < 2; ++dl) {
+				double fr = row - r, fb = column - b, fl = colour - l;
+				fr = fr < 0 ? 0 : (fr > 1 ? 1 : fr);
+				fb = fb < 0 ? 0 : (fb > 1 ? 1 : fb);
+				fl = fl < 0 ? 0 : (fl > 1 ? 1 : fl);
+				sum += (dr ? fr : 1 - fr) * (db ? fb : 1 - fb) * (dl ? fl : 1 - fl) * t[((r + dr) * AIR_BEARINGS + b + db) * AIR_COLOURS + l + dl];
+			}
+	return sum;
+}
+/* atmosphere.cpp:165 airPlaceOf and :222 skyTableAt at a table place */
+static double air_sky_at(const air* A, v3 d, double colour) {
+	const double rise = dotv(d, A->up) < -1 ? -1 : (dotv(d, A->up) > 1 ? 1 : dotv(d, A->up));
+	const double height = asin(rise);
+	const double bearing = fabs(atan2(dotv(d, A->aside), dotv(d, A->level)));
+	const double row = sqrt(maxd(height, 0.0) / (0.5 * PI)) * (AIR_HEIGHTS - 1), column = bearing / PI * (AIR_BEARINGS - 1);
+	const double c = dotv(d, A->sun);
+	return air_phase(c) * air_lookup(A->air, row, column, colour) + haze_phase(c) * air_lookup(A->air + AIR_TABLE, row, column, colour);
+}
+/* atmosphere.cpp:308 atmosphereOf */
+static void air_build(air* A, const double sun_direction[3], double haze) {
+	A->up = mk(0, 0, 1);
+	A->sun = unit(vd(sun_direction));
+	const v3 flat_sun = sub(A->sun, scl(A->up, dotv(A->sun, A->up)));
+	A->level = len(flat_sun) < 1e-9 ? mk(1, 0, 0) : unit(flat_sun);
+	A->aside = crossv(A->up, A->level);
+	A->air = (double*) calloc(2 * (size_t) AIR_TABLE, sizeof(double));
+	const v3 sun = mk(dotv(A->sun, A->level), dotv(A->sun, A->aside), dotv(A->sun, A->up));
+	const v3 eye = mk(0, 0, PLANET + 0.001);
+	for (int row = 0; row < AIR_HEIGHTS; ++row) {
+		const double along = row / (double) (AIR_HEIGHTS - 1), height = 0.5 * PI * along * along;
+		for (int column = 0; column < AIR_BEARINGS; ++column) {
+			const double bearing = PI * column / (double) (AIR_BEARINGS - 1);
+			const v3 view = mk(cos(height) * cos(bearing), cos(height) * sin(bearing), sin(height));
+			double* ta = A->air + (row * AIR_BEARINGS + column) * AIR_COLOURS;
+			double* th = ta + AIR_TABLE;
+			const double reach = shell_leaving(eye, view, AIR_TOP);
+			double seen_a = 0, seen_h = 0;
+			for (int k = 0; k < 40; ++k) {
+				const double n0 = k / 40.0, n1 = (k + 1) / 40.0, mid = (k + 0.5) / 40.0, span = reach * (n1 * n1 - n0 * n0);
+				const v3 at = add(eye, scl(view, reach * mid * mid));
+				double da, dh;
+				air_density(at, &da, &dh);
+				seen_a += da * span * 0.5;
+				seen_h += dh * span * 0.5;
+				if (!ground_ahead(at, sun)) {
+					double la, lh;
+					sunward(at, sun, &la, &lh);
+					for (int c = 0; c < AIR_COLOURS; ++c) {
+						const double nm = air_wavelength(c), scattered = haze_scatter(nm, haze);
+						const double thinned = exp(-(air_scatter(nm) * (seen_a + la) + scattered / 0.9 * (seen_h + lh)));
+						ta[c] += thinned * da * span * air_scatter(nm);
+						th[c] += thinned * dh * span * scattered;
+					}
+				}
+				seen_a += da * span * 0.5;
+				seen_h += dh * span * 0.5;
+			}
+		}
+	}
+	double sa, sh;
+	sunward(eye, sun, &sa, &sh);
+	const int set = ground_ahead(eye, sun);
+	for (int c = 0; c < AIR_COLOURS; ++c) {
+		const double nm = air_wavelength(c);
+		A->passed[c] = set ? 0 : exp(-(air_scatter(nm) * sa + haze_scatter(nm, haze) / 0.9 * sh));
+		A->landing[c] = 0;
+	}
+	for (int ring = 0; ring < 32; ++ring) {
+		const double rise = (ring + 0.5) / 32, level = sqrt(1 - rise * rise);
+		for (int spoke = 0; spoke < 64; ++spoke) {
+			const double turn = 2 * PI * (spoke + 0.5) / 64;
+			const v3 d = add(add(scl(A->level, level * cos(turn)), scl(A->aside, level * sin(turn))), scl(A->up, rise));
+			for (int c = 0; c < AIR_COLOURS; ++c) A->landing[c] += air_sky_at(A, d, c) * rise * (2 * PI / (32 * 64));
+		}
+	}
+	const double overhead = maxd(dotv(A->sun, A->up), 0);
+	for (int c = 0; c < AIR_COLOURS; ++c) A->landing[c] += A->passed[c] * overhead;
+}
+/* math/spectrum.cpp:83 tablePlace, :88 spectrumTableAt */
+static double table_place(double nm) {
+	double along = (nm - 380.0) / 320.0;
+	along = along < 0 ? 0 : (along > 1 ? 1 : along);
+	return along * (AIR_COLOURS - 1);
+}
+static spec table_spectrum(const double* table, const lanes* w) {
+	spec s;
+	for (int k = 0; k < 4; ++k) {
+		const double place = table_place(w->nm[k]);
+		const int low = (int) place < AIR_COLOURS - 2 ? (int) place : AIR_COLOURS - 2;
+		s.v[k] = table[low] + (table[low + 1] - table[low]) * (place - low);
+	}
+	return s;
+}
+/* atmosphere.cpp:312 airSeen */
+static spec air_seen(const air* A, const kp_view* V, const double sunlight[3], v3 d, const lanes* w) {
+	const spec light = spectrum(sunlight, w);
+	const double rise = dotv(d, A->up) < -1 ? -1 : (dotv(d, A->up) > 1 ? 1 : dotv(d, A->up));
+	if (asin(rise) < 0) return sscale(smul(smul(spectrum(V->ground, w), table_spectrum(A->landing, w)), light), 1 / PI);
+	spec s;
+	for (int k = 0; k < 4; ++k) s.v[k] = air_sky_at(A, d, table_place(w->nm[k]));
+	return smul(s, light);
+}
+static double smooth_share(double from, double to, double value) {
+	double s = (value - from) / (to - from);
+	s = s < 0 ? 0 : (s > 1 ? 1 : s);
+	return s * s * (3 - 2 * s);
+}
+
+/* feature.cpp:30 skyAt: the gradient, or the air of a physical sky, and the
+ * glow about the first sun (sky_layers.cpp:181 glowSeen) */
+static spec sky_seen(const job* J, v3 d, const lanes* w) {
+	const kp_view* V = J->view;
+	spec sky;
+	if (J->sky_air != NULL) {
+		sky = air_seen(J->sky_air, V, J->lamps[J->sun_lamp].power, d, w);
+	} else {
+		double rgb[3];
+		sky_colour(V, d, rgb);
+		sky = spectrum(rgb, w);
+	}
+	if (J->glows) {
+		const double above = smooth_share(-0.02, 0.02, d.z);
+		double c = dotv(d, J->sun);
+		c = c < -1 ? -1 : (c > 1 ? 1 : c);
+		const double fade = smooth_share(-8.0 * PI / 180.0, 0.0, J->sun_elevation);
+		const double falling = exp(-acos(c) / maxd(V->spread, 1e-6)) * fade * above;
+		const double g[3] = { J->glow[0] * falling, J->glow[1] * falling, J->glow[2] * falling };
+		sky = sadd(sky, spectrum(g, w));
+	}
+	return sky;
+}
+
+/* feature.cpp:133 lampTint: the first sun's light thinned by the air */
+static spec lamp_tint(const job* J, uint32_t k, const lanes* w) {
+	return J->sky_air != NULL && k == J->sun_lamp ? table_spectrum(J->sky_air->passed, w) : flat(1);
 }
 
 /* sky_map.cpp:138 chartedDirection, :144 chartAim: a direction from the
@@ -1248,20 +1448,19 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 					const double pa = aim_density(&J->lamps[k], from, heading, reach);
 					wgt = drawn * drawn / (drawn * drawn + pa * pa);
 				}
-				R = sadd(R, sscale(smul(smul(T, KEPT(reach)), spectrum(J->lamps[k].radiance, &w)), wgt * moon_lit(&J->lamps[k], J->has_sun, heading)));
+				R = sadd(R, sscale(smul(smul(smul(T, KEPT(reach)), spectrum(J->lamps[k].radiance, &w)), lamp_tint(J, k, &w)), wgt * moon_lit(&J->lamps[k], J->has_sun, heading)));
 			}
 		}
 		if (!found) {
 			/* the sky met, weighed against aiming at it by its chart
 			 * (trace.cpp:294 meetAimDensity, sampler.cpp:344 aimDensityAt) */
-			double sky[3];
-			sky_colour(V, heading, sky);
+			const spec sky = sky_seen(J, heading, &w);
 			double wgt = 1;
 			if (drawn > 0 && J->chart != NULL) {
 				const double pa = chart_density(J->chart, heading);
 				wgt = drawn * drawn / (drawn * drawn + pa * pa);
 			}
-			R = sadd(R, sscale(smul(smul(T, KEPT(INFINITY)), spectrum(sky, &w)), wgt));
+			R = sadd(R, sscale(smul(smul(T, KEPT(INFINITY)), sky), wgt));
 			break;
 		}
 		if (collided) {
@@ -1363,7 +1562,8 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 					const double pm = capped ? 0 : f.density;
 					wgt = a.density * a.density / (a.density * a.density + pm * pm);
 				}
-				const spec offer = sscale(smul(smul(T, f.value), spectrum(a.arriving, &w)), facing * wgt);
+				const spec arriving = k < V->lamp_count ? smul(spectrum(a.arriving, &w), lamp_tint(J, k, &w)) : spectrum(a.arriving, &w);
+				const spec offer = sscale(smul(smul(T, f.value), arriving), facing * wgt);
 				const double weight = smean(offer);
 				if (!(weight > 0)) continue;
 				if (V->each_lamp && depth == 0 && k < V->lamp_count && owned < 4) {
@@ -1496,6 +1696,26 @@ void kp_render_band(const kp_octree* tree, const uint32_t* leaf_material, const 
 		}
 	}
 	J.chart = chart;
+	/* a physical sky lit by the first sun (atmosphere.cpp:308), the glow
+	 * about the first sun (sky_layers.cpp:164 skyGlows) */
+	air sky_air;
+	J.sky_air = NULL;
+	J.sun_lamp = 0xFFFFFFFFu;
+	J.glows = 0;
+	for (uint32_t k = 0; k < view->lamp_count && k < 16; ++k) {
+		if (lamps[k].kind != 4) continue;
+		J.sun_lamp = k;
+		if (view->sky_kind == 1) {
+			air_build(&sky_air, lamps[k].direction, view->haze);
+			J.sky_air = &sky_air;
+		}
+		for (int c = 0; c < 3; ++c) J.glow[c] = view->glow[c] * view->strength;
+		J.glows = J.glow[0] > 0 || J.glow[1] > 0 || J.glow[2] > 0;
+		const v3 s = unit(vd(lamps[k].direction));
+		J.sun = s;
+		J.sun_elevation = asin(s.z < -1 ? -1 : (s.z > 1 ? 1 : s.z));
+		break;
+	}
 	uint32_t* sobol = NULL;
 	if (view->sobol) {
 		sobol = (uint32_t*) malloc(sizeof(uint32_t) * KP_SOBOL_DIMENSIONS * 512);
@@ -1509,5 +1729,6 @@ void kp_render_band(const kp_octree* tree, const uint32_t* leaf_material, const 
 	free(pool);
 	free(sobol);
 	free(chart);
+	if (J.sky_air != NULL) free(sky_air.air);
 	pthread_mutex_destroy(&J.lock);
 }

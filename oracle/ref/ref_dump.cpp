@@ -185,6 +185,9 @@ int dumpScene(const char* sdf, const char* out) {
 	putColour(f, sky.horizon);
 	std::fprintf(f, ",\"ground\":");
 	putColour(f, sky.ground);
+	std::fprintf(f, ",\"glow\":");
+	putColour(f, sky.glow);
+	std::fprintf(f, ",\"strength\":%.9g,\"spread\":%.9g,\"haze\":%.9g", double(sky.strength), double(sky.spread), double(sky.haze));
 	const Camera& c = file.shot.camera;
 	const Render& r = file.shot.render;
 	std::fprintf(f, "},\n\"camera\":{\"eye\":");

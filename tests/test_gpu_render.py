@@ -49,7 +49,7 @@ def compare(a, b):
 
 
 @pytest.mark.parametrize("name", ["room_small", "c1_small", "c2_small", "glow_small", "glass_small", "patterns_small", "rough_small", "films_small",
-                                  "skylit_small", "lamps_small", "far_small", "scatter_small"])
+                                  "skylit_small", "lamps_small", "far_small", "scatter_small", "physical_small"])
 def test_frame_matches_oracle_and_reference(backend, name):
     import oracle.port as op
     sc = scene(name)
@@ -113,6 +113,28 @@ def test_unsupported_material_is_refused(backend, kind, refraction):
         backend.render(8, 8, 1)
     assert e.value.status == K.KDN_BAD_ARG
     backend.upload("looks.materials", blocks["looks.materials"])
+
+
+def test_unsupported_sky_is_refused(backend):
+    """A painted sky is refused with KDN_BAD_ARG, and so is the sky map over
+    a physical sky (the chart is of a gradient sky's brightness); the same
+    scene's physical sky draws without the map."""
+    import kodanuki_gb300 as K
+    sc = scene("physical_small")
+    backend.load(sc)
+    backend.build(5, 10, 64)
+    with pytest.raises(K.KdnError) as e:
+        backend.render(8, 8, 1, sky_map=True)
+    assert e.value.status == K.KDN_BAD_ARG
+    assert np.isfinite(backend.render(8, 8, 1)).all()
+    blocks = K.scene_blocks(sc)
+    sky = blocks["lighting.sky"].copy()
+    sky["kind"] = 2
+    backend.upload("lighting.sky", sky)
+    with pytest.raises(K.KdnError) as e:
+        backend.render(8, 8, 1)
+    assert e.value.status == K.KDN_BAD_ARG
+    backend.upload("lighting.sky", blocks["lighting.sky"])
 
 
 def test_bad_patterns_are_refused(backend):
