@@ -106,6 +106,9 @@ struct Looks {
 struct FrameConstants {
 	float eye[3], forward[3], right[3], up[3];
 	float reach, aspect;
+	// core/camera.cpp:9 lensOf: a thin lens's radius (0: a pinhole) and the
+	// distance it is sharp at along the forward axis
+	float aperture, focus;
 	int32_t width, height;
 	uint64_t seedMix;
 	int32_t surfaces;

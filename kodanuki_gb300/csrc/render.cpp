@@ -465,6 +465,8 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	put(c.right, right);
 	put(c.up, cross(right, forward));
 	c.reach         = float(std::tan(cam.fov / 2));
+	c.aperture      = float(std::max(cam.aperture, 0.0));
+	c.focus         = float(cam.focus > 0 ? cam.focus : length(sub(target, eye)));
 	c.aspect        = float(double(drawnWidth) / double(drawnHeight));
 	c.width         = drawnWidth;
 	c.height        = drawnHeight;

@@ -586,7 +586,27 @@ __global__ void __launch_bounds__(kBlock) cameraKernel(const __grid_constant__ F
 		}
 		const float u  = 2.0f * px / float(cFrame.width) - 1.0f;
 		const float v  = 1.0f - 2.0f * py / float(cFrame.height);
-		const float3 heading = normalizedOf(f3(cFrame.forward) + f3(cFrame.right) * (u * cFrame.reach * cFrame.aspect) + f3(cFrame.up) * (v * cFrame.reach));
+		float3 heading = normalizedOf(f3(cFrame.forward) + f3(cFrame.right) * (u * cFrame.reach * cFrame.aspect) + f3(cFrame.up) * (v * cFrame.reach));
+		float3 origin  = f3(cFrame.eye);
+		if (cFrame.aperture > 0.0f) {
+			// plugins/transport/paths/camera.cpp:14 cameraRay: from a point of
+			// the lens (math/random.cpp:48 concentricDisc of the LensU/LensV
+			// pair) toward where the pinhole ray meets the plane in focus
+			const float ahead = cFrame.focus / fmaxf(dot3(heading, f3(cFrame.forward)), 1e-9f);
+			const float3 sharp = origin + heading * ahead;
+			const float a      = 2.0f * number(cFrame.sobol, stream, sample, 0, LensU) - 1.0f;
+			const float b      = 2.0f * number(cFrame.sobol, stream, sample, 0, LensV) - 1.0f;
+			float du = 0.0f, dv = 0.0f;
+			if (a != 0.0f || b != 0.0f) {
+				const bool wide    = fabsf(a) > fabsf(b);
+				const float radius = wide ? a : b;
+				const float angle  = wide ? 0.78539816f * (b / a) : 1.5707963f - 0.78539816f * (a / b);
+				du                 = radius * cosf(angle);
+				dv                 = radius * sinf(angle);
+			}
+			origin  = origin + f3(cFrame.right) * (du * cFrame.aperture) + f3(cFrame.up) * (dv * cFrame.aperture);
+			heading = normalizedOf(sharp - origin);
+		}
 		P.pixel[p]      = pixel;
 		P.sample[p]     = sample;
 		P.throughput[p] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
@@ -595,13 +615,13 @@ __global__ void __launch_bounds__(kBlock) cameraKernel(const __grid_constant__ F
 		P.density[p]    = make_float4(dens[0], dens[1], dens[2], dens[3]);
 		P.drawn[p]      = 0.0f;
 		P.state[p]      = 1u << 8;
-		P.from[p]       = make_float4(cFrame.eye[0], cFrame.eye[1], cFrame.eye[2], 0.0f);
+		P.from[p]       = make_float4(origin.x, origin.y, origin.z, 0.0f);
 		if (P.held != nullptr) {
 			for (uint32_t k = 0; k < kOwnLines; ++k) P.held[size_t(p) * kOwnLines + k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 		}
 		if (P.collided != nullptr) P.collided[p] = 0u;
 		Q.paths[p]      = p;
-		Q.rays[p]       = makeRay(f3(cFrame.eye), heading, __int_as_float(0x7f800000), kNoMaterial);
+		Q.rays[p]       = makeRay(origin, heading, __int_as_float(0x7f800000), kNoMaterial);
 	}
 }
 

@@ -484,6 +484,30 @@ def scene_scattering(seed: int = 1, width: int = 256, height: int = 256, samples
     return "".join(out)
 
 
+def scene_lens(seed: int = 1, width: int = 256, height: int = 256, samples: int = 16, surfaces: int = 8, count: int = 12) -> str:
+    """Through a thin lens: config-1 primitives (plastics and metals) on a
+    plastic ground, seen through a lens of radius 0.25 sharp 8 units ahead
+    (the nearer and further primitives blurred); one quad light, a dim sky."""
+    rng = random.Random(seed)
+    head = _header(width, height, samples, surfaces, seed, [0.0, -8.5, 3.2], [0.0, 0.0, -0.6], 0.75)
+    head = head.replace("\tfov    = 0.75;\n", "\tfov    = 0.75;\n\taperture = 0.25;\n\tfocus    = 8;\n")
+    assert "aperture" in head
+    out = [head, _sky([0.05, 0.05, 0.06])]
+    out.append(_quad([-1.25, 1.25, 4.5], [2.5, 0.0, 0.0], [0.0, -2.5, 0.0], blackbody_rgb(5000.0, 40.0)))
+    out.append("paint(plastic([0.5, 0.5, 0.5], roughness = 0.5)) plane([0, 0, 1], -2.2);\n\n")
+    out.append("merge(0.05) {\n")
+    for k in range(count):
+        pos = [rng.uniform(-2.5, 2.5), rng.uniform(-3.0, 3.0), rng.uniform(-2.0, 0.5)]
+        if k % 3 == 2:
+            mat = f"metal({_v([rng.uniform(0.5, 0.95) for _ in range(3)])}, roughness = {_f(rng.uniform(0.1, 0.4))})"
+        else:
+            mat = f"plastic({_v([rng.uniform(0.2, 0.8) for _ in range(3)])}, roughness = {_f(rng.uniform(0.1, 0.5))})"
+        shape = f"sphere({_f(rng.uniform(0.25, 0.6))})" if rng.random() < 0.5 else f"box({_v([2 * rng.uniform(0.15, 0.45) for _ in range(3)])}, 0.02)"
+        out.append(f"\tpaint({mat}) at({_v(pos)}) {shape};\n")
+    out.append("}\n")
+    return "".join(out)
+
+
 def scene_physical_sky(seed: int = 1, width: int = 256, height: int = 256, samples: int = 16, surfaces: int = 8, count: int = 12) -> str:
     """Under a physical sky: config-1 primitives (plastics and metals) on a
     plastic ground lit by a low sun (a disc 0.05 radians across) through

@@ -189,6 +189,9 @@ typedef struct kp_view {
 	 * (colour, strength, spread) */
 	uint32_t sky_kind;
 	double haze, glow[3], strength, spread;
+	/* core/camera.cpp:9 lensOf: a thin lens's radius (0: a pinhole) and
+	 * the distance it is sharp at (0: the target's) */
+	double aperture, focus;
 } kp_view;
 
 /*

@@ -1409,8 +1409,26 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 	const double py = factor > 1 ? y + (row + number(J->sobol, stream, index, 0, PIXEL_Y)) / factor : y + number(J->sobol, stream, index, 0, PIXEL_Y);
 	const double u = 2 * px / V->width - 1, v = 1 - 2 * py / V->height;
 	v3 heading = unit(add(add(J->forward, scl(J->right, u * J->reach * J->aspect)), scl(J->up, v * J->reach)));
-	kp_ray ray = ray_of(J->eye, heading, INFINITY, NO_MATERIAL);
 	v3 from = J->eye;
+	if (V->aperture > 0) {
+		/* plugins/transport/paths/camera.cpp:14 cameraRay: from a point of the
+		 * lens (math/random.cpp:48 concentricDisc) toward where the pinhole
+		 * ray meets the plane in focus */
+		const double focus = V->focus > 0 ? V->focus : len(sub(vd(V->target), J->eye));
+		const double ahead = focus / maxd(dotv(heading, J->forward), 1e-9);
+		const v3 sharp = add(J->eye, scl(heading, ahead));
+		const double a = 2 * number(J->sobol, stream, index, 0, LENS_U) - 1, b = 2 * number(J->sobol, stream, index, 0, LENS_V) - 1;
+		double du = 0, dv = 0;
+		if (a != 0 || b != 0) {
+			const int wide = fabs(a) > fabs(b);
+			const double radius = wide ? a : b, angle = wide ? PI / 4 * (b / a) : PI / 2 - PI / 4 * (a / b);
+			du = radius * cos(angle);
+			dv = radius * sin(angle);
+		}
+		from = add(add(J->eye, scl(J->right, du * V->aperture)), scl(J->up, dv * V->aperture));
+		heading = unit(sub(sharp, from));
+	}
+	kp_ray ray = ray_of(from, heading, INFINITY, NO_MATERIAL);
 	spec T = flat(1), R = flat(0);
 	double drawn = 0;
 	int camera = 1, dispersed = 0, collisions = 0;
