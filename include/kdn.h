@@ -226,7 +226,11 @@ typedef struct kdn_frame {
 	/* render.collisions: the most collisions inside scattering bodies a path
 	 * stands on, apart from its surfaces (0: the reference's default, 256) */
 	int32_t collisions;
-	uint32_t pad_;
+	/* render.split: 2, 4 or 8 samples share a first vertex (its camera ray,
+	 * wavelengths and aim; each branch scatters on its own,
+	 * plugins/transport/paths/trace.cpp:1568 branchedFrom), the aim there
+	 * weighed as one of that many (weight.cpp:15 sharedAim); 0 or 1: none */
+	uint32_t split;
 } kdn_frame;
 
 /* With KDN_FRAME_DENOISE a frame returns what the reference shows through

@@ -62,7 +62,7 @@ class BuildOptions(ctypes.Structure):
 class Frame(ctypes.Structure):
     _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("samples", ctypes.c_int32), ("surfaces", ctypes.c_int32),
                 ("seed", ctypes.c_int32), ("first", ctypes.c_uint32), ("accumulate", ctypes.c_uint32), ("flags", ctypes.c_uint32),
-                ("factor", ctypes.c_uint32), ("phase", ctypes.c_uint32), ("collisions", ctypes.c_int32), ("pad", ctypes.c_uint32)]
+                ("factor", ctypes.c_uint32), ("phase", ctypes.c_uint32), ("collisions", ctypes.c_int32), ("split", ctypes.c_uint32)]
 
 
 # core/shown.cpp bayerPhase: the order a film factor's phases are drawn in
@@ -435,7 +435,8 @@ class Backend:
                   seed if seed is not None else int(sc.render["seed"]), first, 1 if accumulate else 0,
                   (FRAME_DENOISE if denoise else 0) | (FRAME_RESTART if restart else 0) | (FRAME_TEMPORAL if temporal_only else 0) |
                   (FRAME_UPSAMPLE if upsample else 0) | (FRAME_SOBOL if sobol else 0) | (FRAME_SKY_MAP if sky_map else 0) |
-                  (FRAME_EACH_LAMP if each_lamp_first else 0), factor, phase, int(sc.render.get("collisions", 0)))
+                  (FRAME_EACH_LAMP if each_lamp_first else 0), factor, phase, int(sc.render.get("collisions", 0)),
+                  int(sc.render.get("split", 1)))
         out = np.zeros((height, width, 3), np.float32)
         self._check(self.lib.kdn_render(self.handle, ctypes.byref(f), _ptr(out)))
         return out

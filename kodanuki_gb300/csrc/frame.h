@@ -137,6 +137,8 @@ struct FrameConstants {
 	// collisions: the most collisions a path stands on (weight.cpp:23 atDepthCap)
 	uint32_t scatters;
 	uint32_t collisionCap;
+	// render.split: how many samples share a first vertex (1: none)
+	uint32_t split;
 	float zenith[3], horizon[3], ground[3];
 	// sdf/scene.cpp:306 firstSun: the first sun's unit direction, where the
 	// scene has one (a moon's phase follows it)

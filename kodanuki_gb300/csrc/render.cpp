@@ -377,6 +377,10 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	if (fr->width <= 0 || fr->height <= 0 || fr->samples <= 0 || fr->surfaces <= 0 || fr->surfaces > 255) return ctx->fail(KDN_BAD_ARG, "kdn_render: width, height, samples and surfaces (1..255) must be positive");
 	if (uint64_t(fr->width) * uint64_t(fr->height) > (uint64_t(1) << 26)) return ctx->fail(KDN_BAD_ARG, "kdn_render: frame larger than 2^26 pixels");
 	if (fr->collisions < 0 || fr->collisions > 4096) return ctx->fail(KDN_BAD_ARG, "kdn_render: collisions must be 0 (the default, 256) or 1..4096");
+	// core/frame.cpp:296 fittedSplit: a split divides the samples into whole groups
+	const uint32_t split = fr->split > 1 ? fr->split : 1u;
+	if ((split != 1 && split != 2 && split != 4 && split != 8) || uint32_t(fr->samples) % split != 0 || fr->first % split != 0)
+		return ctx->fail(KDN_BAD_ARG, "kdn_render: a split of 2, 4 or 8 needs whole groups of samples (samples and first multiples of it)");
 	if (fr->samples > (1 << 20)) return ctx->fail(KDN_BAD_ARG, "kdn_render: more than 2^20 samples a pixel in one call (accumulate over calls)");
 	// core/camera.h:65 FilmPlan: the frame is drawn at 1/factor of its size
 	const uint32_t factor = fr->factor > 1 ? fr->factor : 1u;
@@ -578,6 +582,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 	}
 	c.eachLamp      = ownLines ? 1u : 0u;
 	c.collisionCap  = fr->collisions > 0 ? uint32_t(fr->collisions) : 256u;
+	c.split         = split;
 	c.seedMix       = mixedBits(uint64_t(int64_t(fr->seed)));
 	c.surfaces      = fr->surfaces;
 	c.spp           = spp;

@@ -556,12 +556,15 @@ __global__ void __launch_bounds__(kBlock) cameraKernel(const __grid_constant__ F
 	for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
 		const uint32_t pixel  = firstPixel + p / cFrame.spp;
 		const uint32_t sample = cFrame.firstSample + p % cFrame.spp;
+		// core/pixels.cpp:5 groupSample: with a split the samples of a group
+		// share the first vertex's draws (path.cpp:37 sharedDraw)
+		const uint32_t group  = sample / cFrame.split;
 		const uint32_t x      = pixel % uint32_t(cFrame.width);
 		const uint32_t y      = pixel / uint32_t(cFrame.width);
 		const uint64_t stream = streamOf(cFrame, x, y);
 		// math/colour.cpp:236 sampledWavelengths of the pixel's golden-ratio share
 		const double start  = double(hashedBits(stream, ~uint64_t(0), 0)) * 0x1p-53;
-		const double turned = double(sample) * 0.6180339887498949 + start;
+		const double turned = double(group) * 0.6180339887498949 + start;
 		const double share  = turned - floor(turned);
 		float nm[4], dens[4];
 		for (int lane = 0; lane < 4; ++lane) {
@@ -578,11 +581,11 @@ __global__ void __launch_bounds__(kBlock) cameraKernel(const __grid_constant__ F
 		float px, py;
 		if (cFrame.factor > 1) {
 			const float factor = float(cFrame.factor);
-			px = float(x) + (float(cFrame.phase % cFrame.factor) + number(cFrame.sobol, stream, sample, 0, PixelX)) / factor;
-			py = float(y) + (float(cFrame.phase / cFrame.factor) + number(cFrame.sobol, stream, sample, 0, PixelY)) / factor;
+			px = float(x) + (float(cFrame.phase % cFrame.factor) + number(cFrame.sobol, stream, group, 0, PixelX)) / factor;
+			py = float(y) + (float(cFrame.phase / cFrame.factor) + number(cFrame.sobol, stream, group, 0, PixelY)) / factor;
 		} else {
-			px = float(x) + number(cFrame.sobol, stream, sample, 0, PixelX);
-			py = float(y) + number(cFrame.sobol, stream, sample, 0, PixelY);
+			px = float(x) + number(cFrame.sobol, stream, group, 0, PixelX);
+			py = float(y) + number(cFrame.sobol, stream, group, 0, PixelY);
 		}
 		const float u  = 2.0f * px / float(cFrame.width) - 1.0f;
 		const float v  = 1.0f - 2.0f * py / float(cFrame.height);
@@ -594,8 +597,8 @@ __global__ void __launch_bounds__(kBlock) cameraKernel(const __grid_constant__ F
 			// pair) toward where the pinhole ray meets the plane in focus
 			const float ahead = cFrame.focus / fmaxf(dot3(heading, f3(cFrame.forward)), 1e-9f);
 			const float3 sharp = origin + heading * ahead;
-			const float a      = 2.0f * number(cFrame.sobol, stream, sample, 0, LensU) - 1.0f;
-			const float b      = 2.0f * number(cFrame.sobol, stream, sample, 0, LensV) - 1.0f;
+			const float a      = 2.0f * number(cFrame.sobol, stream, group, 0, LensU) - 1.0f;
+			const float b      = 2.0f * number(cFrame.sobol, stream, group, 0, LensV) - 1.0f;
 			float du = 0.0f, dv = 0.0f;
 			if (a != 0.0f || b != 0.0f) {
 				const bool wide    = fabsf(a) > fabsf(b);
@@ -859,7 +862,8 @@ __global__ void __launch_bounds__(kBlock, 3) shadeKernel(const __grid_constant__
 					if (!meetLamp(l, origin, heading, limit, reach)) continue;
 					float w = 1.0f;
 					if (drawnDensity > 0.0f) {
-						const float pa = aimDensityOf(l, from, heading, reach);
+						// weight.cpp:15 sharedAim: the first vertex's aim counts once a group
+						const float pa = aimDensityOf(l, from, heading, reach) / (depth == 1 ? float(cFrame.split) : 1.0f);
 						w              = drawnDensity * drawnDensity / (drawnDensity * drawnDensity + pa * pa);
 					}
 					R = add4(R, scale4(mul4(mul4(mul4(T, keptOver(reach)), spectrumOf(l.radiance[0], l.radiance[1], l.radiance[2], nm)), lampTint(cFrame, k, nm)),
@@ -895,7 +899,7 @@ __global__ void __launch_bounds__(kBlock, 3) shadeKernel(const __grid_constant__
 				const float4 sky = skySpectrum(cFrame, heading, nm);
 				float w          = 1.0f;
 				if (drawnDensity > 0.0f && cFrame.skyChart != nullptr) {
-					const float pa = float(chartDensity(cFrame.skyChart, heading.x, heading.y, heading.z));
+					const float pa = float(chartDensity(cFrame.skyChart, heading.x, heading.y, heading.z)) / (depth == 1 ? float(cFrame.split) : 1.0f);
 					w              = drawnDensity * drawnDensity / (drawnDensity * drawnDensity + pa * pa);
 				}
 				R = add4(R, scale4(mul4(mul4(T, keptOver(__int_as_float(0x7f800000))), sky), w));
@@ -981,17 +985,21 @@ __global__ void __launch_bounds__(kBlock, 3) shadeKernel(const __grid_constant__
 				// (trace.cpp:935, each_lamp_first.cpp:7 eachLampFirst)
 				if (!m.exact && aimable && (cFrame.lampCount > 0 || cFrame.skyChart != nullptr)) {
 					uint32_t owned   = 0;
-					const float u0   = number(cFrame.sobol, stream, index, depth, LightU);
-					const float v0   = number(cFrame.sobol, stream, index, depth, LightV);
-					float choice     = number(cFrame.sobol, stream, index, depth, Pick);
+					// the first vertex's aim is shared by a group (path.cpp:37 sharedDraw)
+					// and counts once a group in its weight (weight.cpp:15 sharedAim)
+					const uint32_t aimIndex = depth == 0 ? index / cFrame.split : index;
+					const float aimCount    = depth == 0 ? 1.0f / float(cFrame.split) : 1.0f;
+					const float u0   = number(cFrame.sobol, stream, aimIndex, depth, LightU);
+					const float v0   = number(cFrame.sobol, stream, aimIndex, depth, LightV);
+					float choice     = number(cFrame.sobol, stream, aimIndex, depth, Pick);
 					float total      = 0.0f, picked = 0.0f;
 					float4 chosen    = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 					float3 chosenDir = make_float3(0.0f, 0.0f, 1.0f);
 					float chosenDist = 0.0f;
 					for (uint32_t k = 0; k < cFrame.lampCount + (cFrame.skyChart != nullptr ? 1u : 0u); ++k) {
 						Aim a = k < cFrame.lampCount ? aimLamp(cFrame.lamps[k], point, u0, v0)
-						                                   : aimSky(cFrame, u0, v0, plainNumber(stream, index, depth, AimPart), plainNumber(stream, index, depth, AimJitterU),
-						                                            plainNumber(stream, index, depth, AimJitterV));
+						                                   : aimSky(cFrame, u0, v0, plainNumber(stream, aimIndex, depth, AimPart), plainNumber(stream, aimIndex, depth, AimJitterU),
+						                                            plainNumber(stream, aimIndex, depth, AimJitterV));
 						if (!a.found) continue;
 						if (k < cFrame.lampCount) a.arriving = a.arriving * moonLit(cFrame, cFrame.lamps[k], a.toward);
 						const float facing = dot3(open, a.toward);
@@ -1000,7 +1008,8 @@ __global__ void __launch_bounds__(kBlock, 3) shadeKernel(const __grid_constant__
 						float w          = 1.0f;
 						if (a.density > 0.0f) {
 							const float pm = capped ? 0.0f : (lobes ? share * mixtureDensity(lobes, a.toward) + (1.0f - share) * f.density : f.density);
-							w              = a.density * a.density / (a.density * a.density + pm * pm);
+							const float pa = a.density * aimCount;
+							w              = pa * pa / (pa * pa + pm * pm);
 						}
 						float4 arriving    = spectrumOf(a.arriving.x, a.arriving.y, a.arriving.z, nm);
 						if (k < cFrame.lampCount) arriving = mul4(arriving, lampTint(cFrame, k, nm));

@@ -508,6 +508,15 @@ def scene_lens(seed: int = 1, width: int = 256, height: int = 256, samples: int 
     return "".join(out)
 
 
+def scene_split(seed: int = 1, width: int = 256, height: int = 256, samples: int = 16, surfaces: int = 8, count: int = 12) -> str:
+    """The many-lamp scene (scene_lamps) drawn with render.split = 4: each
+    group of four samples shares its camera ray, wavelengths and first
+    vertex's aim, and each branches on its own from there."""
+    text = scene_lamps(seed, width, height, samples, surfaces, count)
+    assert "\tsplit    = 1;\n" in text
+    return text.replace("\tsplit    = 1;\n", "\tsplit    = 4;\n", 1)
+
+
 def scene_physical_sky(seed: int = 1, width: int = 256, height: int = 256, samples: int = 16, surfaces: int = 8, count: int = 12) -> str:
     """Under a physical sky: config-1 primitives (plastics and metals) on a
     plastic ground lit by a low sun (a disc 0.05 radians across) through

@@ -249,7 +249,7 @@ class View(ctypes.Structure):
                 ("factor", ctypes.c_uint32), ("phase", ctypes.c_uint32), ("sobol", ctypes.c_uint32), ("sky_map", ctypes.c_uint32),
                 ("each_lamp", ctypes.c_uint32), ("middle", ctypes.c_double * 3), ("collisions", ctypes.c_int32),
                 ("sky_kind", ctypes.c_uint32), ("haze", ctypes.c_double), ("glow", ctypes.c_double * 3), ("strength", ctypes.c_double),
-                ("spread", ctypes.c_double), ("aperture", ctypes.c_double), ("focus", ctypes.c_double)]
+                ("spread", ctypes.c_double), ("aperture", ctypes.c_double), ("focus", ctypes.c_double), ("split", ctypes.c_uint32)]
 
 
 _trees: dict = {}
@@ -304,6 +304,7 @@ def render_band(scene, width: int, height: int, spp: int, surfaces: int, seed: i
     v.collisions = int(scene.render.get("collisions", 0)) or 256
     v.sky_kind = int(scene.sky.get("kind", 0))
     v.aperture = float(np.float32(scene.camera.get("aperture", 0)))
+    v.split = max(int(scene.render.get("split", 1)), 1)
     v.focus = float(np.float32(scene.camera.get("focus", 0)))
     v.haze = float(np.float32(scene.sky.get("haze", 0)))
     v.strength = float(np.float32(scene.sky.get("strength", 0)))

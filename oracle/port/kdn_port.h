@@ -192,6 +192,8 @@ typedef struct kp_view {
 	/* core/camera.cpp:9 lensOf: a thin lens's radius (0: a pinhole) and
 	 * the distance it is sharp at (0: the target's) */
 	double aperture, focus;
+	/* render.split: samples sharing a first vertex (1: none) */
+	uint32_t split;
 } kp_view;
 
 /*

@@ -1401,12 +1401,19 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 	const kp_view* V = J->view;
 	const uint64_t stream = J->seed_mix ^ kp_mixed_bits(((uint64_t) (uint32_t) x << 32) | (uint64_t) (uint32_t) y);
 	lanes w;
-	kp_sampled_wavelengths(kp_wavelength_share(kp_hashed(stream, ~(uint64_t) 0, 0), index), w.nm, w.density, w.basis);
+	/* core/pixels.cpp:5 groupSample: with a split, the samples of a group
+	 * share the first vertex's draws (path.cpp:37 sharedDraw): its
+	 * wavelengths, camera ray and aim; the aim there counts once a group in
+	 * the weights (weight.cpp:15 sharedAim) and each branch carries it
+	 * (the group's sum is the reference's first branch's share times the
+	 * split, trace.cpp:1570) */
+	const uint32_t split = V->split > 1 ? V->split : 1, group = index / split;
+	kp_sampled_wavelengths(kp_wavelength_share(kp_hashed(stream, ~(uint64_t) 0, 0), group), w.nm, w.density, w.basis);
 	/* trace.cpp:105 filmDraw, :93 phasedDraw */
 	const int factor = V->factor > 1 ? (int) V->factor : 1;
 	const double column = factor > 1 ? (double) (V->phase % (uint32_t) factor) : 0, row = factor > 1 ? (double) (V->phase / (uint32_t) factor) : 0;
-	const double px = factor > 1 ? x + (column + number(J->sobol, stream, index, 0, PIXEL_X)) / factor : x + number(J->sobol, stream, index, 0, PIXEL_X);
-	const double py = factor > 1 ? y + (row + number(J->sobol, stream, index, 0, PIXEL_Y)) / factor : y + number(J->sobol, stream, index, 0, PIXEL_Y);
+	const double px = factor > 1 ? x + (column + number(J->sobol, stream, group, 0, PIXEL_X)) / factor : x + number(J->sobol, stream, group, 0, PIXEL_X);
+	const double py = factor > 1 ? y + (row + number(J->sobol, stream, group, 0, PIXEL_Y)) / factor : y + number(J->sobol, stream, group, 0, PIXEL_Y);
 	const double u = 2 * px / V->width - 1, v = 1 - 2 * py / V->height;
 	v3 heading = unit(add(add(J->forward, scl(J->right, u * J->reach * J->aspect)), scl(J->up, v * J->reach)));
 	v3 from = J->eye;
@@ -1417,7 +1424,7 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 		const double focus = V->focus > 0 ? V->focus : len(sub(vd(V->target), J->eye));
 		const double ahead = focus / maxd(dotv(heading, J->forward), 1e-9);
 		const v3 sharp = add(J->eye, scl(heading, ahead));
-		const double a = 2 * number(J->sobol, stream, index, 0, LENS_U) - 1, b = 2 * number(J->sobol, stream, index, 0, LENS_V) - 1;
+		const double a = 2 * number(J->sobol, stream, group, 0, LENS_U) - 1, b = 2 * number(J->sobol, stream, group, 0, LENS_V) - 1;
 		double du = 0, dv = 0;
 		if (a != 0 || b != 0) {
 			const int wide = fabs(a) > fabs(b);
@@ -1463,7 +1470,7 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 				if (!meet_lamp(&J->lamps[k], origin, heading, limit, &reach)) continue;
 				double wgt = 1;
 				if (drawn > 0) {
-					const double pa = aim_density(&J->lamps[k], from, heading, reach);
+					const double pa = aim_density(&J->lamps[k], from, heading, reach) / (depth == 1 ? split : 1);
 					wgt = drawn * drawn / (drawn * drawn + pa * pa);
 				}
 				R = sadd(R, sscale(smul(smul(smul(T, KEPT(reach)), spectrum(J->lamps[k].radiance, &w)), lamp_tint(J, k, &w)), wgt * moon_lit(&J->lamps[k], J->has_sun, heading)));
@@ -1475,7 +1482,7 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 			const spec sky = sky_seen(J, heading, &w);
 			double wgt = 1;
 			if (drawn > 0 && J->chart != NULL) {
-				const double pa = chart_density(J->chart, heading);
+				const double pa = chart_density(J->chart, heading) / (depth == 1 ? split : 1);
 				wgt = drawn * drawn / (drawn * drawn + pa * pa);
 			}
 			R = sadd(R, sscale(smul(smul(T, KEPT(INFINITY)), sky), wgt));
@@ -1549,8 +1556,10 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 		const int aimable = medium == NO_MATERIAL || (medium == material && bends);
 		const v3 open = s.inside ? scl(normal, -1) : normal;
 		if (!m->exact && aimable && (V->lamp_count > 0 || J->chart != NULL)) {
-			const double u0 = number(J->sobol, stream, index, depth, LIGHT_U), v0 = number(J->sobol, stream, index, depth, LIGHT_V);
-			double choice = number(J->sobol, stream, index, depth, PICK);
+			const uint32_t aim_index = depth == 0 ? group : index;
+			const double aim_count = depth == 0 ? 1.0 / split : 1.0;
+			const double u0 = number(J->sobol, stream, aim_index, depth, LIGHT_U), v0 = number(J->sobol, stream, aim_index, depth, LIGHT_V);
+			double choice = number(J->sobol, stream, aim_index, depth, PICK);
 			double total = 0, picked = 0, chosen_dist = 0;
 			spec chosen = flat(0);
 			v3 chosen_dir = mk(0, 0, 1);
@@ -1565,8 +1574,8 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 			for (uint32_t k = 0; k < V->lamp_count + (J->chart != NULL ? 1u : 0u); ++k) {
 				const uint64_t plain = ((uint64_t) 1 << 20) + 5 * (uint64_t) depth;
 				aim a = k < V->lamp_count ? aim_lamp(&J->lamps[k], point, u0, v0)
-				                                : aim_sky(V, J->chart, u0, v0, kp_hashed(stream, index, plain + 2), kp_hashed(stream, index, plain + 3),
-				                                          kp_hashed(stream, index, plain + 4));
+				                                : aim_sky(V, J->chart, u0, v0, kp_hashed(stream, aim_index, plain + 2), kp_hashed(stream, aim_index, plain + 3),
+				                                          kp_hashed(stream, aim_index, plain + 4));
 				if (!a.found) continue;
 				if (k < V->lamp_count) {
 					const double lit = moon_lit(&J->lamps[k], J->has_sun, a.toward);
@@ -1578,7 +1587,8 @@ static void sample_pixel(job* J, kp_tracer* tracer, int x, int y, uint32_t index
 				double wgt = 1;
 				if (a.density > 0) {
 					const double pm = capped ? 0 : f.density;
-					wgt = a.density * a.density / (a.density * a.density + pm * pm);
+					const double pa = a.density * aim_count;
+					wgt = pa * pa / (pa * pa + pm * pm);
 				}
 				const spec arriving = k < V->lamp_count ? smul(spectrum(a.arriving, &w), lamp_tint(J, k, &w)) : spectrum(a.arriving, &w);
 				const spec offer = sscale(smul(smul(T, f.value), arriving), facing * wgt);

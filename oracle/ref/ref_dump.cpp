@@ -197,7 +197,7 @@ int dumpScene(const char* sdf, const char* out) {
 	std::fprintf(f, ",\"up\":");
 	putVector(f, c.up);
 	std::fprintf(f, ",\"fov\":%.9g,\"aperture\":%.9g,\"focus\":%.9g},\n", double(c.fov), double(c.aperture), double(c.focus));
-	std::fprintf(f, "\"render\":{\"width\":%d,\"height\":%d,\"seed\":%d,\"samples\":%d,\"surfaces\":%d,\"collisions\":%d,\"far\":", r.width, r.height, r.seed, r.samples, r.surfaces, r.collisions);
+	std::fprintf(f, "\"render\":{\"width\":%d,\"height\":%d,\"seed\":%d,\"samples\":%d,\"surfaces\":%d,\"collisions\":%d,\"split\":%d,\"far\":", r.width, r.height, r.seed, r.samples, r.surfaces, r.collisions, r.split);
 	putDouble(f, r.far);
 	std::fprintf(f, "}}\n");
 	std::fclose(f);
