@@ -139,6 +139,10 @@ struct FrameConstants {
 	uint32_t collisionCap;
 	// render.split: how many samples share a first vertex (1: none)
 	uint32_t split;
+	// any of the rarer parts the plain shade kernel leaves out: scattering
+	// bodies, lamps other than quads and spheres, a physical sky or a glow,
+	// the sky map, own lines, a split
+	uint32_t extras;
 	float zenith[3], horizon[3], ground[3];
 	// sdf/scene.cpp:306 firstSun: the first sun's unit direction, where the
 	// scene has one (a moon's phase follows it)

@@ -612,6 +612,8 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		if (dm.back().filmThickness > 0.0f) c.films = 1;
 		if (dm.back().scatter > 0.0f) c.scatters = 1;
 	}
+	c.extras = c.scatters || c.airTables != nullptr || c.glows || c.skyChart != nullptr || c.eachLamp || c.split > 1 ? 1u : 0u;
+	for (const kdn_light& l : lights) c.extras |= l.kind != 2 && l.kind != 3 ? 1u : 0u;
 	// material/energy.h Boundary of each rough glass that loses much
 	std::vector<float> boundaryTables;
 	{

@@ -265,11 +265,10 @@ __device__ __noinline__ Aim aimOther(const DeviceLamp& l, float3 from, float u, 
 	return a;
 }
 
-// aimLight (light.cpp:372) for every kind of lamp.
-__device__ Aim aimLamp(const DeviceLamp& l, float3 from, float u, float v) {
+// aimLight (light.cpp:372) for a quad or a sphere lamp.
+__device__ __forceinline__ Aim aimArea(const DeviceLamp& l, float3 from, float u, float v) {
 	Aim a;
 	a.found = false;
-	if (l.kind != 2 && l.kind != 3) return aimOther(l, from, u, v);
 	if (l.kind == 3) { // quad
 		if (l.area < 1e-12f || dot3(f3(l.facing), from - f3(l.at)) <= 0.0f) return a;
 		float3 spot;
@@ -331,6 +330,11 @@ __device__ Aim aimLamp(const DeviceLamp& l, float3 from, float u, float v) {
 	return a;
 }
 
+// aimLight (light.cpp:372) for every kind of lamp.
+__device__ __forceinline__ Aim aimLamp(const DeviceLamp& l, float3 from, float u, float v) {
+	return l.kind == 2 || l.kind == 3 ? aimArea(l, from, u, v) : aimOther(l, from, u, v);
+}
+
 // Whether a unit direction lies in a far disc's cone: 1 - cos(apart) <=
 // 1 - cos(half), as half the squared distance between the unit vectors
 __device__ __forceinline__ bool inDisc(const DeviceLamp& l, float3 toward) {
@@ -338,9 +342,9 @@ __device__ __forceinline__ bool inDisc(const DeviceLamp& l, float3 toward) {
 	return l.oneLess > 0.0f && 0.5f * dot3(apart, apart) <= l.oneLess;
 }
 
-// aimDensity (light.cpp:463): the density aiming gives a direction.
-__device__ float aimDensityOf(const DeviceLamp& l, float3 from, float3 toward, float distance) {
-	if (l.kind == 4 || l.kind == 5) return inDisc(l, toward) ? 1.0f / (2.0f * 3.14159265358979f * l.oneLess) : 0.0f;
+// aimDensity (light.cpp:463): the density aiming gives a direction, for a
+// quad or a sphere lamp ...
+__device__ __forceinline__ float areaDensityOf(const DeviceLamp& l, float3 from, float3 toward, float distance) {
 	if (l.kind == 3) {
 		if (l.area < 1e-12f || dot3(f3(l.facing), from - f3(l.at)) <= 0.0f) return 0.0f;
 		if (l.square) {
@@ -360,14 +364,15 @@ __device__ float aimDensityOf(const DeviceLamp& l, float3 from, float3 toward, f
 	return 0.0f;
 }
 
-// meetLight (light.cpp:498) for a lamp: where a ray meets it before limit
-// (a point or a directional light is never met; a sun or a moon only by a
-// ray that escaped, light.cpp:478 meetSun).
-__device__ bool meetLamp(const DeviceLamp& l, float3 origin, float3 dir, float limit, float& reach) {
-	if (l.kind == 4 || l.kind == 5) {
-		reach = __int_as_float(0x7f800000);
-		return limit >= 3.0e38f && inDisc(l, dir);
-	}
+// ... and for every kind (a point or a directional light is singular: 0)
+__device__ __forceinline__ float aimDensityOf(const DeviceLamp& l, float3 from, float3 toward, float distance) {
+	if (l.kind == 4 || l.kind == 5) return inDisc(l, toward) ? 1.0f / (2.0f * 3.14159265358979f * l.oneLess) : 0.0f;
+	return areaDensityOf(l, from, toward, distance);
+}
+
+// meetLight (light.cpp:498) for a quad or a sphere lamp: where a ray meets
+// it before limit ...
+__device__ __forceinline__ bool meetArea(const DeviceLamp& l, float3 origin, float3 dir, float limit, float& reach) {
 	if (l.kind == 3) {
 		const float3 facing = f3(l.cross);
 		const float leaning = dot3(facing, dir);
@@ -392,6 +397,16 @@ __device__ bool meetLamp(const DeviceLamp& l, float3 origin, float3 dir, float l
 		return !(reach <= 1e-9f || reach >= limit);
 	}
 	return false;
+}
+
+// ... and for every kind (a point or a directional light is never met; a
+// sun or a moon only by a ray that escaped, light.cpp:478 meetSun)
+__device__ __forceinline__ bool meetLamp(const DeviceLamp& l, float3 origin, float3 dir, float limit, float& reach) {
+	if (l.kind == 4 || l.kind == 5) {
+		reach = __int_as_float(0x7f800000);
+		return limit >= 3.0e38f && inDisc(l, dir);
+	}
+	return meetArea(l, origin, dir, limit, reach);
 }
 
 // light.cpp:575 gradientColour
@@ -753,10 +768,12 @@ __device__ __noinline__ void ownLine(const ShadowBuffers& S, uint32_t lineCapaci
 }
 
 // ---- K-shade ----
-// Films, Scatters: built for each, so that a frame without thin films or
-// scattering bodies runs a kernel with no code for them (the frame's
-// FrameConstants::films and ::scatters pick one)
-template <bool Films, bool Scatters>
+// Films, Extras: built for each, so that a frame without thin films, or
+// without any of the rarer parts (scattering bodies, lamps other than quads
+// and spheres, a physical sky or a glow, the sky map, own lines, a split),
+// runs a kernel with no code for them (FrameConstants::films and ::extras
+// pick one)
+template <bool Films, bool Extras>
 __global__ void __launch_bounds__(kBlock, 3) shadeKernel(const __grid_constant__ FrameConstants cFrame, ShadeArgs A) {
 	const uint32_t n = *A.in.count;
 	for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -793,14 +810,14 @@ __global__ void __launch_bounds__(kBlock, 3) shadeKernel(const __grid_constant__
 			// the surfaces stood on, the collisions inside scattering bodies,
 			// and the path's depth (every vertex: the events its numbers follow)
 			const int surfaceDepth    = int(st & 0xFFu);
-			const uint32_t collisions = Scatters && A.paths.collided != nullptr ? A.paths.collided[p] : 0u;
+			const uint32_t collisions = Extras && A.paths.collided != nullptr ? A.paths.collided[p] : 0u;
 			const int depth           = surfaceDepth + int(collisions);
 			const bool camera   = (st >> 8) & 1u;
 			uint32_t medium     = (st >> 16) == 0 ? kNoMaterial : (st >> 16) - 1u;
 			float4 T            = A.paths.throughput[p];
 			float4 R            = A.paths.radiance[p];
 			// the first vertex's own lines, all answered by now
-			if (depth == 1 && A.paths.held != nullptr) {
+			if (Extras && depth == 1 && A.paths.held != nullptr) {
 				for (uint32_t k = 0; k < kOwnLines; ++k) {
 					R                                        = add4(R, A.paths.held[size_t(p) * kOwnLines + k]);
 					A.paths.held[size_t(p) * kOwnLines + k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -830,7 +847,7 @@ __global__ void __launch_bounds__(kBlock, 3) shadeKernel(const __grid_constant__
 			bool collided    = false;
 			float collidedAt = 0.0f;
 			float flight     = __int_as_float(0x7f800000);
-			if (Scatters && medium != kNoMaterial) {
+			if (Extras && cFrame.scatters && medium != kNoMaterial) {
 				const DeviceMaterial& body = A.looks.materials[medium < cFrame.materialCount ? medium : 0u];
 				if (body.scatter > 0.0f) {
 					const uint32_t px    = A.paths.pixel[p];
@@ -859,15 +876,19 @@ __global__ void __launch_bounds__(kBlock, 3) shadeKernel(const __grid_constant__
 				for (uint32_t k = 0; k < cFrame.lampCount; ++k) {
 					const DeviceLamp& l = cFrame.lamps[k];
 					float reach;
-					if (!meetLamp(l, origin, heading, limit, reach)) continue;
+					if (Extras ? !meetLamp(l, origin, heading, limit, reach) : !meetArea(l, origin, heading, limit, reach)) continue;
 					float w = 1.0f;
 					if (drawnDensity > 0.0f) {
 						// weight.cpp:15 sharedAim: the first vertex's aim counts once a group
-						const float pa = aimDensityOf(l, from, heading, reach) / (depth == 1 ? float(cFrame.split) : 1.0f);
+						const float pa = Extras ? aimDensityOf(l, from, heading, reach) / (depth == 1 ? float(cFrame.split) : 1.0f) : areaDensityOf(l, from, heading, reach);
 						w              = drawnDensity * drawnDensity / (drawnDensity * drawnDensity + pa * pa);
 					}
-					R = add4(R, scale4(mul4(mul4(mul4(T, keptOver(reach)), spectrumOf(l.radiance[0], l.radiance[1], l.radiance[2], nm)), lampTint(cFrame, k, nm)),
-					                   w * moonLit(cFrame, l, heading)));
+					float4 lit = mul4(mul4(T, keptOver(reach)), spectrumOf(l.radiance[0], l.radiance[1], l.radiance[2], nm));
+					if (Extras) {
+						lit = mul4(lit, lampTint(cFrame, k, nm));
+						w *= moonLit(cFrame, l, heading);
+					}
+					R = add4(R, scale4(lit, w));
 				}
 			}
 			// the record's first surface of the pixel's last sample
@@ -896,14 +917,20 @@ __global__ void __launch_bounds__(kBlock, 3) shadeKernel(const __grid_constant__
 			if (!found) {
 				// the sky met, weighed against aiming at it by its chart
 				// (trace.cpp:294 meetAimDensity, sampler.cpp:344 aimDensityAt)
-				const float4 sky = skySpectrum(cFrame, heading, nm);
+				float4 sky;
+				if (Extras) {
+					sky = skySpectrum(cFrame, heading, nm);
+				} else {
+					const float3 rgb = skyColour(cFrame, heading);
+					sky              = spectrumOf(rgb.x, rgb.y, rgb.z, nm);
+				}
 				float w          = 1.0f;
-				if (drawnDensity > 0.0f && cFrame.skyChart != nullptr) {
+				if (Extras && drawnDensity > 0.0f && cFrame.skyChart != nullptr) {
 					const float pa = float(chartDensity(cFrame.skyChart, heading.x, heading.y, heading.z)) / (depth == 1 ? float(cFrame.split) : 1.0f);
 					w              = drawnDensity * drawnDensity / (drawnDensity * drawnDensity + pa * pa);
 				}
 				R = add4(R, scale4(mul4(mul4(T, keptOver(__int_as_float(0x7f800000))), sky), w));
-			} else if (Scatters && collided) {
+			} else if (Extras && collided) {
 				// trace.cpp:502 collidedOn: the phase vertex (trace.cpp:474
 				// phaseVertex) at the collision, what the leg's body kept up
 				// to it; a bending body is not aimed from (trace.cpp:579
@@ -983,12 +1010,12 @@ __global__ void __launch_bounds__(kBlock, 3) shadeKernel(const __grid_constant__
 				// first kOwnLines lamps whose offer is bright traces a line of
 				// its own at the first vertex, outside the reservoir
 				// (trace.cpp:935, each_lamp_first.cpp:7 eachLampFirst)
-				if (!m.exact && aimable && (cFrame.lampCount > 0 || cFrame.skyChart != nullptr)) {
+				if (!m.exact && aimable && (cFrame.lampCount > 0 || (Extras && cFrame.skyChart != nullptr))) {
 					uint32_t owned   = 0;
 					// the first vertex's aim is shared by a group (path.cpp:37 sharedDraw)
 					// and counts once a group in its weight (weight.cpp:15 sharedAim)
-					const uint32_t aimIndex = depth == 0 ? index / cFrame.split : index;
-					const float aimCount    = depth == 0 ? 1.0f / float(cFrame.split) : 1.0f;
+					const uint32_t aimIndex = Extras && depth == 0 ? index / cFrame.split : index;
+					const float aimCount    = Extras && depth == 0 ? 1.0f / float(cFrame.split) : 1.0f;
 					const float u0   = number(cFrame.sobol, stream, aimIndex, depth, LightU);
 					const float v0   = number(cFrame.sobol, stream, aimIndex, depth, LightV);
 					float choice     = number(cFrame.sobol, stream, aimIndex, depth, Pick);
@@ -996,12 +1023,12 @@ __global__ void __launch_bounds__(kBlock, 3) shadeKernel(const __grid_constant__
 					float4 chosen    = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 					float3 chosenDir = make_float3(0.0f, 0.0f, 1.0f);
 					float chosenDist = 0.0f;
-					for (uint32_t k = 0; k < cFrame.lampCount + (cFrame.skyChart != nullptr ? 1u : 0u); ++k) {
-						Aim a = k < cFrame.lampCount ? aimLamp(cFrame.lamps[k], point, u0, v0)
+					for (uint32_t k = 0; k < cFrame.lampCount + (Extras && cFrame.skyChart != nullptr ? 1u : 0u); ++k) {
+						Aim a = k < cFrame.lampCount ? (Extras ? aimLamp(cFrame.lamps[k], point, u0, v0) : aimArea(cFrame.lamps[k], point, u0, v0))
 						                                   : aimSky(cFrame, u0, v0, plainNumber(stream, aimIndex, depth, AimPart), plainNumber(stream, aimIndex, depth, AimJitterU),
 						                                            plainNumber(stream, aimIndex, depth, AimJitterV));
 						if (!a.found) continue;
-						if (k < cFrame.lampCount) a.arriving = a.arriving * moonLit(cFrame, cFrame.lamps[k], a.toward);
+						if (Extras && k < cFrame.lampCount) a.arriving = a.arriving * moonLit(cFrame, cFrame.lamps[k], a.toward);
 						const float facing = dot3(open, a.toward);
 						if (facing <= 0.0f || a.distance <= 0.0f) continue;
 						const Response f = respond(surf, m, outgoing, a.toward, nm);
@@ -1012,11 +1039,11 @@ __global__ void __launch_bounds__(kBlock, 3) shadeKernel(const __grid_constant__
 							w              = pa * pa / (pa * pa + pm * pm);
 						}
 						float4 arriving    = spectrumOf(a.arriving.x, a.arriving.y, a.arriving.z, nm);
-						if (k < cFrame.lampCount) arriving = mul4(arriving, lampTint(cFrame, k, nm));
+						if (Extras && k < cFrame.lampCount) arriving = mul4(arriving, lampTint(cFrame, k, nm));
 						const float4 offer = scale4(mul4(mul4(T, f.value), arriving), facing * w);
 						const float weight = mean4(offer);
 						if (!(weight > 0.0f)) continue;
-						if (cFrame.eachLamp && depth == 0 && k < cFrame.lampCount && owned < kOwnLines) {
+						if (Extras && cFrame.eachLamp && depth == 0 && k < cFrame.lampCount && owned < kOwnLines) {
 							ownLine(A.shadow, A.lineCapacity, p, owned++, point + open * lift, a.toward, a.distance - lift, offer);
 							continue;
 						}
@@ -1214,9 +1241,9 @@ cudaError_t launchCamera(const FrameConstants& frame, const PathBuffers& paths, 
 
 cudaError_t launchShade(const FrameConstants& frame, const ShadeArgs& args, cudaStream_t stream, int smCount) {
 	const uint32_t grid = gridFor(args.capacity, smCount);
-	if (frame.films && frame.scatters) shadeKernel<true, true><<<grid, kBlock, 0, stream>>>(frame, args);
+	if (frame.films && frame.extras) shadeKernel<true, true><<<grid, kBlock, 0, stream>>>(frame, args);
 	else if (frame.films) shadeKernel<true, false><<<grid, kBlock, 0, stream>>>(frame, args);
-	else if (frame.scatters) shadeKernel<false, true><<<grid, kBlock, 0, stream>>>(frame, args);
+	else if (frame.extras) shadeKernel<false, true><<<grid, kBlock, 0, stream>>>(frame, args);
 	else shadeKernel<false, false><<<grid, kBlock, 0, stream>>>(frame, args);
 	return cudaGetLastError();
 }
