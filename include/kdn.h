@@ -161,7 +161,7 @@ typedef struct kdn_light {
 	double power[3]; /* linear RGB */
 } kdn_light;
 
-/* sdf/scene.h Sky, 120 bytes: its kind (SkyKind: 0 gradient, 1 physical;
+/* sdf/scene.h Sky and Stars, 136 bytes: its kind (SkyKind: 0 gradient, 1 physical;
  * a painted sky is refused); a gradient's linear RGB zenith, horizon and
  * ground; a physical sky's haze and ground albedo (`ground`); the glow
  * about the first sun (glow x strength, falling by e over `spread` radians:
@@ -175,6 +175,10 @@ typedef struct kdn_sky {
 	double spread;
 	uint32_t kind;
 	float haze;
+	/* sdf/scene.h Stars (sky_layers.cpp:240 starlight): present (1), about
+	 * how many over the sphere, the brightest's strength, a disc's angle */
+	uint32_t stars;
+	float star_count, star_strength, star_angle;
 } kdn_sky;
 
 /* sdf/scene.h Camera and the Render fields a frame reads. */

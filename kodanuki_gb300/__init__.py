@@ -40,7 +40,8 @@ MATERIAL_DTYPE = np.dtype([("kind", "<u4"), ("albedo", "<f4", 3), ("roughness", 
 LIGHT_DTYPE = np.dtype([("kind", "<u4"), ("radius", "<f4"), ("angle", "<f4"), ("pad", "<f4"), ("at", "<f8", 3), ("direction", "<f8", 3),
                         ("along", "<f8", 3), ("across", "<f8", 3), ("power", "<f8", 3)])
 SKY_DTYPE = np.dtype([("zenith", "<f8", 3), ("horizon", "<f8", 3), ("ground", "<f8", 3), ("glow", "<f8", 3), ("strength", "<f8"),
-                      ("spread", "<f8"), ("kind", "<u4"), ("haze", "<f4")])
+                      ("spread", "<f8"), ("kind", "<u4"), ("haze", "<f4"), ("stars", "<u4"), ("star_count", "<f4"),
+                      ("star_strength", "<f4"), ("star_angle", "<f4")])
 CAMERA_DTYPE = np.dtype([("eye", "<f8", 3), ("target", "<f8", 3), ("up", "<f8", 3), ("fov", "<f8"), ("aperture", "<f8"), ("focus", "<f8")])
 REGION_DTYPE = np.dtype([("lower", "<f8", 3), ("size", "<f8", 3)])
 PATTERN_DTYPE = np.dtype([("first", "<u4"), ("count", "<u4"), ("result", "<u4"), ("argument_first", "<u4"), ("argument_count", "<u4"),
@@ -52,7 +53,7 @@ FINISH_DTYPE = np.dtype([("kind", "<u4"), ("sharp", "<u4"), ("exact", "<u4"), ("
                          ("body", "<f8"), ("index", "<f8"), ("coat_front", "<f8"), ("coat_twice", "<f8"), ("coat_room", "<f8"),
                          ("escape_average", "<f8"), ("escape", "<f8", 32), ("film", "<f8", 2)])
 assert RAY_DTYPE.itemsize == 36 and HIT_DTYPE.itemsize == 56 and MATERIAL_DTYPE.itemsize == 72 and LIGHT_DTYPE.itemsize == 136
-assert FINISH_DTYPE.itemsize == 352 and SKY_DTYPE.itemsize == 120
+assert FINISH_DTYPE.itemsize == 352 and SKY_DTYPE.itemsize == 136
 
 
 class BuildOptions(ctypes.Structure):
@@ -269,7 +270,7 @@ def scene_blocks(scene: Scene) -> dict[str, np.ndarray]:
     sky = np.zeros(1, SKY_DTYPE)
     for k in ("zenith", "horizon", "ground"):
         sky[k] = scene.sky[k]
-    for k in ("glow", "strength", "spread", "kind", "haze"):
+    for k in ("glow", "strength", "spread", "kind", "haze", "stars", "star_count", "star_strength", "star_angle"):
         if k in scene.sky:
             sky[k] = scene.sky[k]
     cam = np.zeros(1, CAMERA_DTYPE)

@@ -47,7 +47,7 @@ static_assert(sizeof(kdn_program_ref) == 12, "kdn_program_ref is 12 bytes");
 static_assert(sizeof(kdn_material) == 72, "kdn_material is 72 bytes");
 static_assert(sizeof(kdn_light) == 136, "kdn_light is 136 bytes");
 static_assert(sizeof(kdn_finish) == 352, "kdn_finish is 352 bytes");
-static_assert(sizeof(kdn_sky) == 120, "kdn_sky is 120 bytes");
+static_assert(sizeof(kdn_sky) == 136, "kdn_sky is 136 bytes");
 static_assert(sizeof(kdn_camera) == 96, "kdn_camera is 96 bytes");
 static_assert(sizeof(kdn_region) == 48, "kdn_region is 48 bytes");
 

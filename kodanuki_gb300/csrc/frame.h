@@ -161,6 +161,10 @@ struct FrameConstants {
 	// times its strength, the angle it falls by e over, the sun's elevation)
 	uint32_t glows;
 	float glow[3], glowSpread, sunElevation;
+	// sky_layers.cpp:240 starlight: the stars (count over the sphere, the
+	// brightest's strength, a disc's angle), seen above the horizon at night
+	uint32_t stars;
+	float starCount, starStrength, starAngle, starNight;
 	DeviceLamp lamps[kMaxLamps];
 	SpectralTables spectral;
 };

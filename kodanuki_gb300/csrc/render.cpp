@@ -545,7 +545,25 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 			c.sunElevation = float(std::asin(std::clamp(sun.z, -1.0, 1.0)));
 		}
 	}
-	if ((fr->flags & KDN_FRAME_SKY_MAP) && (c.airTables != nullptr || c.glows)) return ctx->fail(KDN_BAD_ARG, "kdn_render: the sky map charts a gradient sky without a glow only");
+	// sky_layers.cpp:240 starlight, :264 starNight: the stars fade in as the
+	// first sun sinks from 2 to 12 degrees below the horizon
+	c.stars = 0;
+	if (!skies.empty() && skies[0].stars) {
+		c.stars        = 1;
+		c.starCount    = skies[0].star_count;
+		c.starStrength = skies[0].star_strength;
+		c.starAngle    = skies[0].star_angle;
+		double night   = 1.0;
+		if (hasSun) {
+			const double pi = 3.14159265358979323846;
+			const V3 sun    = normalized(v3(lights[firstSun].direction));
+			const double e  = std::asin(std::clamp(sun.z, -1.0, 1.0));
+			double t        = std::clamp((e - (-12.0 * pi / 180.0)) / ((-2.0 * pi / 180.0) - (-12.0 * pi / 180.0)), 0.0, 1.0);
+			night           = 1.0 - t * t * (3.0 - 2.0 * t);
+		}
+		c.starNight = float(night);
+	}
+	if ((fr->flags & KDN_FRAME_SKY_MAP) && (c.airTables != nullptr || c.glows || c.stars)) return ctx->fail(KDN_BAD_ARG, "kdn_render: the sky map charts a gradient sky without a glow or stars only");
 	c.skyChart = nullptr;
 	if (fr->flags & KDN_FRAME_SKY_MAP) {
 		// plugins/sampler/sky_map/plugin.cpp:15 chartedSkyPrepared: charted
@@ -612,7 +630,7 @@ kdn_status renderFrame(Context* ctx, const kdn_frame* fr, float* out, cudaStream
 		if (dm.back().filmThickness > 0.0f) c.films = 1;
 		if (dm.back().scatter > 0.0f) c.scatters = 1;
 	}
-	c.extras = c.scatters || c.airTables != nullptr || c.glows || c.skyChart != nullptr || c.eachLamp || c.split > 1 ? 1u : 0u;
+	c.extras = c.scatters || c.airTables != nullptr || c.glows || c.stars || c.skyChart != nullptr || c.eachLamp || c.split > 1 ? 1u : 0u;
 	for (const kdn_light& l : lights) c.extras |= l.kind != 2 && l.kind != 3 ? 1u : 0u;
 	// material/energy.h Boundary of each rough glass that loses much
 	std::vector<float> boundaryTables;

@@ -518,6 +518,50 @@ __device__ __noinline__ float4 glowSeen(const FrameConstants& c, float3 dir, flo
 	return spectrumOf(c.glow[0] * falling, c.glow[1] * falling, c.glow[2] * falling, nm);
 }
 
+// sky_layers.cpp:240 starlight: one star a cell of a grid on each cube face
+// (about `count` over the sphere), placed, sized and coloured by hashes of
+// its cell's key; in double (the discs are small)
+__device__ __noinline__ float4 starsSeen(const FrameConstants& c, float3 toward, float4 nm) {
+	const double d[3] = { toward.x, toward.y, toward.z };
+	const double ax = fabs(d[0]), ay = fabs(d[1]), az = fabs(d[2]);
+	uint64_t face;
+	double out[3] = { 0, 0, 0 }, right[3] = { 0, 0, 0 }, up[3] = { 0, 0, 0 };
+	if (ax >= ay && ax >= az) {
+		const double sign = d[0] >= 0 ? 1.0 : -1.0;
+		face = d[0] >= 0 ? 0u : 1u, out[0] = sign, right[1] = sign, up[2] = 1;
+	} else if (ay >= az) {
+		const double sign = d[1] >= 0 ? 1.0 : -1.0;
+		face = d[1] >= 0 ? 2u : 3u, out[1] = sign, right[2] = sign, up[0] = 1;
+	} else {
+		const double sign = d[2] >= 0 ? 1.0 : -1.0;
+		face = d[2] >= 0 ? 4u : 5u, out[2] = sign, right[0] = sign, up[1] = 1;
+	}
+	const double outward = d[0] * out[0] + d[1] * out[1] + d[2] * out[2];
+	const double u = (d[0] * right[0] + d[1] * right[1] + d[2] * right[2]) / outward;
+	const double v = (d[0] * up[0] + d[1] * up[1] + d[2] * up[2]) / outward;
+	const int cells  = max(1, int(ceil(sqrt(double(c.starCount) / 6.0))));
+	const int column = min(max(int((u * 0.5 + 0.5) * cells), 0), cells - 1);
+	const int row    = min(max(int((v * 0.5 + 0.5) * cells), 0), cells - 1);
+	uint64_t key     = (face * 65536u + uint64_t(row)) * 65536u + uint64_t(column);
+	double draw[4];
+	for (int k = 0; k < 4; ++k) {
+		key     = mixedBits(key + 0x9E3779B97F4A7C15ULL);
+		draw[k] = double(key >> 11) * 0x1p-53;
+	}
+	const double across = (column + 0.2 + 0.6 * draw[0]) / cells * 2.0 - 1.0;
+	const double down   = (row + 0.2 + 0.6 * draw[1]) / cells * 2.0 - 1.0;
+	double star[3], size = 0;
+	for (int a = 0; a < 3; ++a) {
+		star[a] = out[a] + right[a] * across + up[a] * down;
+		size += star[a] * star[a];
+	}
+	size = sqrt(size);
+	if ((d[0] * star[0] + d[1] * star[1] + d[2] * star[2]) / size < cos(0.5 * double(c.starAngle))) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+	const double bright = double(c.starStrength) * pow(draw[2], 6.0) * double(c.starNight);
+	const double w      = draw[3];
+	return spectrumOf(float((0.75 * (1 - w) + 1.0 * w) * bright), float((0.85 * (1 - w) + 0.82 * w) * bright), float((1.0 * (1 - w) + 0.62 * w) * bright), nm);
+}
+
 // feature.cpp:30 skyAt: the sky's radiance along a direction, per lane: the
 // gradient, or the air of a physical sky, and the glow about the sun
 __device__ __forceinline__ float4 skySpectrum(const FrameConstants& c, float3 dir, float4 nm) {
@@ -528,7 +572,9 @@ __device__ __forceinline__ float4 skySpectrum(const FrameConstants& c, float3 di
 		const float3 rgb = skyColour(c, dir);
 		sky              = spectrumOf(rgb.x, rgb.y, rgb.z, nm);
 	}
-	return c.glows ? add4(sky, glowSeen(c, dir, nm)) : sky;
+	if (c.glows) sky = add4(sky, glowSeen(c, dir, nm));
+	if (c.stars && dir.z > 0.0f) sky = add4(sky, starsSeen(c, dir, nm));
+	return sky;
 }
 
 // feature.cpp:133 lampTint: what of a lamp's light the air lets through

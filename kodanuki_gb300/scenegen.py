@@ -517,6 +517,30 @@ def scene_split(seed: int = 1, width: int = 256, height: int = 256, samples: int
     return text.replace("\tsplit    = 1;\n", "\tsplit    = 4;\n", 1)
 
 
+def scene_stars(seed: int = 1, width: int = 256, height: int = 256, samples: int = 16, surfaces: int = 8, count: int = 12) -> str:
+    """A starry night: config-1 primitives (plastics and polished metals that
+    mirror the stars) on a dark ground under a dim night-blue sky with 3000
+    stars of discs 0.04 radians across, lit also by a dim quad lamp; the
+    camera looks level enough to see the stars above the horizon."""
+    rng = random.Random(seed)
+    out = [_header(width, height, samples, surfaces, seed, [0.0, -8.5, 1.2], [0.0, 0.0, 0.4], 0.9)]
+    out.append("sky gradient {\n\tzenith  = [0.005, 0.008, 0.02];\n\thorizon = [0.01, 0.012, 0.02];\n\tground  = [0.002, 0.002, 0.002];\n}\n\n")
+    out.append("stars {\n\tcount    = 3000;\n\tstrength = 60;\n\tangle    = 0.04;\n}\n\n")
+    out.append(_quad([-0.5, 0.5, 4.5], [1.0, 0.0, 0.0], [0.0, -1.0, 0.0], blackbody_rgb(4000.0, 4.0)))
+    out.append("paint(plastic([0.3, 0.3, 0.3], roughness = 0.5)) plane([0, 0, 1], -2.2);\n\n")
+    out.append("merge(0.05) {\n")
+    for k in range(count):
+        pos = [rng.uniform(-2.0, 2.0), rng.uniform(-2.0, 2.0), rng.uniform(-2.0, 0.5)]
+        if k % 2 == 1:
+            mat = f"metal({_v([rng.uniform(0.7, 0.95) for _ in range(3)])}, roughness = {_f(rng.uniform(0.02, 0.1))})"
+        else:
+            mat = f"plastic({_v([rng.uniform(0.2, 0.8) for _ in range(3)])}, roughness = {_f(rng.uniform(0.1, 0.5))})"
+        shape = f"sphere({_f(rng.uniform(0.25, 0.6))})" if rng.random() < 0.5 else f"box({_v([2 * rng.uniform(0.15, 0.45) for _ in range(3)])}, 0.02)"
+        out.append(f"\tpaint({mat}) at({_v(pos)}) {shape};\n")
+    out.append("}\n")
+    return "".join(out)
+
+
 def scene_physical_sky(seed: int = 1, width: int = 256, height: int = 256, samples: int = 16, surfaces: int = 8, count: int = 12) -> str:
     """Under a physical sky: config-1 primitives (plastics and metals) on a
     plastic ground lit by a low sun (a disc 0.05 radians across) through

@@ -249,7 +249,8 @@ class View(ctypes.Structure):
                 ("factor", ctypes.c_uint32), ("phase", ctypes.c_uint32), ("sobol", ctypes.c_uint32), ("sky_map", ctypes.c_uint32),
                 ("each_lamp", ctypes.c_uint32), ("middle", ctypes.c_double * 3), ("collisions", ctypes.c_int32),
                 ("sky_kind", ctypes.c_uint32), ("haze", ctypes.c_double), ("glow", ctypes.c_double * 3), ("strength", ctypes.c_double),
-                ("spread", ctypes.c_double), ("aperture", ctypes.c_double), ("focus", ctypes.c_double), ("split", ctypes.c_uint32)]
+                ("spread", ctypes.c_double), ("aperture", ctypes.c_double), ("focus", ctypes.c_double), ("split", ctypes.c_uint32),
+                ("stars", ctypes.c_uint32), ("star_count", ctypes.c_double), ("star_strength", ctypes.c_double), ("star_angle", ctypes.c_double)]
 
 
 _trees: dict = {}
@@ -305,6 +306,10 @@ def render_band(scene, width: int, height: int, spp: int, surfaces: int, seed: i
     v.sky_kind = int(scene.sky.get("kind", 0))
     v.aperture = float(np.float32(scene.camera.get("aperture", 0)))
     v.split = max(int(scene.render.get("split", 1)), 1)
+    v.stars = int(scene.sky.get("stars", 0))
+    v.star_count = float(np.float32(scene.sky.get("star_count", 0)))
+    v.star_strength = float(np.float32(scene.sky.get("star_strength", 0)))
+    v.star_angle = float(np.float32(scene.sky.get("star_angle", 0)))
     v.focus = float(np.float32(scene.camera.get("focus", 0)))
     v.haze = float(np.float32(scene.sky.get("haze", 0)))
     v.strength = float(np.float32(scene.sky.get("strength", 0)))

@@ -194,6 +194,9 @@ typedef struct kp_view {
 	double aperture, focus;
 	/* render.split: samples sharing a first vertex (1: none) */
 	uint32_t split;
+	/* sdf/scene.h Stars: present, count, strength, angle */
+	uint32_t stars;
+	double star_count, star_strength, star_angle;
 } kp_view;
 
 /*

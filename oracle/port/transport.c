@@ -1053,6 +1053,7 @@ typedef struct job {
 	uint32_t sun_lamp;        /* the first sun, whose light the air thins */
 	int glows;                /* sky_layers.cpp:164 skyGlows */
 	double glow[3], sun_elevation;
+	double sun_elevation_any; /* the first sun's elevation, glow or not */
 } job;
 
 /* trace.cpp:179 keptOnLeg with absorption.cpp:28 keptThrough: what a leg of
@@ -1255,6 +1256,48 @@ static double smooth_share(double from, double to, double value) {
 	return s * s * (3 - 2 * s);
 }
 
+/* sky_layers.cpp:240 starlight: one star a cell of a grid on each cube
+ * face, placed, sized and coloured by hashes of its cell's key (:207
+ * starDrawsOf), times the night's share (:264 starNight) */
+static void starlight(const job* J, v3 d, double out_rgb[3]) {
+	const kp_view* V = J->view;
+	out_rgb[0] = out_rgb[1] = out_rgb[2] = 0;
+	const double ax = fabs(d.x), ay = fabs(d.y), az = fabs(d.z);
+	uint64_t face;
+	v3 out, right, up;
+	if (ax >= ay && ax >= az) {
+		const double s = d.x >= 0 ? 1 : -1;
+		face = d.x >= 0 ? 0 : 1, out = mk(s, 0, 0), right = mk(0, s, 0), up = mk(0, 0, 1);
+	} else if (ay >= az) {
+		const double s = d.y >= 0 ? 1 : -1;
+		face = d.y >= 0 ? 2 : 3, out = mk(0, s, 0), right = mk(0, 0, s), up = mk(1, 0, 0);
+	} else {
+		const double s = d.z >= 0 ? 1 : -1;
+		face = d.z >= 0 ? 4 : 5, out = mk(0, 0, s), right = mk(s, 0, 0), up = mk(0, 1, 0);
+	}
+	const double outward = dotv(d, out), u = dotv(d, right) / outward, v = dotv(d, up) / outward;
+	int cells = (int) ceil(sqrt(V->star_count / 6.0));
+	cells = cells < 1 ? 1 : cells;
+	int column = (int) ((u * 0.5 + 0.5) * cells), row = (int) ((v * 0.5 + 0.5) * cells);
+	column = column < 0 ? 0 : (column > cells - 1 ? cells - 1 : column);
+	row = row < 0 ? 0 : (row > cells - 1 ? cells - 1 : row);
+	uint64_t key = (face * 65536u + (uint64_t) row) * 65536u + (uint64_t) column;
+	double draw[4];
+	for (int k = 0; k < 4; ++k) {
+		key = kp_mixed_bits(key + 0x9E3779B97F4A7C15ULL);
+		draw[k] = (double) (key >> 11) * 0x1p-53;
+	}
+	const double across = (column + 0.2 + 0.6 * draw[0]) / cells * 2.0 - 1.0, down = (row + 0.2 + 0.6 * draw[1]) / cells * 2.0 - 1.0;
+	const v3 star = unit(add(add(out, scl(right, across)), scl(up, down)));
+	if (dotv(d, star) < cos(0.5 * V->star_angle)) return;
+	double night = 1;
+	if (J->sun_lamp != 0xFFFFFFFFu) night = 1 - smooth_share(-12.0 * PI / 180.0, -2.0 * PI / 180.0, J->sun_elevation_any);
+	const double bright = V->star_strength * pow(draw[2], 6.0) * night, w = draw[3];
+	out_rgb[0] = (0.75 * (1 - w) + 1.0 * w) * bright;
+	out_rgb[1] = (0.85 * (1 - w) + 0.82 * w) * bright;
+	out_rgb[2] = (1.0 * (1 - w) + 0.62 * w) * bright;
+}
+
 /* feature.cpp:30 skyAt: the gradient, or the air of a physical sky, and the
  * glow about the first sun (sky_layers.cpp:181 glowSeen) */
 static spec sky_seen(const job* J, v3 d, const lanes* w) {
@@ -1275,6 +1318,11 @@ static spec sky_seen(const job* J, v3 d, const lanes* w) {
 		const double falling = exp(-acos(c) / maxd(V->spread, 1e-6)) * fade * above;
 		const double g[3] = { J->glow[0] * falling, J->glow[1] * falling, J->glow[2] * falling };
 		sky = sadd(sky, spectrum(g, w));
+	}
+	if (V->stars && d.z > 0) {
+		double rgb[3];
+		starlight(J, d, rgb);
+		sky = sadd(sky, spectrum(rgb, w));
 	}
 	return sky;
 }
@@ -1742,6 +1790,7 @@ void kp_render_band(const kp_octree* tree, const uint32_t* leaf_material, const 
 		const v3 s = unit(vd(lamps[k].direction));
 		J.sun = s;
 		J.sun_elevation = asin(s.z < -1 ? -1 : (s.z > 1 ? 1 : s.z));
+		J.sun_elevation_any = J.sun_elevation;
 		break;
 	}
 	uint32_t* sobol = NULL;

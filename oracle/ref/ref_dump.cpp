@@ -188,6 +188,8 @@ int dumpScene(const char* sdf, const char* out) {
 	std::fprintf(f, ",\"glow\":");
 	putColour(f, sky.glow);
 	std::fprintf(f, ",\"strength\":%.9g,\"spread\":%.9g,\"haze\":%.9g", double(sky.strength), double(sky.spread), double(sky.haze));
+	const Stars& stars = file.lighting.stars;
+	std::fprintf(f, ",\"stars\":%d,\"star_count\":%.9g,\"star_strength\":%.9g,\"star_angle\":%.9g", stars.present ? 1 : 0, double(stars.count), double(stars.strength), double(stars.angle));
 	const Camera& c = file.shot.camera;
 	const Render& r = file.shot.render;
 	std::fprintf(f, "},\n\"camera\":{\"eye\":");

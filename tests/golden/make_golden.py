@@ -57,7 +57,8 @@ def region_flags(scene: Scene) -> list[str]:
 IMAGES = {"room_small": (16, 64), "c1_small": (16, 64), "c2_small": (16, 64), "glow_small": (16, 64), "glass_small": (16, 64), "patterns_small": (16, 64), "rough_small": (16, 64),
           "films_small": (16, 64), "skylit_small": (16, 64), "lamps_small": (16, 64),
           "far_small": (16, 64), "scatter_small": (16, 64), "physical_small": (16, 64),
-          "lens_small": (16, 64), "split_small": (48, 64)}
+          "lens_small": (16, 64), "split_small": (48, 64),
+          "stars_small": (16, 64)}
 
 # the scenes whose reference frames are also drawn with --use sampler=sobol
 SOBOL_IMAGES = ("c1_small", "glass_small")
@@ -88,6 +89,7 @@ SCENES = {
     "physical_small": (scenegen.scene_physical_sky, dict(seed=14, width=48, height=48, samples=64), 0, 0),
     "lens_small": (scenegen.scene_lens, dict(seed=15, width=48, height=48, samples=64), 0, 0),
     "split_small": (scenegen.scene_split, dict(seed=16, width=48, height=48, samples=64), 0, 0),
+    "stars_small": (scenegen.scene_stars, dict(seed=17, width=48, height=48, samples=64), 0, 0),
 }
 # config 3: the eight resident scenes of the serving run, 256 to 16384
 # config-1-style primitives (merge(0.05) groups of 64)

@@ -50,7 +50,7 @@ def compare(a, b):
 
 @pytest.mark.parametrize("name", ["room_small", "c1_small", "c2_small", "glow_small", "glass_small", "patterns_small", "rough_small", "films_small",
                                   "skylit_small", "lamps_small", "far_small", "scatter_small", "physical_small", "lens_small",
-                                  "split_small"])
+                                  "split_small", "stars_small"])
 def test_frame_matches_oracle_and_reference(backend, name):
     import oracle.port as op
     sc = scene(name)

@@ -75,7 +75,7 @@ def test_denoiser_matches_reference():
 
 @pytest.mark.parametrize("name", ["room_small", "c1_small", "c2_small", "glow_small", "glass_small", "patterns_small", "rough_small", "films_small",
                                   "skylit_small", "lamps_small", "far_small", "scatter_small", "physical_small", "lens_small",
-                                  "split_small"])
+                                  "split_small", "stars_small"])
 def test_renderer_matches_reference_frames(name):
     """The oracle's frames against the reference renderer's own
     (tests/golden/image_*.npz, 12 seeds at the scene's spp): both are
