@@ -171,3 +171,25 @@ def test_sampler_frames_match_reference(name, sampler):
     assert (np.abs(z) > 3).mean() <= 0.015
     if sampler in ("sobol", "each_lamp_first"):
         assert gain > 1.0
+
+
+def test_split_draws_the_same_frame_in_expectation():
+    """render.split: groups of four samples sharing a first vertex (its
+    camera ray, wavelengths and aim, the aim weighed as one of the group)
+    draw the same frame in expectation as independent samples: the
+    oracle's frames at splits 1 and 4 of the same scene agree within 4
+    standard errors on every channel's mean."""
+    import copy
+    sc = scene("split_small")
+    h, w = sc.render["height"], sc.render["width"]
+    build = dict(min_depth=5, max_depth=10, split_steps=64)
+    means = {}
+    for split in (1, 4):
+        s2 = copy.copy(sc)
+        s2.render = dict(sc.render, split=split)
+        frames = np.stack([op.render_band(s2, w, h, 64, int(sc.render["surfaces"]), k, 0, h, os.cpu_count() or 4, build) / 64 for k in range(1, 9)])
+        m = frames.mean(axis=(1, 2))
+        means[split] = (m.mean(0), m.var(0, ddof=1) / len(m))
+    z = (means[4][0] - means[1][0]) / np.sqrt(means[4][1] + means[1][1])
+    print(f"split 4 against 1: {means[4][0]} {means[1][0]} z {z}")
+    assert np.all(np.abs(z) < 4)
