@@ -2,7 +2,7 @@
 reference's sphereTraced.
 
 * At scale (10^5 seeded rays a configuration, tests/golden/hits_*.npz):
-  the benchmark spec's bars -- kinds and leaves (primitive ids, hence materials)
+  the hit bars -- kinds and leaves (primitive ids, hence materials)
   bit-exact, distances and normals within 1e-5 relative -- on every ray
   outside the tie band, the rays whose answer the reference itself does
   not fix to the bar (see the test).
@@ -26,7 +26,7 @@ from hit_rays import hit_rays  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
-# the benchmark spec's bars for the hits, and the share of the bar a ray's reference
+# the bars for the hits (1e-5 relative), and the share of the bar a ray's reference
 # answer may move under the device's stopping rule before the ray counts as
 # undetermined to the bar (the tie band)
 BAR = 1e-5
